@@ -1,0 +1,601 @@
+/*
+ * gl_oracle.c — FP64 CPU restatement of the reference's femgl Newton hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py may load this library, and only as the checker or the
+ * timed CPU baseline.  The product (the CUDA library) never calls it.
+ *
+ * What it restates (reference paths relative to the reference project root):
+ *   - per-quadrature-point physics of the 18 cell kernels
+ *     femgl/src/cell_mat_vec/cell_{mat_lhs,vec_rhs}_{alpha,beta1..5,K1,K2K3}.cc,
+ *     weighted as in femgl/src/assemble.cc:229-276 (K1, K2+K3, alpha, 2*beta_t)
+ *     and femgl/src/residual.cc:206-226.  The reference evaluates every (i,j,q)
+ *     tuple with 3x3 FullMatrix products; here the same quantities come from
+ *     closed forms of the five quartic invariants:
+ *       beta1 |tr(A A^T)|^2, beta2 (tr A A^+)^2, beta3 tr(A A^T (A A^T)^*),
+ *       beta4 tr((A A^+)^2), beta5 tr(A A^+ (A A^+)^*),
+ *     whose quarter-gradient is Re<G_t, Phi> with G1 = tr(AA^T) A^*, G2 = tr(AA^+) A,
+ *     G3 = (AA^T) A^*, G4 = (AA^+) A, G5 = (AA^+)^* A.  The reference kernels
+ *     vec_rhs_beta_t(A;Phi) and mat_lhs_beta_t(A;Phi_i,Phi_j) equal Re<G_t,Phi> and
+ *     Re<dG_t[Phi_j],Phi_i>; tests pin this against the reference kernels compiled
+ *     unmodified (oracle/_ref) and against committed golden vectors.
+ *   - Q1 hexahedra on axis-aligned boxes, QGauss(2) (femgl/src/assemble.cc:123),
+ *     FESystem(FE_Q(1),18) dof order: local dof i -> vertex i/18, component i%18.
+ *   - condensed scatter of AffineConstraints::distribute_local_to_global with
+ *     homogeneous constraints (femgl/src/assemble.cc:356-361, residual.cc:286-289):
+ *     a hanging dof is replaced by its parents with weights 1/2 or 1/4, a zero
+ *     Dirichlet dof is dropped; a constrained row keeps only a diagonal entry
+ *     (sum over cells of |local diagonal|).
+ *   - the free energy density f = K1|grad A|^2 + (K2+K3) sum|div A|^2
+ *     + alpha tr(AA^+) + sum_t beta_t I_t, for which the residual is R = (1/2) df/dx.
+ *     The reference never evaluates f; this is the functional its residual is the
+ *     half-gradient of.
+ *
+ * Layouts: x, R are node-major [node][18]; the 18-vector packs u row-major then v
+ * row-major (reference femgl/src/s_vector2matrix.cc:159-160).  The Jacobian is a
+ * block-CSR of 18x18 row-major blocks on a pattern this file builds itself.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double complex cplx;
+
+/* coefficient vector: {K1, K2+K3, alpha, beta1..beta5} */
+enum { C_K1 = 0, C_K23 = 1, C_ALPHA = 2, C_B1 = 3 };
+
+static void to_cmat(const double *a, cplx M[3][3])
+{
+  for (int c = 0; c < 9; ++c) M[c / 3][c % 3] = a[c] + I * a[9 + c];
+}
+
+static void from_cmat(cplx M[3][3], double *a)
+{
+  for (int c = 0; c < 9; ++c)
+    {
+      a[c] = creal(M[c / 3][c % 3]);
+      a[9 + c] = cimag(M[c / 3][c % 3]);
+    }
+}
+
+static void mm(cplx X[3][3], cplx Y[3][3], cplx Z[3][3]) /* Z = X Y */
+{
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      {
+        cplx s = 0;
+        for (int k = 0; k < 3; ++k) s += X[i][k] * Y[k][j];
+        Z[i][j] = s;
+      }
+}
+
+struct qstate
+{
+  cplx A[3][3], Ac[3][3], P[3][3], Q[3][3], Qc[3][3];
+  cplx p;
+  double q;
+};
+
+static void qstate_init(const double *a, struct qstate *s)
+{
+  to_cmat(a, s->A);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) s->Ac[i][j] = conj(s->A[i][j]);
+  cplx At[3][3], Ah[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      {
+        At[i][j] = s->A[j][i];
+        Ah[i][j] = conj(s->A[j][i]);
+      }
+  mm(s->A, At, s->P);
+  mm(s->A, Ah, s->Q);
+  s->p = s->P[0][0] + s->P[1][1] + s->P[2][2];
+  s->q = creal(s->Q[0][0] + s->Q[1][1] + s->Q[2][2]);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) s->Qc[i][j] = conj(s->Q[i][j]);
+}
+
+/* G_t for t = 1..5 (see file header). */
+static void G_t(const struct qstate *s, int t, cplx G[3][3])
+{
+  cplx T[3][3];
+  switch (t)
+    {
+    case 1:
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G[i][j] = s->p * s->Ac[i][j];
+      break;
+    case 2:
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G[i][j] = s->q * s->A[i][j];
+      break;
+    case 3: memcpy(T, s->P, sizeof T); mm(T, (cplx(*)[3])s->Ac, G); break;
+    case 4: memcpy(T, s->Q, sizeof T); mm(T, (cplx(*)[3])s->A, G); break;
+    default: memcpy(T, s->Qc, sizeof T); mm(T, (cplx(*)[3])s->A, G); break;
+    }
+}
+
+/* dG_t[F]: directional derivative of G_t along F. */
+static void dG_t(const struct qstate *s, int t, cplx F[3][3], cplx D[3][3])
+{
+  cplx Fc[3][3], Ft[3][3], Fh[3][3], At[3][3], Ah[3][3], X[3][3], Y[3][3], Z[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      {
+        Fc[i][j] = conj(F[i][j]);
+        Ft[i][j] = F[j][i];
+        Fh[i][j] = conj(F[j][i]);
+        At[i][j] = s->A[j][i];
+        Ah[i][j] = conj(s->A[j][i]);
+      }
+  switch (t)
+    {
+    case 1:
+      {
+        cplx dp = 0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) dp += 2.0 * s->A[i][j] * F[i][j];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) D[i][j] = dp * s->Ac[i][j] + s->p * Fc[i][j];
+        break;
+      }
+    case 2:
+      {
+        double dq = 0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) dq += 2.0 * creal(s->Ac[i][j] * F[i][j]);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) D[i][j] = dq * s->A[i][j] + s->q * F[i][j];
+        break;
+      }
+    case 3: /* (A F^T + F A^T) A^* + P F^* */
+      mm((cplx(*)[3])s->A, Ft, X);
+      mm(F, At, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) X[i][j] += Y[i][j];
+      mm(X, (cplx(*)[3])s->Ac, Z);
+      mm((cplx(*)[3])s->P, Fc, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D[i][j] = Z[i][j] + Y[i][j];
+      break;
+    case 4: /* (F A^+ + A F^+) A + Q F */
+      mm(F, Ah, X);
+      mm((cplx(*)[3])s->A, Fh, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) X[i][j] += Y[i][j];
+      mm(X, (cplx(*)[3])s->A, Z);
+      mm((cplx(*)[3])s->Q, F, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D[i][j] = Z[i][j] + Y[i][j];
+      break;
+    default: /* (F^* A^T + A^* F^T) A + Q^* F */
+      mm(Fc, At, X);
+      mm((cplx(*)[3])s->Ac, Ft, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) X[i][j] += Y[i][j];
+      mm(X, (cplx(*)[3])s->A, Z);
+      mm((cplx(*)[3])s->Qc, F, Y);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D[i][j] = Z[i][j] + Y[i][j];
+      break;
+    }
+}
+
+/*
+ * Bulk physics at one quadrature point.
+ *   R[18]  = alpha A + 2 sum_t beta_t G_t             (the alpha/beta part of -cell_rhs/JxW)
+ *   H[324] = alpha Id + 2 sum_t beta_t dG_t[e_d]     (column d; symmetric)
+ *   *f     = alpha tr(AA^+) + sum_t beta_t I_t
+ * Any output pointer may be NULL.
+ */
+void orc_bulk_q(const double *coef, const double *a, double *R, double *H, double *f)
+{
+  struct qstate s;
+  qstate_init(a, &s);
+  const double alpha = coef[C_ALPHA];
+  if (R || f)
+    {
+      double r[18], g[18];
+      for (int c = 0; c < 18; ++c) r[c] = alpha * a[c];
+      double fe = alpha * s.q;
+      for (int t = 1; t <= 5; ++t)
+        {
+          cplx G[3][3];
+          G_t(&s, t, G);
+          from_cmat(G, g);
+          const double b = coef[C_B1 + t - 1];
+          double It = 0;
+          for (int c = 0; c < 18; ++c)
+            {
+              r[c] += 2.0 * b * g[c];
+              It += g[c] * a[c];
+            }
+          fe += b * It;
+        }
+      if (R) memcpy(R, r, sizeof r);
+      if (f) *f = fe;
+    }
+  if (H)
+    {
+      for (int d = 0; d < 18; ++d)
+        {
+          cplx F[3][3] = {{0}};
+          if (d < 9) F[d / 3][d % 3] = 1.0;
+          else F[(d - 9) / 3][(d - 9) % 3] = I;
+          double col[18], g[18];
+          for (int c = 0; c < 18; ++c) col[c] = (c == d) ? alpha : 0.0;
+          for (int t = 1; t <= 5; ++t)
+            {
+              cplx D[3][3];
+              dG_t(&s, t, F, D);
+              from_cmat(D, g);
+              const double b = coef[C_B1 + t - 1];
+              for (int c = 0; c < 18; ++c) col[c] += 2.0 * b * g[c];
+            }
+          for (int c = 0; c < 18; ++c) H[18 * c + d] = col[c];
+        }
+    }
+}
+
+/* Reference-element tables for QGauss(2) on a Q1 hex: q = qx + 2 qy + 4 qz. */
+static void q1_tables(const double *h, double val[8][8], double grd[8][8][3])
+{
+  const double g = 0.5 - sqrt(3.0) / 6.0;
+  const double gp[2] = {g, 1.0 - g};
+  for (int q = 0; q < 8; ++q)
+    {
+      const double xi[3] = {gp[q & 1], gp[(q >> 1) & 1], gp[(q >> 2) & 1]};
+      for (int v = 0; v < 8; ++v)
+        {
+          double s[3], ds[3];
+          for (int d = 0; d < 3; ++d)
+            {
+              const int bit = (v >> d) & 1;
+              s[d] = bit ? xi[d] : 1.0 - xi[d];
+              ds[d] = (bit ? 1.0 : -1.0) / h[d];
+            }
+          val[q][v] = s[0] * s[1] * s[2];
+          grd[q][v][0] = ds[0] * s[1] * s[2];
+          grd[q][v][1] = s[0] * ds[1] * s[2];
+          grd[q][v][2] = s[0] * s[1] * ds[2];
+        }
+    }
+}
+
+/*
+ * Local (unconstrained) cell contribution in the reference's sign convention for
+ * the Jacobian and as +R for the residual: K[144*144] (may be NULL), r[144]
+ * (may be NULL), *fcell = cell free energy (may be NULL).
+ */
+void orc_cell_local(const double *h, const double *x, const double *coef, double *K, double *r, double *fcell)
+{
+  double val[8][8], grd[8][8][3];
+  q1_tables(h, val, grd);
+  const double JxW = 0.125 * h[0] * h[1] * h[2];
+  const double K1 = coef[C_K1], K23 = coef[C_K23];
+  if (K) memset(K, 0, sizeof(double) * 144 * 144);
+  if (r) memset(r, 0, sizeof(double) * 144);
+  double fsum = 0.0;
+  for (int q = 0; q < 8; ++q)
+    {
+      double A[18] = {0}, gA[3][18] = {{0}};
+      for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 18; ++c)
+          {
+            A[c] += val[q][v] * x[18 * v + c];
+            for (int k = 0; k < 3; ++k) gA[k][c] += grd[q][v][k] * x[18 * v + c];
+          }
+      double div[6];
+      for (int pm = 0; pm < 6; ++pm)
+        {
+          const int base = 9 * (pm / 3) + 3 * (pm % 3);
+          div[pm] = gA[0][base + 0] + gA[1][base + 1] + gA[2][base + 2];
+        }
+      double Rb[18], Hb[324], fb;
+      orc_bulk_q(coef, A, Rb, K ? Hb : NULL, &fb);
+      double fg = 0.0;
+      for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 18; ++c) fg += K1 * gA[k][c] * gA[k][c];
+      for (int pm = 0; pm < 6; ++pm) fg += K23 * div[pm] * div[pm];
+      fsum += JxW * (fb + fg);
+      if (r)
+        for (int v = 0; v < 8; ++v)
+          for (int c = 0; c < 18; ++c)
+            {
+              const int pm = 3 * (c / 9) + (c % 9) / 3, j = c % 3;
+              double s = val[q][v] * Rb[c];
+              for (int k = 0; k < 3; ++k) s += K1 * grd[q][v][k] * gA[k][c];
+              s += K23 * grd[q][v][j] * div[pm];
+              r[18 * v + c] += JxW * s;
+            }
+      if (K)
+        for (int v = 0; v < 8; ++v)
+          for (int w = 0; w < 8; ++w)
+            {
+              const double vv = val[q][v] * val[q][w];
+              double gg = 0.0;
+              for (int k = 0; k < 3; ++k) gg += grd[q][v][k] * grd[q][w][k];
+              for (int c = 0; c < 18; ++c)
+                {
+                  double *row = K + (size_t)(18 * v + c) * 144 + 18 * w;
+                  const int pmc = 3 * (c / 9) + (c % 9) / 3, jc = c % 3;
+                  for (int d = 0; d < 18; ++d)
+                    {
+                      const int pmd = 3 * (d / 9) + (d % 9) / 3, jd = d % 3;
+                      double s = vv * Hb[18 * c + d];
+                      if (c == d) s += K1 * gg;
+                      if (pmc == pmd) s += K23 * grd[q][v][jc] * grd[q][w][jd];
+                      row[d] += JxW * s;
+                    }
+                }
+            }
+    }
+  if (fcell) *fcell = fsum;
+}
+
+/* ------------------------------------------------------------------------------
+ * Mesh-level assembly with homogeneous constraints.
+ *
+ * Mesh arrays (the same ones the CUDA library's boundary takes):
+ *   nn nodes, xyz[nn*3]; nc cells, cells[nc*8] (deal.II vertex order);
+ *   mask[nn]: bit c set <=> component c of the node is a zero-Dirichlet dof;
+ *   hanging constraints in CSR: hptr[nn+1], hpar[], hw[] (a node with
+ *   hptr[n+1] > hptr[n] is hanging on those parents with those weights).
+ * ------------------------------------------------------------------------------ */
+
+static int is_hanging(const int *hptr, int n) { return hptr[n + 1] > hptr[n]; }
+
+/* Count blocks of the condensed pattern; fill rowptr[nn+1] */
+static int cmp_int(const void *a, const void *b)
+{
+  const int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+/* Expand a node to its unconstrained node list (node level). */
+static int expand_node(const int *hptr, const int *hpar, const double *hw, int n, int *out, double *w)
+{
+  if (!is_hanging(hptr, n))
+    {
+      out[0] = n;
+      w[0] = 1.0;
+      return 1;
+    }
+  int m = 0;
+  for (int k = hptr[n]; k < hptr[n + 1]; ++k)
+    {
+      out[m] = hpar[k];
+      w[m] = hw[k];
+      ++m;
+    }
+  return m;
+}
+
+/*
+ * Pattern: rows are all nodes; a hanging node's row holds only its diagonal block.
+ * Returns nnzb; when rowptr/cols are non-NULL fills them (cols sorted per row).
+ */
+long orc_pattern(int nn, int nc, const int *cells, const int *hptr, const int *hpar, const double *hw, int *rowptr,
+                 int *cols)
+{
+  int *cnt = calloc((size_t)nn, sizeof(int));
+  int *cap = calloc((size_t)nn, sizeof(int));
+  int **lst = calloc((size_t)nn, sizeof(int *));
+  for (int n = 0; n < nn; ++n)
+    if (is_hanging(hptr, n))
+      {
+        lst[n] = malloc(sizeof(int));
+        lst[n][0] = n;
+        cnt[n] = cap[n] = 1;
+      }
+  for (int e = 0; e < nc; ++e)
+    {
+      int ex[8][4], m[8];
+      double w[4];
+      for (int v = 0; v < 8; ++v) m[v] = expand_node(hptr, hpar, hw, cells[8 * e + v], ex[v], w);
+      for (int a = 0; a < 8; ++a)
+        for (int ia = 0; ia < m[a]; ++ia)
+          {
+            const int row = ex[a][ia];
+            for (int b = 0; b < 8; ++b)
+              for (int ib = 0; ib < m[b]; ++ib)
+                {
+                  const int col = ex[b][ib];
+                  int found = 0;
+                  for (int k = 0; k < cnt[row]; ++k)
+                    if (lst[row][k] == col)
+                      {
+                        found = 1;
+                        break;
+                      }
+                  if (!found)
+                    {
+                      if (cnt[row] == cap[row])
+                        {
+                          cap[row] = cap[row] ? 2 * cap[row] : 32;
+                          lst[row] = realloc(lst[row], sizeof(int) * (size_t)cap[row]);
+                        }
+                      lst[row][cnt[row]++] = col;
+                    }
+                }
+          }
+    }
+  long total = 0;
+  for (int n = 0; n < nn; ++n)
+    {
+      qsort(lst[n], (size_t)cnt[n], sizeof(int), cmp_int);
+      if (rowptr) rowptr[n] = (int)total;
+      if (cols) memcpy(cols + total, lst[n], sizeof(int) * (size_t)cnt[n]);
+      total += cnt[n];
+      free(lst[n]);
+    }
+  if (rowptr) rowptr[nn] = (int)total;
+  free(lst);
+  free(cnt);
+  free(cap);
+  return total;
+}
+
+static long find_block(const int *rowptr, const int *cols, int row, int col)
+{
+  int lo = rowptr[row], hi = rowptr[row + 1] - 1;
+  while (lo <= hi)
+    {
+      const int mid = (lo + hi) / 2;
+      if (cols[mid] == col) return mid;
+      if (cols[mid] < col) lo = mid + 1;
+      else hi = mid - 1;
+    }
+  return -1;
+}
+
+/* x <- C x: hanging nodes become their weighted parent sums, Dirichlet components 0
+ * (AffineConstraints::distribute with homogeneous constraints).  A hanging node's
+ * own mask is ignored: its hanging constraint takes precedence, as in deal.II where
+ * boundary values are not added for dofs that are already constrained. */
+void orc_distribute(int nn, const uint32_t *mask, const int *hptr, const int *hpar, const double *hw, double *x)
+{
+  for (int n = 0; n < nn; ++n)
+    if (!is_hanging(hptr, n))
+      for (int c = 0; c < 18; ++c)
+        if (mask[n] >> c & 1u) x[18 * n + c] = 0.0;
+  for (int n = 0; n < nn; ++n)
+    if (is_hanging(hptr, n))
+      for (int c = 0; c < 18; ++c)
+        {
+          double s = 0.0;
+          for (int k = hptr[n]; k < hptr[n + 1]; ++k) s += hw[k] * x[18 * hpar[k] + c];
+          x[18 * n + c] = s;
+        }
+}
+
+static void cell_h(const double *xyz, const int *cell, double *h)
+{
+  for (int d = 0; d < 3; ++d) h[d] = xyz[3 * cell[7] + d] - xyz[3 * cell[0] + d];
+}
+
+/*
+ * Condensed assembly.  J (block values on the orc_pattern pattern, may be NULL),
+ * R[nn*18] = +R condensed (constrained entries 0), *F = free energy.
+ * Returns 0, or -1 if a block is missing from the pattern.
+ */
+int orc_assemble(int nn, const double *xyz, int nc, const int *cells, const uint32_t *mask, const int *hptr,
+                 const int *hpar, const double *hw, const double *coef, const double *x, const int *rowptr,
+                 const int *cols, double *J, double *R, double *F)
+{
+  const long nnzb = rowptr ? rowptr[nn] : 0;
+  if (J) memset(J, 0, sizeof(double) * 324 * (size_t)nnzb);
+  if (R) memset(R, 0, sizeof(double) * 18 * (size_t)nn);
+  double ftot = 0.0;
+  int err = 0;
+  const int chunk = 512;
+  double *Kbuf = J ? malloc(sizeof(double) * 144 * 144 * (size_t)chunk) : NULL;
+  double *rbuf = malloc(sizeof(double) * 144 * (size_t)chunk);
+  double *fbuf = malloc(sizeof(double) * (size_t)chunk);
+  for (int e0 = 0; e0 < nc; e0 += chunk)
+    {
+      const int e1 = (e0 + chunk < nc) ? e0 + chunk : nc;
+#pragma omp parallel for schedule(static)
+      for (int e = e0; e < e1; ++e)
+        {
+          double h[3], xl[144];
+          cell_h(xyz, cells + 8 * e, h);
+          for (int v = 0; v < 8; ++v) memcpy(xl + 18 * v, x + 18 * (size_t)cells[8 * e + v], sizeof(double) * 18);
+          orc_cell_local(h, xl, coef, J ? Kbuf + (size_t)(e - e0) * 144 * 144 : NULL, rbuf + (size_t)(e - e0) * 144,
+                         fbuf + (e - e0));
+        }
+      for (int e = e0; e < e1; ++e)
+        {
+          const double *Kl = J ? Kbuf + (size_t)(e - e0) * 144 * 144 : NULL;
+          const double *rl = rbuf + (size_t)(e - e0) * 144;
+          ftot += fbuf[e - e0];
+          int ex[8][4], m[8];
+          double w[8][4];
+          for (int v = 0; v < 8; ++v) m[v] = expand_node(hptr, hpar, hw, cells[8 * e + v], ex[v], w[v]);
+          for (int a = 0; a < 8; ++a)
+            {
+              const int na = cells[8 * e + a];
+              for (int c = 0; c < 18; ++c)
+                {
+                  const int i = 18 * a + c;
+                  const int a_dir = !is_hanging(hptr, na) && (mask[na] >> c & 1u);
+                  if (a_dir)
+                    { /* constrained row: diagonal only */
+                      if (J)
+                        {
+                          const long blk = find_block(rowptr, cols, na, na);
+                          if (blk < 0) { err = -1; continue; }
+                          J[324 * blk + 18 * c + c] += fabs(Kl[(size_t)i * 144 + i]);
+                        }
+                      continue;
+                    }
+                  if (is_hanging(hptr, na) && J)
+                    {
+                      const long blk = find_block(rowptr, cols, na, na);
+                      if (blk < 0) { err = -1; continue; }
+                      J[324 * blk + 18 * c + c] += fabs(Kl[(size_t)i * 144 + i]);
+                    }
+                  for (int ia = 0; ia < m[a]; ++ia)
+                    {
+                      const int row = ex[a][ia];
+                      if (mask[row] >> c & 1u) continue; /* parent component is Dirichlet */
+                      const double wa = w[a][ia];
+                      if (R) R[18 * (size_t)row + c] += wa * rl[i];
+                      if (!J) continue;
+                      for (int b = 0; b < 8; ++b)
+                        for (int ib = 0; ib < m[b]; ++ib)
+                          {
+                            const int col = ex[b][ib];
+                            const long blk = find_block(rowptr, cols, row, col);
+                            if (blk < 0) { err = -1; continue; }
+                            const double wab = wa * w[b][ib];
+                            double *dst = J + 324 * blk + 18 * c;
+                            const double *src = Kl + (size_t)i * 144 + 18 * b;
+                            for (int d = 0; d < 18; ++d)
+                              if (!(mask[col] >> d & 1u)) dst[d] += wab * src[d];
+                          }
+                    }
+                }
+            }
+        }
+    }
+  free(Kbuf);
+  free(rbuf);
+  free(fbuf);
+  if (F) *F = ftot;
+  return err;
+}
+
+/* y = J x on the pattern (all rows). */
+void orc_spmv(int nn, const int *rowptr, const int *cols, const double *J, const double *x, double *y)
+{
+#pragma omp parallel for schedule(static)
+  for (int n = 0; n < nn; ++n)
+    {
+      double acc[18] = {0};
+      for (int k = rowptr[n]; k < rowptr[n + 1]; ++k)
+        {
+          const double *B = J + 324 * (size_t)k;
+          const double *xv = x + 18 * (size_t)cols[k];
+          for (int c = 0; c < 18; ++c)
+            for (int d = 0; d < 18; ++d) acc[c] += B[18 * c + d] * xv[d];
+        }
+      memcpy(y + 18 * (size_t)n, acc, sizeof acc);
+    }
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
