@@ -1,0 +1,298 @@
+"""Benchmark of the femgl Newton hot path on one GB300.
+
+Workload (the femgl 3D configuration the metric is quoted on): cube [-10, 10]^3
+(L = 20 xi0), 32^3 Q1 hexahedra, matep coefficients at T = 0.6 Tc, p = 20 bar with
+strong-coupling corrections, pair-breaking A_{mu z} = 0 on the z faces, free
+elsewhere, start = B phase + 0.05 N(0,1) per dof (seed 2).  Nd = 646,866 dofs,
+nnzb = 912,673 18x18 blocks.
+
+One step = one complete Newton solve from that start to ||F||_2 < 1e-10 (the
+reference's run() loop), inputs resident in HBM.  value = solves/s of the mixed
+solver (FP32 Jacobian + FP32 GMRES, FP64 residual/line search); the plain FP64 GPU
+Newton is measured in the same run and reported beside it, together with assembly
+GDOF/s.  e2e = the same solves through the C ABI with the start vector copied in
+from host memory and the solution copied out every step.
+
+--impl reference times the CPU implementation instead (see cpu_reference()).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+P_BAR, T_RED, HALF, NCELL, NOISE, SEED = 20.0, 0.6, 10.0, 32, 0.05, 2
+TOL = 1e-10
+METRIC = "GL solves/s at ||F||<1e-10 (femgl 3D, 32^3 Q1, T=0.6Tc, p=20bar)"
+WORKLOAD = "femgl 3D cube L=20, 32^3 Q1 cells, matep(p=20 bar, t=0.6, SCC), z-face pair breaking, B-phase+0.05N(0,1) seed 2"
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 2 + i and "Active" in s[2 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def problem(gl):
+    m = gl.cube_mesh(HALF, NCELL)
+    x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
+    return m, x0
+
+
+def solve_once(f, x0, linear_tol):
+    f.set_solution(x0)
+    return f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+
+
+def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None):
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision, precond=gl.PC_BLOCK_JACOBI)
+    f = gl.FemGL(m, prm)
+    out = None
+    for _ in range(warmup):
+        out = solve_once(f, x0, linear_tol)
+    f.timers(reset=True)
+    f.kernel_timing(kernel_timing, reset=True)
+    launches0 = f.launch_count
+    ms_steps = []
+    stats = []
+    for _ in range(steps):
+        if flush is not None:
+            flush()
+        f.sync()
+        f.event_start()
+        out = solve_once(f, x0, linear_tol)
+        ms_steps.append(f.event_stop())
+        stats.append(out)
+    kms, kn = f.kernel_timing(False)
+    phases = f.timers()
+    launches = f.launch_count - launches0
+    x = f.solution()
+    F = float(f.free_energy()[0])
+    # assembly alone (J + R), timed separately
+    f.set_solution(x0)
+    f.assemble_system()
+    f.sync()
+    f.event_start()
+    na = 5
+    for _ in range(na):
+        f.assemble_system()
+    asm_ms = f.event_stop() / na
+    f.close()
+    return {"ms": ms_steps, "out": stats[-1], "kernel_ms": kms, "kernel_n": kn, "phases": phases,
+            "launches": launches, "x": x, "F": F, "asm_ms": asm_ms}
+
+
+def e2e_mode(gl, m, x0, precision, steps, linear_tol):
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision, precond=gl.PC_BLOCK_JACOBI)
+    f = gl.FemGL(m, prm)
+    xh = np.ascontiguousarray(x0)
+    solve_once(f, xh, linear_tol)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        f.set_solution(xh)  # host -> device
+        f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+        xo = f.solution()  # device -> host
+    dt = time.perf_counter() - t0
+    f.close()
+    return steps / dt, xo
+
+
+def cpu_port_baseline(m, x0, gpu_stats):
+    """Oracle FP64 CPU restatement on all host cores, bounded sample: one Jacobian +
+    residual assembly and one residual evaluation of the 32^3 problem, scaled to a
+    full solve with the GPU run's Newton and line-search counts (the oracle has no
+    iterative Krylov solver, so the linear solves are not included: an optimistic
+    CPU figure)."""
+    from oracle import gl as ogl
+    from oracle import mesh as om
+
+    ogl.build()
+    mm = om.Mesh(m.xyz, m.cells, m.mask, m.hptr, m.hpar, m.hw)
+    gl = importlib.import_module("verkko-hem-repo_gb300")
+    prm = gl.Params.from_matep(P_BAR, T_RED)
+    coef = np.array([prm.K1, prm.K2 + prm.K3, prm.alpha, *prm.beta])
+    sysr = ogl.System(mm, coef)
+    x = sysr.distribute(x0)
+    t0 = time.perf_counter()
+    sysr.assemble(x)
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sysr.residual(x)
+    t_res = time.perf_counter() - t0
+    n_newton = int(gpu_stats["newton_its"][0])
+    t_solve = n_newton * (t_asm + 2 * t_res)
+    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": ogl.lib().orc_num_threads(), "kind": "port",
+            "sample": f"1 oracle J+R assembly ({t_asm:.2f}s) + 1 residual ({t_res:.2f}s) of the 32^3 problem, "
+                      f"scaled by {n_newton} Newton steps x (assembly + 2 residuals); linear solves excluded",
+            "assembly_gdofs": 646866 / t_asm / 1e9}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--linear-tol", type=float, default=1e-4)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+    gl = importlib.import_module("verkko-hem-repo_gb300")
+    gl.build()
+    m, x0 = problem(gl)
+    pk = peaks()
+    hbm = float(pk.get("hbm_gbs", 6800.0))
+
+    import ctypes
+
+    # L2 flush buffer (256 MB > 129 MB L2): written between timed steps
+    flush_buf = None
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    except Exception:
+        flush_buf = None
+
+    def flush():
+        if flush_buf is not None:
+            flush_buf.fill_(1.0)
+            import torch
+
+            torch.cuda.synchronize()
+
+    fp64 = time_mode(gl, m, x0, gl.FP64, max(1, args.steps // 2), 1, args.linear_tol, flush=flush)
+    with ClockSampler() as clk:
+        mixed = time_mode(gl, m, x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
+                          flush=flush)
+    e2e_val, x_e2e = e2e_mode(gl, m, x0, gl.MIXED, max(1, args.steps), args.linear_tol)
+
+    ms_step = float(np.mean(mixed["ms"]))
+    value = 1000.0 / ms_step
+    nd = 18 * m.nn
+    nnzb = 912673
+    # SpMV roofline (FP32 blocks): algorithmic bytes per launch
+    spmv_bytes = nnzb * (324 * 4 + 4) + (m.nn + 1) * 4 + 2 * nd * 4
+    n_spmv = mixed["kernel_n"]["spmv"]
+    spmv_ms = mixed["kernel_ms"]["spmv"] / max(1, n_spmv)
+    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9 if n_spmv else None
+    asm_bytes = nnzb * 324 * 4 + m.nc * 32 + 2 * nd * 8
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 Jacobian/GMRES + f64 residual",
+        "data": "synthetic (seeded B-phase + Gaussian noise start; no dataset)",
+        "config": {"workload": WORKLOAD, "n_dofs": nd, "nnzb": nnzb, "mode": "mixed", "linear_tol": args.linear_tol,
+                   "precond": "block-Jacobi", "gmres_restart": 50,
+                   "l2": "inputs > L2 (FP32 BSR 1.18 GB) and a 256 MB L2 flush between steps"},
+        "newton_its": int(mixed["out"]["newton_its"][0]),
+        "gmres_its": int(mixed["out"]["gmres_its"][0]),
+        "final_residual": float(mixed["out"]["residual"][0]),
+        "free_energy": mixed["F"],
+        "fp64": {"solves_per_s": 1000.0 / float(np.mean(fp64["ms"])), "ms_per_solve": float(np.mean(fp64["ms"])),
+                 "newton_its": int(fp64["out"]["newton_its"][0]), "gmres_its": int(fp64["out"]["gmres_its"][0]),
+                 "free_energy": fp64["F"], "assembly_ms": fp64["asm_ms"], "assembly_gdofs": nd / fp64["asm_ms"] / 1e6},
+        "mixed_vs_fp64": (1000.0 / ms_step) / (1000.0 / float(np.mean(fp64["ms"]))),
+        "free_energy_rel_diff_vs_fp64": abs(mixed["F"] - fp64["F"]) / abs(fp64["F"]),
+        "assembly_gdofs_mixed": nd / mixed["asm_ms"] / 1e6,
+        "phases_ms": mixed["phases"],
+        "kernel_ms": mixed["kernel_ms"],
+        "kernel_launches": mixed["kernel_n"],
+        "gpu_launches": int(mixed["launches"]),
+        "roofline": {"bound": "hbm", "kernel": "k_spmv18<float>", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms,
+                     "assembly_algorithmic_bytes": asm_bytes},
+        "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": nd * 8, "d2h_bytes_per_step": nd * 8},
+        "clocks": clk.summary(),
+    }
+    try:
+        line["cpu_baseline"] = cpu_port_baseline(m, x0, mixed["out"])
+    except Exception as e:  # the CPU baseline must not hide the GPU line
+        line["cpu_baseline"] = {"value": None, "error": str(e)}
+    print(json.dumps(line))
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return 0
+    import importlib as il
+
+    gl = il.import_module("verkko-hem-repo_gb300")
+    gl.build()
+    m, x0 = problem(gl)
+    from oracle import gl as ogl
+
+    ogl.build()
+    R = ogl.ref()
+    if R is None:
+        print(json.dumps({"impl": "reference", "unavailable": "reference kernels not built (oracle/_ref missing)"}))
+        return 0
+    print(json.dumps({"impl": "reference", "unavailable": "reference arm not implemented yet"}))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main() or 0)

@@ -1,0 +1,268 @@
+/*
+ * glgpu.h — C ABI of the GB300 (sm_103a) implementation of femgl's Newton hot path.
+ *
+ * The reference keeps this path in private members of FemGL_mpi::FemGL<3>
+ * (reference femgl/inc/femgl.h:130-137): assemble_system(), compute_residual(),
+ * solve(const double&), newton_iteration(), driven by run().  Their state lives in
+ * class members (local_solution, locally_relevant_newton_solution,
+ * locally_relevant_damped_vector, system_matrix, system_rhs, residual_vector and
+ * the two AffineConstraints, femgl.h:304-316).  Here that state lives in an opaque
+ * context that owns all device memory and one CUDA stream; every entry point below
+ * replaces one reference member (cited beside it).
+ *
+ * Conventions
+ *   - Plain C types only; every array argument is HOST memory, copied in or out.
+ *   - Every function returns a glgpu_status; nothing aborts, traps or exits.
+ *     glgpu_last_error() gives a one-line message for the last failure.
+ *   - One context per host thread.  A context may hold several independent
+ *     instances (meshes with their own coefficients), solved together; the
+ *     single-mesh calls are the 1-instance case.
+ *   - Vectors are node-major: x[18*node + c] (3D) or x[2*node + c] (2D), the
+ *     component packing of femgl/src/s_vector2matrix.cc:159-160 (c < 9: u(c/3,c%3);
+ *     c >= 9: v((c-9)/3,(c-9)%3)).  Instances are concatenated in creation order.
+ *   - Sign convention of the reference: system_rhs = -R (femgl/src/assemble.cc:257).
+ */
+#ifndef GLGPU_H
+#define GLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+  GLGPU_OK = 0,
+  GLGPU_ERR_ARG = 1,          /* invalid argument or mesh */
+  GLGPU_ERR_CUDA = 2,         /* a CUDA call failed; the context should be destroyed */
+  GLGPU_ERR_NOMEM = 3,        /* device allocation failed */
+  GLGPU_ERR_NOT_CONVERGED = 4, /* linear or nonlinear solve stopped before its tolerance */
+  GLGPU_ERR_NAN = 5,          /* NaN or Inf in a residual or a norm */
+  GLGPU_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up */
+  GLGPU_ERR_STATE = 7         /* call out of order (e.g. solve before assemble) */
+} glgpu_status;
+
+typedef enum
+{
+  GLGPU_FP64 = 0,  /* assembly, Krylov solve and residual in FP64 (the reference's arithmetic) */
+  GLGPU_MIXED = 1  /* FP32 Jacobian + FP32 GMRES; FP64 residual, line search and free energy */
+} glgpu_precision;
+
+typedef enum
+{
+  GLGPU_PC_NONE = 0,
+  GLGPU_PC_BLOCK_JACOBI = 1,   /* inverse of each node's diagonal block */
+  GLGPU_PC_CHEBYSHEV = 2       /* Chebyshev polynomial in (block-Jacobi)^-1 J */
+} glgpu_precond;
+
+/*
+ * Mesh of one instance, in the form the reference's setup_system() produces it
+ * (femgl/src/setup_uniform_B-phase.cc:125-198): nodes, Q1 cells, the zero-Dirichlet
+ * component mask of every node and the hanging-node constraints.
+ */
+typedef struct
+{
+  int dim;                       /* 3: femgl tensor GL (18 components); 2: complexGL (2 components) */
+  int n_nodes;
+  int n_cells;
+  const double *xyz;             /* [n_nodes][dim] coordinates */
+  const int32_t *cells;          /* [n_cells][2^dim] deal.II vertex order v = ix + 2 iy (+ 4 iz); axis-aligned boxes */
+  const uint32_t *dirichlet_mask;/* [n_nodes]: bit c set <=> component c is a zero-Dirichlet dof (may be NULL) */
+  const int32_t *hang_ptr;       /* [n_nodes+1] CSR of hanging constraints, or NULL for none */
+  const int32_t *hang_parent;    /* parents of hanging nodes */
+  const double *hang_weight;     /* their weights (1/2 edge, 1/4 face) */
+} glgpu_mesh;
+
+/*
+ * Coefficients and solver controls of one instance.
+ * Physics (femgl/src/assemble.cc:229-252; femgl/inc/femgl.h:320-322):
+ *   J_ij += [K1 k1 + (K2+K3) k23 + alpha a + 2 sum_t beta_t b_t] JxW.
+ * For dim == 2 (complexGL archive, complexGL.cc:479-548): K1 is the gradient
+ * weight K (the residual uses K/2 |grad psi|^2 ... see glgpu_free_energy),
+ * alpha and beta[0] are the bulk coefficients, the rest is unused.
+ */
+typedef struct
+{
+  double K1, K2, K3;
+  double alpha;
+  double beta[5];
+  int precision;        /* glgpu_precision */
+  int precond;          /* glgpu_precond */
+  int cheb_degree;      /* Chebyshev degree (precond == GLGPU_PC_CHEBYSHEV), e.g. 3 */
+  int gmres_restart;    /* Krylov basis size before restart, e.g. 50 */
+  int gmres_max_iter;   /* "maximum linear iteration number" (declare.cc), e.g. 10000 */
+  double ls_step;       /* "primary step length of dampped newton iteration", 0.83 */
+  int ls_max_trials;    /* trials of the backtracking line search, 100 (iteration.cc:170) */
+  int damped;           /* "Using dampped Newton iteration" (1) or full Newton (0) */
+} glgpu_params;
+
+typedef struct glgpu_ctx glgpu_ctx;
+
+/* Fills p with the reference's defaults (declare.cc) and K1 = K2 = K3 = 0.42072. */
+void glgpu_default_params(glgpu_params *p);
+
+/* Library version string. */
+const char *glgpu_version(void);
+
+/* Last error message of this thread (empty string when none). */
+const char *glgpu_last_error(void);
+
+/*
+ * Creates a context for n_inst instances (mesh[k], prm[k]); builds the block-CSR
+ * pattern and the assembly plan once per mesh (the reference does this in
+ * setup_system(), femgl/src/setup_uniform_B-phase.cc:188-198) and allocates all
+ * device memory.  The solution starts at zero.
+ */
+glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst, glgpu_ctx **out);
+glgpu_status glgpu_destroy(glgpu_ctx *ctx);
+
+/* Sizes: total nodes, total block nonzeros, block size (18 or 2), instances. */
+glgpu_status glgpu_sizes(const glgpu_ctx *ctx, int64_t *n_nodes, int64_t *nnzb, int *block, int *n_inst);
+
+/*
+ * local_solution (femgl.h:313).  set_solution copies x in and applies the
+ * solution constraints (constraints_solution.distribute, setup_uniform_B-phase.cc:263).
+ */
+glgpu_status glgpu_set_solution(glgpu_ctx *ctx, const double *x);
+glgpu_status glgpu_get_solution(const glgpu_ctx *ctx, double *x);
+
+/*
+ * FemGL<3>::assemble_system (femgl/src/assemble.cc:109-372): Jacobian (block CSR,
+ * condensed) and system_rhs = -R at the current solution.  In GLGPU_MIXED mode
+ * the Jacobian is FP32 and system_rhs comes from the FP64 residual kernel.
+ * rhs_norm (may be NULL) receives ||system_rhs|| per instance.
+ */
+glgpu_status glgpu_assemble_system(glgpu_ctx *ctx, double *rhs_norm);
+
+/*
+ * FemGL<3>::compute_residual (femgl/src/residual.cc:110-297) evaluated at the
+ * current solution; norm receives ||R|| per instance (residual_vector.l2_norm()).
+ */
+glgpu_status glgpu_compute_residual(glgpu_ctx *ctx, double *norm);
+
+/*
+ * FemGL<3>::solve(tol) (femgl/src/solve.cc:109-187): newton update delta with
+ * ||J delta - rhs|| <= tol ||rhs|| (per instance), then distributed through the
+ * constraints (solve.cc:181).  GMRES(restart) with the preconditioner of prm
+ * replaces FGMRES + Trilinos ML AMG.  its (may be NULL) gets the iteration count
+ * per instance.  Returns GLGPU_ERR_NOT_CONVERGED when gmres_max_iter is reached
+ * (delta is still the last iterate).
+ */
+glgpu_status glgpu_solve(glgpu_ctx *ctx, double tol, int *its);
+
+/*
+ * FemGL<3>::newton_iteration (femgl/src/iteration.cc:110-215): backtracking
+ * x + ls_step^i delta, i < ls_max_trials, accepting the first trial whose residual
+ * norm is below ||system_rhs||; when none is, the last trial is kept.  res (may be
+ * NULL) receives the residual norm at the accepted point, trials the number of
+ * trials evaluated (per instance).
+ */
+glgpu_status glgpu_newton_iteration(glgpu_ctx *ctx, double *res, int *trials);
+
+/*
+ * The free energy F = integral of K1|grad A|^2 + (K2+K3) sum_mu |div A_mu|^2
+ * + alpha tr(AA^+) + sum_t beta_t I_t at the current solution, per instance (FP64).
+ * The reference's residual is (1/2) dF/dx; the reference itself never evaluates F.
+ */
+glgpu_status glgpu_free_energy(glgpu_ctx *ctx, double *F);
+
+/*
+ * FemGL<3>::run Newton loop of one refinement cycle (femgl/src/run.cc:207-252):
+ * up to max_newton+1 times assemble, solve(linear_tol), newton_iteration, stop an
+ * instance when its residual <= converge_acc.  Per instance outputs (any may be
+ * NULL): newton_its, total GMRES iterations, final residual norm.
+ */
+glgpu_status glgpu_run(glgpu_ctx *ctx, int max_newton, double linear_tol, double converge_acc, int *newton_its,
+                       int *gmres_its, double *final_res);
+
+/* Downloads the pattern (rowptr [n_nodes+1], cols [nnzb]) and the Jacobian values
+ * as FP64 [nnzb][B][B] (any pointer may be NULL), plus system_rhs [n_nodes*B]. */
+glgpu_status glgpu_get_system(const glgpu_ctx *ctx, int32_t *rowptr, int32_t *cols, double *vals, double *rhs);
+
+/* Downloads residual_vector (+R, condensed) [n_nodes*B] of the last residual evaluation. */
+glgpu_status glgpu_get_residual(const glgpu_ctx *ctx, double *R);
+
+/* Downloads the last newton update delta [n_nodes*B]. */
+glgpu_status glgpu_get_update(const glgpu_ctx *ctx, double *delta);
+
+/* y = J x with the assembled Jacobian (in its stored precision), host vectors. */
+glgpu_status glgpu_spmv(glgpu_ctx *ctx, const double *x, double *y);
+
+/*
+ * Timing on the context's stream (CUDA events).  phase_ms receives accumulated
+ * milliseconds of {assembly, compute_residual, solve, newton_iteration} since
+ * the last reset, mirroring the reference's TimerOutput sections
+ * (assemble.cc:111, residual.cc:112, solve.cc:111, iteration.cc:112).
+ */
+glgpu_status glgpu_timers(glgpu_ctx *ctx, double *phase_ms, int reset);
+
+/*
+ * Per-kernel-class device time, measured with events around each launch when
+ * enable != 0 (small overhead): kernel_ms[k] and launches[k] for
+ * k = {spmv, cell assembly, row gather, residual, precond, vector ops}.
+ */
+glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, int64_t *launches, int reset);
+
+/* Number of kernels this context has launched since creation. */
+int64_t glgpu_launch_count(const glgpu_ctx *ctx);
+
+/* Blocks until all work of the context's stream is done. */
+glgpu_status glgpu_sync(glgpu_ctx *ctx);
+
+/* Device time (ms) between two calls on the context's stream: start, then stop. */
+glgpu_status glgpu_event_start(glgpu_ctx *ctx);
+glgpu_status glgpu_event_stop(glgpu_ctx *ctx, double *ms);
+
+/* ---------------------------------------------------------------------------
+ * Host-side helpers (no device work).
+ * --------------------------------------------------------------------------- */
+
+/*
+ * Matep (reference matep/src/matep.cc:140-206,213-250) at pressure p [bar] and
+ * t = T/Tc with strong-coupling corrections on (scc != 0) or off.
+ * out[13] = {alpha, beta1..beta5, gap_A, gap_B, Tc_mK, f_A, f_B, beta_A, beta_B}.
+ * p outside [0, 34) is rejected (the reference interpolation is undefined there).
+ */
+glgpu_status glgpu_matep(double p, double t, int scc, double *out);
+
+/*
+ * Structured box mesh in the reference's make_grid form
+ * (femgl/src/makegrid_cube-z-normal_AdGR.cc:157-195): [lo, hi] with n[3] cells,
+ * cells whose centre is within refine_band of a z face refined once (hanging nodes
+ * constrained as DoFTools::make_hanging_node_constraints does for Q1), and the
+ * zero-Dirichlet masks of the pair-breaking boundary (orbital column z of u and v
+ * on z faces, femgl.h:300-301; columns x/y on x/y faces when dirichlet_xy[0/1]).
+ * First call with NULL arrays to get the sizes, then with arrays of those sizes.
+ */
+glgpu_status glgpu_mesh_box(const double *lo, const double *hi, const int *n, double refine_band,
+                            const int *dirichlet_xy, int *n_nodes, int *n_cells, int *n_hang_entries, double *xyz,
+                            int32_t *cells, uint32_t *mask, int32_t *hang_ptr, int32_t *hang_parent,
+                            double *hang_weight);
+
+/*
+ * B-phase initial guess of setup_uniform_B-phase.cc:238-259: u11 = u22 = u33 =
+ * gap_B(p,t) * 0.577350269f, everything else 0, for n_nodes nodes.  When
+ * noise_sigma > 0 adds noise_sigma * N(0,1) per dof from a counter-based
+ * generator keyed by seed (the reference draws from an unseeded std::random_device;
+ * the seeded noise is this implementation's).
+ */
+glgpu_status glgpu_bphase_guess(double p, double t, int scc, int n_nodes, double noise_sigma, uint64_t seed,
+                                double *x);
+
+/*
+ * Host-only inspection of the once-per-mesh plan (no device needed):
+ * info[6] = {n_nodes, nnzb, longest block row, cell contributions, hanging targets,
+ * reduction segments}; the block pattern as CSR (rowptr [n_nodes+1], cols [nnzb]),
+ * the condensed sparsity of DoFTools::make_sparsity_pattern(..., constraints, false)
+ * at node granularity (femgl/src/setup_uniform_B-phase.cc:191-197).
+ */
+glgpu_status glgpu_plan_info(const glgpu_mesh *mesh, int n_inst, int64_t *info);
+glgpu_status glgpu_plan_pattern(const glgpu_mesh *mesh, int n_inst, int32_t *rowptr, int32_t *cols);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLGPU_H */

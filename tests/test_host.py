@@ -1,0 +1,120 @@
+"""CPU tests of the product's host side: the C-ABI library loads and exports every
+declared symbol, material parameters are bit-identical to the reference's, the box
+mesher and the block pattern agree with the oracle's independent ones."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from _lib import ROOT, oracle_mesh, product
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def gl():
+    return product()
+
+
+def test_library_exports_every_declared_symbol(gl):
+    header = open(os.path.join(ROOT, "include", "glgpu.h")).read()
+    declared = set(re.findall(r"\b(glgpu_[a-z_]+)\s*\(", header))
+    assert len(declared) >= 25
+    L = gl.lib()
+    missing = [s for s in sorted(declared) if not hasattr(L, s)]
+    assert not missing, missing
+    assert L.glgpu_version().decode().startswith("glgpu")
+
+
+def test_matep_bit_identical_to_reference(gl):
+    d = json.load(open(os.path.join(GOLD, "matep.json")))
+    fields = d["fields"]
+    for row in d["rows"]:
+        got = gl.matep(row["p"], row["t"], bool(row["scc"]))
+        for f, ref in zip(fields, row["out"]):
+            assert got[f] == ref, (row["p"], row["t"], row["scc"], f, got[f], ref)
+
+
+def test_matep_rejects_pressure_outside_table(gl):
+    with pytest.raises(gl.GLGPUError):
+        gl.matep(34.0, 0.5)
+    with pytest.raises(gl.GLGPUError):
+        gl.matep(-0.1, 0.5)
+
+
+@pytest.mark.parametrize("n,frac", [(3, 0.0), (4, 0.25), (6, 1.0 / 6.0)])
+def test_box_mesh_matches_oracle_mesher(gl, n, frac):
+    from oracle import mesh as om
+
+    p = gl.cube_mesh(10.0, n, frac)
+    o = om.cube_mesh(10.0, n, frac)
+    assert np.array_equal(p.cells, o.cells)
+    assert np.allclose(p.xyz, o.xyz, rtol=0, atol=1e-12)
+    assert np.array_equal(p.mask, o.mask)
+    assert np.array_equal(p.hptr, o.hptr)
+    assert np.array_equal(p.hpar, o.hpar)
+    assert np.allclose(p.hw, o.hw)
+
+
+def test_refined_cube_sizes_match_literal_geometry(gl):
+    """64^3 cube, cells within 0.1 L of a z face refined once: 6 fine layers per side."""
+    m = gl.cube_mesh(10.0, 64, 0.1)
+    assert (m.nn, m.nc, m.n_hanging) == (648141, 606208, 24832)
+    # hanging weights: 1/2 on edges, 1/4 on faces, always summing to 1
+    w = np.add.reduceat(m.hw, m.hptr[:-1][np.diff(m.hptr) > 0])
+    assert np.allclose(w, 1.0)
+
+
+def test_z_faces_pair_breaking_mask(gl):
+    m = gl.cube_mesh(10.0, 4)
+    zmask = sum(1 << (9 * p + 3 * mu + 2) for p in range(2) for mu in range(3))
+    onz = np.isclose(np.abs(m.xyz[:, 2]), 10.0)
+    assert np.all(m.mask[onz] == zmask)
+    assert np.all(m.mask[~onz] == 0)
+
+
+@pytest.mark.parametrize("n,frac", [(4, 0.0), (4, 0.25)])
+def test_block_pattern_matches_oracle(gl, oracle_gl, n, frac):
+    m = gl.cube_mesh(10.0, n, frac)
+    rowptr, cols = gl.plan_pattern([m])
+    sysr = oracle_gl.System(oracle_mesh(m), np.zeros(8))
+    assert np.array_equal(rowptr, sysr.rowptr)
+    assert np.array_equal(cols, sysr.cols)
+
+
+def test_plan_sizes_config_32cube(gl):
+    info = gl.plan_info([gl.cube_mesh(10.0, 32)])
+    assert info["n_nodes"] == 35937
+    assert info["nnzb"] == 912673  # 97^3 node pairs
+    assert info["max_row_blocks"] == 27
+
+
+def test_batched_plan_concatenates(gl):
+    a, b = gl.cube_mesh(10.0, 3), gl.cube_mesh(5.0, 4, 0.25)
+    ia, ib, iab = gl.plan_info([a]), gl.plan_info([b]), gl.plan_info([a, b])
+    assert iab["n_nodes"] == ia["n_nodes"] + ib["n_nodes"]
+    assert iab["nnzb"] == ia["nnzb"] + ib["nnzb"]
+
+
+def test_invalid_meshes_rejected(gl):
+    m = gl.cube_mesh(10.0, 2)
+    bad = gl.Mesh(3, m.xyz.copy(), m.cells.copy(), m.mask.copy())
+    bad.cells[0, 0] = m.nn + 5
+    with pytest.raises(gl.GLGPUError):
+        gl.plan_info([bad])
+    skew = gl.Mesh(3, m.xyz.copy(), m.cells.copy(), m.mask.copy())
+    skew.xyz[skew.cells[0, 7], 0] += 0.3
+    with pytest.raises(gl.GLGPUError):
+        gl.plan_info([skew])
+
+
+def test_bphase_guess(gl):
+    x = gl.bphase_guess(20.0, 0.6, 5).reshape(5, 18)
+    g = gl.matep(20.0, 0.6)["gap_B"] * float(np.float32(0.577350269))
+    assert np.all(x[:, [0, 4, 8]] == g)
+    assert np.all(x[:, [1, 2, 3, 5, 6, 7]] == 0) and np.all(x[:, 9:] == 0)
+    y = gl.bphase_guess(20.0, 0.6, 5, noise=0.05, seed=2).reshape(5, 18)
+    z = gl.bphase_guess(20.0, 0.6, 5, noise=0.05, seed=2).reshape(5, 18)
+    assert np.array_equal(y, z) and 0.0 < np.std(y - x) < 0.2

@@ -1,0 +1,114 @@
+// Device-side data of one context and the launchers the context code calls.
+// All launchers enqueue on the given stream and return cudaError_t of the launch.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace glgpu
+{
+constexpr int kNS3 = 171;   // unique entries of a symmetric 18x18 block
+constexpr int kCoef = 8;    // {K1, K2+K3, alpha, beta1..beta5}
+constexpr int kSegThreads = 256;
+
+// Mesh and plan arrays resident on the device (read-only during solves).
+struct DevMesh
+{
+  int dim, B, nv, n_inst;
+  int64_t nn, nc, nnzb;
+  int max_row_blocks;
+  const int32_t *cells;       // [nc][nv]
+  const double *cell_h;       // [nc][3]
+  const int32_t *cell_inst;   // [nc]
+  const int32_t *node_inst;   // [nn]
+  const uint32_t *mask;       // [nn]
+  const int32_t *hptr, *hpar; // hanging CSR
+  const double *hw;
+  const int32_t *rowptr, *cols, *diag;
+  const int32_t *rc_ptr, *rc_cell, *rc_a;
+  const double *rc_w;
+  const int16_t *rc_slot;
+  const int64_t *ht_off;
+  const void *hang_tg;        // HangTarget[]
+  const double *coef;         // [n_inst][kCoef]
+  // segments for per-instance reductions over scalar vectors (length nn*B)
+  int n_seg;
+  const int64_t *seg_begin, *seg_end;
+  const int32_t *seg_inst;
+  const int32_t *inst_seg_off;
+  const int64_t *cell_off;    // [n_inst+1]
+};
+
+// ---- assembly (kernels_asm.cu) ----
+// Per-cell quadrature data: H [nc][nq][NS] (type T) and/or cell residual
+// r_cell [nc][nv*B] (double) and per-cell free energy (double).
+cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, double *r_cell, double *e_cell,
+                        const uint8_t *inst_active, cudaStream_t s);
+// Row gather of the condensed Jacobian from H (type fp32 ? float : double) into vals.
+cudaError_t launch_rows(const DevMesh &m, bool fp32, const void *H, void *vals, cudaStream_t s);
+// Condensed residual R [nn*B] from r_cell.
+cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *inst_active,
+                              cudaStream_t s);
+cudaError_t init_constants();
+
+// ---- linear algebra (kernels_la.cu) ----
+cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y,
+                        const uint8_t *inst_active, cudaStream_t s);
+cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s);
+cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const void *x, void *y,
+                            const uint8_t *inst_active, cudaStream_t s);
+// partial[s][v] = sum over segment s of X[v][i] * y[i], v < nv (X rows strided by ld)
+cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const void *y,
+                            double *partial, const uint8_t *inst_active, cudaStream_t s);
+// out[inst][v] = sum of partial[s][v] over the instance's segments (ld_out = stride of out per inst)
+cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nvec, double *out, int ld_out,
+                                int take_sqrt, cudaStream_t s);
+// y -= sum_v coef[inst][v] X[v]   (coef ld = ldc doubles per instance)
+cudaError_t launch_seg_maxpy(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
+                             int ldc, void *y, const uint8_t *inst_active, cudaStream_t s);
+// generic per-instance vector update: y = a[inst]*x + b[inst]*y (+ c[inst]*z when z != NULL);
+// a, b, c index per instance with the given strides (stride 0 = a scalar held at a[0])
+struct Axpby
+{
+  const double *a;
+  int sa;
+  const double *b;
+  int sb;
+  const double *c;
+  int sc;
+  double a0, b0, c0; // used when the pointer is NULL
+};
+cudaError_t launch_seg_axpby(const DevMesh &m, bool x32, const void *x, bool y32, void *y, bool z32, const void *z,
+                             const Axpby &k, const uint8_t *inst_active, cudaStream_t s);
+// x_trial = distribute(x + a[inst] * delta) for active instances
+cudaError_t launch_trial(const DevMesh &m, const double *x, const double *delta, const double *a, double *xt,
+                         const uint8_t *inst_active, cudaStream_t s);
+// v <- distribute(v) (hanging = weighted parents, Dirichlet = 0), double vector
+cudaError_t launch_distribute(const DevMesh &m, double *v, cudaStream_t s);
+// out[inst] = sum of e_cell over the instance's cells (deterministic)
+cudaError_t launch_cell_sum(const DevMesh &m, const double *e_cell, double *out, cudaStream_t s);
+
+// GMRES small dense work (per instance, one thread each)
+struct GmresDev
+{
+  int m;                 // restart length
+  double *H;             // [n_inst][(m+1)*m] column-major Hessenberg
+  double *cs, *sn;       // [n_inst][m]
+  double *g;             // [n_inst][m+1]
+  double *y;             // [n_inst][m]
+  double *hcol;          // [n_inst][m+2] column under construction (h_0..h_j, h_{j+1})
+  double *hcol2;         // second CGS pass
+  double *beta;          // [n_inst] norms
+  double *tol;           // [n_inst] absolute tolerance
+  double *res_est;       // [n_inst] current residual estimate
+  int *its;              // [n_inst] columns used in this cycle
+  uint8_t *active;       // [n_inst] still iterating in this cycle
+  double *inv_scale;     // [n_inst] 1/h_{j+1,j} (0 on breakdown)
+};
+cudaError_t launch_gmres_start(const GmresDev &g, int n_inst, const uint8_t *solve_active, cudaStream_t s);
+cudaError_t launch_gmres_column(const GmresDev &g, int n_inst, int j, cudaStream_t s);
+cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);
+// scale factors for the new basis vector from the norm (inv_scale = 1/norm or 0)
+cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s);
+
+} // namespace glgpu

@@ -1,0 +1,1099 @@
+// Context, C ABI entry points and the host-side control flow of the Newton path.
+//
+// Reference control flow restated here (paths relative to the reference root):
+//   run()              femgl/src/run.cc:207-252   assemble -> solve -> newton_iteration -> test
+//   assemble_system()  femgl/src/assemble.cc:109-372
+//   compute_residual() femgl/src/residual.cc:110-297
+//   solve(tol)         femgl/src/solve.cc:109-187 (FGMRES + ML AMG there; GMRES(m) with
+//                      block-Jacobi or Chebyshev/block-Jacobi preconditioning here)
+//   newton_iteration() femgl/src/iteration.cc:110-215
+// All device work goes to the context's stream; the host only decides control flow
+// from per-instance scalars (norms, flags) it reads back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+#include "glgpu.h"
+#include "glgpu_internal.h"
+
+namespace glgpu
+{
+static thread_local std::string g_last_error;
+
+glgpu_status set_error(glgpu_status s, const std::string &msg)
+{
+  g_last_error = msg;
+  return s;
+}
+
+enum KernelKind
+{
+  KK_SPMV = 0,
+  KK_CELL = 1,
+  KK_ROWS = 2,
+  KK_RES = 3,
+  KK_PREC = 4,
+  KK_VEC = 5,
+  KK_N = 6
+};
+
+enum Phase
+{
+  PH_ASM = 0,
+  PH_RES = 1,
+  PH_SOLVE = 2,
+  PH_NEWTON = 3,
+  PH_N = 4
+};
+
+template <typename T> struct DBuf
+{
+  T *p = nullptr;
+  size_t n = 0;
+};
+
+} // namespace glgpu
+
+using namespace glgpu;
+
+struct glgpu_ctx
+{
+  Plan P;
+  DevMesh dm{};
+  std::vector<glgpu_params> prm;
+  int B = 18, n_inst = 1, nq = 8, ns = 171;
+  int64_t nn = 0, N = 0, nnzb = 0;
+  bool mixed = false;
+  int restart = 50;
+  cudaStream_t st = nullptr;
+  std::vector<void *> allocs;
+  // state
+  double *x = nullptr, *xt = nullptr, *delta = nullptr, *R = nullptr, *rhs = nullptr;
+  double *r_cell = nullptr, *e_cell = nullptr;
+  void *H = nullptr, *vals = nullptr, *dinv = nullptr;
+  // Krylov (element type T = float in mixed mode, double otherwise)
+  void *V = nullptr, *Z = nullptr, *X = nullptr, *Tmp = nullptr, *Bv = nullptr, *C1 = nullptr, *C2 = nullptr,
+       *C3 = nullptr;
+  double *partial = nullptr;
+  GmresDev g{};
+  // per-instance small arrays (device)
+  double *d_norm = nullptr, *d_a = nullptr, *d_energy = nullptr, *d_cheb = nullptr, *d_tmp = nullptr;
+  uint8_t *d_act = nullptr, *d_act2 = nullptr;
+  // pinned host mirrors
+  double *h_norm = nullptr, *h_res = nullptr;
+  uint8_t *h_act = nullptr;
+  int *h_its = nullptr;
+  // host-side per-instance state
+  std::vector<double> rhs_norm, res_norm, lam_max;
+  std::vector<uint8_t> inst_on;
+  bool has_J = false, has_rhs = false, has_delta = false, prec_ready = false;
+  // timing
+  bool ktiming = false;
+  int64_t launches = 0;
+  int64_t klaunch[KK_N] = {0};
+  double kms[KK_N] = {0};
+  double phase_ms[PH_N] = {0};
+  struct EvRec
+  {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<EvRec> kev, pev;
+  std::vector<cudaEvent_t> ev_pool;
+  cudaEvent_t ev_user0 = nullptr, ev_user1 = nullptr;
+};
+
+namespace
+{
+#define CK(call)                                                                                                     \
+  do                                                                                                                 \
+    {                                                                                                                \
+      cudaError_t e_ = (call);                                                                                       \
+      if (e_ != cudaSuccess)                                                                                         \
+        return set_error(GLGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    }                                                                                                                \
+  while (0)
+
+#define CKS(call)                                                                                                    \
+  do                                                                                                                 \
+    {                                                                                                                \
+      glgpu_status s_ = (call);                                                                                      \
+      if (s_ != GLGPU_OK) return s_;                                                                                 \
+    }                                                                                                                \
+  while (0)
+
+cudaEvent_t get_event(glgpu_ctx *c)
+{
+  if (!c->ev_pool.empty())
+    {
+      cudaEvent_t e = c->ev_pool.back();
+      c->ev_pool.pop_back();
+      return e;
+    }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// harvest finished event pairs into the accumulators (synchronizes on them)
+void harvest(glgpu_ctx *c)
+{
+  for (auto &r : c->kev)
+    {
+      float ms = 0.f;
+      cudaEventSynchronize(r.b);
+      if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) c->kms[r.kind] += ms;
+      c->ev_pool.push_back(r.a);
+      c->ev_pool.push_back(r.b);
+    }
+  c->kev.clear();
+  for (auto &r : c->pev)
+    {
+      float ms = 0.f;
+      cudaEventSynchronize(r.b);
+      if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) c->phase_ms[r.kind] += ms;
+      c->ev_pool.push_back(r.a);
+      c->ev_pool.push_back(r.b);
+    }
+  c->pev.clear();
+}
+
+// launch wrapper: counts launches, optional per-kind event timing
+template <typename F> glgpu_status launch(glgpu_ctx *c, int kind, int nk, F &&f)
+{
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->ktiming)
+    {
+      a = get_event(c);
+      b = get_event(c);
+      cudaEventRecord(a, c->st);
+    }
+  cudaError_t e = f();
+  if (e != cudaSuccess) return set_error(GLGPU_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  c->launches += nk;
+  c->klaunch[kind] += nk;
+  if (c->ktiming)
+    {
+      cudaEventRecord(b, c->st);
+      c->kev.push_back({kind, a, b});
+      if (c->kev.size() > 4096) harvest(c);
+    }
+  return GLGPU_OK;
+}
+
+struct PhaseScope
+{
+  glgpu_ctx *c;
+  int ph;
+  cudaEvent_t a, b;
+  PhaseScope(glgpu_ctx *c_, int ph_) : c(c_), ph(ph_)
+  {
+    a = get_event(c);
+    b = get_event(c);
+    cudaEventRecord(a, c->st);
+  }
+  ~PhaseScope()
+  {
+    cudaEventRecord(b, c->st);
+    c->pev.push_back({ph, a, b});
+    if (c->pev.size() > 4096) harvest(c);
+  }
+};
+
+template <typename T> glgpu_status dalloc(glgpu_ctx *c, T **p, size_t n)
+{
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T));
+  if (e != cudaSuccess)
+    return set_error(GLGPU_ERR_NOMEM, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " +
+                                          cudaGetErrorString(e));
+  c->allocs.push_back(*p);
+  return GLGPU_OK;
+}
+
+template <typename T> glgpu_status dupload(glgpu_ctx *c, T **p, const std::vector<T> &v)
+{
+  CKS(dalloc(c, p, v.size()));
+  if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return GLGPU_OK;
+}
+
+size_t tsz(const glgpu_ctx *c) { return c->mixed ? sizeof(float) : sizeof(double); }
+
+void *tptr(const glgpu_ctx *c, void *base, int64_t off) { return static_cast<char *>(base) + off * tsz(c); }
+
+glgpu_status sync(glgpu_ctx *c)
+{
+  cudaError_t e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return set_error(GLGPU_ERR_CUDA, std::string("stream sync: ") + cudaGetErrorString(e));
+  return GLGPU_OK;
+}
+
+// per-instance 2-norms of a double vector into d_norm and h_norm (synchronizes)
+glgpu_status norms_d(glgpu_ctx *c, const double *v, const uint8_t *act, std::vector<double> &out)
+{
+  CKS(launch(c, KK_VEC, 1,
+             [&] { return launch_seg_mdot(c->dm, false, v, 0, 1, v, c->partial, act, c->st); }));
+  CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->d_norm, 1, 1, c->st); }));
+  CK(cudaMemcpyAsync(c->h_norm, c->d_norm, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
+  CKS(sync(c));
+  out.assign(c->h_norm, c->h_norm + c->n_inst);
+  return GLGPU_OK;
+}
+
+glgpu_status upload_act(glgpu_ctx *c, uint8_t *dst, const std::vector<uint8_t> &a)
+{
+  std::memcpy(c->h_act, a.data(), a.size());
+  CK(cudaMemcpyAsync(dst, c->h_act, a.size(), cudaMemcpyHostToDevice, c->st));
+  CKS(sync(c)); // h_act is reused; keep the copy ordered with the next host write
+  return GLGPU_OK;
+}
+
+glgpu_status upload_d(glgpu_ctx *c, double *dst, const std::vector<double> &a)
+{
+  std::memcpy(c->h_res, a.data(), a.size() * sizeof(double));
+  CK(cudaMemcpyAsync(dst, c->h_res, a.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CKS(sync(c));
+  return GLGPU_OK;
+}
+
+// residual at vector v (x or xt) for instances in act: R, e_cell
+glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act)
+{
+  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, v, nullptr, c->r_cell, c->e_cell, act, c->st); }));
+  CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
+  return GLGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// preconditioner
+// ---------------------------------------------------------------------------------
+glgpu_status bj(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
+{
+  return launch(c, KK_PREC, 1, [&] { return launch_bj_apply(c->dm, c->mixed, c->dinv, in, out, act, c->st); });
+}
+
+glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
+{
+  return launch(c, KK_SPMV, 1, [&] { return launch_spmv(c->dm, c->mixed, c->vals, in, out, act, c->st); });
+}
+
+glgpu_status axpby(glgpu_ctx *c, const void *x, void *y, const void *z, const Axpby &k, const uint8_t *act,
+                   bool x32, bool y32, bool z32)
+{
+  return launch(c, KK_VEC, 1, [&] { return launch_seg_axpby(c->dm, x32, x, y32, y, z32, z, k, act, c->st); });
+}
+
+Axpby coefs(double a, double b, double cc = 0.0)
+{
+  Axpby k{};
+  k.a0 = a;
+  k.b0 = b;
+  k.c0 = cc;
+  return k;
+}
+
+// Chebyshev coefficients per instance: d_cheb[k][0..1] = theta, delta
+glgpu_status cheb_setup(glgpu_ctx *c)
+{
+  const bool m = c->mixed;
+  const int n_inst = c->n_inst;
+  // power iteration on D^-1 J, 12 steps, deterministic start vector of ones (Dirichlet zeros kept)
+  CKS(axpby(c, nullptr, c->C1, nullptr, coefs(0.0, 0.0), nullptr, m, m, m));
+  // C1 = 1 everywhere: use y = a*x + b*y with x = NULL is zero; set via z trick: use Tmp
+  {
+    std::vector<double> ones(c->N, 1.0);
+    double *tmpd = c->xt; // scratch double vector
+    CK(cudaMemcpyAsync(tmpd, ones.data(), sizeof(double) * c->N, cudaMemcpyHostToDevice, c->st));
+    CK(launch_distribute(c->dm, tmpd, c->st));
+    c->launches += 2;
+    CKS(axpby(c, tmpd, c->C1, nullptr, coefs(1.0, 0.0), nullptr, false, m, m));
+    CKS(sync(c));
+  }
+  std::vector<double> lam(n_inst, 1.0);
+  for (int it = 0; it < 12; ++it)
+    {
+      CKS(spmv(c, c->C1, c->C2, nullptr));
+      CKS(bj(c, c->C2, c->C3, nullptr));
+      // norms of C3 and C1
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m, c->C3, 0, 1, c->C3, c->partial, nullptr, c->st); }));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->d_norm, 1, 1, c->st); }));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m, c->C1, 0, 1, c->C1, c->partial, nullptr, c->st); }));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->d_tmp, 1, 1, c->st); }));
+      CK(cudaMemcpyAsync(c->h_norm, c->d_norm, sizeof(double) * n_inst, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(c->h_res, c->d_tmp, sizeof(double) * n_inst, cudaMemcpyDeviceToHost, c->st));
+      CKS(sync(c));
+      for (int k = 0; k < n_inst; ++k) lam[k] = (c->h_res[k] > 0) ? c->h_norm[k] / c->h_res[k] : 1.0;
+      // C1 = C3 / |C3|
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_inv(c->d_norm, c->d_tmp, n_inst, c->st); }));
+      Axpby k{};
+      k.a = c->d_tmp;
+      k.sa = 1;
+      k.b0 = 0.0;
+      CKS(axpby(c, c->C3, c->C1, nullptr, k, nullptr, m, m, m));
+    }
+  c->lam_max.resize(n_inst);
+  std::vector<double> tc(2 * n_inst);
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const double lmax = 1.1 * lam[k];
+      const double lmin = lmax / 30.0;
+      c->lam_max[k] = lmax;
+      tc[2 * k] = 0.5 * (lmax + lmin);
+      tc[2 * k + 1] = 0.5 * (lmax - lmin);
+    }
+  std::memcpy(c->h_res, tc.data(), sizeof(double) * 2 * n_inst);
+  CK(cudaMemcpyAsync(c->d_cheb, c->h_res, sizeof(double) * 2 * n_inst, cudaMemcpyHostToDevice, c->st));
+  CKS(sync(c));
+  return GLGPU_OK;
+}
+
+// z = M^-1 v
+glgpu_status precond(glgpu_ctx *c, const void *v, void *z, const uint8_t *act)
+{
+  const bool m = c->mixed;
+  const int pc = c->prm[0].precond;
+  if (pc == GLGPU_PC_NONE) return axpby(c, v, z, nullptr, coefs(1.0, 0.0), act, m, m, m);
+  if (pc == GLGPU_PC_BLOCK_JACOBI) return bj(c, v, z, act);
+  // Chebyshev semi-iteration for J z = v preconditioned by D^-1, started at z = 0.
+  // Step scalars per instance live at d_cheb + 2 n_inst as [deg][n_inst][2]:
+  // step 0 uses (0, 1/theta), step i >= 1 uses (rho_i rho_{i-1}, 2 rho_i / delta).
+  const int deg = std::max(1, c->prm[0].cheb_degree);
+  const double *sc = c->d_cheb + 2 * c->n_inst;
+  CKS(axpby(c, v, c->C1, nullptr, coefs(1.0, 0.0), act, m, m, m)); // r = v
+  CKS(bj(c, c->C1, c->C2, act));                                     // d = D^-1 r
+  {
+    Axpby k{};
+    k.a = sc + 1;
+    k.sa = 2;
+    CKS(axpby(c, c->C2, c->C2, nullptr, k, act, m, m, m)); // d = d / theta
+  }
+  CKS(axpby(c, c->C2, z, nullptr, coefs(1.0, 0.0), act, m, m, m)); // z = d
+  for (int i = 1; i < deg; ++i)
+    {
+      CKS(spmv(c, c->C2, c->C3, act));                                       // C3 = J d
+      CKS(axpby(c, c->C3, c->C1, nullptr, coefs(-1.0, 1.0), act, m, m, m));  // r -= J d
+      CKS(bj(c, c->C1, c->C3, act));                                         // C3 = D^-1 r
+      Axpby k{};
+      k.b = sc + static_cast<int64_t>(i) * 2 * c->n_inst;
+      k.sb = 2;
+      k.a = sc + static_cast<int64_t>(i) * 2 * c->n_inst + 1;
+      k.sa = 2;
+      CKS(axpby(c, c->C3, c->C2, nullptr, k, act, m, m, m));                 // d = c_d d + c_r D^-1 r
+      CKS(axpby(c, c->C2, z, nullptr, coefs(1.0, 1.0), act, m, m, m));       // z += d
+    }
+  return GLGPU_OK;
+}
+
+glgpu_status cheb_coeffs(glgpu_ctx *c)
+{
+  const int deg = std::max(1, c->prm[0].cheb_degree);
+  const int n = c->n_inst;
+  std::vector<double> tcv(2 * n);
+  CK(cudaMemcpy(tcv.data(), c->d_cheb, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+  std::vector<double> sc(static_cast<size_t>(deg) * 2 * n, 0.0);
+  for (int k = 0; k < n; ++k)
+    {
+      const double theta = tcv[2 * k], delta = tcv[2 * k + 1];
+      const double sigma = theta / delta;
+      double rho_old = 1.0 / sigma;
+      sc[2 * k + 0] = 0.0;
+      sc[2 * k + 1] = 1.0 / theta;
+      for (int i = 1; i < deg; ++i)
+        {
+          const double rho = 1.0 / (2.0 * sigma - rho_old);
+          sc[(static_cast<size_t>(i) * n + k) * 2 + 0] = rho * rho_old;
+          sc[(static_cast<size_t>(i) * n + k) * 2 + 1] = 2.0 * rho / delta;
+          rho_old = rho;
+        }
+    }
+  CK(cudaMemcpy(c->d_cheb + 2 * n, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice));
+  return GLGPU_OK;
+}
+
+glgpu_status prec_setup(glgpu_ctx *c)
+{
+  if (c->prec_ready) return GLGPU_OK;
+  const int pc = c->prm[0].precond;
+  if (pc >= GLGPU_PC_BLOCK_JACOBI)
+    CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(c->dm, c->mixed, c->vals, c->dinv, c->st); }));
+  if (pc == GLGPU_PC_CHEBYSHEV)
+    {
+      CKS(cheb_setup(c));
+      CKS(cheb_coeffs(c));
+    }
+  c->prec_ready = true;
+  return GLGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// GMRES(m), right preconditioned, classical Gram-Schmidt with one reorthogonalization
+// ---------------------------------------------------------------------------------
+glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std::vector<int> &its_out,
+                   bool &all_conv)
+{
+  const bool m32 = c->mixed;
+  const int n = c->n_inst, mr = c->restart;
+  const int64_t N = c->N;
+  const int maxit = std::max(1, c->prm[0].gmres_max_iter);
+  std::vector<double> tol_abs(n);
+  for (int k = 0; k < n; ++k) tol_abs[k] = tol * c->rhs_norm[k];
+  CKS(upload_d(c, c->g.tol, tol_abs));
+  CKS(upload_act(c, c->d_act2, on));
+  // b in Krylov precision, X = 0
+  CKS(axpby(c, c->rhs, c->Bv, nullptr, coefs(1.0, 0.0), nullptr, false, m32, m32));
+  CKS(axpby(c, nullptr, c->X, nullptr, coefs(0.0, 0.0), nullptr, m32, m32, m32));
+  std::vector<int> total(n, 0);
+  std::vector<uint8_t> solve_on(on);
+  all_conv = false;
+  for (int cycle = 0;; ++cycle)
+    {
+      // V0 = b - J X
+      if (cycle == 0)
+        CKS(axpby(c, c->Bv, c->V, nullptr, coefs(1.0, 0.0), c->d_act2, m32, m32, m32));
+      else
+        {
+          CKS(spmv(c, c->X, c->Tmp, c->d_act2));
+          CKS(axpby(c, c->Bv, c->V, c->Tmp, coefs(1.0, 0.0, -1.0), c->d_act2, m32, m32, m32));
+        }
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m32, c->V, 0, 1, c->V, c->partial, c->d_act2, c->st); }));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->g.beta, 1, 1, c->st); }));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_start(c->g, n, c->d_act2, c->st); }));
+      {
+        Axpby k{};
+        k.a = c->g.inv_scale;
+        k.sa = 1;
+        CKS(axpby(c, c->V, c->V, nullptr, k, c->g.active, m32, m32, m32));
+      }
+      CK(cudaMemcpyAsync(c->h_act, c->g.active, n, cudaMemcpyDeviceToHost, c->st));
+      CKS(sync(c));
+      bool any = false;
+      for (int k = 0; k < n; ++k) any |= c->h_act[k] != 0;
+      if (!any)
+        {
+          all_conv = true;
+          break;
+        }
+      int jdone = 0;
+      for (int j = 0; j < mr; ++j)
+        {
+          void *Vj = tptr(c, c->V, static_cast<int64_t>(j) * N);
+          void *Vj1 = tptr(c, c->V, static_cast<int64_t>(j + 1) * N);
+          CKS(precond(c, Vj, c->Z, c->g.active));
+          CKS(spmv(c, c->Z, Vj1, c->g.active));
+          for (int pass = 0; pass < 2; ++pass)
+            {
+              double *hc = pass == 0 ? c->g.hcol : c->g.hcol2;
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_seg_mdot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.active, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, hc, mr + 2, 0, c->st); }));
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_seg_maxpy(c->dm, m32, c->V, N, j + 1, hc, mr + 2, Vj1, c->g.active, c->st);
+              }));
+            }
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m32, Vj1, 0, 1, Vj1, c->partial, c->g.active, c->st); }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->g.hcol + j + 1, mr + 2, 1, c->st); }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_column(c->g, n, j, c->st); }));
+          {
+            Axpby k{};
+            k.a = c->g.inv_scale;
+            k.sa = 1;
+            CKS(axpby(c, Vj1, Vj1, nullptr, k, c->g.active, m32, m32, m32));
+          }
+          jdone = j + 1;
+          CK(cudaMemcpyAsync(c->h_act, c->g.active, n, cudaMemcpyDeviceToHost, c->st));
+          CKS(sync(c));
+          bool anyj = false;
+          for (int k = 0; k < n; ++k) anyj |= c->h_act[k] != 0;
+          if (!anyj) break;
+        }
+      // X += M^-1 (V y)
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_solve_y(c->g, n, c->st); }));
+      CKS(axpby(c, nullptr, c->Tmp, nullptr, coefs(0.0, 0.0), c->d_act2, m32, m32, m32));
+      CKS(launch(c, KK_VEC, 1, [&] {
+        return launch_seg_maxpy(c->dm, m32, c->V, N, jdone, c->g.y, mr, c->Tmp, c->d_act2, c->st);
+      }));
+      CKS(precond(c, c->Tmp, c->Z, c->d_act2));
+      CKS(axpby(c, c->Z, c->X, nullptr, coefs(1.0, 1.0), c->d_act2, m32, m32, m32));
+      CK(cudaMemcpyAsync(c->h_its, c->g.its, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(c->h_norm, c->g.res_est, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+      CKS(sync(c));
+      bool more = false;
+      for (int k = 0; k < n; ++k)
+        {
+          if (!solve_on[k]) continue;
+          total[k] += c->h_its[k];
+          const bool conv = c->h_norm[k] <= tol_abs[k];
+          if (conv || total[k] >= maxit || !std::isfinite(c->h_norm[k]))
+            solve_on[k] = 0;
+          else
+            more = true;
+        }
+      if (!more)
+        {
+          // converged unless an instance ran out of iterations: verify with the true residual
+          all_conv = true;
+          for (int k = 0; k < n; ++k)
+            if (on[k] && (total[k] >= maxit && c->h_norm[k] > tol_abs[k])) all_conv = false;
+          break;
+        }
+      CKS(upload_act(c, c->d_act2, solve_on));
+    }
+  // delta = X (double), distributed through the constraints
+  CKS(axpby(c, c->X, c->delta, nullptr, coefs(1.0, 0.0), nullptr, m32, false, false));
+  CK(launch_distribute(c->dm, c->delta, c->st));
+  c->launches += 2;
+  its_out = total;
+  return GLGPU_OK;
+}
+
+} // namespace
+
+// =================================================================================
+// C ABI
+// =================================================================================
+extern "C" void glgpu_default_params(glgpu_params *p)
+{
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->K1 = p->K2 = p->K3 = 0.42072;
+  p->alpha = 0.0;
+  p->precision = GLGPU_FP64;
+  p->precond = GLGPU_PC_BLOCK_JACOBI;
+  p->cheb_degree = 3;
+  p->gmres_restart = 50;
+  p->gmres_max_iter = 10000;
+  p->ls_step = 0.83;
+  p->ls_max_trials = 100;
+  p->damped = 1;
+}
+
+extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
+
+extern "C" const char *glgpu_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst, glgpu_ctx **out)
+{
+  if (!out || !prm) return set_error(GLGPU_ERR_ARG, "glgpu_create: NULL argument");
+  *out = nullptr;
+  for (int k = 0; k < n_inst; ++k)
+    {
+      if (prm[k].precision != prm[0].precision || prm[k].precond != prm[0].precond ||
+          prm[k].gmres_restart != prm[0].gmres_restart)
+        return set_error(GLGPU_ERR_ARG, "glgpu_create: precision, preconditioner and restart must match across instances");
+    }
+  if (prm[0].gmres_restart < 1 || prm[0].gmres_restart > 64)
+    return set_error(GLGPU_ERR_ARG, "glgpu_create: gmres_restart must be in [1, 64]");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    return set_error(GLGPU_ERR_CUDA, "glgpu_create: no CUDA device");
+  glgpu_ctx *c = new glgpu_ctx();
+  glgpu_status s = build_plan(mesh, n_inst, c->P);
+  if (s != GLGPU_OK)
+    {
+      delete c;
+      return s;
+    }
+  auto fail = [&](glgpu_status st) {
+    std::string msg = g_last_error;
+    glgpu_destroy(c);
+    g_last_error = msg;
+    return st;
+  };
+  const Plan &P = c->P;
+  c->prm.assign(prm, prm + n_inst);
+  c->B = P.B;
+  c->n_inst = n_inst;
+  c->nn = P.nn;
+  c->N = P.nn * P.B;
+  c->nnzb = P.nnzb;
+  c->nq = (P.dim == 3) ? 8 : 4;
+  c->ns = (P.dim == 3) ? kNS3 : 3;
+  c->mixed = prm[0].precision == GLGPU_MIXED;
+  c->restart = prm[0].gmres_restart;
+  if (P.dim == 3 && static_cast<size_t>(P.max_row_blocks) * 324 * (c->mixed ? 4 : 8) > 220 * 1024)
+    return fail(set_error(GLGPU_ERR_ARG, "glgpu_create: a block row is too long for on-chip accumulation"));
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_error(GLGPU_ERR_CUDA, "glgpu_create: stream creation failed"));
+  if (init_constants() != cudaSuccess) return fail(set_error(GLGPU_ERR_CUDA, "glgpu_create: constant upload failed"));
+  DevMesh &d = c->dm;
+  d.dim = P.dim;
+  d.B = P.B;
+  d.nv = P.nv;
+  d.n_inst = n_inst;
+  d.nn = P.nn;
+  d.nc = P.nc;
+  d.nnzb = P.nnzb;
+  d.max_row_blocks = P.max_row_blocks;
+  int32_t *p_cells, *p_ci, *p_ni, *p_hptr, *p_hpar, *p_rowptr, *p_cols, *p_diag, *p_rcp, *p_rcc, *p_rca, *p_si, *p_iso;
+  uint32_t *p_mask;
+  double *p_h, *p_hw, *p_rcw, *p_coef;
+  int16_t *p_slot;
+  int64_t *p_hto, *p_sb, *p_se, *p_co;
+  HangTarget *p_tg;
+  std::vector<double> coef(static_cast<size_t>(n_inst) * kCoef);
+  for (int k = 0; k < n_inst; ++k)
+    {
+      coef[k * kCoef + 0] = prm[k].K1;
+      coef[k * kCoef + 1] = prm[k].K2 + prm[k].K3;
+      coef[k * kCoef + 2] = prm[k].alpha;
+      for (int t = 0; t < 5; ++t) coef[k * kCoef + 3 + t] = prm[k].beta[t];
+    }
+  if ((s = dupload(c, &p_cells, P.cells)) || (s = dupload(c, &p_h, P.cell_h)) || (s = dupload(c, &p_ci, P.cell_inst)) ||
+      (s = dupload(c, &p_ni, P.node_inst)) || (s = dupload(c, &p_mask, P.mask)) || (s = dupload(c, &p_hptr, P.hptr)) ||
+      (s = dupload(c, &p_hpar, P.hpar)) || (s = dupload(c, &p_hw, P.hw)) || (s = dupload(c, &p_rowptr, P.rowptr)) ||
+      (s = dupload(c, &p_cols, P.cols)) || (s = dupload(c, &p_diag, P.diag)) || (s = dupload(c, &p_rcp, P.rc_ptr)) ||
+      (s = dupload(c, &p_rcc, P.rc_cell)) || (s = dupload(c, &p_rca, P.rc_a)) || (s = dupload(c, &p_rcw, P.rc_w)) ||
+      (s = dupload(c, &p_slot, P.rc_slot)) || (s = dupload(c, &p_hto, P.ht_off)) || (s = dupload(c, &p_tg, P.hang_tg)) ||
+      (s = dupload(c, &p_coef, coef)) || (s = dupload(c, &p_sb, P.seg_begin)) || (s = dupload(c, &p_se, P.seg_end)) ||
+      (s = dupload(c, &p_si, P.seg_inst)) || (s = dupload(c, &p_iso, P.inst_seg_off)) ||
+      (s = dupload(c, &p_co, P.cell_off)))
+    return fail(s);
+  d.cells = p_cells;
+  d.cell_h = p_h;
+  d.cell_inst = p_ci;
+  d.node_inst = p_ni;
+  d.mask = p_mask;
+  d.hptr = p_hptr;
+  d.hpar = p_hpar;
+  d.hw = p_hw;
+  d.rowptr = p_rowptr;
+  d.cols = p_cols;
+  d.diag = p_diag;
+  d.rc_ptr = p_rcp;
+  d.rc_cell = p_rcc;
+  d.rc_a = p_rca;
+  d.rc_w = p_rcw;
+  d.rc_slot = p_slot;
+  d.ht_off = p_hto;
+  d.hang_tg = p_tg;
+  d.coef = p_coef;
+  d.n_seg = static_cast<int>(P.seg_begin.size());
+  d.seg_begin = p_sb;
+  d.seg_end = p_se;
+  d.seg_inst = p_si;
+  d.inst_seg_off = p_iso;
+  d.cell_off = p_co;
+  // state buffers
+  const int64_t N = c->N;
+  const size_t ts = tsz(c);
+  const int mr = c->restart;
+  const int deg = std::max(1, prm[0].cheb_degree);
+  void *pv;
+  if ((s = dalloc(c, &c->x, N)) || (s = dalloc(c, &c->xt, N)) || (s = dalloc(c, &c->delta, N)) ||
+      (s = dalloc(c, &c->R, N)) || (s = dalloc(c, &c->rhs, N)) ||
+      (s = dalloc(c, &c->r_cell, static_cast<size_t>(P.nc) * P.nv * P.B)) || (s = dalloc(c, &c->e_cell, P.nc)))
+    return fail(s);
+  auto talloc = [&](void **p, size_t count) -> glgpu_status {
+    char *q = nullptr;
+    glgpu_status st = dalloc(c, &q, count * ts);
+    *p = q;
+    return st;
+  };
+  if ((s = talloc(&c->H, static_cast<size_t>(P.nc) * c->nq * c->ns)) ||
+      (s = talloc(&c->vals, static_cast<size_t>(P.nnzb) * P.B * P.B)) ||
+      (s = talloc(&c->dinv, static_cast<size_t>(P.nn) * P.B * P.B)) ||
+      (s = talloc(&c->V, static_cast<size_t>(mr + 1) * N)) || (s = talloc(&c->Z, N)) || (s = talloc(&c->X, N)) ||
+      (s = talloc(&c->Tmp, N)) || (s = talloc(&c->Bv, N)) || (s = talloc(&c->C1, N)) || (s = talloc(&c->C2, N)) ||
+      (s = talloc(&c->C3, N)))
+    return fail(s);
+  (void)pv;
+  if ((s = dalloc(c, &c->partial, static_cast<size_t>(d.n_seg) * (mr + 2))) ||
+      (s = dalloc(c, &c->g.H, static_cast<size_t>(n_inst) * (mr + 1) * mr)) ||
+      (s = dalloc(c, &c->g.cs, static_cast<size_t>(n_inst) * mr)) ||
+      (s = dalloc(c, &c->g.sn, static_cast<size_t>(n_inst) * mr)) ||
+      (s = dalloc(c, &c->g.g, static_cast<size_t>(n_inst) * (mr + 1))) ||
+      (s = dalloc(c, &c->g.y, static_cast<size_t>(n_inst) * mr)) ||
+      (s = dalloc(c, &c->g.hcol, static_cast<size_t>(n_inst) * (mr + 2))) ||
+      (s = dalloc(c, &c->g.hcol2, static_cast<size_t>(n_inst) * (mr + 2))) || (s = dalloc(c, &c->g.beta, n_inst)) ||
+      (s = dalloc(c, &c->g.tol, n_inst)) || (s = dalloc(c, &c->g.res_est, n_inst)) ||
+      (s = dalloc(c, &c->g.its, n_inst)) || (s = dalloc(c, &c->g.active, n_inst)) ||
+      (s = dalloc(c, &c->g.inv_scale, n_inst)) || (s = dalloc(c, &c->d_norm, n_inst)) ||
+      (s = dalloc(c, &c->d_a, n_inst)) || (s = dalloc(c, &c->d_energy, n_inst)) ||
+      (s = dalloc(c, &c->d_tmp, n_inst)) ||
+      (s = dalloc(c, &c->d_cheb, static_cast<size_t>(n_inst) * 2 * (deg + 1))) || (s = dalloc(c, &c->d_act, n_inst)) ||
+      (s = dalloc(c, &c->d_act2, n_inst)))
+    return fail(s);
+  c->g.m = mr;
+  if (cudaMallocHost(&c->h_norm, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||
+      cudaMallocHost(&c->h_res, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||
+      cudaMallocHost(&c->h_act, n_inst) != cudaSuccess || cudaMallocHost(&c->h_its, sizeof(int) * n_inst) != cudaSuccess)
+    return fail(set_error(GLGPU_ERR_NOMEM, "glgpu_create: pinned host allocation failed"));
+  if (cudaMemsetAsync(c->x, 0, sizeof(double) * N, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->delta, 0, sizeof(double) * N, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->R, 0, sizeof(double) * N, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->rhs, 0, sizeof(double) * N, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return fail(set_error(GLGPU_ERR_CUDA, "glgpu_create: initialisation failed"));
+  c->rhs_norm.assign(n_inst, 0.0);
+  c->res_norm.assign(n_inst, 0.0);
+  c->inst_on.assign(n_inst, 1);
+  cudaEventCreate(&c->ev_user0);
+  cudaEventCreate(&c->ev_user1);
+  *out = c;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_destroy(glgpu_ctx *c)
+{
+  if (!c) return GLGPU_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (auto &r : c->kev)
+    {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+  for (auto &r : c->pev)
+    {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->ev_user0) cudaEventDestroy(c->ev_user0);
+  if (c->ev_user1) cudaEventDestroy(c->ev_user1);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->h_norm) cudaFreeHost(c->h_norm);
+  if (c->h_res) cudaFreeHost(c->h_res);
+  if (c->h_act) cudaFreeHost(c->h_act);
+  if (c->h_its) cudaFreeHost(c->h_its);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_sizes(const glgpu_ctx *c, int64_t *n_nodes, int64_t *nnzb, int *block, int *n_inst)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_sizes: NULL context");
+  if (n_nodes) *n_nodes = c->nn;
+  if (nnzb) *nnzb = c->nnzb;
+  if (block) *block = c->B;
+  if (n_inst) *n_inst = c->n_inst;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_set_solution(glgpu_ctx *c, const double *x)
+{
+  if (!c || !x) return set_error(GLGPU_ERR_ARG, "glgpu_set_solution: NULL argument");
+  CK(cudaMemcpyAsync(c->x, x, sizeof(double) * c->N, cudaMemcpyHostToDevice, c->st));
+  CK(launch_distribute(c->dm, c->x, c->st));
+  c->launches += 2;
+  c->has_J = c->has_rhs = c->has_delta = false;
+  return sync(c);
+}
+
+extern "C" glgpu_status glgpu_get_solution(const glgpu_ctx *c, double *x)
+{
+  if (!c || !x) return set_error(GLGPU_ERR_ARG, "glgpu_get_solution: NULL argument");
+  CK(cudaMemcpyAsync(x, c->x, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return GLGPU_OK;
+}
+
+static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
+{
+  PhaseScope ps(c, PH_ASM);
+  if (!c->mixed)
+    {
+      CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, false, c->x, c->H, c->r_cell, c->e_cell, act, c->st); }));
+    }
+  else
+    {
+      CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
+      CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, c->e_cell, act, c->st); }));
+    }
+  CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
+  CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
+  CKS(axpby(c, c->R, c->rhs, nullptr, coefs(-1.0, 0.0), act, false, false, false));
+  std::vector<double> nr;
+  CKS(norms_d(c, c->rhs, act, nr));
+  for (int k = 0; k < c->n_inst; ++k)
+    if (!act || c->inst_on[k]) c->rhs_norm[k] = nr[k];
+  c->has_J = c->has_rhs = true;
+  c->prec_ready = false;
+  for (int k = 0; k < c->n_inst; ++k)
+    if ((!act || c->inst_on[k]) && !std::isfinite(c->rhs_norm[k]))
+      return set_error(GLGPU_ERR_NAN, "assemble_system: non-finite residual in instance " + std::to_string(k));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_assemble_system(glgpu_ctx *c, double *rhs_norm)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_assemble_system: NULL context");
+  std::fill(c->inst_on.begin(), c->inst_on.end(), 1);
+  CKS(assemble_impl(c, nullptr));
+  if (rhs_norm) std::copy(c->rhs_norm.begin(), c->rhs_norm.end(), rhs_norm);
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_compute_residual(glgpu_ctx *c, double *norm)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_compute_residual: NULL context");
+  {
+    PhaseScope ps(c, PH_RES);
+    CKS(residual_at(c, c->x, nullptr));
+  }
+  std::vector<double> nr;
+  CKS(norms_d(c, c->R, nullptr, nr));
+  c->res_norm = nr;
+  if (norm) std::copy(nr.begin(), nr.end(), norm);
+  for (double v : nr)
+    if (!std::isfinite(v)) return set_error(GLGPU_ERR_NAN, "compute_residual: non-finite residual");
+  return GLGPU_OK;
+}
+
+static glgpu_status solve_impl(glgpu_ctx *c, double tol, std::vector<int> &its, bool &conv)
+{
+  if (!c->has_J) return set_error(GLGPU_ERR_STATE, "solve: assemble_system must come first");
+  PhaseScope ps(c, PH_SOLVE);
+  CKS(prec_setup(c));
+  CKS(gmres(c, tol, c->inst_on, its, conv));
+  c->has_delta = true;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_solve(glgpu_ctx *c, double tol, int *its)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_solve: NULL context");
+  std::vector<int> it;
+  bool conv = false;
+  CKS(solve_impl(c, tol, it, conv));
+  if (its) std::copy(it.begin(), it.end(), its);
+  if (!conv) return set_error(GLGPU_ERR_NOT_CONVERGED, "solve: GMRES reached the iteration limit");
+  return GLGPU_OK;
+}
+
+static glgpu_status newton_impl(glgpu_ctx *c, std::vector<double> &res, std::vector<int> &trials)
+{
+  if (!c->has_delta || !c->has_rhs) return set_error(GLGPU_ERR_STATE, "newton_iteration: solve must come first");
+  PhaseScope ps(c, PH_NEWTON);
+  const int n = c->n_inst;
+  const glgpu_params &p0 = c->prm[0];
+  const int max_trials = p0.damped ? std::max(1, p0.ls_max_trials) : 1;
+  std::vector<uint8_t> pending(c->inst_on);
+  std::vector<double> cur(n, 0.0), a(n, 0.0);
+  res.assign(n, 0.0);
+  trials.assign(n, 0);
+  for (int i = 0; i < max_trials; ++i)
+    {
+      bool any = false;
+      for (int k = 0; k < n; ++k)
+        if (pending[k])
+          {
+            any = true;
+            a[k] = c->prm[k].damped ? std::pow(c->prm[k].ls_step, static_cast<double>(i)) : 1.0;
+          }
+      if (!any) break;
+      CKS(upload_d(c, c->d_a, a));
+      CKS(upload_act(c, c->d_act, pending));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_trial(c->dm, c->x, c->delta, c->d_a, c->xt, c->d_act, c->st); }));
+      CKS(residual_at(c, c->xt, c->d_act));
+      std::vector<double> nr;
+      CKS(norms_d(c, c->R, c->d_act, nr));
+      for (int k = 0; k < n; ++k)
+        if (pending[k])
+          {
+            cur[k] = nr[k];
+            trials[k] = i + 1;
+            if (nr[k] < c->rhs_norm[k] || !c->prm[k].damped) pending[k] = 0;
+          }
+    }
+  // local_solution = the accepted (or last) trial
+  CKS(upload_act(c, c->d_act, c->inst_on));
+  CKS(axpby(c, c->xt, c->x, nullptr, coefs(1.0, 0.0), c->d_act, false, false, false));
+  for (int k = 0; k < n; ++k)
+    if (c->inst_on[k])
+      {
+        res[k] = cur[k];
+        c->res_norm[k] = cur[k];
+      }
+  c->has_J = c->has_rhs = c->has_delta = false;
+  for (int k = 0; k < n; ++k)
+    if (c->inst_on[k] && !std::isfinite(res[k]))
+      return set_error(GLGPU_ERR_NAN, "newton_iteration: non-finite residual in instance " + std::to_string(k));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_newton_iteration(glgpu_ctx *c, double *res, int *trials)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_newton_iteration: NULL context");
+  std::vector<double> r;
+  std::vector<int> t;
+  CKS(newton_impl(c, r, t));
+  if (res) std::copy(r.begin(), r.end(), res);
+  if (trials) std::copy(t.begin(), t.end(), trials);
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_free_energy(glgpu_ctx *c, double *F)
+{
+  if (!c || !F) return set_error(GLGPU_ERR_ARG, "glgpu_free_energy: NULL argument");
+  CKS(residual_at(c, c->x, nullptr));
+  CKS(launch(c, KK_VEC, 1, [&] { return launch_cell_sum(c->dm, c->e_cell, c->d_energy, c->st); }));
+  CK(cudaMemcpyAsync(c->h_norm, c->d_energy, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
+  CKS(sync(c));
+  std::copy(c->h_norm, c->h_norm + c->n_inst, F);
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_tol, double converge_acc,
+                                  int *newton_its, int *gmres_its, double *final_res)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_run: NULL context");
+  const int n = c->n_inst;
+  std::vector<int> nits(n, 0), gits(n, 0);
+  std::vector<double> fres(n, 0.0);
+  std::fill(c->inst_on.begin(), c->inst_on.end(), 1);
+  glgpu_status result = GLGPU_OK;
+  for (int it = 0; it <= max_newton; ++it)
+    {
+      CKS(upload_act(c, c->d_act, c->inst_on));
+      CKS(assemble_impl(c, c->d_act));
+      std::vector<int> its;
+      bool conv = false;
+      CKS(solve_impl(c, linear_tol, its, conv));
+      std::vector<double> r;
+      std::vector<int> t;
+      CKS(newton_impl(c, r, t));
+      bool any = false;
+      for (int k = 0; k < n; ++k)
+        if (c->inst_on[k])
+          {
+            nits[k] = it + 1;
+            gits[k] += its[k];
+            fres[k] = r[k];
+            if (r[k] <= converge_acc)
+              c->inst_on[k] = 0;
+            else
+              any = true;
+          }
+      if (!any) break;
+    }
+  for (int k = 0; k < n; ++k)
+    if (c->inst_on[k]) result = set_error(GLGPU_ERR_NOT_CONVERGED, "run: Newton iteration limit reached");
+  std::fill(c->inst_on.begin(), c->inst_on.end(), 1);
+  if (newton_its) std::copy(nits.begin(), nits.end(), newton_its);
+  if (gmres_its) std::copy(gits.begin(), gits.end(), gmres_its);
+  if (final_res) std::copy(fres.begin(), fres.end(), final_res);
+  return result;
+}
+
+extern "C" glgpu_status glgpu_get_system(const glgpu_ctx *cc, int32_t *rowptr, int32_t *cols, double *vals,
+                                         double *rhs)
+{
+  glgpu_ctx *c = const_cast<glgpu_ctx *>(cc);
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_get_system: NULL context");
+  if (rowptr) std::memcpy(rowptr, c->P.rowptr.data(), sizeof(int32_t) * c->P.rowptr.size());
+  if (cols) std::memcpy(cols, c->P.cols.data(), sizeof(int32_t) * c->P.cols.size());
+  const size_t nv = static_cast<size_t>(c->nnzb) * c->B * c->B;
+  if (vals)
+    {
+      if (c->mixed)
+        {
+          std::vector<float> tmp(nv);
+          CK(cudaMemcpyAsync(tmp.data(), c->vals, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->st));
+          CK(cudaStreamSynchronize(c->st));
+          for (size_t i = 0; i < nv; ++i) vals[i] = tmp[i];
+        }
+      else
+        CK(cudaMemcpyAsync(vals, c->vals, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->st));
+    }
+  if (rhs) CK(cudaMemcpyAsync(rhs, c->rhs, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_get_residual(const glgpu_ctx *c, double *R)
+{
+  if (!c || !R) return set_error(GLGPU_ERR_ARG, "glgpu_get_residual: NULL argument");
+  CK(cudaMemcpyAsync(R, c->R, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_get_update(const glgpu_ctx *c, double *delta)
+{
+  if (!c || !delta) return set_error(GLGPU_ERR_ARG, "glgpu_get_update: NULL argument");
+  CK(cudaMemcpyAsync(delta, c->delta, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_spmv(glgpu_ctx *c, const double *x, double *y)
+{
+  if (!c || !x || !y) return set_error(GLGPU_ERR_ARG, "glgpu_spmv: NULL argument");
+  if (!c->has_J) return set_error(GLGPU_ERR_STATE, "glgpu_spmv: no assembled Jacobian");
+  CK(cudaMemcpyAsync(c->xt, x, sizeof(double) * c->N, cudaMemcpyHostToDevice, c->st));
+  CKS(axpby(c, c->xt, c->Z, nullptr, coefs(1.0, 0.0), nullptr, false, c->mixed, c->mixed));
+  CKS(spmv(c, c->Z, c->Tmp, nullptr));
+  CKS(axpby(c, c->Tmp, c->xt, nullptr, coefs(1.0, 0.0), nullptr, c->mixed, false, false));
+  CK(cudaMemcpyAsync(y, c->xt, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_timers(glgpu_ctx *c, double *phase_ms, int reset)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_timers: NULL context");
+  CKS(sync(c));
+  harvest(c);
+  if (phase_ms)
+    for (int i = 0; i < PH_N; ++i) phase_ms[i] = c->phase_ms[i];
+  if (reset)
+    for (int i = 0; i < PH_N; ++i) c->phase_ms[i] = 0.0;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_kernel_timing(glgpu_ctx *c, int enable, double *kernel_ms, int64_t *launches,
+                                            int reset)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_kernel_timing: NULL context");
+  CKS(sync(c));
+  harvest(c);
+  if (kernel_ms)
+    for (int i = 0; i < KK_N; ++i) kernel_ms[i] = c->kms[i];
+  if (launches)
+    for (int i = 0; i < KK_N; ++i) launches[i] = c->klaunch[i];
+  if (reset)
+    for (int i = 0; i < KK_N; ++i)
+      {
+        c->kms[i] = 0.0;
+        c->klaunch[i] = 0;
+      }
+  c->ktiming = enable != 0;
+  return GLGPU_OK;
+}
+
+extern "C" int64_t glgpu_launch_count(const glgpu_ctx *c) { return c ? c->launches : 0; }
+
+extern "C" glgpu_status glgpu_sync(glgpu_ctx *c)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_sync: NULL context");
+  return sync(c);
+}
+
+extern "C" glgpu_status glgpu_event_start(glgpu_ctx *c)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_event_start: NULL context");
+  CK(cudaEventRecord(c->ev_user0, c->st));
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_event_stop(glgpu_ctx *c, double *ms)
+{
+  if (!c || !ms) return set_error(GLGPU_ERR_ARG, "glgpu_event_stop: NULL argument");
+  CK(cudaEventRecord(c->ev_user1, c->st));
+  CK(cudaEventSynchronize(c->ev_user1));
+  float f = 0.f;
+  CK(cudaEventElapsedTime(&f, c->ev_user0, c->ev_user1));
+  *ms = f;
+  return GLGPU_OK;
+}

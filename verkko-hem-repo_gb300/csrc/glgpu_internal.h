@@ -1,0 +1,94 @@
+// Internal declarations shared by the host and device translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "glgpu.h"
+
+namespace glgpu
+{
+// ---------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------
+glgpu_status set_error(glgpu_status s, const std::string &msg);
+
+// ---------------------------------------------------------------------------------
+// host helpers (host_util.cc)
+// ---------------------------------------------------------------------------------
+struct BoxMesh
+{
+  int nn = 0, nc = 0;
+  std::vector<double> xyz;
+  std::vector<int32_t> cells, hptr, hpar;
+  std::vector<double> hw;
+  std::vector<uint32_t> mask;
+};
+int matep_eval(double p, double t, bool scc, double *out);
+int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dxy, BoxMesh &m);
+double gaussian(uint64_t seed, uint64_t index);
+
+// Dirichlet mask of the orbital column `axis` of u and v: components 9p + 3mu + axis.
+inline uint32_t column_mask(int axis)
+{
+  uint32_t m = 0;
+  for (int part = 0; part < 2; ++part)
+    for (int mu = 0; mu < 3; ++mu) m |= 1u << (9 * part + 3 * mu + axis);
+  return m;
+}
+
+// ---------------------------------------------------------------------------------
+// Assembly plan built on the host once per mesh (plan.cc).
+//
+// Rows are all nodes of all instances (global node ids).  A hanging node's row
+// holds only its diagonal block.  For a regular row n, a "contribution" is a pair
+// (cell e, local vertex a) whose vertex expands to n (itself with weight 1, or a
+// hanging vertex whose parent is n with weight 1/2 or 1/4).  For every local vertex b
+// of that cell the contribution lists where the (a,b) block lands in row n: a slot
+// (position in the row) when b is a regular node, or an entry of the hanging-target
+// table when b is hanging (up to 4 parent slots with weights).
+// ---------------------------------------------------------------------------------
+constexpr int kMaxParents = 4;
+
+struct HangTarget
+{
+  int32_t count;
+  int32_t slot[kMaxParents];
+  double w[kMaxParents];
+};
+
+struct Plan
+{
+  int dim = 3, B = 18, nv = 8;
+  int n_inst = 0;
+  int64_t nn = 0, nc = 0, nnzb = 0;
+  std::vector<int64_t> node_off, cell_off;   // per instance, size n_inst+1
+  std::vector<int32_t> cells;                 // [nc][nv] global node ids
+  std::vector<double> cell_h;                 // [nc][3] box edge lengths (z = 1 for 2D)
+  std::vector<int32_t> cell_inst;             // [nc]
+  std::vector<int32_t> node_inst;             // [nn]
+  std::vector<uint32_t> mask;                 // [nn]
+  std::vector<int32_t> hptr, hpar;            // [nn+1], global parents
+  std::vector<double> hw;
+  std::vector<int32_t> rowptr, cols;          // block CSR pattern
+  std::vector<int32_t> diag;                  // [nn] index of the diagonal block
+  std::vector<int32_t> rc_ptr;                // [nn+1] contributions per row
+  std::vector<int32_t> rc_cell;
+  std::vector<int32_t> rc_a;
+  std::vector<double> rc_w;
+  std::vector<int16_t> rc_slot;               // [ncontrib][nv]: slot, or -1 - (index into hang_tg - ht_off[row])
+  std::vector<HangTarget> hang_tg;
+  std::vector<int64_t> ht_off;                // [nn+1] first hanging target of each row
+  int max_row_blocks = 0;
+  // reduction segments: every segment lies inside one instance's vector range
+  int seg_len = 0;
+  std::vector<int64_t> seg_begin, seg_end;    // element ranges (in units of scalars)
+  std::vector<int32_t> seg_inst;
+  std::vector<int32_t> inst_seg_off;          // [n_inst+1]
+};
+
+// Validates the meshes and builds the plan; returns 0 or sets an error message.
+glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &plan);
+
+} // namespace glgpu

@@ -1,0 +1,748 @@
+// Assembly kernels (sm_103a).
+//
+// The reference assembles the Jacobian by evaluating nine FullMatrix kernels for
+// every (test dof i, trial dof j, quadrature point q) of every cell, 165,888 tuples
+// per Q1 hexahedron (femgl/src/assemble.cc:188-280).  Here the same matrix comes in
+// two passes that touch HBM once each:
+//
+//  1. k_cell3d: one CTA per 4 cells.  Nodal 18-vectors are gathered into shared
+//     memory, A and grad A are interpolated at the 8 Gauss points, and for every
+//     point the 171 unique entries of the symmetric bulk Hessian
+//     H_q = alpha I + 2 sum_t beta_t d^2(I_t/4) are written out ([cell][q][171]),
+//     together with the cell residual and free energy when asked.
+//  2. k_rows3d: one CTA per block row.  Every cell touching the row contributes
+//     block(a,b) = vol sum_q S_abq H_q + K1 G_ab + (K2+K3) D_ab, accumulated in
+//     shared memory at slots precomputed on the host, then the row (27 blocks on a
+//     structured mesh) is written once, contiguously.  No atomics, no colouring.
+//
+// The per-q formulas are the closed forms of the reference's kernels: the
+// quarter-gradient of invariant I_t is Re<G_t, Phi> with G1 = tr(AA^T) A^*,
+// G2 = tr(AA^+) A, G3 = AA^T A^*, G4 = AA^+ A, G5 = (AA^+)^* A, and the Hessian
+// entries are the directional derivatives of G_t along unit directions.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.h"
+#include "glgpu_internal.h"
+
+namespace glgpu
+{
+// ---------------------------------------------------------------------------------
+// reference-element tables (unit cube, QGauss(2), q = qx + 2 qy + 4 qz)
+// ---------------------------------------------------------------------------------
+__constant__ double c_val3[8][8];    // [q][v]
+__constant__ double c_grd3[8][8][3]; // [q][v][k] derivative on the unit cube
+__constant__ double c_S3[8][8][8];   // [a][b][q] = val[q][a] val[q][b] / 8
+__constant__ double c_D3[8][8][9];   // [a][b][3j+k] = (1/8) sum_q grd[q][a][j] grd[q][b][k]
+__constant__ unsigned char c_symc[kNS3], c_symd[kNS3];
+__constant__ double c_val2[4][4];
+__constant__ double c_grd2[4][4][2];
+__constant__ double c_S2[4][4][4];
+__constant__ double c_D2[4][4][4];
+
+cudaError_t init_constants()
+{
+  const double g = 0.5 - 0.28867513459481288225; // 1/2 - sqrt(3)/6
+  const double gp[2] = {g, 1.0 - g};
+  double val3[8][8], grd3[8][8][3], S3[8][8][8], D3[8][8][9];
+  for (int q = 0; q < 8; ++q)
+    {
+      const double xi[3] = {gp[q & 1], gp[(q >> 1) & 1], gp[(q >> 2) & 1]};
+      for (int v = 0; v < 8; ++v)
+        {
+          double s[3], ds[3];
+          for (int d = 0; d < 3; ++d)
+            {
+              const int bit = (v >> d) & 1;
+              s[d] = bit ? xi[d] : 1.0 - xi[d];
+              ds[d] = bit ? 1.0 : -1.0;
+            }
+          val3[q][v] = s[0] * s[1] * s[2];
+          grd3[q][v][0] = ds[0] * s[1] * s[2];
+          grd3[q][v][1] = s[0] * ds[1] * s[2];
+          grd3[q][v][2] = s[0] * s[1] * ds[2];
+        }
+    }
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b)
+      {
+        for (int q = 0; q < 8; ++q) S3[a][b][q] = val3[q][a] * val3[q][b] * 0.125;
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k)
+            {
+              double s = 0;
+              for (int q = 0; q < 8; ++q) s += grd3[q][a][j] * grd3[q][b][k];
+              D3[a][b][3 * j + k] = 0.125 * s;
+            }
+      }
+  unsigned char sc[kNS3], sd[kNS3];
+  int t = 0;
+  for (int c = 0; c < 18; ++c)
+    for (int d = c; d < 18; ++d)
+      {
+        sc[t] = static_cast<unsigned char>(c);
+        sd[t] = static_cast<unsigned char>(d);
+        ++t;
+      }
+  double val2[4][4], grd2[4][4][2], S2[4][4][4], D2[4][4][4];
+  for (int q = 0; q < 4; ++q)
+    {
+      const double xi[2] = {gp[q & 1], gp[(q >> 1) & 1]};
+      for (int v = 0; v < 4; ++v)
+        {
+          double s[2], ds[2];
+          for (int d = 0; d < 2; ++d)
+            {
+              const int bit = (v >> d) & 1;
+              s[d] = bit ? xi[d] : 1.0 - xi[d];
+              ds[d] = bit ? 1.0 : -1.0;
+            }
+          val2[q][v] = s[0] * s[1];
+          grd2[q][v][0] = ds[0] * s[1];
+          grd2[q][v][1] = s[0] * ds[1];
+        }
+    }
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b)
+      {
+        for (int q = 0; q < 4; ++q) S2[a][b][q] = val2[q][a] * val2[q][b] * 0.25;
+        for (int j = 0; j < 2; ++j)
+          for (int k = 0; k < 2; ++k)
+            {
+              double s = 0;
+              for (int q = 0; q < 4; ++q) s += grd2[q][a][j] * grd2[q][b][k];
+              D2[a][b][2 * j + k] = 0.25 * s;
+            }
+      }
+  cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(c_val3, val3, sizeof val3)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_grd3, grd3, sizeof grd3)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_S3, S3, sizeof S3)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_D3, D3, sizeof D3)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_symc, sc, sizeof sc)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_symd, sd, sizeof sd)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_val2, val2, sizeof val2)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_grd2, grd2, sizeof grd2)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_S2, S2, sizeof S2)) != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_D2, D2, sizeof D2);
+}
+
+// ---------------------------------------------------------------------------------
+// small complex helpers
+// ---------------------------------------------------------------------------------
+template <typename T> struct cx
+{
+  T r, i;
+};
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b)
+{
+  return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
+}
+template <typename T> __device__ __forceinline__ cx<T> cconj(cx<T> a) { return {a.r, -a.i}; }
+template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return {a.r + b.r, a.i + b.i}; }
+template <typename T> __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return {a.r * s, a.i * s}; }
+// multiply by s = 1 (v == 0) or s = i (v == 1)
+template <typename T> __device__ __forceinline__ cx<T> mul_s(cx<T> a, int v)
+{
+  return v ? cx<T>{-a.i, a.r} : a;
+}
+// multiply by conj(s)
+template <typename T> __device__ __forceinline__ cx<T> mul_cs(cx<T> a, int v)
+{
+  return v ? cx<T>{a.i, -a.r} : a;
+}
+
+// per-(cell, q) state in shared memory: complex 3x3 matrices stored as re[9], im[9]
+template <typename T> struct QS
+{
+  T *A;   // [18]: re 0..8, im 9..17 (the 18-vector packing)
+  T *P;   // A A^T
+  T *Q;   // A A^+
+  T *M2;  // A^+ A
+  T *M3;  // A^T A
+  T *pq;  // p.r, p.i, q
+};
+template <typename T> __device__ __forceinline__ cx<T> at(const T *M, int i, int j)
+{
+  return {M[3 * i + j], M[9 + 3 * i + j]};
+}
+
+// Hessian entry H[c][d] (without the alpha term) / 2 of the quartic part:
+// Hb = 2 sum_t beta_t dG_t[s E_{mu j}], output Re (c < 9) or Im (c >= 9) at (i, l).
+template <typename T>
+__device__ __forceinline__ T hess_entry(const QS<T> &s, const T *beta, int c, int d)
+{
+  const int pc = c / 9, i = (c % 9) / 3, l = c % 3;
+  const int pd = d / 9, mu = (d % 9) / 3, j = d % 3;
+  const cx<T> p = {s.pq[0], s.pq[1]};
+  const T q = s.pq[2];
+  const bool dim_ = (i == mu), djl = (j == l);
+  const cx<T> A_mj = at(s.A, mu, j), A_il = at(s.A, i, l), A_ij = at(s.A, i, j), A_ml = at(s.A, mu, l);
+  // T1 = 2 s A_mj conj(A_il) + p conj(s) d_im d_lj
+  cx<T> t1 = cscale(mul_s(cmul(A_mj, cconj(A_il)), pd), T(2));
+  if (dim_ && djl) t1 = cadd(t1, mul_cs(p, pd));
+  // T2 = 2 Re(s conj(A_mj)) A_il + q s d_im d_lj
+  const T re_s_cA = mul_s(cconj(A_mj), pd).r;
+  cx<T> t2 = cscale(A_il, T(2) * re_s_cA);
+  if (dim_ && djl) t2 = cadd(t2, mul_s(cx<T>{q, T(0)}, pd));
+  // T3 = s A_ij conj(A_ml) + s d_im conj(M2_jl) + conj(s) P_im d_jl
+  cx<T> t3 = mul_s(cmul(A_ij, cconj(A_ml)), pd);
+  if (dim_) t3 = cadd(t3, mul_s(cconj(at(s.M2, j, l)), pd));
+  if (djl) t3 = cadd(t3, mul_cs(at(s.P, i, mu), pd));
+  // T4 = s d_im M2_jl + conj(s) A_ij A_ml + s Q_im d_jl
+  cx<T> t4 = mul_cs(cmul(A_ij, A_ml), pd);
+  if (dim_) t4 = cadd(t4, mul_s(at(s.M2, j, l), pd));
+  if (djl) t4 = cadd(t4, mul_s(at(s.Q, i, mu), pd));
+  // T5 = conj(s) d_im M3_jl + s conj(A_ij) A_ml + s conj(Q_im) d_jl
+  cx<T> t5 = mul_s(cmul(cconj(A_ij), A_ml), pd);
+  if (dim_) t5 = cadd(t5, mul_cs(at(s.M3, j, l), pd));
+  if (djl) t5 = cadd(t5, mul_s(cconj(at(s.Q, i, mu)), pd));
+  const cx<T> hb = cadd(cadd(cadd(cscale(t1, beta[0]), cscale(t2, beta[1])), cadd(cscale(t3, beta[2]), cscale(t4, beta[3]))),
+                        cscale(t5, beta[4]));
+  return T(2) * (pc ? hb.i : hb.r);
+}
+
+// ---------------------------------------------------------------------------------
+// k_cell3d: per-cell quadrature data
+// ---------------------------------------------------------------------------------
+constexpr int kCPB = 4;             // cells per CTA
+constexpr int kNPQ = kCPB * 8;      // (cell, q) pairs per CTA
+constexpr int kCellThreads = 128;
+
+template <typename T> struct CellSmem
+{
+  T xs[kCPB][8][18];
+  T A[kNPQ][18];
+  T gA[kNPQ][3][18];
+  T P[kNPQ][18], Q[kNPQ][18], M2[kNPQ][18], M3[kNPQ][18];
+  T pq[kNPQ][3];
+  T rb[kNPQ][18];
+  T dv[kNPQ][6];
+  T en[kNPQ];
+  T ec[kNPQ][18];
+  T coef[kCPB][kCoef];
+  T ih[kCPB][3];
+  T jxw[kCPB];
+};
+
+template <typename T, bool WH, bool WR>
+__global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double *__restrict__ x, T *__restrict__ Hout,
+                                                          double *__restrict__ r_cell, double *__restrict__ e_cell,
+                                                          const uint8_t *__restrict__ inst_active)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CellSmem<T> &S = *reinterpret_cast<CellSmem<T> *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kCPB;
+  const int ncb = static_cast<int>((m.nc - e0) < kCPB ? (m.nc - e0) : kCPB);
+  __shared__ int s_skip[kCPB];
+  if (tid < kCPB)
+    {
+      int skip = 1;
+      if (tid < ncb)
+        {
+          const int64_t e = e0 + tid;
+          const int inst = m.cell_inst[e];
+          skip = (inst_active && !inst_active[inst]) ? 1 : 0;
+          for (int k = 0; k < kCoef; ++k) S.coef[tid][k] = static_cast<T>(m.coef[inst * kCoef + k]);
+          const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
+          S.ih[tid][0] = static_cast<T>(1.0 / hx);
+          S.ih[tid][1] = static_cast<T>(1.0 / hy);
+          S.ih[tid][2] = static_cast<T>(1.0 / hz);
+          S.jxw[tid] = static_cast<T>(0.125 * hx * hy * hz);
+        }
+      s_skip[tid] = skip;
+    }
+  // gather nodal values
+  for (int idx = tid; idx < kCPB * 144; idx += kCellThreads)
+    {
+      const int cl = idx / 144, rem = idx % 144, v = rem / 18, c = rem % 18;
+      T val = T(0);
+      if (cl < ncb)
+        {
+          const int node = m.cells[(e0 + cl) * 8 + v];
+          val = static_cast<T>(x[static_cast<int64_t>(node) * 18 + c]);
+        }
+      S.xs[cl][v][c] = val;
+    }
+  __syncthreads();
+  // A and grad A at the Gauss points
+  for (int idx = tid; idx < kNPQ * 18; idx += kCellThreads)
+    {
+      const int pq = idx / 18, c = idx % 18, cl = pq >> 3, q = pq & 7;
+      T a = 0, g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+        {
+          const T xv = S.xs[cl][v][c];
+          a += static_cast<T>(c_val3[q][v]) * xv;
+          g0 += static_cast<T>(c_grd3[q][v][0]) * xv;
+          g1 += static_cast<T>(c_grd3[q][v][1]) * xv;
+          g2 += static_cast<T>(c_grd3[q][v][2]) * xv;
+        }
+      S.A[pq][c] = a;
+      S.gA[pq][0][c] = g0 * S.ih[cl][0];
+      S.gA[pq][1][c] = g1 * S.ih[cl][1];
+      S.gA[pq][2][c] = g2 * S.ih[cl][2];
+    }
+  __syncthreads();
+  // P = A A^T, Q = A A^+, M2 = A^+ A, M3 = A^T A
+  for (int idx = tid; idx < kNPQ * 36; idx += kCellThreads)
+    {
+      const int pq = idx / 36, r = idx % 36, which = r / 9, ent = r % 9, i = ent / 3, l = ent % 3;
+      const T *A = S.A[pq];
+      cx<T> s = {T(0), T(0)};
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        {
+          cx<T> x1, x2;
+          switch (which)
+            {
+            case 0: x1 = at(A, i, k); x2 = at(A, l, k); break;                  // P_il = sum_k A_ik A_lk
+            case 1: x1 = at(A, i, k); x2 = cconj(at(A, l, k)); break;           // Q_il = sum_k A_ik conj(A_lk)
+            case 2: x1 = cconj(at(A, k, i)); x2 = at(A, k, l); break;           // M2_il = sum_k conj(A_ki) A_kl
+            default: x1 = at(A, k, i); x2 = at(A, k, l); break;                 // M3_il = sum_k A_ki A_kl
+            }
+          s = cadd(s, cmul(x1, x2));
+        }
+      T *dst = (which == 0) ? S.P[pq] : (which == 1) ? S.Q[pq] : (which == 2) ? S.M2[pq] : S.M3[pq];
+      dst[ent] = s.r;
+      dst[9 + ent] = s.i;
+    }
+  __syncthreads();
+  if (tid < kNPQ)
+    {
+      S.pq[tid][0] = S.P[tid][0] + S.P[tid][4] + S.P[tid][8];
+      S.pq[tid][1] = S.P[tid][9] + S.P[tid][13] + S.P[tid][17];
+      S.pq[tid][2] = S.Q[tid][0] + S.Q[tid][4] + S.Q[tid][8];
+    }
+  __syncthreads();
+  if (WH)
+    {
+      for (int idx = tid; idx < kNPQ * kNS3; idx += kCellThreads)
+        {
+          const int pq = idx / kNS3, sidx = idx % kNS3, cl = pq >> 3;
+          if (cl >= ncb || s_skip[cl]) continue;
+          const QS<T> qs = {S.A[pq], S.P[pq], S.Q[pq], S.M2[pq], S.M3[pq], S.pq[pq]};
+          const int c = c_symc[sidx], d = c_symd[sidx];
+          T h = hess_entry(qs, &S.coef[cl][3], c, d);
+          if (c == d) h += S.coef[cl][2];
+          Hout[e0 * 8 * kNS3 + idx] = h;
+        }
+    }
+  if (WR)
+    {
+      // bulk residual Rb = alpha A + 2 sum_t beta_t G_t and the free-energy density
+      for (int idx = tid; idx < kNPQ * 18; idx += kCellThreads)
+        {
+          const int pq = idx / 18, c = idx % 18, cl = pq >> 3;
+          const int part = c / 9, i = (c % 9) / 3, l = c % 3;
+          const T *A = S.A[pq];
+          const cx<T> p = {S.pq[pq][0], S.pq[pq][1]};
+          const T qq = S.pq[pq][2];
+          const cx<T> Ail = at(A, i, l);
+          cx<T> G[5];
+          G[0] = cmul(p, cconj(Ail));
+          G[1] = cscale(Ail, qq);
+          G[2] = G[3] = G[4] = cx<T>{T(0), T(0)};
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            {
+              G[2] = cadd(G[2], cmul(at(S.P[pq], i, k), cconj(at(A, k, l))));
+              G[3] = cadd(G[3], cmul(at(S.Q[pq], i, k), at(A, k, l)));
+              G[4] = cadd(G[4], cmul(cconj(at(S.Q[pq], i, k)), at(A, k, l)));
+            }
+          const T *cf = S.coef[cl];
+          const T ac = A[c];
+          T rb = cf[2] * ac, eb = cf[2] * ac * ac;
+#pragma unroll
+          for (int t = 0; t < 5; ++t)
+            {
+              const T g = part ? G[t].i : G[t].r;
+              rb += T(2) * cf[3 + t] * g;
+              eb += cf[3 + t] * g * ac;
+            }
+          T eg = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) eg += S.gA[pq][k][c] * S.gA[pq][k][c];
+          S.rb[pq][c] = rb;
+          S.ec[pq][c] = eb + cf[0] * eg; // energy density of this component (bulk + K1 part)
+        }
+      __syncthreads();
+      if (tid < kNPQ)
+        {
+          const int pq = tid, cl = pq >> 3;
+          T div[6];
+#pragma unroll
+          for (int pm = 0; pm < 6; ++pm)
+            {
+              const int base = 9 * (pm / 3) + 3 * (pm % 3);
+              div[pm] = S.gA[pq][0][base + 0] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2];
+              S.dv[pq][pm] = div[pm];
+            }
+          T e = 0;
+          for (int c = 0; c < 18; ++c) e += S.ec[pq][c];
+          for (int pm = 0; pm < 6; ++pm) e += S.coef[cl][1] * div[pm] * div[pm];
+          S.en[pq] = e;
+        }
+      __syncthreads();
+      for (int idx = tid; idx < kCPB * 144; idx += kCellThreads)
+        {
+          const int cl = idx / 144, a = (idx % 144) / 18, c = idx % 18;
+          if (cl >= ncb || s_skip[cl]) continue;
+          const int pm = 3 * (c / 9) + (c % 9) / 3, jc = c % 3;
+          const T K1 = S.coef[cl][0], K23 = S.coef[cl][1];
+          T r = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            {
+              const int pq = cl * 8 + q;
+              T s = static_cast<T>(c_val3[q][a]) * S.rb[pq][c];
+              s += K1 * (static_cast<T>(c_grd3[q][a][0]) * S.ih[cl][0] * S.gA[pq][0][c] +
+                         static_cast<T>(c_grd3[q][a][1]) * S.ih[cl][1] * S.gA[pq][1][c] +
+                         static_cast<T>(c_grd3[q][a][2]) * S.ih[cl][2] * S.gA[pq][2][c]);
+              s += K23 * static_cast<T>(c_grd3[q][a][jc]) * S.ih[cl][jc] * S.dv[pq][pm];
+              r += s;
+            }
+          r_cell[(e0 + cl) * 144 + a * 18 + c] = static_cast<double>(r * S.jxw[cl]);
+        }
+      if (tid < kCPB && tid < ncb && !s_skip[tid])
+        {
+          T e = 0;
+          for (int q = 0; q < 8; ++q) e += S.en[tid * 8 + q];
+          e_cell[e0 + tid] = static_cast<double>(e * S.jxw[tid]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// k_rows3d: one CTA per block row, accumulation in shared memory
+// ---------------------------------------------------------------------------------
+constexpr int kRowThreads = 192;
+
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *acc = reinterpret_cast<T *>(smem_raw);
+  __shared__ T sD[8 * 8 * 9];
+  const int64_t n = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int r0 = m.rowptr[n];
+  const int nb = m.rowptr[n + 1] - r0;
+  for (int i = tid; i < nb * 324; i += kRowThreads) acc[i] = T(0);
+  for (int i = tid; i < 576; i += kRowThreads) sD[i] = static_cast<T>((&c_D3[0][0][0])[i]);
+  __syncthreads();
+  const bool act = tid < kNS3;
+  const int c = act ? c_symc[tid] : 0, d = act ? c_symd[tid] : 0;
+  const int pmc = 3 * (c / 9) + (c % 9) / 3, jc = c % 3, pmd = 3 * (d / 9) + (d % 9) / 3, jd = d % 3;
+  const bool kpair = (pmc == pmd);
+  const struct HangTarget *tg = reinterpret_cast<const HangTarget *>(m.hang_tg);
+  const int k0 = m.rc_ptr[n], k1 = m.rc_ptr[n + 1];
+  for (int k = k0; k < k1; ++k)
+    {
+      const int64_t e = m.rc_cell[k];
+      const int a = m.rc_a[k];
+      const T wa = static_cast<T>(m.rc_w[k]);
+      const int inst = m.cell_inst[e];
+      const T K1 = static_cast<T>(m.coef[inst * kCoef + 0]), K23 = static_cast<T>(m.coef[inst * kCoef + 1]);
+      const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
+      const T vol = static_cast<T>(hx * hy * hz);
+      const T ih[3] = {static_cast<T>(1.0 / hx), static_cast<T>(1.0 / hy), static_cast<T>(1.0 / hz)};
+      T hq[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) hq[q] = act ? H[(e * 8 + q) * kNS3 + tid] : T(0);
+      const T kd = K1 * vol;
+      const T kc = K23 * vol * ih[jc] * ih[jd];
+#pragma unroll 1
+      for (int b = 0; b < 8; ++b)
+        {
+          T bulk = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) bulk += static_cast<T>(c_S3[a][b][q]) * hq[q];
+          bulk *= vol;
+          const T *D = sD + (a * 8 + b) * 9;
+          T gcd = 0, gdc = 0;
+          if (c == d)
+            {
+              const T gg = D[0] * ih[0] * ih[0] + D[4] * ih[1] * ih[1] + D[8] * ih[2] * ih[2];
+              gcd = gdc = kd * gg;
+            }
+          if (kpair)
+            {
+              gcd += kc * D[3 * jc + jd];
+              gdc += kc * D[3 * jd + jc];
+            }
+          const int sl = m.rc_slot[static_cast<int64_t>(k) * 8 + b];
+          if (sl >= 0)
+            {
+              if (act)
+                {
+                  acc[sl * 324 + c * 18 + d] += wa * (bulk + gcd);
+                  if (c != d) acc[sl * 324 + d * 18 + c] += wa * (bulk + gdc);
+                }
+            }
+          else
+            {
+              const HangTarget &t = tg[m.ht_off[n] + (-1 - sl)];
+              for (int j = 0; j < t.count; ++j)
+                if (act)
+                  {
+                    const T w = wa * static_cast<T>(t.w[j]);
+                    acc[t.slot[j] * 324 + c * 18 + d] += w * (bulk + gcd);
+                    if (c != d) acc[t.slot[j] * 324 + d * 18 + c] += w * (bulk + gdc);
+                  }
+            }
+        }
+    }
+  __syncthreads();
+  const uint32_t rmask = m.mask[n];
+  const bool hang_row = m.hptr[n + 1] > m.hptr[n];
+  T *out = vals + static_cast<int64_t>(r0) * 324;
+  for (int i = tid; i < nb * 324; i += kRowThreads)
+    {
+      const int sl = i / 324, e2 = i % 324, cc = e2 / 18, dd = e2 % 18;
+      const int col = m.cols[r0 + sl];
+      T v = acc[i];
+      if (hang_row)
+        v = (cc == dd) ? T(1) : T(0);
+      else if ((rmask >> cc) & 1u)
+        v = (col == n && cc == dd) ? (v != T(0) ? fabs(v) : T(1)) : T(0);
+      else if ((m.mask[col] >> dd) & 1u)
+        v = T(0);
+      out[i] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// 2D complex GL (2 components): thread per cell / thread per row
+// ---------------------------------------------------------------------------------
+template <typename T, bool WH, bool WR>
+__global__ void k_cell2d(DevMesh m, const double *__restrict__ x, T *__restrict__ Hout, double *__restrict__ r_cell,
+                         double *__restrict__ e_cell, const uint8_t *__restrict__ inst_active)
+{
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= m.nc) return;
+  const int inst = m.cell_inst[e];
+  if (inst_active && !inst_active[inst]) return;
+  const T gw = static_cast<T>(0.5 * m.coef[inst * kCoef + 0]);
+  const T alpha = static_cast<T>(m.coef[inst * kCoef + 2]);
+  const T beta = static_cast<T>(m.coef[inst * kCoef + 3]);
+  const T ih[2] = {static_cast<T>(1.0 / m.cell_h[3 * e]), static_cast<T>(1.0 / m.cell_h[3 * e + 1])};
+  const T jxw = static_cast<T>(0.25 * m.cell_h[3 * e] * m.cell_h[3 * e + 1]);
+  T xv[4][2];
+  for (int v = 0; v < 4; ++v)
+    {
+      const int node = m.cells[e * 4 + v];
+      xv[v][0] = static_cast<T>(x[2 * static_cast<int64_t>(node)]);
+      xv[v][1] = static_cast<T>(x[2 * static_cast<int64_t>(node) + 1]);
+    }
+  T r[4][2] = {};
+  T en = 0;
+  for (int q = 0; q < 4; ++q)
+    {
+      T u = 0, w = 0, gu[2] = {0, 0}, gv[2] = {0, 0};
+      for (int v = 0; v < 4; ++v)
+        {
+          const T s = static_cast<T>(c_val2[q][v]);
+          u += s * xv[v][0];
+          w += s * xv[v][1];
+          for (int k = 0; k < 2; ++k)
+            {
+              const T g = static_cast<T>(c_grd2[q][v][k]) * ih[k];
+              gu[k] += g * xv[v][0];
+              gv[k] += g * xv[v][1];
+            }
+        }
+      const T s2 = u * u + w * w;
+      if (WH)
+        {
+          T *h = Hout + (e * 4 + q) * 3;
+          h[0] = alpha + beta * (T(3) * u * u + w * w);
+          h[1] = T(2) * beta * u * w;
+          h[2] = alpha + beta * (T(3) * w * w + u * u);
+        }
+      if (WR)
+        {
+          const T bulk = alpha + beta * s2;
+          en += gw * (gu[0] * gu[0] + gu[1] * gu[1] + gv[0] * gv[0] + gv[1] * gv[1]) + alpha * s2 + T(0.5) * beta * s2 * s2;
+          for (int a = 0; a < 4; ++a)
+            {
+              const T va = static_cast<T>(c_val2[q][a]);
+              const T g0 = static_cast<T>(c_grd2[q][a][0]) * ih[0], g1 = static_cast<T>(c_grd2[q][a][1]) * ih[1];
+              r[a][0] += gw * (g0 * gu[0] + g1 * gu[1]) + bulk * u * va;
+              r[a][1] += gw * (g0 * gv[0] + g1 * gv[1]) + bulk * w * va;
+            }
+        }
+    }
+  if (WR)
+    {
+      for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 2; ++c) r_cell[e * 8 + a * 2 + c] = static_cast<double>(r[a][c] * jxw);
+      e_cell[e] = static_cast<double>(en * jxw);
+    }
+}
+
+template <typename T>
+__global__ void k_rows2d(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
+{
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const int r0 = m.rowptr[n], nb = m.rowptr[n + 1] - r0;
+  T *out = vals + static_cast<int64_t>(r0) * 4;
+  for (int i = 0; i < nb * 4; ++i) out[i] = T(0);
+  const struct HangTarget *tg = reinterpret_cast<const HangTarget *>(m.hang_tg);
+  for (int k = m.rc_ptr[n]; k < m.rc_ptr[n + 1]; ++k)
+    {
+      const int64_t e = m.rc_cell[k];
+      const int a = m.rc_a[k];
+      const T wa = static_cast<T>(m.rc_w[k]);
+      const int inst = m.cell_inst[e];
+      const T gw = static_cast<T>(0.5 * m.coef[inst * kCoef + 0]);
+      const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1];
+      const T area = static_cast<T>(hx * hy);
+      const T ih2[2] = {static_cast<T>(1.0 / (hx * hx)), static_cast<T>(1.0 / (hy * hy))};
+      for (int b = 0; b < 4; ++b)
+        {
+          T blk[4] = {0, 0, 0, 0};
+          for (int q = 0; q < 4; ++q)
+            {
+              const T s = static_cast<T>(c_S2[a][b][q]) * area;
+              const T *h = H + (e * 4 + q) * 3;
+              blk[0] += s * h[0];
+              blk[1] += s * h[1];
+              blk[2] += s * h[1];
+              blk[3] += s * h[2];
+            }
+          const T g = gw * area * (static_cast<T>(c_D2[a][b][0]) * ih2[0] + static_cast<T>(c_D2[a][b][3]) * ih2[1]);
+          blk[0] += g;
+          blk[3] += g;
+          const int sl = m.rc_slot[static_cast<int64_t>(k) * 4 + b];
+          if (sl >= 0)
+            for (int i = 0; i < 4; ++i) out[sl * 4 + i] += wa * blk[i];
+          else
+            {
+              const HangTarget &t = tg[m.ht_off[n] + (-1 - sl)];
+              for (int j = 0; j < t.count; ++j)
+                for (int i = 0; i < 4; ++i) out[t.slot[j] * 4 + i] += wa * static_cast<T>(t.w[j]) * blk[i];
+            }
+        }
+    }
+  const uint32_t rmask = m.mask[n];
+  const bool hang_row = m.hptr[n + 1] > m.hptr[n];
+  for (int sl = 0; sl < nb; ++sl)
+    {
+      const int col = m.cols[r0 + sl];
+      for (int cc = 0; cc < 2; ++cc)
+        for (int dd = 0; dd < 2; ++dd)
+          {
+            T &v = out[sl * 4 + cc * 2 + dd];
+            if (hang_row)
+              v = (cc == dd) ? T(1) : T(0);
+            else if ((rmask >> cc) & 1u)
+              v = (col == n && cc == dd) ? (v != T(0) ? fabs(v) : T(1)) : T(0);
+            else if ((m.mask[col] >> dd) & 1u)
+              v = T(0);
+          }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// residual gather
+// ---------------------------------------------------------------------------------
+__global__ void k_res_gather(DevMesh m, const double *__restrict__ r_cell, double *__restrict__ R,
+                             const uint8_t *__restrict__ inst_active)
+{
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m.nn * m.B) return;
+  const int64_t n = idx / m.B;
+  const int c = static_cast<int>(idx % m.B);
+  if (inst_active && !inst_active[m.node_inst[n]]) return;
+  double s = 0.0;
+  const bool hanging = m.hptr[n + 1] > m.hptr[n];
+  if (!hanging && !((m.mask[n] >> c) & 1u))
+    {
+      const int stride = m.nv * m.B;
+      for (int k = m.rc_ptr[n]; k < m.rc_ptr[n + 1]; ++k)
+        s += m.rc_w[k] * r_cell[static_cast<int64_t>(m.rc_cell[k]) * stride + m.rc_a[k] * m.B + c];
+    }
+  R[idx] = s;
+}
+
+// ---------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------
+template <typename T, bool WH, bool WR>
+static cudaError_t launch_cell_t(const DevMesh &m, const double *x, T *H, double *r_cell, double *e_cell,
+                                 const uint8_t *act, cudaStream_t s)
+{
+  if (m.dim == 3)
+    {
+      const size_t sm = sizeof(CellSmem<T>);
+      static bool attr_set = false;
+      if (!attr_set)
+        {
+          cudaError_t e = cudaFuncSetAttribute(k_cell3d<T, WH, WR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(sm));
+          if (e != cudaSuccess) return e;
+          attr_set = true;
+        }
+      const int64_t grid = (m.nc + kCPB - 1) / kCPB;
+      k_cell3d<T, WH, WR><<<static_cast<unsigned>(grid), kCellThreads, sm, s>>>(m, x, H, r_cell, e_cell, act);
+    }
+  else
+    {
+      const int64_t grid = (m.nc + 127) / 128;
+      k_cell2d<T, WH, WR><<<static_cast<unsigned>(grid), 128, 0, s>>>(m, x, H, r_cell, e_cell, act);
+    }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, double *r_cell, double *e_cell,
+                        const uint8_t *act, cudaStream_t s)
+{
+  const bool wh = H != nullptr, wr = r_cell != nullptr;
+  if (fp32)
+    {
+      if (wr) return cudaErrorInvalidValue; // the residual is always FP64
+      return launch_cell_t<float, true, false>(m, x, static_cast<float *>(H), nullptr, nullptr, act, s);
+    }
+  if (wh && wr) return launch_cell_t<double, true, true>(m, x, static_cast<double *>(H), r_cell, e_cell, act, s);
+  if (wh) return launch_cell_t<double, true, false>(m, x, static_cast<double *>(H), nullptr, nullptr, act, s);
+  return launch_cell_t<double, false, true>(m, x, nullptr, r_cell, e_cell, act, s);
+}
+
+template <typename T> static cudaError_t launch_rows_t(const DevMesh &m, const T *H, T *vals, cudaStream_t s)
+{
+  if (m.dim == 3)
+    {
+      const size_t sm = static_cast<size_t>(m.max_row_blocks) * 324 * sizeof(T);
+      static size_t attr = 0;
+      if (sm > attr)
+        {
+          cudaError_t e =
+            cudaFuncSetAttribute(k_rows3d<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+          if (e != cudaSuccess) return e;
+          attr = sm;
+        }
+      k_rows3d<T><<<static_cast<unsigned>(m.nn), kRowThreads, sm, s>>>(m, H, vals);
+    }
+  else
+    k_rows2d<T><<<static_cast<unsigned>((m.nn + 127) / 128), 128, 0, s>>>(m, H, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rows(const DevMesh &m, bool fp32, const void *H, void *vals, cudaStream_t s)
+{
+  if (fp32) return launch_rows_t<float>(m, static_cast<const float *>(H), static_cast<float *>(vals), s);
+  return launch_rows_t<double>(m, static_cast<const double *>(H), static_cast<double *>(vals), s);
+}
+
+cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *act, cudaStream_t s)
+{
+  const int64_t n = m.nn * m.B;
+  k_res_gather<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(m, r_cell, R, act);
+  return cudaGetLastError();
+}
+
+} // namespace glgpu

@@ -1,0 +1,719 @@
+// Linear-algebra kernels (sm_103a): block-CSR SpMV, block-Jacobi, per-instance
+// segmented reductions and vector updates, the GMRES small dense work, the
+// line-search trial update and constraint distribution.
+//
+// Vectors are scalar arrays of length nn*B, node-major.  A context may hold several
+// instances; every reduction and every per-instance scalar goes through "segments":
+// contiguous ranges of at most seg_len scalars that never straddle two instances, one
+// CTA per segment.  Reductions are two-pass (per-segment partials, then an ordered
+// per-instance sum), so results are deterministic run to run.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace glgpu
+{
+template <typename T> struct Vec16;
+template <> struct Vec16<float>
+{
+  using type = float4;
+  static constexpr int n = 4;
+};
+template <> struct Vec16<double>
+{
+  using type = double2;
+  static constexpr int n = 2;
+};
+template <typename V, typename T> __device__ __forceinline__ T vget(const V &v, int k);
+template <> __device__ __forceinline__ float vget<float4, float>(const float4 &v, int k)
+{
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+template <> __device__ __forceinline__ double vget<double2, double>(const double2 &v, int k) { return k == 0 ? v.x : v.y; }
+
+// ---------------------------------------------------------------------------------
+// SpMV, 18x18 blocks: one warp per block row.  Each block (324 scalars, 16-byte
+// aligned) is streamed with 128-bit loads; lane l always owns the same scalars e of
+// every block, so it accumulates sum_blocks J[e] x[col][e % 18] in registers; the 18
+// row sums are formed once per row through shared memory.  x[col] is loaded once per
+// block (lanes 0..17) and broadcast with shuffles.
+// ---------------------------------------------------------------------------------
+constexpr int kSpmvWarps = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *__restrict__ vals,
+                                                            const T *__restrict__ x, T *__restrict__ y,
+                                                            const uint8_t *__restrict__ act)
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  __shared__ T red[kSpmvWarps][324];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
+  if (n >= m.nn) return;
+  if (act && !act[m.node_inst[n]]) return;
+  T acc[NIT][NV];
+#pragma unroll
+  for (int it = 0; it < NIT; ++it)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
+  const int b0 = m.rowptr[n], b1 = m.rowptr[n + 1];
+  for (int blk = b0; blk < b1; ++blk)
+    {
+      const int64_t col = m.cols[blk];
+      const T xv = (lane < 18) ? x[col * 18 + lane] : T(0);
+      const V *bp = reinterpret_cast<const V *>(vals + static_cast<int64_t>(blk) * 324);
+#pragma unroll
+      for (int it = 0; it < NIT; ++it)
+        {
+          const int ch = lane + 32 * it;
+          V w;
+          if (ch < NCH)
+            w = __ldg(bp + ch);
+          else
+            w = V{};
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            {
+              const int e = (ch < NCH) ? ch * NV + v : 0;
+              const T xd = __shfl_sync(0xffffffffu, xv, e % 18);
+              acc[it][v] += vget<V, T>(w, v) * xd;
+            }
+        }
+    }
+#pragma unroll
+  for (int it = 0; it < NIT; ++it)
+    {
+      const int ch = lane + 32 * it;
+      if (ch < NCH)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
+    }
+  __syncwarp();
+  if (lane < 18)
+    {
+      T s = 0;
+#pragma unroll
+      for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
+      y[n * 18 + lane] = s;
+    }
+}
+
+template <typename T>
+__global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y,
+                        const uint8_t *__restrict__ act)
+{
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  if (act && !act[m.node_inst[n]]) return;
+  T y0 = 0, y1 = 0;
+  for (int blk = m.rowptr[n]; blk < m.rowptr[n + 1]; ++blk)
+    {
+      const int64_t col = m.cols[blk];
+      const T *B = vals + static_cast<int64_t>(blk) * 4;
+      const T x0 = x[2 * col], x1 = x[2 * col + 1];
+      y0 += B[0] * x0 + B[1] * x1;
+      y1 += B[2] * x0 + B[3] * x1;
+    }
+  y[2 * n] = y0;
+  y[2 * n + 1] = y1;
+}
+
+cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
+                        cudaStream_t s)
+{
+  if (m.B == 18)
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
+      if (fp32)
+        k_spmv18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
+                                                        static_cast<const float *>(x), static_cast<float *>(y), act);
+      else
+        k_spmv18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+                                                         static_cast<const double *>(x), static_cast<double *>(y), act);
+    }
+  else
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
+      if (fp32)
+        k_spmv2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(vals), static_cast<const float *>(x),
+                                            static_cast<float *>(y), act);
+      else
+        k_spmv2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(vals), static_cast<const double *>(x),
+                                             static_cast<double *>(y), act);
+    }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// block-Jacobi: invert each node's diagonal block (Gauss-Jordan, partial pivoting,
+// FP64 arithmetic), one warp per node for 18x18.  A singular block falls back to
+// the identity so the preconditioner stays defined.
+// ---------------------------------------------------------------------------------
+constexpr int kBjWarps = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T *__restrict__ vals,
+                                                              T *__restrict__ dinv)
+{
+  __shared__ double M[kBjWarps][18][37];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kBjWarps + warp;
+  if (n >= m.nn) return;
+  const T *D = vals + static_cast<int64_t>(m.diag[n]) * 324;
+  for (int i = lane; i < 18 * 36; i += 32)
+    {
+      const int r = i / 36, c = i % 36;
+      M[warp][r][c] = (c < 18) ? static_cast<double>(D[r * 18 + c]) : ((c - 18 == r) ? 1.0 : 0.0);
+    }
+  __syncwarp();
+  bool singular = false;
+  for (int k = 0; k < 18; ++k)
+    {
+      double best = (lane >= k && lane < 18) ? fabs(M[warp][lane][k]) : -1.0;
+      int bi = lane;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        {
+          const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi))
+            {
+              best = ob;
+              bi = oi;
+            }
+        }
+      if (!(best > 1e-300))
+        {
+          singular = true;
+          break;
+        }
+      if (bi != k)
+        for (int c = lane; c < 36; c += 32)
+          {
+            const double t = M[warp][k][c];
+            M[warp][k][c] = M[warp][bi][c];
+            M[warp][bi][c] = t;
+          }
+      __syncwarp();
+      const double piv = M[warp][k][k];
+      __syncwarp();
+      for (int c = lane; c < 36; c += 32) M[warp][k][c] /= piv;
+      __syncwarp();
+      double f[18];
+#pragma unroll
+      for (int r = 0; r < 18; ++r) f[r] = M[warp][r][k];
+      __syncwarp();
+      for (int c = lane; c < 36; c += 32)
+        {
+          const double pk = M[warp][k][c];
+#pragma unroll
+          for (int r = 0; r < 18; ++r)
+            if (r != k) M[warp][r][c] -= f[r] * pk;
+        }
+      __syncwarp();
+    }
+  T *out = dinv + n * 324;
+  for (int i = lane; i < 324; i += 32)
+    {
+      const int r = i / 18, c = i % 18;
+      out[i] = singular ? static_cast<T>(r == c ? 1.0 : 0.0) : static_cast<T>(M[warp][r][18 + c]);
+    }
+}
+
+template <typename T>
+__global__ void k_bj_setup2(DevMesh m, const T *__restrict__ vals, T *__restrict__ dinv)
+{
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  const T *D = vals + static_cast<int64_t>(m.diag[n]) * 4;
+  const double a = D[0], b = D[1], c = D[2], d = D[3];
+  const double det = a * d - b * c;
+  T *o = dinv + n * 4;
+  if (fabs(det) > 1e-300)
+    {
+      o[0] = static_cast<T>(d / det);
+      o[1] = static_cast<T>(-b / det);
+      o[2] = static_cast<T>(-c / det);
+      o[3] = static_cast<T>(a / det);
+    }
+  else
+    {
+      o[0] = T(1);
+      o[1] = T(0);
+      o[2] = T(0);
+      o[3] = T(1);
+    }
+}
+
+cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s)
+{
+  if (m.B == 18)
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + kBjWarps - 1) / kBjWarps);
+      if (fp32)
+        k_bj_setup18<float><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv));
+      else
+        k_bj_setup18<double><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+                                                            static_cast<double *>(dinv));
+    }
+  else
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
+      if (fp32)
+        k_bj_setup2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv));
+      else
+        k_bj_setup2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(vals), static_cast<double *>(dinv));
+    }
+  return cudaGetLastError();
+}
+
+// z[n] = Dinv[n] r[n]: the SpMV kernel over a diagonal-only pattern
+template <typename T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_bj_apply18(DevMesh m, const T *__restrict__ dinv,
+                                                                const T *__restrict__ x, T *__restrict__ y,
+                                                                const uint8_t *__restrict__ act)
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  __shared__ T red[kSpmvWarps][324];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
+  if (n >= m.nn) return;
+  if (act && !act[m.node_inst[n]]) return;
+  const T xv = (lane < 18) ? x[n * 18 + lane] : T(0);
+  const V *bp = reinterpret_cast<const V *>(dinv + n * 324);
+#pragma unroll
+  for (int it = 0; it < NIT; ++it)
+    {
+      const int ch = lane + 32 * it;
+      V w;
+      if (ch < NCH)
+        w = __ldg(bp + ch);
+      else
+        w = V{};
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        {
+          const int e = (ch < NCH) ? ch * NV + v : 0;
+          const T xd = __shfl_sync(0xffffffffu, xv, e % 18);
+          if (ch < NCH) red[warp][e] = vget<V, T>(w, v) * xd;
+        }
+    }
+  __syncwarp();
+  if (lane < 18)
+    {
+      T s = 0;
+#pragma unroll
+      for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
+      y[n * 18 + lane] = s;
+    }
+}
+
+template <typename T>
+__global__ void k_bj_apply2(DevMesh m, const T *__restrict__ dinv, const T *__restrict__ x, T *__restrict__ y,
+                            const uint8_t *__restrict__ act)
+{
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (n >= m.nn) return;
+  if (act && !act[m.node_inst[n]]) return;
+  const T *D = dinv + n * 4;
+  const T x0 = x[2 * n], x1 = x[2 * n + 1];
+  y[2 * n] = D[0] * x0 + D[1] * x1;
+  y[2 * n + 1] = D[2] * x0 + D[3] * x1;
+}
+
+cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const void *x, void *y,
+                            const uint8_t *act, cudaStream_t s)
+{
+  if (m.B == 18)
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
+      if (fp32)
+        k_bj_apply18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(dinv),
+                                                            static_cast<const float *>(x), static_cast<float *>(y), act);
+      else
+        k_bj_apply18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(dinv),
+                                                             static_cast<const double *>(x), static_cast<double *>(y),
+                                                             act);
+    }
+  else
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
+      if (fp32)
+        k_bj_apply2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(dinv), static_cast<const float *>(x),
+                                                static_cast<float *>(y), act);
+      else
+        k_bj_apply2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(dinv), static_cast<const double *>(x),
+                                                 static_cast<double *>(y), act);
+    }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// segmented reductions
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (kSegThreads >> 5); ++w) s += sh[w];
+  return s; // valid in thread 0
+}
+
+constexpr int kSegPer = 16; // scalars per thread and segment (seg_len <= 16 * 256)
+
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(kSegThreads) k_seg_mdot(DevMesh m, const TX *__restrict__ X, int64_t ld, int nvec,
+                                                          const TY *__restrict__ y, double *__restrict__ partial,
+                                                          const uint8_t *__restrict__ act)
+{
+  __shared__ double sh[kSegThreads / 32];
+  const int s = blockIdx.x;
+  const int64_t b = m.seg_begin[s], e = m.seg_end[s];
+  const bool on = !act || act[m.seg_inst[s]];
+  double yv[kSegPer];
+#pragma unroll
+  for (int k = 0; k < kSegPer; ++k)
+    {
+      const int64_t i = b + threadIdx.x + static_cast<int64_t>(k) * kSegThreads;
+      yv[k] = (on && i < e) ? static_cast<double>(y[i]) : 0.0;
+    }
+  for (int v = 0; v < nvec; ++v)
+    {
+      double acc = 0.0;
+      if (on)
+#pragma unroll
+        for (int k = 0; k < kSegPer; ++k)
+          {
+            const int64_t i = b + threadIdx.x + static_cast<int64_t>(k) * kSegThreads;
+            if (i < e) acc += static_cast<double>(X[v * ld + i]) * yv[k];
+          }
+      const double tot = block_sum(acc, sh);
+      if (threadIdx.x == 0) partial[static_cast<int64_t>(s) * nvec + v] = tot;
+    }
+}
+
+cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const void *y,
+                            double *partial, const uint8_t *act, cudaStream_t s)
+{
+  if (fp32)
+    k_seg_mdot<float, float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+                                                             static_cast<const float *>(y), partial, act);
+  else
+    k_seg_mdot<double, double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+                                                               static_cast<const double *>(y), partial, act);
+  return cudaGetLastError();
+}
+
+__global__ void k_seg_finalize(DevMesh m, const double *__restrict__ partial, int nvec, double *__restrict__ out,
+                               int ld_out, int take_sqrt)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m.n_inst * nvec) return;
+  const int inst = t / nvec, v = t % nvec;
+  double s = 0.0;
+  for (int g = m.inst_seg_off[inst]; g < m.inst_seg_off[inst + 1]; ++g) s += partial[static_cast<int64_t>(g) * nvec + v];
+  out[inst * ld_out + v] = take_sqrt ? sqrt(s) : s;
+}
+
+cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nvec, double *out, int ld_out,
+                                int take_sqrt, cudaStream_t s)
+{
+  const int n = m.n_inst * nvec;
+  k_seg_finalize<<<(n + 127) / 128, 128, 0, s>>>(m, partial, nvec, out, ld_out, take_sqrt);
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSegThreads) k_seg_maxpy(DevMesh m, const T *__restrict__ X, int64_t ld, int nvec,
+                                                           const double *__restrict__ coef, int ldc, T *__restrict__ y,
+                                                           const uint8_t *__restrict__ act)
+{
+  __shared__ double cf[64];
+  const int s = blockIdx.x;
+  const int inst = m.seg_inst[s];
+  if (act && !act[inst]) return;
+  for (int v = threadIdx.x; v < nvec; v += kSegThreads) cf[v] = coef[inst * ldc + v];
+  __syncthreads();
+  const int64_t b = m.seg_begin[s], e = m.seg_end[s];
+  for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads)
+    {
+      double acc = static_cast<double>(y[i]);
+      for (int v = 0; v < nvec; ++v) acc -= cf[v] * static_cast<double>(X[v * ld + i]);
+      y[i] = static_cast<T>(acc);
+    }
+}
+
+cudaError_t launch_seg_maxpy(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
+                             int ldc, void *y, const uint8_t *act, cudaStream_t s)
+{
+  if (nvec > 64) return cudaErrorInvalidValue;
+  if (fp32)
+    k_seg_maxpy<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec, coef, ldc,
+                                                       static_cast<float *>(y), act);
+  else
+    k_seg_maxpy<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec, coef, ldc,
+                                                        static_cast<double *>(y), act);
+  return cudaGetLastError();
+}
+
+template <typename TX, typename TY, typename TZ>
+__global__ void __launch_bounds__(kSegThreads) k_seg_axpby(DevMesh m, const TX *__restrict__ x, TY *__restrict__ y,
+                                                           const TZ *__restrict__ z, Axpby k,
+                                                           const uint8_t *__restrict__ act)
+{
+  const int s = blockIdx.x;
+  const int inst = m.seg_inst[s];
+  if (act && !act[inst]) return;
+  const double a = k.a ? k.a[inst * k.sa] : k.a0;
+  const double b = k.b ? k.b[inst * k.sb] : k.b0;
+  const double c = k.c ? k.c[inst * k.sc] : k.c0;
+  const int64_t b0 = m.seg_begin[s], e = m.seg_end[s];
+  for (int64_t i = b0 + threadIdx.x; i < e; i += kSegThreads)
+    {
+      double v = (a != 0.0 && x) ? a * static_cast<double>(x[i]) : 0.0;
+      if (b != 0.0) v += b * static_cast<double>(y[i]);
+      if (z && c != 0.0) v += c * static_cast<double>(z[i]);
+      y[i] = static_cast<TY>(v);
+    }
+}
+
+template <typename TX, typename TY>
+static void axpby_z(const DevMesh &m, const void *x, void *y, bool z32, const void *z, const Axpby &k,
+                    const uint8_t *act, cudaStream_t s)
+{
+  if (z32)
+    k_seg_axpby<TX, TY, float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const TX *>(x), static_cast<TY *>(y),
+                                                               static_cast<const float *>(z), k, act);
+  else
+    k_seg_axpby<TX, TY, double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const TX *>(x), static_cast<TY *>(y),
+                                                                static_cast<const double *>(z), k, act);
+}
+
+cudaError_t launch_seg_axpby(const DevMesh &m, bool x32, const void *x, bool y32, void *y, bool z32, const void *z,
+                             const Axpby &k, const uint8_t *act, cudaStream_t s)
+{
+  if (x32 && y32) axpby_z<float, float>(m, x, y, z32, z, k, act, s);
+  else if (x32) axpby_z<float, double>(m, x, y, z32, z, k, act, s);
+  else if (y32) axpby_z<double, float>(m, x, y, z32, z, k, act, s);
+  else axpby_z<double, double>(m, x, y, z32, z, k, act, s);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// constraints: line-search trial and distribute
+// ---------------------------------------------------------------------------------
+__global__ void k_trial(DevMesh m, const double *__restrict__ x, const double *__restrict__ dl,
+                        const double *__restrict__ a, double *__restrict__ xt, const uint8_t *__restrict__ act)
+{
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m.nn * m.B) return;
+  const int64_t n = idx / m.B;
+  const int c = static_cast<int>(idx % m.B);
+  const int inst = m.node_inst[n];
+  if (act && !act[inst]) return;
+  const double al = a[inst];
+  double v;
+  if (m.hptr[n + 1] > m.hptr[n])
+    {
+      v = 0.0;
+      for (int k = m.hptr[n]; k < m.hptr[n + 1]; ++k)
+        {
+          const int64_t p = m.hpar[k];
+          if (!((m.mask[p] >> c) & 1u)) v += m.hw[k] * (x[p * m.B + c] + al * dl[p * m.B + c]);
+        }
+    }
+  else if ((m.mask[n] >> c) & 1u)
+    v = 0.0;
+  else
+    v = x[idx] + al * dl[idx];
+  xt[idx] = v;
+}
+
+cudaError_t launch_trial(const DevMesh &m, const double *x, const double *delta, const double *a, double *xt,
+                         const uint8_t *act, cudaStream_t s)
+{
+  const int64_t n = m.nn * m.B;
+  k_trial<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(m, x, delta, a, xt, act);
+  return cudaGetLastError();
+}
+
+// two passes: Dirichlet zeros on regular nodes, then hanging nodes from parents
+__global__ void k_dist_regular(DevMesh m, double *__restrict__ v)
+{
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m.nn * m.B) return;
+  const int64_t n = idx / m.B;
+  const int c = static_cast<int>(idx % m.B);
+  if (m.hptr[n + 1] == m.hptr[n] && ((m.mask[n] >> c) & 1u)) v[idx] = 0.0;
+}
+
+__global__ void k_dist_hanging(DevMesh m, double *__restrict__ v)
+{
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= m.nn * m.B) return;
+  const int64_t n = idx / m.B;
+  const int c = static_cast<int>(idx % m.B);
+  if (m.hptr[n + 1] == m.hptr[n]) return;
+  double s = 0.0;
+  for (int k = m.hptr[n]; k < m.hptr[n + 1]; ++k) s += m.hw[k] * v[static_cast<int64_t>(m.hpar[k]) * m.B + c];
+  v[idx] = s;
+}
+
+cudaError_t launch_distribute(const DevMesh &m, double *v, cudaStream_t s)
+{
+  const int64_t n = m.nn * m.B;
+  const unsigned grid = static_cast<unsigned>((n + 255) / 256);
+  k_dist_regular<<<grid, 256, 0, s>>>(m, v);
+  k_dist_hanging<<<grid, 256, 0, s>>>(m, v);
+  return cudaGetLastError();
+}
+
+// ordered per-instance sum of per-cell values
+__global__ void __launch_bounds__(kSegThreads) k_cell_sum(DevMesh m, const double *__restrict__ ec,
+                                                          double *__restrict__ out)
+{
+  __shared__ double sh[kSegThreads / 32];
+  const int inst = blockIdx.x;
+  const int64_t b = m.cell_off[inst], e = m.cell_off[inst + 1];
+  double acc = 0.0;
+  for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads) acc += ec[i];
+  const double tot = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[inst] = tot;
+}
+
+cudaError_t launch_cell_sum(const DevMesh &m, const double *e_cell, double *out, cudaStream_t s)
+{
+  k_cell_sum<<<m.n_inst, kSegThreads, 0, s>>>(m, e_cell, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// GMRES small dense work (one thread per instance)
+// ---------------------------------------------------------------------------------
+__global__ void k_gmres_start(GmresDev g, int n_inst, const uint8_t *__restrict__ solve_active)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_inst) return;
+  const double beta = g.beta[k];
+  for (int i = 0; i <= g.m; ++i) g.g[k * (g.m + 1) + i] = 0.0;
+  g.g[k * (g.m + 1)] = beta;
+  g.its[k] = 0;
+  g.res_est[k] = beta;
+  const bool on = (!solve_active || solve_active[k]) && beta > g.tol[k] && isfinite(beta);
+  g.active[k] = on ? 1 : 0;
+  g.inv_scale[k] = (on && beta > 0.0) ? 1.0 / beta : 0.0;
+}
+
+cudaError_t launch_gmres_start(const GmresDev &g, int n_inst, const uint8_t *solve_active, cudaStream_t s)
+{
+  k_gmres_start<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst, solve_active);
+  return cudaGetLastError();
+}
+
+// hcol[k][0..j] + hcol2[k][0..j]: projections; hcol[k][j+1]: norm of the new vector
+__global__ void k_gmres_column(GmresDev g, int n_inst, int j)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_inst) return;
+  if (!g.active[k])
+    {
+      g.inv_scale[k] = 0.0;
+      return;
+    }
+  const int m = g.m;
+  double *h = g.hcol + k * (m + 2);
+  const double *h2 = g.hcol2 + k * (m + 2);
+  double col[64 + 2];
+  for (int i = 0; i <= j; ++i) col[i] = h[i] + h2[i];
+  col[j + 1] = h[j + 1];
+  double *cs = g.cs + k * m, *sn = g.sn + k * m, *gg = g.g + k * (m + 1);
+  for (int i = 0; i < j; ++i)
+    {
+      const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+      col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+      col[i] = t;
+    }
+  const double a = col[j], b = col[j + 1];
+  const double r = hypot(a, b);
+  double c1 = 1.0, s1 = 0.0;
+  if (r > 0.0)
+    {
+      c1 = a / r;
+      s1 = b / r;
+    }
+  cs[j] = c1;
+  sn[j] = s1;
+  col[j] = r;
+  gg[j + 1] = -s1 * gg[j];
+  gg[j] = c1 * gg[j];
+  double *Hc = g.H + static_cast<int64_t>(k) * (m + 1) * m + static_cast<int64_t>(j) * (m + 1);
+  for (int i = 0; i <= j; ++i) Hc[i] = col[i];
+  const double nrm = h[j + 1];
+  g.inv_scale[k] = (nrm > 0.0 && isfinite(nrm)) ? 1.0 / nrm : 0.0;
+  g.its[k] = j + 1;
+  const double est = fabs(gg[j + 1]);
+  g.res_est[k] = est;
+  if (!(est > g.tol[k]) || !(nrm > 0.0) || !isfinite(est)) g.active[k] = 0;
+}
+
+cudaError_t launch_gmres_column(const GmresDev &g, int n_inst, int j, cudaStream_t s)
+{
+  if (g.m > 64) return cudaErrorInvalidValue;
+  k_gmres_column<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst, j);
+  return cudaGetLastError();
+}
+
+// y = H(0:its,0:its)^-1 g(0:its); stored negated so that maxpy (y -= sum c_v V_v) adds V y
+__global__ void k_gmres_solve_y(GmresDev g, int n_inst)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_inst) return;
+  const int m = g.m, nk = g.its[k];
+  const double *H = g.H + static_cast<int64_t>(k) * (m + 1) * m;
+  const double *gg = g.g + k * (m + 1);
+  double *y = g.y + k * m;
+  for (int i = 0; i < m; ++i) y[i] = 0.0;
+  for (int i = nk - 1; i >= 0; --i)
+    {
+      double s = gg[i];
+      for (int c = i + 1; c < nk; ++c) s -= H[c * (m + 1) + i] * y[c];
+      const double d = H[i * (m + 1) + i];
+      y[i] = (d != 0.0) ? s / d : 0.0;
+    }
+  for (int i = 0; i < nk; ++i) y[i] = -y[i];
+}
+
+cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s)
+{
+  k_gmres_solve_y<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst);
+  return cudaGetLastError();
+}
+
+__global__ void k_inv(const double *__restrict__ in, double *__restrict__ out, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double v = in[k];
+  out[k] = (v > 0.0 && isfinite(v)) ? 1.0 / v : 0.0;
+}
+
+cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s)
+{
+  k_inv<<<(n + 127) / 128, 128, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+} // namespace glgpu

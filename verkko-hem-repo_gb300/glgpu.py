@@ -1,0 +1,417 @@
+"""ctypes binding of libglgpu.so, shaped like the reference's FemGL Newton interface.
+
+The reference's path is a set of members of ``FemGL_mpi::FemGL<3>``
+(femgl/inc/femgl.h:130-137): ``assemble_system()``, ``compute_residual()``,
+``solve(tol)``, ``newton_iteration()`` and the ``run()`` loop that drives them.
+:class:`FemGL` exposes the same calls with the same meaning, on a context that
+holds one or more instances (meshes with their own coefficients).  Every call goes
+through the C ABI declared in ``include/glgpu.h``; there is no other code path: if
+the library cannot be loaded or the device is missing, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import Sequence
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libglgpu.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_up = ctypes.POINTER(ctypes.c_uint32)
+_lp = ctypes.POINTER(ctypes.c_int64)
+
+FP64 = 0
+MIXED = 1
+PC_NONE = 0
+PC_BLOCK_JACOBI = 1
+PC_CHEBYSHEV = 2
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "not converged",
+          5: "NaN/Inf", 6: "device wait timed out", 7: "call out of order"}
+NOT_CONVERGED = 4
+
+KERNEL_KINDS = ("spmv", "cell", "rows", "residual", "precond", "vector")
+PHASES = ("assembly", "compute_residual", "solve", "newton_iteration")
+
+
+class GLGPUError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"glgpu: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("n_nodes", ctypes.c_int), ("n_cells", ctypes.c_int), ("xyz", _dp),
+                ("cells", _ip), ("dirichlet_mask", _up), ("hang_ptr", _ip), ("hang_parent", _ip),
+                ("hang_weight", _dp)]
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("K1", ctypes.c_double), ("K2", ctypes.c_double), ("K3", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double * 5), ("precision", ctypes.c_int),
+                ("precond", ctypes.c_int), ("cheb_degree", ctypes.c_int), ("gmres_restart", ctypes.c_int),
+                ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
+                ("damped", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libglgpu.so (built by ``build.py``); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GLGPUError(1, f"{LIB_PATH} not built; run the package build first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp = ctypes.c_void_p
+    L.glgpu_default_params.argtypes = [ctypes.POINTER(_Params)]
+    L.glgpu_version.restype = ctypes.c_char_p
+    L.glgpu_last_error.restype = ctypes.c_char_p
+    L.glgpu_create.argtypes = [ctypes.POINTER(_Mesh), ctypes.POINTER(_Params), ctypes.c_int, ctypes.POINTER(vp)]
+    L.glgpu_destroy.argtypes = [vp]
+    L.glgpu_sizes.argtypes = [vp, _lp, _lp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.glgpu_set_solution.argtypes = [vp, _dp]
+    L.glgpu_get_solution.argtypes = [vp, _dp]
+    L.glgpu_assemble_system.argtypes = [vp, _dp]
+    L.glgpu_compute_residual.argtypes = [vp, _dp]
+    L.glgpu_solve.argtypes = [vp, ctypes.c_double, _ip]
+    L.glgpu_newton_iteration.argtypes = [vp, _dp, _ip]
+    L.glgpu_free_energy.argtypes = [vp, _dp]
+    L.glgpu_run.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _ip, _ip, _dp]
+    L.glgpu_get_system.argtypes = [vp, _ip, _ip, _dp, _dp]
+    L.glgpu_get_residual.argtypes = [vp, _dp]
+    L.glgpu_get_update.argtypes = [vp, _dp]
+    L.glgpu_spmv.argtypes = [vp, _dp, _dp]
+    L.glgpu_timers.argtypes = [vp, _dp, ctypes.c_int]
+    L.glgpu_kernel_timing.argtypes = [vp, ctypes.c_int, _dp, _lp, ctypes.c_int]
+    L.glgpu_launch_count.argtypes = [vp]
+    L.glgpu_launch_count.restype = ctypes.c_int64
+    L.glgpu_sync.argtypes = [vp]
+    L.glgpu_event_start.argtypes = [vp]
+    L.glgpu_event_stop.argtypes = [vp, _dp]
+    L.glgpu_matep.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
+    L.glgpu_mesh_box.argtypes = [_dp, _dp, _ip, ctypes.c_double, _ip, _ip, _ip, _ip, _dp, _ip, _up, _ip, _ip, _dp]
+    L.glgpu_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_uint64, _dp]
+    L.glgpu_plan_info.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _lp]
+    L.glgpu_plan_pattern.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _ip, _ip]
+    _lib = L
+    return L
+
+
+def _check(status: int, allow: Sequence[int] = ()) -> int:
+    if status != 0 and status not in allow:
+        raise GLGPUError(status, lib().glgpu_last_error().decode())
+    return status
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+# ---------------------------------------------------------------------------------
+# host helpers
+# ---------------------------------------------------------------------------------
+MATEP_FIELDS = ("alpha", "beta1", "beta2", "beta3", "beta4", "beta5", "gap_A", "gap_B", "Tc_mK", "f_A", "f_B",
+                "beta_A", "beta_B")
+
+
+def matep(p: float, t: float, scc: bool = True) -> dict:
+    """Material parameters at pressure p [bar] and t = T/Tc (reference matep)."""
+    out = np.zeros(13)
+    _check(lib().glgpu_matep(float(p), float(t), int(bool(scc)), _p(out)))
+    return dict(zip(MATEP_FIELDS, out.tolist()))
+
+
+@dataclasses.dataclass
+class Mesh:
+    dim: int
+    xyz: np.ndarray
+    cells: np.ndarray
+    mask: np.ndarray
+    hptr: np.ndarray | None = None
+    hpar: np.ndarray | None = None
+    hw: np.ndarray | None = None
+
+    @property
+    def nn(self) -> int:
+        return int(self.xyz.shape[0])
+
+    @property
+    def nc(self) -> int:
+        return int(self.cells.shape[0])
+
+    @property
+    def n_hanging(self) -> int:
+        return 0 if self.hptr is None else int(np.count_nonzero(np.diff(self.hptr)))
+
+    def _struct(self) -> _Mesh:
+        self.xyz = np.ascontiguousarray(self.xyz, np.float64)
+        self.cells = np.ascontiguousarray(self.cells, np.int32)
+        self.mask = np.ascontiguousarray(self.mask, np.uint32)
+        s = _Mesh(self.dim, self.nn, self.nc, _p(self.xyz), _p(self.cells, _ip), _p(self.mask, _up), None, None, None)
+        if self.hptr is not None and len(self.hpar) > 0:
+            self.hptr = np.ascontiguousarray(self.hptr, np.int32)
+            self.hpar = np.ascontiguousarray(self.hpar, np.int32)
+            self.hw = np.ascontiguousarray(self.hw, np.float64)
+            s.hang_ptr = _p(self.hptr, _ip)
+            s.hang_parent = _p(self.hpar, _ip)
+            s.hang_weight = _p(self.hw)
+        return s
+
+
+def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_xy=(0, 0)) -> Mesh:
+    """Box [lo, hi] with n cells per axis, z faces pair-breaking, cells within
+    ``refine_band`` of a z face refined once (hanging nodes constrained)."""
+    L = lib()
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    nv = np.asarray(n, np.int32)
+    dxy = np.asarray(dirichlet_xy, np.int32)
+    nn = ctypes.c_int()
+    nc = ctypes.c_int()
+    nh = ctypes.c_int()
+    _check(L.glgpu_mesh_box(_p(lo), _p(hi), _p(nv, _ip), float(refine_band), _p(dxy, _ip), ctypes.byref(nn),
+                            ctypes.byref(nc), ctypes.byref(nh), None, None, None, None, None, None))
+    xyz = np.zeros((nn.value, 3))
+    cells = np.zeros((nc.value, 8), np.int32)
+    mask = np.zeros(nn.value, np.uint32)
+    hptr = np.zeros(nn.value + 1, np.int32)
+    hpar = np.zeros(max(nh.value, 1), np.int32)
+    hw = np.zeros(max(nh.value, 1))
+    _check(L.glgpu_mesh_box(_p(lo), _p(hi), _p(nv, _ip), float(refine_band), _p(dxy, _ip), ctypes.byref(nn),
+                            ctypes.byref(nc), ctypes.byref(nh), _p(xyz), _p(cells, _ip), _p(mask, _up), _p(hptr, _ip),
+                            _p(hpar, _ip), _p(hw)))
+    return Mesh(3, xyz, cells, mask, hptr, hpar[:nh.value], hw[:nh.value])
+
+
+def cube_mesh(half: float, n: int, refine_frac: float = 0.0) -> Mesh:
+    """The reference's cube [-half, half]^3 (make_grid with "cube half side length")."""
+    return box_mesh([-half] * 3, [half] * 3, (n, n, n), refine_band=refine_frac * 2.0 * half)
+
+
+def square_mesh(n: int) -> Mesh:
+    """Unit square, n x n Q1 quads, psi = 0 on the x = 0 edge (complexGL 2D)."""
+    t = np.linspace(0.0, 1.0, n + 1)
+    X, Y = np.meshgrid(t, t, indexing="xy")
+    xy = np.stack([X.ravel(), Y.ravel()], axis=1)
+    j, i = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    n0 = (j * (n + 1) + i).ravel()
+    cells = np.stack([n0, n0 + 1, n0 + n + 1, n0 + n + 2], axis=1).astype(np.int32)
+    mask = np.where(np.isclose(xy[:, 0], 0.0), 3, 0).astype(np.uint32)
+    return Mesh(2, xy, cells, mask)
+
+
+def bphase_guess(p: float, t: float, nn: int, noise: float = 0.0, seed: int = 0, scc: bool = True) -> np.ndarray:
+    """B-phase start u11 = u22 = u33 = gap_B/sqrt(3) (+ seeded Gaussian noise)."""
+    x = np.zeros(18 * nn)
+    _check(lib().glgpu_bphase_guess(float(p), float(t), int(bool(scc)), int(nn), float(noise), int(seed), _p(x)))
+    return x
+
+
+def plan_info(meshes: Sequence[Mesh]) -> dict:
+    """Host-only plan statistics of a list of instance meshes (no device needed)."""
+    ms = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+    info = np.zeros(6, np.int64)
+    _check(lib().glgpu_plan_info(ms, len(meshes), _p(info, _lp)))
+    keys = ("n_nodes", "nnzb", "max_row_blocks", "contributions", "hanging_targets", "segments")
+    return dict(zip(keys, info.tolist()))
+
+
+def plan_pattern(meshes: Sequence[Mesh]):
+    """Host-only block pattern (rowptr, cols) of the condensed Jacobian."""
+    info = plan_info(meshes)
+    ms = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+    rowptr = np.zeros(info["n_nodes"] + 1, np.int32)
+    cols = np.zeros(info["nnzb"], np.int32)
+    _check(lib().glgpu_plan_pattern(ms, len(meshes), _p(rowptr, _ip), _p(cols, _ip)))
+    return rowptr, cols
+
+
+@dataclasses.dataclass
+class Params:
+    """Coefficients and controls of one instance (see glgpu_params)."""
+    alpha: float
+    beta: Sequence[float] = (0.0, 0.0, 0.0, 0.0, 0.0)
+    K1: float = 0.42072
+    K2: float = 0.42072
+    K3: float = 0.42072
+    precision: int = FP64
+    precond: int = PC_BLOCK_JACOBI
+    cheb_degree: int = 3
+    gmres_restart: int = 50
+    gmres_max_iter: int = 10000
+    ls_step: float = 0.83
+    ls_max_trials: int = 100
+    damped: bool = True
+
+    @classmethod
+    def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
+        m = matep(p, t, scc)
+        return cls(alpha=m["alpha"], beta=[m[f"beta{i}"] for i in range(1, 6)], **kw)
+
+    def _struct(self) -> _Params:
+        s = _Params()
+        lib().glgpu_default_params(ctypes.byref(s))
+        s.K1, s.K2, s.K3, s.alpha = self.K1, self.K2, self.K3, self.alpha
+        for i in range(5):
+            s.beta[i] = float(self.beta[i]) if i < len(self.beta) else 0.0
+        s.precision, s.precond, s.cheb_degree = int(self.precision), int(self.precond), int(self.cheb_degree)
+        s.gmres_restart, s.gmres_max_iter = int(self.gmres_restart), int(self.gmres_max_iter)
+        s.ls_step, s.ls_max_trials, s.damped = float(self.ls_step), int(self.ls_max_trials), int(bool(self.damped))
+        return s
+
+
+class FemGL:
+    """One context: the Newton path of one or more instances on the GPU.
+
+    Methods map one-to-one to the reference members they replace; vectors are the
+    instances' node-major dof vectors concatenated in creation order."""
+
+    def __init__(self, meshes: Mesh | Sequence[Mesh], params: Params | Sequence[Params]):
+        L = lib()
+        if isinstance(meshes, Mesh):
+            meshes = [meshes]
+        if isinstance(params, Params):
+            params = [params] * len(meshes)
+        if len(params) != len(meshes):
+            raise ValueError("one Params per mesh")
+        self.meshes = list(meshes)
+        self._mstructs = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+        self._pstructs = (_Params * len(meshes))(*[p._struct() for p in params])
+        self._ctx = ctypes.c_void_p()
+        _check(L.glgpu_create(self._mstructs, self._pstructs, len(meshes), ctypes.byref(self._ctx)))
+        nn = ctypes.c_int64()
+        nnzb = ctypes.c_int64()
+        blk = ctypes.c_int()
+        ni = ctypes.c_int()
+        _check(L.glgpu_sizes(self._ctx, ctypes.byref(nn), ctypes.byref(nnzb), ctypes.byref(blk), ctypes.byref(ni)))
+        self.n_nodes, self.nnzb, self.block, self.n_inst = nn.value, nnzb.value, blk.value, ni.value
+        self.n_dofs = self.n_nodes * self.block
+        offs = np.cumsum([0] + [m.nn for m in meshes])
+        self.node_offsets = offs
+
+    # -- lifetime --
+    def close(self) -> None:
+        if getattr(self, "_ctx", None) is not None and self._ctx.value:
+            lib().glgpu_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state --
+    def set_solution(self, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        if x.size != self.n_dofs:
+            raise ValueError(f"expected {self.n_dofs} dofs, got {x.size}")
+        _check(lib().glgpu_set_solution(self._ctx, _p(x)))
+
+    def solution(self) -> np.ndarray:
+        x = np.zeros(self.n_dofs)
+        _check(lib().glgpu_get_solution(self._ctx, _p(x)))
+        return x
+
+    # -- the reference's members --
+    def assemble_system(self) -> np.ndarray:
+        out = np.zeros(self.n_inst)
+        _check(lib().glgpu_assemble_system(self._ctx, _p(out)))
+        return out
+
+    def compute_residual(self) -> np.ndarray:
+        out = np.zeros(self.n_inst)
+        _check(lib().glgpu_compute_residual(self._ctx, _p(out)))
+        return out
+
+    def solve(self, tol: float, allow_unconverged: bool = False) -> np.ndarray:
+        its = np.zeros(self.n_inst, np.int32)
+        _check(lib().glgpu_solve(self._ctx, float(tol), _p(its, _ip)), (NOT_CONVERGED,) if allow_unconverged else ())
+        return its
+
+    def newton_iteration(self):
+        res = np.zeros(self.n_inst)
+        trials = np.zeros(self.n_inst, np.int32)
+        _check(lib().glgpu_newton_iteration(self._ctx, _p(res), _p(trials, _ip)))
+        return res, trials
+
+    def run(self, max_newton: int = 40, linear_tol: float = 0.1, converge_acc: float = 5e-6,
+            allow_unconverged: bool = False) -> dict:
+        nits = np.zeros(self.n_inst, np.int32)
+        gits = np.zeros(self.n_inst, np.int32)
+        res = np.zeros(self.n_inst)
+        st = _check(lib().glgpu_run(self._ctx, int(max_newton), float(linear_tol), float(converge_acc),
+                                    _p(nits, _ip), _p(gits, _ip), _p(res)), (NOT_CONVERGED,) if allow_unconverged else ())
+        return {"newton_its": nits, "gmres_its": gits, "residual": res, "converged": st == 0}
+
+    def free_energy(self) -> np.ndarray:
+        out = np.zeros(self.n_inst)
+        _check(lib().glgpu_free_energy(self._ctx, _p(out)))
+        return out
+
+    # -- inspection --
+    def system(self):
+        rowptr = np.zeros(self.n_nodes + 1, np.int32)
+        cols = np.zeros(self.nnzb, np.int32)
+        vals = np.zeros((self.nnzb, self.block, self.block))
+        rhs = np.zeros(self.n_dofs)
+        _check(lib().glgpu_get_system(self._ctx, _p(rowptr, _ip), _p(cols, _ip), _p(vals), _p(rhs)))
+        return rowptr, cols, vals, rhs
+
+    def residual(self) -> np.ndarray:
+        R = np.zeros(self.n_dofs)
+        _check(lib().glgpu_get_residual(self._ctx, _p(R)))
+        return R
+
+    def update(self) -> np.ndarray:
+        d = np.zeros(self.n_dofs)
+        _check(lib().glgpu_get_update(self._ctx, _p(d)))
+        return d
+
+    def spmv(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.n_dofs)
+        _check(lib().glgpu_spmv(self._ctx, _p(x), _p(y)))
+        return y
+
+    # -- timing --
+    def timers(self, reset: bool = False) -> dict:
+        ms = np.zeros(4)
+        _check(lib().glgpu_timers(self._ctx, _p(ms), int(reset)))
+        return dict(zip(PHASES, ms.tolist()))
+
+    def kernel_timing(self, enable: bool, reset: bool = False):
+        ms = np.zeros(6)
+        n = np.zeros(6, np.int64)
+        _check(lib().glgpu_kernel_timing(self._ctx, int(enable), _p(ms), _p(n, _lp), int(reset)))
+        return dict(zip(KERNEL_KINDS, ms.tolist())), dict(zip(KERNEL_KINDS, n.tolist()))
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib().glgpu_launch_count(self._ctx))
+
+    def sync(self) -> None:
+        _check(lib().glgpu_sync(self._ctx))
+
+    def event_start(self) -> None:
+        _check(lib().glgpu_event_start(self._ctx))
+
+    def event_stop(self) -> float:
+        ms = ctypes.c_double()
+        _check(lib().glgpu_event_stop(self._ctx, ctypes.byref(ms)))
+        return ms.value
