@@ -80,7 +80,7 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 2 + i and "Active" in s[2 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 2 + i and s[2 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
@@ -103,7 +103,7 @@ def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=Fal
     for _ in range(warmup):
         out = solve_once(f, x0, linear_tol)
     f.timers(reset=True)
-    f.kernel_timing(kernel_timing, reset=True)
+    f.kernel_timing(1 if kernel_timing else 0, reset=True)  # bit 0: SpMV launches only
     launches0 = f.launch_count
     ms_steps = []
     stats = []

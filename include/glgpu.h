@@ -199,9 +199,10 @@ glgpu_status glgpu_spmv(glgpu_ctx *ctx, const double *x, double *y);
 glgpu_status glgpu_timers(glgpu_ctx *ctx, double *phase_ms, int reset);
 
 /*
- * Per-kernel-class device time, measured with events around each launch when
- * enable != 0 (small overhead): kernel_ms[k] and launches[k] for
- * k = {spmv, cell assembly, row gather, residual, precond, vector ops}.
+ * Per-kernel-class device time, measured with events around each launch of the
+ * kinds whose bit is set in enable (bit k = kind k; -1 = all; 0 = off; small
+ * overhead per timed launch): kernel_ms[k] and launches[k] (launches are always
+ * counted) for k = {spmv, cell assembly, row gather, residual, precond, vector ops}.
  */
 glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, int64_t *launches, int reset);
 

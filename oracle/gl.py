@@ -67,6 +67,9 @@ def lib():
         L.orc_distribute.argtypes = [ctypes.c_int, _up, _ip, _ip, _dp, _dp]
         L.orc_spmv.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_gmres.restype = ctypes.c_int
+        L.orc_gmres.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
+                                _dp]
         _lib = L
     return _lib
 
@@ -197,6 +200,17 @@ class System:
             return None
         return J[k0 + idx]
 
+    def solve_gmres(self, J, rhs, tol=1e-10, restart=50, max_it=10000):
+        """Block-Jacobi GMRES(restart) on all host threads (the timed CPU baseline's
+        linear solve).  Returns (delta distributed, iterations, relative residual)."""
+        d = np.zeros(self.nd)
+        rel = np.zeros(1)
+        its = lib().orc_gmres(self.m.nn, _p(self.rowptr, _ip), _p(self.cols, _ip),
+                              _p(np.ascontiguousarray(J, np.float64).reshape(-1)),
+                              _p(np.ascontiguousarray(rhs, np.float64)), float(tol), int(restart), int(max_it), _p(d),
+                              _p(rel))
+        return self.distribute(d), int(its), float(rel[0])
+
     def solve_exact(self, J, rhs):
         """delta with J_ff delta_f = rhs_f on the unconstrained dofs (sparse LU), then
         distributed through the constraints (reference femgl/src/solve.cc:181)."""
@@ -323,6 +337,17 @@ class System2D:
     def residual(self, x):
         _, R, F = self.assemble(x, want_J=False)
         return R, F
+
+    def solve_gmres(self, J, rhs, tol=1e-10, restart=50, max_it=10000):
+        """Block-Jacobi GMRES(restart) on all host threads (the timed CPU baseline's
+        linear solve).  Returns (delta distributed, iterations, relative residual)."""
+        d = np.zeros(self.nd)
+        rel = np.zeros(1)
+        its = lib().orc_gmres(self.m.nn, _p(self.rowptr, _ip), _p(self.cols, _ip),
+                              _p(np.ascontiguousarray(J, np.float64).reshape(-1)),
+                              _p(np.ascontiguousarray(rhs, np.float64)), float(tol), int(restart), int(max_it), _p(d),
+                              _p(rel))
+        return self.distribute(d), int(its), float(rel[0])
 
     def solve_exact(self, J, rhs):
         import scipy.sparse.linalg as spla

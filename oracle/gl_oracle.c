@@ -599,3 +599,140 @@ int orc_num_threads(void)
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------------
+ * CPU linear solve for the timed CPU baseline: restarted GMRES(m), right
+ * preconditioned with the inverse diagonal blocks (Gauss-Jordan, partial pivoting),
+ * modified Gram-Schmidt, on all OpenMP threads.  Solves J d = b on the pattern;
+ * constrained rows carry only their diagonal, so constrained entries of d stay 0
+ * when b is 0 there.  Returns the iterations done (at most max_it); *relres gets
+ * the final |b - J d| / |b| estimate.
+ * ------------------------------------------------------------------------------ */
+static double dot_omp(long n, const double *a, const double *b)
+{
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (long i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+static void bj_invert(int nn, const int *rowptr, const int *cols, const double *J, double *Dinv)
+{
+#pragma omp parallel for schedule(static)
+  for (int n = 0; n < nn; ++n)
+    {
+      long blk = find_block(rowptr, cols, n, n);
+      double M[18][36];
+      for (int r = 0; r < 18; ++r)
+        for (int c = 0; c < 36; ++c) M[r][c] = (c < 18) ? (blk >= 0 ? J[324 * blk + 18 * r + c] : (r == c)) : (c - 18 == r);
+      int sing = 0;
+      for (int k = 0; k < 18 && !sing; ++k)
+        {
+          int p = k;
+          for (int r = k + 1; r < 18; ++r)
+            if (fabs(M[r][k]) > fabs(M[p][k])) p = r;
+          if (!(fabs(M[p][k]) > 1e-300)) { sing = 1; break; }
+          if (p != k)
+            for (int c = 0; c < 36; ++c) { double t = M[k][c]; M[k][c] = M[p][c]; M[p][c] = t; }
+          const double piv = M[k][k];
+          for (int c = 0; c < 36; ++c) M[k][c] /= piv;
+          for (int r = 0; r < 18; ++r)
+            if (r != k)
+              {
+                const double f = M[r][k];
+                if (f != 0.0)
+                  for (int c = 0; c < 36; ++c) M[r][c] -= f * M[k][c];
+              }
+        }
+      for (int r = 0; r < 18; ++r)
+        for (int c = 0; c < 18; ++c) Dinv[324 * (size_t)n + 18 * r + c] = sing ? (r == c) : M[r][18 + c];
+    }
+}
+
+static void bj_apply(int nn, const double *Dinv, const double *x, double *y)
+{
+#pragma omp parallel for schedule(static)
+  for (int n = 0; n < nn; ++n)
+    for (int r = 0; r < 18; ++r)
+      {
+        double s = 0.0;
+        for (int c = 0; c < 18; ++c) s += Dinv[324 * (size_t)n + 18 * r + c] * x[18 * (size_t)n + c];
+        y[18 * (size_t)n + r] = s;
+      }
+}
+
+int orc_gmres(int nn, const int *rowptr, const int *cols, const double *J, const double *b, double tol, int m,
+              int max_it, double *d, double *relres)
+{
+  const long N = 18L * nn;
+  double *Dinv = malloc(sizeof(double) * 324 * (size_t)nn);
+  double *V = malloc(sizeof(double) * (size_t)(m + 1) * N);
+  double *z = malloc(sizeof(double) * N), *w = malloc(sizeof(double) * N);
+  double *H = calloc((size_t)(m + 1) * m, sizeof(double)), *cs = malloc(sizeof(double) * m),
+         *sn = malloc(sizeof(double) * m), *g = malloc(sizeof(double) * (m + 1)), *y = malloc(sizeof(double) * m);
+  bj_invert(nn, rowptr, cols, J, Dinv);
+  memset(d, 0, sizeof(double) * N);
+  const double bn = sqrt(dot_omp(N, b, b));
+  int total = 0;
+  double res = bn;
+  while (total < max_it && res > tol * bn && bn > 0)
+    {
+      orc_spmv(nn, rowptr, cols, J, d, w);
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < N; ++i) V[i] = b[i] - w[i];
+      const double beta = sqrt(dot_omp(N, V, V));
+      if (!(beta > 0)) break;
+#pragma omp parallel for schedule(static)
+      for (long i = 0; i < N; ++i) V[i] /= beta;
+      memset(g, 0, sizeof(double) * (m + 1));
+      g[0] = beta;
+      int j = 0;
+      for (; j < m && total < max_it; ++j, ++total)
+        {
+          bj_apply(nn, Dinv, V + (size_t)j * N, z);
+          orc_spmv(nn, rowptr, cols, J, z, w);
+          for (int i = 0; i <= j; ++i)
+            {
+              const double h = dot_omp(N, V + (size_t)i * N, w);
+              H[j * (m + 1) + i] = h;
+#pragma omp parallel for schedule(static)
+              for (long k = 0; k < N; ++k) w[k] -= h * V[(size_t)i * N + k];
+            }
+          const double hn = sqrt(dot_omp(N, w, w));
+          H[j * (m + 1) + j + 1] = hn;
+          if (hn > 0)
+#pragma omp parallel for schedule(static)
+            for (long k = 0; k < N; ++k) V[(size_t)(j + 1) * N + k] = w[k] / hn;
+          for (int i = 0; i < j; ++i)
+            {
+              const double a = H[j * (m + 1) + i], c = H[j * (m + 1) + i + 1];
+              H[j * (m + 1) + i] = cs[i] * a + sn[i] * c;
+              H[j * (m + 1) + i + 1] = -sn[i] * a + cs[i] * c;
+            }
+          const double a = H[j * (m + 1) + j], c = H[j * (m + 1) + j + 1], r = hypot(a, c);
+          cs[j] = r > 0 ? a / r : 1.0;
+          sn[j] = r > 0 ? c / r : 0.0;
+          H[j * (m + 1) + j] = r;
+          g[j + 1] = -sn[j] * g[j];
+          g[j] = cs[j] * g[j];
+          res = fabs(g[j + 1]);
+          if (res <= tol * bn || !(hn > 0)) { ++j; ++total; break; }
+        }
+      for (int i = j - 1; i >= 0; --i)
+        {
+          double s = g[i];
+          for (int c2 = i + 1; c2 < j; ++c2) s -= H[c2 * (m + 1) + i] * y[c2];
+          y[i] = H[i * (m + 1) + i] != 0 ? s / H[i * (m + 1) + i] : 0.0;
+        }
+      memset(w, 0, sizeof(double) * N);
+      for (int i = 0; i < j; ++i)
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < N; ++k) w[k] += y[i] * V[(size_t)i * N + k];
+      bj_apply(nn, Dinv, w, z);
+#pragma omp parallel for schedule(static)
+      for (long k = 0; k < N; ++k) d[k] += z[k];
+    }
+  if (relres) *relres = bn > 0 ? res / bn : 0.0;
+  free(Dinv); free(V); free(z); free(w); free(H); free(cs); free(sn); free(g); free(y);
+  return total;
+}

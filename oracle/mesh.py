@@ -179,9 +179,9 @@ class Mesh2D:
         return int(self.xy.shape[0])
 
 
-def square_mesh(n: int) -> Mesh2D:
-    """Unit square, n x n Q1 quads, psi = 0 (both components) on the x = 0 edge."""
-    t = np.linspace(0.0, 1.0, n + 1)
+def square_mesh(n: int, L: float = 1.0) -> Mesh2D:
+    """Square [0, L]^2, n x n Q1 quads, psi = 0 (both components) on the x = 0 edge."""
+    t = np.linspace(0.0, L, n + 1)
     X, Y = np.meshgrid(t, t, indexing="xy")
     xy = np.stack([X.ravel(), Y.ravel()], axis=1)
     j, i = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")

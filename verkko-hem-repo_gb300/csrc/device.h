@@ -10,6 +10,7 @@ namespace glgpu
 constexpr int kNS3 = 171;   // unique entries of a symmetric 18x18 block
 constexpr int kCoef = 8;    // {K1, K2+K3, alpha, beta1..beta5}
 constexpr int kSegThreads = 256;
+constexpr int kSegMax = 1024;   // scalars per reduction segment (one CTA each)
 
 // Mesh and plan arrays resident on the device (read-only during solves).
 struct DevMesh

@@ -88,14 +88,15 @@ struct glgpu_ctx
   uint8_t *d_act = nullptr, *d_act2 = nullptr;
   // pinned host mirrors
   double *h_norm = nullptr, *h_res = nullptr;
-  uint8_t *h_act = nullptr;
+  uint8_t *h_act = nullptr, *h_act_pipe = nullptr;
   int *h_its = nullptr;
+  cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
   // host-side per-instance state
   std::vector<double> rhs_norm, res_norm, lam_max;
   std::vector<uint8_t> inst_on;
   bool has_J = false, has_rhs = false, has_delta = false, prec_ready = false;
   // timing
-  bool ktiming = false;
+  int ktiming = 0; // bitmask of kernel kinds timed with events
   int64_t launches = 0;
   int64_t klaunch[KK_N] = {0};
   double kms[KK_N] = {0};
@@ -169,7 +170,8 @@ void harvest(glgpu_ctx *c)
 template <typename F> glgpu_status launch(glgpu_ctx *c, int kind, int nk, F &&f)
 {
   cudaEvent_t a = nullptr, b = nullptr;
-  if (c->ktiming)
+  const bool timed = (c->ktiming >> kind) & 1;
+  if (timed)
     {
       a = get_event(c);
       b = get_event(c);
@@ -179,7 +181,7 @@ template <typename F> glgpu_status launch(glgpu_ctx *c, int kind, int nk, F &&f)
   if (e != cudaSuccess) return set_error(GLGPU_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   c->launches += nk;
   c->klaunch[kind] += nk;
-  if (c->ktiming)
+  if (timed)
     {
       cudaEventRecord(b, c->st);
       c->kev.push_back({kind, a, b});
@@ -510,11 +512,20 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
             CKS(axpby(c, Vj1, Vj1, nullptr, k, c->g.active, m32, m32, m32));
           }
           jdone = j + 1;
-          CK(cudaMemcpyAsync(c->h_act, c->g.active, n, cudaMemcpyDeviceToHost, c->st));
-          CKS(sync(c));
-          bool anyj = false;
-          for (int k = 0; k < n; ++k) anyj |= c->h_act[k] != 0;
-          if (!anyj) break;
+          // step j's flags are copied out and checked only after step j+1 is enqueued,
+          // so the host round trip overlaps device work; instances that stopped are
+          // masked on the device, which makes a speculative step a no-op for them
+          uint8_t *slot = c->h_act_pipe + (j & 1) * n;
+          CK(cudaMemcpyAsync(slot, c->g.active, n, cudaMemcpyDeviceToHost, c->st));
+          CK(cudaEventRecord(c->ev_pipe[j & 1], c->st));
+          if (j >= 1)
+            {
+              CK(cudaEventSynchronize(c->ev_pipe[(j - 1) & 1]));
+              const uint8_t *prev = c->h_act_pipe + ((j - 1) & 1) * n;
+              bool anyj = false;
+              for (int k = 0; k < n; ++k) anyj |= prev[k] != 0;
+              if (!anyj) break;
+            }
         }
       // X += M^-1 (V y)
       CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_solve_y(c->g, n, c->st); }));
@@ -726,12 +737,17 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   c->g.m = mr;
   if (cudaMallocHost(&c->h_norm, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||
       cudaMallocHost(&c->h_res, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||
-      cudaMallocHost(&c->h_act, n_inst) != cudaSuccess || cudaMallocHost(&c->h_its, sizeof(int) * n_inst) != cudaSuccess)
+      cudaMallocHost(&c->h_act, n_inst) != cudaSuccess || cudaMallocHost(&c->h_act_pipe, 2 * n_inst) != cudaSuccess ||
+      cudaMallocHost(&c->h_its, sizeof(int) * n_inst) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_pipe[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_pipe[1], cudaEventDisableTiming) != cudaSuccess)
     return fail(set_error(GLGPU_ERR_NOMEM, "glgpu_create: pinned host allocation failed"));
   if (cudaMemsetAsync(c->x, 0, sizeof(double) * N, c->st) != cudaSuccess ||
       cudaMemsetAsync(c->delta, 0, sizeof(double) * N, c->st) != cudaSuccess ||
       cudaMemsetAsync(c->R, 0, sizeof(double) * N, c->st) != cudaSuccess ||
       cudaMemsetAsync(c->rhs, 0, sizeof(double) * N, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->V, 0, tsz(c) * static_cast<size_t>(mr + 1) * N, c->st) != cudaSuccess ||
+      cudaMemsetAsync(c->H, 0, tsz(c) * static_cast<size_t>(P.nc) * c->nq * c->ns, c->st) != cudaSuccess ||
       cudaStreamSynchronize(c->st) != cudaSuccess)
     return fail(set_error(GLGPU_ERR_CUDA, "glgpu_create: initialisation failed"));
   c->rhs_norm.assign(n_inst, 0.0);
@@ -764,6 +780,9 @@ extern "C" glgpu_status glgpu_destroy(glgpu_ctx *c)
   if (c->h_norm) cudaFreeHost(c->h_norm);
   if (c->h_res) cudaFreeHost(c->h_res);
   if (c->h_act) cudaFreeHost(c->h_act);
+  if (c->h_act_pipe) cudaFreeHost(c->h_act_pipe);
+  for (auto e : c->ev_pipe)
+    if (e) cudaEventDestroy(e);
   if (c->h_its) cudaFreeHost(c->h_its);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
@@ -1068,7 +1087,7 @@ extern "C" glgpu_status glgpu_kernel_timing(glgpu_ctx *c, int enable, double *ke
         c->kms[i] = 0.0;
         c->klaunch[i] = 0;
       }
-  c->ktiming = enable != 0;
+  c->ktiming = enable;
   return GLGPU_OK;
 }
 

@@ -286,10 +286,11 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
       S.gA[pq][2][c] = g2 * S.ih[cl][2];
     }
   __syncthreads();
-  // P = A A^T, Q = A A^+, M2 = A^+ A, M3 = A^T A
-  for (int idx = tid; idx < kNPQ * 36; idx += kCellThreads)
+  // P = A A^T, Q = A A^+ (residual and Hessian), M2 = A^+ A, M3 = A^T A (Hessian only)
+  for (int idx = tid; idx < kNPQ * (WH ? 36 : 18); idx += kCellThreads)
     {
-      const int pq = idx / 36, r = idx % 36, which = r / 9, ent = r % 9, i = ent / 3, l = ent % 3;
+      constexpr int per = WH ? 36 : 18;
+      const int pq = idx / per, r = idx % per, which = r / 9, ent = r % 9, i = ent / 3, l = ent % 3;
       const T *A = S.A[pq];
       cx<T> s = {T(0), T(0)};
 #pragma unroll
@@ -420,78 +421,104 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
 // ---------------------------------------------------------------------------------
 constexpr int kRowThreads = 192;
 
+constexpr int kRowMaxContrib = 96; // contributions staged in shared memory per pass
+
 template <typename T>
 __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *acc = reinterpret_cast<T *>(smem_raw);
   __shared__ T sD[8 * 8 * 9];
+  __shared__ int s_cell[kRowMaxContrib], s_a[kRowMaxContrib];
+  __shared__ T s_w[kRowMaxContrib];
+  __shared__ int16_t s_slot[kRowMaxContrib * 8];
   const int64_t n = blockIdx.x;
   const int tid = threadIdx.x;
   const int r0 = m.rowptr[n];
   const int nb = m.rowptr[n + 1] - r0;
+  // row metadata (column ids and their Dirichlet masks) follow the accumulator
+  int *s_col = reinterpret_cast<int *>(acc + static_cast<size_t>(m.max_row_blocks) * 324);
+  uint32_t *s_cmask = reinterpret_cast<uint32_t *>(s_col + m.max_row_blocks);
   for (int i = tid; i < nb * 324; i += kRowThreads) acc[i] = T(0);
   for (int i = tid; i < 576; i += kRowThreads) sD[i] = static_cast<T>((&c_D3[0][0][0])[i]);
-  __syncthreads();
+  for (int i = tid; i < nb; i += kRowThreads)
+    {
+      const int col = m.cols[r0 + i];
+      s_col[i] = col;
+      s_cmask[i] = m.mask[col];
+    }
   const bool act = tid < kNS3;
   const int c = act ? c_symc[tid] : 0, d = act ? c_symd[tid] : 0;
   const int pmc = 3 * (c / 9) + (c % 9) / 3, jc = c % 3, pmd = 3 * (d / 9) + (d % 9) / 3, jd = d % 3;
   const bool kpair = (pmc == pmd);
   const struct HangTarget *tg = reinterpret_cast<const HangTarget *>(m.hang_tg);
   const int k0 = m.rc_ptr[n], k1 = m.rc_ptr[n + 1];
-  for (int k = k0; k < k1; ++k)
+  for (int kb = k0; kb < k1; kb += kRowMaxContrib)
     {
-      const int64_t e = m.rc_cell[k];
-      const int a = m.rc_a[k];
-      const T wa = static_cast<T>(m.rc_w[k]);
-      const int inst = m.cell_inst[e];
-      const T K1 = static_cast<T>(m.coef[inst * kCoef + 0]), K23 = static_cast<T>(m.coef[inst * kCoef + 1]);
-      const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
-      const T vol = static_cast<T>(hx * hy * hz);
-      const T ih[3] = {static_cast<T>(1.0 / hx), static_cast<T>(1.0 / hy), static_cast<T>(1.0 / hz)};
-      T hq[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) hq[q] = act ? H[(e * 8 + q) * kNS3 + tid] : T(0);
-      const T kd = K1 * vol;
-      const T kc = K23 * vol * ih[jc] * ih[jd];
-#pragma unroll 1
-      for (int b = 0; b < 8; ++b)
+      const int nk = min(kRowMaxContrib, k1 - kb);
+      __syncthreads();
+      for (int i = tid; i < nk; i += kRowThreads)
         {
-          T bulk = 0;
+          s_cell[i] = m.rc_cell[kb + i];
+          s_a[i] = m.rc_a[kb + i];
+          s_w[i] = static_cast<T>(m.rc_w[kb + i]);
+        }
+      for (int i = tid; i < nk * 8; i += kRowThreads) s_slot[i] = m.rc_slot[static_cast<int64_t>(kb) * 8 + i];
+      __syncthreads();
+      for (int kk = 0; kk < nk; ++kk)
+        {
+          const int64_t e = s_cell[kk];
+          const int a = s_a[kk];
+          const T wa = s_w[kk];
+          T hq[8];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) bulk += static_cast<T>(c_S3[a][b][q]) * hq[q];
-          bulk *= vol;
-          const T *D = sD + (a * 8 + b) * 9;
-          T gcd = 0, gdc = 0;
-          if (c == d)
+          for (int q = 0; q < 8; ++q) hq[q] = act ? __ldg(H + (e * 8 + q) * kNS3 + tid) : T(0);
+          const int inst = m.cell_inst[e];
+          const T K1 = static_cast<T>(m.coef[inst * kCoef + 0]), K23 = static_cast<T>(m.coef[inst * kCoef + 1]);
+          const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
+          const T vol = static_cast<T>(hx * hy * hz);
+          const T i0 = static_cast<T>(1.0 / hx), i1 = static_cast<T>(1.0 / hy), i2 = static_cast<T>(1.0 / hz);
+          const T ihc = jc == 0 ? i0 : (jc == 1 ? i1 : i2);
+          const T ihd = jd == 0 ? i0 : (jd == 1 ? i1 : i2);
+          const T kd = K1 * vol;
+          const T kc = K23 * vol * ihc * ihd;
+          const T g0 = i0 * i0, g1 = i1 * i1, g2 = i2 * i2;
+#pragma unroll 2
+          for (int b = 0; b < 8; ++b)
             {
-              const T gg = D[0] * ih[0] * ih[0] + D[4] * ih[1] * ih[1] + D[8] * ih[2] * ih[2];
-              gcd = gdc = kd * gg;
-            }
-          if (kpair)
-            {
-              gcd += kc * D[3 * jc + jd];
-              gdc += kc * D[3 * jd + jc];
-            }
-          const int sl = m.rc_slot[static_cast<int64_t>(k) * 8 + b];
-          if (sl >= 0)
-            {
-              if (act)
+              T bulk = 0;
+#pragma unroll
+              for (int q = 0; q < 8; ++q) bulk += static_cast<T>(c_S3[a][b][q]) * hq[q];
+              bulk *= vol;
+              const T *D = sD + (a * 8 + b) * 9;
+              T gcd = 0, gdc = 0;
+              if (c == d) gcd = gdc = kd * (D[0] * g0 + D[4] * g1 + D[8] * g2);
+              if (kpair)
                 {
-                  acc[sl * 324 + c * 18 + d] += wa * (bulk + gcd);
-                  if (c != d) acc[sl * 324 + d * 18 + c] += wa * (bulk + gdc);
+                  gcd += kc * D[3 * jc + jd];
+                  gdc += kc * D[3 * jd + jc];
                 }
-            }
-          else
-            {
-              const HangTarget &t = tg[m.ht_off[n] + (-1 - sl)];
-              for (int j = 0; j < t.count; ++j)
-                if (act)
-                  {
-                    const T w = wa * static_cast<T>(t.w[j]);
-                    acc[t.slot[j] * 324 + c * 18 + d] += w * (bulk + gcd);
-                    if (c != d) acc[t.slot[j] * 324 + d * 18 + c] += w * (bulk + gdc);
-                  }
+              const int sl = s_slot[kk * 8 + b];
+              if (sl >= 0)
+                {
+                  if (act)
+                    {
+                      acc[sl * 324 + c * 18 + d] += wa * (bulk + gcd);
+                      if (c != d) acc[sl * 324 + d * 18 + c] += wa * (bulk + gdc);
+                    }
+                }
+              else
+                {
+                  const HangTarget &t = tg[m.ht_off[n] + (-1 - sl)];
+                  const int cnt = t.count;
+                  for (int j = 0; j < cnt; ++j)
+                    if (act)
+                      {
+                        const T w = wa * static_cast<T>(t.w[j]);
+                        acc[t.slot[j] * 324 + c * 18 + d] += w * (bulk + gcd);
+                        if (c != d) acc[t.slot[j] * 324 + d * 18 + c] += w * (bulk + gdc);
+                      }
+                }
             }
         }
     }
@@ -501,14 +528,14 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
   T *out = vals + static_cast<int64_t>(r0) * 324;
   for (int i = tid; i < nb * 324; i += kRowThreads)
     {
-      const int sl = i / 324, e2 = i % 324, cc = e2 / 18, dd = e2 % 18;
-      const int col = m.cols[r0 + sl];
+      const int sl = i / 324, e2 = i - sl * 324, cc = e2 / 18, dd = e2 - cc * 18;
+      const int col = s_col[sl];
       T v = acc[i];
       if (hang_row)
         v = (cc == dd) ? T(1) : T(0);
       else if ((rmask >> cc) & 1u)
         v = (col == n && cc == dd) ? (v != T(0) ? fabs(v) : T(1)) : T(0);
-      else if ((m.mask[col] >> dd) & 1u)
+      else if ((s_cmask[sl] >> dd) & 1u)
         v = T(0);
       out[i] = v;
     }
@@ -716,7 +743,7 @@ template <typename T> static cudaError_t launch_rows_t(const DevMesh &m, const T
 {
   if (m.dim == 3)
     {
-      const size_t sm = static_cast<size_t>(m.max_row_blocks) * 324 * sizeof(T);
+      const size_t sm = static_cast<size_t>(m.max_row_blocks) * (324 * sizeof(T) + 2 * sizeof(int));
       static size_t attr = 0;
       if (sm > attr)
         {

@@ -372,36 +372,56 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
   return s; // valid in thread 0
 }
 
-constexpr int kSegPer = 16; // scalars per thread and segment (seg_len <= 16 * 256)
-
+// Multi-dot partials: the segment of y is staged in shared memory once, then each warp
+// takes basis vectors v = warp, warp + 8, ... and reduces with shuffles only.
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(kSegThreads) k_seg_mdot(DevMesh m, const TX *__restrict__ X, int64_t ld, int nvec,
                                                           const TY *__restrict__ y, double *__restrict__ partial,
                                                           const uint8_t *__restrict__ act)
 {
-  __shared__ double sh[kSegThreads / 32];
+  __shared__ TY ys[kSegMax];
   const int s = blockIdx.x;
-  const int64_t b = m.seg_begin[s], e = m.seg_end[s];
+  const int64_t b = m.seg_begin[s];
+  const int len = static_cast<int>(m.seg_end[s] - b);
   const bool on = !act || act[m.seg_inst[s]];
-  double yv[kSegPer];
-#pragma unroll
-  for (int k = 0; k < kSegPer; ++k)
-    {
-      const int64_t i = b + threadIdx.x + static_cast<int64_t>(k) * kSegThreads;
-      yv[k] = (on && i < e) ? static_cast<double>(y[i]) : 0.0;
-    }
-  for (int v = 0; v < nvec; ++v)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (on)
+    for (int i = threadIdx.x; i < len; i += kSegThreads) ys[i] = y[b + i];
+  __syncthreads();
+  for (int v = warp; v < nvec; v += kSegThreads / 32)
     {
       double acc = 0.0;
       if (on)
+        {
+          const TX *xv = X + v * ld + b;
+          float facc0 = 0.f, facc1 = 0.f;
+          double dacc0 = 0.0, dacc1 = 0.0;
+          int i = lane;
+          for (; i + 32 < len; i += 64)
+            {
+              if (sizeof(TX) == 4)
+                {
+                  facc0 += static_cast<float>(xv[i]) * static_cast<float>(ys[i]);
+                  facc1 += static_cast<float>(xv[i + 32]) * static_cast<float>(ys[i + 32]);
+                }
+              else
+                {
+                  dacc0 += static_cast<double>(xv[i]) * static_cast<double>(ys[i]);
+                  dacc1 += static_cast<double>(xv[i + 32]) * static_cast<double>(ys[i + 32]);
+                }
+            }
+          if (i < len)
+            {
+              if (sizeof(TX) == 4)
+                facc0 += static_cast<float>(xv[i]) * static_cast<float>(ys[i]);
+              else
+                dacc0 += static_cast<double>(xv[i]) * static_cast<double>(ys[i]);
+            }
+          acc = static_cast<double>(facc0) + static_cast<double>(facc1) + dacc0 + dacc1;
+        }
 #pragma unroll
-        for (int k = 0; k < kSegPer; ++k)
-          {
-            const int64_t i = b + threadIdx.x + static_cast<int64_t>(k) * kSegThreads;
-            if (i < e) acc += static_cast<double>(X[v * ld + i]) * yv[k];
-          }
-      const double tot = block_sum(acc, sh);
-      if (threadIdx.x == 0) partial[static_cast<int64_t>(s) * nvec + v] = tot;
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (lane == 0) partial[static_cast<int64_t>(s) * nvec + v] = acc;
     }
 }
 
@@ -417,22 +437,27 @@ cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t 
   return cudaGetLastError();
 }
 
+// one warp per (instance, vector): lanes take segments lane, lane + 32, ... in a fixed
+// order, then a fixed shuffle tree: deterministic
 __global__ void k_seg_finalize(DevMesh m, const double *__restrict__ partial, int nvec, double *__restrict__ out,
                                int ld_out, int take_sqrt)
 {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m.n_inst * nvec) return;
-  const int inst = t / nvec, v = t % nvec;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= m.n_inst * nvec) return;
+  const int inst = w / nvec, v = w % nvec;
   double s = 0.0;
-  for (int g = m.inst_seg_off[inst]; g < m.inst_seg_off[inst + 1]; ++g) s += partial[static_cast<int64_t>(g) * nvec + v];
-  out[inst * ld_out + v] = take_sqrt ? sqrt(s) : s;
+  for (int g = m.inst_seg_off[inst] + lane; g < m.inst_seg_off[inst + 1]; g += 32)
+    s += partial[static_cast<int64_t>(g) * nvec + v];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) out[inst * ld_out + v] = take_sqrt ? sqrt(s) : s;
 }
 
 cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nvec, double *out, int ld_out,
                                 int take_sqrt, cudaStream_t s)
 {
-  const int n = m.n_inst * nvec;
-  k_seg_finalize<<<(n + 127) / 128, 128, 0, s>>>(m, partial, nvec, out, ld_out, take_sqrt);
+  const int nw = m.n_inst * nvec;
+  k_seg_finalize<<<(nw + 3) / 4, 128, 0, s>>>(m, partial, nvec, out, ld_out, take_sqrt);
   return cudaGetLastError();
 }
 
@@ -451,7 +476,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_maxpy(DevMesh m, const T *_
   for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads)
     {
       double acc = static_cast<double>(y[i]);
-      for (int v = 0; v < nvec; ++v) acc -= cf[v] * static_cast<double>(X[v * ld + i]);
+      for (int v = 0; v < nvec; ++v)
+        if (cf[v] != 0.0) acc -= cf[v] * static_cast<double>(X[v * ld + i]); // unused columns may hold stale data
       y[i] = static_cast<T>(acc);
     }
 }

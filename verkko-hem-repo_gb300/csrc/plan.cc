@@ -12,6 +12,11 @@
 
 #include "glgpu_internal.h"
 
+namespace
+{
+constexpr int kSegLen = 1024; // must not exceed kSegMax of the device kernels
+}
+
 namespace glgpu
 {
 namespace
@@ -306,7 +311,7 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   if (bad) return set_error(GLGPU_ERR_ARG, "glgpu_create: inconsistent constraint pattern");
   P.ht_off.assign(ht_off.begin(), ht_off.end());
   // reduction segments
-  P.seg_len = 4096;
+  P.seg_len = kSegLen;
   P.seg_begin.clear();
   P.seg_end.clear();
   P.seg_inst.clear();

@@ -197,9 +197,10 @@ def cube_mesh(half: float, n: int, refine_frac: float = 0.0) -> Mesh:
     return box_mesh([-half] * 3, [half] * 3, (n, n, n), refine_band=refine_frac * 2.0 * half)
 
 
-def square_mesh(n: int) -> Mesh:
-    """Unit square, n x n Q1 quads, psi = 0 on the x = 0 edge (complexGL 2D)."""
-    t = np.linspace(0.0, 1.0, n + 1)
+def square_mesh(n: int, L: float = 1.0) -> Mesh:
+    """Square [0, L]^2, n x n Q1 quads, psi = 0 on the x = 0 edge (complexGL 2D;
+    the archive's configuration is the unit square)."""
+    t = np.linspace(0.0, L, n + 1)
     X, Y = np.meshgrid(t, t, indexing="xy")
     xy = np.stack([X.ravel(), Y.ravel()], axis=1)
     j, i = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
@@ -395,10 +396,12 @@ class FemGL:
         _check(lib().glgpu_timers(self._ctx, _p(ms), int(reset)))
         return dict(zip(PHASES, ms.tolist()))
 
-    def kernel_timing(self, enable: bool, reset: bool = False):
+    def kernel_timing(self, enable, reset: bool = False):
+        """enable: bitmask of kernel kinds to time (bit k = KERNEL_KINDS[k]); True = all."""
         ms = np.zeros(6)
         n = np.zeros(6, np.int64)
-        _check(lib().glgpu_kernel_timing(self._ctx, int(enable), _p(ms), _p(n, _lp), int(reset)))
+        mask = -1 if enable is True else int(enable)
+        _check(lib().glgpu_kernel_timing(self._ctx, mask, _p(ms), _p(n, _lp), int(reset)))
         return dict(zip(KERNEL_KINDS, ms.tolist())), dict(zip(KERNEL_KINDS, n.tolist()))
 
     @property
