@@ -186,8 +186,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--linear-tol", type=float, default=1e-4)
+    ap.add_argument("--ncu-case", type=int, default=0,
+                    help="profiling case: one mixed assembly + 30 GMRES iterations on an N^3 cube, no timing")
+    ap.add_argument("--fp64", action="store_true", help="with --ncu-case: FP64 instead of mixed")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.ncu_case:
+        return ncu_case(args.ncu_case, args.fp64)
     if args.impl == "reference":
         return reference_arm(args, rank)
     gl = importlib.import_module("verkko-hem-repo_gb300")
@@ -273,6 +278,23 @@ def main():
     except Exception as e:  # the CPU baseline must not hide the GPU line
         line["cpu_baseline"] = {"value": None, "error": str(e)}
     print(json.dumps(line))
+
+
+def ncu_case(n, fp64):
+    """Small fixed workload for ncu captures (committed so profiles name runnable commands)."""
+    gl = importlib.import_module("verkko-hem-repo_gb300")
+    gl.build()
+    m = gl.cube_mesh(HALF, n)
+    x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=gl.FP64 if fp64 else gl.MIXED, gmres_max_iter=30)
+    with gl.FemGL(m, prm) as f:
+        f.set_solution(x0)
+        rn = f.assemble_system()
+        its = f.solve(1e-12, allow_unconverged=True)
+        f.sync()
+        print(json.dumps({"ncu_case": n, "fp64": bool(fp64), "rhs_norm": float(rn[0]), "gmres_its": int(its[0]),
+                          "launches": f.launch_count}))
+    return 0
 
 
 def reference_arm(args, rank):
