@@ -223,17 +223,23 @@ class System:
         return self.distribute(d)
 
 
-def newton(system, x0, tol=1e-10, max_iter=40, step=0.83, max_trials=100, damped=True, log=None):
+def newton(system, x0, tol=1e-10, max_iter=40, step=0.83, max_trials=100, damped=True, log=None,
+           linear_tol=None, restart=50):
     """The reference's outer loop (run.cc:207-256) with its damped Newton step
-    (iteration.cc:130-210) and an exact linear solve.  Returns (x, history) where
-    history holds one dict per Newton iteration."""
+    (iteration.cc:130-210).  The linear solve is exact (sparse LU) by default, or
+    block-Jacobi GMRES(restart) to linear_tol * ||rhs|| (solve.cc:159-160) when
+    linear_tol is given.  Returns (x, history) with one dict per Newton iteration."""
     x = system.distribute(x0)
     hist = []
     for it in range(max_iter + 1):
         J, R, F = system.assemble(x)
         rhs = -R
         prev = float(np.linalg.norm(rhs))
-        delta = system.solve_exact(J, rhs)
+        lin_its = 0
+        if linear_tol is None:
+            delta = system.solve_exact(J, rhs)
+        else:
+            delta, lin_its, _ = system.solve_gmres(J, rhs, tol=linear_tol, restart=restart)
         trials = 0
         x_trial = x
         cur = None
@@ -247,7 +253,7 @@ def newton(system, x0, tol=1e-10, max_iter=40, step=0.83, max_trials=100, damped
             if cur < prev:
                 break
         x = x_trial
-        hist.append({"iter": it, "res_before": prev, "res": cur, "trials": trials, "F": Ft})
+        hist.append({"iter": it, "res_before": prev, "res": cur, "trials": trials, "F": Ft, "linear_its": lin_its})
         if log:
             log(hist[-1])
         if cur <= tol:

@@ -12,6 +12,12 @@ constexpr int kCoef = 8;    // {K1, K2+K3, alpha, beta1..beta5}
 constexpr int kSegThreads = 256;
 constexpr int kSegMax = 1024;   // scalars per reduction segment (one CTA each)
 
+// Per-cell geometry of an axis-aligned box cell: {1/hx, 1/hy, 1/hz, hx*hy*hz}.
+struct __align__(32) GeoD
+{
+  double x, y, z, w;
+};
+
 // Mesh and plan arrays resident on the device (read-only during solves).
 struct DevMesh
 {
@@ -20,6 +26,10 @@ struct DevMesh
   int max_row_blocks;
   const int32_t *cells;       // [nc][nv]
   const double *cell_h;       // [nc][3]
+  const GeoD *geo_d;       // [nc] {1/hx, 1/hy, 1/hz, hx*hy*hz}
+  const float4 *geo_f;        // same in FP32 (the FP32 kernels never touch the FP64 pipe)
+  const float *coef_f;        // [n_inst][kCoef] FP32 copy of coef
+  const float *rc_wf;         // FP32 copy of rc_w
   const int32_t *cell_inst;   // [nc]
   const int32_t *node_inst;   // [nn]
   const uint32_t *mask;       // [nn]
@@ -67,6 +77,11 @@ cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nve
 // y -= sum_v coef[inst][v] X[v]   (coef ld = ldc doubles per instance)
 cudaError_t launch_seg_maxpy(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
                              int ldc, void *y, const uint8_t *inst_active, cudaStream_t s);
+// y_seg -= sum_v coef[inst][v] X[v]; then partial2[s][v] = X[v].y (v < nvec2) and,
+// when partial_norm != NULL, partial_norm[s] = y.y, from the updated y in one pass
+cudaError_t launch_seg_update(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
+                              int ldc, void *y, int nvec2, double *partial2, double *partial_norm,
+                              const uint8_t *inst_active, cudaStream_t s);
 // generic per-instance vector update: y = a[inst]*x + b[inst]*y (+ c[inst]*z when z != NULL);
 // a, b, c index per instance with the given strides (stride 0 = a scalar held at a[0])
 struct Axpby

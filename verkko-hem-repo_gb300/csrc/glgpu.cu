@@ -81,7 +81,7 @@ struct glgpu_ctx
   // Krylov (element type T = float in mixed mode, double otherwise)
   void *V = nullptr, *Z = nullptr, *X = nullptr, *Tmp = nullptr, *Bv = nullptr, *C1 = nullptr, *C2 = nullptr,
        *C3 = nullptr;
-  double *partial = nullptr;
+  double *partial = nullptr, *partial_n = nullptr;
   GmresDev g{};
   // per-instance small arrays (device)
   double *d_norm = nullptr, *d_a = nullptr, *d_energy = nullptr, *d_cheb = nullptr, *d_tmp = nullptr;
@@ -491,19 +491,22 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
           void *Vj1 = tptr(c, c->V, static_cast<int64_t>(j + 1) * N);
           CKS(precond(c, Vj, c->Z, c->g.active));
           CKS(spmv(c, c->Z, Vj1, c->g.active));
-          for (int pass = 0; pass < 2; ++pass)
-            {
-              double *hc = pass == 0 ? c->g.hcol : c->g.hcol2;
-              CKS(launch(c, KK_VEC, 1, [&] {
-                return launch_seg_mdot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.active, c->st);
-              }));
-              CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, hc, mr + 2, 0, c->st); }));
-              CKS(launch(c, KK_VEC, 1, [&] {
-                return launch_seg_maxpy(c->dm, m32, c->V, N, j + 1, hc, mr + 2, Vj1, c->g.active, c->st);
-              }));
-            }
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m32, Vj1, 0, 1, Vj1, c->partial, c->g.active, c->st); }));
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->g.hcol + j + 1, mr + 2, 1, c->st); }));
+          // classical Gram-Schmidt with one reorthogonalization; the second projection
+          // and the norm come out of the update passes (3 reads of the basis, not 4)
+          CKS(launch(c, KK_VEC, 1, [&] {
+            return launch_seg_mdot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.active, c->st);
+          }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol, mr + 2, 0, c->st); }));
+          CKS(launch(c, KK_VEC, 1, [&] {
+            return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol, mr + 2, Vj1, j + 1, c->partial, nullptr,
+                                     c->g.active, c->st);
+          }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol2, mr + 2, 0, c->st); }));
+          CKS(launch(c, KK_VEC, 1, [&] {
+            return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol2, mr + 2, Vj1, 0, nullptr, c->partial_n,
+                                     c->g.active, c->st);
+          }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial_n, 1, c->g.hcol + j + 1, mr + 2, 1, c->st); }));
           CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_column(c->g, n, j, c->st); }));
           {
             Axpby k{};
@@ -652,6 +655,19 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   int64_t *p_hto, *p_sb, *p_se, *p_co;
   HangTarget *p_tg;
   std::vector<double> coef(static_cast<size_t>(n_inst) * kCoef);
+  std::vector<GeoD> geo_d(P.nc);
+  std::vector<float4> geo_f(P.nc);
+  for (int64_t e = 0; e < P.nc; ++e)
+    {
+      const double hx = P.cell_h[3 * e], hy = P.cell_h[3 * e + 1], hz = P.cell_h[3 * e + 2];
+      geo_d[e] = GeoD{1.0 / hx, 1.0 / hy, 1.0 / hz, hx * hy * hz};
+      geo_f[e] = make_float4(static_cast<float>(1.0 / hx), static_cast<float>(1.0 / hy), static_cast<float>(1.0 / hz),
+                             static_cast<float>(hx * hy * hz));
+    }
+  std::vector<float> rc_wf(P.rc_w.begin(), P.rc_w.end());
+  GeoD *p_geod;
+  float4 *p_geof;
+  float *p_coeff, *p_rcwf;
   for (int k = 0; k < n_inst; ++k)
     {
       coef[k * kCoef + 0] = prm[k].K1;
@@ -667,8 +683,17 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = dupload(c, &p_slot, P.rc_slot)) || (s = dupload(c, &p_hto, P.ht_off)) || (s = dupload(c, &p_tg, P.hang_tg)) ||
       (s = dupload(c, &p_coef, coef)) || (s = dupload(c, &p_sb, P.seg_begin)) || (s = dupload(c, &p_se, P.seg_end)) ||
       (s = dupload(c, &p_si, P.seg_inst)) || (s = dupload(c, &p_iso, P.inst_seg_off)) ||
-      (s = dupload(c, &p_co, P.cell_off)))
+      (s = dupload(c, &p_co, P.cell_off)) || (s = dupload(c, &p_geod, geo_d)) || (s = dupload(c, &p_geof, geo_f)) ||
+      (s = dupload(c, &p_rcwf, rc_wf)))
     return fail(s);
+  {
+    std::vector<float> cf(coef.begin(), coef.end());
+    if ((s = dupload(c, &p_coeff, cf))) return fail(s);
+  }
+  d.geo_d = p_geod;
+  d.geo_f = p_geof;
+  d.coef_f = p_coeff;
+  d.rc_wf = p_rcwf;
   d.cells = p_cells;
   d.cell_h = p_h;
   d.cell_inst = p_ci;
@@ -719,6 +744,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
     return fail(s);
   (void)pv;
   if ((s = dalloc(c, &c->partial, static_cast<size_t>(d.n_seg) * (mr + 2))) ||
+      (s = dalloc(c, &c->partial_n, static_cast<size_t>(d.n_seg))) ||
       (s = dalloc(c, &c->g.H, static_cast<size_t>(n_inst) * (mr + 1) * mr)) ||
       (s = dalloc(c, &c->g.cs, static_cast<size_t>(n_inst) * mr)) ||
       (s = dalloc(c, &c->g.sn, static_cast<size_t>(n_inst) * mr)) ||

@@ -34,6 +34,10 @@ __constant__ double c_val3[8][8];    // [q][v]
 __constant__ double c_grd3[8][8][3]; // [q][v][k] derivative on the unit cube
 __constant__ double c_S3[8][8][8];   // [a][b][q] = val[q][a] val[q][b] / 8
 __constant__ double c_D3[8][8][9];   // [a][b][3j+k] = (1/8) sum_q grd[q][a][j] grd[q][b][k]
+__constant__ float c_val3f[8][8];
+__constant__ float c_grd3f[8][8][3];
+__constant__ float c_S3f[8][8][8];
+__constant__ float c_D3f[8][8][9];
 __constant__ unsigned char c_symc[kNS3], c_symd[kNS3];
 __constant__ double c_val2[4][4];
 __constant__ double c_grd2[4][4][2];
@@ -114,7 +118,16 @@ cudaError_t init_constants()
               D2[a][b][2 * j + k] = 0.25 * s;
             }
       }
+  float val3f[8][8], grd3f[8][8][3], S3f[8][8][8], D3f[8][8][9];
+  for (int i = 0; i < 64; ++i) (&val3f[0][0])[i] = static_cast<float>((&val3[0][0])[i]);
+  for (int i = 0; i < 192; ++i) (&grd3f[0][0][0])[i] = static_cast<float>((&grd3[0][0][0])[i]);
+  for (int i = 0; i < 512; ++i) (&S3f[0][0][0])[i] = static_cast<float>((&S3[0][0][0])[i]);
+  for (int i = 0; i < 576; ++i) (&D3f[0][0][0])[i] = static_cast<float>((&D3[0][0][0])[i]);
   cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(c_val3f, val3f, sizeof val3f)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_grd3f, grd3f, sizeof grd3f)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_S3f, S3f, sizeof S3f)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_D3f, D3f, sizeof D3f)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_val3, val3, sizeof val3)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_grd3, grd3, sizeof grd3)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_S3, S3, sizeof S3)) != cudaSuccess) return e;
@@ -126,6 +139,29 @@ cudaError_t init_constants()
   if ((e = cudaMemcpyToSymbol(c_S2, S2, sizeof S2)) != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_D2, D2, sizeof D2);
 }
+
+// typed access to the tables, geometry and weights: FP32 kernels read FP32 copies
+template <typename T> struct Tab;
+template <> struct Tab<float>
+{
+  static __device__ __forceinline__ float val(int q, int v) { return c_val3f[q][v]; }
+  static __device__ __forceinline__ float grd(int q, int v, int k) { return c_grd3f[q][v][k]; }
+  static __device__ __forceinline__ float S(int a, int b, int q) { return c_S3f[a][b][q]; }
+  static __device__ __forceinline__ const float *D() { return &c_D3f[0][0][0]; }
+  static __device__ __forceinline__ float4 geo(const DevMesh &m, int64_t e) { return m.geo_f[e]; }
+  static __device__ __forceinline__ float coef(const DevMesh &m, int inst, int k) { return m.coef_f[inst * kCoef + k]; }
+  static __device__ __forceinline__ float w(const DevMesh &m, int64_t k) { return m.rc_wf[k]; }
+};
+template <> struct Tab<double>
+{
+  static __device__ __forceinline__ double val(int q, int v) { return c_val3[q][v]; }
+  static __device__ __forceinline__ double grd(int q, int v, int k) { return c_grd3[q][v][k]; }
+  static __device__ __forceinline__ double S(int a, int b, int q) { return c_S3[a][b][q]; }
+  static __device__ __forceinline__ const double *D() { return &c_D3[0][0][0]; }
+  static __device__ __forceinline__ GeoD geo(const DevMesh &m, int64_t e) { return m.geo_d[e]; }
+  static __device__ __forceinline__ double coef(const DevMesh &m, int inst, int k) { return m.coef[inst * kCoef + k]; }
+  static __device__ __forceinline__ double w(const DevMesh &m, int64_t k) { return m.rc_w[k]; }
+};
 
 // ---------------------------------------------------------------------------------
 // small complex helpers
@@ -244,12 +280,12 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
           const int64_t e = e0 + tid;
           const int inst = m.cell_inst[e];
           skip = (inst_active && !inst_active[inst]) ? 1 : 0;
-          for (int k = 0; k < kCoef; ++k) S.coef[tid][k] = static_cast<T>(m.coef[inst * kCoef + k]);
-          const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
-          S.ih[tid][0] = static_cast<T>(1.0 / hx);
-          S.ih[tid][1] = static_cast<T>(1.0 / hy);
-          S.ih[tid][2] = static_cast<T>(1.0 / hz);
-          S.jxw[tid] = static_cast<T>(0.125 * hx * hy * hz);
+          for (int k = 0; k < kCoef; ++k) S.coef[tid][k] = Tab<T>::coef(m, inst, k);
+          const auto g = Tab<T>::geo(m, e);
+          S.ih[tid][0] = g.x;
+          S.ih[tid][1] = g.y;
+          S.ih[tid][2] = g.z;
+          S.jxw[tid] = T(0.125) * g.w;
         }
       s_skip[tid] = skip;
     }
@@ -275,10 +311,10 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
       for (int v = 0; v < 8; ++v)
         {
           const T xv = S.xs[cl][v][c];
-          a += static_cast<T>(c_val3[q][v]) * xv;
-          g0 += static_cast<T>(c_grd3[q][v][0]) * xv;
-          g1 += static_cast<T>(c_grd3[q][v][1]) * xv;
-          g2 += static_cast<T>(c_grd3[q][v][2]) * xv;
+          a += Tab<T>::val(q, v) * xv;
+          g0 += Tab<T>::grd(q, v, 0) * xv;
+          g1 += Tab<T>::grd(q, v, 1) * xv;
+          g2 += Tab<T>::grd(q, v, 2) * xv;
         }
       S.A[pq][c] = a;
       S.gA[pq][0][c] = g0 * S.ih[cl][0];
@@ -398,11 +434,11 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
           for (int q = 0; q < 8; ++q)
             {
               const int pq = cl * 8 + q;
-              T s = static_cast<T>(c_val3[q][a]) * S.rb[pq][c];
-              s += K1 * (static_cast<T>(c_grd3[q][a][0]) * S.ih[cl][0] * S.gA[pq][0][c] +
-                         static_cast<T>(c_grd3[q][a][1]) * S.ih[cl][1] * S.gA[pq][1][c] +
-                         static_cast<T>(c_grd3[q][a][2]) * S.ih[cl][2] * S.gA[pq][2][c]);
-              s += K23 * static_cast<T>(c_grd3[q][a][jc]) * S.ih[cl][jc] * S.dv[pq][pm];
+              T s = Tab<T>::val(q, a) * S.rb[pq][c];
+              s += K1 * (Tab<T>::grd(q, a, 0) * S.ih[cl][0] * S.gA[pq][0][c] +
+                         Tab<T>::grd(q, a, 1) * S.ih[cl][1] * S.gA[pq][1][c] +
+                         Tab<T>::grd(q, a, 2) * S.ih[cl][2] * S.gA[pq][2][c]);
+              s += K23 * Tab<T>::grd(q, a, jc) * S.ih[cl][jc] * S.dv[pq][pm];
               r += s;
             }
           r_cell[(e0 + cl) * 144 + a * 18 + c] = static_cast<double>(r * S.jxw[cl]);
@@ -440,7 +476,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
   int *s_col = reinterpret_cast<int *>(acc + static_cast<size_t>(m.max_row_blocks) * 324);
   uint32_t *s_cmask = reinterpret_cast<uint32_t *>(s_col + m.max_row_blocks);
   for (int i = tid; i < nb * 324; i += kRowThreads) acc[i] = T(0);
-  for (int i = tid; i < 576; i += kRowThreads) sD[i] = static_cast<T>((&c_D3[0][0][0])[i]);
+  for (int i = tid; i < 576; i += kRowThreads) sD[i] = Tab<T>::D()[i];
   for (int i = tid; i < nb; i += kRowThreads)
     {
       const int col = m.cols[r0 + i];
@@ -461,7 +497,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
         {
           s_cell[i] = m.rc_cell[kb + i];
           s_a[i] = m.rc_a[kb + i];
-          s_w[i] = static_cast<T>(m.rc_w[kb + i]);
+          s_w[i] = Tab<T>::w(m, kb + i);
         }
       for (int i = tid; i < nk * 8; i += kRowThreads) s_slot[i] = m.rc_slot[static_cast<int64_t>(kb) * 8 + i];
       __syncthreads();
@@ -474,10 +510,10 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
 #pragma unroll
           for (int q = 0; q < 8; ++q) hq[q] = act ? __ldg(H + (e * 8 + q) * kNS3 + tid) : T(0);
           const int inst = m.cell_inst[e];
-          const T K1 = static_cast<T>(m.coef[inst * kCoef + 0]), K23 = static_cast<T>(m.coef[inst * kCoef + 1]);
-          const double hx = m.cell_h[3 * e], hy = m.cell_h[3 * e + 1], hz = m.cell_h[3 * e + 2];
-          const T vol = static_cast<T>(hx * hy * hz);
-          const T i0 = static_cast<T>(1.0 / hx), i1 = static_cast<T>(1.0 / hy), i2 = static_cast<T>(1.0 / hz);
+          const T K1 = Tab<T>::coef(m, inst, 0), K23 = Tab<T>::coef(m, inst, 1);
+          const auto g = Tab<T>::geo(m, e);
+          const T vol = g.w;
+          const T i0 = g.x, i1 = g.y, i2 = g.z;
           const T ihc = jc == 0 ? i0 : (jc == 1 ? i1 : i2);
           const T ihd = jd == 0 ? i0 : (jd == 1 ? i1 : i2);
           const T kd = K1 * vol;
@@ -488,7 +524,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
             {
               T bulk = 0;
 #pragma unroll
-              for (int q = 0; q < 8; ++q) bulk += static_cast<T>(c_S3[a][b][q]) * hq[q];
+              for (int q = 0; q < 8; ++q) bulk += Tab<T>::S(a, b, q) * hq[q];
               bulk *= vol;
               const T *D = sD + (a * 8 + b) * 9;
               T gcd = 0, gdc = 0;
@@ -514,7 +550,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
                   for (int j = 0; j < cnt; ++j)
                     if (act)
                       {
-                        const T w = wa * static_cast<T>(t.w[j]);
+                        const T w = wa * static_cast<T>(t.w[j]); // hanging rows only: rare
                         acc[t.slot[j] * 324 + c * 18 + d] += w * (bulk + gcd);
                         if (c != d) acc[t.slot[j] * 324 + d * 18 + c] += w * (bulk + gdc);
                       }

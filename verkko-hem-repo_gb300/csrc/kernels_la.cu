@@ -8,6 +8,7 @@
 // CTA per segment.  Reductions are two-pass (per-segment partials, then an ordered
 // per-instance sum), so results are deterministic run to run.
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "device.h"
@@ -159,7 +160,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T *__restrict__ vals,
                                                               T *__restrict__ dinv)
 {
-  __shared__ double M[kBjWarps][18][37];
+  __shared__ T M[kBjWarps][18][37];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kBjWarps + warp;
   if (n >= m.nn) return;
@@ -167,18 +168,18 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
   for (int i = lane; i < 18 * 36; i += 32)
     {
       const int r = i / 36, c = i % 36;
-      M[warp][r][c] = (c < 18) ? static_cast<double>(D[r * 18 + c]) : ((c - 18 == r) ? 1.0 : 0.0);
+      M[warp][r][c] = (c < 18) ? D[r * 18 + c] : ((c - 18 == r) ? T(1) : T(0));
     }
   __syncwarp();
   bool singular = false;
   for (int k = 0; k < 18; ++k)
     {
-      double best = (lane >= k && lane < 18) ? fabs(M[warp][lane][k]) : -1.0;
+      T best = (lane >= k && lane < 18) ? fabs(M[warp][lane][k]) : T(-1);
       int bi = lane;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1)
         {
-          const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const T ob = __shfl_xor_sync(0xffffffffu, best, off);
           const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
           if (ob > best || (ob == best && oi < bi))
             {
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
               bi = oi;
             }
         }
-      if (!(best > 1e-300))
+      if (!(best > (sizeof(T) == 4 ? T(1e-30) : T(1e-300))))
         {
           singular = true;
           break;
@@ -194,22 +195,22 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
       if (bi != k)
         for (int c = lane; c < 36; c += 32)
           {
-            const double t = M[warp][k][c];
+            const T t = M[warp][k][c];
             M[warp][k][c] = M[warp][bi][c];
             M[warp][bi][c] = t;
           }
       __syncwarp();
-      const double piv = M[warp][k][k];
+      const T piv = M[warp][k][k];
       __syncwarp();
       for (int c = lane; c < 36; c += 32) M[warp][k][c] /= piv;
       __syncwarp();
-      double f[18];
+      T f[18];
 #pragma unroll
       for (int r = 0; r < 18; ++r) f[r] = M[warp][r][k];
       __syncwarp();
       for (int c = lane; c < 36; c += 32)
         {
-          const double pk = M[warp][k][c];
+          const T pk = M[warp][k][c];
 #pragma unroll
           for (int r = 0; r < 18; ++r)
             if (r != k) M[warp][r][c] -= f[r] * pk;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
   for (int i = lane; i < 324; i += 32)
     {
       const int r = i / 18, c = i % 18;
-      out[i] = singular ? static_cast<T>(r == c ? 1.0 : 0.0) : static_cast<T>(M[warp][r][18 + c]);
+      out[i] = singular ? T(r == c ? 1 : 0) : M[warp][r][18 + c];
     }
 }
 
@@ -461,38 +462,93 @@ cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nve
   return cudaGetLastError();
 }
 
+// y_seg -= sum_v coef[inst][v] X[v]_seg (arithmetic in T), then, in the same pass,
+// the partial dots of the updated y_seg with X[0..nvec2) and with itself: the second
+// Gram-Schmidt projection and the norm of the new basis vector need no extra read of y.
 template <typename T>
-__global__ void __launch_bounds__(kSegThreads) k_seg_maxpy(DevMesh m, const T *__restrict__ X, int64_t ld, int nvec,
-                                                           const double *__restrict__ coef, int ldc, T *__restrict__ y,
-                                                           const uint8_t *__restrict__ act)
+__global__ void __launch_bounds__(kSegThreads) k_seg_update(DevMesh m, const T *__restrict__ X, int64_t ld, int nvec,
+                                                            const double *__restrict__ coef, int ldc,
+                                                            T *__restrict__ y, int nvec2, double *__restrict__ partial2,
+                                                            double *__restrict__ partial_norm,
+                                                            const uint8_t *__restrict__ act)
 {
-  __shared__ double cf[64];
+  __shared__ T cf[64];
+  __shared__ T ys[kSegMax];
   const int s = blockIdx.x;
   const int inst = m.seg_inst[s];
-  if (act && !act[inst]) return;
-  for (int v = threadIdx.x; v < nvec; v += kSegThreads) cf[v] = coef[inst * ldc + v];
+  const bool on = !act || act[inst];
+  const int64_t b = m.seg_begin[s];
+  const int len = static_cast<int>(m.seg_end[s] - b);
+  for (int v = threadIdx.x; v < nvec; v += kSegThreads) cf[v] = on ? static_cast<T>(coef[inst * ldc + v]) : T(0);
   __syncthreads();
-  const int64_t b = m.seg_begin[s], e = m.seg_end[s];
-  for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads)
+  if (on)
+    for (int i = threadIdx.x; i < len; i += kSegThreads)
+      {
+        T acc = y[b + i];
+        const T *xp = X + b + i;
+        int v = 0;
+        for (; v + 4 <= nvec; v += 4)
+          {
+            const T x0 = xp[(v + 0) * ld], x1 = xp[(v + 1) * ld], x2 = xp[(v + 2) * ld], x3 = xp[(v + 3) * ld];
+            acc -= cf[v] * x0;
+            acc -= cf[v + 1] * x1;
+            acc -= cf[v + 2] * x2;
+            acc -= cf[v + 3] * x3;
+          }
+        for (; v < nvec; ++v) acc -= cf[v] * xp[v * ld];
+        y[b + i] = acc;
+        ys[i] = acc;
+      }
+  if (nvec2 <= 0 && !partial_norm) return;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntot = nvec2 + (partial_norm ? 1 : 0);
+  for (int v = warp; v < ntot; v += kSegThreads / 32)
     {
-      double acc = static_cast<double>(y[i]);
-      for (int v = 0; v < nvec; ++v)
-        if (cf[v] != 0.0) acc -= cf[v] * static_cast<double>(X[v * ld + i]); // unused columns may hold stale data
-      y[i] = static_cast<T>(acc);
+      T a0 = 0, a1 = 0;
+      if (on)
+        {
+          const T *xv = (v < nvec2) ? X + v * ld + b : nullptr;
+          int i = lane;
+          for (; i + 32 < len; i += 64)
+            {
+              const T y0 = ys[i], y1 = ys[i + 32];
+              a0 += (xv ? xv[i] : y0) * y0;
+              a1 += (xv ? xv[i + 32] : y1) * y1;
+            }
+          if (i < len) a0 += (xv ? xv[i] : ys[i]) * ys[i];
+        }
+      double acc = static_cast<double>(a0) + static_cast<double>(a1);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (lane == 0)
+        {
+          if (v < nvec2)
+            partial2[static_cast<int64_t>(s) * nvec2 + v] = acc;
+          else
+            partial_norm[s] = acc;
+        }
     }
+}
+
+cudaError_t launch_seg_update(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
+                              int ldc, void *y, int nvec2, double *partial2, double *partial_norm, const uint8_t *act,
+                              cudaStream_t s)
+{
+  if (nvec > 64) return cudaErrorInvalidValue;
+  if (fp32)
+    k_seg_update<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec, coef, ldc,
+                                                        static_cast<float *>(y), nvec2, partial2, partial_norm, act);
+  else
+    k_seg_update<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec, coef, ldc,
+                                                         static_cast<double *>(y), nvec2, partial2, partial_norm, act);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_seg_maxpy(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const double *coef,
                              int ldc, void *y, const uint8_t *act, cudaStream_t s)
 {
-  if (nvec > 64) return cudaErrorInvalidValue;
-  if (fp32)
-    k_seg_maxpy<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec, coef, ldc,
-                                                       static_cast<float *>(y), act);
-  else
-    k_seg_maxpy<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec, coef, ldc,
-                                                        static_cast<double *>(y), act);
-  return cudaGetLastError();
+  return launch_seg_update(m, fp32, X, ld, nvec, coef, ldc, y, 0, nullptr, nullptr, act, s);
 }
 
 template <typename TX, typename TY, typename TZ>
@@ -507,11 +563,14 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_axpby(DevMesh m, const TX *
   const double b = k.b ? k.b[inst * k.sb] : k.b0;
   const double c = k.c ? k.c[inst * k.sc] : k.c0;
   const int64_t b0 = m.seg_begin[s], e = m.seg_end[s];
+  // arithmetic in FP32 when every operand is FP32, else FP64
+  using C = typename std::conditional<(sizeof(TX) == 4 && sizeof(TY) == 4 && sizeof(TZ) == 4), float, double>::type;
+  const C ca = static_cast<C>(a), cb = static_cast<C>(b), cc = static_cast<C>(c);
   for (int64_t i = b0 + threadIdx.x; i < e; i += kSegThreads)
     {
-      double v = (a != 0.0 && x) ? a * static_cast<double>(x[i]) : 0.0;
-      if (b != 0.0) v += b * static_cast<double>(y[i]);
-      if (z && c != 0.0) v += c * static_cast<double>(z[i]);
+      C v = (a != 0.0 && x) ? ca * static_cast<C>(x[i]) : C(0);
+      if (b != 0.0) v += cb * static_cast<C>(y[i]);
+      if (z && c != 0.0) v += cc * static_cast<C>(z[i]);
       y[i] = static_cast<TY>(v);
     }
 }
