@@ -33,6 +33,9 @@ sys.path.insert(0, ROOT)
 
 P_BAR, T_RED, HALF, NCELL, NOISE, SEED = 20.0, 0.6, 10.0, 32, 0.05, 2
 TOL = 1e-10
+# DRAM bytes (read + write) of one k_spmv18<float> launch on this workload, from the ncu
+# capture summarised in profiles/k_spmv18_fp32_cube32.md (1.193182 GB + 5.481728 MB)
+SPMV_NCU_TRAFFIC = 1.193182e9 + 5.481728e6
 METRIC = "GL solves/s at ||F||<1e-10 (femgl 3D, 32^3 Q1, T=0.6Tc, p=20bar)"
 WORKLOAD = "femgl 3D cube L=20, 32^3 Q1 cells, matep(p=20 bar, t=0.6, SCC), z-face pair breaking, B-phase+0.05N(0,1) seed 2"
 
@@ -94,6 +97,66 @@ def problem(gl):
 def solve_once(f, x0, linear_tol):
     f.set_solution(x0)
     return f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+
+
+def batch_instances(gl, count, seed=4):
+    """Seeded sample of the batched phase-diagram sweep: T/Tc ~ U(0.3, 0.95),
+    p ~ U(0, 34) bar (kept below 34, where the coefficient tables end), slab thickness
+    D ~ U(8, 40) xi0 across z (pair-breaking faces), lateral 20 xi0, n^3 Q1 cells with
+    n ~ U{16..48}; start = B phase + 0.05 N(0,1)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        t = float(rng.uniform(0.3, 0.95))
+        p = float(min(rng.uniform(0.0, 34.0), 34.0 - 1e-9))
+        D = float(rng.uniform(8.0, 40.0))
+        n = int(rng.integers(16, 49))
+        m = gl.box_mesh([-10.0, -10.0, -D / 2], [10.0, 10.0, D / 2], (n, n, n))
+        x0 = gl.bphase_guess(p, t, m.nn, noise=NOISE, seed=1000 + k)
+        out.append({"t": t, "p": p, "D": D, "n": n, "mesh": m, "x0": x0})
+    return out
+
+
+def batched_leg(gl, count, linear_tol):
+    """Batched mixed solve of `count` instances in one context vs the plain FP64 GPU
+    Newton solving them one at a time; both to ||F|| < 1e-10 per instance."""
+    inst = batch_instances(gl, count)
+    meshes = [d["mesh"] for d in inst]
+    x0 = np.concatenate([d["x0"] for d in inst])
+    prm_m = [gl.Params.from_matep(d["p"], d["t"], precision=gl.MIXED) for d in inst]
+    f = gl.FemGL(meshes, prm_m)
+    f.set_solution(x0)
+    f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)  # warm-up
+    f.set_solution(x0)
+    f.sync()
+    f.event_start()
+    out = f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+    ms_batch = f.event_stop()
+    F_b = f.free_energy()
+    f.close()
+    ms_seq = 0.0
+    F_s = []
+    its_s = []
+    for d in inst:
+        prm = gl.Params.from_matep(d["p"], d["t"], precision=gl.FP64)
+        g = gl.FemGL(d["mesh"], prm)
+        g.set_solution(d["x0"])
+        g.sync()
+        g.event_start()
+        o = g.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+        ms_seq += g.event_stop()
+        F_s.append(g.free_energy()[0])
+        its_s.append(int(o["newton_its"][0]))
+        g.close()
+    F_s = np.array(F_s)
+    return {"instances": count, "total_dofs": int(sum(18 * m.nn for m in meshes)),
+            "mixed_batched_solves_per_s": count / (ms_batch / 1000.0),
+            "fp64_sequential_solves_per_s": count / (ms_seq / 1000.0),
+            "speedup": ms_seq / ms_batch, "all_converged": bool(out["converged"]),
+            "max_final_residual": float(out["residual"].max()),
+            "max_free_energy_rel_diff_vs_fp64": float(np.max(np.abs(F_b - F_s) / np.abs(F_s))),
+            "newton_its_batched": out["newton_its"].tolist(), "newton_its_fp64": its_s,
+            "sample": "seeded (seed 4) instances of the sweep: T/Tc~U(0.3,0.95), p~U(0,34), D~U(8,40), n~U{16..48}"}
 
 
 def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None):
@@ -185,10 +248,17 @@ def main():
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: one mixed assembly + 30 GMRES iterations on an N^3 cube, no timing")
     ap.add_argument("--fp64", action="store_true", help="with --ncu-case: FP64 instead of mixed")
+    ap.add_argument("--batch", type=int, default=8, help="instances in the batched leg (0 = skip)")
+    ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.ncu_case:
         return ncu_case(args.ncu_case, args.fp64)
+    if args.config3:
+        gl = importlib.import_module("verkko-hem-repo_gb300")
+        gl.build()
+        print(json.dumps({"config3": config3_leg(gl, args.linear_tol)}))
+        return 0
     if args.impl == "reference":
         return reference_arm(args, rank)
     gl = importlib.import_module("verkko-hem-repo_gb300")
@@ -221,6 +291,7 @@ def main():
         mixed = time_mode(gl, m, x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
                           flush=flush)
     e2e_val, x_e2e = e2e_mode(gl, m, x0, gl.MIXED, max(1, args.steps), args.linear_tol)
+    batched = batched_leg(gl, args.batch, args.linear_tol) if args.batch > 0 else None
 
     ms_step = float(np.mean(mixed["ms"]))
     value = 1000.0 / ms_step
@@ -263,17 +334,45 @@ def main():
         "kernel_launches": mixed["kernel_n"],
         "gpu_launches": int(mixed["launches"]),
         "roofline": {"bound": "hbm", "kernel": "k_spmv18<float>", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None, "traffic": SPMV_NCU_TRAFFIC,
+                     "traffic_source": "dram read+write of one k_spmv18<float> launch, ncu capture summarised in "
+                                       "profiles/k_spmv18_fp32_cube32.md",
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
                      "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms,
                      "assembly_algorithmic_bytes": asm_bytes},
         "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": nd * 8, "d2h_bytes_per_step": nd * 8},
         "clocks": clk.summary(),
+        "batched": batched,
     }
     try:
         line["cpu_baseline"] = cpu_port_baseline(m, x0, args.linear_tol)
     except Exception as e:  # the CPU baseline must not hide the GPU line
         line["cpu_baseline"] = {"value": None, "error": str(e)}
     print(json.dumps(line))
+
+
+def config3_leg(gl, linear_tol):
+    """Mixed-precision solve of the refined cube: 64^3 Q1 on the same L = 20 cube, cells
+    within 0.1 L of a z face refined once (hanging nodes on two interface planes),
+    against the FP64 GPU Newton on the same mesh and start."""
+    m = gl.cube_mesh(HALF, 64, 0.1)
+    x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
+    res = {"n_nodes": m.nn, "n_dofs": 18 * m.nn, "n_hanging": m.n_hanging, "n_cells": m.nc}
+    for name, prec in (("mixed", gl.MIXED), ("fp64", gl.FP64)):
+        f = gl.FemGL(m, gl.Params.from_matep(P_BAR, T_RED, precision=prec))
+        f.set_solution(x0)
+        f.sync()
+        f.event_start()
+        o = f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL, allow_unconverged=True)
+        ms = f.event_stop()
+        F = float(f.free_energy()[0])
+        res[name] = {"ms": ms, "newton_its": int(o["newton_its"][0]), "gmres_its": int(o["gmres_its"][0]),
+                     "final_residual": float(o["residual"][0]), "converged": bool(o["converged"]), "F": F,
+                     "phases_ms": f.timers()}
+        f.close()
+    res["free_energy_rel_diff"] = abs(res["mixed"]["F"] - res["fp64"]["F"]) / abs(res["fp64"]["F"])
+    res["mixed_vs_fp64"] = res["fp64"]["ms"] / res["mixed"]["ms"]
+    return res
 
 
 def ncu_case(n, fp64):

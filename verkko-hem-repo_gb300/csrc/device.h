@@ -121,6 +121,15 @@ struct GmresDev
   uint8_t *active;       // [n_inst] still iterating in this cycle
   double *inv_scale;     // [n_inst] 1/h_{j+1,j} (0 on breakdown)
 };
+// Arnoldi step kernels with in-kernel per-instance finalisation (cnt: per-instance
+// ticket counters, zero between launches)
+cudaError_t launch_arnoldi_dot(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const void *w,
+                               double *partial, double *hout, int ldh, unsigned int *cnt, const uint8_t *act,
+                               cudaStream_t s);
+cudaError_t launch_arnoldi_update(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, void *w, int mode,
+                                  int j, double *partial, const GmresDev &g, unsigned int *cnt, cudaStream_t s);
+cudaError_t launch_bj_apply_scale(const DevMesh &m, bool fp32, const void *dinv, void *x, void *y,
+                                  const double *scale, const uint8_t *act, cudaStream_t s);
 cudaError_t launch_gmres_start(const GmresDev &g, int n_inst, const uint8_t *solve_active, cudaStream_t s);
 cudaError_t launch_gmres_column(const GmresDev &g, int n_inst, int j, cudaStream_t s);
 cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);

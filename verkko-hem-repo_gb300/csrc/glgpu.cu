@@ -86,6 +86,7 @@ struct glgpu_ctx
   // per-instance small arrays (device)
   double *d_norm = nullptr, *d_a = nullptr, *d_energy = nullptr, *d_cheb = nullptr, *d_tmp = nullptr;
   uint8_t *d_act = nullptr, *d_act2 = nullptr;
+  unsigned int *d_cnt = nullptr; // per-instance tickets of the in-kernel reductions
   // pinned host mirrors
   double *h_norm = nullptr, *h_res = nullptr;
   uint8_t *h_act = nullptr, *h_act_pipe = nullptr;
@@ -489,31 +490,56 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
         {
           void *Vj = tptr(c, c->V, static_cast<int64_t>(j) * N);
           void *Vj1 = tptr(c, c->V, static_cast<int64_t>(j + 1) * N);
-          CKS(precond(c, Vj, c->Z, c->g.active));
+          // fused path: the normalisation of V_j is folded into the block-Jacobi pass and
+          // the Gram-Schmidt finalisation and Givens update run inside the reductions
+          const bool fused = c->B == 18 && c->prm[0].precond == GLGPU_PC_BLOCK_JACOBI;
+          if (fused)
+            {
+              const double *sc = (j == 0) ? nullptr : c->g.inv_scale;
+              CKS(launch(c, KK_PREC, 1, [&] {
+                return launch_bj_apply_scale(c->dm, m32, c->dinv, Vj, c->Z, sc, c->g.active, c->st);
+              }));
+            }
+          else
+            CKS(precond(c, Vj, c->Z, c->g.active));
           CKS(spmv(c, c->Z, Vj1, c->g.active));
-          // classical Gram-Schmidt with one reorthogonalization; the second projection
-          // and the norm come out of the update passes (3 reads of the basis, not 4)
-          CKS(launch(c, KK_VEC, 1, [&] {
-            return launch_seg_mdot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.active, c->st);
-          }));
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol, mr + 2, 0, c->st); }));
-          CKS(launch(c, KK_VEC, 1, [&] {
-            return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol, mr + 2, Vj1, j + 1, c->partial, nullptr,
-                                     c->g.active, c->st);
-          }));
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol2, mr + 2, 0, c->st); }));
-          CKS(launch(c, KK_VEC, 1, [&] {
-            return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol2, mr + 2, Vj1, 0, nullptr, c->partial_n,
-                                     c->g.active, c->st);
-          }));
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial_n, 1, c->g.hcol + j + 1, mr + 2, 1, c->st); }));
-          CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_column(c->g, n, j, c->st); }));
-          {
-            Axpby k{};
-            k.a = c->g.inv_scale;
-            k.sa = 1;
-            CKS(axpby(c, Vj1, Vj1, nullptr, k, c->g.active, m32, m32, m32));
-          }
+          if (fused)
+            {
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_arnoldi_dot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.hcol, mr + 2, c->d_cnt,
+                                          c->g.active, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 1, j, c->partial, c->g, c->d_cnt, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 2, j, c->partial, c->g, c->d_cnt, c->st);
+              }));
+            }
+          else
+            {
+              // classical Gram-Schmidt with one reorthogonalization; the second projection
+              // and the norm come out of the update passes (3 reads of the basis, not 4)
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_seg_mdot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.active, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol, mr + 2, 0, c->st); }));
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol, mr + 2, Vj1, j + 1, c->partial, nullptr,
+                                         c->g.active, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, j + 1, c->g.hcol2, mr + 2, 0, c->st); }));
+              CKS(launch(c, KK_VEC, 1, [&] {
+                return launch_seg_update(c->dm, m32, c->V, N, j + 1, c->g.hcol2, mr + 2, Vj1, 0, nullptr, c->partial_n,
+                                         c->g.active, c->st);
+              }));
+              CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial_n, 1, c->g.hcol + j + 1, mr + 2, 1, c->st); }));
+              CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_column(c->g, n, j, c->st); }));
+              Axpby k{};
+              k.a = c->g.inv_scale;
+              k.sa = 1;
+              CKS(axpby(c, Vj1, Vj1, nullptr, k, c->g.active, m32, m32, m32));
+            }
           jdone = j + 1;
           // step j's flags are copied out and checked only after step j+1 is enqueued,
           // so the host round trip overlaps device work; instances that stopped are
@@ -758,8 +784,10 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = dalloc(c, &c->d_a, n_inst)) || (s = dalloc(c, &c->d_energy, n_inst)) ||
       (s = dalloc(c, &c->d_tmp, n_inst)) ||
       (s = dalloc(c, &c->d_cheb, static_cast<size_t>(n_inst) * 2 * (deg + 1))) || (s = dalloc(c, &c->d_act, n_inst)) ||
-      (s = dalloc(c, &c->d_act2, n_inst)))
+      (s = dalloc(c, &c->d_act2, n_inst)) || (s = dalloc(c, &c->d_cnt, n_inst)))
     return fail(s);
+  if (cudaMemset(c->d_cnt, 0, sizeof(unsigned int) * n_inst) != cudaSuccess)
+    return fail(set_error(GLGPU_ERR_CUDA, "glgpu_create: counter initialisation failed"));
   c->g.m = mr;
   if (cudaMallocHost(&c->h_norm, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||
       cudaMallocHost(&c->h_res, sizeof(double) * std::max(n_inst, 2 * n_inst * (deg + 1))) != cudaSuccess ||

@@ -802,3 +802,311 @@ cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s)
 }
 
 } // namespace glgpu
+
+namespace glgpu
+{
+// =================================================================================
+// Arnoldi step kernels with in-kernel finalization.
+//
+// Every CTA writes its per-segment partial sums, then takes a ticket on a per-instance
+// counter (atomicAdd after __threadfence).  The CTA that draws the last ticket of its
+// instance sums all partials of the instance in segment order (fixed shuffle tree, so
+// results are deterministic), writes the per-instance result and resets the counter.
+// Nothing waits on another CTA: the last CTA only runs after every other CTA of the
+// instance has published its partials.
+// =================================================================================
+__device__ __forceinline__ bool take_last_ticket(unsigned int *cnt, int inst, int nseg_inst)
+{
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0)
+    {
+      const unsigned int t = atomicAdd(cnt + inst, 1u);
+      s_last = (t == static_cast<unsigned int>(nseg_inst - 1));
+    }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// sum partial[g][v] over the instance's segments for v < nv into out[v] (one warp per v)
+__device__ __forceinline__ void instance_sums(const DevMesh &m, int inst, const double *partial, int nv, double *out,
+                                              int take_sqrt)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g0 = m.inst_seg_off[inst], g1 = m.inst_seg_off[inst + 1];
+  for (int v = warp; v < nv; v += kSegThreads / 32)
+    {
+      double s = 0.0;
+      for (int g = g0 + lane; g < g1; g += 32) s += __ldcg(partial + static_cast<int64_t>(g) * nv + v);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) out[v] = take_sqrt ? sqrt(s) : s;
+    }
+}
+
+// h[inst][0..nvec) = V[0..nvec)^T w
+template <typename T>
+__global__ void __launch_bounds__(kSegThreads) k_arnoldi_dot(DevMesh m, const T *__restrict__ X, int64_t ld, int nvec,
+                                                             const T *__restrict__ w, double *__restrict__ partial,
+                                                             double *__restrict__ hout, int ldh,
+                                                             unsigned int *__restrict__ cnt,
+                                                             const uint8_t *__restrict__ act)
+{
+  __shared__ T ys[kSegMax];
+  const int s = blockIdx.x;
+  const int inst = m.seg_inst[s];
+  if (act && !act[inst]) return;
+  const int64_t b = m.seg_begin[s];
+  const int len = static_cast<int>(m.seg_end[s] - b);
+  for (int i = threadIdx.x; i < len; i += kSegThreads) ys[i] = w[b + i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int v = warp; v < nvec; v += kSegThreads / 32)
+    {
+      const T *xv = X + v * ld + b;
+      T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+      int i = lane;
+      for (; i + 96 < len; i += 128)
+        {
+          a0 += xv[i] * ys[i];
+          a1 += xv[i + 32] * ys[i + 32];
+          a2 += xv[i + 64] * ys[i + 64];
+          a3 += xv[i + 96] * ys[i + 96];
+        }
+      for (; i < len; i += 32) a0 += xv[i] * ys[i];
+      double acc = static_cast<double>(a0) + static_cast<double>(a1) + static_cast<double>(a2) + static_cast<double>(a3);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (lane == 0) partial[static_cast<int64_t>(s) * nvec + v] = acc;
+    }
+  const int nseg = m.inst_seg_off[inst + 1] - m.inst_seg_off[inst];
+  if (take_last_ticket(cnt, inst, nseg))
+    {
+      instance_sums(m, inst, partial, nvec, hout + inst * ldh, 0);
+      if (threadIdx.x == 0) cnt[inst] = 0u;
+    }
+}
+
+// Givens update of column j for one instance (same arithmetic as k_gmres_column)
+__device__ void givens_column(GmresDev &g, int k, int j)
+{
+  const int m = g.m;
+  double *h = g.hcol + k * (m + 2);
+  const double *h2 = g.hcol2 + k * (m + 2);
+  double col[64 + 2];
+  for (int i = 0; i <= j; ++i) col[i] = h[i] + h2[i];
+  col[j + 1] = h[j + 1];
+  double *cs = g.cs + k * m, *sn = g.sn + k * m, *gg = g.g + k * (m + 1);
+  for (int i = 0; i < j; ++i)
+    {
+      const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+      col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+      col[i] = t;
+    }
+  const double a = col[j], b = col[j + 1];
+  const double r = hypot(a, b);
+  double c1 = 1.0, s1 = 0.0;
+  if (r > 0.0)
+    {
+      c1 = a / r;
+      s1 = b / r;
+    }
+  cs[j] = c1;
+  sn[j] = s1;
+  col[j] = r;
+  gg[j + 1] = -s1 * gg[j];
+  gg[j] = c1 * gg[j];
+  double *Hc = g.H + static_cast<int64_t>(k) * (m + 1) * m + static_cast<int64_t>(j) * (m + 1);
+  for (int i = 0; i <= j; ++i) Hc[i] = col[i];
+  const double nrm = h[j + 1];
+  g.inv_scale[k] = (nrm > 0.0 && isfinite(nrm)) ? 1.0 / nrm : 0.0;
+  g.its[k] = j + 1;
+  const double est = fabs(gg[j + 1]);
+  g.res_est[k] = est;
+  if (!(est > g.tol[k]) || !(nrm > 0.0) || !isfinite(est)) g.active[k] = 0;
+}
+
+// w -= V h (h = hcol or hcol2 of the instance); then
+//   mode 1: hcol2 = V^T w                     (second Gram-Schmidt projection)
+//   mode 2: hcol[j+1] = |w|, then the Givens update of column j
+template <typename T>
+__global__ void __launch_bounds__(kSegThreads) k_arnoldi_update(DevMesh m, const T *__restrict__ X, int64_t ld,
+                                                                int nvec, T *__restrict__ w, int mode, int j,
+                                                                double *__restrict__ partial, GmresDev g,
+                                                                unsigned int *__restrict__ cnt)
+{
+  __shared__ T cf[64];
+  __shared__ T ys[kSegMax];
+  const int s = blockIdx.x;
+  const int inst = m.seg_inst[s];
+  if (!g.active[inst]) return;
+  const int mr = g.m;
+  const double *h = (mode == 1 ? g.hcol : g.hcol2) + inst * (mr + 2);
+  for (int v = threadIdx.x; v < nvec; v += kSegThreads) cf[v] = static_cast<T>(__ldcg(h + v));
+  __syncthreads();
+  const int64_t b = m.seg_begin[s];
+  const int len = static_cast<int>(m.seg_end[s] - b);
+  // update: four elements per thread in flight, basis vectors in the outer loop
+  for (int i0 = threadIdx.x; i0 < len; i0 += 4 * kSegThreads)
+    {
+      T acc[4];
+      const T *xp = X + b;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        {
+          const int i = i0 + u * kSegThreads;
+          acc[u] = (i < len) ? w[b + i] : T(0);
+        }
+      for (int v = 0; v < nvec; ++v)
+        {
+          const T c = cf[v];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            {
+              const int i = i0 + u * kSegThreads;
+              if (i < len) acc[u] -= c * xp[v * ld + i];
+            }
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        {
+          const int i = i0 + u * kSegThreads;
+          if (i < len)
+            {
+              w[b + i] = acc[u];
+              ys[i] = acc[u];
+            }
+        }
+    }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nout = (mode == 1) ? nvec : 1;
+  for (int v = warp; v < nout; v += kSegThreads / 32)
+    {
+      const T *xv = (mode == 1) ? X + v * ld + b : nullptr;
+      T a0 = 0, a1 = 0;
+      int i = lane;
+      for (; i + 32 < len; i += 64)
+        {
+          a0 += (xv ? xv[i] : ys[i]) * ys[i];
+          a1 += (xv ? xv[i + 32] : ys[i + 32]) * ys[i + 32];
+        }
+      if (i < len) a0 += (xv ? xv[i] : ys[i]) * ys[i];
+      double acc = static_cast<double>(a0) + static_cast<double>(a1);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (lane == 0) partial[static_cast<int64_t>(s) * nout + v] = acc;
+    }
+  const int nseg = m.inst_seg_off[inst + 1] - m.inst_seg_off[inst];
+  if (take_last_ticket(cnt, inst, nseg))
+    {
+      if (mode == 1)
+        instance_sums(m, inst, partial, nvec, g.hcol2 + inst * (mr + 2), 0);
+      else
+        instance_sums(m, inst, partial, 1, g.hcol + inst * (mr + 2) + j + 1, 1);
+      __syncthreads();
+      if (threadIdx.x == 0)
+        {
+          cnt[inst] = 0u;
+          if (mode == 2)
+            {
+              __threadfence();
+              givens_column(g, inst, j);
+            }
+        }
+    }
+}
+
+// z = D^-1 (s v) and, when rescale is set, v <- s v, with s = scale[inst] (the
+// normalisation of the previous Arnoldi vector, folded into this pass)
+template <typename T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_bj_apply_scale18(DevMesh m, const T *__restrict__ dinv,
+                                                                      T *__restrict__ x, T *__restrict__ y,
+                                                                      const double *__restrict__ scale,
+                                                                      const uint8_t *__restrict__ act)
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  __shared__ T red[kSpmvWarps][324];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
+  if (n >= m.nn) return;
+  const int inst = m.node_inst[n];
+  if (act && !act[inst]) return;
+  const T sc = scale ? static_cast<T>(scale[inst]) : T(1);
+  T xv = (lane < 18) ? x[n * 18 + lane] * sc : T(0);
+  if (scale && lane < 18) x[n * 18 + lane] = xv;
+  const V *bp = reinterpret_cast<const V *>(dinv + n * 324);
+#pragma unroll
+  for (int it = 0; it < NIT; ++it)
+    {
+      const int ch = lane + 32 * it;
+      V wv;
+      if (ch < NCH)
+        wv = __ldg(bp + ch);
+      else
+        wv = V{};
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        {
+          const int e = (ch < NCH) ? ch * NV + v : 0;
+          const T xd = __shfl_sync(0xffffffffu, xv, e % 18);
+          if (ch < NCH) red[warp][e] = vget<V, T>(wv, v) * xd;
+        }
+    }
+  __syncwarp();
+  if (lane < 18)
+    {
+      T s = 0;
+#pragma unroll
+      for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
+      y[n * 18 + lane] = s;
+    }
+}
+
+cudaError_t launch_arnoldi_dot(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, const void *w,
+                               double *partial, double *hout, int ldh, unsigned int *cnt, const uint8_t *act,
+                               cudaStream_t s)
+{
+  if (fp32)
+    k_arnoldi_dot<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+                                                         static_cast<const float *>(w), partial, hout, ldh, cnt, act);
+  else
+    k_arnoldi_dot<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+                                                          static_cast<const double *>(w), partial, hout, ldh, cnt, act);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_arnoldi_update(const DevMesh &m, bool fp32, const void *X, int64_t ld, int nvec, void *w, int mode,
+                                  int j, double *partial, const GmresDev &g, unsigned int *cnt, cudaStream_t s)
+{
+  if (nvec > 64 || g.m > 64) return cudaErrorInvalidValue;
+  if (fp32)
+    k_arnoldi_update<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+                                                            static_cast<float *>(w), mode, j, partial, g, cnt);
+  else
+    k_arnoldi_update<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+                                                             static_cast<double *>(w), mode, j, partial, g, cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bj_apply_scale(const DevMesh &m, bool fp32, const void *dinv, void *x, void *y,
+                                  const double *scale, const uint8_t *act, cudaStream_t s)
+{
+  if (m.B != 18) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
+  if (fp32)
+    k_bj_apply_scale18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(dinv),
+                                                               static_cast<float *>(x), static_cast<float *>(y), scale,
+                                                               act);
+  else
+    k_bj_apply_scale18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(dinv),
+                                                                static_cast<double *>(x), static_cast<double *>(y),
+                                                                scale, act);
+  return cudaGetLastError();
+}
+} // namespace glgpu
