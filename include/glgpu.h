@@ -262,6 +262,20 @@ glgpu_status glgpu_bphase_guess(double p, double t, int scc, int n_nodes, double
 glgpu_status glgpu_plan_info(const glgpu_mesh *mesh, int n_inst, int64_t *info);
 glgpu_status glgpu_plan_pattern(const glgpu_mesh *mesh, int n_inst, int32_t *rowptr, int32_t *cols);
 
+/*
+ * Deterministic FP64 dot product result[0] = sum_i x[i] * y[i] of two DEVICE vectors
+ * of length n, written to a DEVICE double, enqueued on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream).  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory where they need a norm (inside stream
+ * capture, in allocation-free loops, or when the host framework owns all device
+ * memory).  It allocates nothing: its partial sums live in a fixed per-device array
+ * of 16,384 doubles, so n <= 16,777,216 (larger n returns GLGPU_ERR_ARG).  The first
+ * call on a device looks up that array's address; make it before any stream capture.
+ * The array is shared by all calls and keeps the last call's partials; calls that
+ * overlap on the GPU race on it and must be serialised by the caller.
+ */
+glgpu_status glgpu_dot_noalloc(const double *x, const double *y, int64_t n, double *result, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

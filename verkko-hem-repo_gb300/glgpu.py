@@ -100,6 +100,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mesh_box.argtypes = [_dp, _dp, _ip, ctypes.c_double, _ip, _ip, _ip, _ip, _dp, _ip, _up, _ip, _ip, _dp]
     L.glgpu_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_uint64, _dp]
+    L.glgpu_dot_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
     L.glgpu_plan_info.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _lp]
     L.glgpu_plan_pattern.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _ip, _ip]
     _lib = L
