@@ -262,6 +262,34 @@ glgpu_status glgpu_bphase_guess(double p, double t, int scc, int n_nodes, double
 glgpu_status glgpu_plan_info(const glgpu_mesh *mesh, int n_inst, int64_t *info);
 glgpu_status glgpu_plan_pattern(const glgpu_mesh *mesh, int n_inst, int32_t *rowptr, int32_t *cols);
 
+/* ---------------------------------------------------------------------------
+ * Learned initial guess (no counterpart in the reference, which starts Newton from a
+ * uniform B phase, setup_uniform_B-phase.cc:238-259).  An MLP
+ *   (x, y, z, t = T/Tc, p [bar], D [xi0]) -> 256 -> 256 -> 256 -> 256 -> 18
+ * with SiLU hidden activations, BF16 weights/activations and FP32 accumulation on the
+ * tcgen05 tensor cores, FP32 master weights trained with Adam on converged states.
+ * Inputs are normalised as (input - shift) * scale.  Arrays are HOST memory:
+ * inputs [P][6], targets/outputs [P][18], parameters in layer order (W [out][in], b [out]).
+ * --------------------------------------------------------------------------- */
+typedef struct glgpu_surrogate glgpu_surrogate;
+
+glgpu_status glgpu_surrogate_create(uint64_t seed, glgpu_surrogate **out);
+glgpu_status glgpu_surrogate_destroy(glgpu_surrogate *s);
+glgpu_status glgpu_surrogate_set_normalization(glgpu_surrogate *s, const float *shift, const float *scale);
+glgpu_status glgpu_surrogate_param_count(int64_t *n);
+glgpu_status glgpu_surrogate_get_params(glgpu_surrogate *s, float *params);
+glgpu_status glgpu_surrogate_set_params(glgpu_surrogate *s, const float *params);
+/* outputs[P][18] = network(inputs[P][6]) */
+glgpu_status glgpu_surrogate_predict(glgpu_surrogate *s, const float *inputs, int P, float *outputs);
+/* loss = (1/2P) sum |y - target|^2 and its gradient (parameter order) for one batch, no update */
+glgpu_status glgpu_surrogate_gradient(glgpu_surrogate *s, const float *inputs, const float *targets, int P,
+                                      float *loss, float *grad);
+/* `steps` Adam steps on minibatches of `batch` rows (seeded shuffle); loss_out = mean loss
+ * of the last steps */
+glgpu_status glgpu_surrogate_train(glgpu_surrogate *s, const float *inputs, const float *targets, int n_rows,
+                                   int steps, int batch, float lr, uint64_t seed, float *loss_out);
+int64_t glgpu_surrogate_launch_count(const glgpu_surrogate *s);
+
 /*
  * Deterministic FP64 dot product result[0] = sum_i x[i] * y[i] of two DEVICE vectors
  * of length n, written to a DEVICE double, enqueued on `stream` (a cudaStream_t;

@@ -101,6 +101,19 @@ def lib() -> ctypes.CDLL:
     L.glgpu_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_uint64, _dp]
     L.glgpu_dot_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.glgpu_surrogate_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.glgpu_surrogate_destroy.argtypes = [vp]
+    L.glgpu_surrogate_set_normalization.argtypes = [vp, fp, fp]
+    L.glgpu_surrogate_param_count.argtypes = [_lp]
+    L.glgpu_surrogate_get_params.argtypes = [vp, fp]
+    L.glgpu_surrogate_set_params.argtypes = [vp, fp]
+    L.glgpu_surrogate_predict.argtypes = [vp, fp, ctypes.c_int, fp]
+    L.glgpu_surrogate_gradient.argtypes = [vp, fp, fp, ctypes.c_int, fp, fp]
+    L.glgpu_surrogate_train.argtypes = [vp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_uint64, fp]
+    L.glgpu_surrogate_launch_count.argtypes = [vp]
+    L.glgpu_surrogate_launch_count.restype = ctypes.c_int64
     L.glgpu_plan_info.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _lp]
     L.glgpu_plan_pattern.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _ip, _ip]
     _lib = L
@@ -419,3 +432,81 @@ class FemGL:
         ms = ctypes.c_double()
         _check(lib().glgpu_event_stop(self._ctx, ctypes.byref(ms)))
         return ms.value
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class Surrogate:
+    """The learned initial guess: an MLP (x, y, z, t, p, D) -> 256 x 4 (SiLU) -> 18 whose
+    dense layers run on the tcgen05 tensor cores in BF16 with FP32 accumulation."""
+
+    N_IN, N_OUT = 6, 18
+    LAYERS = ((6, 256), (256, 256), (256, 256), (256, 256), (256, 18))
+
+    def __init__(self, seed: int = 0):
+        self._s = ctypes.c_void_p()
+        _check(lib().glgpu_surrogate_create(int(seed), ctypes.byref(self._s)))
+        n = ctypes.c_int64()
+        _check(lib().glgpu_surrogate_param_count(ctypes.byref(n)))
+        self.n_params = n.value
+
+    def close(self):
+        if getattr(self, "_s", None) is not None and self._s.value:
+            lib().glgpu_surrogate_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_normalization(self, shift, scale):
+        sh = np.ascontiguousarray(shift, np.float32)
+        sc = np.ascontiguousarray(scale, np.float32)
+        _check(lib().glgpu_surrogate_set_normalization(self._s, _p(sh, _fp), _p(sc, _fp)))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        _check(lib().glgpu_surrogate_get_params(self._s, _p(p, _fp)))
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.n_params:
+            raise ValueError("wrong parameter count")
+        _check(lib().glgpu_surrogate_set_params(self._s, _p(p, _fp)))
+
+    def predict(self, inputs) -> np.ndarray:
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, self.N_IN)
+        y = np.zeros((x.shape[0], self.N_OUT), np.float32)
+        _check(lib().glgpu_surrogate_predict(self._s, _p(x, _fp), x.shape[0], _p(y, _fp)))
+        return y
+
+    def gradient(self, inputs, targets):
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, self.N_IN)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, self.N_OUT)
+        loss = ctypes.c_float()
+        g = np.zeros(self.n_params, np.float32)
+        _check(lib().glgpu_surrogate_gradient(self._s, _p(x, _fp), _p(t, _fp), x.shape[0], ctypes.byref(loss),
+                                              _p(g, _fp)))
+        return float(loss.value), g
+
+    def train(self, inputs, targets, steps: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> float:
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, self.N_IN)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, self.N_OUT)
+        loss = ctypes.c_float()
+        _check(lib().glgpu_surrogate_train(self._s, _p(x, _fp), _p(t, _fp), x.shape[0], int(steps), int(batch),
+                                           float(lr), int(seed), ctypes.byref(loss)))
+        return float(loss.value)
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib().glgpu_surrogate_launch_count(self._s))
