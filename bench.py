@@ -264,10 +264,22 @@ def main():
     ap.add_argument("--batch", type=int, default=8, help="instances in the batched leg (0 = skip)")
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
+    ap.add_argument("--ncu-mlp", type=int, default=0, help="profiling case: surrogate forward on N points + one gradient")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.ncu_case:
         return ncu_case(args.ncu_case, args.fp64)
+    if args.ncu_mlp:
+        gl = importlib.import_module("verkko-hem-repo_gb300")
+        gl.build()
+        rng = np.random.default_rng(0)
+        X = rng.uniform(-1, 1, (args.ncu_mlp, 6)).astype(np.float32)
+        with gl.Surrogate(seed=1) as sm:
+            y = sm.predict(X)
+            T = rng.standard_normal((min(args.ncu_mlp, 16384), 18)).astype(np.float32)
+            loss, _ = sm.gradient(X[: T.shape[0]], T)
+        print(json.dumps({"ncu_mlp": args.ncu_mlp, "out_norm": float(np.linalg.norm(y)), "loss": loss}))
+        return 0
     if args.config3:
         gl = importlib.import_module("verkko-hem-repo_gb300")
         gl.build()
