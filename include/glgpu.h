@@ -54,7 +54,9 @@ typedef enum
 {
   GLGPU_PC_NONE = 0,
   GLGPU_PC_BLOCK_JACOBI = 1,   /* inverse of each node's diagonal block */
-  GLGPU_PC_CHEBYSHEV = 2       /* Chebyshev polynomial in (block-Jacobi)^-1 J */
+  GLGPU_PC_CHEBYSHEV = 2,      /* Chebyshev polynomial in (block-Jacobi)^-1 J */
+  GLGPU_PC_MULTIGRID = 3       /* geometric V-cycle (uniform box meshes; others fall back to block-Jacobi),
+                                  flexible GMRES outside */
 } glgpu_precond;
 
 /*
@@ -96,6 +98,8 @@ typedef struct
   double ls_step;       /* "primary step length of dampped newton iteration", 0.83 */
   int ls_max_trials;    /* trials of the backtracking line search, 100 (iteration.cc:170) */
   int damped;           /* "Using dampped Newton iteration" (1) or full Newton (0) */
+  int mg_pre, mg_post;  /* multigrid: damped block-Jacobi sweeps before / after the coarse correction */
+  double mg_omega;      /* multigrid: smoother damping */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;
@@ -208,6 +212,10 @@ glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, 
 
 /* Number of kernels this context has launched since creation. */
 int64_t glgpu_launch_count(const glgpu_ctx *ctx);
+
+/* Coarse levels of the multigrid hierarchy (0 when the preconditioner is not multigrid
+ * or an instance is not a uniform box grid). */
+int glgpu_mg_levels(const glgpu_ctx *ctx);
 
 /* Blocks until all work of the context's stream is done. */
 glgpu_status glgpu_sync(glgpu_ctx *ctx);

@@ -48,6 +48,7 @@ struct DevMesh
   const int32_t *seg_inst;
   const int32_t *inst_seg_off;
   const int64_t *cell_off;    // [n_inst+1]
+  const int64_t *node_off_ptr; // [n_inst+1]
 };
 
 // ---- assembly (kernels_asm.cu) ----
@@ -135,5 +136,19 @@ cudaError_t launch_gmres_column(const GmresDev &g, int n_inst, int j, cudaStream
 cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);
 // scale factors for the new basis vector from the norm (inv_scale = 1/norm or 0)
 cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s);
+
+// ---- multigrid (kernels_mg.cu) ----
+cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
+                           const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
+                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s);
+cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
+                            const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
+                            const uint8_t *act, cudaStream_t s);
+cudaError_t launch_interp_state(int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const double *w,
+                                const double *xf, double *xc, cudaStream_t s);
+cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
+                               float *inv, int *singular, cudaStream_t s);
+cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,
+                               const void *r, void *z, const uint8_t *act, cudaStream_t s);
 
 } // namespace glgpu

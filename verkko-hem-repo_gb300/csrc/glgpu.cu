@@ -110,6 +110,22 @@ struct glgpu_ctx
   std::vector<EvRec> kev, pev;
   std::vector<cudaEvent_t> ev_pool;
   cudaEvent_t ev_user0 = nullptr, ev_user1 = nullptr;
+  // multigrid (precond == GLGPU_PC_MULTIGRID on uniform box meshes)
+  bool owns_stream = true;
+  int n_levels = 0;                 // coarse levels; lv[0] is the first coarse level
+  std::vector<glgpu_ctx *> lv;
+  struct Transfer
+  {
+    int32_t *p_ptr = nullptr, *p_idx = nullptr, *r_ptr = nullptr, *r_idx = nullptr, *q_ptr = nullptr, *q_idx = nullptr;
+    void *p_w = nullptr, *r_w = nullptr; // T weights
+    double *q_w = nullptr;
+  };
+  std::vector<Transfer> tr;          // tr[l]: level l (fine side) <-> level l+1
+  int64_t *d_dense_off = nullptr;
+  float *d_inv = nullptr;
+  int *d_sing = nullptr;
+  int max_nd = 0;
+  void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
 };
 
 namespace
@@ -437,6 +453,9 @@ glgpu_status prec_setup(glgpu_ctx *c)
   return GLGPU_OK;
 }
 
+glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act);
+glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act);
+
 // ---------------------------------------------------------------------------------
 // GMRES(m), right preconditioned, classical Gram-Schmidt with one reorthogonalization
 // ---------------------------------------------------------------------------------
@@ -491,18 +510,24 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
           void *Vj = tptr(c, c->V, static_cast<int64_t>(j) * N);
           void *Vj1 = tptr(c, c->V, static_cast<int64_t>(j + 1) * N);
           // fused path: the normalisation of V_j is folded into the block-Jacobi pass and
-          // the Gram-Schmidt finalisation and Givens update run inside the reductions
-          const bool fused = c->B == 18 && c->prm[0].precond == GLGPU_PC_BLOCK_JACOBI;
-          if (fused)
+          // the Gram-Schmidt finalisation and Givens update run inside the reductions.
+          // Multigrid (flexible GMRES): Z_j = V-cycle(V_j) is kept for the solution update.
+          const bool mg = c->n_levels > 0;
+          const bool fused_bj = !mg && c->B == 18 && c->prm[0].precond == GLGPU_PC_BLOCK_JACOBI;
+          const bool fused = fused_bj || mg;
+          void *Zj = mg ? tptr(c, c->Zb, static_cast<int64_t>(j) * N) : c->Z;
+          if (fused_bj)
             {
               const double *sc = (j == 0) ? nullptr : c->g.inv_scale;
               CKS(launch(c, KK_PREC, 1, [&] {
                 return launch_bj_apply_scale(c->dm, m32, c->dinv, Vj, c->Z, sc, c->g.active, c->st);
               }));
             }
+          else if (mg)
+            CKS(vcycle(c, 0, Vj, Zj, c->g.active));
           else
             CKS(precond(c, Vj, c->Z, c->g.active));
-          CKS(spmv(c, c->Z, Vj1, c->g.active));
+          CKS(spmv(c, Zj, Vj1, c->g.active));
           if (fused)
             {
               CKS(launch(c, KK_VEC, 1, [&] {
@@ -515,6 +540,13 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
               CKS(launch(c, KK_VEC, 1, [&] {
                 return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 2, j, c->partial, c->g, c->d_cnt, c->st);
               }));
+              if (mg)
+                {
+                  Axpby k{};
+                  k.a = c->g.inv_scale;
+                  k.sa = 1;
+                  CKS(axpby(c, Vj1, Vj1, nullptr, k, c->g.active, m32, m32, m32));
+                }
             }
           else
             {
@@ -556,14 +588,21 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
               if (!anyj) break;
             }
         }
-      // X += M^-1 (V y)
+      // X += M^-1 (V y), or X += Z y for flexible GMRES (y is stored negated)
       CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_solve_y(c->g, n, c->st); }));
-      CKS(axpby(c, nullptr, c->Tmp, nullptr, coefs(0.0, 0.0), c->d_act2, m32, m32, m32));
-      CKS(launch(c, KK_VEC, 1, [&] {
-        return launch_seg_maxpy(c->dm, m32, c->V, N, jdone, c->g.y, mr, c->Tmp, c->d_act2, c->st);
-      }));
-      CKS(precond(c, c->Tmp, c->Z, c->d_act2));
-      CKS(axpby(c, c->Z, c->X, nullptr, coefs(1.0, 1.0), c->d_act2, m32, m32, m32));
+      if (c->n_levels > 0)
+        CKS(launch(c, KK_VEC, 1, [&] {
+          return launch_seg_maxpy(c->dm, m32, c->Zb, N, jdone, c->g.y, mr, c->X, c->d_act2, c->st);
+        }));
+      else
+        {
+          CKS(axpby(c, nullptr, c->Tmp, nullptr, coefs(0.0, 0.0), c->d_act2, m32, m32, m32));
+          CKS(launch(c, KK_VEC, 1, [&] {
+            return launch_seg_maxpy(c->dm, m32, c->V, N, jdone, c->g.y, mr, c->Tmp, c->d_act2, c->st);
+          }));
+          CKS(precond(c, c->Tmp, c->Z, c->d_act2));
+          CKS(axpby(c, c->Z, c->X, nullptr, coefs(1.0, 1.0), c->d_act2, m32, m32, m32));
+        }
       CK(cudaMemcpyAsync(c->h_its, c->g.its, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
       CK(cudaMemcpyAsync(c->h_norm, c->g.res_est, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
       CKS(sync(c));
@@ -596,6 +635,208 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
   return GLGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------
+// geometric multigrid
+// ---------------------------------------------------------------------------------
+template <typename T> glgpu_status upload_w(glgpu_ctx *c, void **dst, const std::vector<double> &w)
+{
+  std::vector<T> tw(w.begin(), w.end());
+  T *p = nullptr;
+  CKS(dupload(c, &p, tw));
+  *dst = p;
+  return GLGPU_OK;
+}
+
+// Jacobian (and block-Jacobi) of a coarse level at its current state; no residual
+glgpu_status level_jacobian(glgpu_ctx *L, const uint8_t *act)
+{
+  CKS(launch(L, KK_CELL, 1, [&] { return launch_cell(L->dm, L->mixed, L->x, L->H, nullptr, nullptr, act, L->st); }));
+  CKS(launch(L, KK_ROWS, 1, [&] { return launch_rows(L->dm, L->mixed, L->H, L->vals, L->st); }));
+  CKS(launch(L, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st); }));
+  L->has_J = true;
+  return GLGPU_OK;
+}
+
+// after the fine assembly: coarse states, coarse Jacobians, coarsest dense inverse
+glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
+{
+  for (int l = 0; l < c->n_levels; ++l)
+    {
+      glgpu_ctx *F = (l == 0) ? c : c->lv[l - 1];
+      glgpu_ctx *L = c->lv[l];
+      const glgpu_ctx::Transfer &t = c->tr[l];
+      CKS(launch(c, KK_VEC, 1, [&] {
+        return launch_interp_state(L->nn, L->B, t.q_ptr, t.q_idx, t.q_w, F->x, L->x, c->st);
+      }));
+      CK(launch_distribute(L->dm, L->x, c->st));
+      c->launches += 2;
+      CKS(level_jacobian(L, act));
+    }
+  glgpu_ctx *Lc = c->lv[c->n_levels - 1];
+  CKS(launch(c, KK_PREC, 1, [&] {
+    return launch_dense_setup(Lc->dm, c->mixed, Lc->vals, c->d_dense_off, c->max_nd, c->d_inv, c->d_sing, c->st);
+  }));
+  return GLGPU_OK;
+}
+
+// z = V-cycle(r) on level l (l = 0: this context); r, z in the Krylov precision
+glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act)
+{
+  const bool m = c->mixed;
+  if (l == c->n_levels)
+    {
+      glgpu_ctx *L = c->lv[l - 1];
+      return launch(c, KK_PREC, 1, [&] {
+        return launch_dense_apply(L->dm, m, c->max_nd, c->d_dense_off, c->d_inv, r, z, act, c->st);
+      });
+    }
+  glgpu_ctx *L = (l == 0) ? c : c->lv[l - 1];
+  void *t = (l == 0) ? c->C2 : L->Tmp;
+  void *t2 = (l == 0) ? c->C3 : L->C1;
+  const double om = c->prm[0].mg_omega;
+  const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
+  // pre-smoothing from z = 0: z = om D^-1 r, then damped block-Jacobi sweeps
+  CKS(bj(L, r, z, act));
+  CKS(axpby(L, z, z, nullptr, coefs(om, 0.0), act, m, m, m));
+  for (int s = 1; s < pre; ++s)
+    {
+      CKS(spmv(L, z, t, act));
+      CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
+      CKS(bj(L, t, t2, act));
+      CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
+    }
+  // coarse-grid correction
+  CKS(spmv(L, z, t, act));
+  CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
+  glgpu_ctx *C = c->lv[l];
+  const glgpu_ctx::Transfer &tr = c->tr[l];
+  CKS(launch(c, KK_PREC, 1, [&] {
+    return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
+                           C->dm.node_inst, act, c->st);
+  }));
+  CKS(vcycle(c, l + 1, C->Bv, C->X, act));
+  CKS(launch(c, KK_PREC, 1, [&] {
+    return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, z, L->dm.mask, L->dm.hptr,
+                          L->dm.node_inst, act, c->st);
+  }));
+  for (int s = 0; s < post; ++s)
+    {
+      CKS(spmv(L, z, t, act));
+      CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
+      CKS(bj(L, t, t2, act));
+      CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
+    }
+  return GLGPU_OK;
+}
+
+glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst)
+{
+  std::vector<MgLevel> lv;
+  std::string why;
+  const int nl = build_hierarchy(mesh, n_inst, 16, lv, why);
+  if (nl == 0) return GLGPU_OK; // multigrid does not apply: block-Jacobi stays in charge
+  // coarse contexts share this context's stream
+  std::vector<glgpu_params> lp(prm, prm + n_inst);
+  for (auto &q : lp)
+    {
+      q.precond = GLGPU_PC_BLOCK_JACOBI;
+      q.gmres_restart = 1;
+    }
+  std::vector<std::vector<BoxGeom>> geo(nl + 1);
+  geo[0].resize(n_inst);
+  for (int k = 0; k < n_inst; ++k) infer_box(mesh[k], geo[0][k]);
+  for (int l = 0; l < nl; ++l) geo[l + 1] = lv[l].geom;
+  for (int l = 0; l < nl; ++l)
+    {
+      std::vector<glgpu_mesh> ms(n_inst);
+      for (int k = 0; k < n_inst; ++k)
+        {
+          const BoxMesh &b = lv[l].meshes[k];
+          ms[k] = glgpu_mesh{3, b.nn, b.nc, b.xyz.data(), b.cells.data(), b.mask.data(), nullptr, nullptr, nullptr};
+        }
+      glgpu_ctx *L = nullptr;
+      glgpu_status st = glgpu_create(ms.data(), lp.data(), n_inst, &L);
+      if (st != GLGPU_OK) return st;
+      cudaStreamSynchronize(L->st);
+      cudaStreamDestroy(L->st);
+      L->st = c->st;
+      L->owns_stream = false;
+      c->lv.push_back(L);
+    }
+  // transfer operators between level l (fine side) and l+1
+  c->tr.resize(nl);
+  for (int l = 0; l < nl; ++l)
+    {
+      glgpu_ctx *C = c->lv[l];
+      const std::vector<int64_t> &foff = (l == 0) ? c->P.node_off : c->lv[l - 1]->P.node_off;
+      const std::vector<int64_t> &coff = C->P.node_off;
+      std::vector<int32_t> pp(1, 0), pi, qp(1, 0), qi;
+      std::vector<double> pw, qw;
+      for (int k = 0; k < n_inst; ++k)
+        {
+          const double *fxyz = (l == 0) ? mesh[k].xyz : lv[l - 1].meshes[k].xyz.data();
+          const int64_t fnn = foff[k + 1] - foff[k];
+          const double *cxyz = lv[l].meshes[k].xyz.data();
+          const int64_t cnn = coff[k + 1] - coff[k];
+          std::vector<int32_t> a, b;
+          std::vector<double> w;
+          trilinear(geo[l + 1][k], fxyz, fnn, a, b, w, coff[k]);
+          for (int64_t i = 0; i < fnn; ++i) pp.push_back(pp.back() + (a[i + 1] - a[i]));
+          pi.insert(pi.end(), b.begin(), b.end());
+          pw.insert(pw.end(), w.begin(), w.end());
+          trilinear(geo[l][k], cxyz, cnn, a, b, w, foff[k]);
+          for (int64_t i = 0; i < cnn; ++i) qp.push_back(qp.back() + (a[i + 1] - a[i]));
+          qi.insert(qi.end(), b.begin(), b.end());
+          qw.insert(qw.end(), w.begin(), w.end());
+        }
+      std::vector<int32_t> rp, ri;
+      std::vector<double> rw;
+      transpose_csr(foff[n_inst], coff[n_inst], pp, pi, pw, rp, ri, rw);
+      glgpu_ctx::Transfer &t = c->tr[l];
+      CKS(dupload(c, &t.p_ptr, pp));
+      CKS(dupload(c, &t.p_idx, pi));
+      CKS(dupload(c, &t.r_ptr, rp));
+      CKS(dupload(c, &t.r_idx, ri));
+      CKS(dupload(c, &t.q_ptr, qp));
+      CKS(dupload(c, &t.q_idx, qi));
+      CKS(dupload(c, &t.q_w, qw));
+      if (c->mixed)
+        {
+          CKS(upload_w<float>(c, &t.p_w, pw));
+          CKS(upload_w<float>(c, &t.r_w, rw));
+        }
+      else
+        {
+          CKS(upload_w<double>(c, &t.p_w, pw));
+          CKS(upload_w<double>(c, &t.r_w, rw));
+        }
+    }
+  // coarsest level: dense inverses
+  glgpu_ctx *Lc = c->lv[nl - 1];
+  std::vector<int64_t> doff(n_inst + 1, 0);
+  int max_nd = 0;
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const int nd = static_cast<int>((Lc->P.node_off[k + 1] - Lc->P.node_off[k]) * Lc->B);
+      max_nd = std::max(max_nd, nd);
+      doff[k + 1] = doff[k] + static_cast<int64_t>(nd) * nd;
+    }
+  if (max_nd > 160) return set_error(GLGPU_ERR_ARG, "multigrid: coarsest level too large for the dense solve");
+  c->max_nd = max_nd;
+  CKS(dupload(c, &c->d_dense_off, doff));
+  CKS(dalloc(c, &c->d_inv, static_cast<size_t>(doff[n_inst])));
+  CKS(dalloc(c, &c->d_sing, static_cast<size_t>(n_inst)));
+  CK(cudaMemset(c->d_sing, 0, sizeof(int) * n_inst));
+  {
+    char *zb = nullptr;
+    CKS(dalloc(c, &zb, tsz(c) * static_cast<size_t>(c->restart) * c->N));
+    CK(cudaMemset(zb, 0, tsz(c) * static_cast<size_t>(c->restart) * c->N));
+    c->Zb = zb;
+  }
+  c->n_levels = nl;
+  return GLGPU_OK;
+}
+
 } // namespace
 
 // =================================================================================
@@ -615,6 +856,9 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->ls_step = 0.83;
   p->ls_max_trials = 100;
   p->damped = 1;
+  p->mg_pre = 2;
+  p->mg_post = 2;
+  p->mg_omega = 0.7;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -678,7 +922,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   uint32_t *p_mask;
   double *p_h, *p_hw, *p_rcw, *p_coef;
   int16_t *p_slot;
-  int64_t *p_hto, *p_sb, *p_se, *p_co;
+  int64_t *p_hto, *p_sb, *p_se, *p_co, *p_noff;
   HangTarget *p_tg;
   std::vector<double> coef(static_cast<size_t>(n_inst) * kCoef);
   std::vector<GeoD> geo_d(P.nc);
@@ -709,7 +953,8 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = dupload(c, &p_slot, P.rc_slot)) || (s = dupload(c, &p_hto, P.ht_off)) || (s = dupload(c, &p_tg, P.hang_tg)) ||
       (s = dupload(c, &p_coef, coef)) || (s = dupload(c, &p_sb, P.seg_begin)) || (s = dupload(c, &p_se, P.seg_end)) ||
       (s = dupload(c, &p_si, P.seg_inst)) || (s = dupload(c, &p_iso, P.inst_seg_off)) ||
-      (s = dupload(c, &p_co, P.cell_off)) || (s = dupload(c, &p_geod, geo_d)) || (s = dupload(c, &p_geof, geo_f)) ||
+      (s = dupload(c, &p_co, P.cell_off)) || (s = dupload(c, &p_noff, P.node_off)) ||
+      (s = dupload(c, &p_geod, geo_d)) || (s = dupload(c, &p_geof, geo_f)) ||
       (s = dupload(c, &p_rcwf, rc_wf)))
     return fail(s);
   {
@@ -745,6 +990,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   d.seg_inst = p_si;
   d.inst_seg_off = p_iso;
   d.cell_off = p_co;
+  d.node_off_ptr = p_noff;
   // state buffers
   const int64_t N = c->N;
   const size_t ts = tsz(c);
@@ -809,6 +1055,10 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   c->inst_on.assign(n_inst, 1);
   cudaEventCreate(&c->ev_user0);
   cudaEventCreate(&c->ev_user1);
+  if (prm[0].precond == GLGPU_PC_MULTIGRID && P.dim == 3)
+    {
+      if ((s = mg_setup(c, mesh, prm, n_inst)) != GLGPU_OK) return fail(s);
+    }
   *out = c;
   return GLGPU_OK;
 }
@@ -838,7 +1088,8 @@ extern "C" glgpu_status glgpu_destroy(glgpu_ctx *c)
   for (auto e : c->ev_pipe)
     if (e) cudaEventDestroy(e);
   if (c->h_its) cudaFreeHost(c->h_its);
-  if (c->st) cudaStreamDestroy(c->st);
+  for (glgpu_ctx *l : c->lv) glgpu_destroy(l);
+  if (c->st && c->owns_stream) cudaStreamDestroy(c->st);
   delete c;
   return GLGPU_OK;
 }
@@ -886,6 +1137,7 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
   CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
   CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   CKS(axpby(c, c->R, c->rhs, nullptr, coefs(-1.0, 0.0), act, false, false, false));
+  if (c->n_levels > 0) CKS(mg_assemble(c, act));
   std::vector<double> nr;
   CKS(norms_d(c, c->rhs, act, nr));
   for (int k = 0; k < c->n_inst; ++k)
@@ -1145,7 +1397,15 @@ extern "C" glgpu_status glgpu_kernel_timing(glgpu_ctx *c, int enable, double *ke
   return GLGPU_OK;
 }
 
-extern "C" int64_t glgpu_launch_count(const glgpu_ctx *c) { return c ? c->launches : 0; }
+extern "C" int64_t glgpu_launch_count(const glgpu_ctx *c)
+{
+  if (!c) return 0;
+  int64_t n = c->launches;
+  for (const glgpu_ctx *l : c->lv) n += glgpu_launch_count(l);
+  return n;
+}
+
+extern "C" int glgpu_mg_levels(const glgpu_ctx *c) { return c ? c->n_levels : 0; }
 
 extern "C" glgpu_status glgpu_sync(glgpu_ctx *c)
 {

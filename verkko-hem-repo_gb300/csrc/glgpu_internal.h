@@ -26,7 +26,31 @@ struct BoxMesh
   std::vector<uint32_t> mask;
 };
 int matep_eval(double p, double t, bool scc, double *out);
-int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dxy, BoxMesh &m);
+// dir3: zero-Dirichlet (orbital column of that axis) on the x, y, z faces
+int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m);
+
+// ---------------------------------------------------------------------------------
+// multigrid hierarchy (mg.cc)
+// ---------------------------------------------------------------------------------
+struct BoxGeom
+{
+  double lo[3], hi[3];
+  int n[3];
+  int dir[3];
+};
+struct MgLevel
+{
+  std::vector<BoxGeom> geom;    // per instance
+  std::vector<BoxMesh> meshes;  // per instance
+};
+bool infer_box(const glgpu_mesh &m, BoxGeom &g);
+void trilinear(const BoxGeom &src, const double *pts, int64_t npts, std::vector<int32_t> &ptr,
+               std::vector<int32_t> &idx, std::vector<double> &w, int64_t src_node_offset);
+void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx,
+                   const std::vector<double> &w, std::vector<int32_t> &tptr, std::vector<int32_t> &tidx,
+                   std::vector<double> &tw);
+int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vector<MgLevel> &levels,
+                    std::string &why);
 double gaussian(uint64_t seed, uint64_t index);
 
 // Dirichlet mask of the orbital column `axis` of u and v: components 9p + 3mu + axis.

@@ -76,7 +76,7 @@ int matep_eval(double p, double t, bool scc, double *out)
 // Box mesh.  Lattice coordinates are in units of half a coarse cell; nodes are
 // numbered by lattice (z, y, x), cells by the lattice of their first vertex.
 // ---------------------------------------------------------------------------------
-int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dxy, BoxMesh &m)
+int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m)
 {
   const int nx = n[0], ny = n[1], nz = n[2];
   if (nx < 1 || ny < 1 || nz < 1) return -1;
@@ -224,7 +224,7 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
       }
   // zero-Dirichlet masks: orbital column `axis` of u and v on that axis' faces
   m.mask.assign(nn, 0u);
-  const bool on[3] = {dxy && dxy[0] != 0, dxy && dxy[1] != 0, true};
+  const bool on[3] = {dir3 && dir3[0] != 0, dir3 && dir3[1] != 0, !dir3 || dir3[2] != 0};
   const int64_t Ls[3] = {Lx, Ly, Lz};
   for (int64_t i = 0; i < nn; ++i)
     {
@@ -274,7 +274,8 @@ extern "C" glgpu_status glgpu_mesh_box(const double *lo, const double *hi, const
 {
   if (!lo || !hi || !n) return set_error(GLGPU_ERR_ARG, "glgpu_mesh_box: NULL argument");
   BoxMesh m;
-  const int rc = mesh_box(lo, hi, n, refine_band, dirichlet_xy, m);
+  const int dir3[3] = {dirichlet_xy ? dirichlet_xy[0] : 0, dirichlet_xy ? dirichlet_xy[1] : 0, 1};
+  const int rc = mesh_box(lo, hi, n, refine_band, dir3, m);
   if (rc != 0) return set_error(GLGPU_ERR_ARG, "glgpu_mesh_box: invalid box or mesh too large");
   if (n_nodes) *n_nodes = m.nn;
   if (n_cells) *n_cells = m.nc;

@@ -30,6 +30,7 @@ MIXED = 1
 PC_NONE = 0
 PC_BLOCK_JACOBI = 1
 PC_CHEBYSHEV = 2
+PC_MULTIGRID = 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "not converged",
           5: "NaN/Inf", 6: "device wait timed out", 7: "call out of order"}
@@ -56,7 +57,8 @@ class _Params(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("beta", ctypes.c_double * 5), ("precision", ctypes.c_int),
                 ("precond", ctypes.c_int), ("cheb_degree", ctypes.c_int), ("gmres_restart", ctypes.c_int),
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
-                ("damped", ctypes.c_int)]
+                ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
+                ("mg_omega", ctypes.c_double)]
 
 
 _lib = None
@@ -91,6 +93,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_spmv.argtypes = [vp, _dp, _dp]
     L.glgpu_timers.argtypes = [vp, _dp, ctypes.c_int]
     L.glgpu_kernel_timing.argtypes = [vp, ctypes.c_int, _dp, _lp, ctypes.c_int]
+    L.glgpu_mg_levels.argtypes = [vp]
     L.glgpu_launch_count.argtypes = [vp]
     L.glgpu_launch_count.restype = ctypes.c_int64
     L.glgpu_sync.argtypes = [vp]
@@ -266,6 +269,9 @@ class Params:
     ls_step: float = 0.83
     ls_max_trials: int = 100
     damped: bool = True
+    mg_pre: int = 2
+    mg_post: int = 2
+    mg_omega: float = 0.7
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -281,6 +287,7 @@ class Params:
         s.precision, s.precond, s.cheb_degree = int(self.precision), int(self.precond), int(self.cheb_degree)
         s.gmres_restart, s.gmres_max_iter = int(self.gmres_restart), int(self.gmres_max_iter)
         s.ls_step, s.ls_max_trials, s.damped = float(self.ls_step), int(self.ls_max_trials), int(bool(self.damped))
+        s.mg_pre, s.mg_post, s.mg_omega = int(self.mg_pre), int(self.mg_post), float(self.mg_omega)
         return s
 
 
@@ -421,6 +428,10 @@ class FemGL:
     @property
     def launch_count(self) -> int:
         return int(lib().glgpu_launch_count(self._ctx))
+
+    @property
+    def mg_levels(self) -> int:
+        return int(lib().glgpu_mg_levels(self._ctx))
 
     def sync(self) -> None:
         _check(lib().glgpu_sync(self._ctx))
