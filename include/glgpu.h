@@ -99,7 +99,7 @@ typedef struct
   int ls_max_trials;    /* trials of the backtracking line search, 100 (iteration.cc:170) */
   int damped;           /* "Using dampped Newton iteration" (1) or full Newton (0) */
   int mg_pre, mg_post;  /* multigrid: damped block-Jacobi sweeps before / after the coarse correction */
-  double mg_omega;      /* multigrid: smoother damping */
+  double mg_omega;      /* multigrid: damping of the l1 block-Jacobi smoother (default 1) */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;
@@ -214,8 +214,26 @@ glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, 
 int64_t glgpu_launch_count(const glgpu_ctx *ctx);
 
 /* Coarse levels of the multigrid hierarchy (0 when the preconditioner is not multigrid
- * or an instance is not a uniform box grid). */
+ * or an instance is not a uniform box grid).  Levels are nested tensor grids (every
+ * other node line per coarsened axis), coarse Jacobians are Galerkin products P^T J P. */
 int glgpu_mg_levels(const glgpu_ctx *ctx);
+
+/* Linear solves whose multigrid cycles stalled (true residual not halved by a restart
+ * cycle) or diverged and that finished with block-Jacobi GMRES. */
+int64_t glgpu_mg_fallbacks(const glgpu_ctx *ctx);
+
+/* Sizes of coarse level `level` (1 = first coarse level .. glgpu_mg_levels): its node
+ * count, block count, and the entries of the prolongation from it to level - 1. */
+glgpu_status glgpu_mg_level_info(const glgpu_ctx *ctx, int level, int64_t *n_nodes, int64_t *nnzb, int64_t *p_nnz);
+
+/* Pattern and FP64 values of the Jacobian of coarse level `level` as of the last
+ * assembly (same layout as glgpu_get_system). */
+glgpu_status glgpu_mg_level_system(const glgpu_ctx *ctx, int level, int32_t *rowptr, int32_t *cols, double *vals);
+
+/* Prolongation from coarse level `level` to level - 1 as node-level CSR over the finer
+ * level's nodes: ptr [fine nodes + 1], idx (coarse node ids), w (weights).  It acts on
+ * every component of a node; restriction is its transpose. */
+glgpu_status glgpu_mg_prolongation(const glgpu_ctx *ctx, int level, int32_t *ptr, int32_t *idx, double *w);
 
 /* Blocks until all work of the context's stream is done. */
 glgpu_status glgpu_sync(glgpu_ctx *ctx);

@@ -1,9 +1,11 @@
-"""Geometric multigrid preconditioner (flexible GMRES) on the GPU: tight linear solves
-agree with the oracle's Jacobian, Newton with multigrid reproduces the oracle's answer,
-batched instances of different sizes work, and non-uniform (refined) meshes fall back
-to block-Jacobi."""
+"""Geometric multigrid preconditioner (flexible GMRES) on the GPU: the coarse Jacobians
+are the Galerkin products P^T J P of the level above, tight linear solves agree with the
+oracle's Jacobian, Newton with multigrid reproduces the oracle's answer, batched
+instances of different sizes work, and non-uniform (refined) meshes fall back to
+block-Jacobi."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from _lib import coef_of, oracle_mesh, product
 
@@ -25,6 +27,50 @@ def _solve(gl, m, x0, precond, precision=0, tol=1e-10):
         _, _, J, rhs = f.system()
         lev = f.mg_levels
     return its[0], d, J, rhs, lev
+
+
+def _bsr(rowptr, cols, vals):
+    nn = rowptr.size - 1
+    return sp.bsr_matrix((vals, cols, rowptr), shape=(nn * 18, nn * 18)).tocsr()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_galerkin_coarse_operators(gl, precision):
+    # anisotropic slab with an odd cell count: semi-coarsening and an uneven last line
+    m = gl.box_mesh([-10, -10, -4], [10, 10, 4], (9, 9, 9))
+    prm = gl.Params.from_matep(20.0, 0.6, precond=gl.PC_MULTIGRID, precision=precision)
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=4)
+    with gl.FemGL(m, prm) as f:
+        f.set_solution(x0)
+        f.assemble_system()
+        rowptr, cols, vals, _ = f.system()
+        levels = [(rowptr, cols, vals, None)] + [f.mg_level(l) for l in range(1, f.mg_levels + 1)]
+        nlev = f.mg_levels
+    assert nlev >= 3
+    fine_mask = np.asarray(m.mask, np.uint32)
+    for l in range(1, nlev + 1):
+        rp_f, c_f, v_f, _ = levels[l - 1]
+        rp_c, c_c, v_c, (ptr, idx, w) = levels[l]
+        nf, nc = rp_f.size - 1, rp_c.size - 1
+        Pn = sp.csr_matrix((w, idx, ptr), shape=(nf, nc))
+        # partition of unity; every coarse node coincides with one fine node (nested grids)
+        assert np.allclose(np.asarray(Pn.sum(axis=1)).ravel(), 1.0, atol=1e-14)
+        single = (np.diff(ptr) == 1) & np.isclose(w[ptr[:-1].clip(max=w.size - 1)], 1.0)
+        assert np.bincount(idx[ptr[:-1][single]], minlength=nc).min() == 1
+        coarse_mask = np.zeros(nc, np.uint32)
+        coarse_mask[idx[ptr[:-1][single]]] = fine_mask[single]
+        P = sp.kron(Pn, sp.identity(18), format="csr")
+        want = (P.T @ _bsr(rp_f, c_f, v_f) @ P).toarray()
+        got = _bsr(rp_c, c_c, v_c).toarray()
+        dmask = ((coarse_mask[:, None] >> np.arange(18)[None, :]) & 1).astype(bool).ravel()
+        free = ~dmask
+        scale = np.abs(want[np.ix_(free, free)]).max()
+        tol = 1e-13 if precision == 0 else 2e-6
+        assert np.abs(got[np.ix_(free, free)] - want[np.ix_(free, free)]).max() <= tol * scale
+        # constrained components: identity rows, zero columns
+        assert np.array_equal(got[dmask], np.eye(got.shape[0])[dmask])
+        assert not got[np.ix_(free, dmask)].any()
+        fine_mask = coarse_mask
 
 
 @pytest.mark.parametrize("n", [8, 7])

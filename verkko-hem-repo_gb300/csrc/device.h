@@ -66,7 +66,8 @@ cudaError_t init_constants();
 // ---- linear algebra (kernels_la.cu) ----
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y,
                         const uint8_t *inst_active, cudaStream_t s);
-cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s);
+// l1: add each row's absolute off-block sum to its diagonal (l1 block-Jacobi smoother)
+cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s, bool l1 = false);
 cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const void *x, void *y,
                             const uint8_t *inst_active, cudaStream_t s);
 // partial[s][v] = sum over segment s of X[v][i] * y[i], v < nv (X rows strided by ld)
@@ -144,8 +145,16 @@ cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, c
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
                             const uint8_t *act, cudaStream_t s);
-cudaError_t launch_interp_state(int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const double *w,
-                                const double *xf, double *xc, cudaStream_t s);
+// Galerkin product J_c = P^T J_f P restricted to the coarse block pattern, one CTA per
+// coarse block row; slot[] lists, in loop order, the coarse slot of every (restriction
+// entry, fine block, prolongation entry) triple of the row.  Zero-Dirichlet rows and
+// columns of the coarse level become identity rows/zero columns.
+cudaError_t launch_galerkin(bool fp32, int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c,
+                            const uint32_t *mask_c, void *vals_c, const int32_t *r_ptr, const int32_t *r_idx,
+                            const void *r_w, const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f,
+                            const int32_t *p_ptr, const void *p_w, const int64_t *g_ptr,
+                            const uint8_t *g_slot, int max_row_blocks_c, const int32_t *node_inst_c,
+                            const uint8_t *act, cudaStream_t s);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

@@ -116,9 +116,12 @@ struct glgpu_ctx
   std::vector<glgpu_ctx *> lv;
   struct Transfer
   {
-    int32_t *p_ptr = nullptr, *p_idx = nullptr, *r_ptr = nullptr, *r_idx = nullptr, *q_ptr = nullptr, *q_idx = nullptr;
+    int32_t *p_ptr = nullptr, *p_idx = nullptr, *r_ptr = nullptr, *r_idx = nullptr;
     void *p_w = nullptr, *r_w = nullptr; // T weights
-    double *q_w = nullptr;
+    int64_t *g_ptr = nullptr;            // Galerkin slot table of each coarse row
+    uint8_t *g_slot = nullptr;
+    std::vector<int32_t> h_ptr, h_idx;   // host copy of P
+    std::vector<double> h_w;
   };
   std::vector<Transfer> tr;          // tr[l]: level l (fine side) <-> level l+1
   int64_t *d_dense_off = nullptr;
@@ -126,6 +129,8 @@ struct glgpu_ctx
   int *d_sing = nullptr;
   int max_nd = 0;
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
+  void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
+  int64_t mg_fallbacks = 0;          // solves handed from multigrid to block-Jacobi
 };
 
 namespace
@@ -295,9 +300,10 @@ glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act)
 // ---------------------------------------------------------------------------------
 // preconditioner
 // ---------------------------------------------------------------------------------
-glgpu_status bj(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
+glgpu_status bj(glgpu_ctx *c, const void *in, void *out, const uint8_t *act, const void *inv = nullptr)
 {
-  return launch(c, KK_PREC, 1, [&] { return launch_bj_apply(c->dm, c->mixed, c->dinv, in, out, act, c->st); });
+  const void *d = inv ? inv : c->dinv;
+  return launch(c, KK_PREC, 1, [&] { return launch_bj_apply(c->dm, c->mixed, d, in, out, act, c->st); });
 }
 
 glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
@@ -381,7 +387,8 @@ glgpu_status precond(glgpu_ctx *c, const void *v, void *z, const uint8_t *act)
   const bool m = c->mixed;
   const int pc = c->prm[0].precond;
   if (pc == GLGPU_PC_NONE) return axpby(c, v, z, nullptr, coefs(1.0, 0.0), act, m, m, m);
-  if (pc == GLGPU_PC_BLOCK_JACOBI) return bj(c, v, z, act);
+  // multigrid contexts fall back to block-Jacobi (refined meshes, stalled cycles)
+  if (pc == GLGPU_PC_BLOCK_JACOBI || pc == GLGPU_PC_MULTIGRID) return bj(c, v, z, act);
   // Chebyshev semi-iteration for J z = v preconditioned by D^-1, started at z = 0.
   // Step scalars per instance live at d_cheb + 2 n_inst as [deg][n_inst][2]:
   // step 0 uses (0, 1/theta), step i >= 1 uses (rho_i rho_{i-1}, 2 rho_i / delta).
@@ -459,6 +466,8 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act);
 // ---------------------------------------------------------------------------------
 // GMRES(m), right preconditioned, classical Gram-Schmidt with one reorthogonalization
 // ---------------------------------------------------------------------------------
+constexpr double kMgStall = 0.5; // least reduction of the true residual per multigrid cycle
+
 glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std::vector<int> &its_out,
                    bool &all_conv)
 {
@@ -476,6 +485,10 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
   std::vector<int> total(n, 0);
   std::vector<uint8_t> solve_on(on);
   all_conv = false;
+  // multigrid runs flexible GMRES; a cycle whose true residual does not at least halve
+  // hands the rest of the solve to block-Jacobi GMRES
+  bool use_mg = c->n_levels > 0;
+  std::vector<double> prev_res(c->rhs_norm);
   for (int cycle = 0;; ++cycle)
     {
       // V0 = b - J X
@@ -512,8 +525,9 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
           // fused path: the normalisation of V_j is folded into the block-Jacobi pass and
           // the Gram-Schmidt finalisation and Givens update run inside the reductions.
           // Multigrid (flexible GMRES): Z_j = V-cycle(V_j) is kept for the solution update.
-          const bool mg = c->n_levels > 0;
-          const bool fused_bj = !mg && c->B == 18 && c->prm[0].precond == GLGPU_PC_BLOCK_JACOBI;
+          const bool mg = use_mg;
+          const bool fused_bj = !mg && c->B == 18 &&
+                                (c->prm[0].precond == GLGPU_PC_BLOCK_JACOBI || c->prm[0].precond == GLGPU_PC_MULTIGRID);
           const bool fused = fused_bj || mg;
           void *Zj = mg ? tptr(c, c->Zb, static_cast<int64_t>(j) * N) : c->Z;
           if (fused_bj)
@@ -590,7 +604,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
         }
       // X += M^-1 (V y), or X += Z y for flexible GMRES (y is stored negated)
       CKS(launch(c, KK_VEC, 1, [&] { return launch_gmres_solve_y(c->g, n, c->st); }));
-      if (c->n_levels > 0)
+      if (use_mg)
         CKS(launch(c, KK_VEC, 1, [&] {
           return launch_seg_maxpy(c->dm, m32, c->Zb, N, jdone, c->g.y, mr, c->X, c->d_act2, c->st);
         }));
@@ -605,7 +619,50 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
         }
       CK(cudaMemcpyAsync(c->h_its, c->g.its, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
       CK(cudaMemcpyAsync(c->h_norm, c->g.res_est, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+      if (use_mg)
+        {
+          // flexible GMRES can stop on a breakdown of the preconditioned basis with a small
+          // estimate: judge the cycle by the true residual |b - J X| instead
+          CKS(spmv(c, c->X, c->Tmp, c->d_act2));
+          CKS(axpby(c, c->Bv, c->Tmp, nullptr, coefs(1.0, -1.0), c->d_act2, m32, m32, m32));
+          CKS(launch(c, KK_VEC, 1, [&] {
+            return launch_seg_mdot(c->dm, m32, c->Tmp, 0, 1, c->Tmp, c->partial, c->d_act2, c->st);
+          }));
+          CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 1, c->d_tmp, 1, 1, c->st); }));
+          CK(cudaMemcpyAsync(c->h_norm, c->d_tmp, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+        }
       CKS(sync(c));
+      if (use_mg)
+        {
+          std::vector<uint8_t> bad(n, 0);
+          bool any_bad = false, stall = false;
+          for (int k = 0; k < n; ++k)
+            {
+              if (!solve_on[k] || c->h_norm[k] <= tol_abs[k]) continue;
+              if (!std::isfinite(c->h_norm[k]) || c->h_norm[k] > prev_res[k])
+                {
+                  bad[k] = 1;
+                  any_bad = true;
+                }
+              else if (c->h_norm[k] > kMgStall * prev_res[k])
+                stall = true;
+            }
+          if (any_bad)
+            {
+              // the cycle made things worse: restart these instances from X = 0
+              CKS(upload_act(c, c->d_act2, bad));
+              CKS(axpby(c, nullptr, c->X, nullptr, coefs(0.0, 0.0), c->d_act2, m32, m32, m32));
+              for (int k = 0; k < n; ++k)
+                if (bad[k]) c->h_norm[k] = c->rhs_norm[k];
+            }
+          for (int k = 0; k < n; ++k)
+            if (solve_on[k]) prev_res[k] = c->h_norm[k];
+          if (any_bad || stall)
+            {
+              use_mg = false;
+              c->mg_fallbacks++;
+            }
+        }
       bool more = false;
       for (int k = 0; k < n; ++k)
         {
@@ -647,30 +704,24 @@ template <typename T> glgpu_status upload_w(glgpu_ctx *c, void **dst, const std:
   return GLGPU_OK;
 }
 
-// Jacobian (and block-Jacobi) of a coarse level at its current state; no residual
-glgpu_status level_jacobian(glgpu_ctx *L, const uint8_t *act)
-{
-  CKS(launch(L, KK_CELL, 1, [&] { return launch_cell(L->dm, L->mixed, L->x, L->H, nullptr, nullptr, act, L->st); }));
-  CKS(launch(L, KK_ROWS, 1, [&] { return launch_rows(L->dm, L->mixed, L->H, L->vals, L->st); }));
-  CKS(launch(L, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st); }));
-  L->has_J = true;
-  return GLGPU_OK;
-}
-
-// after the fine assembly: coarse states, coarse Jacobians, coarsest dense inverse
+// after the fine assembly: the l1 block-Jacobi smoother of the finest level, coarse
+// Jacobians P^T J P level by level with their l1 smoothers, and the dense inverse of
+// the coarsest level
 glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
 {
+  CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(c->dm, c->mixed, c->vals, c->sinv, c->st, true); }));
   for (int l = 0; l < c->n_levels; ++l)
     {
       glgpu_ctx *F = (l == 0) ? c : c->lv[l - 1];
       glgpu_ctx *L = c->lv[l];
       const glgpu_ctx::Transfer &t = c->tr[l];
-      CKS(launch(c, KK_VEC, 1, [&] {
-        return launch_interp_state(L->nn, L->B, t.q_ptr, t.q_idx, t.q_w, F->x, L->x, c->st);
+      CKS(launch(c, KK_PREC, 1, [&] {
+        return launch_galerkin(c->mixed, L->nn, L->dm.rowptr, L->dm.cols, L->dm.mask, L->vals, t.r_ptr, t.r_idx, t.r_w,
+                               F->dm.rowptr, F->dm.cols, F->vals, t.p_ptr, t.p_w, t.g_ptr, t.g_slot,
+                               L->P.max_row_blocks, L->dm.node_inst, act, c->st);
       }));
-      CK(launch_distribute(L->dm, L->x, c->st));
-      c->launches += 2;
-      CKS(level_jacobian(L, act));
+      CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st, true); }));
+      L->has_J = true;
     }
   glgpu_ctx *Lc = c->lv[c->n_levels - 1];
   CKS(launch(c, KK_PREC, 1, [&] {
@@ -691,18 +742,19 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
       });
     }
   glgpu_ctx *L = (l == 0) ? c : c->lv[l - 1];
+  const void *sm = (l == 0) ? c->sinv : L->dinv; // l1 block-Jacobi
   void *t = (l == 0) ? c->C2 : L->Tmp;
   void *t2 = (l == 0) ? c->C3 : L->C1;
   const double om = c->prm[0].mg_omega;
   const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
-  // pre-smoothing from z = 0: z = om D^-1 r, then damped block-Jacobi sweeps
-  CKS(bj(L, r, z, act));
+  // pre-smoothing from z = 0: z = om D^-1 r, then damped l1 block-Jacobi sweeps
+  CKS(bj(L, r, z, act, sm));
   CKS(axpby(L, z, z, nullptr, coefs(om, 0.0), act, m, m, m));
   for (int s = 1; s < pre; ++s)
     {
       CKS(spmv(L, z, t, act));
       CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
-      CKS(bj(L, t, t2, act));
+      CKS(bj(L, t, t2, act, sm));
       CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
     }
   // coarse-grid correction
@@ -723,7 +775,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
     {
       CKS(spmv(L, z, t, act));
       CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
-      CKS(bj(L, t, t2, act));
+      CKS(bj(L, t, t2, act, sm));
       CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
     }
   return GLGPU_OK;
@@ -742,10 +794,6 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       q.precond = GLGPU_PC_BLOCK_JACOBI;
       q.gmres_restart = 1;
     }
-  std::vector<std::vector<BoxGeom>> geo(nl + 1);
-  geo[0].resize(n_inst);
-  for (int k = 0; k < n_inst; ++k) infer_box(mesh[k], geo[0][k]);
-  for (int l = 0; l < nl; ++l) geo[l + 1] = lv[l].geom;
   for (int l = 0; l < nl; ++l)
     {
       std::vector<glgpu_mesh> ms(n_inst);
@@ -763,43 +811,76 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       L->owns_stream = false;
       c->lv.push_back(L);
     }
-  // transfer operators between level l (fine side) and l+1
+  // transfer operators between level l (fine side) and l+1, and the Galerkin slot tables
+  std::vector<TensorGrid> fine_grid(n_inst);
+  for (int k = 0; k < n_inst; ++k)
+    {
+      BoxGeom g;
+      infer_box(mesh[k], g);
+      for (int d = 0; d < 3; ++d)
+        {
+          fine_grid[k].x[d].resize(g.n[d] + 1);
+          fine_grid[k].dir[d] = g.dir[d];
+        }
+    }
   c->tr.resize(nl);
   for (int l = 0; l < nl; ++l)
     {
       glgpu_ctx *C = c->lv[l];
-      const std::vector<int64_t> &foff = (l == 0) ? c->P.node_off : c->lv[l - 1]->P.node_off;
-      const std::vector<int64_t> &coff = C->P.node_off;
-      std::vector<int32_t> pp(1, 0), pi, qp(1, 0), qi;
-      std::vector<double> pw, qw;
+      const Plan &FP = (l == 0) ? c->P : c->lv[l - 1]->P;
+      const Plan &CP = C->P;
+      std::vector<int32_t> pp(1, 0), pi;
+      std::vector<double> pw;
       for (int k = 0; k < n_inst; ++k)
         {
-          const double *fxyz = (l == 0) ? mesh[k].xyz : lv[l - 1].meshes[k].xyz.data();
-          const int64_t fnn = foff[k + 1] - foff[k];
-          const double *cxyz = lv[l].meshes[k].xyz.data();
-          const int64_t cnn = coff[k + 1] - coff[k];
+          const TensorGrid &fg = (l == 0) ? fine_grid[k] : lv[l - 1].grid[k];
+          int nc[3];
+          for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(lv[l].grid[k].x[d].size()) - 1;
           std::vector<int32_t> a, b;
           std::vector<double> w;
-          trilinear(geo[l + 1][k], fxyz, fnn, a, b, w, coff[k]);
-          for (int64_t i = 0; i < fnn; ++i) pp.push_back(pp.back() + (a[i + 1] - a[i]));
+          tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
+          if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
+            return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
+          for (size_t i = 0; i + 1 < a.size(); ++i) pp.push_back(pp.back() + (a[i + 1] - a[i]));
           pi.insert(pi.end(), b.begin(), b.end());
           pw.insert(pw.end(), w.begin(), w.end());
-          trilinear(geo[l][k], cxyz, cnn, a, b, w, foff[k]);
-          for (int64_t i = 0; i < cnn; ++i) qp.push_back(qp.back() + (a[i + 1] - a[i]));
-          qi.insert(qi.end(), b.begin(), b.end());
-          qw.insert(qw.end(), w.begin(), w.end());
         }
       std::vector<int32_t> rp, ri;
       std::vector<double> rw;
-      transpose_csr(foff[n_inst], coff[n_inst], pp, pi, pw, rp, ri, rw);
+      transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
+      // slot of every (restriction entry, fine block, prolongation entry) of each coarse row
+      std::vector<int64_t> gp(CP.nn + 1, 0);
+      std::vector<uint8_t> gs;
+      for (int64_t I = 0; I < CP.nn; ++I)
+        {
+          const int32_t *c0 = CP.cols.data() + CP.rowptr[I], *c1 = CP.cols.data() + CP.rowptr[I + 1];
+          for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
+            {
+              const int32_t i = ri[k];
+              for (int32_t b = FP.rowptr[i]; b < FP.rowptr[i + 1]; ++b)
+                {
+                  const int32_t j = FP.cols[b];
+                  for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
+                    {
+                      const int32_t *f = std::find(c0, c1, pi[q]);
+                      if (f == c1) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
+                      gs.push_back(static_cast<uint8_t>(f - c0));
+                    }
+                }
+            }
+          gp[I + 1] = static_cast<int64_t>(gs.size());
+        }
+      if (CP.max_row_blocks > 255) return set_error(GLGPU_ERR_ARG, "multigrid: coarse rows too long");
       glgpu_ctx::Transfer &t = c->tr[l];
+      t.h_ptr = pp;
+      t.h_idx = pi;
+      t.h_w = pw;
       CKS(dupload(c, &t.p_ptr, pp));
       CKS(dupload(c, &t.p_idx, pi));
       CKS(dupload(c, &t.r_ptr, rp));
       CKS(dupload(c, &t.r_idx, ri));
-      CKS(dupload(c, &t.q_ptr, qp));
-      CKS(dupload(c, &t.q_idx, qi));
-      CKS(dupload(c, &t.q_w, qw));
+      CKS(dupload(c, &t.g_ptr, gp));
+      CKS(dupload(c, &t.g_slot, gs));
       if (c->mixed)
         {
           CKS(upload_w<float>(c, &t.p_w, pw));
@@ -823,6 +904,11 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     }
   if (max_nd > 160) return set_error(GLGPU_ERR_ARG, "multigrid: coarsest level too large for the dense solve");
   c->max_nd = max_nd;
+  {
+    char *si = nullptr;
+    CKS(dalloc(c, &si, tsz(c) * static_cast<size_t>(c->nn) * c->B * c->B));
+    c->sinv = si;
+  }
   CKS(dupload(c, &c->d_dense_off, doff));
   CKS(dalloc(c, &c->d_inv, static_cast<size_t>(doff[n_inst])));
   CKS(dalloc(c, &c->d_sing, static_cast<size_t>(n_inst)));
@@ -858,7 +944,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->damped = 1;
   p->mg_pre = 2;
   p->mg_post = 2;
-  p->mg_omega = 0.7;
+  p->mg_omega = 1.0;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1406,6 +1492,36 @@ extern "C" int64_t glgpu_launch_count(const glgpu_ctx *c)
 }
 
 extern "C" int glgpu_mg_levels(const glgpu_ctx *c) { return c ? c->n_levels : 0; }
+
+extern "C" int64_t glgpu_mg_fallbacks(const glgpu_ctx *c) { return c ? c->mg_fallbacks : 0; }
+
+extern "C" glgpu_status glgpu_mg_level_info(const glgpu_ctx *c, int level, int64_t *n_nodes, int64_t *nnzb,
+                                            int64_t *p_nnz)
+{
+  if (!c || level < 1 || level > c->n_levels) return set_error(GLGPU_ERR_ARG, "glgpu_mg_level_info: bad level");
+  const glgpu_ctx *L = c->lv[level - 1];
+  if (n_nodes) *n_nodes = L->nn;
+  if (nnzb) *nnzb = L->nnzb;
+  if (p_nnz) *p_nnz = static_cast<int64_t>(c->tr[level - 1].h_idx.size());
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_mg_level_system(const glgpu_ctx *c, int level, int32_t *rowptr, int32_t *cols,
+                                              double *vals)
+{
+  if (!c || level < 1 || level > c->n_levels) return set_error(GLGPU_ERR_ARG, "glgpu_mg_level_system: bad level");
+  return glgpu_get_system(c->lv[level - 1], rowptr, cols, vals, nullptr);
+}
+
+extern "C" glgpu_status glgpu_mg_prolongation(const glgpu_ctx *c, int level, int32_t *ptr, int32_t *idx, double *w)
+{
+  if (!c || level < 1 || level > c->n_levels) return set_error(GLGPU_ERR_ARG, "glgpu_mg_prolongation: bad level");
+  const glgpu_ctx::Transfer &t = c->tr[level - 1];
+  if (ptr) std::memcpy(ptr, t.h_ptr.data(), sizeof(int32_t) * t.h_ptr.size());
+  if (idx) std::memcpy(idx, t.h_idx.data(), sizeof(int32_t) * t.h_idx.size());
+  if (w) std::memcpy(w, t.h_w.data(), sizeof(double) * t.h_w.size());
+  return GLGPU_OK;
+}
 
 extern "C" glgpu_status glgpu_sync(glgpu_ctx *c)
 {

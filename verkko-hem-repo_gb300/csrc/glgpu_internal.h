@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "glgpu.h"
@@ -38,14 +39,29 @@ struct BoxGeom
   int n[3];
   int dir[3];
 };
+// tensor grid of one instance on a multigrid level: node lines per axis, Dirichlet faces
+struct TensorGrid
+{
+  std::vector<double> x[3];
+  int dir[3];
+};
+// 1D interpolation of one fine node line from at most two coarse lines
+struct Lin1
+{
+  int n;
+  int c[2];
+  double w[2];
+};
 struct MgLevel
 {
-  std::vector<BoxGeom> geom;    // per instance
-  std::vector<BoxMesh> meshes;  // per instance
+  std::vector<TensorGrid> grid;                   // per instance
+  std::vector<BoxMesh> meshes;                    // per instance
+  std::vector<std::array<std::vector<Lin1>, 3>> map; // per instance: fine line -> coarse lines
 };
 bool infer_box(const glgpu_mesh &m, BoxGeom &g);
-void trilinear(const BoxGeom &src, const double *pts, int64_t npts, std::vector<int32_t> &ptr,
-               std::vector<int32_t> &idx, std::vector<double> &w, int64_t src_node_offset);
+int mesh_tensor(const TensorGrid &g, BoxMesh &m);
+void tensor_prolongation(const TensorGrid &f, const std::vector<Lin1> *map, std::vector<int32_t> &ptr,
+                         std::vector<int32_t> &idx, std::vector<double> &w, int64_t coarse_offset, const int *nc);
 void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx,
                    const std::vector<double> &w, std::vector<int32_t> &tptr, std::vector<int32_t> &tidx,
                    std::vector<double> &tw);

@@ -158,7 +158,7 @@ constexpr int kBjWarps = 4;
 
 template <typename T>
 __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T *__restrict__ vals,
-                                                              T *__restrict__ dinv)
+                                                              T *__restrict__ dinv, int l1)
 {
   __shared__ T M[kBjWarps][18][37];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -171,6 +171,26 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
       M[warp][r][c] = (c < 18) ? D[r * 18 + c] : ((c - 18 == r) ? T(1) : T(0));
     }
   __syncwarp();
+  if (l1)
+    {
+      // l1 block-Jacobi: row r's diagonal grows by the absolute sum of its entries outside
+      // the diagonal block (with the diagonal's sign), which makes the smoother convergent
+      // for every symmetric positive definite matrix, mass-dominated ones included
+      if (lane < 18)
+        {
+          T sum = 0;
+          for (int32_t b = m.rowptr[n]; b < m.rowptr[n + 1]; ++b)
+            {
+              if (b == m.diag[n]) continue;
+              const T *row = vals + static_cast<int64_t>(b) * 324 + lane * 18;
+#pragma unroll
+              for (int c = 0; c < 18; ++c) sum += fabs(row[c]);
+            }
+          const T d = M[warp][lane][lane];
+          M[warp][lane][lane] = d + (d < T(0) ? -sum : sum);
+        }
+      __syncwarp();
+    }
   bool singular = false;
   for (int k = 0; k < 18; ++k)
     {
@@ -250,16 +270,17 @@ __global__ void k_bj_setup2(DevMesh m, const T *__restrict__ vals, T *__restrict
     }
 }
 
-cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s)
+cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s, bool l1)
 {
   if (m.B == 18)
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kBjWarps - 1) / kBjWarps);
       if (fp32)
-        k_bj_setup18<float><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv));
+        k_bj_setup18<float><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv),
+                                                           l1 ? 1 : 0);
       else
         k_bj_setup18<double><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
-                                                            static_cast<double *>(dinv));
+                                                            static_cast<double *>(dinv), l1 ? 1 : 0);
     }
   else
     {

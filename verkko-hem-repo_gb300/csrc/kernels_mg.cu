@@ -3,10 +3,10 @@
 // Transfers are node-level CSR gathers applied to all B components of a node:
 //   prolongation   z_fine[n][c]  += sum_j w_j z_coarse[idx_j][c]   (trilinear, P)
 //   restriction    r_coarse[i][c] = sum_j w_j r_fine[idx_j][c]     (P^T, transposed CSR)
-//   state transfer x_coarse[i][c] = sum_j w_j x_fine[idx_j][c]     (trilinear from the finer grid)
 // Constrained components (zero-Dirichlet, hanging) are left alone on the way up and
 // zeroed on the way down, so every Krylov vector keeps zeros there.
-// The coarsest level (1 cell per axis, 8 nodes, 144 unknowns per instance) is inverted
+// Coarse Jacobians are Galerkin products P^T J P, one CTA per coarse block row.  The
+// coarsest level (1 cell per axis, 8 nodes, 144 unknowns per instance) is inverted
 // densely once per Newton step: one CTA per instance, Gauss-Jordan in shared memory.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -49,16 +49,53 @@ __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr,
   rc[t] = s;
 }
 
-__global__ void k_interp_state(int64_t nn_c, int B, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
-                               const double *__restrict__ w, const double *__restrict__ xf, double *__restrict__ xc)
+constexpr int kBlk = 324;         // 18 x 18 block
+constexpr int kGalThreads = 352; // 11 warps: thread e owns entry e of every block
+
+template <typename T>
+__global__ void __launch_bounds__(kGalThreads)
+  k_galerkin(const int32_t *__restrict__ rowptr_c, const int32_t *__restrict__ cols_c,
+             const uint32_t *__restrict__ mask_c, T *__restrict__ vals_c, const int32_t *__restrict__ r_ptr,
+             const int32_t *__restrict__ r_idx, const T *__restrict__ r_w, const int32_t *__restrict__ rowptr_f,
+             const int32_t *__restrict__ cols_f, const T *__restrict__ vals_f, const int32_t *__restrict__ p_ptr,
+             const T *__restrict__ p_w, const int64_t *__restrict__ g_ptr, const uint8_t *__restrict__ g_slot,
+             const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
 {
-  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= nn_c * B) return;
-  const int64_t n = t / B;
-  const int c = static_cast<int>(t % B);
-  double s = 0;
-  for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * xf[static_cast<int64_t>(idx[k]) * B + c];
-  xc[t] = s;
+  extern __shared__ __align__(16) unsigned char g_smem[];
+  T *acc = reinterpret_cast<T *>(g_smem); // [row blocks][324]
+  const int64_t I = blockIdx.x;
+  if (act && !act[node_inst_c[I]]) return;
+  const int e = threadIdx.x;
+  const int32_t b0 = rowptr_c[I];
+  const int ns = rowptr_c[I + 1] - b0;
+  for (int t = e; t < ns * kBlk; t += kGalThreads) acc[t] = T(0);
+  __syncthreads();
+  if (e < kBlk)
+    {
+      const uint8_t *slot = g_slot + g_ptr[I];
+      int t = 0;
+      for (int32_t k = r_ptr[I]; k < r_ptr[I + 1]; ++k)
+        {
+          const int32_t i = r_idx[k];
+          const T wi = r_w[k];
+          for (int32_t b = rowptr_f[i]; b < rowptr_f[i + 1]; ++b)
+            {
+              const int32_t j = cols_f[b];
+              const T v = wi * vals_f[static_cast<int64_t>(b) * kBlk + e];
+              for (int32_t q = p_ptr[j]; q < p_ptr[j + 1]; ++q, ++t) acc[slot[t] * kBlk + e] += p_w[q] * v;
+            }
+        }
+    }
+  __syncthreads();
+  const uint32_t mI = mask_c[I];
+  for (int t = e; t < ns * kBlk; t += kGalThreads)
+    {
+      const int s = t / kBlk, el = t - s * kBlk, a = el / 18, bb = el - a * 18;
+      const int32_t J = cols_c[b0 + s];
+      T v = acc[t];
+      if (((mI >> a) & 1u) || ((mask_c[J] >> bb) & 1u)) v = (J == I && a == bb) ? T(1) : T(0);
+      vals_c[static_cast<int64_t>(b0 + s) * kBlk + el] = v;
+    }
 }
 
 template <typename T>
@@ -97,20 +134,43 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_interp_state(int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const double *w,
-                                const double *xf, double *xc, cudaStream_t s)
+template <typename T>
+cudaError_t launch_galerkin_t(int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c, const uint32_t *mask_c,
+                              void *vals_c, const int32_t *r_ptr, const int32_t *r_idx, const void *r_w,
+                              const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f, const int32_t *p_ptr,
+                              const void *p_w, const int64_t *g_ptr, const uint8_t *g_slot, int max_row_blocks_c,
+                              const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s)
 {
-  const int64_t n = nn_c * B;
-  k_interp_state<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(nn_c, B, ptr, idx, w, xf, xc);
+  const size_t sm = static_cast<size_t>(max_row_blocks_c) * kBlk * sizeof(T);
+  if (sm > 200 * 1024 || nn_c > 0x7fffffff) return cudaErrorInvalidValue;
+  if (nn_c == 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_galerkin<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  k_galerkin<T><<<static_cast<unsigned>(nn_c), kGalThreads, sm, s>>>(
+    rowptr_c, cols_c, mask_c, static_cast<T *>(vals_c), r_ptr, r_idx, static_cast<const T *>(r_w), rowptr_f, cols_f,
+    static_cast<const T *>(vals_f), p_ptr, static_cast<const T *>(p_w), g_ptr, g_slot, node_inst_c, act);
   return cudaGetLastError();
+}
+
+cudaError_t launch_galerkin(bool fp32, int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c,
+                            const uint32_t *mask_c, void *vals_c, const int32_t *r_ptr, const int32_t *r_idx,
+                            const void *r_w, const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f,
+                            const int32_t *p_ptr, const void *p_w, const int64_t *g_ptr, const uint8_t *g_slot,
+                            int max_row_blocks_c, const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s)
+{
+  return fp32 ? launch_galerkin_t<float>(nn_c, rowptr_c, cols_c, mask_c, vals_c, r_ptr, r_idx, r_w, rowptr_f, cols_f,
+                                         vals_f, p_ptr, p_w, g_ptr, g_slot, max_row_blocks_c, node_inst_c, act, s)
+              : launch_galerkin_t<double>(nn_c, rowptr_c, cols_c, mask_c, vals_c, r_ptr, r_idx, r_w, rowptr_f, cols_f,
+                                          vals_f, p_ptr, p_w, g_ptr, g_slot, max_row_blocks_c, node_inst_c, act, s);
 }
 
 // ---------------------------------------------------------------------------------
 // coarsest level (one cell per axis: 8 nodes, 144 unknowns per instance): dense inverse
-// in shared memory, FP32, one CTA per instance.  It is a preconditioner component, so
+// of the slightly shifted matrix in shared memory, FP32, one CTA per instance.  It is a preconditioner component, so
 // FP32 suffices in both precision modes (the outer flexible GMRES is exact).
 // ---------------------------------------------------------------------------------
 constexpr int kGjThreads = 512;
+constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest solve
 
 template <typename T>
 __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T *__restrict__ vals,
@@ -122,6 +182,7 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
   __shared__ int s_idx[kGjThreads / 32];
   __shared__ int s_piv;
   __shared__ int s_sing;
+  __shared__ float s_shift;
   const int inst = blockIdx.x;
   const int64_t n0 = m.node_off_ptr[inst], n1 = m.node_off_ptr[inst + 1];
   const int B = m.B;
@@ -149,7 +210,17 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       const int row = static_cast<int>((lo - n0) * B + cr), col = static_cast<int>((m.cols[blk] - n0) * B + cd);
       W[row * ld + col] = static_cast<float>(vals[blk * B * B + e]);
     }
-  if (tid == 0) s_sing = 0;
+  if (tid == 0)
+    {
+      s_sing = 0;
+      float sd = 0.f;
+      for (int i = 0; i < nd; ++i) sd += fabsf(W[i * ld + i]);
+      s_shift = nd > 0 ? kCoarseShift * sd / static_cast<float>(nd) : 0.f;
+    }
+  __syncthreads();
+  // near-null modes (global phase and spin rotations near a solution) would be amplified
+  // without bound by an exact inverse: invert A + shift * mean|diag| * I instead
+  for (int i = tid; i < nd; i += kGjThreads) W[i * ld + i] += s_shift;
   __syncthreads();
   for (int k = 0; k < nd; ++k)
     {

@@ -1,13 +1,15 @@
-// Host side of the geometric multigrid preconditioner: level meshes and the
-// inter-level operators, built once per mesh.
+// Host side of the geometric multigrid preconditioner: level grids, inter-level transfer
+// operators and the tables of the Galerkin products, built once per mesh.
 //
 // The reference preconditions its Krylov solve with Trilinos ML AMG
-// (femgl/src/solve.cc:141-152).  Here every instance of a context that is an
-// axis-aligned box with a uniform tensor grid (no hanging nodes) gets a hierarchy of
-// coarser box grids with ceil(n/2) cells per axis, down to one cell per axis.  Coarse
-// operators are rediscretised (the same assembly kernels on the coarse grid, at the
-// state interpolated from the finer level); corrections move between levels by
-// trilinear interpolation P (coarse -> fine) and its transpose (fine -> coarse).
+// (femgl/src/solve.cc:141-152).  Here every instance of a context that is an axis-aligned
+// box with a tensor grid (no hanging nodes) gets a hierarchy of nested coarser tensor
+// grids: a coarsened axis keeps every other node line and the last one.  Prolongation P
+// is the tensor product of 1D linear interpolation along the axes, restriction is P^T,
+// and the coarse Jacobians are the Galerkin products P^T J P (formed on the GPU after each
+// fine assembly), so every coarse operator is consistent with the fine Jacobian.  An axis
+// whose spacing is more than twice the smallest one is left alone until the others catch
+// up (semi-coarsening), so anisotropic slabs become isotropic before full coarsening.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -18,10 +20,40 @@ namespace glgpu
 {
 namespace
 {
-// node id of lattice point (i, j, k) on a box grid with n cells per axis (mesh_box order)
+// node id of lattice point (i, j, k) on a tensor grid with n cells per axis (mesh_box order)
 inline int64_t grid_node(const int *n, int64_t i, int64_t j, int64_t k)
 {
   return (k * (n[1] + 1) + j) * (n[0] + 1) + i;
+}
+
+// Coarse lines of one axis and the interpolation of every fine line from them.
+void line_map(const std::vector<double> &xf, bool coarsen, std::vector<double> &xc, std::vector<Lin1> &map)
+{
+  const int nf = static_cast<int>(xf.size()) - 1;
+  xc.clear();
+  map.assign(nf + 1, Lin1{});
+  if (!coarsen)
+    {
+      xc = xf;
+      for (int i = 0; i <= nf; ++i) map[i] = Lin1{1, {i, 0}, {1.0, 0.0}};
+      return;
+    }
+  for (int i = 0; i <= nf; i += 2) xc.push_back(xf[i]);
+  if (nf % 2) xc.push_back(xf[nf]);
+  const int nc = static_cast<int>(xc.size()) - 1;
+  for (int i = 0; i <= nf; ++i)
+    {
+      if (i % 2 == 0)
+        map[i] = Lin1{1, {i / 2, 0}, {1.0, 0.0}};
+      else if (i == nf)
+        map[i] = Lin1{1, {nc, 0}, {1.0, 0.0}};
+      else
+        {
+          const int a = (i - 1) / 2, b = a + 1;
+          const double t = (xf[i] - xc[a]) / (xc[b] - xc[a]);
+          map[i] = Lin1{2, {a, b}, {1.0 - t, t}};
+        }
+    }
 }
 } // namespace
 
@@ -73,39 +105,46 @@ bool infer_box(const glgpu_mesh &m, BoxGeom &g)
   return true;
 }
 
-// trilinear interpolation from box grid `src` to the given points: CSR over points
-void trilinear(const BoxGeom &src, const double *pts, int64_t npts, std::vector<int32_t> &ptr,
-               std::vector<int32_t> &idx, std::vector<double> &w, int64_t src_node_offset)
+// Hexahedral mesh of a tensor grid: nodes in (k, j, i) lexicographic order, cells in
+// deal.II vertex order, zero-Dirichlet masks on the faces of the axes flagged in dir.
+int mesh_tensor(const TensorGrid &g, BoxMesh &m)
 {
-  ptr.assign(npts + 1, 0);
-  idx.clear();
-  w.clear();
-  double h[3];
-  for (int d = 0; d < 3; ++d) h[d] = (src.hi[d] - src.lo[d]) / src.n[d];
-  for (int64_t p = 0; p < npts; ++p)
+  int n[3];
+  for (int d = 0; d < 3; ++d)
     {
-      int64_t cell[3];
-      double t[3];
-      for (int d = 0; d < 3; ++d)
-        {
-          const double u = (pts[3 * p + d] - src.lo[d]) / h[d];
-          int64_t c0 = static_cast<int64_t>(std::floor(u));
-          c0 = std::min<int64_t>(std::max<int64_t>(c0, 0), src.n[d] - 1);
-          cell[d] = c0;
-          t[d] = std::min(1.0, std::max(0.0, u - static_cast<double>(c0)));
-        }
-      for (int v = 0; v < 8; ++v)
-        {
-          double wt = 1.0;
-          for (int d = 0; d < 3; ++d) wt *= ((v >> d) & 1) ? t[d] : 1.0 - t[d];
-          if (wt < 1e-14) continue;
-          idx.push_back(static_cast<int32_t>(src_node_offset +
-                                             grid_node(src.n, cell[0] + (v & 1), cell[1] + ((v >> 1) & 1),
-                                                       cell[2] + ((v >> 2) & 1))));
-          w.push_back(wt);
-        }
-      ptr[p + 1] = static_cast<int32_t>(idx.size());
+      n[d] = static_cast<int>(g.x[d].size()) - 1;
+      if (n[d] < 1) return -1;
     }
+  const int64_t nn = static_cast<int64_t>(n[0] + 1) * (n[1] + 1) * (n[2] + 1);
+  const int64_t nc = static_cast<int64_t>(n[0]) * n[1] * n[2];
+  if (nn > INT32_MAX / 32 || nc > INT32_MAX / 8) return -1;
+  m.nn = static_cast<int>(nn);
+  m.nc = static_cast<int>(nc);
+  m.xyz.resize(nn * 3);
+  m.mask.assign(nn, 0u);
+  for (int k = 0; k <= n[2]; ++k)
+    for (int j = 0; j <= n[1]; ++j)
+      for (int i = 0; i <= n[0]; ++i)
+        {
+          const int64_t id = grid_node(n, i, j, k);
+          m.xyz[3 * id + 0] = g.x[0][i];
+          m.xyz[3 * id + 1] = g.x[1][j];
+          m.xyz[3 * id + 2] = g.x[2][k];
+          const int c3[3] = {i, j, k};
+          for (int d = 0; d < 3; ++d)
+            if (g.dir[d] && (c3[d] == 0 || c3[d] == n[d])) m.mask[id] |= column_mask(d);
+        }
+  m.cells.resize(nc * 8);
+  int64_t e = 0;
+  for (int k = 0; k < n[2]; ++k)
+    for (int j = 0; j < n[1]; ++j)
+      for (int i = 0; i < n[0]; ++i, ++e)
+        for (int v = 0; v < 8; ++v)
+          m.cells[e * 8 + v] = static_cast<int32_t>(grid_node(n, i + (v & 1), j + ((v >> 1) & 1), k + ((v >> 2) & 1)));
+  m.hptr.assign(nn + 1, 0);
+  m.hpar.clear();
+  m.hw.clear();
+  return 0;
 }
 
 void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx,
@@ -128,37 +167,84 @@ void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr
       }
 }
 
-// Levels below the instance meshes: level l+1 halves (rounding up) every axis of level l,
-// down to one cell per axis.  All instances must be uniform boxes; returns the number of
-// coarse levels (0 when multigrid does not apply).
+// Prolongation of one instance from level grid `c` to the next finer grid `f` (local node
+// ids): the tensor product of the per-axis maps.
+void tensor_prolongation(const TensorGrid &f, const std::vector<Lin1> *map, std::vector<int32_t> &ptr,
+                         std::vector<int32_t> &idx, std::vector<double> &w, int64_t coarse_offset, const int *nc)
+{
+  int nf[3];
+  for (int d = 0; d < 3; ++d) nf[d] = static_cast<int>(f.x[d].size()) - 1;
+  ptr.assign(1, 0);
+  idx.clear();
+  w.clear();
+  for (int k = 0; k <= nf[2]; ++k)
+    for (int j = 0; j <= nf[1]; ++j)
+      for (int i = 0; i <= nf[0]; ++i)
+        {
+          const Lin1 &a = map[0][i], &b = map[1][j], &cz = map[2][k];
+          for (int r = 0; r < cz.n; ++r)
+            for (int q = 0; q < b.n; ++q)
+              for (int p = 0; p < a.n; ++p)
+                {
+                  idx.push_back(static_cast<int32_t>(coarse_offset + grid_node(nc, a.c[p], b.c[q], cz.c[r])));
+                  w.push_back(a.w[p] * b.w[q] * cz.w[r]);
+                }
+          ptr.push_back(static_cast<int32_t>(idx.size()));
+        }
+}
+
+// Levels below the instance meshes, down to one cell per axis.  All instances must be
+// tensor box grids; returns the number of coarse levels (0 when multigrid does not apply).
 int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vector<MgLevel> &levels,
                     std::string &why)
 {
   levels.clear();
-  std::vector<BoxGeom> geo(n_inst);
+  std::vector<TensorGrid> cur(n_inst);
   for (int k = 0; k < n_inst; ++k)
-    if (!infer_box(mesh[k], geo[k]))
-      {
-        why = "instance " + std::to_string(k) + " is not a uniform box grid";
-        return 0;
-      }
-  std::vector<BoxGeom> cur = geo;
+    {
+      BoxGeom g;
+      if (!infer_box(mesh[k], g))
+        {
+          why = "instance " + std::to_string(k) + " is not a uniform box grid";
+          return 0;
+        }
+      for (int d = 0; d < 3; ++d)
+        {
+          cur[k].x[d].resize(g.n[d] + 1);
+          for (int i = 0; i <= g.n[d]; ++i)
+            cur[k].x[d][i] = (i == g.n[d]) ? g.hi[d] : g.lo[d] + (g.hi[d] - g.lo[d]) * i / g.n[d];
+          cur[k].dir[d] = g.dir[d];
+        }
+    }
   for (int l = 0; l < max_levels; ++l)
     {
       bool all_min = true;
       for (auto &g : cur)
         for (int d = 0; d < 3; ++d)
-          if (g.n[d] > 1) all_min = false;
+          if (g.x[d].size() > 2) all_min = false;
       if (all_min) break;
       MgLevel L;
-      L.geom.resize(n_inst);
+      L.grid.resize(n_inst);
       L.meshes.resize(n_inst);
+      L.map.resize(n_inst);
       for (int k = 0; k < n_inst; ++k)
         {
-          BoxGeom c = cur[k];
-          for (int d = 0; d < 3; ++d) c.n[d] = std::max(1, (cur[k].n[d] + 1) / 2);
-          L.geom[k] = c;
-          if (mesh_box(c.lo, c.hi, c.n, 0.0, c.dir, L.meshes[k]) != 0)
+          const TensorGrid &f = cur[k];
+          double h[3], hmin = 1e300;
+          for (int d = 0; d < 3; ++d)
+            {
+              h[d] = f.x[d].size() > 2 ? f.x[d][1] - f.x[d][0] : 1e300;
+              hmin = std::min(hmin, h[d]);
+            }
+          TensorGrid c;
+          for (int d = 0; d < 3; ++d)
+            {
+              const bool coarsen = f.x[d].size() > 2 && h[d] < 2.0 * hmin;
+              line_map(f.x[d], coarsen, c.x[d], L.map[k][d]);
+              c.dir[d] = f.dir[d];
+            }
+          L.grid[k] = c;
+          if (mesh_tensor(c, L.meshes[k]) != 0)
             {
               why = "coarse mesh generation failed";
               levels.clear();
@@ -166,7 +252,7 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
             }
         }
       levels.push_back(std::move(L));
-      cur = levels.back().geom;
+      cur = levels.back().grid;
     }
   return static_cast<int>(levels.size());
 }

@@ -94,6 +94,11 @@ def lib() -> ctypes.CDLL:
     L.glgpu_timers.argtypes = [vp, _dp, ctypes.c_int]
     L.glgpu_kernel_timing.argtypes = [vp, ctypes.c_int, _dp, _lp, ctypes.c_int]
     L.glgpu_mg_levels.argtypes = [vp]
+    L.glgpu_mg_fallbacks.argtypes = [vp]
+    L.glgpu_mg_fallbacks.restype = ctypes.c_int64
+    L.glgpu_mg_level_info.argtypes = [vp, ctypes.c_int, _lp, _lp, _lp]
+    L.glgpu_mg_level_system.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
+    L.glgpu_mg_prolongation.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
     L.glgpu_launch_count.argtypes = [vp]
     L.glgpu_launch_count.restype = ctypes.c_int64
     L.glgpu_sync.argtypes = [vp]
@@ -271,7 +276,7 @@ class Params:
     damped: bool = True
     mg_pre: int = 2
     mg_post: int = 2
-    mg_omega: float = 0.7
+    mg_omega: float = 1.0
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -432,6 +437,32 @@ class FemGL:
     @property
     def mg_levels(self) -> int:
         return int(lib().glgpu_mg_levels(self._ctx))
+
+    def mg_level(self, level: int):
+        """(rowptr, cols, vals [nnzb][B][B], P as (ptr, idx, w)) of coarse level `level`."""
+        L = lib()
+        nn, nb, pn = np.zeros(1, np.int64), np.zeros(1, np.int64), np.zeros(1, np.int64)
+        _check(L.glgpu_mg_level_info(self._ctx, int(level), _p(nn, _lp), _p(nb, _lp), _p(pn, _lp)))
+        rowptr = np.zeros(nn[0] + 1, np.int32)
+        cols = np.zeros(nb[0], np.int32)
+        vals = np.zeros((nb[0], self.block, self.block))
+        _check(L.glgpu_mg_level_system(self._ctx, int(level), _p(rowptr, _ip), _p(cols, _ip), _p(vals)))
+        # prolongation rows are the nodes of the next finer level
+        nf = self.n_nodes if level == 1 else int(self.mg_level_sizes(level - 1)[0])
+        ptr = np.zeros(nf + 1, np.int32)
+        idx = np.zeros(pn[0], np.int32)
+        w = np.zeros(pn[0])
+        _check(L.glgpu_mg_prolongation(self._ctx, int(level), _p(ptr, _ip), _p(idx, _ip), _p(w)))
+        return rowptr, cols, vals, (ptr, idx, w)
+
+    def mg_level_sizes(self, level: int):
+        nn, nb, pn = np.zeros(1, np.int64), np.zeros(1, np.int64), np.zeros(1, np.int64)
+        _check(lib().glgpu_mg_level_info(self._ctx, int(level), _p(nn, _lp), _p(nb, _lp), _p(pn, _lp)))
+        return int(nn[0]), int(nb[0]), int(pn[0])
+
+    @property
+    def mg_fallbacks(self) -> int:
+        return int(lib().glgpu_mg_fallbacks(self._ctx))
 
     def sync(self) -> None:
         _check(lib().glgpu_sync(self._ctx))
