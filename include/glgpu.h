@@ -98,7 +98,7 @@ typedef struct
   double ls_step;       /* "primary step length of dampped newton iteration", 0.83 */
   int ls_max_trials;    /* trials of the backtracking line search, 100 (iteration.cc:170) */
   int damped;           /* "Using dampped Newton iteration" (1) or full Newton (0) */
-  int mg_pre, mg_post;  /* multigrid: damped block-Jacobi sweeps before / after the coarse correction */
+  int mg_pre, mg_post;  /* multigrid: l1 block-Jacobi sweeps before / after the coarse correction (1, 1) */
   double mg_omega;      /* multigrid: damping of the l1 block-Jacobi smoother (default 1) */
 } glgpu_params;
 

@@ -145,16 +145,14 @@ cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, c
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
                             const uint8_t *act, cudaStream_t s);
-// Galerkin product J_c = P^T J_f P restricted to the coarse block pattern, one CTA per
-// coarse block row; slot[] lists, in loop order, the coarse slot of every (restriction
-// entry, fine block, prolongation entry) triple of the row.  Zero-Dirichlet rows and
-// columns of the coarse level become identity rows/zero columns.
-cudaError_t launch_galerkin(bool fp32, int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c,
-                            const uint32_t *mask_c, void *vals_c, const int32_t *r_ptr, const int32_t *r_idx,
-                            const void *r_w, const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f,
-                            const int32_t *p_ptr, const void *p_w, const int64_t *g_ptr,
-                            const uint8_t *g_slot, int max_row_blocks_c, const int32_t *node_inst_c,
-                            const uint8_t *act, cudaStream_t s);
+// Galerkin product J_c = P^T J_f P on the coarse block pattern, one warp per coarse
+// block: block cb (row g_row[cb], column cols_c[cb]) is the sum over its term list
+// [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and
+// columns of the coarse level become identity rows / zero columns.
+cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
+                            const uint32_t *mask_c, void *vals_c, const int64_t *g_toff, const int32_t *g_blk,
+                            const void *g_w, const void *vals_f, const int32_t *node_inst_c, const uint8_t *act,
+                            cudaStream_t s);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

@@ -118,8 +118,10 @@ struct glgpu_ctx
   {
     int32_t *p_ptr = nullptr, *p_idx = nullptr, *r_ptr = nullptr, *r_idx = nullptr;
     void *p_w = nullptr, *r_w = nullptr; // T weights
-    int64_t *g_ptr = nullptr;            // Galerkin slot table of each coarse row
-    uint8_t *g_slot = nullptr;
+    // Galerkin terms of every coarse block: [g_toff[cb], g_toff[cb+1]) of (fine block, weight)
+    int64_t *g_toff = nullptr;
+    int32_t *g_row = nullptr, *g_blk = nullptr;
+    void *g_w = nullptr;
     std::vector<int32_t> h_ptr, h_idx;   // host copy of P
     std::vector<double> h_w;
   };
@@ -130,6 +132,7 @@ struct glgpu_ctx
   int max_nd = 0;
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
+  std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   int64_t mg_fallbacks = 0;          // solves handed from multigrid to block-Jacobi
 };
 
@@ -716,9 +719,8 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
       glgpu_ctx *L = c->lv[l];
       const glgpu_ctx::Transfer &t = c->tr[l];
       CKS(launch(c, KK_PREC, 1, [&] {
-        return launch_galerkin(c->mixed, L->nn, L->dm.rowptr, L->dm.cols, L->dm.mask, L->vals, t.r_ptr, t.r_idx, t.r_w,
-                               F->dm.rowptr, F->dm.cols, F->vals, t.p_ptr, t.p_w, t.g_ptr, t.g_slot,
-                               L->P.max_row_blocks, L->dm.node_inst, act, c->st);
+        return launch_galerkin(c->mixed, L->nnzb, t.g_row, L->dm.cols, L->dm.mask, L->vals, t.g_toff, t.g_blk, t.g_w,
+                               F->vals, L->dm.node_inst, act, c->st);
       }));
       CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st, true); }));
       L->has_J = true;
@@ -848,12 +850,18 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       std::vector<int32_t> rp, ri;
       std::vector<double> rw;
       transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
-      // slot of every (restriction entry, fine block, prolongation entry) of each coarse row
-      std::vector<int64_t> gp(CP.nn + 1, 0);
-      std::vector<uint8_t> gs;
+      // Galerkin terms, grouped by coarse block: every (restriction entry i of row I,
+      // fine block (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to
+      // block (I, J); fine blocks come in increasing order within each list
+      std::vector<int64_t> gt(static_cast<size_t>(CP.nnzb) + 1, 0);
+      std::vector<int32_t> grow(CP.nnzb), gb;
+      std::vector<double> gw;
+      std::vector<std::vector<std::pair<int32_t, double>>> slot_terms(CP.max_row_blocks);
       for (int64_t I = 0; I < CP.nn; ++I)
         {
-          const int32_t *c0 = CP.cols.data() + CP.rowptr[I], *c1 = CP.cols.data() + CP.rowptr[I + 1];
+          const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
+          const int32_t *c0 = CP.cols.data() + b0, *c1 = c0 + ns;
+          for (int s = 0; s < ns; ++s) slot_terms[s].clear();
           for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
             {
               const int32_t i = ri[k];
@@ -864,13 +872,21 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
                     {
                       const int32_t *f = std::find(c0, c1, pi[q]);
                       if (f == c1) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
-                      gs.push_back(static_cast<uint8_t>(f - c0));
+                      slot_terms[f - c0].emplace_back(b, rw[k] * pw[q]);
                     }
                 }
             }
-          gp[I + 1] = static_cast<int64_t>(gs.size());
+          for (int s = 0; s < ns; ++s)
+            {
+              grow[b0 + s] = static_cast<int32_t>(I);
+              for (const auto &tw : slot_terms[s])
+                {
+                  gb.push_back(tw.first);
+                  gw.push_back(tw.second);
+                }
+              gt[b0 + s + 1] = static_cast<int64_t>(gb.size());
+            }
         }
-      if (CP.max_row_blocks > 255) return set_error(GLGPU_ERR_ARG, "multigrid: coarse rows too long");
       glgpu_ctx::Transfer &t = c->tr[l];
       t.h_ptr = pp;
       t.h_idx = pi;
@@ -879,17 +895,20 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       CKS(dupload(c, &t.p_idx, pi));
       CKS(dupload(c, &t.r_ptr, rp));
       CKS(dupload(c, &t.r_idx, ri));
-      CKS(dupload(c, &t.g_ptr, gp));
-      CKS(dupload(c, &t.g_slot, gs));
+      CKS(dupload(c, &t.g_toff, gt));
+      CKS(dupload(c, &t.g_row, grow));
+      CKS(dupload(c, &t.g_blk, gb));
       if (c->mixed)
         {
           CKS(upload_w<float>(c, &t.p_w, pw));
           CKS(upload_w<float>(c, &t.r_w, rw));
+          CKS(upload_w<float>(c, &t.g_w, gw));
         }
       else
         {
           CKS(upload_w<double>(c, &t.p_w, pw));
           CKS(upload_w<double>(c, &t.r_w, rw));
+          CKS(upload_w<double>(c, &t.g_w, gw));
         }
     }
   // coarsest level: dense inverses
@@ -942,8 +961,8 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->ls_step = 0.83;
   p->ls_max_trials = 100;
   p->damped = 1;
-  p->mg_pre = 2;
-  p->mg_post = 2;
+  p->mg_pre = 1;
+  p->mg_post = 1;
   p->mg_omega = 1.0;
 }
 
@@ -1139,6 +1158,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   c->rhs_norm.assign(n_inst, 0.0);
   c->res_norm.assign(n_inst, 0.0);
   c->inst_on.assign(n_inst, 1);
+  c->r_ok.assign(n_inst, 0);
   cudaEventCreate(&c->ev_user0);
   cudaEventCreate(&c->ev_user1);
   if (prm[0].precond == GLGPU_PC_MULTIGRID && P.dim == 3)
@@ -1197,6 +1217,7 @@ extern "C" glgpu_status glgpu_set_solution(glgpu_ctx *c, const double *x)
   CK(launch_distribute(c->dm, c->x, c->st));
   c->launches += 2;
   c->has_J = c->has_rhs = c->has_delta = false;
+  std::fill(c->r_ok.begin(), c->r_ok.end(), 0);
   return sync(c);
 }
 
@@ -1211,17 +1232,28 @@ extern "C" glgpu_status glgpu_get_solution(const glgpu_ctx *c, double *x)
 static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
 {
   PhaseScope ps(c, PH_ASM);
+  // the line search of the previous Newton step already evaluated R at the accepted
+  // state (same kernels, same x): reuse it instead of recomputing the FP64 residual
+  bool need_r = false;
+  for (int k = 0; k < c->n_inst; ++k)
+    if ((!act || c->inst_on[k]) && !c->r_ok[k]) need_r = true;
   if (!c->mixed)
     {
-      CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, false, c->x, c->H, c->r_cell, c->e_cell, act, c->st); }));
+      CKS(launch(c, KK_CELL, 1, [&] {
+        return launch_cell(c->dm, false, c->x, c->H, need_r ? c->r_cell : nullptr, need_r ? c->e_cell : nullptr, act,
+                           c->st);
+      }));
     }
   else
     {
       CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
-      CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, c->e_cell, act, c->st); }));
+      if (need_r)
+        CKS(launch(c, KK_RES, 1, [&] {
+          return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, c->e_cell, act, c->st);
+        }));
     }
   CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
-  CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
+  if (need_r) CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   CKS(axpby(c, c->R, c->rhs, nullptr, coefs(-1.0, 0.0), act, false, false, false));
   if (c->n_levels > 0) CKS(mg_assemble(c, act));
   std::vector<double> nr;
@@ -1229,6 +1261,8 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
   for (int k = 0; k < c->n_inst; ++k)
     if (!act || c->inst_on[k]) c->rhs_norm[k] = nr[k];
   c->has_J = c->has_rhs = true;
+  for (int k = 0; k < c->n_inst; ++k)
+    if (!act || c->inst_on[k]) c->r_ok[k] = 1;
   c->prec_ready = false;
   for (int k = 0; k < c->n_inst; ++k)
     if ((!act || c->inst_on[k]) && !std::isfinite(c->rhs_norm[k]))
@@ -1251,6 +1285,7 @@ extern "C" glgpu_status glgpu_compute_residual(glgpu_ctx *c, double *norm)
   {
     PhaseScope ps(c, PH_RES);
     CKS(residual_at(c, c->x, nullptr));
+    std::fill(c->r_ok.begin(), c->r_ok.end(), 1);
   }
   std::vector<double> nr;
   CKS(norms_d(c, c->R, nullptr, nr));
@@ -1291,6 +1326,8 @@ static glgpu_status newton_impl(glgpu_ctx *c, std::vector<double> &res, std::vec
   const int max_trials = p0.damped ? std::max(1, p0.ls_max_trials) : 1;
   std::vector<uint8_t> pending(c->inst_on);
   std::vector<double> cur(n, 0.0), a(n, 0.0);
+  for (int k = 0; k < n; ++k)
+    if (c->inst_on[k]) c->r_ok[k] = 0; // the trials overwrite R
   res.assign(n, 0.0);
   trials.assign(n, 0);
   for (int i = 0; i < max_trials; ++i)
@@ -1327,6 +1364,9 @@ static glgpu_status newton_impl(glgpu_ctx *c, std::vector<double> &res, std::vec
         c->res_norm[k] = cur[k];
       }
   c->has_J = c->has_rhs = c->has_delta = false;
+  // R, r_cell, e_cell now hold the values at the new x of every instance of the step
+  for (int k = 0; k < n; ++k)
+    if (c->inst_on[k]) c->r_ok[k] = 1;
   for (int k = 0; k < n; ++k)
     if (c->inst_on[k] && !std::isfinite(res[k]))
       return set_error(GLGPU_ERR_NAN, "newton_iteration: non-finite residual in instance " + std::to_string(k));
@@ -1348,6 +1388,7 @@ extern "C" glgpu_status glgpu_free_energy(glgpu_ctx *c, double *F)
 {
   if (!c || !F) return set_error(GLGPU_ERR_ARG, "glgpu_free_energy: NULL argument");
   CKS(residual_at(c, c->x, nullptr));
+  std::fill(c->r_ok.begin(), c->r_ok.end(), 1);
   CKS(launch(c, KK_VEC, 1, [&] { return launch_cell_sum(c->dm, c->e_cell, c->d_energy, c->st); }));
   CK(cudaMemcpyAsync(c->h_norm, c->d_energy, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
   CKS(sync(c));

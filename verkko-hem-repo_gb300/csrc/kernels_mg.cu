@@ -5,7 +5,7 @@
 //   restriction    r_coarse[i][c] = sum_j w_j r_fine[idx_j][c]     (P^T, transposed CSR)
 // Constrained components (zero-Dirichlet, hanging) are left alone on the way up and
 // zeroed on the way down, so every Krylov vector keeps zeros there.
-// Coarse Jacobians are Galerkin products P^T J P, one CTA per coarse block row.  The
+// Coarse Jacobians are Galerkin products P^T J P, one warp per coarse block.  The
 // coarsest level (1 cell per axis, 8 nodes, 144 unknowns per instance) is inverted
 // densely once per Newton step: one CTA per instance, Gauss-Jordan in shared memory.
 #include <cstdint>
@@ -49,52 +49,92 @@ __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr,
   rc[t] = s;
 }
 
-constexpr int kBlk = 324;         // 18 x 18 block
-constexpr int kGalThreads = 352; // 11 warps: thread e owns entry e of every block
+// Galerkin product: one warp per coarse block (I, J).  The block is
+//   J_c(I, J) = sum over fine blocks (i, j) with P(i, I) P(j, J) != 0 of P(i, I) P(j, J) J_f(i, j),
+// a weighted sum of whole fine blocks whose (block index, weight) list is built on the
+// host once per mesh.  Each fine block is streamed with 128-bit loads; lane l owns the
+// same scalars of every block (the SpMV lane map), so the sum stays in registers.
+constexpr int kGalWarps = 8;
+
+template <typename T> struct GVec;
+template <> struct GVec<float>
+{
+  using type = float4;
+  static constexpr int n = 4;
+};
+template <> struct GVec<double>
+{
+  using type = double2;
+  static constexpr int n = 2;
+};
+__device__ __forceinline__ void gfma(float4 &a, float w, const float4 &v)
+{
+  a.x = fmaf(w, v.x, a.x);
+  a.y = fmaf(w, v.y, a.y);
+  a.z = fmaf(w, v.z, a.z);
+  a.w = fmaf(w, v.w, a.w);
+}
+__device__ __forceinline__ void gfma(double2 &a, double w, const double2 &v)
+{
+  a.x = fma(w, v.x, a.x);
+  a.y = fma(w, v.y, a.y);
+}
+__device__ __forceinline__ float &gcomp(float4 &v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+__device__ __forceinline__ double &gcomp(double2 &v, int k) { return k == 0 ? v.x : v.y; }
 
 template <typename T>
-__global__ void __launch_bounds__(kGalThreads)
-  k_galerkin(const int32_t *__restrict__ rowptr_c, const int32_t *__restrict__ cols_c,
-             const uint32_t *__restrict__ mask_c, T *__restrict__ vals_c, const int32_t *__restrict__ r_ptr,
-             const int32_t *__restrict__ r_idx, const T *__restrict__ r_w, const int32_t *__restrict__ rowptr_f,
-             const int32_t *__restrict__ cols_f, const T *__restrict__ vals_f, const int32_t *__restrict__ p_ptr,
-             const T *__restrict__ p_w, const int64_t *__restrict__ g_ptr, const uint8_t *__restrict__ g_slot,
+__global__ void __launch_bounds__(kGalWarps * 32)
+  k_galerkin(int64_t nnzb_c, const int32_t *__restrict__ g_row, const int32_t *__restrict__ cols_c,
+             const uint32_t *__restrict__ mask_c, T *__restrict__ vals_c, const int64_t *__restrict__ g_toff,
+             const int32_t *__restrict__ g_blk, const T *__restrict__ g_w, const T *__restrict__ vals_f,
              const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
 {
-  extern __shared__ __align__(16) unsigned char g_smem[];
-  T *acc = reinterpret_cast<T *>(g_smem); // [row blocks][324]
-  const int64_t I = blockIdx.x;
+  using V = typename GVec<T>::type;
+  constexpr int NV = GVec<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t cb = static_cast<int64_t>(blockIdx.x) * kGalWarps + warp;
+  if (cb >= nnzb_c) return;
+  const int32_t I = g_row[cb];
   if (act && !act[node_inst_c[I]]) return;
-  const int e = threadIdx.x;
-  const int32_t b0 = rowptr_c[I];
-  const int ns = rowptr_c[I + 1] - b0;
-  for (int t = e; t < ns * kBlk; t += kGalThreads) acc[t] = T(0);
-  __syncthreads();
-  if (e < kBlk)
+  V acc[NIT];
+#pragma unroll
+  for (int k = 0; k < NIT; ++k)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) gcomp(acc[k], q) = T(0);
+  const V *src = reinterpret_cast<const V *>(vals_f);
+  const int64_t t1 = g_toff[cb + 1];
+#pragma unroll 2
+  for (int64_t t = g_toff[cb]; t < t1; ++t)
     {
-      const uint8_t *slot = g_slot + g_ptr[I];
-      int t = 0;
-      for (int32_t k = r_ptr[I]; k < r_ptr[I + 1]; ++k)
+      const V *bp = src + static_cast<int64_t>(__ldg(g_blk + t)) * NCH;
+      const T w = __ldg(g_w + t);
+#pragma unroll
+      for (int k = 0; k < NIT; ++k)
         {
-          const int32_t i = r_idx[k];
-          const T wi = r_w[k];
-          for (int32_t b = rowptr_f[i]; b < rowptr_f[i + 1]; ++b)
-            {
-              const int32_t j = cols_f[b];
-              const T v = wi * vals_f[static_cast<int64_t>(b) * kBlk + e];
-              for (int32_t q = p_ptr[j]; q < p_ptr[j + 1]; ++q, ++t) acc[slot[t] * kBlk + e] += p_w[q] * v;
-            }
+          const int ch = lane + 32 * k;
+          if (ch < NCH) gfma(acc[k], w, __ldg(bp + ch));
         }
     }
-  __syncthreads();
-  const uint32_t mI = mask_c[I];
-  for (int t = e; t < ns * kBlk; t += kGalThreads)
+  // zero-Dirichlet components of the coarse level: identity rows, zero columns
+  const int32_t J = cols_c[cb];
+  const uint32_t mI = mask_c[I], mJ = mask_c[J];
+  V *dst = reinterpret_cast<V *>(vals_c) + cb * NCH;
+#pragma unroll
+  for (int k = 0; k < NIT; ++k)
     {
-      const int s = t / kBlk, el = t - s * kBlk, a = el / 18, bb = el - a * 18;
-      const int32_t J = cols_c[b0 + s];
-      T v = acc[t];
-      if (((mI >> a) & 1u) || ((mask_c[J] >> bb) & 1u)) v = (J == I && a == bb) ? T(1) : T(0);
-      vals_c[static_cast<int64_t>(b0 + s) * kBlk + el] = v;
+      const int ch = lane + 32 * k;
+      if (ch >= NCH) continue;
+      V o = acc[k];
+      if (mI | mJ)
+#pragma unroll
+        for (int q = 0; q < NV; ++q)
+          {
+            const int el = ch * NV + q, a = el / 18, bb = el - 18 * (el / 18);
+            if (((mI >> a) & 1u) || ((mJ >> bb) & 1u)) gcomp(o, q) = (J == I && a == bb) ? T(1) : T(0);
+          }
+      dst[ch] = o;
     }
 }
 
@@ -134,34 +174,23 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_galerkin_t(int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c, const uint32_t *mask_c,
-                              void *vals_c, const int32_t *r_ptr, const int32_t *r_idx, const void *r_w,
-                              const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f, const int32_t *p_ptr,
-                              const void *p_w, const int64_t *g_ptr, const uint8_t *g_slot, int max_row_blocks_c,
-                              const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s)
+cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
+                            const uint32_t *mask_c, void *vals_c, const int64_t *g_toff, const int32_t *g_blk,
+                            const void *g_w, const void *vals_f, const int32_t *node_inst_c, const uint8_t *act,
+                            cudaStream_t s)
 {
-  const size_t sm = static_cast<size_t>(max_row_blocks_c) * kBlk * sizeof(T);
-  if (sm > 200 * 1024 || nn_c > 0x7fffffff) return cudaErrorInvalidValue;
-  if (nn_c == 0) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_galerkin<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
-  if (e != cudaSuccess) return e;
-  k_galerkin<T><<<static_cast<unsigned>(nn_c), kGalThreads, sm, s>>>(
-    rowptr_c, cols_c, mask_c, static_cast<T *>(vals_c), r_ptr, r_idx, static_cast<const T *>(r_w), rowptr_f, cols_f,
-    static_cast<const T *>(vals_f), p_ptr, static_cast<const T *>(p_w), g_ptr, g_slot, node_inst_c, act);
+  if (nnzb_c == 0) return cudaSuccess;
+  const int64_t grid = (nnzb_c + kGalWarps - 1) / kGalWarps;
+  if (grid > 0x7fffffff) return cudaErrorInvalidValue;
+  if (fp32)
+    k_galerkin<float><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, static_cast<float *>(vals_c), g_toff, g_blk, static_cast<const float *>(g_w),
+      static_cast<const float *>(vals_f), node_inst_c, act);
+  else
+    k_galerkin<double><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, static_cast<double *>(vals_c), g_toff, g_blk, static_cast<const double *>(g_w),
+      static_cast<const double *>(vals_f), node_inst_c, act);
   return cudaGetLastError();
-}
-
-cudaError_t launch_galerkin(bool fp32, int64_t nn_c, const int32_t *rowptr_c, const int32_t *cols_c,
-                            const uint32_t *mask_c, void *vals_c, const int32_t *r_ptr, const int32_t *r_idx,
-                            const void *r_w, const int32_t *rowptr_f, const int32_t *cols_f, const void *vals_f,
-                            const int32_t *p_ptr, const void *p_w, const int64_t *g_ptr, const uint8_t *g_slot,
-                            int max_row_blocks_c, const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s)
-{
-  return fp32 ? launch_galerkin_t<float>(nn_c, rowptr_c, cols_c, mask_c, vals_c, r_ptr, r_idx, r_w, rowptr_f, cols_f,
-                                         vals_f, p_ptr, p_w, g_ptr, g_slot, max_row_blocks_c, node_inst_c, act, s)
-              : launch_galerkin_t<double>(nn_c, rowptr_c, cols_c, mask_c, vals_c, r_ptr, r_idx, r_w, rowptr_f, cols_f,
-                                          vals_f, p_ptr, p_w, g_ptr, g_slot, max_row_blocks_c, node_inst_c, act, s);
 }
 
 // ---------------------------------------------------------------------------------
@@ -169,31 +198,42 @@ cudaError_t launch_galerkin(bool fp32, int64_t nn_c, const int32_t *rowptr_c, co
 // of the slightly shifted matrix in shared memory, FP32, one CTA per instance.  It is a preconditioner component, so
 // FP32 suffices in both precision modes (the outer flexible GMRES is exact).
 // ---------------------------------------------------------------------------------
-constexpr int kGjThreads = 512;
+constexpr int kGjThreads = 320;       // >= the 2 * 144 + 1 columns of one augmented row
+constexpr int kMaxDense = 160;        // largest coarsest system (unknowns per instance)
 constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest solve
 
+// Gauss-Jordan on [A + shift I | I] with implicit partial pivoting: in step k one warp
+// picks the largest unused entry of column k (row p_k) and snapshots the column; then
+// every thread updates the augmented columns it owns (row p_k scaled, every other row
+// minus its column-k multiple), so a step needs two barriers.  Afterwards row p_k of
+// the right half is row k of the inverse.  Rows are padded to an odd length so that
+// column reads hit distinct banks.
 template <typename T>
 __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T *__restrict__ vals,
                                                              const int64_t *__restrict__ dense_off,
                                                              float *__restrict__ inv, int *__restrict__ singular)
 {
-  extern __shared__ float W[]; // [nd][2 nd]
-  __shared__ float s_val[kGjThreads / 32];
-  __shared__ int s_idx[kGjThreads / 32];
-  __shared__ int s_piv;
+  extern __shared__ float W[]; // [nd][ld]
+  __shared__ float colk[kMaxDense];
+  __shared__ int prow[kMaxDense];
+  __shared__ unsigned char used[kMaxDense];
+  __shared__ int s_p;
   __shared__ int s_sing;
+  __shared__ float s_piv;
   __shared__ float s_shift;
   const int inst = blockIdx.x;
   const int64_t n0 = m.node_off_ptr[inst], n1 = m.node_off_ptr[inst + 1];
   const int B = m.B;
   const int nd = static_cast<int>((n1 - n0) * B);
-  const int ld = 2 * nd;
+  const int ld = 2 * nd + 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (nd > kMaxDense) return; // rejected by the host before launch
   for (int e = tid; e < nd * ld; e += kGjThreads)
     {
-      const int r = e / ld, c = e % ld;
+      const int r = e / ld, c = e - r * ld;
       W[e] = (c >= nd && c - nd == r) ? 1.f : 0.f;
     }
+  for (int i = tid; i < nd; i += kGjThreads) used[i] = 0;
   __syncthreads();
   const int64_t b0 = m.rowptr[n0], b1 = m.rowptr[n1];
   for (int64_t i = tid; i < (b1 - b0) * B * B; i += kGjThreads)
@@ -210,6 +250,7 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       const int row = static_cast<int>((lo - n0) * B + cr), col = static_cast<int>((m.cols[blk] - n0) * B + cd);
       W[row * ld + col] = static_cast<float>(vals[blk * B * B + e]);
     }
+  __syncthreads();
   if (tid == 0)
     {
       s_sing = 0;
@@ -224,79 +265,70 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
   __syncthreads();
   for (int k = 0; k < nd; ++k)
     {
-      float best = -1.f;
-      int bi = k;
-      for (int i = k + tid; i < nd; i += kGjThreads)
+      if (warp == 0)
         {
-          const float v = fabsf(W[i * ld + k]);
-          if (v > best)
+          float best = -1.f;
+          int bi = nd;
+          for (int i = lane; i < nd; i += 32)
             {
-              best = v;
-              bi = i;
+              const float v = W[i * ld + k];
+              colk[i] = v;
+              if (!used[i] && fabsf(v) > best)
+                {
+                  best = fabsf(v);
+                  bi = i;
+                }
             }
-        }
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1)
-        {
-          const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi))
+          for (int off = 16; off > 0; off >>= 1)
             {
-              best = ob;
-              bi = oi;
+              const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+              const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+              if (ob > best || (ob == best && oi < bi))
+                {
+                  best = ob;
+                  bi = oi;
+                }
             }
-        }
-      if (lane == 0)
-        {
-          s_val[warp] = best;
-          s_idx[warp] = bi;
-        }
-      __syncthreads();
-      if (tid == 0)
-        {
-          float bv = -1.f;
-          int bidx = k;
-          for (int w = 0; w < kGjThreads / 32; ++w)
-            if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bidx))
-              {
-                bv = s_val[w];
-                bidx = s_idx[w];
-              }
-          s_piv = bidx;
-          if (!(bv > 1e-30f)) s_sing = 1;
+          if (lane == 0)
+            {
+              if (!(best > 1e-30f) || bi >= nd)
+                s_sing = 1;
+              else
+                {
+                  s_p = bi;
+                  s_piv = W[bi * ld + k];
+                  used[bi] = 1;
+                  prow[k] = bi;
+                }
+            }
         }
       __syncthreads();
       if (s_sing) break;
-      const int p = s_piv;
-      if (p != k)
-        for (int c = tid; c < ld; c += kGjThreads)
-          {
-            const float t = W[k * ld + c];
-            W[k * ld + c] = W[p * ld + c];
-            W[p * ld + c] = t;
-          }
-      __syncthreads();
-      const float pinv = 1.f / W[k * ld + k];
-      __syncthreads();
-      for (int c = tid; c < ld; c += kGjThreads) W[k * ld + c] *= pinv;
-      __syncthreads();
-      for (int e = tid; e < nd * ld; e += kGjThreads)
+      const int p = s_p;
+      const float rp = 1.f / s_piv;
+      // columns left of k are unit columns already: row p is zero there
+      for (int c = k + tid; c < 2 * nd; c += kGjThreads)
         {
-          const int i = e / ld, c = e - i * ld;
-          if (i == k || c == k) continue;
-          const float f = W[i * ld + k];
-          if (f != 0.f) W[e] -= f * W[k * ld + c];
+          const float wp = W[p * ld + c] * rp;
+          for (int i = 0; i < nd; ++i)
+            {
+              if (i == p)
+                W[i * ld + c] = wp;
+              else
+                {
+                  const float f = colk[i];
+                  if (f != 0.f) W[i * ld + c] -= f * wp;
+                }
+            }
         }
-      __syncthreads();
-      for (int i = tid; i < nd; i += kGjThreads)
-        if (i != k) W[i * ld + k] = 0.f;
       __syncthreads();
     }
   float *out = inv + dense_off[inst];
   for (int e = tid; e < nd * nd; e += kGjThreads)
     {
-      const int i = e / nd, c = e % nd;
-      out[e] = s_sing ? (i == c ? 1.f : 0.f) : W[i * ld + nd + c];
+      const int i = e / nd, c = e - i * nd;
+      out[e] = s_sing ? (i == c ? 1.f : 0.f) : W[prow[i] * ld + nd + c];
     }
   if (tid == 0 && s_sing) singular[inst] = 1;
 }
@@ -324,8 +356,8 @@ __global__ void k_dense_apply(DevMesh m, const int64_t *__restrict__ dense_off, 
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, cudaStream_t s)
 {
-  const size_t sm = static_cast<size_t>(max_nd) * 2 * max_nd * sizeof(float);
-  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  const size_t sm = static_cast<size_t>(max_nd) * (2 * max_nd + 1) * sizeof(float);
+  if (max_nd > kMaxDense || sm > 227 * 1024) return cudaErrorInvalidValue;
   if (fp32)
     {
       cudaError_t e = cudaFuncSetAttribute(k_dense_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -274,8 +274,8 @@ class Params:
     ls_step: float = 0.83
     ls_max_trials: int = 100
     damped: bool = True
-    mg_pre: int = 2
-    mg_post: int = 2
+    mg_pre: int = 1
+    mg_post: int = 1
     mg_omega: float = 1.0
 
     @classmethod
