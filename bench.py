@@ -119,14 +119,15 @@ def batch_instances(gl, count, seed=4):
     return out
 
 
-def batched_leg(gl, count, linear_tol, sur=None):
+def batched_leg(gl, count, linear_tol, sur=None, precond=None):
     """Batched mixed solve of `count` instances in one context (from the B phase and, with
     a surrogate, from its guess) vs the plain FP64 GPU Newton solving them one at a time
     from the B phase; all to ||F|| < 1e-10 per instance."""
     inst = batch_instances(gl, count)
     meshes = [d["mesh"] for d in inst]
     x0 = np.concatenate([d["x0"] for d in inst])
-    prm_m = [gl.Params.from_matep(d["p"], d["t"], precision=gl.MIXED) for d in inst]
+    pc = gl.PC_BLOCK_JACOBI if precond is None else precond
+    prm_m = [gl.Params.from_matep(d["p"], d["t"], precision=gl.MIXED, precond=pc) for d in inst]
     f = gl.FemGL(meshes, prm_m)
     f.set_solution(x0)
     f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)  # warm-up
@@ -141,7 +142,7 @@ def batched_leg(gl, count, linear_tol, sur=None):
     F_s = []
     its_s = []
     for d in inst:
-        prm = gl.Params.from_matep(d["p"], d["t"], precision=gl.FP64)
+        prm = gl.Params.from_matep(d["p"], d["t"], precision=gl.FP64, precond=pc)
         g = gl.FemGL(d["mesh"], prm)
         g.set_solution(d["x0"])
         g.sync()
@@ -156,8 +157,8 @@ def batched_leg(gl, count, linear_tol, sur=None):
     if sur is not None:
         L = importlib.import_module("verkko-hem-repo_gb300.learned")
         li = [L.Instance(d["t"], d["p"], d["D"], d["n"], d["mesh"]) for d in inst]
-        L.solve_learned(gl, sur, li, gl.MIXED, linear_tol)  # warm-up
-        _, ol, ms_l, finfo = L.solve_learned(gl, sur, li, gl.MIXED, linear_tol)
+        L.solve_learned(gl, sur, li, gl.MIXED, linear_tol, precond=pc)  # warm-up
+        _, ol, ms_l, finfo = L.solve_learned(gl, sur, li, gl.MIXED, linear_tol, precond=pc)
         learned = {"mixed_batched_learned_solves_per_s": count / (ms_l / 1000.0),
                    "speedup_vs_fp64_sequential": ms_seq / ms_l, "newton_its": ol["newton_its"].tolist(),
                    "max_free_energy_rel_diff_vs_fp64": float(np.max(np.abs(ol["free_energy"] - F_s) / np.abs(F_s))),
@@ -172,8 +173,9 @@ def batched_leg(gl, count, linear_tol, sur=None):
             "sample": "seeded (seed 4) instances of the sweep: T/Tc~U(0.3,0.95), p~U(0,34), D~U(8,40), n~U{16..48}"}
 
 
-def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None):
-    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision, precond=gl.PC_BLOCK_JACOBI)
+def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None, precond=None):
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision,
+                               precond=gl.PC_BLOCK_JACOBI if precond is None else precond)
     f = gl.FemGL(m, prm)
     out = None
     for _ in range(warmup):
@@ -194,6 +196,7 @@ def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=Fal
     kms, kn = f.kernel_timing(False)
     phases = f.timers()
     launches = f.launch_count - launches0
+    mg = {"levels": f.mg_levels, "fallbacks": f.mg_fallbacks}
     x = f.solution()
     F = float(f.free_energy()[0])
     # assembly alone (J + R), timed separately
@@ -207,11 +210,12 @@ def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=Fal
     asm_ms = f.event_stop() / na
     f.close()
     return {"ms": ms_steps, "out": stats[-1], "kernel_ms": kms, "kernel_n": kn, "phases": phases,
-            "launches": launches, "x": x, "F": F, "asm_ms": asm_ms}
+            "launches": launches, "x": x, "F": F, "asm_ms": asm_ms, "mg": mg}
 
 
-def e2e_mode(gl, m, x0, precision, steps, linear_tol):
-    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision, precond=gl.PC_BLOCK_JACOBI)
+def e2e_mode(gl, m, x0, precision, steps, linear_tol, precond=None):
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision,
+                               precond=gl.PC_BLOCK_JACOBI if precond is None else precond)
     f = gl.FemGL(m, prm)
     start = x0 if callable(x0) else (lambda: np.ascontiguousarray(x0))
     solve_once(f, start(), linear_tol)
@@ -265,6 +269,8 @@ def main():
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
     ap.add_argument("--ncu-mlp", type=int, default=0, help="profiling case: surrogate forward on N points + one gradient")
+    ap.add_argument("--precond", default="mg", choices=["mg", "bj"],
+                    help="preconditioner of every GPU leg: geometric multigrid (default) or block-Jacobi")
     ap.add_argument("--headline-start", default="bphase", choices=["bphase", "learned"],
                     help="start of the headline solves (the other start is reported beside it)")
     args = ap.parse_args()
@@ -314,13 +320,14 @@ def main():
 
             torch.cuda.synchronize()
 
+    pc = gl.PC_MULTIGRID if args.precond == "mg" else gl.PC_BLOCK_JACOBI
     # learned initial guess: trained once, before any timing, on converged states of
     # seeded slab instances (none of them is the benchmark instance)
     sur, learn_info = None, None
     if args.learned:
         L = importlib.import_module("verkko-hem-repo_gb300.learned")
         t0 = time.perf_counter()
-        Xtr, Ytr, ginfo = L.generate(gl, 32, seed=11, n_lo=10, n_hi=14, per_instance=2048)
+        Xtr, Ytr, ginfo = L.generate(gl, 32, seed=11, n_lo=10, n_hi=14, per_instance=2048, precond=pc)
         t_gen = time.perf_counter() - t0
         sur, tinfo = L.train(gl, Xtr, Ytr, steps=1500, batch=4096, lr=1e-3, seed=0)
         inst2 = L.Instance(T_RED, P_BAR, 2 * HALF, NCELL, m)
@@ -330,18 +337,21 @@ def main():
                       "mlp_launches": sur.launch_count,
                       "note": "trained once before timing on 32 seeded slab instances (10^3-14^3 cells), "
                               "not including the benchmark instance"}
-    fp64 = time_mode(gl, m, x0, gl.FP64, max(1, args.steps // 2), 1, args.linear_tol, flush=flush)
+    fp64 = time_mode(gl, m, x0, gl.FP64, max(1, args.steps // 2), 1, args.linear_tol, flush=flush, precond=pc)
+    # block-Jacobi beside multigrid (same start, same precision)
+    bj = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                   precond=gl.PC_BLOCK_JACOBI) if pc != gl.PC_BLOCK_JACOBI else None
     # the headline uses the start that solves faster; the other start is reported beside it
     alt_x0 = learned_x0 if sur is not None else None
     alt = time_mode(gl, m, alt_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol,
-                    flush=flush) if alt_x0 is not None else None
+                    flush=flush, precond=pc) if alt_x0 is not None else None
     use_learned = alt is not None and args.headline_start == "learned"
     head_x0 = learned_x0 if use_learned else x0
     with ClockSampler() as clk:
         mixed = time_mode(gl, m, head_x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
-                          flush=flush)
-    e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol)
-    batched = batched_leg(gl, args.batch, args.linear_tol, sur) if args.batch > 0 else None
+                          flush=flush, precond=pc)
+    e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc)
+    batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc) if args.batch > 0 else None
 
     ms_step = float(np.mean(mixed["ms"]))
     value = 1000.0 / ms_step
@@ -368,7 +378,9 @@ def main():
         "data": "synthetic (seeded B-phase + Gaussian noise start; no dataset)",
         "config": {"workload": WORKLOAD, "n_dofs": nd, "nnzb": nnzb,
                    "mode": "mixed+learned" if use_learned else "mixed", "linear_tol": args.linear_tol,
-                   "precond": "block-Jacobi", "gmres_restart": 50,
+                   "precond": ("geometric multigrid V(1,1): Galerkin coarse levels, l1 block-Jacobi smoothing, "
+                               "flexible GMRES(50)") if pc == gl.PC_MULTIGRID else "block-Jacobi, GMRES(50)",
+                   "mg_levels": mixed["mg"]["levels"], "gmres_restart": 50,
                    "l2": "inputs > L2 (FP32 BSR 1.18 GB) and a 256 MB L2 flush between steps"},
         "newton_its": int(mixed["out"]["newton_its"][0]),
         "gmres_its": int(mixed["out"]["gmres_its"][0]),
@@ -377,6 +389,11 @@ def main():
         "fp64": {"solves_per_s": 1000.0 / float(np.mean(fp64["ms"])), "ms_per_solve": float(np.mean(fp64["ms"])),
                  "newton_its": int(fp64["out"]["newton_its"][0]), "gmres_its": int(fp64["out"]["gmres_its"][0]),
                  "free_energy": fp64["F"], "assembly_ms": fp64["asm_ms"], "assembly_gdofs": nd / fp64["asm_ms"] / 1e6},
+        "mixed_block_jacobi": None if bj is None else {
+            "solves_per_s": 1000.0 / float(np.mean(bj["ms"])), "ms_per_solve": float(np.mean(bj["ms"])),
+            "newton_its": int(bj["out"]["newton_its"][0]), "gmres_its": int(bj["out"]["gmres_its"][0]),
+            "free_energy": bj["F"]},
+        "mg_fallbacks": mixed["mg"]["fallbacks"],
         "mixed_learned_start": None if alt is None else {
             "solves_per_s": 1000.0 / float(np.mean(alt["ms"])), "newton_its": int(alt["out"]["newton_its"][0]),
             "gmres_its": int(alt["out"]["gmres_its"][0]), "free_energy": alt["F"]},

@@ -69,10 +69,11 @@ def bphase_starts(gl, insts, noise: float, seed: int):
     return [gl.bphase_guess(d.p, d.t, d.mesh.nn, noise=noise, seed=seed + k) for k, d in enumerate(insts)]
 
 
-def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40):
+def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40, precond=None):
     """One batched Newton run over the instances from the given starts.  Returns
     (solutions, stats, ms)."""
-    prms = [gl.Params.from_matep(d.p, d.t, precision=precision) for d in insts]
+    pc = gl.PC_BLOCK_JACOBI if precond is None else precond
+    prms = [gl.Params.from_matep(d.p, d.t, precision=precision, precond=pc) for d in insts]
     f = gl.FemGL([d.mesh for d in insts], prms)
     f.set_solution(np.concatenate(starts))
     f.sync()
@@ -89,10 +90,10 @@ def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=4
 
 
 def generate(gl, count: int, seed: int = 11, n_lo: int = 10, n_hi: int = 14, per_instance: int = 2048,
-             noise: float = 0.05):
+             noise: float = 0.05, precond=None):
     """Training pairs from `count` converged batched solves."""
     insts = sample(gl, count, seed, n_lo, n_hi)
-    sols, out, ms = solve(gl, insts, bphase_starts(gl, insts, noise, seed * 1000), gl.MIXED)
+    sols, out, ms = solve(gl, insts, bphase_starts(gl, insts, noise, seed * 1000), gl.MIXED, precond=precond)
     rng = np.random.default_rng(seed)
     X, Y = [], []
     for d, x, ok in zip(insts, sols, out["residual"] <= 1e-10):
@@ -124,19 +125,19 @@ def guess(gl, surrogate, insts):
 
 
 def solve_learned(gl, surrogate, insts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40, noise_fallback=0.05,
-                  fallback_seed=0):
+                  fallback_seed=0, precond=None):
     """Newton from the surrogate; instances that do not reach tol (or stall) are re-solved
     from the B phase.  Returns (solutions, per-instance stats dict, total ms)."""
     t0 = time.perf_counter()
     starts = guess(gl, surrogate, insts)
     t_guess = (time.perf_counter() - t0) * 1000.0
-    sols, out, ms = solve(gl, insts, starts, precision, linear_tol, tol, max_newton)
+    sols, out, ms = solve(gl, insts, starts, precision, linear_tol, tol, max_newton, precond)
     failed = [k for k in range(len(insts)) if not (out["residual"][k] <= tol)]
     fb_ms = 0.0
     if failed:
         sub = [insts[k] for k in failed]
         s2, o2, fb_ms = solve(gl, sub, bphase_starts(gl, sub, noise_fallback, fallback_seed), precision, linear_tol, tol,
-                              max_newton)
+                              max_newton, precond)
         for j, k in enumerate(failed):
             sols[k] = s2[j]
             out["newton_its"][k] += o2["newton_its"][j]
