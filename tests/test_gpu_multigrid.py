@@ -43,6 +43,7 @@ def test_galerkin_coarse_operators(gl, precision):
     with gl.FemGL(m, prm) as f:
         f.set_solution(x0)
         f.assemble_system()
+        f.solve(1e-2, allow_unconverged=True)  # the hierarchy is built by the solve's setup
         rowptr, cols, vals, _ = f.system()
         levels = [(rowptr, cols, vals, None)] + [f.mg_level(l) for l in range(1, f.mg_levels + 1)]
         nlev = f.mg_levels

@@ -133,6 +133,12 @@ struct glgpu_ctx
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
+  bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
+  // the V-cycle as a CUDA graph (captured on first use; every pointer it touches is fixed)
+  cudaGraphExec_t vc_exec = nullptr;
+  void *mg_in = nullptr, *mg_out = nullptr;
+  int64_t vc_nodes = 0;
+  bool vc_failed = false;
   int64_t mg_fallbacks = 0;          // solves handed from multigrid to block-Jacobi
 };
 
@@ -448,12 +454,27 @@ glgpu_status cheb_coeffs(glgpu_ctx *c)
   return GLGPU_OK;
 }
 
-glgpu_status prec_setup(glgpu_ctx *c)
+glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act);
+
+glgpu_status bj_setup(glgpu_ctx *c)
+{
+  if (c->dinv_ready) return GLGPU_OK;
+  CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(c->dm, c->mixed, c->vals, c->dinv, c->st); }));
+  c->dinv_ready = true;
+  return GLGPU_OK;
+}
+
+// Preconditioner setup for the current Jacobian (the reference builds its AMG inside
+// solve, solve.cc:141-152): the multigrid hierarchy, or the block-Jacobi inverses
+// (multigrid computes those only when a solve falls back to them).
+glgpu_status prec_setup(glgpu_ctx *c, const uint8_t *act)
 {
   if (c->prec_ready) return GLGPU_OK;
   const int pc = c->prm[0].precond;
-  if (pc >= GLGPU_PC_BLOCK_JACOBI)
-    CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(c->dm, c->mixed, c->vals, c->dinv, c->st); }));
+  if (pc == GLGPU_PC_MULTIGRID && c->n_levels > 0)
+    CKS(mg_assemble(c, act));
+  else if (pc >= GLGPU_PC_BLOCK_JACOBI)
+    CKS(bj_setup(c));
   if (pc == GLGPU_PC_CHEBYSHEV)
     {
       CKS(cheb_setup(c));
@@ -464,7 +485,56 @@ glgpu_status prec_setup(glgpu_ctx *c)
 }
 
 glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act);
-glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act);
+
+// z = V-cycle(r) for the flexible GMRES basis, masked by the GMRES activity flags.  The
+// cycle's ~9 launches per level are captured once into a CUDA graph over fixed input and
+// output buffers and replayed; if capture is unavailable the cycle runs launch by launch.
+glgpu_status vcycle_run(glgpu_ctx *c, const void *r, void *z)
+{
+  const size_t bytes = tsz(c) * static_cast<size_t>(c->N);
+  if (!c->vc_exec && !c->vc_failed)
+    {
+      std::vector<glgpu_ctx *> all(1, c);
+      all.insert(all.end(), c->lv.begin(), c->lv.end());
+      std::vector<int64_t> l0, k0;
+      std::vector<int> t0;
+      for (glgpu_ctx *x : all)
+        {
+          l0.push_back(x->launches);
+          for (int k = 0; k < KK_N; ++k) k0.push_back(x->klaunch[k]);
+          t0.push_back(x->ktiming);
+          x->ktiming = 0;
+        }
+      cudaGraph_t g = nullptr;
+      glgpu_status st = GLGPU_OK;
+      if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        st = GLGPU_ERR_CUDA;
+      else
+        {
+          st = vcycle(c, 0, c->mg_in, c->mg_out, c->g.active);
+          if (cudaStreamEndCapture(c->st, &g) != cudaSuccess) st = GLGPU_ERR_CUDA;
+        }
+      if (st == GLGPU_OK && g && cudaGraphInstantiate(&c->vc_exec, g, 0) != cudaSuccess) c->vc_exec = nullptr;
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      int64_t nodes = 0;
+      for (size_t i = 0; i < all.size(); ++i)
+        {
+          nodes += all[i]->launches - l0[i];
+          all[i]->launches = l0[i];
+          for (int k = 0; k < KK_N; ++k) all[i]->klaunch[k] = k0[i * KK_N + k];
+          all[i]->ktiming = t0[i];
+        }
+      c->vc_nodes = nodes;
+      if (!c->vc_exec) c->vc_failed = true;
+    }
+  if (!c->vc_exec) return vcycle(c, 0, r, z, c->g.active);
+  CK(cudaMemcpyAsync(c->mg_in, r, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaGraphLaunch(c->vc_exec, c->st));
+  CK(cudaMemcpyAsync(z, c->mg_out, bytes, cudaMemcpyDeviceToDevice, c->st));
+  c->launches += c->vc_nodes;
+  return GLGPU_OK;
+}
 
 // ---------------------------------------------------------------------------------
 // GMRES(m), right preconditioned, classical Gram-Schmidt with one reorthogonalization
@@ -541,7 +611,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
               }));
             }
           else if (mg)
-            CKS(vcycle(c, 0, Vj, Zj, c->g.active));
+            CKS(vcycle_run(c, Vj, Zj));
           else
             CKS(precond(c, Vj, c->Z, c->g.active));
           CKS(spmv(c, Zj, Vj1, c->g.active));
@@ -664,6 +734,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
             {
               use_mg = false;
               c->mg_fallbacks++;
+              CKS(bj_setup(c));
             }
         }
       bool more = false;
@@ -927,6 +998,13 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     char *si = nullptr;
     CKS(dalloc(c, &si, tsz(c) * static_cast<size_t>(c->nn) * c->B * c->B));
     c->sinv = si;
+    char *a = nullptr, *b = nullptr;
+    CKS(dalloc(c, &a, tsz(c) * static_cast<size_t>(c->N)));
+    CKS(dalloc(c, &b, tsz(c) * static_cast<size_t>(c->N)));
+    CK(cudaMemset(a, 0, tsz(c) * static_cast<size_t>(c->N)));
+    CK(cudaMemset(b, 0, tsz(c) * static_cast<size_t>(c->N)));
+    c->mg_in = a;
+    c->mg_out = b;
   }
   CKS(dupload(c, &c->d_dense_off, doff));
   CKS(dalloc(c, &c->d_inv, static_cast<size_t>(doff[n_inst])));
@@ -1194,6 +1272,7 @@ extern "C" glgpu_status glgpu_destroy(glgpu_ctx *c)
   for (auto e : c->ev_pipe)
     if (e) cudaEventDestroy(e);
   if (c->h_its) cudaFreeHost(c->h_its);
+  if (c->vc_exec) cudaGraphExecDestroy(c->vc_exec);
   for (glgpu_ctx *l : c->lv) glgpu_destroy(l);
   if (c->st && c->owns_stream) cudaStreamDestroy(c->st);
   delete c;
@@ -1255,7 +1334,6 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
   CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
   if (need_r) CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   CKS(axpby(c, c->R, c->rhs, nullptr, coefs(-1.0, 0.0), act, false, false, false));
-  if (c->n_levels > 0) CKS(mg_assemble(c, act));
   std::vector<double> nr;
   CKS(norms_d(c, c->rhs, act, nr));
   for (int k = 0; k < c->n_inst; ++k)
@@ -1263,7 +1341,7 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
   c->has_J = c->has_rhs = true;
   for (int k = 0; k < c->n_inst; ++k)
     if (!act || c->inst_on[k]) c->r_ok[k] = 1;
-  c->prec_ready = false;
+  c->prec_ready = c->dinv_ready = false;
   for (int k = 0; k < c->n_inst; ++k)
     if ((!act || c->inst_on[k]) && !std::isfinite(c->rhs_norm[k]))
       return set_error(GLGPU_ERR_NAN, "assemble_system: non-finite residual in instance " + std::to_string(k));
@@ -1300,7 +1378,10 @@ static glgpu_status solve_impl(glgpu_ctx *c, double tol, std::vector<int> &its, 
 {
   if (!c->has_J) return set_error(GLGPU_ERR_STATE, "solve: assemble_system must come first");
   PhaseScope ps(c, PH_SOLVE);
-  CKS(prec_setup(c));
+  bool all_on = true;
+  for (int k = 0; k < c->n_inst; ++k) all_on &= c->inst_on[k] != 0;
+  if (!all_on) CKS(upload_act(c, c->d_act, c->inst_on));
+  CKS(prec_setup(c, all_on ? nullptr : c->d_act));
   CKS(gmres(c, tol, c->inst_on, its, conv));
   c->has_delta = true;
   return GLGPU_OK;
