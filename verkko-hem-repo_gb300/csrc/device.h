@@ -49,6 +49,13 @@ struct DevMesh
   const int32_t *inst_seg_off;
   const int64_t *cell_off;    // [n_inst+1]
   const int64_t *node_off_ptr; // [n_inst+1]
+  // row kernel partition (3D): full interior rows and the rest
+  const int32_t *reg_rows, *gen_rows;
+  int64_t n_reg, n_gen;
+  // per instance: the gradient (K1, K2+K3) part of a full interior row, [n_inst][27][324]
+  // (zero for instances without uniform cells, whose rows are never regular)
+  const double *reg_tmpl_d;
+  const float *reg_tmpl_f;
 };
 
 // ---- assembly (kernels_asm.cu) ----
@@ -56,6 +63,9 @@ struct DevMesh
 // r_cell [nc][nv*B] (double) and per-cell free energy (double).
 cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, double *r_cell, double *e_cell,
                         const uint8_t *inst_active, cudaStream_t s);
+// Gradient part of a full interior row (27 blocks [27][324], slots as in the row kernel)
+// for cells with edges h and coefficients K1, K2+K3.
+void regular_row_stiffness(double K1, double K23, const double *h, double *out);
 // Row gather of the condensed Jacobian from H (type fp32 ? float : double) into vals.
 cudaError_t launch_rows(const DevMesh &m, bool fp32, const void *H, void *vals, cudaStream_t s);
 // Condensed residual R [nn*B] from r_cell.

@@ -1141,6 +1141,26 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = dupload(c, &p_rcwf, rc_wf)))
     return fail(s);
   {
+    int32_t *p_reg = nullptr, *p_gen = nullptr;
+    if ((s = dupload(c, &p_reg, P.reg_rows)) || (s = dupload(c, &p_gen, P.gen_rows))) return fail(s);
+    d.reg_rows = p_reg;
+    d.gen_rows = p_gen;
+    d.n_reg = static_cast<int64_t>(P.reg_rows.size());
+    d.n_gen = static_cast<int64_t>(P.gen_rows.size());
+    // gradient part of the interior rows of every instance with cells of one size
+    std::vector<double> tmpl(static_cast<size_t>(n_inst) * 27 * 324, 0.0);
+    if (P.dim == 3 && P.B == 18)
+      for (int k = 0; k < n_inst; ++k)
+        if (P.inst_uniform[k])
+          regular_row_stiffness(prm[k].K1, prm[k].K2 + prm[k].K3, &P.inst_h[3 * k], &tmpl[static_cast<size_t>(k) * 27 * 324]);
+    std::vector<float> tmpl_f(tmpl.begin(), tmpl.end());
+    double *p_td = nullptr;
+    float *p_tf = nullptr;
+    if ((s = dupload(c, &p_td, tmpl)) || (s = dupload(c, &p_tf, tmpl_f))) return fail(s);
+    d.reg_tmpl_d = p_td;
+    d.reg_tmpl_f = p_tf;
+  }
+  {
     std::vector<float> cf(coef.begin(), coef.end());
     if ((s = dupload(c, &p_coeff, cf))) return fail(s);
   }

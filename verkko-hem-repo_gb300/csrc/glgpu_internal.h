@@ -121,6 +121,12 @@ struct Plan
   std::vector<HangTarget> hang_tg;
   std::vector<int64_t> ht_off;                // [nn+1] first hanging target of each row
   int max_row_blocks = 0;
+  // rows of the specialised 3D row kernel (full 27-block stencil, eight unit-weight cell
+  // contributions, no constraint on the row) and all other rows
+  std::vector<int32_t> reg_rows, gen_rows;
+  // per instance: 1 when every cell has the same box edges (inst_h, [n_inst][3])
+  std::vector<uint8_t> inst_uniform;
+  std::vector<double> inst_h;
   // reduction segments: every segment lies inside one instance's vector range
   int seg_len = 0;
   std::vector<int64_t> seg_begin, seg_end;    // element ranges (in units of scalars)

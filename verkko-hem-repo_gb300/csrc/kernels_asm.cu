@@ -8,12 +8,13 @@
 //  1. k_cell3d: one CTA per 4 cells.  Nodal 18-vectors are gathered into shared
 //     memory, A and grad A are interpolated at the 8 Gauss points, and for every
 //     point the 171 unique entries of the symmetric bulk Hessian
-//     H_q = alpha I + 2 sum_t beta_t d^2(I_t/4) are written out ([cell][q][171]),
+//     H_q = alpha I + 2 sum_t beta_t d^2(I_t/4) are written out ([cell][171][q]),
 //     together with the cell residual and free energy when asked.
-//  2. k_rows3d: one CTA per block row.  Every cell touching the row contributes
-//     block(a,b) = vol sum_q S_abq H_q + K1 G_ab + (K2+K3) D_ab, accumulated in
-//     shared memory at slots precomputed on the host, then the row (27 blocks on a
-//     structured mesh) is written once, contiguously.  No atomics, no colouring.
+//  2. k_rows3d_reg / k_rows3d: one CTA per block row.  Every cell touching the row
+//     contributes block(a,b) = vol sum_q S_abq H_q + K1 G_ab + (K2+K3) D_ab; full
+//     interior rows accumulate their 27 blocks in registers at compile-time slots,
+//     the other rows (boundary, constrained) in shared memory at slots precomputed on
+//     the host.  Each row is written once, contiguously.  No atomics, no colouring.
 //
 // The per-q formulas are the closed forms of the reference's kernels: the
 // quarter-gradient of invariant I_t is Re<G_t, Phi> with G1 = tr(AA^T) A^*,
@@ -140,6 +141,55 @@ cudaError_t init_constants()
   return cudaMemcpyToSymbol(c_D2, D2, sizeof D2);
 }
 
+void regular_row_stiffness(double K1, double K23, const double *h, double *out)
+{
+  const double g = 0.5 - 0.28867513459481288225;
+  const double gp[2] = {g, 1.0 - g};
+  double grd[8][8][3];
+  for (int q = 0; q < 8; ++q)
+    {
+      const double xi[3] = {gp[q & 1], gp[(q >> 1) & 1], gp[(q >> 2) & 1]};
+      for (int v = 0; v < 8; ++v)
+        {
+          double s3[3], ds[3];
+          for (int d = 0; d < 3; ++d)
+            {
+              const int bit = (v >> d) & 1;
+              s3[d] = bit ? xi[d] : 1.0 - xi[d];
+              ds[d] = bit ? 1.0 : -1.0;
+            }
+          grd[q][v][0] = ds[0] * s3[1] * s3[2];
+          grd[q][v][1] = s3[0] * ds[1] * s3[2];
+          grd[q][v][2] = s3[0] * s3[1] * ds[2];
+        }
+    }
+  const double vol = h[0] * h[1] * h[2];
+  const double ih[3] = {1.0 / h[0], 1.0 / h[1], 1.0 / h[2]};
+  for (int i = 0; i < 27 * 324; ++i) out[i] = 0.0;
+  for (int a = 0; a < 8; ++a)
+    for (int b = 0; b < 8; ++b)
+      {
+        double D[9];
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k)
+            {
+              double sum = 0;
+              for (int q = 0; q < 8; ++q) sum += grd[q][a][j] * grd[q][b][k];
+              D[3 * j + k] = 0.125 * sum;
+            }
+        const int sl = 13 + ((b & 1) - (a & 1)) + 3 * (((b >> 1) & 1) - ((a >> 1) & 1)) + 9 * (((b >> 2) & 1) - ((a >> 2) & 1));
+        const double kd = K1 * vol * (D[0] * ih[0] * ih[0] + D[4] * ih[1] * ih[1] + D[8] * ih[2] * ih[2]);
+        for (int c = 0; c < 18; ++c)
+          for (int d = 0; d < 18; ++d)
+            {
+              double v = (c == d) ? kd : 0.0;
+              const int pmc = 3 * (c / 9) + (c % 9) / 3, jc = c % 3, pmd = 3 * (d / 9) + (d % 9) / 3, jd = d % 3;
+              if (pmc == pmd) v += K23 * vol * ih[jc] * ih[jd] * D[3 * jc + jd];
+              out[sl * 324 + c * 18 + d] += v;
+            }
+      }
+}
+
 // typed access to the tables, geometry and weights: FP32 kernels read FP32 copies
 template <typename T> struct Tab;
 template <> struct Tab<float>
@@ -151,6 +201,7 @@ template <> struct Tab<float>
   static __device__ __forceinline__ float4 geo(const DevMesh &m, int64_t e) { return m.geo_f[e]; }
   static __device__ __forceinline__ float coef(const DevMesh &m, int inst, int k) { return m.coef_f[inst * kCoef + k]; }
   static __device__ __forceinline__ float w(const DevMesh &m, int64_t k) { return m.rc_wf[k]; }
+  static __device__ __forceinline__ const float *tmpl(const DevMesh &m) { return m.reg_tmpl_f; }
 };
 template <> struct Tab<double>
 {
@@ -161,6 +212,7 @@ template <> struct Tab<double>
   static __device__ __forceinline__ GeoD geo(const DevMesh &m, int64_t e) { return m.geo_d[e]; }
   static __device__ __forceinline__ double coef(const DevMesh &m, int inst, int k) { return m.coef[inst * kCoef + k]; }
   static __device__ __forceinline__ double w(const DevMesh &m, int64_t k) { return m.rc_w[k]; }
+  static __device__ __forceinline__ const double *tmpl(const DevMesh &m) { return m.reg_tmpl_d; }
 };
 
 // ---------------------------------------------------------------------------------
@@ -248,9 +300,10 @@ constexpr int kCellThreads = 128;
 template <typename T> struct CellSmem
 {
   T xs[kCPB][8][18];
-  T A[kNPQ][18];
+  // per-point rows padded to 19 scalars: lane = point reads hit distinct banks
+  T A[kNPQ][19];
   T gA[kNPQ][3][18];
-  T P[kNPQ][18], Q[kNPQ][18], M2[kNPQ][18], M3[kNPQ][18];
+  T P[kNPQ][19], Q[kNPQ][19], M2[kNPQ][19], M3[kNPQ][19];
   T pq[kNPQ][3];
   T rb[kNPQ][18];
   T dv[kNPQ][6];
@@ -356,15 +409,22 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
   __syncthreads();
   if (WH)
     {
-      for (int idx = tid; idx < kNPQ * kNS3; idx += kCellThreads)
+      // lane = (cell, point) pair, warps stride over the 171 entries: all lanes of a warp
+      // evaluate the same entry (no divergence), and a cell's 8 points fill 32 contiguous
+      // bytes of H[cell][entry][point]
+      static_assert(kNPQ == 32, "one warp covers the CTA's (cell, point) pairs");
+      const int pq = tid & 31, cl = pq >> 3;
+      const bool live = cl < ncb && !s_skip[cl];
+      const QS<T> qs = {S.A[pq], S.P[pq], S.Q[pq], S.M2[pq], S.M3[pq], S.pq[pq]};
+      const T *beta = &S.coef[cl][3];
+      const T alpha = S.coef[cl][2];
+      T *hdst = Hout + (e0 + cl) * static_cast<int64_t>(kNS3) * 8 + (pq & 7);
+      for (int sidx = tid >> 5; sidx < kNS3; sidx += kCellThreads / 32)
         {
-          const int pq = idx / kNS3, sidx = idx % kNS3, cl = pq >> 3;
-          if (cl >= ncb || s_skip[cl]) continue;
-          const QS<T> qs = {S.A[pq], S.P[pq], S.Q[pq], S.M2[pq], S.M3[pq], S.pq[pq]};
           const int c = c_symc[sidx], d = c_symd[sidx];
-          T h = hess_entry(qs, &S.coef[cl][3], c, d);
-          if (c == d) h += S.coef[cl][2];
-          Hout[e0 * 8 * kNS3 + idx] = h;
+          T h = hess_entry(qs, beta, c, d);
+          if (c == d) h += alpha;
+          if (live) hdst[sidx * 8] = h;
         }
     }
   if (WR)
@@ -457,6 +517,134 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
 // ---------------------------------------------------------------------------------
 constexpr int kRowThreads = 192;
 
+// the 8 point values of Hessian entry `ent` of cell e: 32 (FP32) or 64 (FP64) contiguous bytes
+__device__ __forceinline__ void load_hq(const float *H, int64_t e, int ent, bool act, float (&hq)[8])
+{
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+  if (act)
+    {
+      const float4 *p = reinterpret_cast<const float4 *>(H + (e * kNS3 + ent) * 8);
+      a = __ldg(p);
+      b = __ldg(p + 1);
+    }
+  hq[0] = a.x; hq[1] = a.y; hq[2] = a.z; hq[3] = a.w;
+  hq[4] = b.x; hq[5] = b.y; hq[6] = b.z; hq[7] = b.w;
+}
+__device__ __forceinline__ void load_hq(const double *H, int64_t e, int ent, bool act, double (&hq)[8])
+{
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    {
+      double2 v = make_double2(0.0, 0.0);
+      if (act) v = __ldg(reinterpret_cast<const double2 *>(H + (e * kNS3 + ent) * 8) + k);
+      hq[2 * k] = v.x;
+      hq[2 * k + 1] = v.y;
+    }
+}
+
+// k_rows3d_reg: full interior rows (27 blocks, eight unit-weight cell contributions stored
+// in local-vertex order, no constraint on the row, cells of one size; classified on the
+// host).  Only the bulk term depends on the state: block (a, b) of the cell whose vertex a
+// is the row node adds vol sum_q S_abq H_q to slot 13 + dx + 3 dy + 9 dz, (dx, dy, dz) =
+// bits(b) - bits(a).  Thread t owns entry t = 18 c + d of all 27 blocks (the symmetric
+// Hessian entry is read for both halves), so loads of the template and stores of the row
+// are contiguous across a warp; the loops are fully unrolled, so every slot is a
+// compile-time register.  The gradient part of the row is the same for every interior row
+// of an instance and comes from the instance's template; columns' Dirichlet masks apply
+// at the store.
+constexpr int kRegThreads = 324;
+
+template <typename T>
+__global__ void __launch_bounds__(kRegThreads) k_rows3d_reg(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
+{
+  __shared__ uint32_t s_cmask[27];
+  const int64_t n = m.reg_rows[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int r0 = m.rowptr[n];
+  if (tid < 27) s_cmask[tid] = m.mask[m.cols[r0 + tid]];
+  const int c = tid / 18, d = tid - 18 * (tid / 18);
+  const int lo = c < d ? c : d, hi = c < d ? d : c;
+  const int ent = 18 * lo - (lo * (lo - 1)) / 2 + (hi - lo); // index of (lo, hi) in the upper triangle
+  T acc[27];
+#pragma unroll
+  for (int s = 0; s < 27; ++s) acc[s] = T(0);
+  const int k0 = m.rc_ptr[n];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+    {
+      const int64_t e = m.rc_cell[k0 + a];
+      T hq[8];
+      load_hq(H, e, ent, true, hq);
+      const T vol = Tab<T>::geo(m, e).w;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) hq[q] *= vol;
+#pragma unroll
+      for (int b = 0; b < 8; ++b)
+        {
+          const int sl = 13 + ((b & 1) - (a & 1)) + 3 * (((b >> 1) & 1) - ((a >> 1) & 1)) + 9 * (((b >> 2) & 1) - ((a >> 2) & 1));
+          T bulk = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) bulk += Tab<T>::S(a, b, q) * hq[q];
+          acc[sl] += bulk;
+        }
+    }
+  __syncthreads();
+  const T *tp = Tab<T>::tmpl(m) + static_cast<int64_t>(m.node_inst[n]) * 27 * 324 + tid;
+  T *out = vals + static_cast<int64_t>(r0) * 324 + tid;
+#pragma unroll
+  for (int s = 0; s < 27; ++s) out[s * 324] = ((s_cmask[s] >> d) & 1u) ? T(0) : acc[s] + __ldg(tp + s * 324);
+}
+
+// The FP64 variant: the FP64 pipe, not the store pattern, bounds it, so thread t owns the
+// symmetric pair (c, d) / (d, c) of Hessian entry t and evaluates each bulk sum once.
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads) k_rows3d_reg_sym(DevMesh m, const T *__restrict__ H,
+                                                               T *__restrict__ vals)
+{
+  __shared__ uint32_t s_cmask[27];
+  const int64_t n = m.reg_rows[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int r0 = m.rowptr[n];
+  if (tid < 27) s_cmask[tid] = m.mask[m.cols[r0 + tid]];
+  const bool act = tid < kNS3;
+  const int c = act ? c_symc[tid] : 0, d = act ? c_symd[tid] : 0;
+  T acc[27];
+#pragma unroll
+  for (int s = 0; s < 27; ++s) acc[s] = T(0);
+  const int k0 = m.rc_ptr[n];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+    {
+      const int64_t e = m.rc_cell[k0 + a];
+      T hq[8];
+      load_hq(H, e, tid, act, hq);
+      const T vol = Tab<T>::geo(m, e).w;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) hq[q] *= vol;
+#pragma unroll
+      for (int b = 0; b < 8; ++b)
+        {
+          const int sl = 13 + ((b & 1) - (a & 1)) + 3 * (((b >> 1) & 1) - ((a >> 1) & 1)) + 9 * (((b >> 2) & 1) - ((a >> 2) & 1));
+          T bulk = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) bulk += Tab<T>::S(a, b, q) * hq[q];
+          acc[sl] += bulk;
+        }
+    }
+  __syncthreads();
+  if (!act) return;
+  const T *tp = Tab<T>::tmpl(m) + static_cast<int64_t>(m.node_inst[n]) * 27 * 324;
+  T *out = vals + static_cast<int64_t>(r0) * 324;
+  const int cd = c * 18 + d, dc = d * 18 + c;
+#pragma unroll
+  for (int s = 0; s < 27; ++s)
+    {
+      const uint32_t cm = s_cmask[s];
+      out[s * 324 + cd] = ((cm >> d) & 1u) ? T(0) : acc[s] + __ldg(tp + s * 324 + cd);
+      if (c != d) out[s * 324 + dc] = ((cm >> c) & 1u) ? T(0) : acc[s] + __ldg(tp + s * 324 + dc);
+    }
+}
+
 constexpr int kRowMaxContrib = 96; // contributions staged in shared memory per pass
 
 template <typename T>
@@ -468,7 +656,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
   __shared__ int s_cell[kRowMaxContrib], s_a[kRowMaxContrib];
   __shared__ T s_w[kRowMaxContrib];
   __shared__ int16_t s_slot[kRowMaxContrib * 8];
-  const int64_t n = blockIdx.x;
+  const int64_t n = m.gen_rows ? m.gen_rows[blockIdx.x] : static_cast<int64_t>(blockIdx.x);
   const int tid = threadIdx.x;
   const int r0 = m.rowptr[n];
   const int nb = m.rowptr[n + 1] - r0;
@@ -507,8 +695,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
           const int a = s_a[kk];
           const T wa = s_w[kk];
           T hq[8];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) hq[q] = act ? __ldg(H + (e * 8 + q) * kNS3 + tid) : T(0);
+          load_hq(H, e, tid, act, hq);
           const int inst = m.cell_inst[e];
           const T K1 = Tab<T>::coef(m, inst, 0), K23 = Tab<T>::coef(m, inst, 1);
           const auto g = Tab<T>::geo(m, e);
@@ -788,7 +975,14 @@ template <typename T> static cudaError_t launch_rows_t(const DevMesh &m, const T
           if (e != cudaSuccess) return e;
           attr = sm;
         }
-      k_rows3d<T><<<static_cast<unsigned>(m.nn), kRowThreads, sm, s>>>(m, H, vals);
+      if (m.n_gen > 0) k_rows3d<T><<<static_cast<unsigned>(m.n_gen), kRowThreads, sm, s>>>(m, H, vals);
+      if (m.n_reg > 0)
+        {
+          if (sizeof(T) == 4)
+            k_rows3d_reg<T><<<static_cast<unsigned>(m.n_reg), kRegThreads, 0, s>>>(m, H, vals);
+          else
+            k_rows3d_reg_sym<T><<<static_cast<unsigned>(m.n_reg), kRowThreads, 0, s>>>(m, H, vals);
+        }
     }
   else
     k_rows2d<T><<<static_cast<unsigned>((m.nn + 127) / 128), 128, 0, s>>>(m, H, vals);

@@ -310,6 +310,73 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   }
   if (bad) return set_error(GLGPU_ERR_ARG, "glgpu_create: inconsistent constraint pattern");
   P.ht_off.assign(ht_off.begin(), ht_off.end());
+  // regular rows: in the block row of node n, block (a, b) of a cell whose vertex a is n
+  // lands in slot 13 + dx + 3 dy + 9 dz, (dx, dy, dz) = bits(b) - bits(a), when the 27
+  // columns are the lattice neighbours sorted by node id; verified entry by entry, and
+  // the row's eight contributions are then stored in vertex order
+  P.reg_rows.clear();
+  P.gen_rows.clear();
+  P.inst_uniform.assign(n_inst, 1);
+  P.inst_h.assign(static_cast<size_t>(n_inst) * 3, 0.0);
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const int64_t c0 = P.cell_off[k], c1 = P.cell_off[k + 1];
+      if (c1 <= c0)
+        {
+          P.inst_uniform[k] = 0;
+          continue;
+        }
+      for (int d = 0; d < 3; ++d) P.inst_h[3 * k + d] = P.cell_h[3 * c0 + d];
+      for (int64_t e = c0; e < c1 && P.inst_uniform[k]; ++e)
+        for (int d = 0; d < 3; ++d)
+          if (P.cell_h[3 * e + d] != P.inst_h[3 * k + d]) P.inst_uniform[k] = 0;
+    }
+  for (int64_t n = 0; n < nn; ++n)
+    {
+      bool reg = P.dim == 3 && B == 18 && nv == 8 && row_len[n] == 27 && rc_len[n] == 8 && P.mask[n] == 0 &&
+                 P.hptr[n + 1] == P.hptr[n] && P.inst_uniform[P.node_inst[n]];
+      unsigned seen = 0;
+      for (int k = 0; reg && k < 8; ++k)
+        {
+          const int64_t r = P.rc_ptr[n] + k;
+          const int a = P.rc_a[r];
+          if (P.rc_w[r] != 1.0 || (seen >> a) & 1u)
+            {
+              reg = false;
+              break;
+            }
+          seen |= 1u << a;
+          for (int b = 0; b < 8; ++b)
+            {
+              const int want = 13 + ((b & 1) - (a & 1)) + 3 * (((b >> 1) & 1) - ((a >> 1) & 1)) +
+                               9 * (((b >> 2) & 1) - ((a >> 2) & 1));
+              if (P.rc_slot[r * nv + b] != want) reg = false;
+            }
+        }
+      if (reg)
+        {
+          // store the contributions in local-vertex order: contribution a has vertex a
+          const int64_t r0 = P.rc_ptr[n];
+          int32_t cell[8];
+          double w[8];
+          int16_t sl[8][8];
+          for (int k = 0; k < 8; ++k)
+            {
+              const int a = P.rc_a[r0 + k];
+              cell[a] = P.rc_cell[r0 + k];
+              w[a] = P.rc_w[r0 + k];
+              for (int b = 0; b < 8; ++b) sl[a][b] = P.rc_slot[(r0 + k) * nv + b];
+            }
+          for (int a = 0; a < 8; ++a)
+            {
+              P.rc_cell[r0 + a] = cell[a];
+              P.rc_a[r0 + a] = a;
+              P.rc_w[r0 + a] = w[a];
+              for (int b = 0; b < 8; ++b) P.rc_slot[(r0 + a) * nv + b] = sl[a][b];
+            }
+        }
+      (reg ? P.reg_rows : P.gen_rows).push_back(static_cast<int32_t>(n));
+    }
   // reduction segments
   P.seg_len = kSegLen;
   P.seg_begin.clear();
