@@ -299,9 +299,11 @@ glgpu_status upload_d(glgpu_ctx *c, double *dst, const std::vector<double> &a)
 }
 
 // residual at vector v (x or xt) for instances in act: R, e_cell
-glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act)
+// R at v (and the cell free energies when `energy`; the line search needs only |R|)
+glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act, bool energy = false)
 {
-  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, v, nullptr, c->r_cell, c->e_cell, act, c->st); }));
+  double *ec = energy ? c->e_cell : nullptr;
+  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, v, nullptr, c->r_cell, ec, act, c->st); }));
   CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   return GLGPU_OK;
 }
@@ -1348,7 +1350,7 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
       CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
       if (need_r)
         CKS(launch(c, KK_RES, 1, [&] {
-          return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, c->e_cell, act, c->st);
+          return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, nullptr, act, c->st);
         }));
     }
   CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
@@ -1488,7 +1490,7 @@ extern "C" glgpu_status glgpu_newton_iteration(glgpu_ctx *c, double *res, int *t
 extern "C" glgpu_status glgpu_free_energy(glgpu_ctx *c, double *F)
 {
   if (!c || !F) return set_error(GLGPU_ERR_ARG, "glgpu_free_energy: NULL argument");
-  CKS(residual_at(c, c->x, nullptr));
+  CKS(residual_at(c, c->x, nullptr, true));
   std::fill(c->r_ok.begin(), c->r_ok.end(), 1);
   CKS(launch(c, KK_VEC, 1, [&] { return launch_cell_sum(c->dm, c->e_cell, c->d_energy, c->st); }));
   CK(cudaMemcpyAsync(c->h_norm, c->d_energy, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
