@@ -267,7 +267,9 @@ def main():
     ap.add_argument("--linear-tol", type=float, default=1e-4)
     ap.add_argument("--ncu-case", type=int, default=0,
                     help="profiling case: one mixed assembly + 30 GMRES iterations on an N^3 cube, no timing")
-    ap.add_argument("--fp64", action="store_true", help="with --ncu-case: FP64 instead of mixed")
+    ap.add_argument("--fp64", action="store_true", help="with --ncu-case / --ncu-solve: FP64 instead of mixed")
+    ap.add_argument("--ncu-solve", type=int, default=0,
+                    help="profiling case: one complete Newton solve of the N^3 cube (--precond), no timing")
     ap.add_argument("--batch", type=int, default=8, help="instances in the batched leg (0 = skip)")
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
@@ -280,6 +282,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.ncu_case:
         return ncu_case(args.ncu_case, args.fp64)
+    if args.ncu_solve:
+        return ncu_solve(args.ncu_solve, args.fp64, args.precond)
     if args.ncu_mlp:
         gl = importlib.import_module("verkko-hem-repo_gb300")
         gl.build()
@@ -465,6 +469,23 @@ def ncu_case(n, fp64):
         f.sync()
         print(json.dumps({"ncu_case": n, "fp64": bool(fp64), "rhs_norm": float(rn[0]), "gmres_its": int(its[0]),
                           "launches": f.launch_count}))
+    return 0
+
+
+def ncu_solve(n, fp64, precond):
+    """One complete Newton solve of the workload's physics on an n^3 cube (profiling case)."""
+    gl = importlib.import_module("verkko-hem-repo_gb300")
+    gl.build()
+    m = gl.cube_mesh(HALF, n)
+    x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
+    pc = gl.PC_MULTIGRID if precond == "mg" else gl.PC_BLOCK_JACOBI
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=gl.FP64 if fp64 else gl.MIXED, precond=pc)
+    with gl.FemGL(m, prm) as f:
+        f.set_solution(x0)
+        out = f.run(max_newton=40, linear_tol=1e-4, converge_acc=TOL)
+        print(json.dumps({"ncu_solve": n, "fp64": bool(fp64), "precond": precond,
+                          "newton_its": int(out["newton_its"][0]), "gmres_its": int(out["gmres_its"][0]),
+                          "residual": float(out["residual"][0]), "launches": f.launch_count}))
     return 0
 
 

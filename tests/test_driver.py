@@ -1,0 +1,85 @@
+"""The C++ host driver (csrc/femgl_main.cc): it reads the reference's configuration file
+format and keys, and on the GPU runs the Newton loop through the C ABI to the same answer
+as the Python binding."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from _lib import product
+
+CONFIG = """# a small cube: 4^3 cells of side 1.25
+subsection physical parameters
+  set pressure in bar = 20.0   # bar
+  set t_reduced = 0.6
+  set trun on Strong Coupling Correction = true
+end
+subsection control parameters
+  set cube half side length = 2.5
+  set Number of initial global refinments = 2
+  set Number of refinements = 0
+  set Number of interations = 40
+  set Cycle 0 linear solver tol = 1e-4
+  set converge accuracy = 1e-10
+end
+"""
+
+
+@pytest.fixture(scope="module")
+def driver():
+    pkg = product()
+    path = os.path.join(os.path.dirname(pkg.build()), "femgl_gb300")
+    assert os.path.exists(path)
+    return path
+
+
+def _write(tmp_path, text, name="configuration.prm"):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def test_driver_reads_configuration(driver, tmp_path):
+    out = subprocess.run([driver, _write(tmp_path, CONFIG), "--dry-run"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert "p = 20 bar, t = 0.6, SCC on, cube half side 2.5, 4^3 cells" in out.stdout
+    assert "linear tol 0.0001, converge accuracy 1e-10" in out.stdout
+
+
+def test_driver_defaults_and_errors(driver, tmp_path):
+    # unset keys take the reference's declared defaults (cube half side 20, 2^4 cells)
+    out = subprocess.run([driver, _write(tmp_path, "subsection physical parameters\nend\n"), "--dry-run"],
+                         capture_output=True, text=True)
+    assert out.returncode == 0 and "cube half side 20, 16^3 cells" in out.stdout
+    assert "converge accuracy 5e-06" in out.stdout
+    for bad in ("set x = 1\nend\n", "subsection a\n", "subsection a\n  set b\nend\n", "what\n"):
+        r = subprocess.run([driver, _write(tmp_path, bad, "bad.prm"), "--dry-run"], capture_output=True, text=True)
+        assert r.returncode == 2, bad
+    r = subprocess.run([driver, str(tmp_path / "missing.prm"), "--dry-run"], capture_output=True, text=True)
+    assert r.returncode == 2 and "cannot open" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_driver_solves_like_the_binding(driver, tmp_path, precision):
+    gl = product()
+    out = subprocess.run([driver, _write(tmp_path, CONFIG), "--precision", precision, "--out",
+                          str(tmp_path / "x.bin")], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    m = re.search(r"converged after (\d+) Newton iterations .*\|R\| = (\S+), F = (\S+),", out.stdout)
+    assert m, out.stdout
+    its, res, F = int(m.group(1)), float(m.group(2)), float(m.group(3))
+    assert res <= 1e-10
+    mesh = gl.cube_mesh(2.5, 4)
+    prm = gl.Params.from_matep(20.0, 0.6, precision=gl.FP64 if precision == "fp64" else gl.MIXED,
+                               precond=gl.PC_MULTIGRID)
+    with gl.FemGL(mesh, prm) as f:
+        f.set_solution(gl.bphase_guess(20.0, 0.6, mesh.nn))
+        o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        x, Fb = f.solution(), f.free_energy()[0]
+    assert its == int(o["newton_its"][0])
+    assert abs(F - Fb) <= 1e-12 * abs(Fb)
+    xd = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
+    assert np.array_equal(xd, x)

@@ -74,8 +74,12 @@ cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R,
 cudaError_t init_constants();
 
 // ---- linear algebra (kernels_la.cu) ----
-cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y,
-                        const uint8_t *inst_active, cudaStream_t s);
+cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
+                        cudaStream_t s, const void *b = nullptr);
+// One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives
+// y = omega D^-1 b.  18x18 blocks only; y must not alias z.
+cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,
+                          void *y, double omega, const uint8_t *act, cudaStream_t s);
 // l1: add each row's absolute off-block sum to its diagonal (l1 block-Jacobi smoother)
 cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s, bool l1 = false);
 cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const void *x, void *y,
@@ -149,9 +153,10 @@ cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);
 cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s);
 
 // ---- multigrid (kernels_mg.cu) ----
+// zf = base + P zc, or zf += P zc when base is nullptr (constrained components keep base)
 cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                            const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s);
+                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base = nullptr);
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
                             const uint8_t *act, cudaStream_t s);

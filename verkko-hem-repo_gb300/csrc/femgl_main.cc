@@ -1,0 +1,298 @@
+// femgl_gb300: host driver for the GPU Newton path, a stand-in for the reference's
+// sol/src/main.cc + FemGL<3>::run (femgl/src/run.cc:110-258) on the cube geometry of
+// femgl/src/makegrid_cube-z-normal_AdGR.cc.
+//
+// It reads the reference's configuration file format (deal.II ParameterHandler text:
+// "subsection <name>", "set <key> = <value>", "end", '#' comments) with the keys and
+// defaults of confreader/src/declare.cc:115-290, builds the 2^r x 2^r x 2^r cube of side
+// 2 * "cube half side length" (pair-breaking z faces), evaluates the material parameters
+// at (p, t), starts from the uniform B phase (setup_uniform_B-phase.cc:238-263, plus
+// optional seeded Gaussian noise), and runs the Newton loop through the C ABI of
+// include/glgpu.h: assemble_system, solve(tol of the cycle), newton_iteration, stop at
+// |R| <= "converge accuracy".  Mesh refinement cycles stay with the host mesher and are
+// not performed here: every iteration uses the cycle-0 mesh and solver tolerance.
+//
+// usage: femgl_gb300 [configuration.prm] [--precision mixed|fp64]
+//                    [--precond mg|bj|cheb|none] [--noise sigma] [--seed s]
+//                    [--out solution.bin] [--dry-run]
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "glgpu.h"
+
+namespace
+{
+// "subsection/key" -> value, seeded with the reference's declared defaults
+struct Config
+{
+  std::map<std::string, std::string> kv;
+
+  Config()
+  {
+    const char *phys = "physical parameters/";
+    const char *ctrl = "control parameters/";
+    const std::pair<std::string, std::string> defaults[] = {
+      {std::string(phys) + "pressure in bar", "0.0"},
+      {std::string(phys) + "t_reduced", "0.0"},
+      {std::string(phys) + "AdGR diffuse length", "1.0e10"},
+      {std::string(phys) + "gaussian random mean value", "2.0"},
+      {std::string(phys) + "gaussian random STD", "0.1"},
+      {std::string(phys) + "trun on Strong Coupling Correction", "true"},
+      {std::string(phys) + "amplitude u parameter", "1.0"},
+      {std::string(ctrl) + "cube half side length", "20"},
+      {std::string(ctrl) + "Number of refinements", "4"},
+      {std::string(ctrl) + "Number of interations", "40"},
+      {std::string(ctrl) + "Cycle 0 refinement threshold", "1.0e0"},
+      {std::string(ctrl) + "Cycle 0 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "converge accuracy", "5.0e-6"},
+      {std::string(ctrl) + "Number of initial global refinments", "4"},
+      {std::string(ctrl) + "maximum linear iteration number", "10000"},
+      {std::string(ctrl) + "Using dampped Newton iteration", "true"},
+      {std::string(ctrl) + "primary step length of dampped newton iteration", "0.83"},
+    };
+    for (const auto &d : defaults) kv[d.first] = d.second;
+  }
+
+  static std::string trim(const std::string &s)
+  {
+    const size_t a = s.find_first_not_of(" \t\r\n");
+    if (a == std::string::npos) return "";
+    const size_t b = s.find_last_not_of(" \t\r\n");
+    return s.substr(a, b - a + 1);
+  }
+
+  bool read(const std::string &path, std::string &err)
+  {
+    std::ifstream in(path);
+    if (!in)
+      {
+        err = "cannot open " + path;
+        return false;
+      }
+    std::vector<std::string> stack;
+    std::string line;
+    int ln = 0;
+    while (std::getline(in, line))
+      {
+        ++ln;
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line = line.substr(0, hash);
+        line = trim(line);
+        if (line.empty()) continue;
+        if (line.compare(0, 11, "subsection ") == 0)
+          stack.push_back(trim(line.substr(11)));
+        else if (line == "end")
+          {
+            if (stack.empty())
+              {
+                err = path + ":" + std::to_string(ln) + ": 'end' without subsection";
+                return false;
+              }
+            stack.pop_back();
+          }
+        else if (line.compare(0, 4, "set ") == 0)
+          {
+            const size_t eq = line.find('=');
+            if (eq == std::string::npos)
+              {
+                err = path + ":" + std::to_string(ln) + ": 'set' without '='";
+                return false;
+              }
+            std::string key;
+            for (const auto &s : stack) key += s + "/";
+            key += trim(line.substr(4, eq - 4));
+            kv[key] = trim(line.substr(eq + 1));
+          }
+        else
+          {
+            err = path + ":" + std::to_string(ln) + ": cannot parse '" + line + "'";
+            return false;
+          }
+      }
+    if (!stack.empty())
+      {
+        err = path + ": subsection '" + stack.back() + "' not closed";
+        return false;
+      }
+    return true;
+  }
+
+  std::string get(const std::string &key) const
+  {
+    auto it = kv.find(key);
+    return it == kv.end() ? std::string() : it->second;
+  }
+  double num(const std::string &key) const { return std::strtod(get(key).c_str(), nullptr); }
+  bool flag(const std::string &key) const
+  {
+    const std::string v = get(key);
+    return v == "true" || v == "1" || v == "yes";
+  }
+};
+
+int fail(const char *what)
+{
+  std::fprintf(stderr, "femgl_gb300: %s: %s\n", what, glgpu_last_error());
+  return 1;
+}
+} // namespace
+
+int main(int argc, char **argv)
+{
+  std::string prm_path = "configuration.prm", out_path;
+  int precision = GLGPU_MIXED, precond = GLGPU_PC_MULTIGRID;
+  double noise = 0.0;
+  uint64_t seed = 0;
+  bool dry = false;
+  for (int i = 1; i < argc; ++i)
+    {
+      const std::string a = argv[i];
+      auto next = [&](const char *name) -> std::string {
+        if (i + 1 >= argc)
+          {
+            std::fprintf(stderr, "femgl_gb300: %s needs a value\n", name);
+            std::exit(2);
+          }
+        return argv[++i];
+      };
+      if (a == "--precision")
+        {
+          const std::string v = next("--precision");
+          precision = (v == "fp64") ? GLGPU_FP64 : GLGPU_MIXED;
+        }
+      else if (a == "--precond")
+        {
+          const std::string v = next("--precond");
+          precond = v == "bj" ? GLGPU_PC_BLOCK_JACOBI
+                  : v == "cheb" ? GLGPU_PC_CHEBYSHEV
+                  : v == "none" ? GLGPU_PC_NONE
+                                : GLGPU_PC_MULTIGRID;
+        }
+      else if (a == "--noise")
+        noise = std::strtod(next("--noise").c_str(), nullptr);
+      else if (a == "--seed")
+        seed = std::strtoull(next("--seed").c_str(), nullptr, 10);
+      else if (a == "--out")
+        out_path = next("--out");
+      else if (a == "--dry-run")
+        dry = true;
+      else if (!a.empty() && a[0] != '-')
+        prm_path = a;
+      else
+        {
+          std::fprintf(stderr, "femgl_gb300: unknown option %s\n", a.c_str());
+          return 2;
+        }
+    }
+  Config conf;
+  std::string err;
+  if (!conf.read(prm_path, err))
+    {
+      std::fprintf(stderr, "femgl_gb300: %s\n", err.c_str());
+      return 2;
+    }
+  const std::string P = "physical parameters/", C = "control parameters/";
+  const double p = conf.num(P + "pressure in bar"), t = conf.num(P + "t_reduced");
+  const bool scc = conf.flag(P + "trun on Strong Coupling Correction");
+  const double bt = conf.num(P + "AdGR diffuse length");
+  const double half = conf.num(C + "cube half side length");
+  const int nref = static_cast<int>(conf.num(C + "Number of initial global refinments"));
+  const int n_iter = static_cast<int>(conf.num(C + "Number of interations"));
+  const double tol0 = conf.num(C + "Cycle 0 linear solver tol");
+  const double acc = conf.num(C + "converge accuracy");
+  const int n = 1 << nref;
+  std::printf("femgl_gb300: %s  p = %g bar, t = %g, SCC %s, cube half side %g, %d^3 cells\n", glgpu_version(), p, t,
+              scc ? "on" : "off", half, n);
+  std::printf("  Newton: <= %d iterations, linear tol %g, converge accuracy %g, %s, %s\n", n_iter + 1, tol0, acc,
+              precision == GLGPU_FP64 ? "FP64" : "mixed FP32/FP64",
+              precond == GLGPU_PC_MULTIGRID ? "multigrid" : precond == GLGPU_PC_BLOCK_JACOBI ? "block-Jacobi"
+                                            : precond == GLGPU_PC_CHEBYSHEV ? "Chebyshev" : "unpreconditioned");
+  if (bt < 1e10) std::printf("  note: Robin faces (AdGR diffuse length %g) are not assembled; z faces are pair-breaking\n", bt);
+  if (conf.num(C + "Number of refinements") > 0)
+    std::printf("  note: refinement cycles are not performed; the cycle-0 mesh is solved to convergence\n");
+  if (dry) return 0;
+
+  // mesh: cube with pair-breaking z faces (zero orbital-z column)
+  const double lo[3] = {-half, -half, -half}, hi[3] = {half, half, half};
+  const int cells[3] = {n, n, n}, dxy[2] = {0, 0};
+  int nn = 0, nc = 0, nh = 0;
+  if (glgpu_mesh_box(lo, hi, cells, 0.0, dxy, &nn, &nc, &nh, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr))
+    return fail("mesh");
+  std::vector<double> xyz(3 * static_cast<size_t>(nn));
+  std::vector<int32_t> cell(8 * static_cast<size_t>(nc)), hptr(static_cast<size_t>(nn) + 1), hpar(nh > 0 ? nh : 1);
+  std::vector<uint32_t> mask(nn);
+  std::vector<double> hw(nh > 0 ? nh : 1);
+  if (glgpu_mesh_box(lo, hi, cells, 0.0, dxy, &nn, &nc, &nh, xyz.data(), cell.data(), mask.data(), hptr.data(),
+                     hpar.data(), hw.data()))
+    return fail("mesh");
+  glgpu_mesh mesh{3, nn, nc, xyz.data(), cell.data(), mask.data(), hptr.data(), hpar.data(), hw.data()};
+
+  // material parameters at (p, t)
+  double mp[13];
+  if (glgpu_matep(p, t, scc ? 1 : 0, mp)) return fail("matep");
+  glgpu_params prm;
+  glgpu_default_params(&prm);
+  prm.alpha = mp[0];
+  for (int k = 0; k < 5; ++k) prm.beta[k] = mp[1 + k];
+  prm.precision = precision;
+  prm.precond = precond;
+  prm.gmres_max_iter = static_cast<int>(conf.num(C + "maximum linear iteration number"));
+  prm.ls_step = conf.num(C + "primary step length of dampped newton iteration");
+  prm.damped = conf.flag(C + "Using dampped Newton iteration") ? 1 : 0;
+
+  glgpu_ctx *ctx = nullptr;
+  if (glgpu_create(&mesh, &prm, 1, &ctx)) return fail("create");
+  std::vector<double> x(18 * static_cast<size_t>(nn));
+  if (glgpu_bphase_guess(p, t, scc ? 1 : 0, nn, noise, seed, x.data()) || glgpu_set_solution(ctx, x.data()))
+    return fail("initial state");
+
+  glgpu_event_start(ctx);
+  double res = 0.0;
+  int total_its = 0, it = 0;
+  bool converged = false;
+  for (it = 0; it <= n_iter; ++it)
+    {
+      double rhs = 0.0, r = 0.0;
+      int its = 0, trials = 0;
+      if (glgpu_assemble_system(ctx, &rhs)) return fail("assemble_system");
+      const glgpu_status st = glgpu_solve(ctx, tol0, &its);
+      if (st != GLGPU_OK && st != GLGPU_ERR_NOT_CONVERGED) return fail("solve");
+      if (glgpu_newton_iteration(ctx, &r, &trials)) return fail("newton_iteration");
+      total_its += its;
+      res = r;
+      std::printf("  iteration %2d: |rhs| %.6e, GMRES %4d%s, line-search trials %d, |R| %.6e\n", it, rhs, its,
+                  st == GLGPU_ERR_NOT_CONVERGED ? " (limit)" : "", trials, r);
+      if (r <= acc)
+        {
+          converged = true;
+          break;
+        }
+    }
+  double ms = 0.0, F = 0.0;
+  glgpu_event_stop(ctx, &ms);
+  if (glgpu_free_energy(ctx, &F)) return fail("free_energy");
+  std::printf("%s after %d Newton iterations (%d GMRES): |R| = %.6e, F = %.15e, %.1f ms on the GPU\n",
+              converged ? "converged" : "NOT converged", converged ? it + 1 : it, total_its, res, F, ms);
+  if (!out_path.empty())
+    {
+      if (glgpu_get_solution(ctx, x.data())) return fail("get_solution");
+      FILE *f = std::fopen(out_path.c_str(), "wb");
+      if (!f || std::fwrite(x.data(), sizeof(double), x.size(), f) != x.size())
+        {
+          std::fprintf(stderr, "femgl_gb300: cannot write %s\n", out_path.c_str());
+          if (f) std::fclose(f);
+          return 1;
+        }
+      std::fclose(f);
+    }
+  glgpu_destroy(ctx);
+  return converged ? 0 : 1;
+}

@@ -805,7 +805,11 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
   return GLGPU_OK;
 }
 
-// z = V-cycle(r) on level l (l = 0: this context); r, z in the Krylov precision
+// z = V-cycle(r) on level l (l = 0: this context); r, z in the Krylov precision.
+// Per level: smoothing sweeps are fused kernels (y = z + omega D1^-1 (r - J z), D1 the
+// l1 block-Jacobi blocks), the residual is the SpMV's residual form, and the coarse
+// correction is written next to the smoothed iterate, so the buffers ping-pong instead
+// of being copied.
 glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act)
 {
   const bool m = c->mixed;
@@ -822,19 +826,19 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   void *t2 = (l == 0) ? c->C3 : L->C1;
   const double om = c->prm[0].mg_omega;
   const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
-  // pre-smoothing from z = 0: z = om D^-1 r, then damped l1 block-Jacobi sweeps
-  CKS(bj(L, r, z, act, sm));
-  CKS(axpby(L, z, z, nullptr, coefs(om, 0.0), act, m, m, m));
+  auto smooth = [&](const void *zin, void *zout) {
+    return launch(L, KK_PREC, 1, [&] { return launch_smooth(L->dm, m, L->vals, sm, r, zin, zout, om, act, L->st); });
+  };
+  // pre-smoothing from zero, ping-ponging between z and t2; `cur` holds the iterate
+  void *cur = z, *oth = t2;
+  CKS(smooth(nullptr, cur));
   for (int s = 1; s < pre; ++s)
     {
-      CKS(spmv(L, z, t, act));
-      CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
-      CKS(bj(L, t, t2, act, sm));
-      CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
+      CKS(smooth(cur, oth));
+      std::swap(cur, oth);
     }
-  // coarse-grid correction
-  CKS(spmv(L, z, t, act));
-  CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
+  // coarse-grid correction: oth = cur + P e, e = V-cycle(R (r - J cur))
+  CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
   glgpu_ctx *C = c->lv[l];
   const glgpu_ctx::Transfer &tr = c->tr[l];
   CKS(launch(c, KK_PREC, 1, [&] {
@@ -843,16 +847,16 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   }));
   CKS(vcycle(c, l + 1, C->Bv, C->X, act));
   CKS(launch(c, KK_PREC, 1, [&] {
-    return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, z, L->dm.mask, L->dm.hptr,
-                          L->dm.node_inst, act, c->st);
+    return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, oth, L->dm.mask, L->dm.hptr,
+                          L->dm.node_inst, act, c->st, cur);
   }));
+  std::swap(cur, oth);
   for (int s = 0; s < post; ++s)
     {
-      CKS(spmv(L, z, t, act));
-      CKS(axpby(L, r, t, nullptr, coefs(1.0, -1.0), act, m, m, m));
-      CKS(bj(L, t, t2, act, sm));
-      CKS(axpby(L, t2, z, nullptr, coefs(om, 1.0), act, m, m, m));
+      CKS(smooth(cur, oth));
+      std::swap(cur, oth);
     }
+  if (cur != z) CKS(axpby(L, cur, z, nullptr, coefs(1.0, 0.0), act, m, m, m));
   return GLGPU_OK;
 }
 

@@ -42,10 +42,55 @@ template <> __device__ __forceinline__ double vget<double2, double>(const double
 // ---------------------------------------------------------------------------------
 constexpr int kSpmvWarps = 8;
 
+// Row n's products: acc[it][v] = sum over the row's blocks of block[e] * x[col][e % 18] for
+// the scalars e = (lane + 32 it) * NV + v this lane owns.  The row's column ids are loaded
+// once, one per lane, and broadcast by shuffle, and the block loop is unrolled, so the
+// loads of several blocks are in flight together: short rows on small grids (coarse
+// multigrid levels) would otherwise serialise on the cols -> x load chain.
 template <typename T>
+__device__ __forceinline__ void row_products(const DevMesh &m, const T *__restrict__ vals, const T *__restrict__ x,
+                                             int64_t n, int lane,
+                                             T (&acc)[(324 / Vec16<T>::n + 31) / 32][Vec16<T>::n])
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+#pragma unroll
+  for (int it = 0; it < NIT; ++it)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
+  const int b0 = m.rowptr[n], b1 = m.rowptr[n + 1];
+  for (int base = b0; base < b1; base += 32)
+    {
+      const int nbk = (b1 - base) < 32 ? (b1 - base) : 32;
+      const int mycol = (lane < nbk) ? m.cols[base + lane] : 0;
+#pragma unroll 4
+      for (int k = 0; k < nbk; ++k)
+        {
+          const int64_t col = __shfl_sync(0xffffffffu, mycol, k);
+          const T xv = (lane < 18) ? x[col * 18 + lane] : T(0);
+          const V *bp = reinterpret_cast<const V *>(vals + static_cast<int64_t>(base + k) * 324);
+#pragma unroll
+          for (int it = 0; it < NIT; ++it)
+            {
+              const int ch = lane + 32 * it;
+              const V w = (ch < NCH) ? __ldg(bp + ch) : V{};
+#pragma unroll
+              for (int v = 0; v < NV; ++v)
+                {
+                  const int e = (ch < NCH) ? ch * NV + v : 0;
+                  acc[it][v] += vget<V, T>(w, v) * __shfl_sync(0xffffffffu, xv, e % 18);
+                }
+            }
+        }
+    }
+}
+
+template <typename T, bool RES>
 __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *__restrict__ vals,
                                                             const T *__restrict__ x, T *__restrict__ y,
-                                                            const uint8_t *__restrict__ act)
+                                                            const uint8_t *__restrict__ act, const T *__restrict__ b)
 {
   using V = typename Vec16<T>::type;
   constexpr int NV = Vec16<T>::n;
@@ -56,35 +101,10 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
   if (n >= m.nn) return;
   if (act && !act[m.node_inst[n]]) return;
+  T bv = T(0);
+  if (RES && lane < 18) bv = b[n * 18 + lane];
   T acc[NIT][NV];
-#pragma unroll
-  for (int it = 0; it < NIT; ++it)
-#pragma unroll
-    for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
-  const int b0 = m.rowptr[n], b1 = m.rowptr[n + 1];
-  for (int blk = b0; blk < b1; ++blk)
-    {
-      const int64_t col = m.cols[blk];
-      const T xv = (lane < 18) ? x[col * 18 + lane] : T(0);
-      const V *bp = reinterpret_cast<const V *>(vals + static_cast<int64_t>(blk) * 324);
-#pragma unroll
-      for (int it = 0; it < NIT; ++it)
-        {
-          const int ch = lane + 32 * it;
-          V w;
-          if (ch < NCH)
-            w = __ldg(bp + ch);
-          else
-            w = V{};
-#pragma unroll
-          for (int v = 0; v < NV; ++v)
-            {
-              const int e = (ch < NCH) ? ch * NV + v : 0;
-              const T xd = __shfl_sync(0xffffffffu, xv, e % 18);
-              acc[it][v] += vget<V, T>(w, v) * xd;
-            }
-        }
-    }
+  row_products<T>(m, vals, x, n, lane, acc);
 #pragma unroll
   for (int it = 0; it < NIT; ++it)
     {
@@ -99,7 +119,84 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *
       T s = 0;
 #pragma unroll
       for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
-      y[n * 18 + lane] = s;
+      y[n * 18 + lane] = RES ? bv - s : s; // A x, or the residual b - A x
+    }
+}
+
+// One damped block-Jacobi sweep, fused: y = z + omega D^-1 (b - A z) (z == nullptr: the
+// sweep from zero, y = omega D^-1 b).  One warp per block row: the row's SpMV as in
+// k_spmv18, then the 18x18 inverse block applied with the same lane map.  y must not
+// alias z (neighbouring rows read z).
+template <typename T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T *__restrict__ vals,
+                                                              const T *__restrict__ dinv, const T *__restrict__ b,
+                                                              const T *__restrict__ z, T *__restrict__ y, T omega,
+                                                              const uint8_t *__restrict__ act)
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  __shared__ T red[kSpmvWarps][324];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
+  if (n >= m.nn) return;
+  if (act && !act[m.node_inst[n]]) return;
+  T t = (lane < 18) ? b[n * 18 + lane] : T(0);
+  if (z)
+    {
+      T acc[NIT][NV];
+      row_products<T>(m, vals, z, n, lane, acc);
+#pragma unroll
+      for (int it = 0; it < NIT; ++it)
+        {
+          const int ch = lane + 32 * it;
+          if (ch < NCH)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
+        }
+      __syncwarp();
+      if (lane < 18)
+        {
+          T s = 0;
+#pragma unroll
+          for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
+          t -= s;
+        }
+      __syncwarp();
+    }
+  // u = D^-1 t
+  {
+    T acc[NIT][NV];
+    const V *bp = reinterpret_cast<const V *>(dinv + n * 324);
+#pragma unroll
+    for (int it = 0; it < NIT; ++it)
+      {
+        const int ch = lane + 32 * it;
+        const V w = (ch < NCH) ? __ldg(bp + ch) : V{};
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          {
+            const int e = (ch < NCH) ? ch * NV + v : 0;
+            acc[it][v] = vget<V, T>(w, v) * __shfl_sync(0xffffffffu, t, e % 18);
+          }
+      }
+#pragma unroll
+    for (int it = 0; it < NIT; ++it)
+      {
+        const int ch = lane + 32 * it;
+        if (ch < NCH)
+#pragma unroll
+          for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
+      }
+    __syncwarp();
+  }
+  if (lane < 18)
+    {
+      T u = 0;
+#pragma unroll
+      for (int d = 0; d < 18; ++d) u += red[warp][lane * 18 + d];
+      y[n * 18 + lane] = (z ? z[n * 18 + lane] : T(0)) + omega * u;
     }
 }
 
@@ -124,20 +221,39 @@ __global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restri
 }
 
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
-                        cudaStream_t s)
+                        cudaStream_t s, const void *b)
 {
   if (m.B == 18)
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
       if (fp32)
-        k_spmv18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
-                                                        static_cast<const float *>(x), static_cast<float *>(y), act);
+        {
+          const float *bb = static_cast<const float *>(b);
+          if (b)
+            k_spmv18<float, true><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
+                                                                  static_cast<const float *>(x),
+                                                                  static_cast<float *>(y), act, bb);
+          else
+            k_spmv18<float, false><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
+                                                                   static_cast<const float *>(x),
+                                                                   static_cast<float *>(y), act, bb);
+        }
       else
-        k_spmv18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
-                                                         static_cast<const double *>(x), static_cast<double *>(y), act);
+        {
+          const double *bb = static_cast<const double *>(b);
+          if (b)
+            k_spmv18<double, true><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+                                                                   static_cast<const double *>(x),
+                                                                   static_cast<double *>(y), act, bb);
+          else
+            k_spmv18<double, false><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+                                                                    static_cast<const double *>(x),
+                                                                    static_cast<double *>(y), act, bb);
+        }
     }
   else
     {
+      if (b) return cudaErrorInvalidValue; // the residual form exists for 18x18 blocks only
       const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
       if (fp32)
         k_spmv2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(vals), static_cast<const float *>(x),
@@ -146,6 +262,24 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
         k_spmv2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(vals), static_cast<const double *>(x),
                                              static_cast<double *>(y), act);
     }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,
+                          void *y, double omega, const uint8_t *act, cudaStream_t s)
+{
+  if (m.B != 18) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
+  if (fp32)
+    k_smooth18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
+                                                      static_cast<const float *>(dinv), static_cast<const float *>(b),
+                                                      static_cast<const float *>(z), static_cast<float *>(y),
+                                                      static_cast<float>(omega), act);
+  else
+    k_smooth18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+                                                       static_cast<const double *>(dinv), static_cast<const double *>(b),
+                                                       static_cast<const double *>(z), static_cast<double *>(y), omega,
+                                                       act);
   return cudaGetLastError();
 }
 

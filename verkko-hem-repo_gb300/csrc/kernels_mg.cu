@@ -15,21 +15,28 @@
 
 namespace glgpu
 {
+// zf = base + P zc (base == nullptr: zf += P zc); constrained components keep base
 template <typename T>
 __global__ void k_prolong_add(int64_t nn_f, int B, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
                               const T *__restrict__ w, const T *__restrict__ zc, T *__restrict__ zf,
                               const uint32_t *__restrict__ mask_f, const int32_t *__restrict__ hptr_f,
-                              const int32_t *__restrict__ node_inst, const uint8_t *__restrict__ act)
+                              const int32_t *__restrict__ node_inst, const uint8_t *__restrict__ act,
+                              const T *__restrict__ base)
 {
   const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= nn_f * B) return;
   const int64_t n = t / B;
   const int c = static_cast<int>(t % B);
   if (act && !act[node_inst[n]]) return;
-  if (hptr_f[n + 1] > hptr_f[n] || ((mask_f[n] >> c) & 1u)) return;
+  const T b0 = base ? base[t] : zf[t];
+  if (hptr_f[n + 1] > hptr_f[n] || ((mask_f[n] >> c) & 1u))
+    {
+      if (base) zf[t] = b0;
+      return;
+    }
   T s = 0;
   for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * zc[static_cast<int64_t>(idx[k]) * B + c];
-  zf[t] += s;
+  zf[t] = b0 + s;
 }
 
 template <typename T>
@@ -141,21 +148,21 @@ __global__ void __launch_bounds__(kGalWarps * 32)
 template <typename T>
 cudaError_t launch_prolong_add(int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                                const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                               const int32_t *node_inst, const uint8_t *act, cudaStream_t s)
+                               const int32_t *node_inst, const uint8_t *act, const void *base, cudaStream_t s)
 {
   const int64_t n = nn_f * B;
   k_prolong_add<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
     nn_f, B, ptr, idx, static_cast<const T *>(w), static_cast<const T *>(zc), static_cast<T *>(zf), mask_f, hptr_f,
-    node_inst, act);
+    node_inst, act, static_cast<const T *>(base));
   return cudaGetLastError();
 }
 
 cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                            const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s)
+                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base)
 {
-  return fp32 ? launch_prolong_add<float>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, s)
-              : launch_prolong_add<double>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, s);
+  return fp32 ? launch_prolong_add<float>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s)
+              : launch_prolong_add<double>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s);
 }
 
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
@@ -204,8 +211,8 @@ constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest
 
 // Gauss-Jordan on [A + shift I | I] with implicit partial pivoting: in step k one warp
 // picks the largest unused entry of column k (row p_k) and snapshots the column; then
-// every thread updates the augmented columns it owns (row p_k scaled, every other row
-// minus its column-k multiple), so a step needs two barriers.  Afterwards row p_k of
+// every thread updates the augmented columns it owns (every row minus its column-k
+// multiple, then row p_k scaled), so a step needs two barriers.  Afterwards row p_k of
 // the right half is row k of the inverse.  Rows are padded to an odd length so that
 // column reads hit distinct banks.
 template <typename T>
@@ -307,20 +314,16 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       if (s_sing) break;
       const int p = s_p;
       const float rp = 1.f / s_piv;
-      // columns left of k are unit columns already: row p is zero there
+      // columns left of k are unit columns already: row p is zero there.  Every row,
+      // the pivot row included, takes W -= colk * wp (branch-free, so the loop pipelines);
+      // that zeroes row p (colk[p] is the pivot), which then receives the scaled row.
       for (int c = k + tid; c < 2 * nd; c += kGjThreads)
         {
           const float wp = W[p * ld + c] * rp;
-          for (int i = 0; i < nd; ++i)
-            {
-              if (i == p)
-                W[i * ld + c] = wp;
-              else
-                {
-                  const float f = colk[i];
-                  if (f != 0.f) W[i * ld + c] -= f * wp;
-                }
-            }
+          float *col = W + c;
+#pragma unroll 8
+          for (int i = 0; i < nd; ++i) col[i * ld] = fmaf(-colk[i], wp, col[i * ld]);
+          col[p * ld] = wp;
         }
       __syncthreads();
     }
