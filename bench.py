@@ -36,6 +36,7 @@ TOL = 1e-10
 # DRAM bytes (read + write) of one k_spmv18<float> launch on this workload, from the ncu
 # capture summarised in profiles/k_spmv18_fp32_cube32.md (1.193182 GB + 5.481728 MB)
 SPMV_NCU_TRAFFIC = 1.193182e9 + 5.481728e6
+MF_NCU_TRAFFIC = 1.83917568e8 + 1.1717376e7 + 2.2766848e7  # k_mf_cell + k_mf_gather, one apply, 32^3
 METRIC = "GL solves/s at ||F||<1e-10 (femgl 3D, 32^3 Q1, T=0.6Tc, p=20bar)"
 WORKLOAD = "femgl 3D cube L=20, 32^3 Q1 cells, matep(p=20 bar, t=0.6, SCC), z-face pair breaking, B-phase+0.05N(0,1) seed 2"
 
@@ -344,7 +345,8 @@ def main():
                       "mlp_launches": sur.launch_count,
                       "note": "trained once before timing on 32 seeded slab instances (10^3-14^3 cells), "
                               "not including the benchmark instance"}
-    fp64 = time_mode(gl, m, x0, gl.FP64, max(1, args.steps // 2), 1, args.linear_tol, flush=flush, precond=pc)
+    fp64 = time_mode(gl, m, x0, gl.FP64, max(1, args.steps // 2), 1, args.linear_tol, kernel_timing=True, flush=flush,
+                     precond=pc)
     # block-Jacobi beside multigrid (same start, same precision)
     bj = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
                    precond=gl.PC_BLOCK_JACOBI) if pc != gl.PC_BLOCK_JACOBI else None
@@ -364,11 +366,19 @@ def main():
     value = 1000.0 / ms_step
     nd = 18 * m.nn
     nnzb = 912673
-    # SpMV roofline (FP32 blocks): algorithmic bytes per launch
-    spmv_bytes = nnzb * (324 * 4 + 4) + (m.nn + 1) * 4 + 2 * nd * 4
-    n_spmv = mixed["kernel_n"]["spmv"]
-    spmv_ms = mixed["kernel_ms"]["spmv"] / max(1, n_spmv)
-    achieved = spmv_bytes / (spmv_ms * 1e-3) / 1e9 if n_spmv else None
+    # the Krylov operator of the mixed path: J z applied matrix-free from the FP32
+    # quadrature Hessians (k_mf_cell + k_mf_gather, two launches per apply); algorithmic
+    # bytes per apply: H (171 entries x 8 points x 4 B per cell), cell connectivity and
+    # geometry, z in, y out
+    mf_bytes = m.nc * (171 * 8 * 4 + 8 * 4 + 16) + 2 * nd * 4
+    n_mf = mixed["kernel_n"]["spmv"] // 2
+    mf_ms = mixed["kernel_ms"]["spmv"] / max(1, n_mf)
+    achieved = mf_bytes / (mf_ms * 1e-3) / 1e9 if n_mf else None
+    # the FP64 path's operator: the assembled block SpMV, timed in the FP64 leg
+    spmv_bytes = nnzb * (324 * 8 + 4) + (m.nn + 1) * 4 + 2 * nd * 8
+    n_spmv = fp64["kernel_n"]["spmv"]
+    spmv_ms = fp64["kernel_ms"]["spmv"] / max(1, n_spmv)
+    spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9 if n_spmv else None
     asm_bytes = nnzb * 324 * 4 + m.nc * 32 + 2 * nd * 8
     line = {
         "metric": METRIC,
@@ -413,12 +423,16 @@ def main():
         "kernel_ms": mixed["kernel_ms"],
         "kernel_launches": mixed["kernel_n"],
         "gpu_launches": int(mixed["launches"]),
-        "roofline": {"bound": "hbm", "kernel": "k_spmv18<float>", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": SPMV_NCU_TRAFFIC,
-                     "traffic_source": "dram read+write of one k_spmv18<float> launch, ncu capture summarised in "
-                                       "profiles/k_spmv18_fp32_cube32.md",
+        "roofline": {"bound": "hbm", "kernel": "k_mf_cell + k_mf_gather (matrix-free FP32 J z)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": MF_NCU_TRAFFIC,
+                     "traffic_source": "dram read+write of one apply (both kernels) on the 32^3 cube, ncu capture "
+                                       "summarised in profiles/matrix_free_apply_cube32.md",
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
-                     "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms,
+                     "algorithmic_bytes_per_launch": mf_bytes, "avg_launch_ms": mf_ms,
+                     "fp64_block_spmv": {"kernel": "k_spmv18<double>", "achieved": spmv_gbs,
+                                         "frac": (spmv_gbs / hbm) if spmv_gbs else None,
+                                         "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms},
                      "assembly_algorithmic_bytes": asm_bytes},
         "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": nd * 8, "d2h_bytes_per_step": nd * 8},
         "clocks": clk.summary(),

@@ -92,6 +92,28 @@ def test_assembly_mixed_fp32_jacobian(gl, oracle_gl):
     assert np.abs(rhs + Rr).max() <= 1e-12 * np.abs(Rr).max()
 
 
+@pytest.mark.parametrize("refine", [0.25, 0.0])
+def test_spmv_mixed_matrix_free(gl, oracle_gl, refine):
+    # mixed mode applies J matrix-free from the FP32 quadrature Hessians; on every
+    # unconstrained row it must equal the assembled FP32 matrix and the oracle's FP64 J
+    m, prm, x0 = _problem(gl, 4, refine, precision=gl.MIXED)
+    sysr = oracle_gl.System(oracle_mesh(m), coef_of(prm))
+    Jr, _, _ = sysr.assemble(sysr.distribute(x0))
+    v = np.random.default_rng(7).standard_normal(18 * m.nn)
+    with gl.FemGL(m, prm) as f:
+        f.set_solution(x0)
+        f.assemble_system()
+        y = f.spmv(v)
+        _, _, J, _ = f.system()
+    fr = sysr.free
+    v32 = v.astype(np.float32).astype(np.float64)
+    y_bsr = sysr.spmv(J, v32)
+    y_ref = sysr.spmv(Jr, v32)
+    scale = np.abs(y_ref[fr]).max()
+    assert np.abs(y - y_bsr)[fr].max() <= 2e-5 * scale
+    assert np.abs(y - y_ref)[fr].max() <= 2e-5 * scale
+
+
 @pytest.mark.parametrize("precond", ["bj", "cheb", "none"])
 def test_linear_solve_tight(gl, oracle_gl, precond):
     pc = {"bj": gl.PC_BLOCK_JACOBI, "cheb": gl.PC_CHEBYSHEV, "none": gl.PC_NONE}[precond]

@@ -76,6 +76,14 @@ cudaError_t init_constants();
 // ---- linear algebra (kernels_la.cu) ----
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
                         cudaStream_t s, const void *b = nullptr);
+// Matrix-free FP32 Jacobian from the quadrature Hessians H [Nc][171][8] (3D, 18 components):
+// mode 0: y = J z, 1: y = b - J z, 2: y = z + omega D^-1 (b - J z) with D^-1 [Nn][324].
+// ycell [Nc][8][18] is scratch; constrained rows act as the identity.
+// err (optional): set to 1 when a CTA's wait for its Hessian copy times out (the
+// output is then NaN, which the solver's norms report).
+cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *ycell, float *y, const float *b,
+                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
+                      int *err = nullptr);
 // One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives
 // y = omega D^-1 b.  18x18 blocks only; y must not alias z.
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,

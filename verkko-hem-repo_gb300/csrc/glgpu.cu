@@ -133,6 +133,9 @@ struct glgpu_ctx
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
+  bool mf = false;                   // the Krylov operator is applied matrix-free from H (FP32, 3D)
+  float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
+  int *d_err = nullptr;              // device-side wait timeouts (matrix-free Hessian copies)
   bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
   // the V-cycle as a CUDA graph (captured on first use; every pointer it touches is fixed)
   cudaGraphExec_t vc_exec = nullptr;
@@ -319,6 +322,11 @@ glgpu_status bj(glgpu_ctx *c, const void *in, void *out, const uint8_t *act, con
 
 glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
 {
+  if (c->mf)
+    return launch(c, KK_SPMV, 2, [&] {
+      return launch_mf(c->dm, static_cast<const float *>(c->H), static_cast<const float *>(in), c->ycell,
+                       static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err);
+    });
   return launch(c, KK_SPMV, 1, [&] { return launch_spmv(c->dm, c->mixed, c->vals, in, out, act, c->st); });
 }
 
@@ -827,6 +835,12 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   const double om = c->prm[0].mg_omega;
   const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
   auto smooth = [&](const void *zin, void *zout) {
+    if (L->mf && zin)
+      return launch(L, KK_PREC, 2, [&] {
+        return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(zin), L->ycell,
+                         static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
+                         static_cast<float>(om), 2, act, L->st, L->d_err);
+      });
     return launch(L, KK_PREC, 1, [&] { return launch_smooth(L->dm, m, L->vals, sm, r, zin, zout, om, act, L->st); });
   };
   // pre-smoothing from zero, ping-ponging between z and t2; `cur` holds the iterate
@@ -838,7 +852,13 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
       std::swap(cur, oth);
     }
   // coarse-grid correction: oth = cur + P e, e = V-cycle(R (r - J cur))
-  CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
+  if (L->mf)
+    CKS(launch(L, KK_SPMV, 2, [&] {
+      return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(cur), L->ycell,
+                       static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err);
+    }));
+  else
+    CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
   glgpu_ctx *C = c->lv[l];
   const glgpu_ctx::Transfer &tr = c->tr[l];
   CKS(launch(c, KK_PREC, 1, [&] {
@@ -888,6 +908,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       cudaStreamDestroy(L->st);
       L->st = c->st;
       L->owns_stream = false;
+      L->mf = false; // coarse operators exist only assembled (Galerkin products)
       c->lv.push_back(L);
     }
   // transfer operators between level l (fine side) and l+1, and the Galerkin slot tables
@@ -1224,6 +1245,14 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = talloc(&c->C3, N)))
     return fail(s);
   (void)pv;
+  // mixed 3D contexts apply the Krylov operator matrix-free from the FP32 Hessians
+  if (c->mixed && P.dim == 3 && P.B == 18 && P.nv == 8)
+    {
+      if ((s = dalloc(c, &c->ycell, static_cast<size_t>(P.nc) * P.nv * P.B)) || (s = dalloc(c, &c->d_err, 1)))
+        return fail(s);
+      if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(GLGPU_ERR_CUDA, "cudaMemset"));
+      c->mf = true;
+    }
   if ((s = dalloc(c, &c->partial, static_cast<size_t>(d.n_seg) * (mr + 2))) ||
       (s = dalloc(c, &c->partial_n, static_cast<size_t>(d.n_seg))) ||
       (s = dalloc(c, &c->g.H, static_cast<size_t>(n_inst) * (mr + 1) * mr)) ||
@@ -1408,7 +1437,19 @@ static glgpu_status solve_impl(glgpu_ctx *c, double tol, std::vector<int> &its, 
   for (int k = 0; k < c->n_inst; ++k) all_on &= c->inst_on[k] != 0;
   if (!all_on) CKS(upload_act(c, c->d_act, c->inst_on));
   CKS(prec_setup(c, all_on ? nullptr : c->d_act));
-  CKS(gmres(c, tol, c->inst_on, its, conv));
+  const glgpu_status gs = gmres(c, tol, c->inst_on, its, conv);
+  if (c->d_err)
+    {
+      int h_err = 0;
+      CK(cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      if (h_err)
+        {
+          CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+          return set_error(GLGPU_ERR_TIMEOUT, "solve: a device wait for the matrix-free operator's data timed out");
+        }
+    }
+  CKS(gs);
   c->has_delta = true;
   return GLGPU_OK;
 }

@@ -841,7 +841,7 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   if (tid < kRPts)
     {
       const int pq = tid, cl = pq >> 3;
-      const double *A = S.A[pq], *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
+      const double *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
       const double pr = P[0] + P[4] + P[8], pi = P[9] + P[13] + P[17], q = Q[0] + Q[4] + Q[8];
       double i3 = 0, i4 = 0, i5 = 0;
 #pragma unroll
@@ -865,7 +865,6 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
           const double dv = S.gA[pq][0][base] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2];
           ed += dv * dv;
         }
-      (void)A;
       S.en[pq] = e + cf[0] * eg + cf[1] * ed;
     }
   __syncthreads();

@@ -69,11 +69,12 @@ def bphase_starts(gl, insts, noise: float, seed: int):
     return [gl.bphase_guess(d.p, d.t, d.mesh.nn, noise=noise, seed=seed + k) for k, d in enumerate(insts)]
 
 
-def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40, precond=None):
+def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40, precond=None, gmres_max_iter=None):
     """One batched Newton run over the instances from the given starts.  Returns
     (solutions, stats, ms)."""
     pc = gl.PC_BLOCK_JACOBI if precond is None else precond
-    prms = [gl.Params.from_matep(d.p, d.t, precision=precision, precond=pc) for d in insts]
+    kw = {} if gmres_max_iter is None else {"gmres_max_iter": int(gmres_max_iter)}
+    prms = [gl.Params.from_matep(d.p, d.t, precision=precision, precond=pc, **kw) for d in insts]
     f = gl.FemGL([d.mesh for d in insts], prms)
     f.set_solution(np.concatenate(starts))
     f.sync()
@@ -124,14 +125,21 @@ def guess(gl, surrogate, insts):
     return out
 
 
+# GMRES iterations per Newton step allowed from a learned start: the learned state's
+# remaining error lies largely along near-symmetry (phase, rotation) directions, where a
+# linear solve can stall; a stalled instance is re-solved from the B phase instead
+LEARNED_GMRES_CAP = 300
+
+
 def solve_learned(gl, surrogate, insts, precision, linear_tol=1e-4, tol=1e-10, max_newton=40, noise_fallback=0.05,
-                  fallback_seed=0, precond=None):
-    """Newton from the surrogate; instances that do not reach tol (or stall) are re-solved
-    from the B phase.  Returns (solutions, per-instance stats dict, total ms)."""
+                  fallback_seed=0, precond=None, gmres_cap=LEARNED_GMRES_CAP):
+    """Newton from the surrogate; instances that do not reach tol (their residual or a
+    linear solve stalls) are re-solved from the B phase.  Returns (solutions, per-instance
+    stats dict, total ms, info)."""
     t0 = time.perf_counter()
     starts = guess(gl, surrogate, insts)
     t_guess = (time.perf_counter() - t0) * 1000.0
-    sols, out, ms = solve(gl, insts, starts, precision, linear_tol, tol, max_newton, precond)
+    sols, out, ms = solve(gl, insts, starts, precision, linear_tol, tol, max_newton, precond, gmres_cap)
     failed = [k for k in range(len(insts)) if not (out["residual"][k] <= tol)]
     fb_ms = 0.0
     if failed:
