@@ -28,19 +28,20 @@ constexpr int kMThreads = 192;           // 3 threads per point in the Hessian p
 constexpr float kGaF = 0.21132486540518711775f; // Gauss point 1/2 - sqrt(3)/6 on [0, 1]
 constexpr float kGbF = 0.78867513459481288225f;
 
-constexpr uint32_t kMfWaitLimit = 1u << 24; // bounded wait for the Hessian copy
-
 struct MfSmem
 {
-  float Hs[kMCells][kNS3][8]; // the CTA's Hessians, copied in by TMA at kernel start
-  float zs[kMCells][8][18];
+  union
+  {
+    float zs[kMCells][8][18];     // nodal values (gather -> interpolation)
+    float part[3][kMPts][18];     // H Z per point, in three partial sums (product -> contraction)
+  } u;
   float Z[kMPts][19];
   float gZ[kMPts][3][18];
-  float w[kMPts][18];
   float ih[kMCells][3];
   float jxw[kMCells];
   float K1[kMCells], K23[kMCells];
 };
+
 
 __device__ __forceinline__ void gauss2f(float f0, float f1, float &q0, float &q1)
 {
@@ -69,31 +70,164 @@ constexpr SymTable make_sym_table()
 }
 __constant__ SymTable c_sym = make_sym_table();
 
+// the t-th pair (c, d), c <= d, of the upper-triangle enumeration (t = 0..170)
+__host__ __device__ constexpr int pair_c(int t)
+{
+  int c = 0;
+  while (t >= 18 - c)
+    {
+      t -= 18 - c;
+      ++c;
+    }
+  return c;
+}
+__host__ __device__ constexpr int pair_d(int t)
+{
+  int c = 0;
+  while (t >= 18 - c)
+    {
+      t -= 18 - c;
+      ++c;
+    }
+  return c + t;
+}
+static_assert(pair_c(170) == 17 && pair_d(170) == 17 && pair_c(17) == 0 && pair_d(18) == 1, "pair enumeration");
+
+// entries T .. END-1 of H_q Z_q, each loaded once and applied to both w_c and w_d (H is
+// symmetric); a compile-time recursion, so every (c, d) is a constant register index
+template <int T, int END>
+__device__ __forceinline__ void hz_terms(const float *__restrict__ Hc, const float (&zq)[18], float (&acc)[18])
+{
+  if constexpr (T < END)
+    {
+      constexpr int c = pair_c(T), d = pair_d(T);
+      const float h = __ldg(Hc + T * 8);
+      acc[c] = fmaf(h, zq[d], acc[c]);
+      if constexpr (c != d) acc[d] = fmaf(h, zq[c], acc[d]);
+      hz_terms<T + 1, END>(Hc, zq, acc);
+    }
+}
+
+// one third of H_q Z_q: entries G*57 .. G*57+56
+template <int G>
+__device__ __forceinline__ void hz_part(const float *__restrict__ Hc, const float (&zq)[18], float (&acc)[18])
+{
+#pragma unroll
+  for (int i = 0; i < 18; ++i) acc[i] = 0.f;
+  hz_terms<G * 57, G * 57 + 57>(Hc, zq, acc);
+}
+
+// r[a] = sum_q val_q(a) w[q] + sum_k sum_q dval_q(a)/dxi_k F_k[q] (reference cube), a = ax + 2 ay + 4 az:
+// the transposed interpolation, sum-factorised axis by axis
+__device__ __forceinline__ void mf_contract(const float (&w)[8], const float (&F)[3][8], float (&r)[8])
+{
+      {
+    float tx[2][4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      {
+        tx[0][t] = kGbF * w[2 * t] + kGaF * w[2 * t + 1];
+        tx[1][t] = kGaF * w[2 * t] + kGbF * w[2 * t + 1];
+      }
+    float ty[2][2][2];
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax)
+#pragma unroll
+      for (int qz = 0; qz < 2; ++qz)
+        {
+          ty[ax][0][qz] = kGbF * tx[ax][2 * qz] + kGaF * tx[ax][2 * qz + 1];
+          ty[ax][1][qz] = kGaF * tx[ax][2 * qz] + kGbF * tx[ax][2 * qz + 1];
+        }
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax)
+#pragma unroll
+      for (int ay = 0; ay < 2; ++ay)
+        {
+          r[ax + 2 * ay] = kGbF * ty[ax][ay][0] + kGaF * ty[ax][ay][1];
+          r[ax + 2 * ay + 4] = kGaF * ty[ax][ay][0] + kGbF * ty[ax][ay][1];
+        }
+  }
+  {
+    float sx[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) sx[t] = F[0][2 * t] + F[0][2 * t + 1];
+    float uy[2][2];
+#pragma unroll
+    for (int qz = 0; qz < 2; ++qz)
+      {
+        uy[0][qz] = kGbF * sx[2 * qz] + kGaF * sx[2 * qz + 1];
+        uy[1][qz] = kGaF * sx[2 * qz] + kGbF * sx[2 * qz + 1];
+      }
+#pragma unroll
+    for (int ay = 0; ay < 2; ++ay)
+#pragma unroll
+      for (int az = 0; az < 2; ++az)
+        {
+          const float v = az ? kGaF * uy[ay][0] + kGbF * uy[ay][1] : kGbF * uy[ay][0] + kGaF * uy[ay][1];
+          r[1 + 2 * ay + 4 * az] += v;
+          r[2 * ay + 4 * az] -= v;
+        }
+  }
+  {
+    float sy[4];
+#pragma unroll
+    for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+      for (int qx = 0; qx < 2; ++qx) sy[qx + 2 * qz] = F[1][qx + 4 * qz] + F[1][qx + 2 + 4 * qz];
+    float ux[2][2];
+#pragma unroll
+    for (int qz = 0; qz < 2; ++qz)
+      {
+        ux[0][qz] = kGbF * sy[2 * qz] + kGaF * sy[2 * qz + 1];
+        ux[1][qz] = kGaF * sy[2 * qz] + kGbF * sy[2 * qz + 1];
+      }
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax)
+#pragma unroll
+      for (int az = 0; az < 2; ++az)
+        {
+          const float v = az ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
+          r[ax + 2 + 4 * az] += v;
+          r[ax + 4 * az] -= v;
+        }
+  }
+  {
+    float sz[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) sz[t] = F[2][t] + F[2][t + 4];
+    float ux[2][2];
+#pragma unroll
+    for (int qy = 0; qy < 2; ++qy)
+      {
+        ux[0][qy] = kGbF * sz[2 * qy] + kGaF * sz[2 * qy + 1];
+        ux[1][qy] = kGaF * sz[2 * qy] + kGbF * sz[2 * qy + 1];
+      }
+#pragma unroll
+    for (int ax = 0; ax < 2; ++ax)
+#pragma unroll
+      for (int ay = 0; ay < 2; ++ay)
+        {
+          const float v = ay ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
+          r[ax + 2 * ay + 4] += v;
+          r[ax + 2 * ay] -= v;
+        }
+  }
+}
+
 __global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *__restrict__ H,
                                                        const float *__restrict__ z, float *__restrict__ ycell,
                                                        const uint8_t *__restrict__ act, int *__restrict__ err)
 {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   MfSmem &S = *reinterpret_cast<MfSmem *>(smem_raw);
-  __shared__ __align__(8) uint64_t s_bar;
   const int tid = threadIdx.x;
   const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kMCells;
   const int ncb = static_cast<int>((m.nc - e0) < kMCells ? (m.nc - e0) : kMCells);
-  // the CTA's cells are consecutive, so their Hessians are one contiguous run of
-  // ncb * 5472 bytes (16-byte aligned): start its copy now, wait just before the product
+  const float *Hb = H + e0 * static_cast<int64_t>(kNS3) * 8;
   if (tid == 0)
-    {
-      const uint32_t bar = smem_addr(&s_bar);
-      const uint32_t bytes = static_cast<uint32_t>(ncb) * kNS3 * 8 * sizeof(float);
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1));
-      asm volatile("fence.mbarrier_init.release.cluster;");
-      asm volatile("fence.proxy.async.shared::cta;");
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes));
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(&S.Hs[0][0][0])),
-                   "l"(H + e0 * static_cast<int64_t>(kNS3) * 8), "r"(bytes), "r"(bar)
-                   : "memory");
-    }
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(Hb),
+                 "r"(static_cast<uint32_t>(ncb) * kNS3 * 8 * static_cast<uint32_t>(sizeof(float)))
+                 : "memory");
   if (tid < kMCells)
     {
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -130,14 +264,14 @@ __global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *_
           else if (!((mk >> c) & 1u))
             val = zv;
         }
-      S.zs[cl][v][c] = val;
+      S.u.zs[cl][v][c] = val;
     }
   __syncthreads();
   // Z and its physical gradient at the points: thread (cell, component)
   if (tid < kMCells * 18)
     {
       const int cl = tid / 18, c = tid - 18 * cl;
-      const float *xv = &S.zs[cl][0][c]; // xv[18 v], v = vx + 2 vy + 4 vz
+      const float *xv = &S.u.zs[cl][0][c]; // xv[18 v], v = vx + 2 vy + 4 vz
       float zq[2][4], zd[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t)
@@ -200,39 +334,26 @@ __global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *_
             }
         }
     }
-  __syncthreads();
-  // bounded wait for the Hessian copy; on timeout flag the error and poison the output
-  bool ready = false;
+  __syncthreads(); // Z, gZ complete
+  // w = H_q Z_q in three partial sums: thread (point, third of the 171 entries); a warp's
+  // lanes read the same entry for the 8 points of 4 cells (4 x 32 contiguous bytes, L2)
   {
-    const uint32_t bar = smem_addr(&s_bar);
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kMfWaitLimit && !done; ++it)
-      asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                   "selp.u32 %0, 1, 0, p;\n\t}"
-                   : "=r"(done)
-                   : "r"(bar), "r"(0)
-                   : "memory");
-    ready = done != 0;
-    if (!ready && tid == 0 && err) atomicExch(err, 1);
-  }
-  // w = H_q Z_q: thread (point, six rows); a warp's lanes read the same entry for the
-  // 8 points of 4 cells, which fall in distinct shared-memory banks
-  {
-    const int pq = tid & (kMPts - 1), part = tid / kMPts, cl = pq >> 3, q = pq & 7;
+    const int pq = tid & (kMPts - 1), g = tid / kMPts, cl = pq >> 3, q = pq & 7;
+    float zq[18], acc[18];
+#pragma unroll
+    for (int i = 0; i < 18; ++i) zq[i] = S.Z[pq][i];
+    __syncthreads(); // zs (aliased by the partial sums) is no longer read
     if (cl < ncb)
       {
-        const float *Hc = &S.Hs[cl][0][q];
-        const float *Zq = S.Z[pq];
-        const float nan = __int_as_float(0x7fc00000);
+        const float *Hc = Hb + cl * kNS3 * 8 + q;
+        if (g == 0)
+          hz_part<0>(Hc, zq, acc);
+        else if (g == 1)
+          hz_part<1>(Hc, zq, acc);
+        else
+          hz_part<2>(Hc, zq, acc);
 #pragma unroll
-        for (int r = 0; r < 6; ++r)
-          {
-            const int c = part * 6 + r;
-            float s = 0.f;
-#pragma unroll
-            for (int d = 0; d < 18; ++d) s += Hc[c_sym.off[c][d]] * Zq[d]; // c is warp-uniform
-            S.w[pq][c] = ready ? s : nan;
-          }
+        for (int i = 0; i < 18; ++i) S.u.part[g][pq][i] = acc[i];
       }
   }
   __syncthreads();
@@ -248,104 +369,14 @@ __global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *_
       for (int q = 0; q < 8; ++q)
         {
           const int pq = cl * 8 + q;
-          w[q] = S.w[pq][c];
+          w[q] = S.u.part[0][pq][c] + S.u.part[1][pq][c] + S.u.part[2][pq][c];
           const int base = 9 * part + 3 * mu;
           const float dterm = K23 * (S.gZ[pq][0][base] + S.gZ[pq][1][base + 1] + S.gZ[pq][2][base + 2]);
 #pragma unroll
           for (int k = 0; k < 3; ++k) F[k][q] = ih[k] * (K1 * S.gZ[pq][k][c] + (k == jc ? dterm : 0.f));
         }
       float r[8];
-      {
-        float tx[2][4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-          {
-            tx[0][t] = kGbF * w[2 * t] + kGaF * w[2 * t + 1];
-            tx[1][t] = kGaF * w[2 * t] + kGbF * w[2 * t + 1];
-          }
-        float ty[2][2][2];
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-          for (int qz = 0; qz < 2; ++qz)
-            {
-              ty[ax][0][qz] = kGbF * tx[ax][2 * qz] + kGaF * tx[ax][2 * qz + 1];
-              ty[ax][1][qz] = kGaF * tx[ax][2 * qz] + kGbF * tx[ax][2 * qz + 1];
-            }
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-          for (int ay = 0; ay < 2; ++ay)
-            {
-              r[ax + 2 * ay] = kGbF * ty[ax][ay][0] + kGaF * ty[ax][ay][1];
-              r[ax + 2 * ay + 4] = kGaF * ty[ax][ay][0] + kGbF * ty[ax][ay][1];
-            }
-      }
-      {
-        float sx[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) sx[t] = F[0][2 * t] + F[0][2 * t + 1];
-        float uy[2][2];
-#pragma unroll
-        for (int qz = 0; qz < 2; ++qz)
-          {
-            uy[0][qz] = kGbF * sx[2 * qz] + kGaF * sx[2 * qz + 1];
-            uy[1][qz] = kGaF * sx[2 * qz] + kGbF * sx[2 * qz + 1];
-          }
-#pragma unroll
-        for (int ay = 0; ay < 2; ++ay)
-#pragma unroll
-          for (int az = 0; az < 2; ++az)
-            {
-              const float v = az ? kGaF * uy[ay][0] + kGbF * uy[ay][1] : kGbF * uy[ay][0] + kGaF * uy[ay][1];
-              r[1 + 2 * ay + 4 * az] += v;
-              r[2 * ay + 4 * az] -= v;
-            }
-      }
-      {
-        float sy[4];
-#pragma unroll
-        for (int qz = 0; qz < 2; ++qz)
-#pragma unroll
-          for (int qx = 0; qx < 2; ++qx) sy[qx + 2 * qz] = F[1][qx + 4 * qz] + F[1][qx + 2 + 4 * qz];
-        float ux[2][2];
-#pragma unroll
-        for (int qz = 0; qz < 2; ++qz)
-          {
-            ux[0][qz] = kGbF * sy[2 * qz] + kGaF * sy[2 * qz + 1];
-            ux[1][qz] = kGaF * sy[2 * qz] + kGbF * sy[2 * qz + 1];
-          }
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-          for (int az = 0; az < 2; ++az)
-            {
-              const float v = az ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
-              r[ax + 2 + 4 * az] += v;
-              r[ax + 4 * az] -= v;
-            }
-      }
-      {
-        float sz[4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t) sz[t] = F[2][t] + F[2][t + 4];
-        float ux[2][2];
-#pragma unroll
-        for (int qy = 0; qy < 2; ++qy)
-          {
-            ux[0][qy] = kGbF * sz[2 * qy] + kGaF * sz[2 * qy + 1];
-            ux[1][qy] = kGaF * sz[2 * qy] + kGbF * sz[2 * qy + 1];
-          }
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-          for (int ay = 0; ay < 2; ++ay)
-            {
-              const float v = ay ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
-              r[ax + 2 * ay + 4] += v;
-              r[ax + 2 * ay] -= v;
-            }
-      }
+      mf_contract(w, F, r);
       if (cl < ncb)
         {
           const float jxw = S.jxw[cl];
@@ -355,6 +386,7 @@ __global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *_
         }
     }
   (void)act;
+  (void)err;
 }
 
 // Node gather, one warp per node: s = sum of the row's cell contributions (the identity on
