@@ -174,9 +174,12 @@ def batched_leg(gl, count, linear_tol, sur=None, precond=None):
             "sample": "seeded (seed 4) instances of the sweep: T/Tc~U(0.3,0.95), p~U(0,34), D~U(8,40), n~U{16..48}"}
 
 
-def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None, precond=None):
+def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None, precond=None,
+              cfg=None):
     prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision,
                                precond=gl.PC_BLOCK_JACOBI if precond is None else precond)
+    if cfg is not None:
+        prm = importlib.import_module("verkko-hem-repo_gb300.autotune").params_with(gl, prm, cfg)
     f = gl.FemGL(m, prm)
     out = None
     for _ in range(warmup):
@@ -217,9 +220,11 @@ def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=Fal
             "launches": launches, "x": x, "F": F, "asm_ms": asm_ms, "mg": mg}
 
 
-def e2e_mode(gl, m, x0, precision, steps, linear_tol, precond=None):
+def e2e_mode(gl, m, x0, precision, steps, linear_tol, precond=None, cfg=None):
     prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision,
                                precond=gl.PC_BLOCK_JACOBI if precond is None else precond)
+    if cfg is not None:
+        prm = importlib.import_module("verkko-hem-repo_gb300.autotune").params_with(gl, prm, cfg)
     f = gl.FemGL(m, prm)
     start = x0 if callable(x0) else (lambda: np.ascontiguousarray(x0))
     solve_once(f, start(), linear_tol)
@@ -277,6 +282,8 @@ def main():
     ap.add_argument("--ncu-mlp", type=int, default=0, help="profiling case: surrogate forward on N points + one gradient")
     ap.add_argument("--precond", default="mg", choices=["mg", "bj"],
                     help="preconditioner of every GPU leg: geometric multigrid (default) or block-Jacobi")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the autotuner (the headline then uses the default configuration)")
     ap.add_argument("--headline-start", default="bphase", choices=["bphase", "learned"],
                     help="start of the headline solves (the other start is reported beside it)")
     args = ap.parse_args()
@@ -356,10 +363,19 @@ def main():
                     flush=flush, precond=pc) if alt_x0 is not None else None
     use_learned = alt is not None and args.headline_start == "learned"
     head_x0 = learned_x0 if use_learned else x0
+    # the autotuner picks preconditioner, restart, multigrid sweeps and the matrix-free
+    # operator's cell batch for this workload (complete solves timed before the timed region)
+    tuned = None
+    if args.autotune:
+        AT = importlib.import_module("verkko-hem-repo_gb300.autotune")
+        t0 = time.perf_counter()
+        tuned = AT.tune(gl, [m], [gl.Params.from_matep(P_BAR, T_RED, precision=gl.MIXED)], x0, args.linear_tol, TOL)
+        tuned["tuning_s"] = time.perf_counter() - t0
+    head_cfg = tuned["config"] if tuned else None
     with ClockSampler() as clk:
         mixed = time_mode(gl, m, head_x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
-                          flush=flush, precond=pc)
-    e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc)
+                          flush=flush, precond=pc, cfg=head_cfg)
+    e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
     batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc) if args.batch > 0 else None
 
     ms_step = float(np.mean(mixed["ms"]))
@@ -395,8 +411,10 @@ def main():
         "data": "synthetic (seeded B-phase + Gaussian noise start; no dataset)",
         "config": {"workload": WORKLOAD, "n_dofs": nd, "nnzb": nnzb,
                    "mode": "mixed+learned" if use_learned else "mixed", "linear_tol": args.linear_tol,
-                   "precond": ("geometric multigrid V(1,1): Galerkin coarse levels, l1 block-Jacobi smoothing, "
-                               "flexible GMRES(50)") if pc == gl.PC_MULTIGRID else "block-Jacobi, GMRES(50)",
+                   "precond": ("geometric multigrid: Galerkin coarse levels, l1 block-Jacobi smoothing, "
+                               "flexible GMRES") if (head_cfg or {"precond": "mg" if pc == gl.PC_MULTIGRID else "bj"})[
+                                   "precond"] == "mg" else "block-Jacobi, GMRES",
+                   "solver_config": head_cfg,
                    "mg_levels": mixed["mg"]["levels"], "gmres_restart": 50,
                    "l2": "inputs > L2 (FP32 BSR 1.18 GB) and a 256 MB L2 flush between steps"},
         "newton_its": int(mixed["out"]["newton_its"][0]),
@@ -411,6 +429,9 @@ def main():
             "newton_its": int(bj["out"]["newton_its"][0]), "gmres_its": int(bj["out"]["gmres_its"][0]),
             "free_energy": bj["F"]},
         "mg_fallbacks": mixed["mg"]["fallbacks"],
+        "autotune": None if tuned is None else {
+            "config": tuned["config"], "ms_best_trial": tuned["ms"], "tuning_s": tuned["tuning_s"],
+            "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]]},
         "mixed_learned_start": None if alt is None else {
             "solves_per_s": 1000.0 / float(np.mean(alt["ms"])), "newton_its": int(alt["out"]["newton_its"][0]),
             "gmres_its": int(alt["out"]["gmres_its"][0]), "free_energy": alt["F"]},

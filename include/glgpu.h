@@ -100,6 +100,7 @@ typedef struct
   int damped;           /* "Using dampped Newton iteration" (1) or full Newton (0) */
   int mg_pre, mg_post;  /* multigrid: l1 block-Jacobi sweeps before / after the coarse correction (1, 1) */
   double mg_omega;      /* multigrid: damping of the l1 block-Jacobi smoother (default 1) */
+  int mf_cells;         /* cells per CTA of the matrix-free FP32 operator: 4, 8 (default) or 16 */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;

@@ -83,7 +83,7 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
 // output is then NaN, which the solver's norms report).
 cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *ycell, float *y, const float *b,
                       const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
-                      int *err = nullptr);
+                      int *err = nullptr, int cells_per_cta = 8);
 // One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives
 // y = omega D^-1 b.  18x18 blocks only; y must not alias z.
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,

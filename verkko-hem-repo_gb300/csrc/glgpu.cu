@@ -325,7 +325,7 @@ glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
   if (c->mf)
     return launch(c, KK_SPMV, 2, [&] {
       return launch_mf(c->dm, static_cast<const float *>(c->H), static_cast<const float *>(in), c->ycell,
-                       static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err);
+                       static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err, c->prm[0].mf_cells);
     });
   return launch(c, KK_SPMV, 1, [&] { return launch_spmv(c->dm, c->mixed, c->vals, in, out, act, c->st); });
 }
@@ -839,7 +839,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
       return launch(L, KK_PREC, 2, [&] {
         return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(zin), L->ycell,
                          static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
-                         static_cast<float>(om), 2, act, L->st, L->d_err);
+                         static_cast<float>(om), 2, act, L->st, L->d_err, L->prm[0].mf_cells);
       });
     return launch(L, KK_PREC, 1, [&] { return launch_smooth(L->dm, m, L->vals, sm, r, zin, zout, om, act, L->st); });
   };
@@ -855,7 +855,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   if (L->mf)
     CKS(launch(L, KK_SPMV, 2, [&] {
       return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(cur), L->ycell,
-                       static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err);
+                       static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err, L->prm[0].mf_cells);
     }));
   else
     CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
@@ -1069,6 +1069,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->mg_pre = 1;
   p->mg_post = 1;
   p->mg_omega = 1.0;
+  p->mf_cells = 8;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1082,11 +1083,14 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   for (int k = 0; k < n_inst; ++k)
     {
       if (prm[k].precision != prm[0].precision || prm[k].precond != prm[0].precond ||
-          prm[k].gmres_restart != prm[0].gmres_restart)
-        return set_error(GLGPU_ERR_ARG, "glgpu_create: precision, preconditioner and restart must match across instances");
+          prm[k].gmres_restart != prm[0].gmres_restart || prm[k].mf_cells != prm[0].mf_cells)
+        return set_error(GLGPU_ERR_ARG,
+                         "glgpu_create: precision, preconditioner, restart and mf_cells must match across instances");
     }
   if (prm[0].gmres_restart < 1 || prm[0].gmres_restart > 64)
     return set_error(GLGPU_ERR_ARG, "glgpu_create: gmres_restart must be in [1, 64]");
+  if (prm[0].mf_cells != 4 && prm[0].mf_cells != 8 && prm[0].mf_cells != 16)
+    return set_error(GLGPU_ERR_ARG, "glgpu_create: mf_cells must be 4, 8 or 16");
   int dev_count = 0;
   if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
     return set_error(GLGPU_ERR_CUDA, "glgpu_create: no CUDA device");

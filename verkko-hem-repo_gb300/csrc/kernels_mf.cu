@@ -22,26 +22,24 @@
 
 namespace glgpu
 {
-constexpr int kMCells = 8;               // cells per CTA
-constexpr int kMPts = kMCells * 8;       // (cell, point) pairs per CTA
-constexpr int kMThreads = 192;           // 3 threads per point in the Hessian product
+// cells per CTA (NC = 4, 8 or 16, a run-time choice): 8 NC (cell, point) pairs and 24 NC
+// threads (3 per point in the Hessian product)
 constexpr float kGaF = 0.21132486540518711775f; // Gauss point 1/2 - sqrt(3)/6 on [0, 1]
 constexpr float kGbF = 0.78867513459481288225f;
 
-struct MfSmem
+template <int NC> struct MfSmem
 {
   union
   {
-    float zs[kMCells][8][18];     // nodal values (gather -> interpolation)
-    float part[3][kMPts][18];     // H Z per point, in three partial sums (product -> contraction)
+    float zs[NC][8][18];       // nodal values (gather -> interpolation)
+    float part[3][NC * 8][18]; // H Z per point, in three partial sums (product -> contraction)
   } u;
-  float Z[kMPts][19];
-  float gZ[kMPts][3][18];
-  float ih[kMCells][3];
-  float jxw[kMCells];
-  float K1[kMCells], K23[kMCells];
+  float Z[NC * 8][19];
+  float gZ[NC * 8][3][18];
+  float ih[NC][3];
+  float jxw[NC];
+  float K1[NC], K23[NC];
 };
-
 
 __device__ __forceinline__ void gauss2f(float f0, float f1, float &q0, float &q1)
 {
@@ -214,12 +212,14 @@ __device__ __forceinline__ void mf_contract(const float (&w)[8], const float (&F
   }
 }
 
-__global__ void __launch_bounds__(kMThreads) k_mf_cell(DevMesh m, const float *__restrict__ H,
-                                                       const float *__restrict__ z, float *__restrict__ ycell,
-                                                       const uint8_t *__restrict__ act, int *__restrict__ err)
+template <int NC>
+__global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__restrict__ H,
+                                                     const float *__restrict__ z, float *__restrict__ ycell,
+                                                     const uint8_t *__restrict__ act, int *__restrict__ err)
 {
+  constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 24 * NC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  MfSmem &S = *reinterpret_cast<MfSmem *>(smem_raw);
+  MfSmem<NC> &S = *reinterpret_cast<MfSmem<NC> *>(smem_raw);
   const int tid = threadIdx.x;
   const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kMCells;
   const int ncb = static_cast<int>((m.nc - e0) < kMCells ? (m.nc - e0) : kMCells);
@@ -470,22 +470,34 @@ __global__ void __launch_bounds__(kMgWarps * 32) k_mf_gather(DevMesh m, const fl
     }
 }
 
+template <int NC>
+static cudaError_t launch_mf_cell(const DevMesh &m, const float *H, const float *z, float *ycell, const uint8_t *act,
+                                  int *err, cudaStream_t s)
+{
+  static bool attr = false;
+  if (!attr)
+    {
+      cudaError_t e = cudaFuncSetAttribute(k_mf_cell<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(sizeof(MfSmem<NC>)));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+  const int64_t gc = (m.nc + NC - 1) / NC;
+  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, H, z, ycell, act, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *ycell, float *y, const float *b,
-                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s, int *err)
+                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s, int *err,
+                      int cells_per_cta)
 {
   if (m.dim != 3 || m.B != 18 || m.nv != 8) return cudaErrorInvalidValue;
   if (mode == 2 && !dinv) return cudaErrorInvalidValue;
   if (mode >= 1 && !b) return cudaErrorInvalidValue;
-  static bool attr = false;
-  if (!attr)
-    {
-      cudaError_t e =
-        cudaFuncSetAttribute(k_mf_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(MfSmem)));
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
-  const int64_t gc = (m.nc + kMCells - 1) / kMCells;
-  k_mf_cell<<<static_cast<unsigned>(gc), kMThreads, sizeof(MfSmem), s>>>(m, H, z, ycell, act, err);
+  cudaError_t e = cells_per_cta == 4    ? launch_mf_cell<4>(m, H, z, ycell, act, err, s)
+                  : cells_per_cta == 16 ? launch_mf_cell<16>(m, H, z, ycell, act, err, s)
+                                        : launch_mf_cell<8>(m, H, z, ycell, act, err, s);
+  if (e != cudaSuccess) return e;
   const int64_t gn = (m.nn + kMgWarps - 1) / kMgWarps;
   k_mf_gather<<<static_cast<unsigned>(gn), kMgWarps * 32, 0, s>>>(m, ycell, z, b, dinv, y, omega, mode, act);
   return cudaGetLastError();
