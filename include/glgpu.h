@@ -101,6 +101,9 @@ typedef struct
   int mg_pre, mg_post;  /* multigrid: l1 block-Jacobi sweeps before / after the coarse correction (1, 1) */
   double mg_omega;      /* multigrid: damping of the l1 block-Jacobi smoother (default 1) */
   int mf_cells;         /* cells per CTA of the matrix-free FP32 operator: 4, 8 (default) or 16 */
+  double prec_reuse;    /* mixed multigrid: keep the previous Newton step's preconditioner (and skip
+                           re-assembling the block matrix, rebuilt on demand) while the last step
+                           |a delta| / |x| < prec_reuse; 0 (default) rebuilds every step */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;

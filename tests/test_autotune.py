@@ -23,22 +23,25 @@ def _fake(costs, fails=()):
         if key in fails:
             return None
         return 100.0 + costs["precond"][cfg["precond"]] + costs["restart"][cfg["gmres_restart"]] + \
-            costs["sweeps"][(cfg["mg_pre"], cfg["mg_post"])] + costs["cells"][cfg["mf_cells"]]
+            costs["sweeps"][(cfg["mg_pre"], cfg["mg_post"])] + costs["cells"][cfg["mf_cells"]] + \
+            costs.get("reuse", {}).get(cfg["prec_reuse"], 0.0)
 
     return measure, calls
 
 
 COSTS = {"precond": {"mg": 0.0, "bj": 50.0}, "restart": {30: 5.0, 50: 0.0, 64: -8.0},
-         "sweeps": {(1, 1): 0.0, (2, 1): -3.0, (2, 2): 4.0}, "cells": {4: 6.0, 8: 0.0, 16: -10.0}}
+         "sweeps": {(1, 1): 0.0, (2, 1): -3.0, (2, 2): 4.0}, "cells": {4: 6.0, 8: 0.0, 16: -10.0},
+         "reuse": {0.0: 0.0, 1e-2: -2.0, 1e-1: -4.0, 1.0: 3.0}}
 
 
 def test_search_finds_the_best_coordinates():
     measure, calls = _fake(COSTS)
     out = at.search(measure, margin=0.0)
-    assert out["config"] == {"precond": "mg", "gmres_restart": 64, "mg_pre": 2, "mg_post": 1, "mf_cells": 16}
-    assert out["ms"] == pytest.approx(100.0 - 8.0 - 3.0 - 10.0)
-    # one start plus the other values of each coordinate: 1 + 1 + 2 + 2 + 2
-    assert len(calls) == 8 and len(out["trials"]) == 8
+    assert out["config"] == {"precond": "mg", "gmres_restart": 64, "mg_pre": 2, "mg_post": 1, "mf_cells": 16,
+                             "prec_reuse": 1e-1}
+    assert out["ms"] == pytest.approx(100.0 - 8.0 - 3.0 - 10.0 - 4.0)
+    # one start plus the other values of each coordinate: 1 + 1 + 2 + 2 + 2 + 3
+    assert len(calls) == 11 and len(out["trials"]) == 11
 
 
 def test_search_margin_and_failures():
@@ -56,6 +59,7 @@ def test_search_margin_and_failures():
     out = at.search(measure, margin=0.0, multigrid=False)
     assert all(c["precond"] == "bj" for c in calls) and out["config"]["precond"] == "bj"
     assert {(c["mg_pre"], c["mg_post"]) for c in calls} == {(1, 1)}
+    assert {c["prec_reuse"] for c in calls} == {0.0}
     # a start that does not converge is an error
     with pytest.raises(RuntimeError):
         at.search(lambda cfg: None)

@@ -133,3 +133,32 @@ def test_multigrid_falls_back_on_refined_mesh(gl):
     x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=1)
     its, d, J, rhs, lev = _solve(gl, m, x0, gl.PC_MULTIGRID)
     assert lev == 0 and its > 0
+
+
+def test_preconditioner_reuse(gl):
+    # keeping the previous step's multigrid hierarchy for small Newton steps changes the
+    # Krylov path only: same Newton history and free energy; and the block matrix, not
+    # re-assembled on such steps, is rebuilt when it is read
+    m = gl.cube_mesh(5.0, 8)
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=2)
+    res = {}
+    for reuse in (0.0, 1e-2):
+        prm = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID, prec_reuse=reuse)
+        with gl.FemGL(m, prm) as f:
+            f.set_solution(x0)
+            out = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+            x, F = f.solution(), f.free_energy()[0]
+            f.assemble_system()
+            _, _, J, _ = f.system()
+        res[reuse] = (out, x, F, J)
+    o0, x0r, F0, _ = res[0.0]
+    o1, x1, F1, J1 = res[1e-2]
+    assert o0["converged"] and o1["converged"]
+    assert o1["newton_its"][0] == o0["newton_its"][0]
+    assert abs(F1 - F0) <= 1e-12 * abs(F0)
+    prm = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID)
+    with gl.FemGL(m, prm) as g:
+        g.set_solution(x1)
+        g.assemble_system()
+        _, _, Jf, _ = g.system()
+    assert np.array_equal(J1, Jf)

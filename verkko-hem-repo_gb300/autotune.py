@@ -8,7 +8,8 @@ picks the configuration that solves fastest:
   block-Jacobi;
 * the GMRES restart length;
 * the multigrid smoothing sweeps before / after the coarse correction;
-* the cell batch of the matrix-free FP32 operator (cells per CTA: 4, 8 or 16).
+* the cell batch of the matrix-free FP32 operator (cells per CTA: 4, 8 or 16);
+* how small a Newton step must be for the next step to keep the multigrid preconditioner.
 
 Each candidate is timed on one complete Newton solve of the instances from the given start
 (CUDA events around ``run``, after a warm-up solve that also builds the CUDA graphs).
@@ -23,12 +24,13 @@ import json
 import os
 from typing import Callable, Optional, Sequence
 
-DEFAULT = {"precond": "mg", "gmres_restart": 50, "mg_pre": 1, "mg_post": 1, "mf_cells": 8}
+DEFAULT = {"precond": "mg", "gmres_restart": 50, "mg_pre": 1, "mg_post": 1, "mf_cells": 8, "prec_reuse": 0.0}
 SEARCH = (
     ("precond", ("mg", "bj")),
     ("gmres_restart", (30, 50, 64)),
     ("mg_sweeps", ((1, 1), (2, 1), (2, 2))),
     ("mf_cells", (4, 8, 16)),
+    ("prec_reuse", (0.0, 1e-2, 1e-1, 1.0)),
 )
 
 
@@ -65,7 +67,7 @@ def search(measure: Callable[[dict], Optional[float]], start: Optional[dict] = N
     if best is None:
         raise RuntimeError("autotune: the starting configuration does not converge")
     for key, values in SEARCH:
-        if key == "mg_sweeps" and cfg["precond"] != "mg":
+        if key in ("mg_sweeps", "prec_reuse") and cfg["precond"] != "mg":
             continue
         if key == "precond" and not multigrid:
             continue
@@ -86,7 +88,8 @@ def params_with(gl, params, cfg: dict):
 
     pc = gl.PC_MULTIGRID if cfg["precond"] == "mg" else gl.PC_BLOCK_JACOBI
     return dataclasses.replace(params, precond=pc, gmres_restart=int(cfg["gmres_restart"]), mg_pre=int(cfg["mg_pre"]),
-                               mg_post=int(cfg["mg_post"]), mf_cells=int(cfg["mf_cells"]))
+                               mg_post=int(cfg["mg_post"]), mf_cells=int(cfg["mf_cells"]),
+                               prec_reuse=float(cfg.get("prec_reuse", 0.0)))
 
 
 def tune(gl, meshes: Sequence, params: Sequence, x0, linear_tol: float = 1e-4, tol: float = 1e-10,

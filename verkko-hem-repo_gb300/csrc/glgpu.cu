@@ -137,6 +137,9 @@ struct glgpu_ctx
   float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
   int *d_err = nullptr;              // device-side wait timeouts (matrix-free Hessian copies)
   bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
+  bool prec_built = false;           // a multigrid hierarchy exists for some earlier Jacobian
+  bool bsr_stale = false;            // the block matrix lags the Hessians (matrix-free steps)
+  double last_step_rel = 1e300;      // max over instances of |a delta| / |x| of the last step
   // the V-cycle as a CUDA graph (captured on first use; every pointer it touches is fixed)
   cudaGraphExec_t vc_exec = nullptr;
   void *mg_in = nullptr, *mg_out = nullptr;
@@ -482,7 +485,10 @@ glgpu_status prec_setup(glgpu_ctx *c, const uint8_t *act)
   if (c->prec_ready) return GLGPU_OK;
   const int pc = c->prm[0].precond;
   if (pc == GLGPU_PC_MULTIGRID && c->n_levels > 0)
-    CKS(mg_assemble(c, act));
+    {
+      CKS(mg_assemble(c, act));
+      c->prec_built = true;
+    }
   else if (pc >= GLGPU_PC_BLOCK_JACOBI)
     CKS(bj_setup(c));
   if (pc == GLGPU_PC_CHEBYSHEV)
@@ -1070,6 +1076,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->mg_post = 1;
   p->mg_omega = 1.0;
   p->mf_cells = 8;
+  p->prec_reuse = 0.0;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1356,6 +1363,8 @@ extern "C" glgpu_status glgpu_set_solution(glgpu_ctx *c, const double *x)
   c->launches += 2;
   c->has_J = c->has_rhs = c->has_delta = false;
   std::fill(c->r_ok.begin(), c->r_ok.end(), 0);
+  c->prec_built = false;
+  c->last_step_rel = 1e300;
   return sync(c);
 }
 
@@ -1390,7 +1399,17 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
           return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, nullptr, act, c->st);
         }));
     }
-  CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
+  // a small last Newton step keeps the previous preconditioner; the matrix-free operator
+  // needs only H, so the block matrix is then rebuilt only on demand
+  const double reuse = c->prm[0].prec_reuse;
+  const bool keep_prec = reuse > 0 && c->mf && c->n_levels > 0 && c->prec_built && c->last_step_rel < reuse;
+  if (keep_prec)
+    c->bsr_stale = true;
+  else
+    {
+      CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
+      c->bsr_stale = false;
+    }
   if (need_r) CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   CKS(axpby(c, c->R, c->rhs, nullptr, coefs(-1.0, 0.0), act, false, false, false));
   std::vector<double> nr;
@@ -1400,7 +1419,7 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
   c->has_J = c->has_rhs = true;
   for (int k = 0; k < c->n_inst; ++k)
     if (!act || c->inst_on[k]) c->r_ok[k] = 1;
-  c->prec_ready = c->dinv_ready = false;
+  if (!keep_prec) c->prec_ready = c->dinv_ready = false;
   for (int k = 0; k < c->n_inst; ++k)
     if ((!act || c->inst_on[k]) && !std::isfinite(c->rhs_norm[k]))
       return set_error(GLGPU_ERR_NAN, "assemble_system: non-finite residual in instance " + std::to_string(k));
@@ -1519,6 +1538,16 @@ static glgpu_status newton_impl(glgpu_ctx *c, std::vector<double> &res, std::vec
   // R, r_cell, e_cell now hold the values at the new x of every instance of the step
   for (int k = 0; k < n; ++k)
     if (c->inst_on[k]) c->r_ok[k] = 1;
+  if (c->prm[0].prec_reuse > 0)
+    {
+      std::vector<double> nd, nx;
+      CKS(norms_d(c, c->delta, c->d_act, nd));
+      CKS(norms_d(c, c->x, c->d_act, nx));
+      double rel = 0.0;
+      for (int k = 0; k < n; ++k)
+        if (c->inst_on[k]) rel = std::max(rel, (nx[k] > 0 ? a[k] * nd[k] / nx[k] : 1e300));
+      c->last_step_rel = rel;
+    }
   for (int k = 0; k < n; ++k)
     if (c->inst_on[k] && !std::isfinite(res[k]))
       return set_error(GLGPU_ERR_NAN, "newton_iteration: non-finite residual in instance " + std::to_string(k));
@@ -1595,6 +1624,11 @@ extern "C" glgpu_status glgpu_get_system(const glgpu_ctx *cc, int32_t *rowptr, i
 {
   glgpu_ctx *c = const_cast<glgpu_ctx *>(cc);
   if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_get_system: NULL context");
+  if (c->bsr_stale)
+    {
+      CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
+      c->bsr_stale = false;
+    }
   if (rowptr) std::memcpy(rowptr, c->P.rowptr.data(), sizeof(int32_t) * c->P.rowptr.size());
   if (cols) std::memcpy(cols, c->P.cols.data(), sizeof(int32_t) * c->P.cols.size());
   const size_t nv = static_cast<size_t>(c->nnzb) * c->B * c->B;

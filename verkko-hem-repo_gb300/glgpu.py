@@ -58,7 +58,7 @@ class _Params(ctypes.Structure):
                 ("precond", ctypes.c_int), ("cheb_degree", ctypes.c_int), ("gmres_restart", ctypes.c_int),
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
                 ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
-                ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int)]
+                ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double)]
 
 
 _lib = None
@@ -278,6 +278,7 @@ class Params:
     mg_post: int = 1
     mg_omega: float = 1.0
     mf_cells: int = 8
+    prec_reuse: float = 0.0
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -295,6 +296,7 @@ class Params:
         s.ls_step, s.ls_max_trials, s.damped = float(self.ls_step), int(self.ls_max_trials), int(bool(self.damped))
         s.mg_pre, s.mg_post, s.mg_omega = int(self.mg_pre), int(self.mg_post), float(self.mg_omega)
         s.mf_cells = int(self.mf_cells)
+        s.prec_reuse = float(self.prec_reuse)
         return s
 
 
