@@ -120,15 +120,19 @@ def batch_instances(gl, count, seed=4):
     return out
 
 
-def batched_leg(gl, count, linear_tol, sur=None, precond=None):
+def batched_leg(gl, count, linear_tol, sur=None, precond=None, cfg=None):
     """Batched mixed solve of `count` instances in one context (from the B phase and, with
-    a surrogate, from its guess) vs the plain FP64 GPU Newton solving them one at a time
-    from the B phase; all to ||F|| < 1e-10 per instance."""
+    a surrogate, from its guess) vs FP64 GPU Newton solving them one at a time from the B
+    phase, with the same preconditioner and with the plain method (block-Jacobi GMRES);
+    all to ||F|| < 1e-10 per instance."""
     inst = batch_instances(gl, count)
     meshes = [d["mesh"] for d in inst]
     x0 = np.concatenate([d["x0"] for d in inst])
     pc = gl.PC_BLOCK_JACOBI if precond is None else precond
     prm_m = [gl.Params.from_matep(d["p"], d["t"], precision=gl.MIXED, precond=pc) for d in inst]
+    if cfg is not None:  # the configuration the autotuner chose for the headline workload
+        AT = importlib.import_module("verkko-hem-repo_gb300.autotune")
+        prm_m = [AT.params_with(gl, p, cfg) for p in prm_m]
     f = gl.FemGL(meshes, prm_m)
     f.set_solution(x0)
     f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)  # warm-up
@@ -154,6 +158,18 @@ def batched_leg(gl, count, linear_tol, sur=None, precond=None):
         its_s.append(int(o["newton_its"][0]))
         g.close()
     F_s = np.array(F_s)
+    # the plain FP64 GPU Newton (block-Jacobi GMRES, the method without multigrid) on the
+    # same instances, one at a time
+    ms_plain = 0.0
+    for d in inst:
+        prm = gl.Params.from_matep(d["p"], d["t"], precision=gl.FP64, precond=gl.PC_BLOCK_JACOBI)
+        g = gl.FemGL(d["mesh"], prm)
+        g.set_solution(d["x0"])
+        g.sync()
+        g.event_start()
+        g.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+        ms_plain += g.event_stop()
+        g.close()
     learned = None
     if sur is not None:
         L = importlib.import_module("verkko-hem-repo_gb300.learned")
@@ -161,13 +177,16 @@ def batched_leg(gl, count, linear_tol, sur=None, precond=None):
         L.solve_learned(gl, sur, li, gl.MIXED, linear_tol, precond=pc)  # warm-up
         _, ol, ms_l, finfo = L.solve_learned(gl, sur, li, gl.MIXED, linear_tol, precond=pc)
         learned = {"mixed_batched_learned_solves_per_s": count / (ms_l / 1000.0),
-                   "speedup_vs_fp64_sequential": ms_seq / ms_l, "newton_its": ol["newton_its"].tolist(),
+                   "speedup_vs_fp64_sequential": ms_seq / ms_l, "speedup_vs_plain_fp64": ms_plain / ms_l,
+                   "newton_its": ol["newton_its"].tolist(),
                    "max_free_energy_rel_diff_vs_fp64": float(np.max(np.abs(ol["free_energy"] - F_s) / np.abs(F_s))),
                    "all_converged": bool(np.all(ol["residual"] <= TOL)), "fallbacks": finfo["fallbacks"]}
     return {"instances": count, "learned": learned, "total_dofs": int(sum(18 * m.nn for m in meshes)),
             "mixed_batched_solves_per_s": count / (ms_batch / 1000.0),
             "fp64_sequential_solves_per_s": count / (ms_seq / 1000.0),
-            "speedup": ms_seq / ms_batch, "all_converged": bool(out["converged"]),
+            "plain_fp64_sequential_solves_per_s": count / (ms_plain / 1000.0),
+            "speedup": ms_seq / ms_batch, "speedup_vs_plain_fp64": ms_plain / ms_batch,
+            "all_converged": bool(out["converged"]),
             "max_final_residual": float(out["residual"].max()),
             "max_free_energy_rel_diff_vs_fp64": float(np.max(np.abs(F_b - F_s) / np.abs(F_s))),
             "newton_its_batched": out["newton_its"].tolist(), "newton_its_fp64": its_s,
@@ -376,7 +395,7 @@ def main():
         mixed = time_mode(gl, m, head_x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
                           flush=flush, precond=pc, cfg=head_cfg)
     e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
-    batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc) if args.batch > 0 else None
+    batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc, cfg=head_cfg) if args.batch > 0 else None
 
     ms_step = float(np.mean(mixed["ms"]))
     value = 1000.0 / ms_step

@@ -30,7 +30,7 @@ def _fake(costs, fails=()):
 
 
 COSTS = {"precond": {"mg": 0.0, "bj": 50.0}, "restart": {30: 5.0, 50: 0.0, 64: -8.0},
-         "sweeps": {(1, 1): 0.0, (2, 1): -3.0, (2, 2): 4.0}, "cells": {4: 6.0, 8: 0.0, 16: -10.0},
+         "sweeps": {(1, 1): 0.0, (1, 0): 1.0, (2, 1): -3.0, (2, 2): 4.0}, "cells": {4: 6.0, 8: 0.0, 16: -10.0},
          "reuse": {0.0: 0.0, 1e-2: -2.0, 1e-1: -4.0, 1.0: 3.0}}
 
 
@@ -40,14 +40,14 @@ def test_search_finds_the_best_coordinates():
     assert out["config"] == {"precond": "mg", "gmres_restart": 64, "mg_pre": 2, "mg_post": 1, "mf_cells": 16,
                              "prec_reuse": 1e-1}
     assert out["ms"] == pytest.approx(100.0 - 8.0 - 3.0 - 10.0 - 4.0)
-    # one start plus the other values of each coordinate: 1 + 1 + 2 + 2 + 2 + 3
-    assert len(calls) == 11 and len(out["trials"]) == 11
+    # one start plus the other values of each coordinate: 1 + 1 + 2 + 3 + 2 + 3
+    assert len(calls) == 12 and len(out["trials"]) == 12
 
 
 def test_search_margin_and_failures():
     # a 2% margin keeps the default when the gain is smaller
     small = {"precond": {"mg": 0.0, "bj": 50.0}, "restart": {30: 5.0, 50: 0.0, 64: -1.0},
-             "sweeps": {(1, 1): 0.0, (2, 1): 0.5, (2, 2): 0.5}, "cells": {4: 0.0, 8: 0.0, 16: 0.0}}
+             "sweeps": {(1, 1): 0.0, (1, 0): 0.5, (2, 1): 0.5, (2, 2): 0.5}, "cells": {4: 0.0, 8: 0.0, 16: 0.0}}
     measure, _ = _fake(small)
     assert at.search(measure, margin=0.02)["config"] == at.DEFAULT
     # a candidate that does not converge is skipped even when it would be fastest

@@ -28,7 +28,7 @@ DEFAULT = {"precond": "mg", "gmres_restart": 50, "mg_pre": 1, "mg_post": 1, "mf_
 SEARCH = (
     ("precond", ("mg", "bj")),
     ("gmres_restart", (30, 50, 64)),
-    ("mg_sweeps", ((1, 1), (2, 1), (2, 2))),
+    ("mg_sweeps", ((1, 1), (1, 0), (2, 1), (2, 2))),
     ("mf_cells", (4, 8, 16)),
     ("prec_reuse", (0.0, 1e-2, 1e-1, 1.0)),
 )
