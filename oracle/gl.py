@@ -58,7 +58,7 @@ def lib():
             build()
         L = ctypes.CDLL(ORACLE_SO)
         L.orc_bulk_q.argtypes = [_dp, _dp, _dp, _dp, _dp]
-        L.orc_cell_local.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_cell_local.argtypes = [_dp, _dp, _dp, ctypes.c_int, _dp, _dp, _dp]
         L.orc_pattern.restype = ctypes.c_long
         L.orc_pattern.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _ip, _ip, _dp, _ip, _ip]
         L.orc_assemble.restype = ctypes.c_int
@@ -87,6 +87,7 @@ def ref():
         L.ref_grad_vec.argtypes = [ctypes.c_int, _dp, _dp]
         L.ref_matep.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
         L.ref_cell_assemble.argtypes = [_dp, _dp, _dp, _dp, _dp]
+        L.ref_face_assemble.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
         _ref = L
     return _ref
 
@@ -97,9 +98,16 @@ def ref():
 K_REF = 0.42072  # K1 = K2 = K3 (reference femgl/inc/femgl.h:320-322)
 
 
-def coef_vector(alpha, betas, K1=K_REF, K2=K_REF, K3=K_REF):
-    """{K1, K2+K3, alpha, beta1..beta5}: the weights of assemble.cc:229-252."""
-    return np.array([K1, K2 + K3, alpha, *betas], dtype=np.float64)
+def coef_vector(alpha, betas, K1=K_REF, K2=K_REF, K3=K_REF, bt=1e10):
+    """{K1, K2+K3, alpha, beta1..beta5, K1/bt}: the weights of assemble.cc:229-252 and of
+    the Robin faces (assemble.cc:286-348; 0 when bt >= 1e10)."""
+    return np.array([K1, K2 + K3, alpha, *betas, K1 / bt if bt < 1e10 else 0.0], dtype=np.float64)
+
+
+def _coef9(coef):
+    c = np.zeros(9)
+    c[: len(coef)] = coef
+    return c
 
 
 # ---------------------------------------------------------------------------------
@@ -109,19 +117,19 @@ def bulk_q(coef, A):
     R = np.zeros(18)
     H = np.zeros(324)
     f = np.zeros(1)
-    lib().orc_bulk_q(_p(np.ascontiguousarray(coef, np.float64)), _p(np.ascontiguousarray(A, np.float64)), _p(R),
+    lib().orc_bulk_q(_p(_coef9(coef)), _p(np.ascontiguousarray(A, np.float64)), _p(R),
                      _p(H), _p(f))
     return R, H.reshape(18, 18), float(f[0])
 
 
-def cell_local(h, x, coef, want_K=True):
+def cell_local(h, x, coef, want_K=True, faces=0):
+    """One cell's matrix, residual pieces and energy; faces: bitmask of its Robin faces."""
     h = np.ascontiguousarray(h, np.float64)
     x = np.ascontiguousarray(x, np.float64).reshape(144)
     K = np.zeros((144, 144)) if want_K else None
     r = np.zeros(144)
     f = np.zeros(1)
-    lib().orc_cell_local(_p(h), _p(x), _p(np.ascontiguousarray(coef, np.float64)), _p(K) if want_K else None, _p(r),
-                         _p(f))
+    lib().orc_cell_local(_p(h), _p(x), _p(_coef9(coef)), int(faces), _p(K) if want_K else None, _p(r), _p(f))
     return K, r, float(f[0])
 
 
@@ -133,7 +141,7 @@ class System:
 
     def __init__(self, m: omesh.Mesh, coef):
         self.m = m
-        self.coef = np.ascontiguousarray(coef, np.float64)
+        self.coef = _coef9(coef)
         self.xyz = np.ascontiguousarray(m.xyz, np.float64)
         self.cells = np.ascontiguousarray(m.cells, np.int32)
         self.mask = np.ascontiguousarray(m.mask, np.uint32)

@@ -47,8 +47,9 @@
 
 typedef double complex cplx;
 
-/* coefficient vector: {K1, K2+K3, alpha, beta1..beta5} */
-enum { C_K1 = 0, C_K23 = 1, C_ALPHA = 2, C_B1 = 3 };
+/* coefficient vector: {K1, K2+K3, alpha, beta1..beta5, K1/bt} (the last is the Robin
+ * weight of the pair-breaking faces, 0 when bt >= 1e10: assemble.cc:286-348) */
+enum { C_K1 = 0, C_K23 = 1, C_ALPHA = 2, C_B1 = 3, C_ROBIN = 8 };
 
 static void to_cmat(const double *a, cplx M[3][3])
 {
@@ -274,7 +275,55 @@ static void q1_tables(const double *h, double val[8][8], double grd[8][8][3])
  * the Jacobian and as +R for the residual: K[144*144] (may be NULL), r[144]
  * (may be NULL), *fcell = cell free energy (may be NULL).
  */
-void orc_cell_local(const double *h, const double *x, const double *coef, double *K, double *r, double *fcell)
+/* The Robin (AdGR) term of one face of the cell: face `f` = 2 * axis + side, its four vertices
+ * are the v with bit `axis` of v equal to `side`.  On the face, with the 2x2 Gauss rule
+ * (assemble.cc:286-348, residual.cc:235-278, QGauss<dim-1>(2)):
+ *   K(i, j) += wR tr(phi_i phi_j^T) JxW,  r(i) += wR tr(A phi_i^T) JxW,  f += wR |A|^2 JxW,
+ * where every matrix has its normal column (orbital index = axis) zeroed
+ * (s_vector2matrix.cc:257-292) and wR = K1/bt. */
+static void robin_face(const double *h, const double *x, double wR, int f, double *K, double *r, double *fcell)
+{
+  const int axis = f / 2, side = f % 2;
+  const int t1 = (axis == 0) ? 1 : 0, t2 = (axis == 2) ? 1 : 2;
+  const double g = 0.5 - 0.28867513459481288225;
+  const double gp[2] = {g, 1.0 - g};
+  const double JxW = 0.25 * h[t1] * h[t2];
+  for (int q1 = 0; q1 < 2; ++q1)
+    for (int q2 = 0; q2 < 2; ++q2)
+      {
+        double phi[8];
+        for (int v = 0; v < 8; ++v)
+          {
+            if (((v >> axis) & 1) != side)
+              {
+                phi[v] = 0.0;
+                continue;
+              }
+            const int b1 = (v >> t1) & 1, b2 = (v >> t2) & 1;
+            phi[v] = (b1 ? gp[q1] : 1.0 - gp[q1]) * (b2 ? gp[q2] : 1.0 - gp[q2]);
+          }
+        double A[18] = {0};
+        for (int v = 0; v < 8; ++v)
+          for (int c = 0; c < 18; ++c) A[c] += phi[v] * x[18 * v + c];
+        for (int c = 0; c < 18; ++c)
+          {
+            if (c % 3 == axis) continue; /* the normal column */
+            if (fcell) *fcell += wR * A[c] * A[c] * JxW;
+            for (int v = 0; v < 8; ++v)
+              {
+                if (phi[v] == 0.0) continue;
+                if (r) r[18 * v + c] += wR * A[c] * phi[v] * JxW;
+                if (K)
+                  for (int w = 0; w < 8; ++w)
+                    if (phi[w] != 0.0) K[(size_t)(18 * v + c) * 144 + 18 * w + c] += wR * phi[v] * phi[w] * JxW;
+              }
+          }
+      }
+}
+
+/* faces: bit f set for each Robin face f = 2 * axis + side of the cell */
+void orc_cell_local(const double *h, const double *x, const double *coef, int faces, double *K, double *r,
+                    double *fcell)
 {
   double val[8][8], grd[8][8][3];
   q1_tables(h, val, grd);
@@ -338,6 +387,9 @@ void orc_cell_local(const double *h, const double *x, const double *coef, double
             }
     }
   if (fcell) *fcell = fsum;
+  if (faces && coef[C_ROBIN] != 0.0)
+    for (int f = 0; f < 6; ++f)
+      if ((faces >> f) & 1) robin_face(h, x, coef[C_ROBIN], f, K, r, fcell);
 }
 
 /* ------------------------------------------------------------------------------
@@ -476,6 +528,36 @@ void orc_distribute(int nn, const uint32_t *mask, const int *hptr, const int *hp
         }
 }
 
+/* Robin faces of a cell: the pair-breaking faces (boundary ids 2, 3, 4 in the reference,
+ * which also carry the zero-Dirichlet normal column, setup_uniform_B-phase.cc:134-157), i.e.
+ * faces perpendicular to an axis whose four vertices lie on a boundary plane with that
+ * axis' column masked.  An unconstrained node lies there when its mask holds the column; a
+ * hanging node when all its parents do (it sits on the segment or face they span). */
+static int on_masked_plane(const uint32_t *mask, const int *hptr, const int *hpar, int n, uint32_t col)
+{
+  if (!is_hanging(hptr, n)) return (mask[n] & col) == col;
+  for (int k = hptr[n]; k < hptr[n + 1]; ++k)
+    if ((mask[hpar[k]] & col) != col) return 0;
+  return 1;
+}
+
+static int robin_faces(const int *cell, const uint32_t *mask, const int *hptr, const int *hpar)
+{
+  int bits = 0;
+  for (int f = 0; f < 6; ++f)
+    {
+      const int axis = f / 2, side = f % 2;
+      uint32_t col = 0;
+      for (int part = 0; part < 2; ++part)
+        for (int mu = 0; mu < 3; ++mu) col |= 1u << (9 * part + 3 * mu + axis);
+      int ok = 1;
+      for (int v = 0; v < 8 && ok; ++v)
+        if (((v >> axis) & 1) == side && !on_masked_plane(mask, hptr, hpar, cell[v], col)) ok = 0;
+      if (ok) bits |= 1 << f;
+    }
+  return bits;
+}
+
 static void cell_h(const double *xyz, const int *cell, double *h)
 {
   for (int d = 0; d < 3; ++d) h[d] = xyz[3 * cell[7] + d] - xyz[3 * cell[0] + d];
@@ -508,7 +590,8 @@ int orc_assemble(int nn, const double *xyz, int nc, const int *cells, const uint
           double h[3], xl[144];
           cell_h(xyz, cells + 8 * e, h);
           for (int v = 0; v < 8; ++v) memcpy(xl + 18 * v, x + 18 * (size_t)cells[8 * e + v], sizeof(double) * 18);
-          orc_cell_local(h, xl, coef, J ? Kbuf + (size_t)(e - e0) * 144 * 144 : NULL, rbuf + (size_t)(e - e0) * 144,
+          orc_cell_local(h, xl, coef, robin_faces(cells + 8 * e, mask, hptr, hpar),
+                         J ? Kbuf + (size_t)(e - e0) * 144 * 144 : NULL, rbuf + (size_t)(e - e0) * 144,
                          fbuf + (e - e0));
         }
       for (int e = e0; e < e1; ++e)

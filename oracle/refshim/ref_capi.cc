@@ -265,4 +265,66 @@ void ref_cell_assemble(const double *h, const double *x, const double *coef, dou
     }
 }
 
+/*
+ * The Robin (AdGR) face term of one face of the same axis-aligned Q1 cell, evaluated the
+ * way the reference's assemble_system does it (femgl/src/assemble.cc:286-348): for every
+ * point of the face rule QGauss<2>(2), the iterate and every test / trial tensor are built
+ * with the face's normal column zeroed (femgl/src/s_vector2matrix.cc:220-292,
+ * femgl/src/phi_vector2matrix.cc:153-190) and the reference's face kernels are called with
+ * the weights and signs of assemble.cc:322-336.
+ *
+ * face = 2 * axis + side: the face whose vertices have bit `axis` of v equal to `side`;
+ * it plays the boundary id 2 + axis.  Adds into cell_matrix [144][144] (may be NULL) and
+ * cell_rhs [144].
+ */
+void ref_face_assemble(const double *h, const double *x, double K1, double bt, int face, double *cell_matrix,
+                       double *cell_rhs)
+{
+  const int axis = face / 2, side = face % 2;
+  const int t1 = (axis == 0) ? 1 : 0, t2 = (axis == 2) ? 1 : 2;
+  const double g = 0.5 - std::sqrt(3.0) / 6.0;
+  const double gp[2] = {g, 1.0 - g};
+  const double JxW = 0.25 * h[t1] * h[t2];
+  FemGL<3> &f = obj();
+  FullMatrix<double> u0(3, 3), v0(3, 3), pui(3, 3), pvi(3, 3), puj(3, 3), pvj(3, 3);
+
+  for (int q = 0; q < 4; ++q)
+    {
+      double val[8];
+      for (int v = 0; v < 8; ++v)
+        {
+          const int b1 = (v >> t1) & 1, b2 = (v >> t2) & 1;
+          const double s1 = b1 ? gp[q & 1] : 1.0 - gp[q & 1], s2 = b2 ? gp[q >> 1] : 1.0 - gp[q >> 1];
+          val[v] = (((v >> axis) & 1) == side) ? s1 * s2 : 0.0;
+        }
+      auto shape = [&](int i, FullMatrix<double> &pu, FullMatrix<double> &pv) {
+        pu = 0.0;
+        pv = 0.0;
+        const int v = i / 18, c = i % 18, cc = c % 9;
+        if (cc % 3 == axis) return; /* the normal column stays zero */
+        ((c < 9) ? pu : pv)(cc / 3, cc % 3) = val[v];
+      };
+      u0 = 0.0;
+      v0 = 0.0;
+      for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 18; ++c)
+          {
+            const int cc = c % 9;
+            if (cc % 3 == axis) continue;
+            ((c < 9) ? u0 : v0)(cc / 3, cc % 3) += x[18 * v + c] * val[v];
+          }
+      for (int i = 0; i < 144; ++i)
+        {
+          shape(i, pui, pvi);
+          if (cell_matrix)
+            for (int j = 0; j < 144; ++j)
+              {
+                shape(j, puj, pvj);
+                cell_matrix[144 * i + j] -= K1 * (-1.0 / bt) * f.mat_face_lhs_K1(pui, puj, pvi, pvj) * JxW;
+              }
+          cell_rhs[i] -= (-K1) * (-1.0 / bt) * f.vec_face_rhs_K1(pui, pvi, u0, v0) * JxW;
+        }
+    }
+}
+
 } // extern "C"

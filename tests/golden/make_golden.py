@@ -13,7 +13,10 @@ material parameters (matep/src/matep.cc) unmodified with
 * ``matep.json``: Matep coefficients on a (p, t, SCC) grid;
 * ``cell.npz``: one Q1 cell (h = 0.625, the 32^3 cube's spacing) assembled the way
   femgl/src/assemble.cc:188-280 does it, i.e. 165,888 (i,j,q) tuples each calling
-  the nine reference kernels: the 144x144 cell matrix and the cell right-hand side.
+  the nine reference kernels: the 144x144 cell matrix and the cell right-hand side;
+* ``face.npz``: the Robin (AdGR) term of each of the six faces of one anisotropic cell,
+  assembled the way femgl/src/assemble.cc:286-348 does it with the reference's face
+  kernels (bt = 3).
 
 The tests read only these files; nothing at test time needs the reference tree.
 """
@@ -89,6 +92,19 @@ def main(ref_root: str | None = None) -> None:
     R.ref_cell_assemble(p(h), p(x), p(coef9), K.ctypes.data_as(dp), r.ctypes.data_as(dp))
     np.savez_compressed(os.path.join(OUT, "cell.npz"), h=h, x=x, coef9=coef9, cell_matrix=K.reshape(144, 144),
                         cell_rhs=r)
+
+    # the Robin faces of one anisotropic cell, verbatim reference face loop (assemble.cc:286-348)
+    frng = np.random.default_rng(20240602)
+    hf = np.array([0.5, 0.625, 0.75])
+    xf = frng.standard_normal((8, 18))
+    bt = 3.0
+    Kf = np.zeros((6, 144 * 144))
+    rf = np.zeros((6, 144))
+    for face in range(6):
+        R.ref_face_assemble(p(hf), p(xf), ctypes.c_double(gl.K_REF), ctypes.c_double(bt), face,
+                            Kf[face].ctypes.data_as(dp), rf[face].ctypes.data_as(dp))
+    np.savez_compressed(os.path.join(OUT, "face.npz"), h=hf, x=xf, K1=gl.K_REF, bt=bt,
+                        face_matrix=Kf.reshape(6, 144, 144), face_rhs=rf)
     print("golden fixtures written to", OUT)
 
 

@@ -111,6 +111,29 @@ def test_cell_matrix_matches_reference_loop(oracle_gl):
     assert np.abs(r + g["cell_rhs"]).max() <= 1e-13 * np.abs(g["cell_rhs"]).max()
 
 
+def test_robin_faces_match_reference_face_loop(oracle_gl):
+    """Each Robin face of the oracle's cell equals the reference's face loop (assemble.cc:286-348)."""
+    g = np.load(os.path.join(GOLD, "face.npz"))
+    coef = oracle_gl.coef_vector(-0.4, np.full(5, 0.01), K1=float(g["K1"]), bt=float(g["bt"]))
+    K0, r0, f0 = oracle_gl.cell_local(g["h"], g["x"], coef)
+    for face in range(6):
+        K, r, f = oracle_gl.cell_local(g["h"], g["x"], coef, faces=1 << face)
+        Kref, rref = g["face_matrix"][face], g["face_rhs"][face]
+        assert np.abs(Kref).max() > 0
+        assert np.abs((K - K0) - Kref).max() <= 1e-13 * np.abs(Kref).max()
+        assert np.abs((r - r0) + rref).max() <= 1e-13 * np.abs(rref).max()
+        # the surface energy wR |A_t|^2 has the face residual as half its gradient and is
+        # homogeneous of degree 2, so x . R_face = x . dF/dx / 2 = F_face
+        assert np.isclose(f - f0, (r - r0) @ g["x"].reshape(144), rtol=1e-12)
+    # all six at once add up
+    K6, r6, _ = oracle_gl.cell_local(g["h"], g["x"], coef, faces=63)
+    assert np.abs((K6 - K0) - g["face_matrix"].sum(0)).max() <= 1e-13 * np.abs(g["face_matrix"]).max()
+    # inactive when bt >= 1e10
+    coef_off = oracle_gl.coef_vector(-0.4, np.full(5, 0.01), K1=float(g["K1"]))
+    Koff, _, _ = oracle_gl.cell_local(g["h"], g["x"], coef_off, faces=63)
+    assert np.array_equal(Koff, oracle_gl.cell_local(g["h"], g["x"], coef_off)[0])
+
+
 def test_live_reference_kernels_when_built(oracle_gl):
     """With the reference tree present (this container), also compare on fresh samples."""
     R = oracle_gl.ref()
