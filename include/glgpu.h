@@ -104,6 +104,10 @@ typedef struct
   double prec_reuse;    /* mixed multigrid: keep the previous Newton step's preconditioner (and skip
                            re-assembling the block matrix, rebuilt on demand) while the last step
                            |a delta| / |x| < prec_reuse; 0 (default) rebuilds every step */
+  double bt;            /* "AdGR diffuse length" (declare.cc:123, femgl.cc:150): bt < 1e10 adds the
+                           Robin term (K1/bt) int |A_t|^2 dS of the pair-breaking faces
+                           (assemble.cc:286-348, residual.cc:235-278), A_t = A with the face's
+                           normal column zeroed; default 1e10 (no Robin term); must be > 0 */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;
@@ -291,6 +295,11 @@ glgpu_status glgpu_bphase_guess(double p, double t, int scc, int n_nodes, double
  */
 glgpu_status glgpu_plan_info(const glgpu_mesh *mesh, int n_inst, int64_t *info);
 glgpu_status glgpu_plan_pattern(const glgpu_mesh *mesh, int n_inst, int32_t *rowptr, int32_t *cols);
+/* faces[nc] (cells of all instances in order): bit f = 2 axis + side set when face f of the
+ * cell is a Robin (AdGR) face, i.e. a boundary face with boundary id 2/3/4 in the reference
+ * (assemble.cc:286-292), recognised by the zero-Dirichlet normal column of its nodes.
+ * The term is assembled only where bt < 1e10. */
+glgpu_status glgpu_plan_robin(const glgpu_mesh *mesh, int n_inst, uint8_t *faces);
 
 /* ---------------------------------------------------------------------------
  * Learned initial guess (no counterpart in the reference, which starts Newton from a

@@ -65,6 +65,7 @@ def lib():
         L.orc_assemble.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _up, _ip, _ip, _dp, _dp, _dp, _ip, _ip,
                                    _dp, _dp, _dp]
         L.orc_distribute.argtypes = [ctypes.c_int, _up, _ip, _ip, _dp, _dp]
+        L.orc_robin_faces.argtypes = [ctypes.c_int, _ip, _up, _ip, _ip, ctypes.POINTER(ctypes.c_uint8)]
         L.orc_spmv.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_gmres.restype = ctypes.c_int
@@ -164,6 +165,13 @@ class System:
             free[(self.mask >> np.uint32(c)) & np.uint32(1) == 1, c] = False
         free[hanging, :] = False
         self.free = free.ravel()
+
+    def robin_faces(self):
+        """Per cell the bits f = 2 axis + side of its Robin (pair-breaking) faces."""
+        out = np.zeros(self.m.nc, np.uint8)
+        lib().orc_robin_faces(self.m.nc, _p(self.cells, _ip), _p(self.mask, _up), _p(self.hptr, _ip),
+                              _p(self.hpar, _ip), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        return out
 
     def assemble(self, x, want_J=True):
         x = np.ascontiguousarray(x, np.float64).reshape(-1)

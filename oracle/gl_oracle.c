@@ -558,6 +558,13 @@ static int robin_faces(const int *cell, const uint32_t *mask, const int *hptr, c
   return bits;
 }
 
+/* out[e] = robin_faces of cell e (bit f = 2 * axis + side) */
+void orc_robin_faces(int nc, const int *cells, const uint32_t *mask, const int *hptr, const int *hpar,
+                     unsigned char *out)
+{
+  for (int e = 0; e < nc; ++e) out[e] = (unsigned char)robin_faces(cells + 8 * e, mask, hptr, hpar);
+}
+
 static void cell_h(const double *xyz, const int *cell, double *h)
 {
   for (int d = 0; d < 3; ++d) h[d] = xyz[3 * cell[7] + d] - xyz[3 * cell[0] + d];

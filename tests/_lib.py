@@ -15,10 +15,11 @@ def product():
 
 
 def coef_of(params):
-    """Oracle coefficient vector {K1, K2+K3, alpha, beta1..5} of a product Params."""
+    """Oracle coefficient vector {K1, K2+K3, alpha, beta1..5, K1/bt} of a product Params."""
     import numpy as np
 
-    return np.array([params.K1, params.K2 + params.K3, params.alpha, *params.beta], dtype=np.float64)
+    wR = params.K1 / params.bt if params.bt < 1e10 else 0.0
+    return np.array([params.K1, params.K2 + params.K3, params.alpha, *params.beta, wR], dtype=np.float64)
 
 
 def oracle_mesh(m):

@@ -83,3 +83,38 @@ def test_driver_solves_like_the_binding(driver, tmp_path, precision):
     assert abs(F - Fb) <= 1e-12 * abs(Fb)
     xd = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
     assert np.array_equal(xd, x)
+
+
+@pytest.mark.gpu
+def test_driver_robin_faces_like_the_binding(driver, tmp_path):
+    """The configuration's AdGR diffuse length turns on the Robin faces of the z boundary."""
+    gl = product()
+    cfg = CONFIG.replace("  set t_reduced = 0.6\n", "  set t_reduced = 0.6\n  set AdGR diffuse length = 2.0\n")
+    out = subprocess.run([driver, _write(tmp_path, cfg), "--out", str(tmp_path / "x.bin")], capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "Robin (AdGR) term" in out.stdout
+    m = re.search(r"converged after (\d+) Newton iterations .*\|R\| = (\S+), F = (\S+),", out.stdout)
+    assert m, out.stdout
+    its, F = int(m.group(1)), float(m.group(3))
+    mesh = gl.cube_mesh(2.5, 4)
+    prm = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID, bt=2.0)
+    with gl.FemGL(mesh, prm) as f:
+        f.set_solution(gl.bphase_guess(20.0, 0.6, mesh.nn))
+        o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        x, Fb = f.solution(), f.free_energy()[0]
+    assert its == int(o["newton_its"][0])
+    assert abs(F - Fb) <= 1e-12 * abs(Fb)
+    assert np.array_equal(np.fromfile(tmp_path / "x.bin", dtype=np.float64), x)
+    # and differs from the run without the face term
+    prm0 = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID)
+    with gl.FemGL(mesh, prm0) as f:
+        f.set_solution(gl.bphase_guess(20.0, 0.6, mesh.nn))
+        f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        assert abs(f.free_energy()[0] - Fb) > 1e-6 * abs(Fb)
+
+
+def test_driver_rejects_nonpositive_bt(driver, tmp_path):
+    cfg = CONFIG.replace("  set t_reduced = 0.6\n", "  set t_reduced = 0.6\n  set AdGR diffuse length = 0\n")
+    r = subprocess.run([driver, _write(tmp_path, cfg), "--dry-run"], capture_output=True, text=True)
+    assert r.returncode == 2 and "AdGR" in r.stderr

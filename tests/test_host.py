@@ -118,3 +118,32 @@ def test_bphase_guess(gl):
     y = gl.bphase_guess(20.0, 0.6, 5, noise=0.05, seed=2).reshape(5, 18)
     z = gl.bphase_guess(20.0, 0.6, 5, noise=0.05, seed=2).reshape(5, 18)
     assert np.array_equal(y, z) and 0.0 < np.std(y - x) < 0.2
+
+
+@pytest.mark.parametrize("dxy,frac", [((0, 0), 0.0), ((0, 0), 0.25), ((1, 1), 0.3), ((1, 0), 0.0)])
+def test_robin_faces_match_oracle(gl, oracle_gl, dxy, frac):
+    """Pair-breaking (Robin) faces: the plan's classification equals the oracle's, including
+    refined faces whose hanging nodes sit on the boundary."""
+    m = gl.box_mesh([-1.0, -1.5, -1.25], [1.0, 1.5, 1.25], (4, 5, 4), refine_band=frac * 2.5, dirichlet_xy=dxy)
+    bits = gl.plan_robin([m])
+    ref = oracle_gl.System(oracle_mesh(m), np.zeros(9)).robin_faces()
+    assert np.array_equal(bits, ref)
+    # faces counted by geometry: every boundary face of a masked axis, nothing else
+    lo, hi = m.xyz.min(0), m.xyz.max(0)
+    expect = 0
+    for e in range(m.nc):
+        v = m.xyz[m.cells[e]]
+        for ax, on in ((0, dxy[0]), (1, dxy[1]), (2, 1)):
+            if on:
+                for side, plane in ((0, lo[ax]), (1, hi[ax])):
+                    on_face = [(vv >> ax) & 1 == side for vv in range(8)]
+                    expect += int(np.all(v[on_face, ax] == plane))
+    assert sum(bin(int(b)).count("1") for b in bits) == expect > 0
+    if frac > 0:
+        assert m.n_hanging > 0
+
+
+def test_robin_bt_must_be_positive(gl):
+    m = gl.cube_mesh(1.0, 2)
+    with pytest.raises(gl.GLGPUError, match="bt"):
+        gl.FemGL(m, gl.Params.from_matep(20.0, 0.6, bt=0.0))

@@ -8,7 +8,7 @@
 namespace glgpu
 {
 constexpr int kNS3 = 171;   // unique entries of a symmetric 18x18 block
-constexpr int kCoef = 8;    // {K1, K2+K3, alpha, beta1..beta5}
+constexpr int kCoef = 9;    // {K1, K2+K3, alpha, beta1..beta5, K1/bt (0: no Robin term)}
 constexpr int kSegThreads = 256;
 constexpr int kSegMax = 1024;   // scalars per reduction segment (one CTA each)
 
@@ -56,7 +56,34 @@ struct DevMesh
   // (zero for instances without uniform cells, whose rows are never regular)
   const double *reg_tmpl_d;
   const float *reg_tmpl_f;
+  // Robin (AdGR) faces: per cell the bits f = 2 axis + side of its pair-breaking faces
+  // (nullptr when no instance has an active Robin term) and the cells with any
+  const uint8_t *robin;
+  const int32_t *robin_cells;
+  int64_t n_robin;
 };
+
+#ifdef __CUDACC__
+// Robin weight between cell vertices a and b for component column `col` (= c % 3):
+// wR sum over the cell's Robin faces f (axis != col) holding both a and b of
+// int_f phi_a phi_b dS = area_f (1/9, 1/18, 1/36 for 0, 1, 2 differing tangential bits).
+// ih = {1/hx, 1/hy, 1/hz}, vol = hx hy hz, so area_f = vol ih[axis].
+template <typename T>
+__device__ __forceinline__ T robin_weight(int bits, int a, int b, int col, T wR, T vol, T i0, T i1, T i2)
+{
+  T s = T(0);
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+    {
+      const int ax = f >> 1, side = f & 1;
+      if (!((bits >> f) & 1) || ax == col || ((a >> ax) & 1) != side || ((b >> ax) & 1) != side) continue;
+      const int diff = __popc((a ^ b) & 7);
+      const T mab = diff == 0 ? T(1) / T(9) : (diff == 1 ? T(1) / T(18) : T(1) / T(36));
+      s += mab * vol * (ax == 0 ? i0 : (ax == 1 ? i1 : i2));
+    }
+  return wR * s;
+}
+#endif
 
 // ---- assembly (kernels_asm.cu) ----
 // Per-cell quadrature data: H [nc][nq][NS] (type T) and/or cell residual
@@ -68,6 +95,14 @@ cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, d
 void regular_row_stiffness(double K1, double K23, const double *h, double *out);
 // Row gather of the condensed Jacobian from H (type fp32 ? float : double) into vals.
 cudaError_t launch_rows(const DevMesh &m, bool fp32, const void *H, void *vals, cudaStream_t s);
+// Robin face terms added into the per-cell outputs of the Robin cells (after the cell
+// kernels, before the gathers): r_cell += wR M x (and e_cell += x . wR M x when e_cell)
+// from the FP64 state x, or ycell += wR M z from the FP32 direction z expanded through the
+// constraints and column masks like the matrix-free cell kernel does.
+cudaError_t launch_robin_res(const DevMesh &m, const double *x, double *r_cell, double *e_cell, const uint8_t *act,
+                             cudaStream_t s);
+cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, const uint8_t *act, cudaStream_t s);
+
 // Condensed residual R [nn*B] from r_cell.
 cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *inst_active,
                               cudaStream_t s);

@@ -215,7 +215,12 @@ int main(int argc, char **argv)
               precision == GLGPU_FP64 ? "FP64" : "mixed FP32/FP64",
               precond == GLGPU_PC_MULTIGRID ? "multigrid" : precond == GLGPU_PC_BLOCK_JACOBI ? "block-Jacobi"
                                             : precond == GLGPU_PC_CHEBYSHEV ? "Chebyshev" : "unpreconditioned");
-  if (bt < 1e10) std::printf("  note: Robin faces (AdGR diffuse length %g) are not assembled; z faces are pair-breaking\n", bt);
+  if (bt < 1e10) std::printf("  Robin (AdGR) term on the pair-breaking z faces, diffuse length %g\n", bt);
+  if (!(bt > 0.0))
+    {
+      std::fprintf(stderr, "femgl_gb300: AdGR diffuse length must be > 0\n");
+      return 2;
+    }
   if (conf.num(C + "Number of refinements") > 0)
     std::printf("  note: refinement cycles are not performed; the cycle-0 mesh is solved to convergence\n");
   if (dry) return 0;
@@ -247,6 +252,7 @@ int main(int argc, char **argv)
   prm.gmres_max_iter = static_cast<int>(conf.num(C + "maximum linear iteration number"));
   prm.ls_step = conf.num(C + "primary step length of dampped newton iteration");
   prm.damped = conf.flag(C + "Using dampped Newton iteration") ? 1 : 0;
+  prm.bt = bt;
 
   glgpu_ctx *ctx = nullptr;
   if (glgpu_create(&mesh, &prm, 1, &ctx)) return fail("create");

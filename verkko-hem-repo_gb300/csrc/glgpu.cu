@@ -304,12 +304,23 @@ glgpu_status upload_d(glgpu_ctx *c, double *dst, const std::vector<double> &a)
   return GLGPU_OK;
 }
 
+// Robin face terms into r_cell (and e_cell) at state v, after the cell kernel
+glgpu_status robin_res(glgpu_ctx *c, const double *v, double *ec, const uint8_t *act)
+{
+  if (c->dm.n_robin == 0) return GLGPU_OK;
+  return launch(c, KK_RES, 1, [&] { return launch_robin_res(c->dm, v, c->r_cell, ec, act, c->st); });
+}
+
+// kernels of one matrix-free operator application: cell, (Robin faces,) gather
+int mf_launches(const glgpu_ctx *c) { return 2 + (c->dm.n_robin > 0 ? 1 : 0); }
+
 // residual at vector v (x or xt) for instances in act: R, e_cell
 // R at v (and the cell free energies when `energy`; the line search needs only |R|)
 glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act, bool energy = false)
 {
   double *ec = energy ? c->e_cell : nullptr;
   CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, v, nullptr, c->r_cell, ec, act, c->st); }));
+  CKS(robin_res(c, v, ec, act));
   CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   return GLGPU_OK;
 }
@@ -326,7 +337,7 @@ glgpu_status bj(glgpu_ctx *c, const void *in, void *out, const uint8_t *act, con
 glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
 {
   if (c->mf)
-    return launch(c, KK_SPMV, 2, [&] {
+    return launch(c, KK_SPMV, mf_launches(c), [&] {
       return launch_mf(c->dm, static_cast<const float *>(c->H), static_cast<const float *>(in), c->ycell,
                        static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err, c->prm[0].mf_cells);
     });
@@ -842,7 +853,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
   auto smooth = [&](const void *zin, void *zout) {
     if (L->mf && zin)
-      return launch(L, KK_PREC, 2, [&] {
+      return launch(L, KK_PREC, mf_launches(L), [&] {
         return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(zin), L->ycell,
                          static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
                          static_cast<float>(om), 2, act, L->st, L->d_err, L->prm[0].mf_cells);
@@ -859,7 +870,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
     }
   // coarse-grid correction: oth = cur + P e, e = V-cycle(R (r - J cur))
   if (L->mf)
-    CKS(launch(L, KK_SPMV, 2, [&] {
+    CKS(launch(L, KK_SPMV, mf_launches(L), [&] {
       return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(cur), L->ycell,
                        static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err, L->prm[0].mf_cells);
     }));
@@ -898,6 +909,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     {
       q.precond = GLGPU_PC_BLOCK_JACOBI;
       q.gmres_restart = 1;
+      q.bt = 1e10; // coarse operators are Galerkin products of the fine one, Robin term included
     }
   for (int l = 0; l < nl; ++l)
     {
@@ -1077,6 +1089,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->mg_omega = 1.0;
   p->mf_cells = 8;
   p->prec_reuse = 0.0;
+  p->bt = 1e10;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1094,6 +1107,8 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
         return set_error(GLGPU_ERR_ARG,
                          "glgpu_create: precision, preconditioner, restart and mf_cells must match across instances");
     }
+  for (int k = 0; k < n_inst; ++k)
+    if (!(prm[k].bt > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_create: bt (AdGR diffuse length) must be > 0");
   if (prm[0].gmres_restart < 1 || prm[0].gmres_restart > 64)
     return set_error(GLGPU_ERR_ARG, "glgpu_create: gmres_restart must be in [1, 64]");
   if (prm[0].mf_cells != 4 && prm[0].mf_cells != 8 && prm[0].mf_cells != 16)
@@ -1165,6 +1180,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       coef[k * kCoef + 1] = prm[k].K2 + prm[k].K3;
       coef[k * kCoef + 2] = prm[k].alpha;
       for (int t = 0; t < 5; ++t) coef[k * kCoef + 3 + t] = prm[k].beta[t];
+      coef[k * kCoef + 8] = (prm[k].bt < 1e10) ? prm[k].K1 / prm[k].bt : 0.0; // assemble.cc:292
     }
   if ((s = dupload(c, &p_cells, P.cells)) || (s = dupload(c, &p_h, P.cell_h)) || (s = dupload(c, &p_ci, P.cell_inst)) ||
       (s = dupload(c, &p_ni, P.node_inst)) || (s = dupload(c, &p_mask, P.mask)) || (s = dupload(c, &p_hptr, P.hptr)) ||
@@ -1197,6 +1213,26 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
     if ((s = dupload(c, &p_td, tmpl)) || (s = dupload(c, &p_tf, tmpl_f))) return fail(s);
     d.reg_tmpl_d = p_td;
     d.reg_tmpl_f = p_tf;
+  }
+  {
+    // Robin faces of the instances with bt < 1e10
+    std::vector<uint8_t> on(n_inst, 0), robin;
+    for (int k = 0; k < n_inst; ++k) on[k] = (P.dim == 3 && P.B == 18 && prm[k].bt < 1e10) ? 1 : 0;
+    robin_faces(P, on, robin);
+    std::vector<int32_t> rcells;
+    for (int64_t e = 0; e < P.nc; ++e)
+      if (robin[e]) rcells.push_back(static_cast<int32_t>(e));
+    d.robin = nullptr;
+    d.robin_cells = nullptr;
+    d.n_robin = static_cast<int64_t>(rcells.size());
+    if (!rcells.empty())
+      {
+        uint8_t *p_rb = nullptr;
+        int32_t *p_rc = nullptr;
+        if ((s = dupload(c, &p_rb, robin)) || (s = dupload(c, &p_rc, rcells))) return fail(s);
+        d.robin = p_rb;
+        d.robin_cells = p_rc;
+      }
   }
   {
     std::vector<float> cf(coef.begin(), coef.end());
@@ -1390,14 +1426,18 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
         return launch_cell(c->dm, false, c->x, c->H, need_r ? c->r_cell : nullptr, need_r ? c->e_cell : nullptr, act,
                            c->st);
       }));
+      if (need_r) CKS(robin_res(c, c->x, c->e_cell, act));
     }
   else
     {
       CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
       if (need_r)
-        CKS(launch(c, KK_RES, 1, [&] {
-          return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, nullptr, act, c->st);
-        }));
+        {
+          CKS(launch(c, KK_RES, 1, [&] {
+            return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, nullptr, act, c->st);
+          }));
+          CKS(robin_res(c, c->x, nullptr, act));
+        }
     }
   // a small last Newton step keeps the previous preconditioner; the matrix-free operator
   // needs only H, so the block matrix is then rebuilt only on demand

@@ -137,4 +137,10 @@ struct Plan
 // Validates the meshes and builds the plan; returns 0 or sets an error message.
 glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &plan);
 
+// Robin (AdGR) faces of the 3D cells: bit f = 2 * axis + side of robin[e] is set when face f
+// of cell e is a pair-breaking boundary face (femgl/src/assemble.cc:286-348, boundary ids
+// 2/3/4 carrying the zero-Dirichlet normal column).  Only cells of instances with
+// active[inst] != 0 are marked.
+void robin_faces(const Plan &plan, const std::vector<uint8_t> &active, std::vector<uint8_t> &robin);
+
 } // namespace glgpu

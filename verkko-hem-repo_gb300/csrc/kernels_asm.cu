@@ -1063,6 +1063,8 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
           load_hq(H, e, tid, act, hq);
           const int inst = m.cell_inst[e];
           const T K1 = Tab<T>::coef(m, inst, 0), K23 = Tab<T>::coef(m, inst, 1);
+          const int rbits = (m.robin && c == d) ? m.robin[e] : 0;
+          const T wR = rbits ? Tab<T>::coef(m, inst, 8) : T(0);
           const auto g = Tab<T>::geo(m, e);
           const T vol = g.w;
           const T i0 = g.x, i1 = g.y, i2 = g.z;
@@ -1081,6 +1083,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__re
               const T *D = sD + (a * 8 + b) * 9;
               T gcd = 0, gdc = 0;
               if (c == d) gcd = gdc = kd * (D[0] * g0 + D[4] * g1 + D[8] * g2);
+              if (rbits) gcd += robin_weight<T>(rbits, a, b, c % 3, wR, vol, i0, i1, i2); // diagonal entries only
               if (kpair)
                 {
                   gcd += kc * D[3 * jc + jd];
@@ -1372,6 +1375,61 @@ cudaError_t launch_rows(const DevMesh &m, bool fp32, const void *H, void *vals, 
 {
   if (fp32) return launch_rows_t<float>(m, static_cast<const float *>(H), static_cast<float *>(vals), s);
   return launch_rows_t<double>(m, static_cast<const double *>(H), static_cast<double *>(vals), s);
+}
+
+// ---------------------------------------------------------------------------------
+// Robin (AdGR) faces of the pair-breaking boundary (assemble.cc:286-348, residual.cc:235-278):
+// on face f the surface energy wR int |A_t|^2 dS, wR = K1/bt, A_t = A with the orbital column
+// of the face normal zeroed.  The face mass of Q1 is exact in closed form (robin_weight), so
+// the term is sum_b W_ab(c) x_b[c] for the tangential components c of the faces holding a.
+// One CTA per Robin cell, thread = (vertex a, component c): every output element is written
+// by one thread after the cell kernel, so the sums stay deterministic.
+// ---------------------------------------------------------------------------------
+constexpr int kRobinThreads = 160; // 144 (vertex, component) threads, padded to whole warps
+
+__global__ void __launch_bounds__(kRobinThreads) k_robin_res(DevMesh m, const double *__restrict__ x,
+                                                             double *__restrict__ r_cell, double *__restrict__ e_cell,
+                                                             const uint8_t *__restrict__ act)
+{
+  __shared__ double xs[144];
+  __shared__ double red[kRobinThreads / 32];
+  const int64_t e = m.robin_cells[blockIdx.x];
+  const int inst = m.cell_inst[e];
+  if (act && !act[inst]) return; // uniform over the CTA
+  const int tid = threadIdx.x;
+  if (tid < 144) xs[tid] = x[static_cast<int64_t>(m.cells[e * 8 + tid / 18]) * 18 + tid % 18];
+  __syncthreads();
+  double en = 0.0;
+  if (tid < 144)
+    {
+      const int a = tid / 18, c = tid % 18;
+      const GeoD g = m.geo_d[e];
+      const double wR = m.coef[inst * kCoef + 8];
+      const int bits = m.robin[e];
+      double y = 0.0;
+      for (int b = 0; b < 8; ++b) y += robin_weight<double>(bits, a, b, c % 3, wR, g.w, g.x, g.y, g.z) * xs[18 * b + c];
+      r_cell[e * 144 + tid] += y;
+      en = xs[tid] * y;
+    }
+  if (!e_cell) return;
+  for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
+  if ((tid & 31) == 0) red[tid >> 5] = en;
+  __syncthreads();
+  if (tid == 0)
+    {
+      double t = 0.0;
+      for (int w = 0; w < kRobinThreads / 32; ++w) t += red[w];
+      e_cell[e] += t;
+    }
+}
+
+cudaError_t launch_robin_res(const DevMesh &m, const double *x, double *r_cell, double *e_cell, const uint8_t *act,
+                             cudaStream_t s)
+{
+  if (m.n_robin == 0) return cudaSuccess;
+  if (m.dim != 3 || m.B != 18 || !m.robin || !m.robin_cells) return cudaErrorInvalidValue;
+  k_robin_res<<<static_cast<unsigned>(m.n_robin), kRobinThreads, 0, s>>>(m, x, r_cell, e_cell, act);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *act, cudaStream_t s)

@@ -260,7 +260,10 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
           const uint32_t mk = m.mask[node];
           if (h1 > h0)
             for (int k = h0; k < h1; ++k)
-              val += static_cast<float>(m.hw[k]) * z[static_cast<int64_t>(m.hpar[k]) * 18 + c];
+              {
+                const int par = m.hpar[k]; // a parent's zero-Dirichlet components do not enter
+                if (!((m.mask[par] >> c) & 1u)) val += static_cast<float>(m.hw[k]) * z[static_cast<int64_t>(par) * 18 + c];
+              }
           else if (!((mk >> c) & 1u))
             val = zv;
         }
@@ -470,6 +473,54 @@ __global__ void __launch_bounds__(kMgWarps * 32) k_mf_gather(DevMesh m, const fl
     }
 }
 
+// Robin faces in the matrix-free operator: ycell[e] += W z_e for the Robin cells, z_e the
+// cell's vertex values expanded through the constraints and column masks exactly as
+// k_mf_cell reads them (one CTA per Robin cell, thread = (vertex, component)).
+constexpr int kRobinMfThreads = 160;
+
+__global__ void __launch_bounds__(kRobinMfThreads) k_robin_mf(DevMesh m, const float *__restrict__ z,
+                                                              float *__restrict__ ycell, const uint8_t *__restrict__ act)
+{
+  __shared__ float zs[144];
+  const int64_t e = m.robin_cells[blockIdx.x];
+  const int inst = m.cell_inst[e];
+  if (act && !act[inst]) return; // uniform over the CTA
+  const int tid = threadIdx.x;
+  if (tid < 144)
+    {
+      const int v = tid / 18, c = tid - 18 * v;
+      const int node = m.cells[e * 8 + v];
+      const int h0 = m.hptr[node], h1 = m.hptr[node + 1];
+      float val = 0.f;
+      if (h1 > h0)
+        for (int k = h0; k < h1; ++k)
+          {
+            const int par = m.hpar[k];
+            if (!((m.mask[par] >> c) & 1u)) val += static_cast<float>(m.hw[k]) * z[static_cast<int64_t>(par) * 18 + c];
+          }
+      else if (!((m.mask[node] >> c) & 1u))
+        val = z[static_cast<int64_t>(node) * 18 + c];
+      zs[tid] = val;
+    }
+  __syncthreads();
+  if (tid >= 144) return;
+  const int a = tid / 18, c = tid - 18 * a;
+  const float4 g = m.geo_f[e];
+  const float wR = m.coef_f[inst * kCoef + 8];
+  const int bits = m.robin[e];
+  float y = 0.f;
+  for (int b = 0; b < 8; ++b) y += robin_weight<float>(bits, a, b, c % 3, wR, g.w, g.x, g.y, g.z) * zs[18 * b + c];
+  ycell[e * 144 + tid] += y;
+}
+
+cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, const uint8_t *act, cudaStream_t s)
+{
+  if (m.n_robin == 0) return cudaSuccess;
+  if (m.dim != 3 || m.B != 18 || !m.robin || !m.robin_cells) return cudaErrorInvalidValue;
+  k_robin_mf<<<static_cast<unsigned>(m.n_robin), kRobinMfThreads, 0, s>>>(m, z, ycell, act);
+  return cudaGetLastError();
+}
+
 template <int NC>
 static cudaError_t launch_mf_cell(const DevMesh &m, const float *H, const float *z, float *ycell, const uint8_t *act,
                                   int *err, cudaStream_t s)
@@ -498,6 +549,7 @@ cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *y
                   : cells_per_cta == 16 ? launch_mf_cell<16>(m, H, z, ycell, act, err, s)
                                         : launch_mf_cell<8>(m, H, z, ycell, act, err, s);
   if (e != cudaSuccess) return e;
+  if ((e = launch_robin_mf(m, z, ycell, act, s)) != cudaSuccess) return e;
   const int64_t gn = (m.nn + kMgWarps - 1) / kMgWarps;
   k_mf_gather<<<static_cast<unsigned>(gn), kMgWarps * 32, 0, s>>>(m, ycell, z, b, dinv, y, omega, mode, act);
   return cudaGetLastError();

@@ -397,6 +397,46 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   return GLGPU_OK;
 }
 
+// A face perpendicular to `axis` is a pair-breaking boundary face when its four vertices lie
+// on a boundary plane whose nodes carry the zero-Dirichlet mask of that axis' orbital column
+// (setup_uniform_B-phase.cc:134-157 masks exactly the faces with ids 2/3/4).  An unconstrained
+// node lies there when its mask holds the column; a hanging node when all its parents do
+// (it sits on the edge or face they span).
+void robin_faces(const Plan &P, const std::vector<uint8_t> &active, std::vector<uint8_t> &robin)
+{
+  robin.assign(static_cast<size_t>(P.nc), 0);
+  if (P.dim != 3 || P.B != 18) return;
+  uint32_t col[3];
+  for (int ax = 0; ax < 3; ++ax)
+    {
+      col[ax] = 0;
+      for (int part = 0; part < 2; ++part)
+        for (int mu = 0; mu < 3; ++mu) col[ax] |= 1u << (9 * part + 3 * mu + ax);
+    }
+  auto on_plane = [&](int32_t n, int ax) {
+    const int32_t h0 = P.hptr[n], h1 = P.hptr[n + 1];
+    if (h1 == h0) return (P.mask[n] & col[ax]) == col[ax];
+    for (int32_t k = h0; k < h1; ++k)
+      if ((P.mask[P.hpar[k]] & col[ax]) != col[ax]) return false;
+    return true;
+  };
+  for (int64_t e = 0; e < P.nc; ++e)
+    {
+      if (!active[P.cell_inst[e]]) continue;
+      const int32_t *cv = &P.cells[8 * e];
+      uint8_t bits = 0;
+      for (int f = 0; f < 6; ++f)
+        {
+          const int ax = f / 2, side = f % 2;
+          bool ok = true;
+          for (int v = 0; v < 8 && ok; ++v)
+            if (((v >> ax) & 1) == side && !on_plane(cv[v], ax)) ok = false;
+          if (ok) bits |= static_cast<uint8_t>(1u << f);
+        }
+      robin[e] = bits;
+    }
+}
+
 } // namespace glgpu
 
 using namespace glgpu;
@@ -413,6 +453,18 @@ extern "C" glgpu_status glgpu_plan_info(const glgpu_mesh *mesh, int n_inst, int6
   info[3] = static_cast<int64_t>(P.rc_cell.size());
   info[4] = static_cast<int64_t>(P.hang_tg.size());
   info[5] = static_cast<int64_t>(P.seg_begin.size());
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_plan_robin(const glgpu_mesh *mesh, int n_inst, uint8_t *faces)
+{
+  if (!faces) return set_error(GLGPU_ERR_ARG, "glgpu_plan_robin: faces is NULL");
+  Plan P;
+  glgpu_status s = build_plan(mesh, n_inst, P);
+  if (s != GLGPU_OK) return s;
+  std::vector<uint8_t> robin;
+  robin_faces(P, std::vector<uint8_t>(static_cast<size_t>(n_inst), 1), robin);
+  std::memcpy(faces, robin.data(), robin.size());
   return GLGPU_OK;
 }
 

@@ -58,7 +58,8 @@ class _Params(ctypes.Structure):
                 ("precond", ctypes.c_int), ("cheb_degree", ctypes.c_int), ("gmres_restart", ctypes.c_int),
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
                 ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
-                ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double)]
+                ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double),
+                ("bt", ctypes.c_double)]
 
 
 _lib = None
@@ -248,6 +249,14 @@ def plan_info(meshes: Sequence[Mesh]) -> dict:
     return dict(zip(keys, info.tolist()))
 
 
+def plan_robin(meshes: Sequence[Mesh]) -> np.ndarray:
+    """Host-only Robin face bits per cell (bit 2 axis + side), all instances concatenated."""
+    ms = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+    out = np.zeros(sum(m.nc for m in meshes), np.uint8)
+    _check(lib().glgpu_plan_robin(ms, len(meshes), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+    return out
+
+
 def plan_pattern(meshes: Sequence[Mesh]):
     """Host-only block pattern (rowptr, cols) of the condensed Jacobian."""
     info = plan_info(meshes)
@@ -279,6 +288,8 @@ class Params:
     mg_omega: float = 1.0
     mf_cells: int = 8
     prec_reuse: float = 0.0
+    #: "AdGR diffuse length": bt < 1e10 adds the Robin term (K1/bt) |A_t|^2 on the pair-breaking faces
+    bt: float = 1e10
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -297,6 +308,7 @@ class Params:
         s.mg_pre, s.mg_post, s.mg_omega = int(self.mg_pre), int(self.mg_post), float(self.mg_omega)
         s.mf_cells = int(self.mf_cells)
         s.prec_reuse = float(self.prec_reuse)
+        s.bt = float(self.bt)
         return s
 
 
