@@ -268,7 +268,13 @@ glgpu_status glgpu_matep(double p, double t, int scc, double *out);
  * cells whose centre is within refine_band of a z face refined once (hanging nodes
  * constrained as DoFTools::make_hanging_node_constraints does for Q1), and the
  * zero-Dirichlet masks of the pair-breaking boundary (orbital column z of u and v
- * on z faces, femgl.h:300-301; columns x/y on x/y faces when dirichlet_xy[0/1]).
+ * on z faces, femgl.h:300-301).  dirichlet_xy[0/1] selects the x / y faces' condition:
+ *   0 natural (homogeneous Neumann), 1 pair-breaking (zero orbital column x / y),
+ *   2 periodic: every node of the upper face is constrained to its image on the lower
+ *     face (makegrid_retangle-z-AdGR_xy-periodic.cc:150-200 with
+ *     DoFTools::make_periodicity_constraints, setup_weak-coupling-PDW-configuration.cc:192-202),
+ *     chains (edges of two periodic axes, hanging nodes on a periodic face) resolved to
+ *     unconstrained parents as AffineConstraints::close does.
  * First call with NULL arrays to get the sizes, then with arrays of those sizes.
  */
 glgpu_status glgpu_mesh_box(const double *lo, const double *hi, const int *n, double refine_band,

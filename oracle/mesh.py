@@ -56,10 +56,15 @@ class Mesh:
 
 
 def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_z: bool = True, dirichlet_x: bool = False,
-             dirichlet_y: bool = False) -> Mesh:
+             dirichlet_y: bool = False, periodic_x: bool = False, periodic_y: bool = False) -> Mesh:
     """Box [lo, hi] with n = (nx, ny, nz) cells; cells whose centre lies within
     ``refine_band`` of a z face are refined once.  Zero-Dirichlet masks on the z
-    faces (and optionally x, y faces) as in the reference's pair-breaking setup."""
+    faces (and optionally x, y faces) as in the reference's pair-breaking setup.
+    periodic_x / periodic_y identify the upper x / y face with the lower one
+    (makegrid_retangle-z-AdGR_xy-periodic.cc:150-200; the constraints of
+    DoFTools::make_periodicity_constraints, closed like AffineConstraints::close)."""
+    if (dirichlet_x and periodic_x) or (dirichlet_y and periodic_y):
+        raise ValueError("an axis is either pair-breaking or periodic")
     lo = np.asarray(lo, dtype=np.float64)
     hi = np.asarray(hi, dtype=np.float64)
     nx, ny, nz = (int(v) for v in n)
@@ -143,6 +148,34 @@ def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_z: bool = True, diri
                                 q1[tb] -= 1
                                 q2[tb] += 1
                             parents[n_id] = ([nid(q1), nid(q2)], [0.5, 0.5])
+    if periodic_x or periodic_y:
+        # each node of an upper periodic face -> its image on the lower face (weight 1),
+        # replacing a hanging constraint there; then substitute constrained parents until
+        # all parents are unconstrained
+        con = {k: list(zip(p, w)) for k, (p, w) in parents.items()}
+        for axis, on in ((0, periodic_x), (1, periodic_y)):
+            if not on:
+                continue
+            for idx in np.nonzero(lat[:, axis] == L[axis] - 1)[0]:
+                q = lat[idx].copy()
+                q[axis] = 0
+                img = nid(q)
+                assert img >= 0, "periodic image missing"
+                con[int(idx)] = [(img, 1.0)]
+        changed = True
+        while changed:
+            changed = False
+            for k in list(con):
+                acc = {}
+                for p, w in con[k]:
+                    if p in con:
+                        changed = True
+                        for pp, ww in con[p]:
+                            acc[pp] = acc.get(pp, 0.0) + w * ww
+                    else:
+                        acc[p] = acc.get(p, 0.0) + w
+                con[k] = sorted(acc.items())
+        parents = {k: ([p for p, _ in t], [w for _, w in t]) for k, t in con.items()}
     hptr = np.zeros(nn + 1, dtype=np.int32)
     for n_id, (par, _) in parents.items():
         hptr[n_id + 1] = len(par)

@@ -4,7 +4,8 @@ residual.cc:235-278).  The oracle's face term is pinned to the reference's own f
 tests/golden/face.npz.
 
 Tolerances as in the bulk parity tests: FP64 Jacobian, residual and energy 1e-12 relative;
-FP32 (mixed) operator 2e-5 of the row scale; converged states (FP64) and free energies 1e-9."""
+FP32 (mixed) operator 2e-5 of the row scale; free energies of converged states 1e-9, the
+states themselves 1e-6 (soft directions of the B phase)."""
 import numpy as np
 import pytest
 
@@ -99,7 +100,11 @@ def test_robin_newton_fp64_matches_oracle(gl, oracle_gl):
     assert out["converged"] and out["residual"][0] <= 1e-10
     assert np.abs(xr).max() > 0.5  # not the normal state
     assert out["newton_its"][0] == len(hist)
-    assert np.abs(x - xr).max() <= 1e-9 * np.abs(xr).max()
+    # |R| < 1e-10 fixes the state only to |R| / (smallest Hessian eigenvalue): the B phase
+    # keeps soft directions, and with these boundaries the GPU's and the oracle's Krylov
+    # rounding leave the converged states ~1e-8 apart along them; the energy is quadratic
+    # there and agrees to 1e-9
+    assert np.abs(x - xr).max() <= 1e-6 * np.abs(xr).max()
     assert abs(F[0] - Fr) <= 1e-9 * abs(Fr)
 
 

@@ -147,3 +147,42 @@ def test_robin_bt_must_be_positive(gl):
     m = gl.cube_mesh(1.0, 2)
     with pytest.raises(gl.GLGPUError, match="bt"):
         gl.FemGL(m, gl.Params.from_matep(20.0, 0.6, bt=0.0))
+
+
+@pytest.mark.parametrize("per,frac,dxy", [((1, 1), 0.0, (0, 0)), ((1, 0), 0.25, (0, 1)), ((1, 1), 0.3, (0, 0)),
+                                          ((0, 1), 0.0, (1, 0))])
+def test_periodic_box_mesh_matches_oracle_mesher(gl, oracle_gl, per, frac, dxy):
+    """Periodic x / y faces (makegrid_retangle-z-AdGR_xy-periodic.cc): the upper face's
+    nodes are constrained to their images, chains through edges and hanging nodes resolved."""
+    from oracle import mesh as om
+
+    lo, hi, n = [-1.0, -1.5, -1.25], [1.0, 1.5, 1.25], (4, 3, 4)
+    p = gl.box_mesh(lo, hi, n, refine_band=frac * 2.5, dirichlet_xy=dxy, periodic_xy=per)
+    o = om.box_mesh(lo, hi, n, refine_band=frac * 2.5, dirichlet_x=bool(dxy[0]), dirichlet_y=bool(dxy[1]),
+                    periodic_x=bool(per[0]), periodic_y=bool(per[1]))
+    assert np.array_equal(p.cells, o.cells)
+    assert np.array_equal(p.mask, o.mask)
+    assert np.array_equal(p.hptr, o.hptr)
+    assert np.array_equal(p.hpar, o.hpar)
+    assert np.array_equal(p.hw, o.hw)
+    # every constrained node's parents are unconstrained, weights sum to one, and the
+    # upper periodic faces are all constrained to nodes off those faces
+    con = np.diff(p.hptr) > 0
+    assert not con[p.hpar].any()
+    assert np.allclose(np.add.reduceat(p.hw, p.hptr[:-1][con]), 1.0)
+    top = np.max(p.xyz, axis=0)
+    for axis in range(2):
+        if per[axis]:
+            upper = p.xyz[:, axis] == top[axis]
+            assert con[upper].all()
+            assert not (p.xyz[p.hpar, axis] == top[axis]).any()
+    # block pattern and Robin faces agree with the oracle's on the periodic mesh
+    rowptr, cols = gl.plan_pattern([p])
+    sysr = oracle_gl.System(oracle_mesh(p), np.zeros(9))
+    assert np.array_equal(rowptr, sysr.rowptr) and np.array_equal(cols, sysr.cols)
+    assert np.array_equal(gl.plan_robin([p]), sysr.robin_faces())
+
+
+def test_periodic_and_pair_breaking_exclusive(gl):
+    with pytest.raises(ValueError):
+        gl.box_mesh([0, 0, 0], [1, 1, 1], (2, 2, 2), dirichlet_xy=(1, 0), periodic_xy=(1, 0))

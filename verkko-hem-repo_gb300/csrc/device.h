@@ -206,11 +206,12 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
 // Galerkin product J_c = P^T J_f P on the coarse block pattern, one warp per coarse
 // block: block cb (row g_row[cb], column cols_c[cb]) is the sum over its term list
 // [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and
-// columns of the coarse level become identity rows / zero columns.
+// columns and the constrained nodes (hptr_c) of the coarse level become identity rows /
+// zero columns.
 cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
-                            const uint32_t *mask_c, void *vals_c, const int64_t *g_toff, const int32_t *g_blk,
-                            const void *g_w, const void *vals_f, const int32_t *node_inst_c, const uint8_t *act,
-                            cudaStream_t s);
+                            const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
+                            const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
+                            const uint8_t *act, cudaStream_t s);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

@@ -817,8 +817,8 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
       glgpu_ctx *L = c->lv[l];
       const glgpu_ctx::Transfer &t = c->tr[l];
       CKS(launch(c, KK_PREC, 1, [&] {
-        return launch_galerkin(c->mixed, L->nnzb, t.g_row, L->dm.cols, L->dm.mask, L->vals, t.g_toff, t.g_blk, t.g_w,
-                               F->vals, L->dm.node_inst, act, c->st);
+        return launch_galerkin(c->mixed, L->nnzb, t.g_row, L->dm.cols, L->dm.mask, L->dm.hptr, L->vals, t.g_toff,
+                               t.g_blk, t.g_w, F->vals, L->dm.node_inst, act, c->st);
       }));
       CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st, true); }));
       L->has_J = true;
@@ -917,7 +917,9 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       for (int k = 0; k < n_inst; ++k)
         {
           const BoxMesh &b = lv[l].meshes[k];
-          ms[k] = glgpu_mesh{3, b.nn, b.nc, b.xyz.data(), b.cells.data(), b.mask.data(), nullptr, nullptr, nullptr};
+          const bool con = !b.hpar.empty(); // periodic images
+          ms[k] = glgpu_mesh{3, b.nn, b.nc, b.xyz.data(), b.cells.data(), b.mask.data(),
+                             con ? b.hptr.data() : nullptr, con ? b.hpar.data() : nullptr, con ? b.hw.data() : nullptr};
         }
       glgpu_ctx *L = nullptr;
       glgpu_status st = glgpu_create(ms.data(), lp.data(), n_inst, &L);
@@ -939,6 +941,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
         {
           fine_grid[k].x[d].resize(g.n[d] + 1);
           fine_grid[k].dir[d] = g.dir[d];
+          fine_grid[k].per[d] = g.per[d];
         }
     }
   c->tr.resize(nl);
@@ -959,9 +962,36 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
           tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
           if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
             return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
-          for (size_t i = 0; i + 1 < a.size(); ++i) pp.push_back(pp.back() + (a[i + 1] - a[i]));
-          pi.insert(pi.end(), b.begin(), b.end());
-          pw.insert(pw.end(), w.begin(), w.end());
+          // prolongation between the free spaces: constrained fine nodes (periodic images)
+          // get no row, constrained coarse nodes are replaced by their parents
+          const int64_t f0 = FP.node_off[k];
+          for (size_t i = 0; i + 1 < a.size(); ++i)
+            {
+              const int64_t fi = f0 + static_cast<int64_t>(i);
+              std::vector<std::pair<int32_t, double>> row;
+              if (FP.hptr[fi + 1] == FP.hptr[fi])
+                for (int32_t q = a[i]; q < a[i + 1]; ++q)
+                  {
+                    const int32_t j = b[q];
+                    if (CP.hptr[j + 1] == CP.hptr[j])
+                      row.push_back({j, w[q]});
+                    else
+                      for (int32_t h = CP.hptr[j]; h < CP.hptr[j + 1]; ++h) row.push_back({CP.hpar[h], w[q] * CP.hw[h]});
+                  }
+              std::sort(row.begin(), row.end());
+              size_t nr = 0;
+              for (size_t q = 0; q < row.size(); ++q)
+                if (nr > 0 && row[nr - 1].first == row[q].first)
+                  row[nr - 1].second += row[q].second;
+                else
+                  row[nr++] = row[q];
+              for (size_t q = 0; q < nr; ++q)
+                {
+                  pi.push_back(row[q].first);
+                  pw.push_back(row[q].second);
+                }
+              pp.push_back(static_cast<int32_t>(pi.size()));
+            }
         }
       std::vector<int32_t> rp, ri;
       std::vector<double> rw;

@@ -38,12 +38,15 @@ struct BoxGeom
   double lo[3], hi[3];
   int n[3];
   int dir[3];
+  int per[3]; // upper face identified with the lower one (periodic axis)
 };
-// tensor grid of one instance on a multigrid level: node lines per axis, Dirichlet faces
+// tensor grid of one instance on a multigrid level: node lines per axis, Dirichlet faces,
+// periodic axes
 struct TensorGrid
 {
   std::vector<double> x[3];
   int dir[3];
+  int per[3] = {0, 0, 0};
 };
 // 1D interpolation of one fine node line from at most two coarse lines
 struct Lin1

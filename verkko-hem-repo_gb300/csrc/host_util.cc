@@ -1,6 +1,7 @@
 // Host-side helpers of the C ABI: material parameters, structured box meshes with
 // one level of refinement, and the B-phase initial guess.  No device work here.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -80,6 +81,9 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
 {
   const int nx = n[0], ny = n[1], nz = n[2];
   if (nx < 1 || ny < 1 || nz < 1) return -1;
+  if (dir3)
+    for (int d = 0; d < 2; ++d)
+      if (dir3[d] < 0 || dir3[d] > 2) return -1;
   double h[3];
   for (int d = 0; d < 3; ++d)
     {
@@ -212,6 +216,69 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
                 }
           }
     }
+  // periodic axes: the upper face's nodes are constrained to their images on the lower face;
+  // then every constraint is resolved to unconstrained parents (weights multiply, repeated
+  // parents add, parents sorted)
+  const bool per[2] = {dir3 && dir3[0] == 2, dir3 && dir3[1] == 2};
+  if (per[0] || per[1])
+    {
+      const int64_t Lp[2] = {Lx, Ly};
+      std::vector<std::vector<std::pair<int32_t, double>>> raw(nn);
+      for (int64_t i = 0; i < nn; ++i)
+        for (int k = 0; k < npar[i]; ++k) raw[i].push_back({par[i * 4 + k], wt[i * 4 + k]});
+      for (int axis = 0; axis < 2; ++axis)
+        if (per[axis])
+          for (int64_t i = 0; i < nn; ++i)
+            {
+              const int64_t key = ukey[i];
+              int64_t c3[3] = {key % Lx, (key / Lx) % Ly, key / (Lx * Ly)};
+              if (c3[axis] != Lp[axis] - 1) continue;
+              c3[axis] = 0;
+              const int64_t img = nid(c3[0], c3[1], c3[2]);
+              if (img < 0) return -2;
+              raw[i].assign(1, {static_cast<int32_t>(img), 1.0});
+            }
+      std::vector<std::vector<std::pair<int32_t, double>>> res(nn);
+      std::vector<char> done(nn, 0);
+      // images lie on lower faces and hanging parents on coarse vertices, so the
+      // substitution terminates; depth is bounded by two periodic steps and one hanging step
+      std::function<const std::vector<std::pair<int32_t, double>> &(int64_t, int)> resolve =
+        [&](int64_t i, int depth) -> const std::vector<std::pair<int32_t, double>> & {
+        if (!done[i])
+          {
+            std::vector<std::pair<int32_t, double>> out;
+            if (raw[i].empty())
+              out.push_back({static_cast<int32_t>(i), 1.0});
+            else if (depth < 8)
+              for (const auto &pw : raw[i])
+                for (const auto &qw : resolve(pw.first, depth + 1)) out.push_back({qw.first, pw.second * qw.second});
+            std::sort(out.begin(), out.end());
+            std::vector<std::pair<int32_t, double>> merged;
+            for (const auto &t : out)
+              if (!merged.empty() && merged.back().first == t.first)
+                merged.back().second += t.second;
+              else
+                merged.push_back(t);
+            res[i] = std::move(merged);
+            done[i] = 1;
+          }
+        return res[i];
+      };
+      for (int64_t i = 0; i < nn; ++i)
+        {
+          npar[i] = 0;
+          if (raw[i].empty()) continue;
+          const auto &r = resolve(i, 0);
+          if (r.empty() || r.size() > 4) return -2;
+          for (size_t k = 0; k < r.size(); ++k)
+            {
+              if (!raw[r[k].first].empty()) return -2;
+              par[i * 4 + k] = r[k].first;
+              wt[i * 4 + k] = r[k].second;
+            }
+          npar[i] = static_cast<int32_t>(r.size());
+        }
+    }
   m.hptr.assign(nn + 1, 0);
   for (int64_t i = 0; i < nn; ++i) m.hptr[i + 1] = m.hptr[i] + npar[i];
   m.hpar.resize(m.hptr[nn]);
@@ -224,7 +291,7 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
       }
   // zero-Dirichlet masks: orbital column `axis` of u and v on that axis' faces
   m.mask.assign(nn, 0u);
-  const bool on[3] = {dir3 && dir3[0] != 0, dir3 && dir3[1] != 0, !dir3 || dir3[2] != 0};
+  const bool on[3] = {dir3 && dir3[0] == 1, dir3 && dir3[1] == 1, !dir3 || dir3[2] != 0};
   const int64_t Ls[3] = {Lx, Ly, Lz};
   for (int64_t i = 0; i < nn; ++i)
     {

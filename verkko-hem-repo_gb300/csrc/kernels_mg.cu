@@ -92,9 +92,9 @@ __device__ __forceinline__ double &gcomp(double2 &v, int k) { return k == 0 ? v.
 template <typename T>
 __global__ void __launch_bounds__(kGalWarps * 32)
   k_galerkin(int64_t nnzb_c, const int32_t *__restrict__ g_row, const int32_t *__restrict__ cols_c,
-             const uint32_t *__restrict__ mask_c, T *__restrict__ vals_c, const int64_t *__restrict__ g_toff,
-             const int32_t *__restrict__ g_blk, const T *__restrict__ g_w, const T *__restrict__ vals_f,
-             const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
+             const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ hptr_c, T *__restrict__ vals_c,
+             const int64_t *__restrict__ g_toff, const int32_t *__restrict__ g_blk, const T *__restrict__ g_w,
+             const T *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
 {
   using V = typename GVec<T>::type;
   constexpr int NV = GVec<T>::n;
@@ -124,9 +124,12 @@ __global__ void __launch_bounds__(kGalWarps * 32)
           if (ch < NCH) gfma(acc[k], w, __ldg(bp + ch));
         }
     }
-  // zero-Dirichlet components of the coarse level: identity rows, zero columns
+  // zero-Dirichlet components and constrained (periodic image) nodes of the coarse level:
+  // identity rows, zero columns
   const int32_t J = cols_c[cb];
-  const uint32_t mI = mask_c[I], mJ = mask_c[J];
+  constexpr uint32_t kAll = (1u << 18) - 1u;
+  const uint32_t mI = (hptr_c[I + 1] > hptr_c[I]) ? kAll : mask_c[I];
+  const uint32_t mJ = (hptr_c[J + 1] > hptr_c[J]) ? kAll : mask_c[J];
   V *dst = reinterpret_cast<V *>(vals_c) + cb * NCH;
 #pragma unroll
   for (int k = 0; k < NIT; ++k)
@@ -182,20 +185,20 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
 }
 
 cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
-                            const uint32_t *mask_c, void *vals_c, const int64_t *g_toff, const int32_t *g_blk,
-                            const void *g_w, const void *vals_f, const int32_t *node_inst_c, const uint8_t *act,
-                            cudaStream_t s)
+                            const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
+                            const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
+                            const uint8_t *act, cudaStream_t s)
 {
   if (nnzb_c == 0) return cudaSuccess;
   const int64_t grid = (nnzb_c + kGalWarps - 1) / kGalWarps;
   if (grid > 0x7fffffff) return cudaErrorInvalidValue;
   if (fp32)
     k_galerkin<float><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
-      nnzb_c, g_row, cols_c, mask_c, static_cast<float *>(vals_c), g_toff, g_blk, static_cast<const float *>(g_w),
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, static_cast<const float *>(g_w),
       static_cast<const float *>(vals_f), node_inst_c, act);
   else
     k_galerkin<double><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
-      nnzb_c, g_row, cols_c, mask_c, static_cast<double *>(vals_c), g_toff, g_blk, static_cast<const double *>(g_w),
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<double *>(vals_c), g_toff, g_blk, static_cast<const double *>(g_w),
       static_cast<const double *>(vals_f), node_inst_c, act);
   return cudaGetLastError();
 }

@@ -3,7 +3,7 @@
 //
 // The reference preconditions its Krylov solve with Trilinos ML AMG
 // (femgl/src/solve.cc:141-152).  Here every instance of a context that is an axis-aligned
-// box with a tensor grid (no hanging nodes) gets a hierarchy of nested coarser tensor
+// box with a tensor grid (no hanging nodes; periodic axes allowed) gets a hierarchy of nested coarser tensor
 // grids: a coarsened axis keeps every other node line and the last one.  Prolongation P
 // is the tensor product of 1D linear interpolation along the axes, restriction is P^T,
 // and the coarse Jacobians are the Galerkin products P^T J P (formed on the GPU after each
@@ -57,12 +57,13 @@ void line_map(const std::vector<double> &xf, bool coarsen, std::vector<double> &
 }
 } // namespace
 
-// A mesh is a uniform box grid when it has no hanging nodes and its node count matches
-// (nx+1)(ny+1)(nz+1) for the cell counts implied by the cell size.
+// A mesh is a uniform box grid when its node count matches (nx+1)(ny+1)(nz+1) for the
+// cell counts implied by the cell size and its only constraints are periodic
+// identifications: on a periodic axis every node of the upper face has exactly one parent,
+// weight 1, its image with every periodic coordinate at the lower face.
 bool infer_box(const glgpu_mesh &m, BoxGeom &g)
 {
   if (m.dim != 3 || m.n_nodes <= 0 || m.n_cells <= 0) return false;
-  if (m.hang_ptr && m.hang_ptr[m.n_nodes] > 0) return false;
   for (int d = 0; d < 3; ++d)
     {
       g.lo[d] = 1e300;
@@ -96,17 +97,54 @@ bool infer_box(const glgpu_mesh &m, BoxGeom &g)
         }
       if (grid_node(g.n, ijk[0], ijk[1], ijk[2]) != i) return false;
     }
+  // periodic axes: every node of the upper face constrained
+  auto constrained = [&](int64_t i) { return m.hang_ptr && m.hang_ptr[i + 1] > m.hang_ptr[i]; };
+  for (int d = 0; d < 3; ++d) g.per[d] = 0;
+  if (m.hang_ptr && m.hang_ptr[m.n_nodes] > 0)
+    for (int d = 0; d < 2; ++d)
+      {
+        bool all = true;
+        for (int k = 0; k <= g.n[2] && all; ++k)
+          for (int j = 0; j <= g.n[1] && all; ++j)
+            for (int i = 0; i <= g.n[0] && all; ++i)
+              {
+                const int64_t c3[3] = {i, j, k};
+                if (c3[d] == g.n[d] && !constrained(grid_node(g.n, i, j, k))) all = false;
+              }
+        g.per[d] = all ? 1 : 0;
+      }
+  if (m.hang_ptr)
+    for (int64_t i = 0; i < m.n_nodes; ++i)
+      {
+        if (!constrained(i)) continue;
+        const int64_t ii = i % (g.n[0] + 1), jj = (i / (g.n[0] + 1)) % (g.n[1] + 1), kk = i / ((g.n[0] + 1) * (g.n[1] + 1));
+        int64_t c3[3] = {ii, jj, kk};
+        bool upper = false;
+        for (int d = 0; d < 2; ++d)
+          if (g.per[d] && c3[d] == g.n[d])
+            {
+              c3[d] = 0;
+              upper = true;
+            }
+        const int32_t h0 = m.hang_ptr[i];
+        if (!upper || m.hang_ptr[i + 1] - h0 != 1 || m.hang_weight[h0] != 1.0 ||
+            m.hang_parent[h0] != grid_node(g.n, c3[0], c3[1], c3[2]))
+          return false;
+      }
   // which axis' faces carry a zero-Dirichlet mask (orbital column of that axis)
   for (int d = 0; d < 3; ++d) g.dir[d] = 0;
   if (m.dirichlet_mask)
     for (int64_t i = 0; i < m.n_nodes; ++i)
       for (int d = 0; d < 3; ++d)
         if ((m.dirichlet_mask[i] & column_mask(d)) == column_mask(d)) g.dir[d] = 1;
+  for (int d = 0; d < 3; ++d)
+    if (g.dir[d] && g.per[d]) return false;
   return true;
 }
 
 // Hexahedral mesh of a tensor grid: nodes in (k, j, i) lexicographic order, cells in
-// deal.II vertex order, zero-Dirichlet masks on the faces of the axes flagged in dir.
+// deal.II vertex order, zero-Dirichlet masks on the faces of the axes flagged in dir, and
+// on periodic axes the upper face's nodes constrained to their images (weight 1).
 int mesh_tensor(const TensorGrid &g, BoxMesh &m)
 {
   int n[3];
@@ -131,6 +169,9 @@ int mesh_tensor(const TensorGrid &g, BoxMesh &m)
           m.xyz[3 * id + 1] = g.x[1][j];
           m.xyz[3 * id + 2] = g.x[2][k];
           const int c3[3] = {i, j, k};
+          bool slave = false;
+          for (int d = 0; d < 3; ++d) slave = slave || (g.per[d] && c3[d] == n[d]);
+          if (slave) continue; // constrained nodes carry no mask
           for (int d = 0; d < 3; ++d)
             if (g.dir[d] && (c3[d] == 0 || c3[d] == n[d])) m.mask[id] |= column_mask(d);
         }
@@ -144,6 +185,26 @@ int mesh_tensor(const TensorGrid &g, BoxMesh &m)
   m.hptr.assign(nn + 1, 0);
   m.hpar.clear();
   m.hw.clear();
+  for (int k = 0; k <= n[2]; ++k)
+    for (int j = 0; j <= n[1]; ++j)
+      for (int i = 0; i <= n[0]; ++i)
+        {
+          int c3[3] = {i, j, k};
+          bool slave = false;
+          for (int d = 0; d < 3; ++d)
+            if (g.per[d] && c3[d] == n[d])
+              {
+                c3[d] = 0;
+                slave = true;
+              }
+          const int64_t id = grid_node(n, i, j, k);
+          if (slave)
+            {
+              m.hpar.push_back(static_cast<int32_t>(grid_node(n, c3[0], c3[1], c3[2])));
+              m.hw.push_back(1.0);
+            }
+          m.hptr[id + 1] = static_cast<int32_t>(m.hpar.size());
+        }
   return 0;
 }
 
@@ -214,6 +275,7 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
           for (int i = 0; i <= g.n[d]; ++i)
             cur[k].x[d][i] = (i == g.n[d]) ? g.hi[d] : g.lo[d] + (g.hi[d] - g.lo[d]) * i / g.n[d];
           cur[k].dir[d] = g.dir[d];
+          cur[k].per[d] = g.per[d];
         }
     }
   for (int l = 0; l < max_levels; ++l)
@@ -242,6 +304,7 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
               const bool coarsen = f.x[d].size() > 2 && h[d] < 2.0 * hmin;
               line_map(f.x[d], coarsen, c.x[d], L.map[k][d]);
               c.dir[d] = f.dir[d];
+              c.per[d] = f.per[d];
             }
           L.grid[k] = c;
           if (mesh_tensor(c, L.meshes[k]) != 0)

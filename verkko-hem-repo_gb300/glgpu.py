@@ -190,14 +190,17 @@ class Mesh:
         return s
 
 
-def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_xy=(0, 0)) -> Mesh:
+def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_xy=(0, 0), periodic_xy=(0, 0)) -> Mesh:
     """Box [lo, hi] with n cells per axis, z faces pair-breaking, cells within
-    ``refine_band`` of a z face refined once (hanging nodes constrained)."""
+    ``refine_band`` of a z face refined once (hanging nodes constrained).  x / y faces:
+    pair-breaking where dirichlet_xy, periodic where periodic_xy, natural otherwise."""
     L = lib()
     lo = np.asarray(lo, np.float64)
     hi = np.asarray(hi, np.float64)
     nv = np.asarray(n, np.int32)
-    dxy = np.asarray(dirichlet_xy, np.int32)
+    if any(d and p for d, p in zip(dirichlet_xy, periodic_xy)):
+        raise ValueError("an axis is either pair-breaking or periodic")
+    dxy = np.asarray([2 if p else (1 if d else 0) for d, p in zip(dirichlet_xy, periodic_xy)], np.int32)
     nn = ctypes.c_int()
     nc = ctypes.c_int()
     nh = ctypes.c_int()
