@@ -293,6 +293,18 @@ glgpu_status glgpu_bphase_guess(double p, double t, int scc, int n_nodes, double
                                 double *x);
 
 /*
+ * Weak-coupling pair-density-wave initial state of
+ * setup_weak-coupling-PDW-configuration.cc:286-320 (femgl/inc/pdw_config.h:111-298) at
+ * the n_nodes points xyz[n][3]: the B phase gap_B(p,t)/sqrt(3) on the diagonal of u plus
+ * the modulation of amplitude gap_B * u ("amplitude u parameter") across a slab of
+ * thickness 2 half_D ("half z length of retangle") with in-plane wave number
+ * pi / (2 sqrt(3) half_D).  glgpu_set_solution then applies the constraints
+ * (constraints_solution.distribute in the reference).
+ */
+glgpu_status glgpu_pdw_guess(double p, double t, int scc, double u, double half_D, int n_nodes, const double *xyz,
+                             double *x);
+
+/*
  * Host-only inspection of the once-per-mesh plan (no device needed):
  * info[6] = {n_nodes, nnzb, longest block row, cell contributions, hanging targets,
  * reduction segments}; the block pattern as CSR (rowptr [n_nodes+1], cols [nnzb]),

@@ -89,6 +89,7 @@ def ref():
         L.ref_matep.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp]
         L.ref_cell_assemble.argtypes = [_dp, _dp, _dp, _dp, _dp]
         L.ref_face_assemble.argtypes = [_dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.ref_pdw_value.argtypes = [ctypes.c_double] * 7 + [_dp]
         _ref = L
     return _ref
 

@@ -1,7 +1,8 @@
 /*
- * Minimal stand-ins for the two deal.II linear-algebra classes that the
- * reference's cell kernels (femgl/src/cell_mat_vec/*.cc) use: FullMatrix<double>
- * and Vector<double>.  TEST INFRASTRUCTURE ONLY: this header lets the oracle
+ * Minimal stand-ins for the deal.II classes that the reference's cell kernels
+ * (femgl/src/cell_mat_vec/*.cc) use, FullMatrix<double> and Vector<double>, and that
+ * its PDW initial-state function (femgl/inc/pdw_config.h) uses: Point<3>, Function<3>
+ * and the Assert macro.  TEST INFRASTRUCTURE ONLY: this header lets the oracle
  * build compile the reference's own kernel sources unmodified, so that their
  * outputs can pin the CPU restatement and the CUDA path.  Nothing in the
  * product links against it.
@@ -114,6 +115,8 @@ namespace dealii
     }
     number &operator()(const size_type i) { return v_[i]; }
     const number &operator()(const size_type i) const { return v_[i]; }
+    number &operator[](const size_type i) { return v_[i]; }
+    const number &operator[](const size_type i) const { return v_[i]; }
     Vector &operator+=(const Vector &o)
     {
       for (size_type i = 0; i < v_.size(); ++i) v_[i] += o.v_[i];
@@ -130,6 +133,40 @@ namespace dealii
   private:
     std::vector<number> v_;
   };
+
+  // Point<dim>: coordinates read with operator()(i)
+  template <int dim>
+  class Point
+  {
+  public:
+    Point() : c_{} {}
+    Point(double x, double y, double z) : c_{x, y, z} {}
+    double operator()(const unsigned int i) const { return c_[i]; }
+
+  private:
+    double c_[3];
+  };
+
+  // Function<dim>: a vector-valued function of n_components components
+  template <int dim>
+  class Function
+  {
+  public:
+    explicit Function(const unsigned int n_components = 1) : n_components(n_components) {}
+    virtual ~Function() = default;
+    virtual void vector_value(const Point<dim> &, Vector<double> &) const {}
+    virtual void vector_value_list(const std::vector<Point<dim>> &, std::vector<Vector<double>> &) const {}
+    const unsigned int n_components;
+  };
+
+  struct ExcDimensionMismatch
+  {
+    ExcDimensionMismatch(std::size_t, std::size_t) {}
+  };
 } // namespace dealii
+
+#ifndef Assert
+#define Assert(cond, exc) ((void)0)
+#endif
 
 #endif

@@ -16,7 +16,9 @@ material parameters (matep/src/matep.cc) unmodified with
   the nine reference kernels: the 144x144 cell matrix and the cell right-hand side;
 * ``face.npz``: the Robin (AdGR) term of each of the six faces of one anisotropic cell,
   assembled the way femgl/src/assemble.cc:286-348 does it with the reference's face
-  kernels (bt = 3).
+  kernels (bt = 3);
+* ``pdw.npz``: the reference's weak-coupling PDW initial state (femgl/inc/pdw_config.h)
+  at 64 points of a slab, at p = 20 bar, t = 0.6.
 
 The tests read only these files; nothing at test time needs the reference tree.
 """
@@ -105,6 +107,19 @@ def main(ref_root: str | None = None) -> None:
                             Kf[face].ctypes.data_as(dp), rf[face].ctypes.data_as(dp))
     np.savez_compressed(os.path.join(OUT, "face.npz"), h=hf, x=xf, K1=gl.K_REF, bt=bt,
                         face_matrix=Kf.reshape(6, 144, 144), face_rhs=rf)
+
+    # the weak-coupling PDW initial state (femgl/inc/pdw_config.h) at random points of a slab,
+    # with the parameters setup_weak-coupling-PDW-configuration.cc:286-315 passes
+    prng = np.random.default_rng(20240603)
+    half_D, u_amp = 5.0, 0.3
+    q = 3.141592653589793 / (1.7320508075688772 * 2.0 * half_D)
+    pts = np.column_stack([prng.uniform(-12, 12, 64), prng.uniform(-12, 12, 64), prng.uniform(-half_D, half_D, 64)])
+    pts[:4, 2] = [-half_D, half_D, 0.0, -half_D]
+    vals = np.zeros((64, 18))
+    for i in range(64):
+        R.ref_pdw_value(u_amp, q, half_D, gapB, *pts[i], vals[i].ctypes.data_as(dp))
+    np.savez_compressed(os.path.join(OUT, "pdw.npz"), p=20.0, t=0.6, scc=1, u=u_amp, half_D=half_D, gap=gapB,
+                        points=pts, values=vals)
     print("golden fixtures written to", OUT)
 
 

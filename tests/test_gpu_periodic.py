@@ -215,3 +215,25 @@ def test_periodic_multigrid_tight_solve(gl, oracle_gl):
         assert np.linalg.norm(r) <= 2e-10 * np.linalg.norm(rhs)
         assert np.allclose(sysr.distribute(d), d, rtol=0, atol=1e-14)
     assert its["mg"] < its["bj"], its
+
+
+def test_pdw_start_on_periodic_slab(gl, oracle_gl):
+    """The reference's weak-coupling PDW scenario: x / y periodic slab between pair-breaking z
+    walls, Newton from the PDW initial state; FP64 follows the oracle's Newton path."""
+    half_D = 5.0
+    m = gl.box_mesh([-6.0, -6.0, -half_D], [6.0, 6.0, half_D], (6, 6, 5), periodic_xy=(1, 1))
+    prm = gl.Params.from_matep(P_BAR, T_RED)
+    x0 = gl.pdw_guess(P_BAR, T_RED, m.xyz, 0.3, half_D)
+    sysr = oracle_gl.System(oracle_mesh(m), coef_of(prm))
+    # |R| reaches the FP64 floor (~1e-10 here) right after the quadratic phase: stop at 1e-9 so
+    # that the iteration count is not decided by rounding
+    xr, hist = oracle_gl.newton(sysr, x0, tol=1e-9, max_iter=40)
+    _, Fr = sysr.residual(xr)
+    with gl.FemGL(m, prm) as f:
+        f.set_solution(x0)
+        assert np.allclose(f.solution(), sysr.distribute(x0), rtol=0, atol=1e-15)
+        out = f.run(max_newton=40, linear_tol=1e-12, converge_acc=1e-9)
+        F = f.free_energy()
+    assert out["converged"] and out["residual"][0] <= 1e-9
+    assert out["newton_its"][0] == len(hist)
+    assert abs(F[0] - Fr) <= 1e-9 * abs(Fr)

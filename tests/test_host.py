@@ -186,3 +186,27 @@ def test_periodic_box_mesh_matches_oracle_mesher(gl, oracle_gl, per, frac, dxy):
 def test_periodic_and_pair_breaking_exclusive(gl):
     with pytest.raises(ValueError):
         gl.box_mesh([0, 0, 0], [1, 1, 1], (2, 2, 2), dirichlet_xy=(1, 0), periodic_xy=(1, 0))
+
+
+def test_pdw_guess_matches_reference_function(gl, oracle_gl):
+    """The weak-coupling PDW initial state equals the reference's PDWconfig (pdw_config.h),
+    recorded in tests/golden/pdw.npz (and compared live where the reference is built)."""
+    g = np.load(os.path.join(GOLD, "pdw.npz"))
+    x = gl.pdw_guess(float(g["p"]), float(g["t"]), g["points"], float(g["u"]), float(g["half_D"]),
+                     scc=bool(g["scc"])).reshape(-1, 18)
+    ref = g["values"]
+    assert gl.matep(float(g["p"]), float(g["t"]))["gap_B"] == float(g["gap"])
+    assert np.abs(x - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.abs(ref[:, 9:]).max() == 0.0 and np.abs(ref[:, :9]).max() > 0
+    R = oracle_gl.ref()
+    if R is None:
+        return
+    rng = np.random.default_rng(5)
+    for _ in range(32):
+        half_D, u = rng.uniform(2, 20), rng.uniform(-1, 1)
+        q = 3.141592653589793 / (1.7320508075688772 * 2.0 * half_D)
+        pt = np.array([rng.uniform(-30, 30), rng.uniform(-30, 30), rng.uniform(-half_D, half_D)])
+        out = np.zeros(18)
+        R.ref_pdw_value(u, q, half_D, float(g["gap"]), *pt, out.ctypes.data_as(oracle_gl._dp))
+        mine = gl.pdw_guess(float(g["p"]), float(g["t"]), pt[None, :], u, half_D).reshape(18)
+        assert np.abs(mine - out).max() <= 1e-12 * max(1.0, np.abs(out).max())

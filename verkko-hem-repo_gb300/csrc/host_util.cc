@@ -322,6 +322,56 @@ double gaussian(uint64_t seed, uint64_t index)
   return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
 }
 
+// Weak-coupling pair-density-wave initial state (femgl/inc/pdw_config.h:111-298, set up by
+// setup_weak-coupling-PDW-configuration.cc:286-320): the B phase gap/sqrt(3) on the diagonal
+// of u plus a modulation of amplitude gap * u built from four fitted profiles across the
+// slab (argument s = (z + half_D) / D in [0, 1]) and the hexagonal harmonics of wave number
+// q = pi / (sqrt(3) D) in the plane.  The profile coefficients are the reference's fits.
+namespace
+{
+double horner(const double *c, int n, double s)
+{
+  double v = 0.0;
+  for (int k = n - 1; k >= 0; --k) v = v * s + c[k];
+  return v;
+}
+const double kPdwF1[7] = {-0.010674533968153196, -0.04928146307995591, 0.4123298769345518, -5.957210687551436,
+                          15.697110273856326,    -14.963347649994844,  4.860888318571941};
+const double kPdwF2[10] = {0.005381764646081998, -0.09659207269737603, 3.059717163195402, -35.01132629189211,
+                           193.9107091164305,    -594.3817533999686,   1058.3851407510472, -1088.4440880311813,
+                           599.3158862587954,    -136.74038236803835};
+const double kPdwF3[8] = {-0.008476309862633497, -0.15843411116780842, 1.1880072170146772, -8.79341508668322,
+                          32.93035389045762,     -56.473628486426286,  44.90526146438388,  -13.60443812339298};
+const double kPdwF4[4] = {0.703221673991666, 0.07213025175696147, -4.458423083418102, 2.9780246543754445};
+} // namespace
+
+void pdw_state(double gap, double u, double half_D, double x, double y, double z, double *a)
+{
+  const double D = 2.0 * half_D, q = 3.141592653589793 / (1.7320508075688772 * D);
+  const double s = (z + half_D) / D;
+  const double f1 = horner(kPdwF1, 7, s), f2 = horner(kPdwF2, 10, s), f3 = horner(kPdwF3, 8, s),
+               f4 = horner(kPdwF4, 4, s);
+  const double r2 = std::sqrt(2.0), r3 = std::sqrt(3.0), r6 = std::sqrt(6.0);
+  const double cx = std::cos(q * x), hx_c = std::cos(0.5 * q * x), hx_s = std::sin(0.5 * q * x);
+  const double hy_c = std::cos(0.5 * r3 * q * y), hy_s = std::sin(0.5 * r3 * q * y);
+  const double c1 = cx - hx_c * hy_c;             // cos qx - cos(qx/2) cos(sqrt3 qy/2)
+  const double c2 = cx + 2.0 * hx_c * hy_c;       // cos qx + 2 cos(qx/2) cos(sqrt3 qy/2)
+  const double s1 = hx_s * hy_s;                  // sin(qx/2) sin(sqrt3 qy/2)
+  const double s2 = hy_c * hx_s + std::sin(q * x); // cos(sqrt3 qy/2) sin(qx/2) + sin qx
+  const double s3 = hx_c * hy_s;                  // cos(qx/2) sin(sqrt3 qy/2)
+  const double b = gap / r3, g = gap * u;
+  for (int c = 0; c < 18; ++c) a[c] = 0.0;
+  a[0] = b + g * (2.0 * f1 + 2.0 * f2 * c1);
+  a[1] = g * (2.0 * f1 - 2.0 * r3 * f2 * s1);
+  a[2] = g * (2.0 * f1 + 2.0 * r2 * f3 * s2);
+  a[3] = g * (2.0 * r3 * f1 * c2 - 2.0 * r3 * f2 * s1);
+  a[4] = b + g * (-2.0 * f2 * c1 + 2.0 * r3 * f1 * c2);
+  a[5] = g * (2.0 * r3 * f1 * c2 + 2.0 * r6 * f3 * s3);
+  a[6] = g * (2.0 * r2 * f4 * s2);
+  a[7] = g * (2.0 * r6 * f4 * s3);
+  a[8] = b;
+}
+
 } // namespace glgpu
 
 using namespace glgpu;
@@ -353,6 +403,17 @@ extern "C" glgpu_status glgpu_mesh_box(const double *lo, const double *hi, const
   if (hang_ptr) std::memcpy(hang_ptr, m.hptr.data(), sizeof(int32_t) * m.hptr.size());
   if (hang_parent && !m.hpar.empty()) std::memcpy(hang_parent, m.hpar.data(), sizeof(int32_t) * m.hpar.size());
   if (hang_weight && !m.hw.empty()) std::memcpy(hang_weight, m.hw.data(), sizeof(double) * m.hw.size());
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_pdw_guess(double p, double t, int scc, double u, double half_D, int n_nodes,
+                                        const double *xyz, double *x)
+{
+  if (!x || !xyz || n_nodes < 0 || !(half_D > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_pdw_guess: bad argument");
+  double mp[13];
+  if (matep_eval(p, t, scc != 0, mp) != 0) return set_error(GLGPU_ERR_ARG, "glgpu_pdw_guess: bad (p, t)");
+  for (int64_t i = 0; i < static_cast<int64_t>(n_nodes); ++i)
+    pdw_state(mp[7], u, half_D, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], x + 18 * i);
   return GLGPU_OK;
 }
 

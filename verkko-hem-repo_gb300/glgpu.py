@@ -109,6 +109,8 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mesh_box.argtypes = [_dp, _dp, _ip, ctypes.c_double, _ip, _ip, _ip, _ip, _dp, _ip, _up, _ip, _ip, _dp]
     L.glgpu_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_uint64, _dp]
+    L.glgpu_pdw_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_int, _dp, _dp]
     L.glgpu_dot_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
     fp = ctypes.POINTER(ctypes.c_float)
     L.glgpu_surrogate_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(vp)]
@@ -125,6 +127,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_surrogate_launch_count.restype = ctypes.c_int64
     L.glgpu_plan_info.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _lp]
     L.glgpu_plan_pattern.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, _ip, _ip]
+    L.glgpu_plan_robin.argtypes = [ctypes.POINTER(_Mesh), ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]
     _lib = L
     return L
 
@@ -234,6 +237,16 @@ def square_mesh(n: int, L: float = 1.0) -> Mesh:
     cells = np.stack([n0, n0 + 1, n0 + n + 1, n0 + n + 2], axis=1).astype(np.int32)
     mask = np.where(np.isclose(xy[:, 0], 0.0), 3, 0).astype(np.uint32)
     return Mesh(2, xy, cells, mask)
+
+
+def pdw_guess(p: float, t: float, xyz: np.ndarray, u: float, half_D: float, scc: bool = True) -> np.ndarray:
+    """Weak-coupling pair-density-wave start (B phase + modulation of amplitude u across a slab
+    of thickness 2 half_D) at the node coordinates xyz [nn][3]."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    nn = xyz.shape[0]
+    x = np.zeros(18 * nn)
+    _check(lib().glgpu_pdw_guess(float(p), float(t), int(bool(scc)), float(u), float(half_D), int(nn), _p(xyz), _p(x)))
+    return x
 
 
 def bphase_guess(p: float, t: float, nn: int, noise: float = 0.0, seed: int = 0, scc: bool = True) -> np.ndarray:
