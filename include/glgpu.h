@@ -283,6 +283,26 @@ glgpu_status glgpu_mesh_box(const double *lo, const double *hi, const int *n, do
                             double *hang_weight);
 
 /*
+ * The same box with the cells chosen by flags[n[0] n[1] n[2]] (cells of the unrefined grid,
+ * x fastest, the order glgpu_mesh_box gives them) refined once, e.g. the refinement flags of
+ * glgpu_refine_flags on an unrefined box (refine.cc:155-170: execute_coarsening_and_refinement,
+ * one level; coarsening flags are ignored).  Hanging constraints, masks and periodic faces as
+ * in glgpu_mesh_box; periodic faces need the same refinement on both sides.
+ */
+glgpu_status glgpu_mesh_box_refine(const double *lo, const double *hi, const int *n, const int8_t *flags,
+                                   const int *dirichlet_xy, int *n_nodes, int *n_cells, int *n_hang_entries,
+                                   double *xyz, int32_t *cells, uint32_t *mask, int32_t *hang_ptr,
+                                   int32_t *hang_parent, double *hang_weight);
+
+/*
+ * Solution transfer onto a refined box (SolutionTransfer::interpolate, refine.cc:160-170):
+ * x[p] = the trilinear interpolant of x_box (values at the (n+1)^3 nodes of the unrefined
+ * n-grid, node-major 18-vectors) at the points xyz[p].
+ */
+glgpu_status glgpu_box_interpolate(const double *lo, const double *hi, const int *n, const double *x_box, int n_points,
+                                   const double *xyz, double *x);
+
+/*
  * B-phase initial guess of setup_uniform_B-phase.cc:238-259: u11 = u22 = u33 =
  * gap_B(p,t) * 0.577350269f, everything else 0, for n_nodes nodes.  When
  * noise_sigma > 0 adds noise_sigma * N(0,1) per dof from a counter-based
@@ -305,6 +325,25 @@ glgpu_status glgpu_pdw_guess(double p, double t, int scc, double u, double half_
                              double *x);
 
 /*
+ * Kelly error estimator on the GPU (replaces KellyErrorEstimator::estimate, refine.cc:147-152,
+ * QGauss<2>(2) faces, no Neumann boundaries, all components) at the current solution:
+ *   eta_K = sqrt( diam_K / 24 * sum over interior faces F of K of int_F |[du/dn]|^2 dS ),
+ * boundary faces contributing nothing, periodic faces interior, a coarse-fine face split
+ * into the fine faces.  eta [n_cells of all instances] (host, FP32; may be NULL to keep it
+ * on the device for glgpu_refine_flags).  3D contexts with at most one level of refinement
+ * difference across a face.
+ */
+glgpu_status glgpu_estimate_error(glgpu_ctx *ctx, float *eta);
+
+/*
+ * refine_and_coarsen_fixed_number (refine.cc:154-157) on the last estimate, per instance of
+ * n_K cells: the floor(top_fraction n_K) cells of largest eta get flag 1 (every cell with
+ * eta >= that rank's value), the floor(bottom_fraction n_K) of smallest eta flag -1, others 0.
+ * The rank values are found on the GPU by an exact radix select.  flags [n_cells] (host).
+ */
+glgpu_status glgpu_refine_flags(glgpu_ctx *ctx, double top_fraction, double bottom_fraction, int8_t *flags);
+
+/*
  * Host-only inspection of the once-per-mesh plan (no device needed):
  * info[6] = {n_nodes, nnzb, longest block row, cell contributions, hanging targets,
  * reduction segments}; the block pattern as CSR (rowptr [n_nodes+1], cols [nnzb]),
@@ -318,6 +357,11 @@ glgpu_status glgpu_plan_pattern(const glgpu_mesh *mesh, int n_inst, int32_t *row
  * (assemble.cc:286-292), recognised by the zero-Dirichlet normal column of its nodes.
  * The term is assembled only where bt < 1e10. */
 glgpu_status glgpu_plan_robin(const glgpu_mesh *mesh, int n_inst, uint8_t *faces);
+/* Interior face pairs of the error estimator: pair k joins face fa[k] (2 axis + side) of cell
+ * a[k] with face fb[k] of cell b[k]; sub[k] = 1 when a's face is a quarter of b's (coarse-fine),
+ * 0 when they coincide (periodic pairs included).  First call with NULL arrays for n_pairs. */
+glgpu_status glgpu_plan_kelly(const glgpu_mesh *mesh, int n_inst, int64_t *n_pairs, int32_t *a, int8_t *fa,
+                              int32_t *b, int8_t *fb, int8_t *sub);
 
 /* ---------------------------------------------------------------------------
  * Learned initial guess (no counterpart in the reference, which starts Newton from a

@@ -56,10 +56,11 @@ class Mesh:
 
 
 def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_z: bool = True, dirichlet_x: bool = False,
-             dirichlet_y: bool = False, periodic_x: bool = False, periodic_y: bool = False) -> Mesh:
+             dirichlet_y: bool = False, periodic_x: bool = False, periodic_y: bool = False, refine_cells=None) -> Mesh:
     """Box [lo, hi] with n = (nx, ny, nz) cells; cells whose centre lies within
     ``refine_band`` of a z face are refined once.  Zero-Dirichlet masks on the z
     faces (and optionally x, y faces) as in the reference's pair-breaking setup.
+    refine_cells (flags per cell of the n-grid, x fastest) replaces the band rule.
     periodic_x / periodic_y identify the upper x / y face with the lower one
     (makegrid_retangle-z-AdGR_xy-periodic.cc:150-200; the constraints of
     DoFTools::make_periodicity_constraints, closed like AffineConstraints::close)."""
@@ -73,12 +74,14 @@ def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_z: bool = True, diri
     kz = np.arange(nz)
     zc = lo[2] + (kz + 0.5) * h[2]
     refine_layer = (np.abs(zc - lo[2]) < refine_band) | (np.abs(hi[2] - zc) < refine_band)
+    if refine_cells is not None:  # explicit per-cell flags of the n-grid, x fastest
+        refine_cells = np.asarray(refine_cells).reshape(nz, ny, nx) > 0
     cell_list = []  # (corner lattice coord (3,), size in fine units)
     for k in range(nz):
         for j in range(ny):
             for i in range(nx):
                 base = np.array([2 * i, 2 * j, 2 * k])
-                if refine_layer[k]:
+                if (refine_cells[k, j, i] if refine_cells is not None else refine_layer[k]):
                     for dk in range(2):
                         for dj in range(2):
                             for di in range(2):

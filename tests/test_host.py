@@ -210,3 +210,96 @@ def test_pdw_guess_matches_reference_function(gl, oracle_gl):
         R.ref_pdw_value(u, q, half_D, float(g["gap"]), *pt, out.ctypes.data_as(oracle_gl._dp))
         mine = gl.pdw_guess(float(g["p"]), float(g["t"]), pt[None, :], u, half_D).reshape(18)
         assert np.abs(mine - out).max() <= 1e-12 * max(1.0, np.abs(out).max())
+
+
+@pytest.mark.parametrize("per", [(0, 0), (1, 1)])
+def test_refined_box_mesh_matches_oracle_mesher(gl, oracle_gl, per):
+    """Cells chosen by flags refined once (the host half of adaptive refinement)."""
+    from oracle import mesh as om
+
+    lo, hi, n = [-1.0, -1.5, -1.25], [1.0, 1.5, 1.25], (4, 3, 4)
+    flags = np.zeros(np.prod(n), np.int8)
+    rng = np.random.default_rng(3)
+    if per == (0, 0):
+        flags[rng.choice(flags.size, 9, replace=False)] = 1
+    else:  # periodic faces need matching refinement: refine whole z layers
+        flags.reshape(n[2], n[1], n[0])[1] = 1
+    p = gl.box_mesh_refine(lo, hi, n, flags, periodic_xy=per)
+    o = om.box_mesh(lo, hi, n, refine_cells=flags, periodic_x=bool(per[0]), periodic_y=bool(per[1]))
+    for f in ("cells", "mask", "hptr", "hpar", "hw"):
+        assert np.array_equal(getattr(p, f), getattr(o, f)), f
+    assert p.nc == np.prod(n) + 7 * int(flags.sum())
+    rowptr, cols = gl.plan_pattern([p])
+    sysr = oracle_gl.System(oracle_mesh(p), np.zeros(9))
+    assert np.array_equal(rowptr, sysr.rowptr) and np.array_equal(cols, sysr.cols)
+    if per == (1, 1):
+        return
+    # refinement that differs across periodic faces is refused
+    with pytest.raises(gl.GLGPUError, match="periodic"):
+        f2 = np.zeros(np.prod(n), np.int8)
+        f2[0] = 1
+        gl.box_mesh_refine(lo, hi, n, f2, periodic_xy=(1, 0))
+
+
+def test_box_interpolate_is_trilinear(gl):
+    lo, hi, n = [-1.0, -2.0, 0.0], [1.0, 2.0, 3.0], (2, 4, 3)
+    coarse = gl.box_mesh(lo, hi, n)
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((18, 3))
+    b = rng.standard_normal(18)
+    xc = (coarse.xyz @ A.T + b).ravel()  # a linear field is reproduced exactly
+    flags = np.ones(np.prod(n), np.int8)
+    fine = gl.box_mesh_refine(lo, hi, n, flags)
+    xf = gl.box_interpolate(lo, hi, n, xc, fine.xyz)
+    assert np.allclose(xf, (fine.xyz @ A.T + b).ravel(), rtol=0, atol=1e-12)
+    # nodes of the coarse grid keep their values exactly
+    xn = gl.box_interpolate(lo, hi, n, rng.standard_normal(xc.size), coarse.xyz)
+    xr = gl.box_interpolate(lo, hi, n, xn, coarse.xyz)
+    assert np.array_equal(xn, xr)
+
+
+def test_oracle_kelly_basic_properties():
+    """The estimator's restatement: zero for a linear field, symmetric under mirror images,
+    and fixed-number flags pick the largest estimates."""
+    from oracle import kelly as ok
+    from oracle import mesh as om
+
+    lo, hi, n = [0.0, 0.0, 0.0], [2.0, 2.0, 2.0], (4, 4, 4)
+    m = om.box_mesh(lo, hi, n, refine_band=0.6)
+    x = np.tile(m.xyz @ np.array([0.3, -0.2, 0.7]), (18, 1)).T.ravel()
+    assert np.abs(ok.kelly(m, x, lo, hi, n)).max() < 1e-12
+    # a kink across the plane x = 1: only the cells touching it see a jump
+    x = np.tile(np.abs(m.xyz[:, 0] - 1.0), (18, 1)).T.ravel()
+    eta = ok.kelly(m, x, lo, hi, n)
+    xc = m.xyz[m.cells].mean(axis=1)[:, 0]
+    touch = (m.xyz[m.cells][:, :, 0] == 1.0).any(axis=1)
+    assert np.all(eta[touch] > 0) and np.all(eta[~touch] < 1e-12)
+    assert np.allclose(np.sort(eta[xc < 1]), np.sort(eta[xc > 1]))
+    f = ok.fixed_number_flags(eta, 0.3)
+    assert f.sum() >= int(0.3 * m.nc) and eta[f == 1].min() >= eta[f == 0].max()
+
+
+@pytest.mark.parametrize("kind", ["band", "periodic", "periodic_band", "flags"])
+def test_estimator_face_pairs_match_oracle(gl, kind):
+    """The product's face pairing (node keys) equals the oracle's (point location)."""
+    from oracle import kelly as ok
+
+    lo, hi, n = [-2.0, -2.5, -1.5], [2.0, 2.5, 1.5], (4, 5, 3)
+    per = (1, 1) if kind.startswith("periodic") else (0, 0)
+    if kind == "flags":
+        flags = np.zeros(np.prod(n), np.int8)
+        flags[np.random.default_rng(8).choice(flags.size, 17, replace=False)] = 1
+        m = gl.box_mesh_refine(lo, hi, n, flags)
+    else:
+        m = gl.box_mesh(lo, hi, n, refine_band=0.9 if "band" in kind else 0.0, periodic_xy=per)
+    a, fa, b, fb, sub = gl.plan_kelly([m])
+    mine = set()
+    for k in range(a.size):
+        if sub[k]:
+            mine.add((int(a[k]), int(fa[k]), int(b[k]), 1))
+        else:
+            lo_c, hi_c = sorted((int(a[k]), int(b[k])))
+            mine.add((lo_c, int(fa[k]) if a[k] < b[k] else int(fb[k]), hi_c, 0))
+        assert fa[k] // 2 == fb[k] // 2 and fa[k] != fb[k]
+    _, ref = ok.kelly(oracle_mesh(m), np.zeros(18 * m.nn), lo, hi, n, periodic=per, return_pairs=True)
+    assert mine == ref

@@ -21,8 +21,9 @@ LIB = os.path.join(LIBDIR, "libglgpu.so")
 DRIVER = os.path.join(LIBDIR, "femgl_gb300")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["kernels_asm.cu", "kernels_la.cu", "kernels_mg.cu", "kernels_mf.cu", "glgpu.cu", "noalloc.cu", "mlp.cu"]
-CC_SOURCES = ["host_util.cc", "plan.cc", "mg.cc"]
+CU_SOURCES = ["kernels_asm.cu", "kernels_la.cu", "kernels_mg.cu", "kernels_mf.cu", "kernels_est.cu", "glgpu.cu", "noalloc.cu",
+              "mlp.cu"]
+CC_SOURCES = ["host_util.cc", "plan.cc", "mg.cc", "kelly.cc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

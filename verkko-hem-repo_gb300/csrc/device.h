@@ -103,6 +103,17 @@ cudaError_t launch_robin_res(const DevMesh &m, const double *x, double *r_cell, 
                              cudaStream_t s);
 cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, const uint8_t *act, cudaStream_t s);
 
+// ---- Kelly error estimator and refinement flags (kernels_est.cu) ----
+// I[np] face-pair integrals of |[du/dn]|^2 and eta[nc] = sqrt(diam/24 sum of the cell's I)
+cudaError_t launch_kelly(const DevMesh &m, const double *x, const int32_t *pa, const int32_t *pb, const int8_t *fa,
+                         const int8_t *ob, const int8_t *sub, int64_t np, const int32_t *cptr, const int32_t *cpair,
+                         double *I, float *eta, cudaStream_t s);
+// hist[n_inst][256]: bits [shift, shift+8) of the estimates whose higher bits equal prefix[inst]
+cudaError_t launch_radix_hist(const DevMesh &m, const float *eta, const uint32_t *prefix, int shift, uint32_t *hist,
+                              cudaStream_t s);
+cudaError_t launch_flags(const DevMesh &m, const float *eta, const uint32_t *thr_refine, const uint32_t *thr_coarsen,
+                         int8_t *flags, cudaStream_t s);
+
 // Condensed residual R [nn*B] from r_cell.
 cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *inst_active,
                               cudaStream_t s);

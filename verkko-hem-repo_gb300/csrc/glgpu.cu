@@ -68,6 +68,17 @@ struct glgpu_ctx
   Plan P;
   DevMesh dm{};
   std::vector<glgpu_params> prm;
+  // Kelly error estimator (built on first use): face pairs, per-cell lists, estimates
+  struct Kelly
+  {
+    bool ready = false, eta_valid = false;
+    int64_t np = 0;
+    int32_t *a = nullptr, *b = nullptr, *cptr = nullptr, *cpair = nullptr;
+    int8_t *fa = nullptr, *ob = nullptr, *sub = nullptr, *flags = nullptr;
+    double *I = nullptr;
+    float *eta = nullptr;
+    uint32_t *prefix = nullptr, *hist = nullptr, *thr_r = nullptr, *thr_c = nullptr;
+  } kelly;
   int B = 18, n_inst = 1, nq = 8, ns = 171;
   int64_t nn = 0, N = 0, nnzb = 0;
   bool mixed = false;
@@ -1644,6 +1655,121 @@ extern "C" glgpu_status glgpu_free_energy(glgpu_ctx *c, double *F)
   CK(cudaMemcpyAsync(c->h_norm, c->d_energy, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
   CKS(sync(c));
   std::copy(c->h_norm, c->h_norm + c->n_inst, F);
+  return GLGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Kelly error estimator and refinement flags (refine.cc:147-157)
+// ---------------------------------------------------------------------------------
+namespace
+{
+glgpu_status kelly_setup(glgpu_ctx *c)
+{
+  glgpu_ctx::Kelly &K = c->kelly;
+  if (K.ready) return GLGPU_OK;
+  KellyFaces F;
+  CKS(kelly_faces(c->P, F));
+  K.np = static_cast<int64_t>(F.a.size());
+  if (K.np > 0)
+    {
+      CKS(dupload(c, &K.a, F.a));
+      CKS(dupload(c, &K.b, F.b));
+      CKS(dupload(c, &K.fa, F.fa));
+      CKS(dupload(c, &K.ob, F.ob));
+      CKS(dupload(c, &K.sub, F.sub));
+      CKS(dupload(c, &K.cpair, F.cell_pair));
+      CKS(dalloc(c, &K.I, static_cast<size_t>(K.np)));
+    }
+  CKS(dupload(c, &K.cptr, F.cell_ptr));
+  CKS(dalloc(c, &K.eta, static_cast<size_t>(c->P.nc)));
+  CKS(dalloc(c, &K.flags, static_cast<size_t>(c->P.nc)));
+  CKS(dalloc(c, &K.prefix, static_cast<size_t>(c->n_inst)));
+  CKS(dalloc(c, &K.thr_r, static_cast<size_t>(c->n_inst)));
+  CKS(dalloc(c, &K.thr_c, static_cast<size_t>(c->n_inst)));
+  CKS(dalloc(c, &K.hist, static_cast<size_t>(c->n_inst) * 256));
+  K.ready = true;
+  return GLGPU_OK;
+}
+
+// bit patterns of the rank[k]-th largest estimate of every instance (rank >= 1), or
+// 0xffffffff where rank[k] == 0
+glgpu_status kelly_select(glgpu_ctx *c, const std::vector<int64_t> &rank, std::vector<uint32_t> &out)
+{
+  glgpu_ctx::Kelly &K = c->kelly;
+  const int n = c->n_inst;
+  std::vector<uint32_t> prefix(n, 0u), hist(static_cast<size_t>(n) * 256);
+  std::vector<int64_t> r(rank);
+  for (int shift = 24; shift >= 0; shift -= 8)
+    {
+      CK(cudaMemcpyAsync(K.prefix, prefix.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->st));
+      CKS(launch(c, KK_VEC, 1, [&] { return launch_radix_hist(c->dm, K.eta, K.prefix, shift, K.hist, c->st); }));
+      CK(cudaMemcpyAsync(hist.data(), K.hist, sizeof(uint32_t) * 256 * n, cudaMemcpyDeviceToHost, c->st));
+      CKS(sync(c));
+      for (int k = 0; k < n; ++k)
+        {
+          if (r[k] <= 0) continue;
+          int64_t above = 0;
+          for (int bin = 255; bin >= 0; --bin)
+            {
+              const int64_t h = hist[static_cast<size_t>(k) * 256 + bin];
+              if (above + h >= r[k])
+                {
+                  prefix[k] |= static_cast<uint32_t>(bin) << shift;
+                  r[k] -= above;
+                  break;
+                }
+              above += h;
+            }
+        }
+    }
+  out.assign(n, 0xffffffffu);
+  for (int k = 0; k < n; ++k)
+    if (rank[k] > 0) out[k] = prefix[k];
+  return GLGPU_OK;
+}
+} // namespace
+
+extern "C" glgpu_status glgpu_estimate_error(glgpu_ctx *c, float *eta)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_estimate_error: NULL context");
+  if (c->P.dim != 3 || c->B != 18) return set_error(GLGPU_ERR_ARG, "glgpu_estimate_error: 3D femgl contexts only");
+  CKS(kelly_setup(c));
+  glgpu_ctx::Kelly &K = c->kelly;
+  CKS(launch(c, KK_VEC, K.np > 0 ? 2 : 1, [&] {
+    return launch_kelly(c->dm, c->x, K.a, K.b, K.fa, K.ob, K.sub, K.np, K.cptr, K.cpair, K.I, K.eta, c->st);
+  }));
+  if (eta) CK(cudaMemcpyAsync(eta, K.eta, sizeof(float) * c->P.nc, cudaMemcpyDeviceToHost, c->st));
+  CKS(sync(c));
+  K.eta_valid = true;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_refine_flags(glgpu_ctx *c, double top_fraction, double bottom_fraction, int8_t *flags)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_refine_flags: NULL context");
+  if (!(top_fraction >= 0.0 && bottom_fraction >= 0.0 && top_fraction + bottom_fraction <= 1.0))
+    return set_error(GLGPU_ERR_ARG, "glgpu_refine_flags: need 0 <= fractions and top + bottom <= 1");
+  if (!c->kelly.ready || !c->kelly.eta_valid)
+    return set_error(GLGPU_ERR_STATE, "glgpu_refine_flags: call glgpu_estimate_error first");
+  const int n = c->n_inst;
+  std::vector<int64_t> rr(n), rc(n);
+  for (int k = 0; k < n; ++k)
+    {
+      const int64_t nk = c->P.cell_off[k + 1] - c->P.cell_off[k];
+      const int64_t kr = static_cast<int64_t>(top_fraction * static_cast<double>(nk));
+      const int64_t kc = static_cast<int64_t>(bottom_fraction * static_cast<double>(nk));
+      rr[k] = kr;
+      rc[k] = kc > 0 ? nk - kc + 1 : 0; // the kc-th smallest is the (nk - kc + 1)-th largest
+    }
+  std::vector<uint32_t> tr, tc;
+  CKS(kelly_select(c, rr, tr));
+  CKS(kelly_select(c, rc, tc));
+  glgpu_ctx::Kelly &K = c->kelly;
+  CK(cudaMemcpyAsync(K.thr_r, tr.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(K.thr_c, tc.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->st));
+  CKS(launch(c, KK_VEC, 1, [&] { return launch_flags(c->dm, K.eta, K.thr_r, K.thr_c, K.flags, c->st); }));
+  if (flags) CK(cudaMemcpyAsync(flags, K.flags, sizeof(int8_t) * c->P.nc, cudaMemcpyDeviceToHost, c->st));
+  CKS(sync(c));
   return GLGPU_OK;
 }
 

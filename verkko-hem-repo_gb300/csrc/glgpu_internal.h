@@ -28,7 +28,10 @@ struct BoxMesh
 };
 int matep_eval(double p, double t, bool scc, double *out);
 // dir3: zero-Dirichlet (orbital column of that axis) on the x, y, z faces
-int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m);
+// refine: per cell of the n-grid (x fastest), > 0 refines it once; nullptr refines the cells
+// within `band` of a z face
+int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m,
+             const int8_t *refine = nullptr);
 
 // ---------------------------------------------------------------------------------
 // multigrid hierarchy (mg.cc)
@@ -109,6 +112,7 @@ struct Plan
   std::vector<int64_t> node_off, cell_off;   // per instance, size n_inst+1
   std::vector<int32_t> cells;                 // [nc][nv] global node ids
   std::vector<double> cell_h;                 // [nc][3] box edge lengths (z = 1 for 2D)
+  std::vector<double> cell_x0;                // [nc][3] coordinates of local vertex 0
   std::vector<int32_t> cell_inst;             // [nc]
   std::vector<int32_t> node_inst;             // [nn]
   std::vector<uint32_t> mask;                 // [nn]
@@ -145,5 +149,20 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &plan);
 // 2/3/4 carrying the zero-Dirichlet normal column).  Only cells of instances with
 // active[inst] != 0 are marked.
 void robin_faces(const Plan &plan, const std::vector<uint8_t> &active, std::vector<uint8_t> &robin);
+
+// Interior face pairs of the 3D cells for the Kelly error estimator (kelly.cc).  Pair k joins
+// face fa[k] (= 2 axis + side) of cell a[k] with face fb[k] of cell b[k]; the integration
+// domain is cell a's face, which lies inside cell b's face: ob[k] = bit 0 / 1 set when it is
+// the upper half of b's face along the first / second tangential axis, sub[k] = 1 when b's
+// face is twice as large (coarse-fine interface), 0 when the faces coincide.  Faces
+// identified by periodic constraints are interior pairs.  cell_ptr / cell_pair list the
+// pairs each cell takes part in.
+struct KellyFaces
+{
+  std::vector<int32_t> a, b;
+  std::vector<int8_t> fa, fb, ob, sub;
+  std::vector<int32_t> cell_ptr, cell_pair;
+};
+glgpu_status kelly_faces(const Plan &plan, KellyFaces &out);
 
 } // namespace glgpu

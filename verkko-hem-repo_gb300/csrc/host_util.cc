@@ -77,7 +77,8 @@ int matep_eval(double p, double t, bool scc, double *out)
 // Box mesh.  Lattice coordinates are in units of half a coarse cell; nodes are
 // numbered by lattice (z, y, x), cells by the lattice of their first vertex.
 // ---------------------------------------------------------------------------------
-int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m)
+int mesh_box(const double *lo, const double *hi, const int *n, double band, const int *dir3, BoxMesh &m,
+             const int8_t *refine)
 {
   const int nx = n[0], ny = n[1], nz = n[2];
   if (nx < 1 || ny < 1 || nz < 1) return -1;
@@ -108,7 +109,7 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i)
         {
-          if (fine_layer[k])
+          if (refine ? refine[(static_cast<int64_t>(k) * ny + j) * nx + i] > 0 : fine_layer[k] != 0)
             for (int dk = 0; dk < 2; ++dk)
               for (int dj = 0; dj < 2; ++dj)
                 for (int di = 0; di < 2; ++di)
@@ -232,6 +233,13 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
             {
               const int64_t key = ukey[i];
               int64_t c3[3] = {key % Lx, (key / Lx) % Ly, key / (Lx * Ly)};
+              if (c3[axis] == 0)
+                {
+                  // the two faces must carry the same nodes
+                  c3[axis] = Lp[axis] - 1;
+                  if (nid(c3[0], c3[1], c3[2]) < 0) return -2;
+                  continue;
+                }
               if (c3[axis] != Lp[axis] - 1) continue;
               c3[axis] = 0;
               const int64_t img = nid(c3[0], c3[1], c3[2]);
@@ -414,6 +422,70 @@ extern "C" glgpu_status glgpu_pdw_guess(double p, double t, int scc, double u, d
   if (matep_eval(p, t, scc != 0, mp) != 0) return set_error(GLGPU_ERR_ARG, "glgpu_pdw_guess: bad (p, t)");
   for (int64_t i = 0; i < static_cast<int64_t>(n_nodes); ++i)
     pdw_state(mp[7], u, half_D, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], x + 18 * i);
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_mesh_box_refine(const double *lo, const double *hi, const int *n, const int8_t *flags,
+                                              const int *dirichlet_xy, int *n_nodes, int *n_cells,
+                                              int *n_hang_entries, double *xyz, int32_t *cells, uint32_t *mask,
+                                              int32_t *hang_ptr, int32_t *hang_parent, double *hang_weight)
+{
+  if (!lo || !hi || !n || !flags) return set_error(GLGPU_ERR_ARG, "glgpu_mesh_box_refine: NULL argument");
+  BoxMesh m;
+  const int dir3[3] = {dirichlet_xy ? dirichlet_xy[0] : 0, dirichlet_xy ? dirichlet_xy[1] : 0, 1};
+  const int rc = mesh_box(lo, hi, n, 0.0, dir3, m, flags);
+  if (rc == -2)
+    return set_error(GLGPU_ERR_ARG, "glgpu_mesh_box_refine: refinement differs across a periodic face pair");
+  if (rc != 0) return set_error(GLGPU_ERR_ARG, "glgpu_mesh_box_refine: invalid box or mesh too large");
+  if (n_nodes) *n_nodes = m.nn;
+  if (n_cells) *n_cells = m.nc;
+  if (n_hang_entries) *n_hang_entries = static_cast<int>(m.hpar.size());
+  if (xyz) std::memcpy(xyz, m.xyz.data(), sizeof(double) * m.xyz.size());
+  if (cells) std::memcpy(cells, m.cells.data(), sizeof(int32_t) * m.cells.size());
+  if (mask) std::memcpy(mask, m.mask.data(), sizeof(uint32_t) * m.mask.size());
+  if (hang_ptr) std::memcpy(hang_ptr, m.hptr.data(), sizeof(int32_t) * m.hptr.size());
+  if (hang_parent && !m.hpar.empty()) std::memcpy(hang_parent, m.hpar.data(), sizeof(int32_t) * m.hpar.size());
+  if (hang_weight && !m.hw.empty()) std::memcpy(hang_weight, m.hw.data(), sizeof(double) * m.hw.size());
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_box_interpolate(const double *lo, const double *hi, const int *n, const double *x_box,
+                                              int n_points, const double *xyz, double *x)
+{
+  if (!lo || !hi || !n || !x_box || !xyz || !x || n_points < 0)
+    return set_error(GLGPU_ERR_ARG, "glgpu_box_interpolate: bad argument");
+  for (int d = 0; d < 3; ++d)
+    if (n[d] < 1 || !(hi[d] > lo[d])) return set_error(GLGPU_ERR_ARG, "glgpu_box_interpolate: invalid box");
+  const int64_t sx = 1, sy = n[0] + 1, sz = static_cast<int64_t>(n[0] + 1) * (n[1] + 1);
+  for (int64_t p = 0; p < n_points; ++p)
+    {
+      int64_t i0[3];
+      double t[3];
+      for (int d = 0; d < 3; ++d)
+        {
+          const double u = (xyz[3 * p + d] - lo[d]) / (hi[d] - lo[d]) * n[d];
+          int64_t c = static_cast<int64_t>(std::floor(u));
+          c = std::min<int64_t>(std::max<int64_t>(c, 0), n[d] - 1);
+          i0[d] = c;
+          t[d] = std::min(1.0, std::max(0.0, u - static_cast<double>(c)));
+        }
+      double *out = x + 18 * p;
+      for (int c = 0; c < 18; ++c) out[c] = 0.0;
+      for (int v = 0; v < 8; ++v)
+        {
+          double w = 1.0;
+          int64_t node = 0;
+          const int64_t st[3] = {sx, sy, sz};
+          for (int d = 0; d < 3; ++d)
+            {
+              const int b = (v >> d) & 1;
+              w *= b ? t[d] : 1.0 - t[d];
+              node += (i0[d] + b) * st[d];
+            }
+          if (w == 0.0) continue;
+          for (int c = 0; c < 18; ++c) out[c] += w * x_box[18 * node + c];
+        }
+    }
   return GLGPU_OK;
 }
 

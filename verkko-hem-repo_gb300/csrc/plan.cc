@@ -100,6 +100,7 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   const int64_t nn = P.nn, nc = P.nc;
   P.cells.resize(nc * nv);
   P.cell_h.resize(nc * 3);
+  P.cell_x0.resize(nc * 3);
   P.cell_inst.resize(nc);
   P.node_inst.resize(nn);
   P.mask.assign(nn, 0u);
@@ -113,7 +114,10 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
           const int32_t *c = m.cells + e * nv;
           for (int v = 0; v < nv; ++v) P.cells[(co + e) * nv + v] = static_cast<int32_t>(no + c[v]);
           for (int d = 0; d < 3; ++d)
-            P.cell_h[(co + e) * 3 + d] = (d < m.dim) ? m.xyz[c[nv - 1] * m.dim + d] - m.xyz[c[0] * m.dim + d] : 1.0;
+            {
+              P.cell_h[(co + e) * 3 + d] = (d < m.dim) ? m.xyz[c[nv - 1] * m.dim + d] - m.xyz[c[0] * m.dim + d] : 1.0;
+              P.cell_x0[(co + e) * 3 + d] = (d < m.dim) ? m.xyz[c[0] * m.dim + d] : 0.0;
+            }
           P.cell_inst[co + e] = k;
         }
       for (int64_t i = 0; i < m.n_nodes; ++i)

@@ -109,6 +109,11 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mesh_box.argtypes = [_dp, _dp, _ip, ctypes.c_double, _ip, _ip, _ip, _ip, _dp, _ip, _up, _ip, _ip, _dp]
     L.glgpu_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_uint64, _dp]
+    L.glgpu_mesh_box_refine.argtypes = [_dp, _dp, _ip, ctypes.POINTER(ctypes.c_int8), _ip, _ip, _ip, _ip, _dp, _ip,
+                                        _up, _ip, _ip, _dp]
+    L.glgpu_box_interpolate.argtypes = [_dp, _dp, _ip, _dp, ctypes.c_int, _dp, _dp]
+    L.glgpu_estimate_error.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.glgpu_refine_flags.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int8)]
     L.glgpu_pdw_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int, _dp, _dp]
     L.glgpu_dot_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
@@ -221,6 +226,47 @@ def box_mesh(lo, hi, n, refine_band: float = 0.0, dirichlet_xy=(0, 0), periodic_
     return Mesh(3, xyz, cells, mask, hptr, hpar[:nh.value], hw[:nh.value])
 
 
+def box_mesh_refine(lo, hi, n, flags, dirichlet_xy=(0, 0), periodic_xy=(0, 0)) -> Mesh:
+    """The box [lo, hi] with n cells per axis and the cells with flags > 0 (cells of the
+    unrefined grid, x fastest) refined once (hanging nodes constrained)."""
+    L = lib()
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    nv = np.asarray(n, np.int32)
+    f = np.ascontiguousarray(flags, np.int8)
+    if f.size != int(np.prod(nv)):
+        raise ValueError("one flag per cell of the unrefined grid")
+    if any(d and p for d, p in zip(dirichlet_xy, periodic_xy)):
+        raise ValueError("an axis is either pair-breaking or periodic")
+    dxy = np.asarray([2 if p else (1 if d else 0) for d, p in zip(dirichlet_xy, periodic_xy)], np.int32)
+    fp = f.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))
+    nn, nc, nh = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(L.glgpu_mesh_box_refine(_p(lo), _p(hi), _p(nv, _ip), fp, _p(dxy, _ip), ctypes.byref(nn), ctypes.byref(nc),
+                                   ctypes.byref(nh), None, None, None, None, None, None))
+    xyz = np.zeros((nn.value, 3))
+    cells = np.zeros((nc.value, 8), np.int32)
+    mask = np.zeros(nn.value, np.uint32)
+    hptr = np.zeros(nn.value + 1, np.int32)
+    hpar = np.zeros(max(nh.value, 1), np.int32)
+    hw = np.zeros(max(nh.value, 1))
+    _check(L.glgpu_mesh_box_refine(_p(lo), _p(hi), _p(nv, _ip), fp, _p(dxy, _ip), ctypes.byref(nn), ctypes.byref(nc),
+                                   ctypes.byref(nh), _p(xyz), _p(cells, _ip), _p(mask, _up), _p(hptr, _ip),
+                                   _p(hpar, _ip), _p(hw)))
+    return Mesh(3, xyz, cells, mask, hptr, hpar[:nh.value], hw[:nh.value])
+
+
+def box_interpolate(lo, hi, n, x_box: np.ndarray, xyz: np.ndarray) -> np.ndarray:
+    """Trilinear transfer of node values on the unrefined n-grid of [lo, hi] to points xyz."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    nv = np.asarray(n, np.int32)
+    xb = np.ascontiguousarray(x_box, np.float64)
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    out = np.zeros(18 * xyz.shape[0])
+    _check(lib().glgpu_box_interpolate(_p(lo), _p(hi), _p(nv, _ip), _p(xb), int(xyz.shape[0]), _p(xyz), _p(out)))
+    return out
+
+
 def cube_mesh(half: float, n: int, refine_frac: float = 0.0) -> Mesh:
     """The reference's cube [-half, half]^3 (make_grid with "cube half side length")."""
     return box_mesh([-half] * 3, [half] * 3, (n, n, n), refine_band=refine_frac * 2.0 * half)
@@ -271,6 +317,21 @@ def plan_robin(meshes: Sequence[Mesh]) -> np.ndarray:
     out = np.zeros(sum(m.nc for m in meshes), np.uint8)
     _check(lib().glgpu_plan_robin(ms, len(meshes), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
     return out
+
+
+def plan_kelly(meshes: Sequence[Mesh]):
+    """Host-only face pairs of the error estimator: arrays (a, fa, b, fb, sub)."""
+    ms = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+    L = lib()
+    i8 = ctypes.POINTER(ctypes.c_int8)
+    npairs = ctypes.c_int64()
+    _check(L.glgpu_plan_kelly(ms, len(meshes), ctypes.byref(npairs), None, None, None, None, None))
+    n = npairs.value
+    a, b = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    fa, fb, sub = np.zeros(n, np.int8), np.zeros(n, np.int8), np.zeros(n, np.int8)
+    _check(L.glgpu_plan_kelly(ms, len(meshes), ctypes.byref(npairs), _p(a, _ip), fa.ctypes.data_as(i8), _p(b, _ip),
+                              fb.ctypes.data_as(i8), sub.ctypes.data_as(i8)))
+    return a, fa, b, fb, sub
 
 
 def plan_pattern(meshes: Sequence[Mesh]):
@@ -356,6 +417,7 @@ class FemGL:
         self.n_dofs = self.n_nodes * self.block
         offs = np.cumsum([0] + [m.nn for m in meshes])
         self.node_offsets = offs
+        self.n_cells = int(sum(m.nc for m in meshes))
 
     # -- lifetime --
     def close(self) -> None:
@@ -491,6 +553,19 @@ class FemGL:
         nn, nb, pn = np.zeros(1, np.int64), np.zeros(1, np.int64), np.zeros(1, np.int64)
         _check(lib().glgpu_mg_level_info(self._ctx, int(level), _p(nn, _lp), _p(nb, _lp), _p(pn, _lp)))
         return int(nn[0]), int(nb[0]), int(pn[0])
+
+    def estimate_error(self) -> np.ndarray:
+        """Kelly error estimate per cell at the current solution (FP32, all instances)."""
+        eta = np.zeros(self.n_cells, np.float32)
+        _check(lib().glgpu_estimate_error(self._ctx, eta.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return eta
+
+    def refine_flags(self, top_fraction: float, bottom_fraction: float = 0.0) -> np.ndarray:
+        """Fixed-number refinement (1) / coarsening (-1) flags from the last estimate."""
+        flags = np.zeros(self.n_cells, np.int8)
+        _check(lib().glgpu_refine_flags(self._ctx, float(top_fraction), float(bottom_fraction),
+                                        flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return flags
 
     @property
     def mg_fallbacks(self) -> int:
