@@ -118,3 +118,69 @@ def test_driver_rejects_nonpositive_bt(driver, tmp_path):
     cfg = CONFIG.replace("  set t_reduced = 0.6\n", "  set t_reduced = 0.6\n  set AdGR diffuse length = 0\n")
     r = subprocess.run([driver, _write(tmp_path, cfg), "--dry-run"], capture_output=True, text=True)
     assert r.returncode == 2 and "AdGR" in r.stderr
+
+
+CYCLES = """subsection physical parameters
+  set pressure in bar = 20.0
+  set t_reduced = 0.6
+end
+subsection control parameters
+  set cube half side length = 5.0
+  set Number of initial global refinments = 2
+  set Number of refinements = 2
+  set Number of interations = 40
+  set Cycle 0 refinement threshold = 1e6
+  set Cycle 0 linear solver tol = 1e-3
+  set Cycle 1 refinement threshold = 1e6
+  set Cycle 1 do global refinement = true
+  set Cycle 1 linear solver tol = 1e-3
+  set Cycle 2 do global refinement = false
+  set Cycle 2 linear solver tol = 1e-4
+  set adaptive refinment ratio = 0.3
+  set converge accuracy = 1e-10
+end
+"""
+
+
+@pytest.mark.gpu
+def test_driver_refinement_cycles_like_the_binding(driver, tmp_path):
+    """run.cc's cycle loop: cycle 0 and 1 stall at once (threshold 1e6) and refine, globally
+    then adaptively (GPU Kelly estimate, 30 % of the cells refined once), with the solution
+    transferred each time; the same steps through the binding give the same answer."""
+    gl = product()
+    out = subprocess.run([driver, _write(tmp_path, CYCLES), "--out", str(tmp_path / "x.bin")], capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "refinement cycle 1 (global): 512 cells" in out.stdout
+    assert "refinement cycle 2 (adaptive)" in out.stdout
+    m_its = re.search(r"converged after (\d+) Newton iterations .*\|R\| = (\S+), F = (\S+),", out.stdout)
+    assert m_its, out.stdout
+    F_drv = float(m_its.group(3))
+
+    lo, hi = [-5.0] * 3, [5.0] * 3
+    prm = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID)
+    m0 = gl.cube_mesh(5.0, 4)
+    with gl.FemGL(m0, prm) as f:
+        f.set_solution(gl.bphase_guess(20.0, 0.6, m0.nn))
+        f.assemble_system()
+        f.solve(1e-3, allow_unconverged=True)
+        f.newton_iteration()
+        x0 = f.solution()
+    m1 = gl.cube_mesh(5.0, 8)
+    with gl.FemGL(m1, prm) as f:
+        f.set_solution(gl.box_interpolate(lo, hi, (4, 4, 4), x0, m1.xyz))
+        f.assemble_system()
+        f.solve(1e-3, allow_unconverged=True)
+        f.newton_iteration()
+        x1 = f.solution()
+        f.estimate_error()
+        flags = f.refine_flags(0.3)
+    m2 = gl.box_mesh_refine(lo, hi, (8, 8, 8), flags)
+    assert f"refinement cycle 2 (adaptive): {m2.nc} cells" in out.stdout
+    with gl.FemGL(m2, prm) as f:
+        f.set_solution(gl.box_interpolate(lo, hi, (8, 8, 8), x1, m2.xyz))
+        o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        x, F = f.solution(), f.free_energy()[0]
+    assert o["converged"]
+    assert abs(F_drv - F) <= 1e-12 * abs(F)
+    assert np.array_equal(np.fromfile(tmp_path / "x.bin", dtype=np.float64), x)

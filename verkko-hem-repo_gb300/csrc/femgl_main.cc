@@ -9,8 +9,13 @@
 // at (p, t), starts from the uniform B phase (setup_uniform_B-phase.cc:238-263, plus
 // optional seeded Gaussian noise), and runs the Newton loop through the C ABI of
 // include/glgpu.h: assemble_system, solve(tol of the cycle), newton_iteration, stop at
-// |R| <= "converge accuracy".  Mesh refinement cycles stay with the host mesher and are
-// not performed here: every iteration uses the cycle-0 mesh and solver tolerance.
+// |R| <= "converge accuracy".  Refinement cycles follow run.cc:156-256: a cycle ends when
+// its residual stalls (change below "Cycle c refinement threshold") or converges; the next
+// cycle refines globally ("Cycle c do global refinement") or adaptively (GPU Kelly
+// estimate, the "adaptive refinment ratio" of cells with the largest estimates refined
+// once, refine.cc:131-176) and transfers the solution.  The host mesher supports one
+// adaptive level on top of any number of global ones; a further adaptive cycle ends the
+// cycle loop with a note.
 //
 // usage: femgl_gb300 [configuration.prm] [--precision mixed|fp64]
 //                    [--precond mg|bj|cheb|none] [--noise sigma] [--seed s]
@@ -52,6 +57,19 @@ struct Config
       {std::string(ctrl) + "Number of interations", "40"},
       {std::string(ctrl) + "Cycle 0 refinement threshold", "1.0e0"},
       {std::string(ctrl) + "Cycle 0 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "Cycle 1 refinement threshold", "1.0e0"},
+      {std::string(ctrl) + "Cycle 1 do global refinement", "false"},
+      {std::string(ctrl) + "Cycle 1 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "Cycle 2 refinement threshold", "1.0e0"},
+      {std::string(ctrl) + "Cycle 2 do global refinement", "false"},
+      {std::string(ctrl) + "Cycle 2 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "Cycle 3 refinement threshold", "1.0e0"},
+      {std::string(ctrl) + "Cycle 3 do global refinement", "false"},
+      {std::string(ctrl) + "Cycle 3 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "Cycle 4 do global refinement", "false"},
+      {std::string(ctrl) + "Cycle 4 linear solver tol", "1.0e-1"},
+      {std::string(ctrl) + "adaptive refinment ratio", "0.3"},
+      {std::string(ctrl) + "adaptive coarsen ratio", "0.0"},
       {std::string(ctrl) + "converge accuracy", "5.0e-6"},
       {std::string(ctrl) + "Number of initial global refinments", "4"},
       {std::string(ctrl) + "maximum linear iteration number", "10000"},
@@ -208,7 +226,9 @@ int main(int argc, char **argv)
   const int n_iter = static_cast<int>(conf.num(C + "Number of interations"));
   const double tol0 = conf.num(C + "Cycle 0 linear solver tol");
   const double acc = conf.num(C + "converge accuracy");
-  const int n = 1 << nref;
+  const int n_cycles = static_cast<int>(conf.num(C + "Number of refinements"));
+  const double ratio = conf.num(C + "adaptive refinment ratio"), coarsen = conf.num(C + "adaptive coarsen ratio");
+  int n = 1 << nref;
   std::printf("femgl_gb300: %s  p = %g bar, t = %g, SCC %s, cube half side %g, %d^3 cells\n", glgpu_version(), p, t,
               scc ? "on" : "off", half, n);
   std::printf("  Newton: <= %d iterations, linear tol %g, converge accuracy %g, %s, %s\n", n_iter + 1, tol0, acc,
@@ -221,24 +241,13 @@ int main(int argc, char **argv)
       std::fprintf(stderr, "femgl_gb300: AdGR diffuse length must be > 0\n");
       return 2;
     }
-  if (conf.num(C + "Number of refinements") > 0)
-    std::printf("  note: refinement cycles are not performed; the cycle-0 mesh is solved to convergence\n");
+  if (n_cycles > 4)
+    {
+      std::fprintf(stderr, "femgl_gb300: at most 4 refinement cycles (run.cc declares cycles 0-4)\n");
+      return 2;
+    }
+  if (n_cycles > 0) std::printf("  refinement cycles: %d (adaptive ratio %g)\n", n_cycles, ratio);
   if (dry) return 0;
-
-  // mesh: cube with pair-breaking z faces (zero orbital-z column)
-  const double lo[3] = {-half, -half, -half}, hi[3] = {half, half, half};
-  const int cells[3] = {n, n, n}, dxy[2] = {0, 0};
-  int nn = 0, nc = 0, nh = 0;
-  if (glgpu_mesh_box(lo, hi, cells, 0.0, dxy, &nn, &nc, &nh, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr))
-    return fail("mesh");
-  std::vector<double> xyz(3 * static_cast<size_t>(nn));
-  std::vector<int32_t> cell(8 * static_cast<size_t>(nc)), hptr(static_cast<size_t>(nn) + 1), hpar(nh > 0 ? nh : 1);
-  std::vector<uint32_t> mask(nn);
-  std::vector<double> hw(nh > 0 ? nh : 1);
-  if (glgpu_mesh_box(lo, hi, cells, 0.0, dxy, &nn, &nc, &nh, xyz.data(), cell.data(), mask.data(), hptr.data(),
-                     hpar.data(), hw.data()))
-    return fail("mesh");
-  glgpu_mesh mesh{3, nn, nc, xyz.data(), cell.data(), mask.data(), hptr.data(), hpar.data(), hw.data()};
 
   // material parameters at (p, t)
   double mp[13];
@@ -254,41 +263,141 @@ int main(int argc, char **argv)
   prm.damped = conf.flag(C + "Using dampped Newton iteration") ? 1 : 0;
   prm.bt = bt;
 
+  // cube with pair-breaking z faces (zero orbital-z column); cells of an adaptive level
+  const double lo[3] = {-half, -half, -half}, hi[3] = {half, half, half};
+  const int dxy[2] = {0, 0};
+  struct Mesh
+  {
+    int nn = 0, nc = 0, nh = 0;
+    std::vector<double> xyz, hw;
+    std::vector<int32_t> cell, hptr, hpar;
+    std::vector<uint32_t> mask;
+  } M;
+  auto make_mesh = [&](const int8_t *flags) -> bool {
+    const int cells[3] = {n, n, n};
+    auto call = [&](bool sizes) {
+      return flags ? glgpu_mesh_box_refine(lo, hi, cells, flags, dxy, &M.nn, &M.nc, &M.nh,
+                                           sizes ? nullptr : M.xyz.data(), sizes ? nullptr : M.cell.data(),
+                                           sizes ? nullptr : M.mask.data(), sizes ? nullptr : M.hptr.data(),
+                                           sizes ? nullptr : M.hpar.data(), sizes ? nullptr : M.hw.data())
+                   : glgpu_mesh_box(lo, hi, cells, 0.0, dxy, &M.nn, &M.nc, &M.nh, sizes ? nullptr : M.xyz.data(),
+                                    sizes ? nullptr : M.cell.data(), sizes ? nullptr : M.mask.data(),
+                                    sizes ? nullptr : M.hptr.data(), sizes ? nullptr : M.hpar.data(),
+                                    sizes ? nullptr : M.hw.data());
+    };
+    if (call(true)) return false;
+    M.xyz.resize(3 * static_cast<size_t>(M.nn));
+    M.cell.resize(8 * static_cast<size_t>(M.nc));
+    M.mask.resize(M.nn);
+    M.hptr.resize(static_cast<size_t>(M.nn) + 1);
+    M.hpar.resize(M.nh > 0 ? M.nh : 1);
+    M.hw.resize(M.nh > 0 ? M.nh : 1);
+    return call(false) == GLGPU_OK;
+  };
+  if (!make_mesh(nullptr)) return fail("mesh");
   glgpu_ctx *ctx = nullptr;
-  if (glgpu_create(&mesh, &prm, 1, &ctx)) return fail("create");
-  std::vector<double> x(18 * static_cast<size_t>(nn));
-  if (glgpu_bphase_guess(p, t, scc ? 1 : 0, nn, noise, seed, x.data()) || glgpu_set_solution(ctx, x.data()))
+  auto open = [&]() -> bool {
+    glgpu_mesh mesh{3, M.nn, M.nc, M.xyz.data(), M.cell.data(), M.mask.data(), M.hptr.data(), M.hpar.data(),
+                    M.hw.data()};
+    if (ctx) glgpu_destroy(ctx);
+    ctx = nullptr;
+    return glgpu_create(&mesh, &prm, 1, &ctx) == GLGPU_OK;
+  };
+  if (!open()) return fail("create");
+  std::vector<double> x(18 * static_cast<size_t>(M.nn));
+  if (glgpu_bphase_guess(p, t, scc ? 1 : 0, M.nn, noise, seed, x.data()) || glgpu_set_solution(ctx, x.data()))
     return fail("initial state");
 
-  glgpu_event_start(ctx);
-  double res = 0.0;
-  int total_its = 0, it = 0;
-  bool converged = false;
-  for (it = 0; it <= n_iter; ++it)
+  const char *thr_key[4] = {"Cycle 0 refinement threshold", "Cycle 1 refinement threshold",
+                            "Cycle 2 refinement threshold", "Cycle 3 refinement threshold"};
+  const char *tol_key[5] = {"Cycle 0 linear solver tol", "Cycle 1 linear solver tol", "Cycle 2 linear solver tol",
+                            "Cycle 3 linear solver tol", "Cycle 4 linear solver tol"};
+  const char *glob_key[4] = {"Cycle 1 do global refinement", "Cycle 2 do global refinement",
+                             "Cycle 3 do global refinement", "Cycle 4 do global refinement"};
+  bool adaptive_done = false, converged = false;
+  double res = 0.0, gpu_ms = 0.0;
+  int total_newton = 0, total_its = 0;
+  for (int cycle = 0; cycle <= n_cycles; ++cycle)
     {
-      double rhs = 0.0, r = 0.0;
-      int its = 0, trials = 0;
-      if (glgpu_assemble_system(ctx, &rhs)) return fail("assemble_system");
-      const glgpu_status st = glgpu_solve(ctx, tol0, &its);
-      if (st != GLGPU_OK && st != GLGPU_ERR_NOT_CONVERGED) return fail("solve");
-      if (glgpu_newton_iteration(ctx, &r, &trials)) return fail("newton_iteration");
-      total_its += its;
-      res = r;
-      std::printf("  iteration %2d: |rhs| %.6e, GMRES %4d%s, line-search trials %d, |R| %.6e\n", it, rhs, its,
-                  st == GLGPU_ERR_NOT_CONVERGED ? " (limit)" : "", trials, r);
-      if (r <= acc)
+      if (cycle > 0)
+        {
+          // refine_grid (refine.cc:110-176): global or adaptive, then solution transfer
+          const bool global = conf.flag(C + glob_key[cycle - 1]);
+          if (!global && adaptive_done)
+            {
+              std::printf("  note: cycle %d would refine an adaptively refined mesh a second level; the host mesher "
+                          "supports one adaptive level, so the cycles end here\n", cycle);
+              break;
+            }
+          if (global && adaptive_done)
+            {
+              std::printf("  note: cycle %d would refine an adaptively refined mesh globally; the cycles end here\n",
+                          cycle);
+              break;
+            }
+          std::vector<double> xu(x.size());
+          if (glgpu_get_solution(ctx, xu.data())) return fail("get_solution");
+          const int n_old = n;
+          std::vector<int8_t> flags;
+          if (global)
+            {
+              n *= 2;
+              if (!make_mesh(nullptr)) return fail("mesh");
+            }
+          else
+            {
+              flags.resize(M.nc);
+              if (glgpu_estimate_error(ctx, nullptr) || glgpu_refine_flags(ctx, ratio, coarsen, flags.data()))
+                return fail("error estimate");
+              if (!make_mesh(flags.data())) return fail("mesh");
+              adaptive_done = true;
+            }
+          const int cells_old[3] = {n_old, n_old, n_old};
+          x.assign(18 * static_cast<size_t>(M.nn), 0.0);
+          if (glgpu_box_interpolate(lo, hi, cells_old, xu.data(), M.nn, M.xyz.data(), x.data()))
+            return fail("solution transfer");
+          if (!open()) return fail("create");
+          if (glgpu_set_solution(ctx, x.data())) return fail("set_solution");
+          std::printf("refinement cycle %d (%s): %d cells, %d nodes, %d hanging-constraint entries\n", cycle,
+                      global ? "global" : "adaptive", M.nc, M.nn, M.nh);
+        }
+      const double tol = conf.num(C + tol_key[cycle]);
+      const double thr = cycle < 4 ? conf.num(C + thr_key[cycle]) : 0.0;
+      double last = 0.0;
+      glgpu_event_start(ctx);
+      for (int it = 0; it <= n_iter; ++it)
+        {
+          double rhs = 0.0, r = 0.0;
+          int its = 0, trials = 0;
+          if (glgpu_assemble_system(ctx, &rhs)) return fail("assemble_system");
+          const glgpu_status st = glgpu_solve(ctx, tol, &its);
+          if (st != GLGPU_OK && st != GLGPU_ERR_NOT_CONVERGED) return fail("solve");
+          if (glgpu_newton_iteration(ctx, &r, &trials)) return fail("newton_iteration");
+          total_its += its;
+          ++total_newton;
+          res = r;
+          std::printf("  iteration %2d: |rhs| %.6e, GMRES %4d%s, line-search trials %d, |R| %.6e\n", it, rhs, its,
+                      st == GLGPU_ERR_NOT_CONVERGED ? " (limit)" : "", trials, r);
+          if (std::fabs(r - last) < thr && r > acc && cycle < n_cycles) break; // stalled: refine
+          if (r <= acc) break;
+          last = r;
+        }
+      double ms = 0.0;
+      glgpu_event_stop(ctx, &ms);
+      gpu_ms += ms;
+      if (res <= acc)
         {
           converged = true;
           break;
         }
     }
-  double ms = 0.0, F = 0.0;
-  glgpu_event_stop(ctx, &ms);
+  double F = 0.0;
   if (glgpu_free_energy(ctx, &F)) return fail("free_energy");
   std::printf("%s after %d Newton iterations (%d GMRES): |R| = %.6e, F = %.15e, %.1f ms on the GPU\n",
-              converged ? "converged" : "NOT converged", converged ? it + 1 : it, total_its, res, F, ms);
+              converged ? "converged" : "NOT converged", total_newton, total_its, res, F, gpu_ms);
   if (!out_path.empty())
     {
+      x.resize(18 * static_cast<size_t>(M.nn));
       if (glgpu_get_solution(ctx, x.data())) return fail("get_solution");
       FILE *f = std::fopen(out_path.c_str(), "wb");
       if (!f || std::fwrite(x.data(), sizeof(double), x.size(), f) != x.size())
