@@ -122,12 +122,12 @@ cudaError_t init_constants();
 // ---- linear algebra (kernels_la.cu) ----
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
                         cudaStream_t s, const void *b = nullptr);
-// Matrix-free FP32 Jacobian from the quadrature Hessians H [Nc][171][8] (3D, 18 components):
+// Matrix-free FP32 Jacobian at the state xs [Nn][18] (FP32 copy of the distributed Newton
+// state; 3D, 18 components): the bulk Hessian is applied at each quadrature point from the
+// interpolated state without forming it.
 // mode 0: y = J z, 1: y = b - J z, 2: y = z + omega D^-1 (b - J z) with D^-1 [Nn][324].
-// ycell [Nc][8][18] is scratch; constrained rows act as the identity.
-// err (optional): set to 1 when a CTA's wait for its Hessian copy times out (the
-// output is then NaN, which the solver's norms report).
-cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *ycell, float *y, const float *b,
+// ycell [Nc][8][18] is scratch; constrained rows act as the identity.  err is unused.
+cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
                       const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
                       int *err = nullptr, int cells_per_cta = 8);
 // One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives

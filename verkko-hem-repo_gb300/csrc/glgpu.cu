@@ -146,6 +146,7 @@ struct glgpu_ctx
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   bool mf = false;                   // the Krylov operator is applied matrix-free from H (FP32, 3D)
   float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
+  float *x32 = nullptr;              // FP32 copy of the state the matrix-free operator linearises at
   int *d_err = nullptr;              // device-side wait timeouts (matrix-free Hessian copies)
   bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
   bool prec_built = false;           // a multigrid hierarchy exists for some earlier Jacobian
@@ -349,7 +350,7 @@ glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
 {
   if (c->mf)
     return launch(c, KK_SPMV, mf_launches(c), [&] {
-      return launch_mf(c->dm, static_cast<const float *>(c->H), static_cast<const float *>(in), c->ycell,
+      return launch_mf(c->dm, c->x32, static_cast<const float *>(in), c->ycell,
                        static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err, c->prm[0].mf_cells);
     });
   return launch(c, KK_SPMV, 1, [&] { return launch_spmv(c->dm, c->mixed, c->vals, in, out, act, c->st); });
@@ -865,7 +866,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   auto smooth = [&](const void *zin, void *zout) {
     if (L->mf && zin)
       return launch(L, KK_PREC, mf_launches(L), [&] {
-        return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(zin), L->ycell,
+        return launch_mf(L->dm, L->x32, static_cast<const float *>(zin), L->ycell,
                          static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
                          static_cast<float>(om), 2, act, L->st, L->d_err, L->prm[0].mf_cells);
       });
@@ -882,7 +883,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   // coarse-grid correction: oth = cur + P e, e = V-cycle(R (r - J cur))
   if (L->mf)
     CKS(launch(L, KK_SPMV, mf_launches(L), [&] {
-      return launch_mf(L->dm, static_cast<const float *>(L->H), static_cast<const float *>(cur), L->ycell,
+      return launch_mf(L->dm, L->x32, static_cast<const float *>(cur), L->ycell,
                        static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err, L->prm[0].mf_cells);
     }));
   else
@@ -1336,7 +1337,8 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   // mixed 3D contexts apply the Krylov operator matrix-free from the FP32 Hessians
   if (c->mixed && P.dim == 3 && P.B == 18 && P.nv == 8)
     {
-      if ((s = dalloc(c, &c->ycell, static_cast<size_t>(P.nc) * P.nv * P.B)) || (s = dalloc(c, &c->d_err, 1)))
+      if ((s = dalloc(c, &c->ycell, static_cast<size_t>(P.nc) * P.nv * P.B)) || (s = dalloc(c, &c->d_err, 1)) ||
+          (s = dalloc(c, &c->x32, static_cast<size_t>(c->N))))
         return fail(s);
       if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(GLGPU_ERR_CUDA, "cudaMemset"));
       c->mf = true;
@@ -1469,9 +1471,16 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
       }));
       if (need_r) CKS(robin_res(c, c->x, c->e_cell, act));
     }
-  else
+  // a small last Newton step keeps the previous preconditioner; the matrix-free operator
+  // works from the state alone, so the Hessians and the block matrix are then formed only
+  // on demand
+  const double reuse = c->prm[0].prec_reuse;
+  const bool keep_prec = reuse > 0 && c->mf && c->n_levels > 0 && c->prec_built && c->last_step_rel < reuse;
+  if (c->mixed)
     {
-      CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
+      if (c->mf) CKS(axpby(c, c->x, c->x32, nullptr, coefs(1.0, 0.0), act, false, true, true));
+      if (!keep_prec)
+        CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, act, c->st); }));
       if (need_r)
         {
           CKS(launch(c, KK_RES, 1, [&] {
@@ -1480,10 +1489,6 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
           CKS(robin_res(c, c->x, nullptr, act));
         }
     }
-  // a small last Newton step keeps the previous preconditioner; the matrix-free operator
-  // needs only H, so the block matrix is then rebuilt only on demand
-  const double reuse = c->prm[0].prec_reuse;
-  const bool keep_prec = reuse > 0 && c->mf && c->n_levels > 0 && c->prec_built && c->last_step_rel < reuse;
   if (keep_prec)
     c->bsr_stale = true;
   else
@@ -1822,6 +1827,8 @@ extern "C" glgpu_status glgpu_get_system(const glgpu_ctx *cc, int32_t *rowptr, i
   if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_get_system: NULL context");
   if (c->bsr_stale)
     {
+      // the Hessians were not formed at this state (matrix-free step): form them, then the rows
+      CKS(launch(c, KK_CELL, 1, [&] { return launch_cell(c->dm, true, c->x, c->H, nullptr, nullptr, nullptr, c->st); }));
       CKS(launch(c, KK_ROWS, 1, [&] { return launch_rows(c->dm, c->mixed, c->H, c->vals, c->st); }));
       c->bsr_stale = false;
     }

@@ -1,20 +1,22 @@
 // Matrix-free application of the FP32 Jacobian (mixed mode, 3D Q1, 18 components).
 //
-// The assembled block row of a node holds 27 x 324 scalars; the cell data it is built from
-// is 171 x 8 quadrature Hessian entries per cell plus the cell geometry, about 6.6x less.
-// So the Krylov operator y = J z is applied cell by cell from the Hessians H that the
-// assembly already wrote, and summed per node by a gather over the plan's (cell, vertex,
-// weight) contributions (the same lists that condense the residual: hanging vertices pass
-// to their parents, no atomics):
+// The assembled block row of a node holds 27 x 324 scalars.  Here the Krylov operator
+// y = J z is applied cell by cell from the state itself: the state A and the direction Z
+// are interpolated to the 2x2x2 Gauss points, the bulk Hessian is applied to Z at each
+// point in closed form (complex 3x3 algebra, hvp_part) without being formed, and the
+// gradient terms act on the interpolated derivatives:
 //
-//   (J z)_a = jxw sum_q [ val_q(a) H_q Z_q + sum_k dval_q(a)/dx_k F_k(q) ],
+//   (J z)_a = jxw sum_q [ val_q(a) (H(A_q) Z_q) + sum_k dval_q(a)/dx_k F_k(q) ],
 //   F_k = K1 dZ/dx_k + [k == j(c)] (K2+K3) div_pm(c) Z,
 //
 // the same bilinear form as the assembled block (a, b) = vol sum_q S_abq H_q + gradient
-// terms.  Interpolation to the 2x2x2 Gauss points and the transposed contraction are
+// terms.  The cell results are summed per node by a gather over the plan's (cell, vertex,
+// weight) contributions (the lists that condense the residual: hanging vertices pass to
+// their parents, no atomics).  Interpolation and the transposed contraction are
 // sum-factorised along the axes.  Constrained rows (hanging nodes, zero-Dirichlet
-// components) act as the identity, and constrained components of z are read as zero;
-// Krylov vectors are zero there.
+// components) act as the identity, and constrained components of z are read as zero.
+// Per apply the operator reads the two nodal vectors and writes / reads the cell results,
+// instead of the 171 x 8 Hessian entries per cell.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -23,7 +25,7 @@
 namespace glgpu
 {
 // cells per CTA (NC = 4, 8 or 16, a run-time choice): 8 NC (cell, point) pairs and 24 NC
-// threads (3 per point in the Hessian product)
+// threads (3 per point in the Hessian-vector product)
 constexpr float kGaF = 0.21132486540518711775f; // Gauss point 1/2 - sqrt(3)/6 on [0, 1]
 constexpr float kGbF = 0.78867513459481288225f;
 
@@ -31,14 +33,20 @@ template <int NC> struct MfSmem
 {
   union
   {
-    float zs[NC][8][18];       // nodal values (gather -> interpolation)
+    struct
+    {
+      float zs[NC][8][18]; // nodal values of the direction (gather -> interpolation)
+      float xs[NC][8][18]; // nodal values of the state
+    } g;
     float part[3][NC * 8][18]; // H Z per point, in three partial sums (product -> contraction)
   } u;
   float Z[NC * 8][19];
+  float X[NC * 8][19]; // the state A at the points
   float gZ[NC * 8][3][18];
   float ih[NC][3];
   float jxw[NC];
   float K1[NC], K23[NC];
+  float bulk[NC][6]; // alpha, beta1..beta5
 };
 
 __device__ __forceinline__ void gauss2f(float f0, float f1, float &q0, float &q1)
@@ -49,70 +57,174 @@ __device__ __forceinline__ void gauss2f(float f0, float f1, float &q0, float &q1
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
-// offset (times 8 points) of the symmetric pair (c, d) in the upper-triangle enumeration of
-// an 18x18 block: 8 * (18 lo - lo (lo - 1) / 2 + hi - lo), lo = min(c, d), hi = max(c, d)
-struct SymTable
+// ---------------------------------------------------------------------------------
+// The bulk Hessian applied to a direction without forming it.  With A = u + i v the 3x3
+// complex order parameter at a point (component c < 9: u(c/3, c%3), else v), P = A A^T,
+// Q = A A^+, p = tr P, q = tr Q and the direction F (packed like A), the product is
+//   H F = alpha F + 2 sum_t beta_t dG_t[F],
+//   dG_1 = dp A^* + p F^*,  dp = 2 sum A_ij F_ij
+//   dG_2 = dq A + q F,      dq = 2 Re sum conj(A_ij) F_ij
+//   dG_3 = (S + S^T) A^* + P F^*,   S = A F^T
+//   dG_4 = (S + S^+) A + Q F,       S = F A^+
+//   dG_5 = (S + S^+) A + Q^* F,     S = F^* A^T
+// (G_t = (1/2) d I_t / dA^*, I_1 = |tr A A^T|^2, I_2 = (tr A A^+)^2, I_3 = tr(A A^T (A A^T)^*),
+// I_4 = tr((A A^+)^2), I_5 = tr(A A^+ (A A^+)^*): femgl/src/cell_mat_vec/cell_mat_lhs_beta*.cc).
+// FP32 complex 3x3 algebra in registers; every index is a compile-time constant.
+// ---------------------------------------------------------------------------------
+struct Cf
 {
-  unsigned short off[18][18];
+  float r, i;
 };
-constexpr SymTable make_sym_table()
+__device__ __forceinline__ Cf cm(Cf a, Cf b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+__device__ __forceinline__ Cf cma(Cf a, Cf b, Cf acc) // acc + a b
 {
-  SymTable t{};
-  for (int c = 0; c < 18; ++c)
-    for (int d = 0; d < 18; ++d)
-      {
-        const int lo = c < d ? c : d, hi = c < d ? d : c;
-        t.off[c][d] = static_cast<unsigned short>(8 * (18 * lo - (lo * (lo - 1)) / 2 + (hi - lo)));
-      }
-  return t;
+  return {fmaf(a.r, b.r, fmaf(-a.i, b.i, acc.r)), fmaf(a.r, b.i, fmaf(a.i, b.r, acc.i))};
 }
-__constant__ SymTable c_sym = make_sym_table();
+__device__ __forceinline__ Cf cj(Cf a) { return {a.r, -a.i}; }
+using M3 = Cf[3][3];
 
-// the t-th pair (c, d), c <= d, of the upper-triangle enumeration (t = 0..170)
-__host__ __device__ constexpr int pair_c(int t)
-{
-  int c = 0;
-  while (t >= 18 - c)
-    {
-      t -= 18 - c;
-      ++c;
-    }
-  return c;
-}
-__host__ __device__ constexpr int pair_d(int t)
-{
-  int c = 0;
-  while (t >= 18 - c)
-    {
-      t -= 18 - c;
-      ++c;
-    }
-  return c + t;
-}
-static_assert(pair_c(170) == 17 && pair_d(170) == 17 && pair_c(17) == 0 && pair_d(18) == 1, "pair enumeration");
-
-// entries T .. END-1 of H_q Z_q, each loaded once and applied to both w_c and w_d (H is
-// symmetric); a compile-time recursion, so every (c, d) is a constant register index
-template <int T, int END>
-__device__ __forceinline__ void hz_terms(const float *__restrict__ Hc, const float (&zq)[18], float (&acc)[18])
-{
-  if constexpr (T < END)
-    {
-      constexpr int c = pair_c(T), d = pair_d(T);
-      const float h = __ldg(Hc + T * 8);
-      acc[c] = fmaf(h, zq[d], acc[c]);
-      if constexpr (c != d) acc[d] = fmaf(h, zq[c], acc[d]);
-      hz_terms<T + 1, END>(Hc, zq, acc);
-    }
-}
-
-// one third of H_q Z_q: entries G*57 .. G*57+56
-template <int G>
-__device__ __forceinline__ void hz_part(const float *__restrict__ Hc, const float (&zq)[18], float (&acc)[18])
+__device__ __forceinline__ void load_m3(const float *a, M3 &A)
 {
 #pragma unroll
-  for (int i = 0; i < 18; ++i) acc[i] = 0.f;
-  hz_terms<G * 57, G * 57 + 57>(Hc, zq, acc);
+  for (int k = 0; k < 9; ++k) A[k / 3][k % 3] = {a[k], a[9 + k]};
+}
+// out += w D
+__device__ __forceinline__ void acc_m3(const M3 &D, float w, float (&out)[18])
+{
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    {
+      out[k] = fmaf(w, D[k / 3][k % 3].r, out[k]);
+      out[9 + k] = fmaf(w, D[k / 3][k % 3].i, out[9 + k]);
+    }
+}
+// C = op_a(X) op_b(Y) with op: 0 plain, 1 transpose, 2 conjugate, 3 conjugate transpose
+template <int OA, int OB> __device__ __forceinline__ void mm3(const M3 &X, const M3 &Y, M3 &C)
+{
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      {
+        Cf acc = {0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          {
+            Cf x = (OA & 1) ? X[k][i] : X[i][k];
+            if (OA & 2) x = cj(x);
+            Cf y = (OB & 1) ? Y[j][k] : Y[k][j];
+            if (OB & 2) y = cj(y);
+            acc = cma(x, y, acc);
+          }
+        C[i][j] = acc;
+      }
+}
+
+// out += w op_a(X) op_b(Y), packed like A (no 3x3 temporary)
+template <int OA, int OB> __device__ __forceinline__ void mm3_acc(const M3 &X, const M3 &Y, float w, float (&out)[18])
+{
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      {
+        Cf acc = {0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          {
+            Cf x = (OA & 1) ? X[k][i] : X[i][k];
+            if (OA & 2) x = cj(x);
+            Cf y = (OB & 1) ? Y[j][k] : Y[k][j];
+            if (OB & 2) y = cj(y);
+            acc = cma(x, y, acc);
+          }
+        out[3 * i + j] = fmaf(w, acc.r, out[3 * i + j]);
+        out[9 + 3 * i + j] = fmaf(w, acc.i, out[9 + 3 * i + j]);
+      }
+}
+
+// terms of thread group G for the point with state a and direction f: out = the group's
+// share of alpha f + sum_t 2 beta_t dG_t[f]; the three groups carry about the same work:
+// G = 0: alpha f + dG_3;  G = 1: dG_4 + dG_1;  G = 2: dG_5 + dG_2
+template <int G>
+__device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[18], const float *cf, float (&out)[18])
+{
+  M3 A, F, S, X;
+  load_m3(a, A);
+  load_m3(f, F);
+  if constexpr (G == 0)
+    {
+#pragma unroll
+      for (int k = 0; k < 18; ++k) out[k] = cf[0] * f[k];
+      // dG_3 = (S + S^T) A^* + P F^*, S = A F^T, P = A A^T
+      const float w3 = 2.f * cf[3];
+      mm3<0, 1>(A, F, S);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) X[i][j] = {S[i][j].r + S[j][i].r, S[i][j].i + S[j][i].i};
+      mm3_acc<0, 2>(X, A, w3, out);
+      mm3<0, 1>(A, A, S); // P
+      mm3_acc<0, 2>(S, F, w3, out);
+    }
+  else
+    {
+#pragma unroll
+      for (int k = 0; k < 18; ++k) out[k] = 0.f;
+      if constexpr (G == 1)
+        {
+          // dG_1 = dp A^* + p F^*, p = tr A A^T, dp = 2 sum A_ij F_ij
+          Cf p = {0.f, 0.f}, dp = {0.f, 0.f};
+#pragma unroll
+          for (int k = 0; k < 9; ++k)
+            {
+              const Cf x = A[k / 3][k % 3], y = F[k / 3][k % 3];
+              p = cma(x, x, p);
+              dp = cma(x, y, dp);
+            }
+          dp = {2.f * dp.r, 2.f * dp.i};
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) X[i][j] = cma(p, cj(F[i][j]), cm(dp, cj(A[i][j])));
+          acc_m3(X, 2.f * cf[1], out);
+        }
+      else
+        {
+          // dG_2 = dq A + q F, q = tr A A^+, dq = 2 Re sum conj(A_ij) F_ij
+          float q = 0.f, dq = 0.f;
+#pragma unroll
+          for (int k = 0; k < 9; ++k)
+            {
+              const Cf x = A[k / 3][k % 3], y = F[k / 3][k % 3];
+              q = fmaf(x.r, x.r, fmaf(x.i, x.i, q));
+              dq = fmaf(x.r, y.r, fmaf(x.i, y.i, dq));
+            }
+          dq *= 2.f;
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              X[i][j] = {fmaf(dq, A[i][j].r, q * F[i][j].r), fmaf(dq, A[i][j].i, q * F[i][j].i)};
+          acc_m3(X, 2.f * cf[2], out);
+        }
+      // dG_4 (G = 1) / dG_5 (G = 2) = (S + S^+) A + Q F (Q^* F), S = F A^+ (F^* A^T), Q = A A^+
+      const float w = 2.f * cf[3 + G];
+      if constexpr (G == 1)
+        mm3<0, 3>(F, A, S);
+      else
+        mm3<2, 1>(F, A, S);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) X[i][j] = {S[i][j].r + S[j][i].r, S[i][j].i - S[j][i].i};
+      mm3_acc<0, 0>(X, A, w, out);
+      mm3<0, 3>(A, A, S); // Q
+      if constexpr (G == 1)
+        mm3_acc<0, 0>(S, F, w, out);
+      else
+        mm3_acc<2, 0>(S, F, w, out);
+    }
 }
 
 // r[a] = sum_q val_q(a) w[q] + sum_k sum_q dval_q(a)/dxi_k F_k[q] (reference cube), a = ax + 2 ay + 4 az:
@@ -213,7 +325,7 @@ __device__ __forceinline__ void mf_contract(const float (&w)[8], const float (&F
 }
 
 template <int NC>
-__global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__restrict__ H,
+__global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
                                                      const float *__restrict__ z, float *__restrict__ ycell,
                                                      const uint8_t *__restrict__ act, int *__restrict__ err)
 {
@@ -223,15 +335,11 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
   const int tid = threadIdx.x;
   const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kMCells;
   const int ncb = static_cast<int>((m.nc - e0) < kMCells ? (m.nc - e0) : kMCells);
-  const float *Hb = H + e0 * static_cast<int64_t>(kNS3) * 8;
-  if (tid == 0)
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(Hb),
-                 "r"(static_cast<uint32_t>(ncb) * kNS3 * 8 * static_cast<uint32_t>(sizeof(float)))
-                 : "memory");
   if (tid < kMCells)
     {
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
       float K1 = 0.f, K23 = 0.f;
+      float bk[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if (tid < ncb)
         {
           const int64_t e = e0 + tid;
@@ -239,6 +347,8 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
           g = m.geo_f[e];
           K1 = m.coef_f[inst * kCoef + 0];
           K23 = m.coef_f[inst * kCoef + 1];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) bk[k] = m.coef_f[inst * kCoef + 2 + k];
         }
       S.ih[tid][0] = g.x;
       S.ih[tid][1] = g.y;
@@ -246,35 +356,88 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
       S.jxw[tid] = 0.125f * g.w;
       S.K1[tid] = K1;
       S.K23[tid] = K23;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) S.bulk[tid][k] = bk[k];
     }
-  for (int idx = tid; idx < kMCells * 144; idx += kMThreads)
-    {
-      const int cl = idx / 144, rem = idx - 144 * cl, v = rem / 18, c = rem - 18 * v;
-      float val = 0.f;
-      if (cl < ncb)
-        {
-          // the node's value, its constraint range and mask are independent loads
-          const int node = m.cells[(e0 + cl) * 8 + v];
-          const float zv = z[static_cast<int64_t>(node) * 18 + c];
-          const int h0 = m.hptr[node], h1 = m.hptr[node + 1];
-          const uint32_t mk = m.mask[node];
-          if (h1 > h0)
-            for (int k = h0; k < h1; ++k)
-              {
-                const int par = m.hpar[k]; // a parent's zero-Dirichlet components do not enter
-                if (!((m.mask[par] >> c) & 1u)) val += static_cast<float>(m.hw[k]) * z[static_cast<int64_t>(par) * 18 + c];
-              }
-          else if (!((mk >> c) & 1u))
-            val = zv;
-        }
-      S.u.zs[cl][v][c] = val;
-    }
+  // nodal values: thread entries idx = tid + k kMThreads, k < 6 (144 NC entries over 24 NC
+  // threads); node ids, then values, ranges and masks are requested together
+  {
+    constexpr int kPer = 6;
+    static_assert(kMCells * 144 == kPer * kMThreads, "six entries per thread");
+    int node[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+      {
+        const int idx = tid + k * kMThreads, cl = idx / 144, v = (idx - 144 * cl) / 18;
+        node[k] = (cl < ncb) ? m.cells[(e0 + cl) * 8 + v] : -1;
+      }
+    float zv[kPer], xv[kPer];
+    int h0[kPer], h1[kPer];
+    uint32_t mk[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+      {
+        const int idx = tid + k * kMThreads, c = (idx % 144) % 18;
+        const bool ok = node[k] >= 0;
+        const int64_t b = ok ? static_cast<int64_t>(node[k]) * 18 + c : 0;
+        zv[k] = ok ? z[b] : 0.f;
+        xv[k] = ok ? xs[b] : 0.f;
+        h0[k] = ok ? m.hptr[node[k]] : 0;
+        h1[k] = ok ? m.hptr[node[k] + 1] : 0;
+        mk[k] = ok ? m.mask[node[k]] : ~0u;
+      }
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+      {
+        const int idx = tid + k * kMThreads, cl = idx / 144, rem = idx - 144 * cl, v = rem / 18, c = rem - 18 * v;
+        float val = 0.f;
+        if (h1[k] > h0[k])
+          for (int j = h0[k]; j < h1[k]; ++j)
+            {
+              const int par = m.hpar[j]; // a parent's zero-Dirichlet components do not enter
+              if (!((m.mask[par] >> c) & 1u)) val += static_cast<float>(m.hw[j]) * z[static_cast<int64_t>(par) * 18 + c];
+            }
+        else if (!((mk[k] >> c) & 1u))
+          val = zv[k];
+        S.u.g.zs[cl][v][c] = val;
+        S.u.g.xs[cl][v][c] = xv[k]; // the state is stored distributed: vertex values as they are
+      }
+  }
   __syncthreads();
   // Z and its physical gradient at the points: thread (cell, component)
   if (tid < kMCells * 18)
     {
       const int cl = tid / 18, c = tid - 18 * cl;
-      const float *xv = &S.u.zs[cl][0][c]; // xv[18 v], v = vx + 2 vy + 4 vz
+      const float *xv = &S.u.g.zs[cl][0][c]; // xv[18 v], v = vx + 2 vy + 4 vz
+      // the state at the 8 points: the same tensor interpolation, values only
+      {
+        const float *sv = &S.u.g.xs[cl][0][c];
+        float aq[2][4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) gauss2f(sv[18 * t], sv[18 * (t + 4)], aq[0][t], aq[1][t]);
+        // along y, in place: aq[qz][2 qy + vx]
+#pragma unroll
+        for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+          for (int vx = 0; vx < 2; ++vx)
+            {
+              float y0, y1;
+              gauss2f(aq[qz][vx], aq[qz][2 + vx], y0, y1);
+              aq[qz][vx] = y0;
+              aq[qz][2 + vx] = y1;
+            }
+#pragma unroll
+        for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+          for (int qy = 0; qy < 2; ++qy)
+            {
+              float v0, v1;
+              gauss2f(aq[qz][2 * qy], aq[qz][2 * qy + 1], v0, v1);
+              const int p0 = cl * 8 + 2 * qy + 4 * qz;
+              S.X[p0][c] = v0;
+              S.X[p0 + 1][c] = v1;
+            }
+      }
       float zq[2][4], zd[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t)
@@ -338,23 +501,29 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
         }
     }
   __syncthreads(); // Z, gZ complete
-  // w = H_q Z_q in three partial sums: thread (point, third of the 171 entries); a warp's
-  // lanes read the same entry for the 8 points of 4 cells (4 x 32 contiguous bytes, L2)
+  // w = H_q Z_q in three partial sums, thread (point, group of bulk terms), from the state
+  // and the direction at the point (hvp_part)
   {
-    const int pq = tid & (kMPts - 1), g = tid / kMPts, cl = pq >> 3, q = pq & 7;
-    float zq[18], acc[18];
+    const int pq = tid & (kMPts - 1), g = tid / kMPts, cl = pq >> 3;
+    float zq[18], aq[18], acc[18];
 #pragma unroll
-    for (int i = 0; i < 18; ++i) zq[i] = S.Z[pq][i];
-    __syncthreads(); // zs (aliased by the partial sums) is no longer read
+    for (int i = 0; i < 18; ++i)
+      {
+        zq[i] = S.Z[pq][i];
+        aq[i] = S.X[pq][i];
+      }
+    float cf[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) cf[k] = S.bulk[cl][k];
+    __syncthreads(); // zs / xs (aliased by the partial sums) are no longer read
     if (cl < ncb)
       {
-        const float *Hc = Hb + cl * kNS3 * 8 + q;
         if (g == 0)
-          hz_part<0>(Hc, zq, acc);
+          hvp_part<0>(aq, zq, cf, acc);
         else if (g == 1)
-          hz_part<1>(Hc, zq, acc);
+          hvp_part<1>(aq, zq, cf, acc);
         else
-          hz_part<2>(Hc, zq, acc);
+          hvp_part<2>(aq, zq, cf, acc);
 #pragma unroll
         for (int i = 0; i < 18; ++i) S.u.part[g][pq][i] = acc[i];
       }
@@ -392,85 +561,75 @@ __global__ void __launch_bounds__(24 * NC) k_mf_cell(DevMesh m, const float *__r
   (void)err;
 }
 
-// Node gather, one warp per node: s = sum of the row's cell contributions (the identity on
-// constrained rows and components), then by mode
+// Node gather: thread (node, component), 16 nodes per CTA.  s = sum of the row's cell
+// contributions (the identity on constrained rows and components), then by mode
 //   0: y = s,  1: y = b - s,  2: y = z + omega D^-1 (b - s)  (D^-1 [Nn][324], one sweep).
-constexpr int kMgWarps = 8;
+// The 18 threads of a node read the same contribution entries (one transaction each) and
+// 18 consecutive floats of every cell result; the contribution lists are loaded for all
+// (up to 8 at a time) before the cell values, so the value loads are in flight together.
+constexpr int kMgNodes = 16;
+constexpr int kMgThreads = kMgNodes * 18;
 
-__global__ void __launch_bounds__(kMgWarps * 32) k_mf_gather(DevMesh m, const float *__restrict__ ycell,
-                                                             const float *__restrict__ z, const float *__restrict__ b,
-                                                             const float *__restrict__ dinv, float *__restrict__ y,
-                                                             float omega, int mode, const uint8_t *__restrict__ act)
+__global__ void __launch_bounds__(kMgThreads) k_mf_gather(DevMesh m, const float *__restrict__ ycell,
+                                                          const float *__restrict__ z, const float *__restrict__ b,
+                                                          const float *__restrict__ dinv, float *__restrict__ y,
+                                                          float omega, int mode, const uint8_t *__restrict__ act)
 {
-  __shared__ float red[kMgWarps][324];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t n = static_cast<int64_t>(blockIdx.x) * kMgWarps + warp;
-  if (n >= m.nn) return;
-  if (act && !act[m.node_inst[n]]) return;
-  // the row's contributions: indices and weights loaded once, one per lane, then the
-  // cell values of all of them requested together
+  __shared__ float t_s[kMgNodes][18];
+  const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kMgNodes + ln;
+  const bool on = n < m.nn && !(act && !act[m.node_inst[n]]);
   float s = 0.f;
-  const bool hang = m.hptr[n + 1] > m.hptr[n];
-  const int k0 = m.rc_ptr[n], k1 = m.rc_ptr[n + 1];
-  for (int base = k0; base < k1; base += 32)
+  if (on)
     {
-      const int nk = (k1 - base) < 32 ? (k1 - base) : 32;
-      int cell = 0, vtx = 0;
-      float wt = 0.f;
-      if (lane < nk)
+      const int k0 = m.rc_ptr[n], k1 = m.rc_ptr[n + 1];
+      for (int base = k0; base < k1; base += 8)
         {
-          cell = m.rc_cell[base + lane];
-          vtx = m.rc_a[base + lane];
-          wt = m.rc_wf[base + lane];
+          const int nk = (k1 - base) < 8 ? (k1 - base) : 8;
+          int cell[8], vtx[8];
+          float w[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            {
+              cell[k] = 0;
+              vtx[k] = 0;
+              w[k] = 0.f;
+              if (k < nk)
+                {
+                  cell[k] = m.rc_cell[base + k];
+                  vtx[k] = m.rc_a[base + k];
+                  w[k] = m.rc_wf[base + k];
+                }
+            }
+          float v[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            v[k] = (k < nk) ? __ldg(ycell + static_cast<int64_t>(cell[k]) * 144 + vtx[k] * 18 + c) : 0.f;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) s = fmaf(w[k], v[k], s);
         }
-#pragma unroll 4
-      for (int k = 0; k < nk; ++k)
-        {
-          const int ck = __shfl_sync(0xffffffffu, cell, k), ak = __shfl_sync(0xffffffffu, vtx, k);
-          const float w = __shfl_sync(0xffffffffu, wt, k);
-          if (lane < 18) s += w * ycell[static_cast<int64_t>(ck) * 144 + ak * 18 + lane];
-        }
+      if (m.hptr[n + 1] > m.hptr[n] || ((m.mask[n] >> c) & 1u)) s = z[n * 18 + c];
     }
-  if (lane < 18 && (hang || ((m.mask[n] >> lane) & 1u))) s = z[n * 18 + lane];
   if (mode == 0)
     {
-      if (lane < 18) y[n * 18 + lane] = s;
+      if (on) y[n * 18 + c] = s;
       return;
     }
-  const float t = (lane < 18) ? b[n * 18 + lane] - s : 0.f;
+  const float t = on ? b[n * 18 + c] - s : 0.f;
   if (mode == 1)
     {
-      if (lane < 18) y[n * 18 + lane] = t;
+      if (on) y[n * 18 + c] = t;
       return;
     }
-  // u = D^-1 t with the SpMV lane map: lane owns float4 chunks lane, lane + 32, lane + 64
-  const float4 *bp = reinterpret_cast<const float4 *>(dinv + n * 324);
+  // u = D^-1 t: row c of the node's 18 x 18 block against the node's t
+  t_s[ln][c] = t;
+  __syncthreads();
+  if (!on) return;
+  const float *row = dinv + n * 324 + c * 18;
+  float u = 0.f;
 #pragma unroll
-  for (int it = 0; it < 3; ++it)
-    {
-      const int ch = lane + 32 * it;
-      const float4 wv = (ch < 81) ? __ldg(bp + ch) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const int e = (ch < 81) ? ch * 4 : 0;
-      const float p0 = wv.x * __shfl_sync(0xffffffffu, t, (e + 0) % 18);
-      const float p1 = wv.y * __shfl_sync(0xffffffffu, t, (e + 1) % 18);
-      const float p2 = wv.z * __shfl_sync(0xffffffffu, t, (e + 2) % 18);
-      const float p3 = wv.w * __shfl_sync(0xffffffffu, t, (e + 3) % 18);
-      if (ch < 81)
-        {
-          red[warp][e + 0] = p0;
-          red[warp][e + 1] = p1;
-          red[warp][e + 2] = p2;
-          red[warp][e + 3] = p3;
-        }
-    }
-  __syncwarp();
-  if (lane < 18)
-    {
-      float u = 0.f;
-#pragma unroll
-      for (int d = 0; d < 18; ++d) u += red[warp][lane * 18 + d];
-      y[n * 18 + lane] = z[n * 18 + lane] + omega * u;
-    }
+  for (int d = 0; d < 18; ++d) u = fmaf(__ldg(row + d), t_s[ln][d], u);
+  y[n * 18 + c] = z[n * 18 + c] + omega * u;
 }
 
 // Robin faces in the matrix-free operator: ycell[e] += W z_e for the Robin cells, z_e the
@@ -522,7 +681,7 @@ cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, cons
 }
 
 template <int NC>
-static cudaError_t launch_mf_cell(const DevMesh &m, const float *H, const float *z, float *ycell, const uint8_t *act,
+static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float *z, float *ycell, const uint8_t *act,
                                   int *err, cudaStream_t s)
 {
   static bool attr = false;
@@ -534,24 +693,24 @@ static cudaError_t launch_mf_cell(const DevMesh &m, const float *H, const float 
       attr = true;
     }
   const int64_t gc = (m.nc + NC - 1) / NC;
-  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, H, z, ycell, act, err);
+  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mf(const DevMesh &m, const float *H, const float *z, float *ycell, float *y, const float *b,
+cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
                       const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s, int *err,
                       int cells_per_cta)
 {
   if (m.dim != 3 || m.B != 18 || m.nv != 8) return cudaErrorInvalidValue;
   if (mode == 2 && !dinv) return cudaErrorInvalidValue;
   if (mode >= 1 && !b) return cudaErrorInvalidValue;
-  cudaError_t e = cells_per_cta == 4    ? launch_mf_cell<4>(m, H, z, ycell, act, err, s)
-                  : cells_per_cta == 16 ? launch_mf_cell<16>(m, H, z, ycell, act, err, s)
-                                        : launch_mf_cell<8>(m, H, z, ycell, act, err, s);
+  cudaError_t e = cells_per_cta == 4    ? launch_mf_cell<4>(m, xs, z, ycell, act, err, s)
+                  : cells_per_cta == 16 ? launch_mf_cell<16>(m, xs, z, ycell, act, err, s)
+                                        : launch_mf_cell<8>(m, xs, z, ycell, act, err, s);
   if (e != cudaSuccess) return e;
   if ((e = launch_robin_mf(m, z, ycell, act, s)) != cudaSuccess) return e;
-  const int64_t gn = (m.nn + kMgWarps - 1) / kMgWarps;
-  k_mf_gather<<<static_cast<unsigned>(gn), kMgWarps * 32, 0, s>>>(m, ycell, z, b, dinv, y, omega, mode, act);
+  const int64_t gn = (m.nn + kMgNodes - 1) / kMgNodes;
+  k_mf_gather<<<static_cast<unsigned>(gn), kMgThreads, 0, s>>>(m, ycell, z, b, dinv, y, omega, mode, act);
   return cudaGetLastError();
 }
 
