@@ -295,6 +295,8 @@ def main():
     ap.add_argument("--fp64", action="store_true", help="with --ncu-case / --ncu-solve: FP64 instead of mixed")
     ap.add_argument("--ncu-solve", type=int, default=0,
                     help="profiling case: one complete Newton solve of the N^3 cube (--precond), no timing")
+    ap.add_argument("--prec-reuse", type=float, default=0.0,
+                    help="with --ncu-solve: keep the preconditioner while the last step is below this")
     ap.add_argument("--batch", type=int, default=8, help="instances in the batched leg (0 = skip)")
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
@@ -310,7 +312,7 @@ def main():
     if args.ncu_case:
         return ncu_case(args.ncu_case, args.fp64)
     if args.ncu_solve:
-        return ncu_solve(args.ncu_solve, args.fp64, args.precond)
+        return ncu_solve(args.ncu_solve, args.fp64, args.precond, args.prec_reuse)
     if args.ncu_mlp:
         gl = importlib.import_module("verkko-hem-repo_gb300")
         gl.build()
@@ -526,18 +528,19 @@ def ncu_case(n, fp64):
     return 0
 
 
-def ncu_solve(n, fp64, precond):
+def ncu_solve(n, fp64, precond, prec_reuse=0.0):
     """One complete Newton solve of the workload's physics on an n^3 cube (profiling case)."""
     gl = importlib.import_module("verkko-hem-repo_gb300")
     gl.build()
     m = gl.cube_mesh(HALF, n)
     x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
     pc = gl.PC_MULTIGRID if precond == "mg" else gl.PC_BLOCK_JACOBI
-    prm = gl.Params.from_matep(P_BAR, T_RED, precision=gl.FP64 if fp64 else gl.MIXED, precond=pc)
+    prm = gl.Params.from_matep(P_BAR, T_RED, precision=gl.FP64 if fp64 else gl.MIXED, precond=pc,
+                               prec_reuse=prec_reuse)
     with gl.FemGL(m, prm) as f:
         f.set_solution(x0)
         out = f.run(max_newton=40, linear_tol=1e-4, converge_acc=TOL)
-        print(json.dumps({"ncu_solve": n, "fp64": bool(fp64), "precond": precond,
+        print(json.dumps({"ncu_solve": n, "fp64": bool(fp64), "precond": precond, "prec_reuse": prec_reuse,
                           "newton_its": int(out["newton_its"][0]), "gmres_its": int(out["gmres_its"][0]),
                           "residual": float(out["residual"][0]), "launches": f.launch_count}))
     return 0

@@ -42,14 +42,15 @@ template <> __device__ __forceinline__ double vget<double2, double>(const double
 // ---------------------------------------------------------------------------------
 constexpr int kSpmvWarps = 8;
 
-// Row n's products: acc[it][v] = sum over the row's blocks of block[e] * x[col][e % 18] for
-// the scalars e = (lane + 32 it) * NV + v this lane owns.  The row's column ids are loaded
-// once, one per lane, and broadcast by shuffle, and the block loop is unrolled, so the
-// loads of several blocks are in flight together: short rows on small grids (coarse
-// multigrid levels) would otherwise serialise on the cols -> x load chain.
-template <typename T>
+// Row n's products: acc[it][v] = sum over the row's blocks b = kw, kw + WPR, ... of
+// block[e] * x[col][e % 18] for the scalars e = (lane + 32 it) * NV + v this lane owns.  The
+// row's column ids are loaded once, one per lane, and broadcast by shuffle, and the block
+// loop is unrolled, so the loads of several blocks are in flight together.  With WPR > 1
+// warps per row (small coarse levels, where one warp per 27-block row would leave the
+// GPU latency-bound) warp kw of the row takes every WPR-th block.
+template <typename T, int WPR>
 __device__ __forceinline__ void row_products(const DevMesh &m, const T *__restrict__ vals, const T *__restrict__ x,
-                                             int64_t n, int lane,
+                                             int64_t n, int lane, int kw,
                                              T (&acc)[(324 / Vec16<T>::n + 31) / 32][Vec16<T>::n])
 {
   using V = typename Vec16<T>::type;
@@ -66,7 +67,7 @@ __device__ __forceinline__ void row_products(const DevMesh &m, const T *__restri
       const int nbk = (b1 - base) < 32 ? (b1 - base) : 32;
       const int mycol = (lane < nbk) ? m.cols[base + lane] : 0;
 #pragma unroll 4
-      for (int k = 0; k < nbk; ++k)
+      for (int k = kw; k < nbk; k += WPR)
         {
           const int64_t col = __shfl_sync(0xffffffffu, mycol, k);
           const T xv = (lane < 18) ? x[col * 18 + lane] : T(0);
@@ -87,47 +88,75 @@ __device__ __forceinline__ void row_products(const DevMesh &m, const T *__restri
     }
 }
 
-template <typename T, bool RES>
-__global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *__restrict__ vals,
-                                                            const T *__restrict__ x, T *__restrict__ y,
-                                                            const uint8_t *__restrict__ act, const T *__restrict__ b)
+// the row sums of red[w0 .. w0 + WPR - 1] for component `lane` (< 18)
+template <typename T, int WPR>
+__device__ __forceinline__ T row_sum(const T (*red)[324], int w0, int lane)
 {
-  using V = typename Vec16<T>::type;
+  T s = 0;
+#pragma unroll
+  for (int j = 0; j < WPR; ++j)
+#pragma unroll
+    for (int d = 0; d < 18; ++d) s += red[w0 + j][lane * 18 + d];
+  return s;
+}
+
+// spill a warp's products into its red row
+template <typename T>
+__device__ __forceinline__ void store_products(T *red_w, const T (&acc)[(324 / Vec16<T>::n + 31) / 32][Vec16<T>::n],
+                                               int lane)
+{
   constexpr int NV = Vec16<T>::n;
   constexpr int NCH = 324 / NV;
   constexpr int NIT = (NCH + 31) / 32;
-  __shared__ T red[kSpmvWarps][324];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
-  if (n >= m.nn) return;
-  if (act && !act[m.node_inst[n]]) return;
-  T bv = T(0);
-  if (RES && lane < 18) bv = b[n * 18 + lane];
-  T acc[NIT][NV];
-  row_products<T>(m, vals, x, n, lane, acc);
 #pragma unroll
   for (int it = 0; it < NIT; ++it)
     {
       const int ch = lane + 32 * it;
       if (ch < NCH)
 #pragma unroll
-        for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
+        for (int v = 0; v < NV; ++v) red_w[ch * NV + v] = acc[it][v];
     }
-  __syncwarp();
-  if (lane < 18)
+}
+
+// y = A x (RES: y = b - A x); kSpmvWarps / WPR rows per CTA
+template <typename T, bool RES, int WPR>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *__restrict__ vals,
+                                                            const T *__restrict__ x, T *__restrict__ y,
+                                                            const uint8_t *__restrict__ act, const T *__restrict__ b)
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NIT = (324 / NV + 31) / 32;
+  __shared__ T red[kSpmvWarps][324];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int kw = warp % WPR, w0 = warp - kw;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * (kSpmvWarps / WPR) + warp / WPR;
+  const bool on = n < m.nn && !(act && !act[m.node_inst[n]]);
+  if (WPR == 1 && !on) return;
+  T bv = T(0);
+  if (on && RES && kw == 0 && lane < 18) bv = b[n * 18 + lane];
+  if (on)
     {
-      T s = 0;
-#pragma unroll
-      for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
+      T acc[NIT][NV];
+      row_products<T, WPR>(m, vals, x, n, lane, kw, acc);
+      store_products<T>(red[warp], acc, lane);
+    }
+  if (WPR > 1)
+    __syncthreads();
+  else
+    __syncwarp();
+  if (on && kw == 0 && lane < 18)
+    {
+      const T s = row_sum<T, WPR>(red, w0, lane);
       y[n * 18 + lane] = RES ? bv - s : s; // A x, or the residual b - A x
     }
 }
 
 // One damped block-Jacobi sweep, fused: y = z + omega D^-1 (b - A z) (z == nullptr: the
-// sweep from zero, y = omega D^-1 b).  One warp per block row: the row's SpMV as in
-// k_spmv18, then the 18x18 inverse block applied with the same lane map.  y must not
-// alias z (neighbouring rows read z).
-template <typename T>
+// sweep from zero, y = omega D^-1 b).  The row's SpMV as in k_spmv18 (WPR warps per row),
+// then the 18x18 inverse block applied by the row's first warp with the same lane map.
+// y must not alias z (neighbouring rows read z).
+template <typename T, int WPR>
 __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T *__restrict__ vals,
                                                               const T *__restrict__ dinv, const T *__restrict__ b,
                                                               const T *__restrict__ z, T *__restrict__ y, T omega,
@@ -139,32 +168,30 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T
   constexpr int NIT = (NCH + 31) / 32;
   __shared__ T red[kSpmvWarps][324];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSpmvWarps + warp;
-  if (n >= m.nn) return;
-  if (act && !act[m.node_inst[n]]) return;
-  T t = (lane < 18) ? b[n * 18 + lane] : T(0);
+  const int kw = warp % WPR, w0 = warp - kw;
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * (kSpmvWarps / WPR) + warp / WPR;
+  const bool on = n < m.nn && !(act && !act[m.node_inst[n]]);
+  if (WPR == 1 && !on) return;
+  T t = (on && lane < 18) ? b[n * 18 + lane] : T(0);
   if (z)
     {
-      T acc[NIT][NV];
-      row_products<T>(m, vals, z, n, lane, acc);
-#pragma unroll
-      for (int it = 0; it < NIT; ++it)
+      if (on)
         {
-          const int ch = lane + 32 * it;
-          if (ch < NCH)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
+          T acc[NIT][NV];
+          row_products<T, WPR>(m, vals, z, n, lane, kw, acc);
+          store_products<T>(red[warp], acc, lane);
         }
-      __syncwarp();
-      if (lane < 18)
-        {
-          T s = 0;
-#pragma unroll
-          for (int d = 0; d < 18; ++d) s += red[warp][lane * 18 + d];
-          t -= s;
-        }
-      __syncwarp();
+      if (WPR > 1)
+        __syncthreads();
+      else
+        __syncwarp();
+      if (lane < 18 && on) t -= row_sum<T, WPR>(red, w0, lane);
+      if (WPR > 1)
+        __syncthreads();
+      else
+        __syncwarp();
     }
+  if (!on || kw != 0) return;
   // u = D^-1 t
   {
     T acc[NIT][NV];
@@ -181,21 +208,12 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T
             acc[it][v] = vget<V, T>(w, v) * __shfl_sync(0xffffffffu, t, e % 18);
           }
       }
-#pragma unroll
-    for (int it = 0; it < NIT; ++it)
-      {
-        const int ch = lane + 32 * it;
-        if (ch < NCH)
-#pragma unroll
-          for (int v = 0; v < NV; ++v) red[warp][ch * NV + v] = acc[it][v];
-      }
+    store_products<T>(red[warp], acc, lane);
     __syncwarp();
   }
   if (lane < 18)
     {
-      T u = 0;
-#pragma unroll
-      for (int d = 0; d < 18; ++d) u += red[warp][lane * 18 + d];
+      const T u = row_sum<T, 1>(red, warp, lane);
       y[n * 18 + lane] = (z ? z[n * 18 + lane] : T(0)) + omega * u;
     }
 }
@@ -220,36 +238,39 @@ __global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restri
   y[2 * n + 1] = y1;
 }
 
+// Rows below this count (coarse multigrid levels) get 4 warps per row.
+constexpr int64_t kSmallRows = 20000;
+
+template <typename T, bool RES, int WPR>
+static void spmv18_t(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act, const void *b,
+                     cudaStream_t s)
+{
+  constexpr int rows = kSpmvWarps / WPR;
+  const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
+  k_spmv18<T, RES, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const T *>(vals), static_cast<const T *>(x),
+                                                          static_cast<T *>(y), act, static_cast<const T *>(b));
+}
+
+template <typename T>
+static void spmv18_dispatch(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act,
+                            const void *b, cudaStream_t s)
+{
+  const bool small = m.nn < kSmallRows;
+  if (b)
+    small ? spmv18_t<T, true, 4>(m, vals, x, y, act, b, s) : spmv18_t<T, true, 1>(m, vals, x, y, act, b, s);
+  else
+    small ? spmv18_t<T, false, 4>(m, vals, x, y, act, b, s) : spmv18_t<T, false, 1>(m, vals, x, y, act, b, s);
+}
+
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
                         cudaStream_t s, const void *b)
 {
   if (m.B == 18)
     {
-      const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
       if (fp32)
-        {
-          const float *bb = static_cast<const float *>(b);
-          if (b)
-            k_spmv18<float, true><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
-                                                                  static_cast<const float *>(x),
-                                                                  static_cast<float *>(y), act, bb);
-          else
-            k_spmv18<float, false><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
-                                                                   static_cast<const float *>(x),
-                                                                   static_cast<float *>(y), act, bb);
-        }
+        spmv18_dispatch<float>(m, vals, x, y, act, b, s);
       else
-        {
-          const double *bb = static_cast<const double *>(b);
-          if (b)
-            k_spmv18<double, true><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
-                                                                   static_cast<const double *>(x),
-                                                                   static_cast<double *>(y), act, bb);
-          else
-            k_spmv18<double, false><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
-                                                                    static_cast<const double *>(x),
-                                                                    static_cast<double *>(y), act, bb);
-        }
+        spmv18_dispatch<double>(m, vals, x, y, act, b, s);
     }
   else
     {
@@ -265,21 +286,28 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
   return cudaGetLastError();
 }
 
+template <typename T, int WPR>
+static void smooth18_t(const DevMesh &m, const void *vals, const void *dinv, const void *b, const void *z, void *y,
+                       double omega, const uint8_t *act, cudaStream_t s)
+{
+  constexpr int rows = kSpmvWarps / WPR;
+  const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
+  k_smooth18<T, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const T *>(vals), static_cast<const T *>(dinv),
+                                                       static_cast<const T *>(b), static_cast<const T *>(z),
+                                                       static_cast<T *>(y), static_cast<T>(omega), act);
+}
+
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,
                           void *y, double omega, const uint8_t *act, cudaStream_t s)
 {
   if (m.B != 18) return cudaErrorInvalidValue;
-  const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
+  const bool small = m.nn < kSmallRows;
   if (fp32)
-    k_smooth18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(vals),
-                                                      static_cast<const float *>(dinv), static_cast<const float *>(b),
-                                                      static_cast<const float *>(z), static_cast<float *>(y),
-                                                      static_cast<float>(omega), act);
+    small ? smooth18_t<float, 4>(m, vals, dinv, b, z, y, omega, act, s)
+          : smooth18_t<float, 1>(m, vals, dinv, b, z, y, omega, act, s);
   else
-    k_smooth18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
-                                                       static_cast<const double *>(dinv), static_cast<const double *>(b),
-                                                       static_cast<const double *>(z), static_cast<double *>(y), omega,
-                                                       act);
+    small ? smooth18_t<double, 4>(m, vals, dinv, b, z, y, omega, act, s)
+          : smooth18_t<double, 1>(m, vals, dinv, b, z, y, omega, act, s);
   return cudaGetLastError();
 }
 
