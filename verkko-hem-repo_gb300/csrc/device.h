@@ -214,6 +214,11 @@ cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, c
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
                             const uint8_t *act, cudaStream_t s);
+// restriction fused with the coarse level's first sweep from zero (18x18 blocks):
+// rc = P^T rf, z = omega D^-1 rc
+cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, const int32_t *idx, const void *w,
+                                   const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
+                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s);
 // Galerkin product J_c = P^T J_f P on the coarse block pattern, one warp per coarse
 // block: block cb (row g_row[cb], column cols_c[cb]) is the sum over its term list
 // [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and

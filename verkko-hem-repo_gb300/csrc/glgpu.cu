@@ -523,7 +523,8 @@ glgpu_status prec_setup(glgpu_ctx *c, const uint8_t *act)
   return GLGPU_OK;
 }
 
-glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act);
+// pre_done: z already holds the first sweep from zero (omega D^-1 r, fused with the restriction)
+glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act, bool pre_done = false);
 
 // z = V-cycle(r) for the flexible GMRES basis, masked by the GMRES activity flags.  The
 // cycle's ~9 launches per level are captured once into a CUDA graph over fixed input and
@@ -847,7 +848,7 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
 // l1 block-Jacobi blocks), the residual is the SpMV's residual form, and the coarse
 // correction is written next to the smoothed iterate, so the buffers ping-pong instead
 // of being copied.
-glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act)
+glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act, bool pre_done)
 {
   const bool m = c->mixed;
   if (l == c->n_levels)
@@ -874,7 +875,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   };
   // pre-smoothing from zero, ping-ponging between z and t2; `cur` holds the iterate
   void *cur = z, *oth = t2;
-  CKS(smooth(nullptr, cur));
+  if (!pre_done) CKS(smooth(nullptr, cur));
   for (int s = 1; s < pre; ++s)
     {
       CKS(smooth(cur, oth));
@@ -890,11 +891,18 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
     CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
   glgpu_ctx *C = c->lv[l];
   const glgpu_ctx::Transfer &tr = c->tr[l];
-  CKS(launch(c, KK_PREC, 1, [&] {
-    return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
-                           C->dm.node_inst, act, c->st);
-  }));
-  CKS(vcycle(c, l + 1, C->Bv, C->X, act));
+  const bool fuse = (l + 1 < c->n_levels) && C->B == 18; // the next level smooths (not the dense solve)
+  if (fuse)
+    CKS(launch(c, KK_PREC, 1, [&] {
+      return launch_restrict_smooth(m, C->nn, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask, C->dm.node_inst, act,
+                                    C->dinv, om, C->X, c->st);
+    }));
+  else
+    CKS(launch(c, KK_PREC, 1, [&] {
+      return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
+                             C->dm.node_inst, act, c->st);
+    }));
+  CKS(vcycle(c, l + 1, C->Bv, C->X, act, fuse));
   CKS(launch(c, KK_PREC, 1, [&] {
     return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, oth, L->dm.mask, L->dm.hptr,
                           L->dm.node_inst, act, c->st, cur);

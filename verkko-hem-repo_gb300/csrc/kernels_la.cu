@@ -238,8 +238,9 @@ __global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restri
   y[2 * n + 1] = y1;
 }
 
-// Rows below this count (coarse multigrid levels) get 4 warps per row.
+// Rows below these counts (coarse multigrid levels) get 4 / 8 warps per row.
 constexpr int64_t kSmallRows = 20000;
+constexpr int64_t kTinyRows = 2000;
 
 template <typename T, bool RES, int WPR>
 static void spmv18_t(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act, const void *b,
@@ -255,11 +256,14 @@ template <typename T>
 static void spmv18_dispatch(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act,
                             const void *b, cudaStream_t s)
 {
-  const bool small = m.nn < kSmallRows;
   if (b)
-    small ? spmv18_t<T, true, 4>(m, vals, x, y, act, b, s) : spmv18_t<T, true, 1>(m, vals, x, y, act, b, s);
+    m.nn < kTinyRows    ? spmv18_t<T, true, 8>(m, vals, x, y, act, b, s)
+    : m.nn < kSmallRows ? spmv18_t<T, true, 4>(m, vals, x, y, act, b, s)
+                        : spmv18_t<T, true, 1>(m, vals, x, y, act, b, s);
   else
-    small ? spmv18_t<T, false, 4>(m, vals, x, y, act, b, s) : spmv18_t<T, false, 1>(m, vals, x, y, act, b, s);
+    m.nn < kTinyRows    ? spmv18_t<T, false, 8>(m, vals, x, y, act, b, s)
+    : m.nn < kSmallRows ? spmv18_t<T, false, 4>(m, vals, x, y, act, b, s)
+                        : spmv18_t<T, false, 1>(m, vals, x, y, act, b, s);
 }
 
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
@@ -301,13 +305,14 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
                           void *y, double omega, const uint8_t *act, cudaStream_t s)
 {
   if (m.B != 18) return cudaErrorInvalidValue;
-  const bool small = m.nn < kSmallRows;
   if (fp32)
-    small ? smooth18_t<float, 4>(m, vals, dinv, b, z, y, omega, act, s)
-          : smooth18_t<float, 1>(m, vals, dinv, b, z, y, omega, act, s);
+    m.nn < kTinyRows    ? smooth18_t<float, 8>(m, vals, dinv, b, z, y, omega, act, s)
+    : m.nn < kSmallRows ? smooth18_t<float, 4>(m, vals, dinv, b, z, y, omega, act, s)
+                        : smooth18_t<float, 1>(m, vals, dinv, b, z, y, omega, act, s);
   else
-    small ? smooth18_t<double, 4>(m, vals, dinv, b, z, y, omega, act, s)
-          : smooth18_t<double, 1>(m, vals, dinv, b, z, y, omega, act, s);
+    m.nn < kTinyRows    ? smooth18_t<double, 8>(m, vals, dinv, b, z, y, omega, act, s)
+    : m.nn < kSmallRows ? smooth18_t<double, 4>(m, vals, dinv, b, z, y, omega, act, s)
+                        : smooth18_t<double, 1>(m, vals, dinv, b, z, y, omega, act, s);
   return cudaGetLastError();
 }
 

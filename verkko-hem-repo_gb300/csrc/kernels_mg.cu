@@ -56,6 +56,37 @@ __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr,
   rc[t] = s;
 }
 
+// Restriction fused with the first smoothing sweep of the coarse level, which starts from
+// zero: rc = P^T rf (zero on zero-Dirichlet components) and z = omega D^-1 rc.  Thread
+// (coarse node, component), 16 nodes per CTA; the node's 18 restricted values meet in
+// shared memory for the 18 x 18 inverse block (18x18 blocks only).
+constexpr int kRsNodes = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(kRsNodes * 18)
+  k_restrict_smooth(int64_t nn_c, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
+                    const T *__restrict__ w, const T *__restrict__ rf, T *__restrict__ rc,
+                    const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ node_inst,
+                    const uint8_t *__restrict__ act, const T *__restrict__ dinv, T omega, T *__restrict__ z)
+{
+  __shared__ T t_s[kRsNodes][18];
+  const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kRsNodes + ln;
+  const bool on = n < nn_c && !(act && !act[node_inst[n]]);
+  T s = 0;
+  if (on && !((mask_c[n] >> c) & 1u))
+    for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * rf[static_cast<int64_t>(idx[k]) * 18 + c];
+  if (on) rc[n * 18 + c] = s;
+  t_s[ln][c] = s;
+  __syncthreads();
+  if (!on) return;
+  const T *row = dinv + n * 324 + c * 18;
+  T u = 0;
+#pragma unroll
+  for (int d = 0; d < 18; ++d) u += row[d] * t_s[ln][d];
+  z[n * 18 + c] = omega * u;
+}
+
 // Galerkin product: one warp per coarse block (I, J).  The block is
 //   J_c(I, J) = sum over fine blocks (i, j) with P(i, I) P(j, J) != 0 of P(i, I) P(j, J) J_f(i, j),
 // a weighted sum of whole fine blocks whose (block index, weight) list is built on the
@@ -181,6 +212,22 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
     k_restrict<double><<<g, 256, 0, s>>>(nn_c, B, ptr, idx, static_cast<const double *>(w),
                                          static_cast<const double *>(rf), static_cast<double *>(rc), mask_c, node_inst,
                                          act);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, const int32_t *idx, const void *w,
+                                   const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
+                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s)
+{
+  const unsigned g = static_cast<unsigned>((nn_c + kRsNodes - 1) / kRsNodes);
+  if (fp32)
+    k_restrict_smooth<float><<<g, kRsNodes * 18, 0, s>>>(
+      nn_c, ptr, idx, static_cast<const float *>(w), static_cast<const float *>(rf), static_cast<float *>(rc), mask_c,
+      node_inst, act, static_cast<const float *>(dinv), static_cast<float>(omega), static_cast<float *>(z));
+  else
+    k_restrict_smooth<double><<<g, kRsNodes * 18, 0, s>>>(
+      nn_c, ptr, idx, static_cast<const double *>(w), static_cast<const double *>(rf), static_cast<double *>(rc), mask_c,
+      node_inst, act, static_cast<const double *>(dinv), omega, static_cast<double *>(z));
   return cudaGetLastError();
 }
 
