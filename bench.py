@@ -36,7 +36,14 @@ TOL = 1e-10
 # DRAM bytes (read + write) of one k_spmv18<float> launch on this workload, from the ncu
 # capture summarised in profiles/k_spmv18_fp32_cube32.md (1.193182 GB + 5.481728 MB)
 SPMV_NCU_TRAFFIC = 1.193182e9 + 5.481728e6
-MF_NCU_TRAFFIC = 1.83917568e8 + 1.1717376e7 + 2.2766848e7  # k_mf_cell + k_mf_gather, one apply, 32^3
+# DRAM bytes of one matrix-free apply (k_mf_cell + k_mf_gather) on this workload, from the ncu
+# capture summarised in profiles/matrix_free_apply_cube32.md (cold caches: the cell results the
+# gather reads come from DRAM there, from L2 in the live solve)
+MF_NCU_TRAFFIC = 7.213824e6 + 0.0 + 2.2760960e7
+# FP32 operations of one matrix-free apply per cell: the closed-form Hessian-vector product at
+# 8 points (3456 per point: alpha f, dG_1..dG_5 with their complex 3x3 products) plus the
+# interpolation of state and direction, the gradient terms and the transposed contraction
+MF_FLOP_PER_CELL = 8 * 3456 + 4500
 METRIC = "GL solves/s at ||F||<1e-10 (femgl 3D, 32^3 Q1, T=0.6Tc, p=20bar)"
 WORKLOAD = "femgl 3D cube L=20, 32^3 Q1 cells, matep(p=20 bar, t=0.6, SCC), z-face pair breaking, B-phase+0.05N(0,1) seed 2"
 
@@ -245,14 +252,22 @@ def e2e_mode(gl, m, x0, precision, steps, linear_tol, precond=None, cfg=None):
     if cfg is not None:
         prm = importlib.import_module("verkko-hem-repo_gb300.autotune").params_with(gl, prm, cfg)
     f = gl.FemGL(m, prm)
-    start = x0 if callable(x0) else (lambda: np.ascontiguousarray(x0))
+    # the step's input and output live in page-locked host memory
+    x_in = gl.pinned_array(f.n_dofs)
+    x_out = gl.pinned_array(f.n_dofs)
+    if callable(x0):
+        start = x0  # the learned start: network inference on host inputs gives the vector
+    else:
+        x_in[:] = x0
+        start = lambda: x_in  # noqa: E731
     solve_once(f, start(), linear_tol)
     t0 = time.perf_counter()
     for _ in range(steps):
-        f.set_solution(start())  # (network inference on host inputs and) host -> device
+        f.set_solution(start())  # host -> device
         f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
-        xo = f.solution()  # device -> host
+        f.solution(out=x_out)  # device -> host
     dt = time.perf_counter() - t0
+    xo = np.array(x_out)
     f.close()
     return steps / dt, xo
 
@@ -403,14 +418,19 @@ def main():
     value = 1000.0 / ms_step
     nd = 18 * m.nn
     nnzb = 912673
-    # the Krylov operator of the mixed path: J z applied matrix-free from the FP32
-    # quadrature Hessians (k_mf_cell + k_mf_gather, two launches per apply); algorithmic
-    # bytes per apply: H (171 entries x 8 points x 4 B per cell), cell connectivity and
-    # geometry, z in, y out
-    mf_bytes = m.nc * (171 * 8 * 4 + 8 * 4 + 16) + 2 * nd * 4
+    # the Krylov operator of the mixed path: J z applied matrix-free at the state
+    # (k_mf_cell + k_mf_gather, two launches per apply); algorithmic bytes per apply: the FP32
+    # state and z in, y out, cell connectivity, geometry and instance id.  It is bound by FP32
+    # issue, not HBM: the fp32 entry gives its arithmetic rate against the CUDA-core peak at
+    # the SM clock sampled during the run
+    mf_bytes = 3 * nd * 4 + m.nc * (8 * 4 + 16 + 4)
     n_mf = mixed["kernel_n"]["spmv"] // 2
     mf_ms = mixed["kernel_ms"]["spmv"] / max(1, n_mf)
     achieved = mf_bytes / (mf_ms * 1e-3) / 1e9 if n_mf else None
+    mf_flop = m.nc * MF_FLOP_PER_CELL
+    sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s, 152 SMs x 128 FP32 lanes x FMA
+    mf_tflops = mf_flop / (mf_ms * 1e-3) / 1e12 if n_mf else None
     # the FP64 path's operator: the assembled block SpMV, timed in the FP64 leg
     spmv_bytes = nnzb * (324 * 8 + 4) + (m.nn + 1) * 4 + 2 * nd * 8
     n_spmv = fp64["kernel_n"]["spmv"]
@@ -472,6 +492,11 @@ def main():
                                        "summarised in profiles/matrix_free_apply_cube32.md",
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
                      "algorithmic_bytes_per_launch": mf_bytes, "avg_launch_ms": mf_ms,
+                     "fp32": {"achieved_tflops": mf_tflops, "peak_tflops": fp32_peak,
+                              "frac": (mf_tflops / fp32_peak) if mf_tflops else None,
+                              "flop_per_apply": mf_flop,
+                              "peak_source": "nominal CUDA-core FP32 (152 SMs x 128 lanes x 2) at the sampled SM clock",
+                              "note": "the operator is bound by FP32 issue and latency, not HBM"},
                      "fp64_block_spmv": {"kernel": "k_spmv18<double>", "achieved": spmv_gbs,
                                          "frac": (spmv_gbs / hbm) if spmv_gbs else None,
                                          "algorithmic_bytes_per_launch": spmv_bytes, "avg_launch_ms": spmv_ms},

@@ -140,6 +140,12 @@ glgpu_status glgpu_sizes(const glgpu_ctx *ctx, int64_t *n_nodes, int64_t *nnzb, 
 glgpu_status glgpu_set_solution(glgpu_ctx *ctx, const double *x);
 glgpu_status glgpu_get_solution(const glgpu_ctx *ctx, double *x);
 
+/* Page-locked host memory for the arrays passed to set_solution / get_solution (and the
+ * other host-array entry points): copies from and to it run as direct DMA instead of
+ * being staged by the driver.  Free with glgpu_host_free. */
+glgpu_status glgpu_host_alloc(size_t bytes, void **p);
+glgpu_status glgpu_host_free(void *p);
+
 /*
  * FemGL<3>::assemble_system (femgl/src/assemble.cc:109-372): Jacobian (block CSR,
  * condensed) and system_rhs = -R at the current solution.  In GLGPU_MIXED mode

@@ -275,3 +275,21 @@ def test_state_errors(gl):
             f.compute_residual()
         assert e.value.status == 5
         assert f.launch_count > 0
+
+
+def test_pinned_host_arrays(gl):
+    """Page-locked host arrays from the library give the same copies as ordinary ones."""
+    m, prm, x0 = _problem(gl, 3, 0.0)
+    with gl.FemGL(m, prm) as f:
+        xin = gl.pinned_array(f.n_dofs)
+        xin[:] = x0
+        f.set_solution(xin)
+        a = f.solution()
+        out = gl.pinned_array(f.n_dofs)
+        b = f.solution(out=out)
+        assert b is out and np.array_equal(a, b)
+        f.set_solution(x0)
+        assert np.array_equal(f.solution(), a)
+        with pytest.raises(ValueError):
+            f.solution(out=np.zeros(3))
+    del xin, out  # the allocations are released with their arrays

@@ -1455,6 +1455,21 @@ extern "C" glgpu_status glgpu_set_solution(glgpu_ctx *c, const double *x)
   return sync(c);
 }
 
+extern "C" glgpu_status glgpu_host_alloc(size_t bytes, void **p)
+{
+  if (!p) return set_error(GLGPU_ERR_ARG, "glgpu_host_alloc: NULL argument");
+  *p = nullptr;
+  if (cudaMallocHost(p, bytes > 0 ? bytes : 1) != cudaSuccess)
+    return set_error(GLGPU_ERR_NOMEM, "glgpu_host_alloc: cudaMallocHost failed");
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_host_free(void *p)
+{
+  if (p && cudaFreeHost(p) != cudaSuccess) return set_error(GLGPU_ERR_CUDA, "glgpu_host_free: cudaFreeHost failed");
+  return GLGPU_OK;
+}
+
 extern "C" glgpu_status glgpu_get_solution(const glgpu_ctx *c, double *x)
 {
   if (!c || !x) return set_error(GLGPU_ERR_ARG, "glgpu_get_solution: NULL argument");

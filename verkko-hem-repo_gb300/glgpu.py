@@ -114,6 +114,8 @@ def lib() -> ctypes.CDLL:
     L.glgpu_box_interpolate.argtypes = [_dp, _dp, _ip, _dp, ctypes.c_int, _dp, _dp]
     L.glgpu_estimate_error.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     L.glgpu_refine_flags.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int8)]
+    L.glgpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.glgpu_host_free.argtypes = [vp]
     L.glgpu_pdw_guess.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int, _dp, _dp]
     L.glgpu_dot_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp, vp]
@@ -285,6 +287,28 @@ def square_mesh(n: int, L: float = 1.0) -> Mesh:
     return Mesh(2, xy, cells, mask)
 
 
+class _Pinned:
+    """Owner of a page-locked host allocation (freed when the last array view goes)."""
+
+    def __init__(self, nbytes: int):
+        self.ptr = ctypes.c_void_p()
+        _check(lib().glgpu_host_alloc(int(nbytes), ctypes.byref(self.ptr)))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) is not None and self.ptr.value:
+            lib().glgpu_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_array(n: int, dtype=np.float64) -> np.ndarray:
+    """A numpy array of n elements in page-locked host memory (direct DMA to and from the GPU)."""
+    dt = np.dtype(dtype)
+    owner = _Pinned(n * dt.itemsize)
+    buf = (ctypes.c_char * (n * dt.itemsize)).from_address(owner.ptr.value)
+    buf._owner = owner  # every view's base chain ends at buf, which keeps the allocation
+    return np.frombuffer(buf, dtype=dt, count=n)
+
+
 def pdw_guess(p: float, t: float, xyz: np.ndarray, u: float, half_D: float, scc: bool = True) -> np.ndarray:
     """Weak-coupling pair-density-wave start (B phase + modulation of amplitude u across a slab
     of thickness 2 half_D) at the node coordinates xyz [nn][3]."""
@@ -444,8 +468,11 @@ class FemGL:
             raise ValueError(f"expected {self.n_dofs} dofs, got {x.size}")
         _check(lib().glgpu_set_solution(self._ctx, _p(x)))
 
-    def solution(self) -> np.ndarray:
-        x = np.zeros(self.n_dofs)
+    def solution(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The current solution (into `out` when given, e.g. a pinned_array)."""
+        x = np.zeros(self.n_dofs) if out is None else out
+        if x.dtype != np.float64 or x.size != self.n_dofs or not x.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float64 array of n_dofs entries")
         _check(lib().glgpu_get_solution(self._ctx, _p(x)))
         return x
 
