@@ -87,7 +87,9 @@ __device__ __forceinline__ T robin_weight(int bits, int a, int b, int col, T wR,
 
 // ---- assembly (kernels_asm.cu) ----
 // Per-cell quadrature data: H [nc][nq][NS] (type T) and/or cell residual
-// r_cell [nc][nv*B] (double) and per-cell free energy (double).
+// r_cell [nc][nv*B] (double) and per-cell free energy (double).  fp32 with r_cell and no H
+// (3D, 18 components: the mixed mode's residual) evaluates the residual in double-float
+// arithmetic on the FP32 pipe; otherwise the residual is FP64.
 cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, double *r_cell, double *e_cell,
                         const uint8_t *inst_active, cudaStream_t s);
 // Gradient part of a full interior row (27 blocks [27][324], slots as in the row kernel)

@@ -331,7 +331,7 @@ int mf_launches(const glgpu_ctx *c) { return 2 + (c->dm.n_robin > 0 ? 1 : 0); }
 glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act, bool energy = false)
 {
   double *ec = energy ? c->e_cell : nullptr;
-  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, false, v, nullptr, c->r_cell, ec, act, c->st); }));
+  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, c->mixed, v, nullptr, c->r_cell, ec, act, c->st); }));
   CKS(robin_res(c, v, ec, act));
   CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   return GLGPU_OK;
@@ -1507,7 +1507,7 @@ static glgpu_status assemble_impl(glgpu_ctx *c, const uint8_t *act)
       if (need_r)
         {
           CKS(launch(c, KK_RES, 1, [&] {
-            return launch_cell(c->dm, false, c->x, nullptr, c->r_cell, nullptr, act, c->st);
+            return launch_cell(c->dm, true, c->x, nullptr, c->r_cell, nullptr, act, c->st);
           }));
           CKS(robin_res(c, c->x, nullptr, act));
         }

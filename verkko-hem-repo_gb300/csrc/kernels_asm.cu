@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "device.h"
+#include "dfloat.h"
 #include "glgpu_internal.h"
 
 namespace glgpu
@@ -532,19 +533,21 @@ constexpr int kRThreads = 192;           // = 3 * kRPts (one thread per (point, 
 constexpr double kGa = 0.21132486540518711775; // 1/2 - sqrt(3)/6: Gauss point on [0, 1]
 constexpr double kGb = 0.78867513459481288225; // 1/2 + sqrt(3)/6
 
-struct ResSmem
+// R = double (FP64 mode) or DF (double-float on the FP32 pipe, mixed mode)
+template <typename R> struct ResSmemT
 {
-  double xs[kRCells][8][18];
-  double A[kRPts][19];
-  double gA[kRPts][3][18];
-  double P[kRPts][19], Q[kRPts][19];
-  double rb[kRPts][18];
-  double en[kRPts];
-  double coef[kRCells][kCoef];
-  double ih[kRCells][3];
-  double jxw[kRCells];
+  R xs[kRCells][8][18];
+  R A[kRPts][19];
+  R gA[kRPts][3][18];
+  R P[kRPts][19], Q[kRPts][19];
+  R rb[kRPts][18];
+  R en[kRPts];
+  R coef[kRCells][kCoef];
+  R ih[kRCells][3];
+  R jxw[kRCells];
   int skip[kRCells];
 };
+using ResSmem = ResSmemT<double>;
 
 // linear interpolation of (f0, f1) to the two Gauss points of [0, 1]
 __device__ __forceinline__ void gauss2(double f0, double f1, double &q0, double &q1)
@@ -552,12 +555,19 @@ __device__ __forceinline__ void gauss2(double f0, double f1, double &q0, double 
   q0 = kGb * f0 + kGa * f1;
   q1 = kGa * f0 + kGb * f1;
 }
+template <typename R> __device__ __forceinline__ void gauss2r(R ga, R gb, R f0, R f1, R &q0, R &q1)
+{
+  q0 = gb * f0 + ga * f1;
+  q1 = ga * f0 + gb * f1;
+}
 
+template <typename R>
 __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__restrict__ x, double *__restrict__ r_cell,
                                                      double *__restrict__ e_cell, const uint8_t *__restrict__ inst_active)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ResSmem &S = *reinterpret_cast<ResSmem *>(smem_raw);
+  ResSmemT<R> &S = *reinterpret_cast<ResSmemT<R> *>(smem_raw);
+  const R ga = from_d<R>(kGa), gb = from_d<R>(kGb);
   const int tid = threadIdx.x;
   const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kRCells;
   const int ncb = static_cast<int>((m.nc - e0) < kRCells ? (m.nc - e0) : kRCells);
@@ -569,23 +579,23 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
           const int64_t e = e0 + tid;
           const int inst = m.cell_inst[e];
           skip = (inst_active && !inst_active[inst]) ? 1 : 0;
-          for (int k = 0; k < kCoef; ++k) S.coef[tid][k] = m.coef[inst * kCoef + k];
+          for (int k = 0; k < kCoef; ++k) S.coef[tid][k] = from_d<R>(m.coef[inst * kCoef + k]);
           const GeoD g = m.geo_d[e];
-          S.ih[tid][0] = g.x;
-          S.ih[tid][1] = g.y;
-          S.ih[tid][2] = g.z;
-          S.jxw[tid] = 0.125 * g.w;
+          S.ih[tid][0] = from_d<R>(g.x);
+          S.ih[tid][1] = from_d<R>(g.y);
+          S.ih[tid][2] = from_d<R>(g.z);
+          S.jxw[tid] = from_d<R>(0.125 * g.w);
         }
       S.skip[tid] = skip;
     }
   for (int idx = tid; idx < kRCells * 144; idx += kRThreads)
     {
       const int cl = idx / 144, rem = idx - 144 * cl, v = rem / 18, c = rem - 18 * v;
-      double val = 0.0;
+      R val = R(0.f);
       if (cl < ncb)
         {
           const int node = m.cells[(e0 + cl) * 8 + v];
-          val = x[static_cast<int64_t>(node) * 18 + c];
+          val = from_d<R>(x[static_cast<int64_t>(node) * 18 + c]);
         }
       S.xs[cl][v][c] = val;
     }
@@ -594,36 +604,36 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   if (tid < kRCells * 18)
     {
       const int cl = tid / 18, c = tid - 18 * cl;
-      const double *xv = &S.xs[cl][0][c]; // xv[18 * v], v = vx + 2 vy + 4 vz
-      double zq[2][4], zd[4];             // [qz][vy vx], z-difference [vy vx]
+      const R *xv = &S.xs[cl][0][c]; // xv[18 * v], v = vx + 2 vy + 4 vz
+      R zq[2][4], zd[4];             // [qz][vy vx], z-difference [vy vx]
 #pragma unroll
       for (int t = 0; t < 4; ++t)
         {
-          const double f0 = xv[18 * t], f1 = xv[18 * (t + 4)];
-          gauss2(f0, f1, zq[0][t], zq[1][t]);
+          const R f0 = xv[18 * t], f1 = xv[18 * (t + 4)];
+          gauss2r(ga, gb, f0, f1, zq[0][t], zq[1][t]);
           zd[t] = f1 - f0;
         }
-      double yq[2][2][2], ydy[2][2], zdq[2][2]; // [qz][qy][vx], [qz][vx], [qy][vx]
+      R yq[2][2][2], ydy[2][2], zdq[2][2]; // [qz][qy][vx], [qz][vx], [qy][vx]
 #pragma unroll
       for (int vx = 0; vx < 2; ++vx)
         {
 #pragma unroll
           for (int qz = 0; qz < 2; ++qz)
             {
-              gauss2(zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
+              gauss2r(ga, gb, zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
               ydy[qz][vx] = zq[qz][2 + vx] - zq[qz][vx];
             }
-          gauss2(zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
+          gauss2r(ga, gb, zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
         }
-      const double i0 = S.ih[cl][0], i1 = S.ih[cl][1], i2 = S.ih[cl][2];
+      const R i0 = S.ih[cl][0], i1 = S.ih[cl][1], i2 = S.ih[cl][2];
 #pragma unroll
       for (int qz = 0; qz < 2; ++qz)
 #pragma unroll
         for (int qy = 0; qy < 2; ++qy)
           {
-            double v0, v1;
-            gauss2(yq[qz][qy][0], yq[qz][qy][1], v0, v1);
-            const double dx = (yq[qz][qy][1] - yq[qz][qy][0]) * i0;
+            R v0, v1;
+            gauss2r(ga, gb, yq[qz][qy][0], yq[qz][qy][1], v0, v1);
+            const R dx = (yq[qz][qy][1] - yq[qz][qy][0]) * i0;
             const int p0 = cl * 8 + 2 * qy + 4 * qz;
             S.A[p0][c] = v0;
             S.A[p0 + 1][c] = v1;
@@ -633,8 +643,8 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
 #pragma unroll
       for (int qz = 0; qz < 2; ++qz)
         {
-          double d0, d1;
-          gauss2(ydy[qz][0], ydy[qz][1], d0, d1);
+          R d0, d1;
+          gauss2r(ga, gb, ydy[qz][0], ydy[qz][1], d0, d1);
 #pragma unroll
           for (int qy = 0; qy < 2; ++qy)
             {
@@ -646,8 +656,8 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
 #pragma unroll
       for (int qy = 0; qy < 2; ++qy)
         {
-          double d0, d1;
-          gauss2(zdq[qy][0], zdq[qy][1], d0, d1);
+          R d0, d1;
+          gauss2r(ga, gb, zdq[qy][0], zdq[qy][1], d0, d1);
 #pragma unroll
           for (int qz = 0; qz < 2; ++qz)
             {
@@ -661,15 +671,15 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   // P = A A^T and Q = A A^+: thread (point, row i)
   {
     const int pq = tid / 3, i = tid - 3 * pq;
-    const double *A = S.A[pq];
+    const R *A = S.A[pq];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       {
-        cx<double> pp = {0.0, 0.0}, qq = {0.0, 0.0};
+        cx<R> pp = {R(0.f), R(0.f)}, qq = {R(0.f), R(0.f)};
 #pragma unroll
         for (int k = 0; k < 3; ++k)
           {
-            const cx<double> aik = at(A, i, k), ajk = at(A, j, k);
+            const cx<R> aik = at(A, i, k), ajk = at(A, j, k);
             pp = cadd(pp, cmul(aik, ajk));
             qq = cadd(qq, cmul(aik, cconj(ajk)));
           }
@@ -683,27 +693,27 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   // rho, row i: thread (point, row i)
   {
     const int pq = tid / 3, i = tid - 3 * pq, cl = pq >> 3;
-    const double *A = S.A[pq], *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
-    const cx<double> p = {P[0] + P[4] + P[8], P[9] + P[13] + P[17]};
-    const double q = Q[0] + Q[4] + Q[8];
-    const double s0 = cf[2] + 2.0 * cf[4] * q;
-    cx<double> N[3], M[3];
+    const R *A = S.A[pq], *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
+    const cx<R> p = {P[0] + P[4] + P[8], P[9] + P[13] + P[17]};
+    const R q = Q[0] + Q[4] + Q[8];
+    const R s0 = cf[2] + R(2.f) * cf[4] * q;
+    cx<R> N[3], M[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
       {
-        const cx<double> pik = at(P, i, k), qik = at(Q, i, k);
-        N[k] = cscale(pik, 2.0 * cf[5]);
-        if (k == i) N[k] = cadd(N[k], cscale(p, 2.0 * cf[3]));
-        M[k] = {2.0 * (cf[6] + cf[7]) * qik.r, 2.0 * (cf[6] - cf[7]) * qik.i};
+        const cx<R> pik = at(P, i, k), qik = at(Q, i, k);
+        N[k] = cscale(pik, R(2.f) * cf[5]);
+        if (k == i) N[k] = cadd(N[k], cscale(p, R(2.f) * cf[3]));
+        M[k] = {R(2.f) * (cf[6] + cf[7]) * qik.r, R(2.f) * (cf[6] - cf[7]) * qik.i};
       }
 #pragma unroll
     for (int l = 0; l < 3; ++l)
       {
-        cx<double> r = cscale(at(A, i, l), s0);
+        cx<R> r = cscale(at(A, i, l), s0);
 #pragma unroll
         for (int k = 0; k < 3; ++k)
           {
-            const cx<double> akl = at(A, k, l);
+            const cx<R> akl = at(A, k, l);
             r = cadd(r, cmul(N[k], cconj(akl)));
             r = cadd(r, cmul(M[k], akl));
           }
@@ -717,123 +727,123 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
     {
       const int cl = tid / 18, c = tid - 18 * cl;
       const int part = c / 9, mu = (c % 9) / 3, jc = c % 3;
-      const double K1 = S.coef[cl][0], K23 = S.coef[cl][1];
-      const double ih[3] = {S.ih[cl][0], S.ih[cl][1], S.ih[cl][2]};
+      const R K1 = S.coef[cl][0], K23 = S.coef[cl][1];
+      const R ih[3] = {S.ih[cl][0], S.ih[cl][1], S.ih[cl][2]};
       // w = rho, F_k = K1 ih_k dA/dx_k + [k == jc] K23 ih_jc div, at the 8 points
-      double w[8], F[3][8];
+      R w[8], F[3][8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
         {
           const int pq = cl * 8 + q;
           w[q] = S.rb[pq][c];
           const int base = 9 * part + 3 * mu;
-          const double dterm = K23 * (S.gA[pq][0][base] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2]);
+          const R dterm = K23 * (S.gA[pq][0][base] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2]);
 #pragma unroll
-          for (int k = 0; k < 3; ++k) F[k][q] = ih[k] * (K1 * S.gA[pq][k][c] + (k == jc ? dterm : 0.0));
+          for (int k = 0; k < 3; ++k) F[k][q] = ih[k] * (K1 * S.gA[pq][k][c] + (k == jc ? dterm : R(0.f)));
         }
       // r[a] = sum_q val_q(a) w[q] + sum_k sum_q dval_q(a)/dxi_k F_k[q], a = ax + 2 ay + 4 az
-      double r[8];
+      R r[8];
       {
         // value part: transpose of the interpolation, axis by axis (x, then y, then z)
-        double tx[2][4]; // [ax][qy + 2 qz]
+        R tx[2][4]; // [ax][qy + 2 qz]
 #pragma unroll
         for (int t = 0; t < 4; ++t)
           {
-            tx[0][t] = kGb * w[2 * t] + kGa * w[2 * t + 1];
-            tx[1][t] = kGa * w[2 * t] + kGb * w[2 * t + 1];
+            tx[0][t] = gb * w[2 * t] + ga * w[2 * t + 1];
+            tx[1][t] = ga * w[2 * t] + gb * w[2 * t + 1];
           }
-        double ty[2][2][2]; // [ax][ay][qz]
+        R ty[2][2][2]; // [ax][ay][qz]
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
           for (int qz = 0; qz < 2; ++qz)
             {
-              ty[ax][0][qz] = kGb * tx[ax][2 * qz] + kGa * tx[ax][2 * qz + 1];
-              ty[ax][1][qz] = kGa * tx[ax][2 * qz] + kGb * tx[ax][2 * qz + 1];
+              ty[ax][0][qz] = gb * tx[ax][2 * qz] + ga * tx[ax][2 * qz + 1];
+              ty[ax][1][qz] = ga * tx[ax][2 * qz] + gb * tx[ax][2 * qz + 1];
             }
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
           for (int ay = 0; ay < 2; ++ay)
             {
-              r[ax + 2 * ay] = kGb * ty[ax][ay][0] + kGa * ty[ax][ay][1];
-              r[ax + 2 * ay + 4] = kGa * ty[ax][ay][0] + kGb * ty[ax][ay][1];
+              r[ax + 2 * ay] = gb * ty[ax][ay][0] + ga * ty[ax][ay][1];
+              r[ax + 2 * ay + 4] = ga * ty[ax][ay][0] + gb * ty[ax][ay][1];
             }
       }
       {
         // x gradient: dval/dxi_x = (2 ax - 1) L(qy, ay) L(qz, az): sum over qx first
-        double sx[4]; // [qy + 2 qz]
+        R sx[4]; // [qy + 2 qz]
 #pragma unroll
         for (int t = 0; t < 4; ++t) sx[t] = F[0][2 * t] + F[0][2 * t + 1];
-        double uy[2][2]; // [ay][qz]
+        R uy[2][2]; // [ay][qz]
 #pragma unroll
         for (int qz = 0; qz < 2; ++qz)
           {
-            uy[0][qz] = kGb * sx[2 * qz] + kGa * sx[2 * qz + 1];
-            uy[1][qz] = kGa * sx[2 * qz] + kGb * sx[2 * qz + 1];
+            uy[0][qz] = gb * sx[2 * qz] + ga * sx[2 * qz + 1];
+            uy[1][qz] = ga * sx[2 * qz] + gb * sx[2 * qz + 1];
           }
 #pragma unroll
         for (int ay = 0; ay < 2; ++ay)
 #pragma unroll
           for (int az = 0; az < 2; ++az)
             {
-              const double v = az ? kGa * uy[ay][0] + kGb * uy[ay][1] : kGb * uy[ay][0] + kGa * uy[ay][1];
+              const R v = az ? ga * uy[ay][0] + gb * uy[ay][1] : gb * uy[ay][0] + ga * uy[ay][1];
               r[1 + 2 * ay + 4 * az] += v;
               r[2 * ay + 4 * az] -= v;
             }
       }
       {
         // y gradient: sum over qy first
-        double sy[4]; // [qx + 2 qz]
+        R sy[4]; // [qx + 2 qz]
 #pragma unroll
         for (int qz = 0; qz < 2; ++qz)
 #pragma unroll
           for (int qx = 0; qx < 2; ++qx) sy[qx + 2 * qz] = F[1][qx + 4 * qz] + F[1][qx + 2 + 4 * qz];
-        double ux[2][2]; // [ax][qz]
+        R ux[2][2]; // [ax][qz]
 #pragma unroll
         for (int qz = 0; qz < 2; ++qz)
           {
-            ux[0][qz] = kGb * sy[2 * qz] + kGa * sy[2 * qz + 1];
-            ux[1][qz] = kGa * sy[2 * qz] + kGb * sy[2 * qz + 1];
+            ux[0][qz] = gb * sy[2 * qz] + ga * sy[2 * qz + 1];
+            ux[1][qz] = ga * sy[2 * qz] + gb * sy[2 * qz + 1];
           }
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
           for (int az = 0; az < 2; ++az)
             {
-              const double v = az ? kGa * ux[ax][0] + kGb * ux[ax][1] : kGb * ux[ax][0] + kGa * ux[ax][1];
+              const R v = az ? ga * ux[ax][0] + gb * ux[ax][1] : gb * ux[ax][0] + ga * ux[ax][1];
               r[ax + 2 + 4 * az] += v;
               r[ax + 4 * az] -= v;
             }
       }
       {
         // z gradient: sum over qz first
-        double sz[4]; // [qx + 2 qy]
+        R sz[4]; // [qx + 2 qy]
 #pragma unroll
         for (int t = 0; t < 4; ++t) sz[t] = F[2][t] + F[2][t + 4];
-        double ux[2][2]; // [ax][qy]
+        R ux[2][2]; // [ax][qy]
 #pragma unroll
         for (int qy = 0; qy < 2; ++qy)
           {
-            ux[0][qy] = kGb * sz[2 * qy] + kGa * sz[2 * qy + 1];
-            ux[1][qy] = kGa * sz[2 * qy] + kGb * sz[2 * qy + 1];
+            ux[0][qy] = gb * sz[2 * qy] + ga * sz[2 * qy + 1];
+            ux[1][qy] = ga * sz[2 * qy] + gb * sz[2 * qy + 1];
           }
 #pragma unroll
         for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
           for (int ay = 0; ay < 2; ++ay)
             {
-              const double v = ay ? kGa * ux[ax][0] + kGb * ux[ax][1] : kGb * ux[ax][0] + kGa * ux[ax][1];
+              const R v = ay ? ga * ux[ax][0] + gb * ux[ax][1] : gb * ux[ax][0] + ga * ux[ax][1];
               r[ax + 2 * ay + 4] += v;
               r[ax + 2 * ay] -= v;
             }
       }
       if (cl < ncb && !S.skip[cl])
         {
-          const double jxw = S.jxw[cl];
+          const R jxw = S.jxw[cl];
           double *out = r_cell + (e0 + cl) * 144 + c;
 #pragma unroll
-          for (int a = 0; a < 8; ++a) out[18 * a] = r[a] * jxw;
+          for (int a = 0; a < 8; ++a) out[18 * a] = to_d(r[a] * jxw);
         }
     }
   if (!e_cell) return;
@@ -841,9 +851,9 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   if (tid < kRPts)
     {
       const int pq = tid, cl = pq >> 3;
-      const double *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
-      const double pr = P[0] + P[4] + P[8], pi = P[9] + P[13] + P[17], q = Q[0] + Q[4] + Q[8];
-      double i3 = 0, i4 = 0, i5 = 0;
+      const R *P = S.P[pq], *Q = S.Q[pq], *cf = S.coef[cl];
+      const R pr = P[0] + P[4] + P[8], pi = P[9] + P[13] + P[17], q = Q[0] + Q[4] + Q[8];
+      R i3 = R(0.f), i4 = R(0.f), i5 = R(0.f);
 #pragma unroll
       for (int t = 0; t < 9; ++t)
         {
@@ -851,18 +861,18 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
           i4 += Q[t] * Q[t] + Q[9 + t] * Q[9 + t];
           i5 += Q[t] * Q[t] - Q[9 + t] * Q[9 + t];
         }
-      double e = cf[2] * q + cf[3] * (pr * pr + pi * pi) + cf[4] * q * q + cf[5] * i3 + cf[6] * i4 + cf[7] * i5;
-      double eg = 0;
+      R e = cf[2] * q + cf[3] * (pr * pr + pi * pi) + cf[4] * q * q + cf[5] * i3 + cf[6] * i4 + cf[7] * i5;
+      R eg = R(0.f);
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int c = 0; c < 18; ++c) eg += S.gA[pq][k][c] * S.gA[pq][k][c];
-      double ed = 0;
+      R ed = R(0.f);
 #pragma unroll
       for (int pm = 0; pm < 6; ++pm)
         {
           const int base = 9 * (pm / 3) + 3 * (pm % 3);
-          const double dv = S.gA[pq][0][base] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2];
+          const R dv = S.gA[pq][0][base] + S.gA[pq][1][base + 1] + S.gA[pq][2][base + 2];
           ed += dv * dv;
         }
       S.en[pq] = e + cf[0] * eg + cf[1] * ed;
@@ -870,10 +880,10 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   __syncthreads();
   if (tid < ncb && !S.skip[tid])
     {
-      double e = 0;
+      R e = R(0.f);
 #pragma unroll
       for (int q = 0; q < 8; ++q) e += S.en[tid * 8 + q];
-      e_cell[e0 + tid] = e * S.jxw[tid];
+      e_cell[e0 + tid] = to_d(e * S.jxw[tid]);
     }
 }
 
@@ -1316,31 +1326,37 @@ static cudaError_t launch_cell_t(const DevMesh &m, const double *x, T *H, double
   return cudaGetLastError();
 }
 
+template <typename R>
+static cudaError_t launch_res3d(const DevMesh &m, const double *x, double *r_cell, double *e_cell, const uint8_t *act,
+                                cudaStream_t s)
+{
+  static bool attr = false;
+  if (!attr)
+    {
+      cudaError_t e = cudaFuncSetAttribute(k_res3d<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(sizeof(ResSmemT<R>)));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+  const int64_t grid = (m.nc + kRCells - 1) / kRCells;
+  k_res3d<R><<<static_cast<unsigned>(grid), kRThreads, sizeof(ResSmemT<R>), s>>>(m, x, r_cell, e_cell, act);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cell(const DevMesh &m, bool fp32, const double *x, void *H, double *r_cell, double *e_cell,
                         const uint8_t *act, cudaStream_t s)
 {
   const bool wh = H != nullptr, wr = r_cell != nullptr;
   if (fp32)
     {
-      if (wr) return cudaErrorInvalidValue; // the residual is always FP64
+      // the mixed mode's residual (and energy): double-float arithmetic on the FP32 pipe
+      if (wr && !wh && m.dim == 3 && m.B == 18) return launch_res3d<DF>(m, x, r_cell, e_cell, act, s);
+      if (wr) return cudaErrorInvalidValue;
       return launch_cell_t<float, true, false>(m, x, static_cast<float *>(H), nullptr, nullptr, act, s);
     }
   if (wh && wr) return launch_cell_t<double, true, true>(m, x, static_cast<double *>(H), r_cell, e_cell, act, s);
   if (wh) return launch_cell_t<double, true, false>(m, x, static_cast<double *>(H), nullptr, nullptr, act, s);
-  if (m.dim == 3)
-    {
-      static bool attr = false;
-      if (!attr)
-        {
-          cudaError_t e = cudaFuncSetAttribute(k_res3d, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               static_cast<int>(sizeof(ResSmem)));
-          if (e != cudaSuccess) return e;
-          attr = true;
-        }
-      const int64_t grid = (m.nc + kRCells - 1) / kRCells;
-      k_res3d<<<static_cast<unsigned>(grid), kRThreads, sizeof(ResSmem), s>>>(m, x, r_cell, e_cell, act);
-      return cudaGetLastError();
-    }
+  if (m.dim == 3) return launch_res3d<double>(m, x, r_cell, e_cell, act, s);
   return launch_cell_t<double, false, true>(m, x, nullptr, r_cell, e_cell, act, s);
 }
 
