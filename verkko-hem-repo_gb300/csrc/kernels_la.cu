@@ -626,17 +626,27 @@ cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t 
   return cudaGetLastError();
 }
 
-// one warp per (instance, vector): lanes take segments lane, lane + 32, ... in a fixed
-// order, then a fixed shuffle tree: deterministic
+// one warp per (instance, vector): lanes take segments lane, lane + 32, ... into four
+// interleaved sums (four loads in flight) in a fixed order, then a fixed shuffle tree:
+// deterministic
 __global__ void k_seg_finalize(DevMesh m, const double *__restrict__ partial, int nvec, double *__restrict__ out,
                                int ld_out, int take_sqrt)
 {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= m.n_inst * nvec) return;
   const int inst = w / nvec, v = w % nvec;
-  double s = 0.0;
-  for (int g = m.inst_seg_off[inst] + lane; g < m.inst_seg_off[inst + 1]; g += 32)
-    s += partial[static_cast<int64_t>(g) * nvec + v];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const int g1 = m.inst_seg_off[inst + 1];
+  int g = m.inst_seg_off[inst] + lane;
+  for (; g + 96 < g1; g += 128)
+    {
+      s0 += partial[static_cast<int64_t>(g) * nvec + v];
+      s1 += partial[static_cast<int64_t>(g + 32) * nvec + v];
+      s2 += partial[static_cast<int64_t>(g + 64) * nvec + v];
+      s3 += partial[static_cast<int64_t>(g + 96) * nvec + v];
+    }
+  for (; g < g1; g += 32) s0 += partial[static_cast<int64_t>(g) * nvec + v];
+  double s = (s0 + s1) + (s2 + s3);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   if (lane == 0) out[inst * ld_out + v] = take_sqrt ? sqrt(s) : s;
@@ -1026,8 +1036,19 @@ __device__ __forceinline__ void instance_sums(const DevMesh &m, int inst, const 
   const int g0 = m.inst_seg_off[inst], g1 = m.inst_seg_off[inst + 1];
   for (int v = warp; v < nv; v += kSegThreads / 32)
     {
-      double s = 0.0;
-      for (int g = g0 + lane; g < g1; g += 32) s += __ldcg(partial + static_cast<int64_t>(g) * nv + v);
+      // four independent partial sums per lane keep four loads in flight; the order of the
+      // additions is fixed, so the result is deterministic
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      int g = g0 + lane;
+      for (; g + 96 < g1; g += 128)
+        {
+          s0 += __ldcg(partial + static_cast<int64_t>(g) * nv + v);
+          s1 += __ldcg(partial + static_cast<int64_t>(g + 32) * nv + v);
+          s2 += __ldcg(partial + static_cast<int64_t>(g + 64) * nv + v);
+          s3 += __ldcg(partial + static_cast<int64_t>(g + 96) * nv + v);
+        }
+      for (; g < g1; g += 32) s0 += __ldcg(partial + static_cast<int64_t>(g) * nv + v);
+      double s = (s0 + s1) + (s2 + s3);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (lane == 0) out[v] = take_sqrt ? sqrt(s) : s;
