@@ -33,13 +33,10 @@ sys.path.insert(0, ROOT)
 
 P_BAR, T_RED, HALF, NCELL, NOISE, SEED = 20.0, 0.6, 10.0, 32, 0.05, 2
 TOL = 1e-10
-# DRAM bytes (read + write) of one k_spmv18<float> launch on this workload, from the ncu
-# capture summarised in profiles/k_spmv18_fp32_cube32.md (1.193182 GB + 5.481728 MB)
-SPMV_NCU_TRAFFIC = 1.193182e9 + 5.481728e6
 # DRAM bytes of one matrix-free apply (k_mf_cell + k_mf_gather) on this workload, from the ncu
 # capture summarised in profiles/matrix_free_apply_cube32.md (cold caches: the cell results the
 # gather reads come from DRAM there, from L2 in the live solve)
-MF_NCU_TRAFFIC = 7.213824e6 + 0.0 + 2.2760960e7
+MF_NCU_TRAFFIC = 7.246080e6 + 0.0 + 2.2761472e7
 # FP32 operations of one matrix-free apply per cell: the closed-form Hessian-vector product at
 # 8 points (3456 per point: alpha f, dG_1..dG_5 with their complex 3x3 products) plus the
 # interpolation of state and direction, the gradient terms and the transposed contraction
