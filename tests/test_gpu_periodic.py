@@ -189,7 +189,9 @@ def test_periodic_multigrid_galerkin(gl, precision):
         dmask = dmask.ravel()
         free = ~dmask
         scale = np.abs(want[np.ix_(free, free)]).max()
-        tol = 1e-13 if precision == 0 else 2e-6
+        # mixed mode stores the large coarse levels in FP16 (unit roundoff 4.9e-4), the others in FP32
+        half = precision == 1 and nc >= 2000
+        tol = 1e-13 if precision == 0 else (1e-3 if half else 2e-6)
         assert np.abs(got[np.ix_(free, free)] - want[np.ix_(free, free)]).max() <= tol * scale
         assert np.array_equal(got[dmask], np.eye(got.shape[0])[dmask])
         assert not got[np.ix_(free, dmask)].any()

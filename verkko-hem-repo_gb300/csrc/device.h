@@ -56,6 +56,9 @@ struct DevMesh
   // (zero for instances without uniform cells, whose rows are never regular)
   const double *reg_tmpl_d;
   const float *reg_tmpl_f;
+  // the block values are stored in FP16 (coarse multigrid levels of a mixed context); the
+  // kernels that read them widen to FP32
+  int half_vals;
   // Robin (AdGR) faces: per cell the bits f = 2 axis + side of its pair-breaking faces
   // (nullptr when no instance has an active Robin term) and the cells with any
   const uint8_t *robin;
@@ -226,10 +229,11 @@ cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, 
 // [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and
 // columns and the constrained nodes (hptr_c) of the coarse level become identity rows /
 // zero columns.
+// half_in / half_out: the fine / coarse blocks are stored in FP16 (mixed mode, summed in FP32).
 cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
                             const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
                             const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
-                            const uint8_t *act, cudaStream_t s);
+                            const uint8_t *act, cudaStream_t s, bool half_in = false, bool half_out = false);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

@@ -19,6 +19,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda_fp16.h>
+
 #include "device.h"
 #include "glgpu.h"
 #include "glgpu_internal.h"
@@ -831,7 +833,8 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
       const glgpu_ctx::Transfer &t = c->tr[l];
       CKS(launch(c, KK_PREC, 1, [&] {
         return launch_galerkin(c->mixed, L->nnzb, t.g_row, L->dm.cols, L->dm.mask, L->dm.hptr, L->vals, t.g_toff,
-                               t.g_blk, t.g_w, F->vals, L->dm.node_inst, act, c->st);
+                               t.g_blk, t.g_w, F->vals, L->dm.node_inst, act, c->st, F->dm.half_vals != 0,
+                               L->dm.half_vals != 0);
       }));
       CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st, true); }));
       L->has_J = true;
@@ -949,6 +952,11 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       L->st = c->st;
       L->owns_stream = false;
       L->mf = false; // coarse operators exist only assembled (Galerkin products)
+      // in mixed mode the large coarse operators are stored in FP16: they serve only the
+      // preconditioner of the flexible GMRES, and are swept twice per V-cycle at full bandwidth.
+      // Small levels (latency-bound, and with the largest cells, whose mass-like entries grow
+      // with the cell volume toward FP16's 65504) stay FP32.
+      L->dm.half_vals = (c->mixed && L->nn >= 2000) ? 1 : 0;
       c->lv.push_back(L);
     }
   // transfer operators between level l (fine side) and l+1, and the Galerkin slot tables
@@ -1860,7 +1868,14 @@ extern "C" glgpu_status glgpu_get_system(const glgpu_ctx *cc, int32_t *rowptr, i
   const size_t nv = static_cast<size_t>(c->nnzb) * c->B * c->B;
   if (vals)
     {
-      if (c->mixed)
+      if (c->mixed && c->dm.half_vals)
+        {
+          std::vector<__half> tmp(nv);
+          CK(cudaMemcpyAsync(tmp.data(), c->vals, sizeof(__half) * nv, cudaMemcpyDeviceToHost, c->st));
+          CK(cudaStreamSynchronize(c->st));
+          for (size_t i = 0; i < nv; ++i) vals[i] = static_cast<double>(__half2float(tmp[i]));
+        }
+      else if (c->mixed)
         {
           std::vector<float> tmp(nv);
           CK(cudaMemcpyAsync(tmp.data(), c->vals, sizeof(float) * nv, cudaMemcpyDeviceToHost, c->st));

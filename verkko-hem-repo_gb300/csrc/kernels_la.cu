@@ -11,6 +11,8 @@
 #include <type_traits>
 #include <cuda_runtime.h>
 
+#include <cuda_fp16.h>
+
 #include "device.h"
 
 namespace glgpu
@@ -26,12 +28,28 @@ template <> struct Vec16<double>
   using type = double2;
   static constexpr int n = 2;
 };
+// FP16 storage (the coarse multigrid matrices in mixed mode): four halves per 8-byte load, so
+// a 324-entry block is 81 chunks like the FP32 float4 chunks (648-byte blocks are 8-byte aligned)
+template <> struct Vec16<__half>
+{
+  using type = uint2;
+  static constexpr int n = 4;
+};
 template <typename V, typename T> __device__ __forceinline__ T vget(const V &v, int k);
 template <> __device__ __forceinline__ float vget<float4, float>(const float4 &v, int k)
 {
   return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
 template <> __device__ __forceinline__ double vget<double2, double>(const double2 &v, int k) { return k == 0 ? v.x : v.y; }
+template <> __device__ __forceinline__ float vget<uint2, float>(const uint2 &v, int k)
+{
+  const unsigned w = (k < 2) ? v.x : v.y;
+  const unsigned short b = static_cast<unsigned short>((k & 1) ? (w >> 16) : (w & 0xffffu));
+  return __half2float(__ushort_as_half(b));
+}
+// scalar read of a stored matrix entry as T
+template <typename T> __device__ __forceinline__ T mval(const T *p) { return *p; }
+__device__ __forceinline__ float mval(const __half *p) { return __half2float(*p); }
 
 // ---------------------------------------------------------------------------------
 // SpMV, 18x18 blocks: one warp per block row.  Each block (324 scalars, 16-byte
@@ -48,13 +66,13 @@ constexpr int kSpmvWarps = 8;
 // loop is unrolled, so the loads of several blocks are in flight together.  With WPR > 1
 // warps per row (small coarse levels, where one warp per 27-block row would leave the
 // GPU latency-bound) warp kw of the row takes every WPR-th block.
-template <typename T, int WPR>
-__device__ __forceinline__ void row_products(const DevMesh &m, const T *__restrict__ vals, const T *__restrict__ x,
+template <typename T, typename MT, int WPR>
+__device__ __forceinline__ void row_products(const DevMesh &m, const MT *__restrict__ vals, const T *__restrict__ x,
                                              int64_t n, int lane, int kw,
-                                             T (&acc)[(324 / Vec16<T>::n + 31) / 32][Vec16<T>::n])
+                                             T (&acc)[(324 / Vec16<MT>::n + 31) / 32][Vec16<MT>::n])
 {
-  using V = typename Vec16<T>::type;
-  constexpr int NV = Vec16<T>::n;
+  using V = typename Vec16<MT>::type;
+  constexpr int NV = Vec16<MT>::n;
   constexpr int NCH = 324 / NV;
   constexpr int NIT = (NCH + 31) / 32;
 #pragma unroll
@@ -101,11 +119,11 @@ __device__ __forceinline__ T row_sum(const T (*red)[324], int w0, int lane)
 }
 
 // spill a warp's products into its red row
-template <typename T>
-__device__ __forceinline__ void store_products(T *red_w, const T (&acc)[(324 / Vec16<T>::n + 31) / 32][Vec16<T>::n],
+template <typename T, typename MT = T>
+__device__ __forceinline__ void store_products(T *red_w, const T (&acc)[(324 / Vec16<MT>::n + 31) / 32][Vec16<MT>::n],
                                                int lane)
 {
-  constexpr int NV = Vec16<T>::n;
+  constexpr int NV = Vec16<MT>::n;
   constexpr int NCH = 324 / NV;
   constexpr int NIT = (NCH + 31) / 32;
 #pragma unroll
@@ -119,13 +137,12 @@ __device__ __forceinline__ void store_products(T *red_w, const T (&acc)[(324 / V
 }
 
 // y = A x (RES: y = b - A x); kSpmvWarps / WPR rows per CTA
-template <typename T, bool RES, int WPR>
-__global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *__restrict__ vals,
+template <typename T, typename MT, bool RES, int WPR>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const MT *__restrict__ vals,
                                                             const T *__restrict__ x, T *__restrict__ y,
                                                             const uint8_t *__restrict__ act, const T *__restrict__ b)
 {
-  using V = typename Vec16<T>::type;
-  constexpr int NV = Vec16<T>::n;
+  constexpr int NV = Vec16<MT>::n;
   constexpr int NIT = (324 / NV + 31) / 32;
   __shared__ T red[kSpmvWarps][324];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -138,8 +155,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *
   if (on)
     {
       T acc[NIT][NV];
-      row_products<T, WPR>(m, vals, x, n, lane, kw, acc);
-      store_products<T>(red[warp], acc, lane);
+      row_products<T, MT, WPR>(m, vals, x, n, lane, kw, acc);
+      store_products<T, MT>(red[warp], acc, lane);
     }
   if (WPR > 1)
     __syncthreads();
@@ -156,8 +173,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const T *
 // sweep from zero, y = omega D^-1 b).  The row's SpMV as in k_spmv18 (WPR warps per row),
 // then the 18x18 inverse block applied by the row's first warp with the same lane map.
 // y must not alias z (neighbouring rows read z).
-template <typename T, int WPR>
-__global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T *__restrict__ vals,
+template <typename T, typename MT, int WPR>
+__global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const MT *__restrict__ vals,
                                                               const T *__restrict__ dinv, const T *__restrict__ b,
                                                               const T *__restrict__ z, T *__restrict__ y, T omega,
                                                               const uint8_t *__restrict__ act)
@@ -166,6 +183,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T
   constexpr int NV = Vec16<T>::n;
   constexpr int NCH = 324 / NV;
   constexpr int NIT = (NCH + 31) / 32;
+  constexpr int MNV = Vec16<MT>::n;
+  constexpr int MNIT = (324 / MNV + 31) / 32;
   __shared__ T red[kSpmvWarps][324];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kw = warp % WPR, w0 = warp - kw;
@@ -177,9 +196,9 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const T
     {
       if (on)
         {
-          T acc[NIT][NV];
-          row_products<T, WPR>(m, vals, z, n, lane, kw, acc);
-          store_products<T>(red[warp], acc, lane);
+          T acc[MNIT][MNV];
+          row_products<T, MT, WPR>(m, vals, z, n, lane, kw, acc);
+          store_products<T, MT>(red[warp], acc, lane);
         }
       if (WPR > 1)
         __syncthreads();
@@ -242,28 +261,29 @@ __global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restri
 constexpr int64_t kSmallRows = 20000;
 constexpr int64_t kTinyRows = 2000;
 
-template <typename T, bool RES, int WPR>
+template <typename T, typename MT, bool RES, int WPR>
 static void spmv18_t(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act, const void *b,
                      cudaStream_t s)
 {
   constexpr int rows = kSpmvWarps / WPR;
   const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
-  k_spmv18<T, RES, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const T *>(vals), static_cast<const T *>(x),
-                                                          static_cast<T *>(y), act, static_cast<const T *>(b));
+  k_spmv18<T, MT, RES, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const MT *>(vals),
+                                                              static_cast<const T *>(x), static_cast<T *>(y), act,
+                                                              static_cast<const T *>(b));
 }
 
-template <typename T>
+template <typename T, typename MT>
 static void spmv18_dispatch(const DevMesh &m, const void *vals, const void *x, void *y, const uint8_t *act,
                             const void *b, cudaStream_t s)
 {
   if (b)
-    m.nn < kTinyRows    ? spmv18_t<T, true, 8>(m, vals, x, y, act, b, s)
-    : m.nn < kSmallRows ? spmv18_t<T, true, 4>(m, vals, x, y, act, b, s)
-                        : spmv18_t<T, true, 1>(m, vals, x, y, act, b, s);
+    m.nn < kTinyRows    ? spmv18_t<T, MT, true, 8>(m, vals, x, y, act, b, s)
+    : m.nn < kSmallRows ? spmv18_t<T, MT, true, 4>(m, vals, x, y, act, b, s)
+                        : spmv18_t<T, MT, true, 1>(m, vals, x, y, act, b, s);
   else
-    m.nn < kTinyRows    ? spmv18_t<T, false, 8>(m, vals, x, y, act, b, s)
-    : m.nn < kSmallRows ? spmv18_t<T, false, 4>(m, vals, x, y, act, b, s)
-                        : spmv18_t<T, false, 1>(m, vals, x, y, act, b, s);
+    m.nn < kTinyRows    ? spmv18_t<T, MT, false, 8>(m, vals, x, y, act, b, s)
+    : m.nn < kSmallRows ? spmv18_t<T, MT, false, 4>(m, vals, x, y, act, b, s)
+                        : spmv18_t<T, MT, false, 1>(m, vals, x, y, act, b, s);
 }
 
 cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const void *x, void *y, const uint8_t *act,
@@ -271,10 +291,12 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
 {
   if (m.B == 18)
     {
-      if (fp32)
-        spmv18_dispatch<float>(m, vals, x, y, act, b, s);
+      if (fp32 && m.half_vals)
+        spmv18_dispatch<float, __half>(m, vals, x, y, act, b, s);
+      else if (fp32)
+        spmv18_dispatch<float, float>(m, vals, x, y, act, b, s);
       else
-        spmv18_dispatch<double>(m, vals, x, y, act, b, s);
+        spmv18_dispatch<double, double>(m, vals, x, y, act, b, s);
     }
   else
     {
@@ -290,29 +312,37 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
   return cudaGetLastError();
 }
 
-template <typename T, int WPR>
+template <typename T, typename MT, int WPR>
 static void smooth18_t(const DevMesh &m, const void *vals, const void *dinv, const void *b, const void *z, void *y,
                        double omega, const uint8_t *act, cudaStream_t s)
 {
   constexpr int rows = kSpmvWarps / WPR;
   const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
-  k_smooth18<T, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const T *>(vals), static_cast<const T *>(dinv),
-                                                       static_cast<const T *>(b), static_cast<const T *>(z),
-                                                       static_cast<T *>(y), static_cast<T>(omega), act);
+  k_smooth18<T, MT, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const MT *>(vals),
+                                                           static_cast<const T *>(dinv), static_cast<const T *>(b),
+                                                           static_cast<const T *>(z), static_cast<T *>(y),
+                                                           static_cast<T>(omega), act);
+}
+
+template <typename T, typename MT>
+static void smooth18_dispatch(const DevMesh &m, const void *vals, const void *dinv, const void *b, const void *z,
+                              void *y, double omega, const uint8_t *act, cudaStream_t s)
+{
+  m.nn < kTinyRows    ? smooth18_t<T, MT, 8>(m, vals, dinv, b, z, y, omega, act, s)
+  : m.nn < kSmallRows ? smooth18_t<T, MT, 4>(m, vals, dinv, b, z, y, omega, act, s)
+                      : smooth18_t<T, MT, 1>(m, vals, dinv, b, z, y, omega, act, s);
 }
 
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,
                           void *y, double omega, const uint8_t *act, cudaStream_t s)
 {
   if (m.B != 18) return cudaErrorInvalidValue;
-  if (fp32)
-    m.nn < kTinyRows    ? smooth18_t<float, 8>(m, vals, dinv, b, z, y, omega, act, s)
-    : m.nn < kSmallRows ? smooth18_t<float, 4>(m, vals, dinv, b, z, y, omega, act, s)
-                        : smooth18_t<float, 1>(m, vals, dinv, b, z, y, omega, act, s);
+  if (fp32 && m.half_vals)
+    smooth18_dispatch<float, __half>(m, vals, dinv, b, z, y, omega, act, s);
+  else if (fp32)
+    smooth18_dispatch<float, float>(m, vals, dinv, b, z, y, omega, act, s);
   else
-    m.nn < kTinyRows    ? smooth18_t<double, 8>(m, vals, dinv, b, z, y, omega, act, s)
-    : m.nn < kSmallRows ? smooth18_t<double, 4>(m, vals, dinv, b, z, y, omega, act, s)
-                        : smooth18_t<double, 1>(m, vals, dinv, b, z, y, omega, act, s);
+    smooth18_dispatch<double, double>(m, vals, dinv, b, z, y, omega, act, s);
   return cudaGetLastError();
 }
 
@@ -323,19 +353,19 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
 // ---------------------------------------------------------------------------------
 constexpr int kBjWarps = 4;
 
-template <typename T>
-__global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T *__restrict__ vals,
+template <typename T, typename MT = T>
+__global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const MT *__restrict__ vals,
                                                               T *__restrict__ dinv, int l1)
 {
   __shared__ T M[kBjWarps][18][37];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kBjWarps + warp;
   if (n >= m.nn) return;
-  const T *D = vals + static_cast<int64_t>(m.diag[n]) * 324;
+  const MT *D = vals + static_cast<int64_t>(m.diag[n]) * 324;
   for (int i = lane; i < 18 * 36; i += 32)
     {
       const int r = i / 36, c = i % 36;
-      M[warp][r][c] = (c < 18) ? D[r * 18 + c] : ((c - 18 == r) ? T(1) : T(0));
+      M[warp][r][c] = (c < 18) ? static_cast<T>(mval(D + r * 18 + c)) : ((c - 18 == r) ? T(1) : T(0));
     }
   __syncwarp();
   if (l1)
@@ -349,9 +379,9 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const T
           for (int32_t b = m.rowptr[n]; b < m.rowptr[n + 1]; ++b)
             {
               if (b == m.diag[n]) continue;
-              const T *row = vals + static_cast<int64_t>(b) * 324 + lane * 18;
+              const MT *row = vals + static_cast<int64_t>(b) * 324 + lane * 18;
 #pragma unroll
-              for (int c = 0; c < 18; ++c) sum += fabs(row[c]);
+              for (int c = 0; c < 18; ++c) sum += fabs(static_cast<T>(mval(row + c)));
             }
           const T d = M[warp][lane][lane];
           M[warp][lane][lane] = d + (d < T(0) ? -sum : sum);
@@ -442,7 +472,10 @@ cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void 
   if (m.B == 18)
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kBjWarps - 1) / kBjWarps);
-      if (fp32)
+      if (fp32 && m.half_vals)
+        k_bj_setup18<float, __half><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const __half *>(vals),
+                                                                   static_cast<float *>(dinv), l1 ? 1 : 0);
+      else if (fp32)
         k_bj_setup18<float><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv),
                                                            l1 ? 1 : 0);
       else

@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <cuda_fp16.h>
+
 #include "device.h"
 
 namespace glgpu
@@ -87,6 +89,10 @@ __global__ void __launch_bounds__(kRsNodes * 18)
   z[n * 18 + c] = omega * u;
 }
 
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(double v) { return static_cast<float>(v); }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+
 // Galerkin product: one warp per coarse block (I, J).  The block is
 //   J_c(I, J) = sum over fine blocks (i, j) with P(i, I) P(j, J) != 0 of P(i, I) P(j, J) J_f(i, j),
 // a weighted sum of whole fine blocks whose (block index, weight) list is built on the
@@ -120,12 +126,38 @@ __device__ __forceinline__ void gfma(double2 &a, double w, const double2 &v)
 __device__ __forceinline__ float &gcomp(float4 &v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
 __device__ __forceinline__ double &gcomp(double2 &v, int k) { return k == 0 ? v.x : v.y; }
 
-template <typename T>
+// chunk ch of a stored block (FP32 / FP64: 16-byte loads; FP16: 8-byte loads of four halves)
+__device__ __forceinline__ float4 gload(const float *blk, int ch) { return __ldg(reinterpret_cast<const float4 *>(blk) + ch); }
+__device__ __forceinline__ double2 gload(const double *blk, int ch)
+{
+  return __ldg(reinterpret_cast<const double2 *>(blk) + ch);
+}
+__device__ __forceinline__ float4 gload(const __half *blk, int ch)
+{
+  const uint2 u = __ldg(reinterpret_cast<const uint2 *>(blk) + ch);
+  const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void gstore(float *blk, int ch, const float4 &v) { reinterpret_cast<float4 *>(blk)[ch] = v; }
+__device__ __forceinline__ void gstore(double *blk, int ch, const double2 &v) { reinterpret_cast<double2 *>(blk)[ch] = v; }
+__device__ __forceinline__ void gstore(__half *blk, int ch, const float4 &v)
+{
+  const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+  uint2 u;
+  u.x = *reinterpret_cast<const unsigned *>(&a);
+  u.y = *reinterpret_cast<const unsigned *>(&b);
+  reinterpret_cast<uint2 *>(blk)[ch] = u;
+}
+
+// T: accumulation type; IN / OUT: storage of the fine and coarse blocks (FP16 on the coarse
+// levels of a mixed context, summed in FP32)
+template <typename T, typename IN, typename OUT>
 __global__ void __launch_bounds__(kGalWarps * 32)
   k_galerkin(int64_t nnzb_c, const int32_t *__restrict__ g_row, const int32_t *__restrict__ cols_c,
-             const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ hptr_c, T *__restrict__ vals_c,
+             const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ hptr_c, OUT *__restrict__ vals_c,
              const int64_t *__restrict__ g_toff, const int32_t *__restrict__ g_blk, const T *__restrict__ g_w,
-             const T *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
+             const IN *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
 {
   using V = typename GVec<T>::type;
   constexpr int NV = GVec<T>::n;
@@ -141,18 +173,17 @@ __global__ void __launch_bounds__(kGalWarps * 32)
   for (int k = 0; k < NIT; ++k)
 #pragma unroll
     for (int q = 0; q < NV; ++q) gcomp(acc[k], q) = T(0);
-  const V *src = reinterpret_cast<const V *>(vals_f);
   const int64_t t1 = g_toff[cb + 1];
 #pragma unroll 2
   for (int64_t t = g_toff[cb]; t < t1; ++t)
     {
-      const V *bp = src + static_cast<int64_t>(__ldg(g_blk + t)) * NCH;
+      const IN *bp = vals_f + static_cast<int64_t>(__ldg(g_blk + t)) * 324;
       const T w = __ldg(g_w + t);
 #pragma unroll
       for (int k = 0; k < NIT; ++k)
         {
           const int ch = lane + 32 * k;
-          if (ch < NCH) gfma(acc[k], w, __ldg(bp + ch));
+          if (ch < NCH) gfma(acc[k], w, gload(bp, ch));
         }
     }
   // zero-Dirichlet components and constrained (periodic image) nodes of the coarse level:
@@ -161,7 +192,7 @@ __global__ void __launch_bounds__(kGalWarps * 32)
   constexpr uint32_t kAll = (1u << 18) - 1u;
   const uint32_t mI = (hptr_c[I + 1] > hptr_c[I]) ? kAll : mask_c[I];
   const uint32_t mJ = (hptr_c[J + 1] > hptr_c[J]) ? kAll : mask_c[J];
-  V *dst = reinterpret_cast<V *>(vals_c) + cb * NCH;
+  OUT *dst = vals_c + cb * 324;
 #pragma unroll
   for (int k = 0; k < NIT; ++k)
     {
@@ -175,7 +206,7 @@ __global__ void __launch_bounds__(kGalWarps * 32)
             const int el = ch * NV + q, a = el / 18, bb = el - 18 * (el / 18);
             if (((mI >> a) & 1u) || ((mJ >> bb) & 1u)) gcomp(o, q) = (J == I && a == bb) ? T(1) : T(0);
           }
-      dst[ch] = o;
+      gstore(dst, ch, o);
     }
 }
 
@@ -234,19 +265,35 @@ cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, 
 cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
                             const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
                             const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
-                            const uint8_t *act, cudaStream_t s)
+                            const uint8_t *act, cudaStream_t s, bool half_in, bool half_out)
 {
   if (nnzb_c == 0) return cudaSuccess;
   const int64_t grid = (nnzb_c + kGalWarps - 1) / kGalWarps;
   if (grid > 0x7fffffff) return cudaErrorInvalidValue;
-  if (fp32)
-    k_galerkin<float><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, static_cast<const float *>(g_w),
+  const unsigned g = static_cast<unsigned>(grid);
+  const float *wf = static_cast<const float *>(g_w);
+  if (fp32 && half_in && half_out)
+    k_galerkin<float, __half, __half><<<g, kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
+      static_cast<const __half *>(vals_f), node_inst_c, act);
+  else if (fp32 && half_out)
+    k_galerkin<float, float, __half><<<g, kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
       static_cast<const float *>(vals_f), node_inst_c, act);
+  else if (fp32 && half_in)
+    k_galerkin<float, __half, float><<<g, kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
+      static_cast<const __half *>(vals_f), node_inst_c, act);
+  else if (fp32)
+    k_galerkin<float, float, float><<<g, kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
+      static_cast<const float *>(vals_f), node_inst_c, act);
+  else if (!fp32 && !half_in && !half_out)
+    k_galerkin<double, double, double><<<g, kGalWarps * 32, 0, s>>>(
+      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<double *>(vals_c), g_toff, g_blk,
+      static_cast<const double *>(g_w), static_cast<const double *>(vals_f), node_inst_c, act);
   else
-    k_galerkin<double><<<static_cast<unsigned>(grid), kGalWarps * 32, 0, s>>>(
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<double *>(vals_c), g_toff, g_blk, static_cast<const double *>(g_w),
-      static_cast<const double *>(vals_f), node_inst_c, act);
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
@@ -305,7 +352,7 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
           else hi = mid - 1;
         }
       const int row = static_cast<int>((lo - n0) * B + cr), col = static_cast<int>((m.cols[blk] - n0) * B + cd);
-      W[row * ld + col] = static_cast<float>(vals[blk * B * B + e]);
+      W[row * ld + col] = to_f(vals[blk * B * B + e]);
     }
   __syncthreads();
   if (tid == 0)
@@ -411,7 +458,15 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
 {
   const size_t sm = static_cast<size_t>(max_nd) * (2 * max_nd + 1) * sizeof(float);
   if (max_nd > kMaxDense || sm > 227 * 1024) return cudaErrorInvalidValue;
-  if (fp32)
+  if (fp32 && m.half_vals)
+    {
+      cudaError_t e = cudaFuncSetAttribute(k_dense_invert<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(sm));
+      if (e != cudaSuccess) return e;
+      k_dense_invert<__half><<<m.n_inst, kGjThreads, sm, s>>>(m, static_cast<const __half *>(vals), dense_off, inv,
+                                                              singular);
+    }
+  else if (fp32)
     {
       cudaError_t e = cudaFuncSetAttribute(k_dense_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(sm));
