@@ -144,8 +144,12 @@ template <int OA, int OB> __device__ __forceinline__ void mm3_acc(const M3 &X, c
 }
 
 // terms of thread group G for the point with state a and direction f: out = the group's
-// share of alpha f + sum_t 2 beta_t dG_t[f]; the three groups carry about the same work:
-// G = 0: alpha f + dG_3;  G = 1: dG_4 + dG_1;  G = 2: dG_5 + dG_2
+// share of alpha f + sum_t 2 beta_t dG_t[f].  dG_4 and dG_5 are evaluated together: with
+// S = F A^+ the matrix of dG_5 is conj(S) (F^* A^T = conj(F A^+)), and both terms multiply A and
+// F from the right, so
+//   w4 dG_4 + w5 dG_5 = [w4 (S + S^+) + w5 (conj(S) + S^T)] A + (w4 Q + w5 Q^*) F.
+// G = 0: alpha f + dG_3;  G = 1: dG_1 and the A-product of dG_4, dG_5;  G = 2: dG_2 and their
+// F-product.
 template <int G>
 __device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[18], const float *cf, float (&out)[18])
 {
@@ -171,6 +175,7 @@ __device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[
     {
 #pragma unroll
       for (int k = 0; k < 18; ++k) out[k] = 0.f;
+      const float w4 = 2.f * cf[4], w5 = 2.f * cf[5];
       if constexpr (G == 1)
         {
           // dG_1 = dp A^* + p F^*, p = tr A A^T, dp = 2 sum A_ij F_ij
@@ -188,6 +193,18 @@ __device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[
 #pragma unroll
             for (int j = 0; j < 3; ++j) X[i][j] = cma(p, cj(F[i][j]), cm(dp, cj(A[i][j])));
           acc_m3(X, 2.f * cf[1], out);
+          // [w4 (S + S^+) + w5 (conj(S) + S^T)] A, S = F A^+
+          mm3<0, 3>(F, A, S);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              {
+                const Cf sij = S[i][j], sji = S[j][i];
+                // S + S^+ = (s_ij + conj s_ji); conj(S) + S^T = (conj s_ij + s_ji)
+                X[i][j] = {(w4 + w5) * (sij.r + sji.r), w4 * (sij.i - sji.i) + w5 * (sji.i - sij.i)};
+              }
+          mm3_acc<0, 0>(X, A, 1.f, out);
         }
       else
         {
@@ -207,23 +224,14 @@ __device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[
             for (int j = 0; j < 3; ++j)
               X[i][j] = {fmaf(dq, A[i][j].r, q * F[i][j].r), fmaf(dq, A[i][j].i, q * F[i][j].i)};
           acc_m3(X, 2.f * cf[2], out);
+          // (w4 Q + w5 Q^*) F, Q = A A^+
+          mm3<0, 3>(A, A, S);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) X[i][j] = {(w4 + w5) * S[i][j].r, (w4 - w5) * S[i][j].i};
+          mm3_acc<0, 0>(X, F, 1.f, out);
         }
-      // dG_4 (G = 1) / dG_5 (G = 2) = (S + S^+) A + Q F (Q^* F), S = F A^+ (F^* A^T), Q = A A^+
-      const float w = 2.f * cf[3 + G];
-      if constexpr (G == 1)
-        mm3<0, 3>(F, A, S);
-      else
-        mm3<2, 1>(F, A, S);
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) X[i][j] = {S[i][j].r + S[j][i].r, S[i][j].i - S[j][i].i};
-      mm3_acc<0, 0>(X, A, w, out);
-      mm3<0, 3>(A, A, S); // Q
-      if constexpr (G == 1)
-        mm3_acc<0, 0>(S, F, w, out);
-      else
-        mm3_acc<2, 0>(S, F, w, out);
     }
 }
 
@@ -570,7 +578,7 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
 constexpr int kMgNodes = 16;
 constexpr int kMgThreads = kMgNodes * 18;
 
-__global__ void __launch_bounds__(kMgThreads) k_mf_gather(DevMesh m, const float *__restrict__ ycell,
+__global__ void __launch_bounds__(kMgThreads, 5) k_mf_gather(DevMesh m, const float *__restrict__ ycell,
                                                           const float *__restrict__ z, const float *__restrict__ b,
                                                           const float *__restrict__ dinv, float *__restrict__ y,
                                                           float omega, int mode, const uint8_t *__restrict__ act)
