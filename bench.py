@@ -36,7 +36,7 @@ TOL = 1e-10
 # DRAM bytes of one matrix-free apply (k_mf_cell + k_mf_gather) on this workload, from the ncu
 # capture summarised in profiles/matrix_free_apply_cube32.md (cold caches: the cell results the
 # gather reads come from DRAM there, from L2 in the live solve)
-MF_NCU_TRAFFIC = 7.246080e6 + 0.0 + 2.2761472e7
+MF_NCU_TRAFFIC = 7.239424e6 + 0.0 + 2.2761216e7
 # FP32 operations of one matrix-free apply per cell: the closed-form Hessian-vector product at
 # 8 points (3456 per point: alpha f, dG_1..dG_5 with their complex 3x3 products) plus the
 # interpolation of state and direction, the gradient terms and the transposed contraction
