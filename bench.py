@@ -38,9 +38,10 @@ TOL = 1e-10
 # gather reads come from DRAM there, from L2 in the live solve)
 MF_NCU_TRAFFIC = 7.239424e6 + 0.0 + 2.2761216e7
 # FP32 operations of one matrix-free apply per cell: the closed-form Hessian-vector product at
-# 8 points (3456 per point: alpha f, dG_1..dG_5 with their complex 3x3 products) plus the
-# interpolation of state and direction, the gradient terms and the transposed contraction
-MF_FLOP_PER_CELL = 8 * 3456 + 4500
+# 8 points (2592 per point: alpha f and dG_1..dG_3 with their complex 3x3 products, dG_4 and dG_5
+# through their two shared products) plus the interpolation of state and direction, the
+# gradient terms and the transposed contraction
+MF_FLOP_PER_CELL = 8 * 2592 + 4500
 METRIC = "GL solves/s at ||F||<1e-10 (femgl 3D, 32^3 Q1, T=0.6Tc, p=20bar)"
 WORKLOAD = "femgl 3D cube L=20, 32^3 Q1 cells, matep(p=20 bar, t=0.6, SCC), z-face pair breaking, B-phase+0.05N(0,1) seed 2"
 
