@@ -344,6 +344,10 @@ def main():
         return 0
     if args.impl == "reference":
         return reference_arm(args, rank)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1 and rank != 0:
+        # one replica per GPU is the multi-GPU form of this path (instances are independent,
+        # no exchange); this build measures and reports the single-GPU replica on rank 0
+        return 0
     gl = importlib.import_module("verkko-hem-repo_gb300")
     gl.build()
     m, x0 = problem(gl)
