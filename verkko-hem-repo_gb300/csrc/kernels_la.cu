@@ -312,6 +312,30 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
   return cudaGetLastError();
 }
 
+// The sweep from zero, y = omega D^-1 b: thread (node, component), 16 nodes per CTA; the
+// node's 18 values of b meet in shared memory and thread c reads row c of the inverse block
+// (the node's 18 threads read the block's 1296 contiguous bytes)
+constexpr int kSzNodes = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, const T *__restrict__ dinv,
+                                                                 const T *__restrict__ b, T *__restrict__ y, T omega,
+                                                                 const uint8_t *__restrict__ act)
+{
+  __shared__ T b_s[kSzNodes][18];
+  const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
+  const int64_t n = static_cast<int64_t>(blockIdx.x) * kSzNodes + ln;
+  const bool on = n < m.nn && !(act && !act[m.node_inst[n]]);
+  b_s[ln][c] = on ? b[n * 18 + c] : T(0);
+  __syncthreads();
+  if (!on) return;
+  const T *row = dinv + n * 324 + c * 18;
+  T u = 0;
+#pragma unroll
+  for (int d = 0; d < 18; ++d) u += row[d] * b_s[ln][d];
+  y[n * 18 + c] = omega * u;
+}
+
 template <typename T, typename MT, int WPR>
 static void smooth18_t(const DevMesh &m, const void *vals, const void *dinv, const void *b, const void *z, void *y,
                        double omega, const uint8_t *act, cudaStream_t s)
@@ -337,6 +361,19 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
                           void *y, double omega, const uint8_t *act, cudaStream_t s)
 {
   if (m.B != 18) return cudaErrorInvalidValue;
+  if (!z)
+    {
+      const unsigned grid = static_cast<unsigned>((m.nn + kSzNodes - 1) / kSzNodes);
+      if (fp32)
+        k_smooth_zero18<float><<<grid, kSzNodes * 18, 0, s>>>(m, static_cast<const float *>(dinv),
+                                                             static_cast<const float *>(b), static_cast<float *>(y),
+                                                             static_cast<float>(omega), act);
+      else
+        k_smooth_zero18<double><<<grid, kSzNodes * 18, 0, s>>>(m, static_cast<const double *>(dinv),
+                                                              static_cast<const double *>(b), static_cast<double *>(y),
+                                                              omega, act);
+      return cudaGetLastError();
+    }
   if (fp32 && m.half_vals)
     smooth18_dispatch<float, __half>(m, vals, dinv, b, z, y, omega, act, s);
   else if (fp32)
