@@ -131,10 +131,10 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
 // state; 3D, 18 components): the bulk Hessian is applied at each quadrature point from the
 // interpolated state without forming it.
 // mode 0: y = J z, 1: y = b - J z, 2: y = z + omega D^-1 (b - J z) with D^-1 [Nn][324].
-// ycell [Nc][8][18] is scratch; constrained rows act as the identity.  err is unused.
+// ycell [Nc][8][18] is scratch; constrained rows act as the identity.
 cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
                       const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
-                      int *err = nullptr, int cells_per_cta = 8);
+                      int cells_per_cta = 8);
 // One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives
 // y = omega D^-1 b.  18x18 blocks only; y must not alias z.
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,

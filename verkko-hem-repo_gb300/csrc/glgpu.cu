@@ -149,7 +149,6 @@ struct glgpu_ctx
   bool mf = false;                   // the Krylov operator is applied matrix-free from H (FP32, 3D)
   float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
   float *x32 = nullptr;              // FP32 copy of the state the matrix-free operator linearises at
-  int *d_err = nullptr;              // device-side wait timeouts (matrix-free Hessian copies)
   bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
   bool prec_built = false;           // a multigrid hierarchy exists for some earlier Jacobian
   bool bsr_stale = false;            // the block matrix lags the Hessians (matrix-free steps)
@@ -353,7 +352,7 @@ glgpu_status spmv(glgpu_ctx *c, const void *in, void *out, const uint8_t *act)
   if (c->mf)
     return launch(c, KK_SPMV, mf_launches(c), [&] {
       return launch_mf(c->dm, c->x32, static_cast<const float *>(in), c->ycell,
-                       static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->d_err, c->prm[0].mf_cells);
+                       static_cast<float *>(out), nullptr, nullptr, 0.f, 0, act, c->st, c->prm[0].mf_cells);
     });
   return launch(c, KK_SPMV, 1, [&] { return launch_spmv(c->dm, c->mixed, c->vals, in, out, act, c->st); });
 }
@@ -872,7 +871,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
       return launch(L, KK_PREC, mf_launches(L), [&] {
         return launch_mf(L->dm, L->x32, static_cast<const float *>(zin), L->ycell,
                          static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
-                         static_cast<float>(om), 2, act, L->st, L->d_err, L->prm[0].mf_cells);
+                         static_cast<float>(om), 2, act, L->st, L->prm[0].mf_cells);
       });
     return launch(L, KK_PREC, 1, [&] { return launch_smooth(L->dm, m, L->vals, sm, r, zin, zout, om, act, L->st); });
   };
@@ -888,7 +887,7 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   if (L->mf)
     CKS(launch(L, KK_SPMV, mf_launches(L), [&] {
       return launch_mf(L->dm, L->x32, static_cast<const float *>(cur), L->ycell,
-                       static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->d_err, L->prm[0].mf_cells);
+                       static_cast<float *>(t), static_cast<const float *>(r), nullptr, 0.f, 1, act, L->st, L->prm[0].mf_cells);
     }));
   else
     CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
@@ -1350,13 +1349,12 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       (s = talloc(&c->C3, N)))
     return fail(s);
   (void)pv;
-  // mixed 3D contexts apply the Krylov operator matrix-free from the FP32 Hessians
+  // mixed 3D contexts apply the Krylov operator matrix-free at the state
   if (c->mixed && P.dim == 3 && P.B == 18 && P.nv == 8)
     {
-      if ((s = dalloc(c, &c->ycell, static_cast<size_t>(P.nc) * P.nv * P.B)) || (s = dalloc(c, &c->d_err, 1)) ||
+      if ((s = dalloc(c, &c->ycell, static_cast<size_t>(P.nc) * P.nv * P.B)) ||
           (s = dalloc(c, &c->x32, static_cast<size_t>(c->N))))
         return fail(s);
-      if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(set_error(GLGPU_ERR_CUDA, "cudaMemset"));
       c->mf = true;
     }
   if ((s = dalloc(c, &c->partial, static_cast<size_t>(d.n_seg) * (mr + 2))) ||
@@ -1577,19 +1575,7 @@ static glgpu_status solve_impl(glgpu_ctx *c, double tol, std::vector<int> &its, 
   for (int k = 0; k < c->n_inst; ++k) all_on &= c->inst_on[k] != 0;
   if (!all_on) CKS(upload_act(c, c->d_act, c->inst_on));
   CKS(prec_setup(c, all_on ? nullptr : c->d_act));
-  const glgpu_status gs = gmres(c, tol, c->inst_on, its, conv);
-  if (c->d_err)
-    {
-      int h_err = 0;
-      CK(cudaMemcpyAsync(&h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-      CK(cudaStreamSynchronize(c->st));
-      if (h_err)
-        {
-          CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
-          return set_error(GLGPU_ERR_TIMEOUT, "solve: a device wait for the matrix-free operator's data timed out");
-        }
-    }
-  CKS(gs);
+  CKS(gmres(c, tol, c->inst_on, its, conv));
   c->has_delta = true;
   return GLGPU_OK;
 }

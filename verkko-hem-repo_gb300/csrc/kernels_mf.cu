@@ -335,7 +335,7 @@ __device__ __forceinline__ void mf_contract(const float (&w)[8], const float (&F
 template <int NC>
 __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
                                                      const float *__restrict__ z, float *__restrict__ ycell,
-                                                     const uint8_t *__restrict__ act, int *__restrict__ err)
+                                                     const uint8_t *__restrict__ act)
 {
   constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 24 * NC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -566,7 +566,6 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
         }
     }
   (void)act;
-  (void)err;
 }
 
 // Node gather: thread (node, component), 16 nodes per CTA.  s = sum of the row's cell
@@ -690,7 +689,7 @@ cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, cons
 
 template <int NC>
 static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float *z, float *ycell, const uint8_t *act,
-                                  int *err, cudaStream_t s)
+                                  cudaStream_t s)
 {
   static bool attr = false;
   if (!attr)
@@ -701,20 +700,20 @@ static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float
       attr = true;
     }
   const int64_t gc = (m.nc + NC - 1) / NC;
-  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act, err);
+  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
-                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s, int *err,
+                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
                       int cells_per_cta)
 {
   if (m.dim != 3 || m.B != 18 || m.nv != 8) return cudaErrorInvalidValue;
   if (mode == 2 && !dinv) return cudaErrorInvalidValue;
   if (mode >= 1 && !b) return cudaErrorInvalidValue;
-  cudaError_t e = cells_per_cta == 4    ? launch_mf_cell<4>(m, xs, z, ycell, act, err, s)
-                  : cells_per_cta == 16 ? launch_mf_cell<16>(m, xs, z, ycell, act, err, s)
-                                        : launch_mf_cell<8>(m, xs, z, ycell, act, err, s);
+  cudaError_t e = cells_per_cta == 4    ? launch_mf_cell<4>(m, xs, z, ycell, act, s)
+                  : cells_per_cta == 16 ? launch_mf_cell<16>(m, xs, z, ycell, act, s)
+                                        : launch_mf_cell<8>(m, xs, z, ycell, act, s);
   if (e != cudaSuccess) return e;
   if ((e = launch_robin_mf(m, z, ycell, act, s)) != cudaSuccess) return e;
   const int64_t gn = (m.nn + kMgNodes - 1) / kMgNodes;
