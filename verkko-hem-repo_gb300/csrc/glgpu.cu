@@ -146,7 +146,7 @@ struct glgpu_ctx
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
-  bool mf = false;                   // the Krylov operator is applied matrix-free from H (FP32, 3D)
+  bool mf = false;                   // the Krylov operator is applied matrix-free at the state (FP32, 3D)
   float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
   float *x32 = nullptr;              // FP32 copy of the state the matrix-free operator linearises at
   bool dinv_ready = false;           // block-Jacobi inverses of the current Jacobian
