@@ -158,3 +158,38 @@ def test_matep_golden_self_consistent():
     assert row[0] == -0.4
     assert row[1] == -0.010867967005548968
     assert row[7] == 3.581731300383963
+
+
+def _cm(a):
+    return (a[:9] + 1j * a[9:]).reshape(3, 3)
+
+
+def _pack(M):
+    return np.concatenate([M.real.ravel(), M.imag.ravel()])
+
+
+def test_hessian_vector_product_grouping(oracle_gl):
+    """The matrix-free operator's closed form of H f (the grouping of its three thread groups)
+    equals the oracle's bulk Hessian, which the golden kernels pin to the reference:
+      alpha f + 2 b3 dG_3;  2 b1 dG_1 + [w4 (S + S^+) + w5 (conj S + S^T)] A;
+      2 b2 dG_2 + (w4 Q + w5 Q^*) F,  with S = F A^+, Q = A A^+, w_t = 2 b_t."""
+    rng = np.random.default_rng(21)
+    H_ = lambda M: M.conj().T  # noqa: E731
+    for _ in range(8):
+        a, f = rng.standard_normal(18), rng.standard_normal(18)
+        alpha, b = rng.standard_normal(), rng.standard_normal(5)
+        coef = np.array([0.0, 0.0, alpha, *b])
+        _, H, _ = oracle_gl.bulk_q(coef, a)
+        ref = H.reshape(18, 18) @ f
+        A, F = _cm(a), _cm(f)
+        P, Q = A @ A.T, A @ H_(A)
+        S3 = A @ F.T
+        g0 = alpha * F + 2 * b[2] * ((S3 + S3.T) @ A.conj() + P @ F.conj())
+        p, dp = np.trace(P), 2 * np.sum(A * F)
+        S = F @ H_(A)
+        w4, w5 = 2 * b[3], 2 * b[4]
+        g1 = 2 * b[0] * (dp * A.conj() + p * F.conj()) + (w4 * (S + H_(S)) + w5 * (S.conj() + S.T)) @ A
+        q, dq = np.trace(Q).real, 2 * np.sum((A.conj() * F).real)
+        g2 = 2 * b[1] * (dq * A + q * F) + (w4 * Q + w5 * Q.conj()) @ F
+        got = _pack(g0 + g1 + g2)
+        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
