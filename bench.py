@@ -516,13 +516,17 @@ def main():
 
 def config3_leg(gl, linear_tol):
     """Mixed-precision solve of the refined cube: 64^3 Q1 on the same L = 20 cube, cells
-    within 0.1 L of a z face refined once (hanging nodes on two interface planes),
-    against the FP64 GPU Newton on the same mesh and start."""
+    within 0.1 L of a z face refined once (hanging nodes on two interface planes), with
+    multigrid (first coarse level: the unrefined 64^3 grid) and with block-Jacobi, against
+    the FP64 GPU Newton on the same mesh and start (multigrid, and the plain block-Jacobi
+    method)."""
     m = gl.cube_mesh(HALF, 64, 0.1)
     x0 = gl.bphase_guess(P_BAR, T_RED, m.nn, noise=NOISE, seed=SEED)
     res = {"n_nodes": m.nn, "n_dofs": 18 * m.nn, "n_hanging": m.n_hanging, "n_cells": m.nc}
-    for name, prec in (("mixed", gl.MIXED), ("fp64", gl.FP64)):
-        f = gl.FemGL(m, gl.Params.from_matep(P_BAR, T_RED, precision=prec))
+    legs = (("mixed", gl.MIXED, gl.PC_MULTIGRID), ("mixed_bj", gl.MIXED, gl.PC_BLOCK_JACOBI),
+            ("fp64_mg", gl.FP64, gl.PC_MULTIGRID), ("fp64", gl.FP64, gl.PC_BLOCK_JACOBI))
+    for name, prec, pc in legs:
+        f = gl.FemGL(m, gl.Params.from_matep(P_BAR, T_RED, precision=prec, precond=pc))
         f.set_solution(x0)
         f.sync()
         f.event_start()
@@ -531,10 +535,11 @@ def config3_leg(gl, linear_tol):
         F = float(f.free_energy()[0])
         res[name] = {"ms": ms, "newton_its": int(o["newton_its"][0]), "gmres_its": int(o["gmres_its"][0]),
                      "final_residual": float(o["residual"][0]), "converged": bool(o["converged"]), "F": F,
-                     "phases_ms": f.timers()}
+                     "mg_levels": f.mg_levels, "mg_fallbacks": f.mg_fallbacks, "phases_ms": f.timers()}
         f.close()
     res["free_energy_rel_diff"] = abs(res["mixed"]["F"] - res["fp64"]["F"]) / abs(res["fp64"]["F"])
     res["mixed_vs_fp64"] = res["fp64"]["ms"] / res["mixed"]["ms"]
+    res["mixed_vs_fp64_mg"] = res["fp64_mg"]["ms"] / res["mixed"]["ms"]
     return res
 
 

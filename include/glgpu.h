@@ -55,8 +55,8 @@ typedef enum
   GLGPU_PC_NONE = 0,
   GLGPU_PC_BLOCK_JACOBI = 1,   /* inverse of each node's diagonal block */
   GLGPU_PC_CHEBYSHEV = 2,      /* Chebyshev polynomial in (block-Jacobi)^-1 J */
-  GLGPU_PC_MULTIGRID = 3       /* geometric V-cycle (uniform box meshes; others fall back to block-Jacobi),
-                                  flexible GMRES outside */
+  GLGPU_PC_MULTIGRID = 3       /* geometric V-cycle (box meshes, uniform or once-refined; others fall back
+                                  to block-Jacobi), flexible GMRES outside */
 } glgpu_precond;
 
 /*
@@ -228,8 +228,9 @@ glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, 
 int64_t glgpu_launch_count(const glgpu_ctx *ctx);
 
 /* Coarse levels of the multigrid hierarchy (0 when the preconditioner is not multigrid
- * or an instance is not a uniform box grid).  Levels are nested tensor grids (every
- * other node line per coarsened axis), coarse Jacobians are Galerkin products P^T J P. */
+ * or an instance is neither a uniform box grid nor a once-refined one).  Levels are nested
+ * tensor grids (every other node line per coarsened axis; the first coarse level of a
+ * once-refined box is its unrefined grid), coarse Jacobians are Galerkin products P^T J P. */
 int glgpu_mg_levels(const glgpu_ctx *ctx);
 
 /* Linear solves whose multigrid cycles stalled (true residual not halved by a restart
@@ -368,6 +369,14 @@ glgpu_status glgpu_plan_robin(const glgpu_mesh *mesh, int n_inst, uint8_t *faces
  * 0 when they coincide (periodic pairs included).  First call with NULL arrays for n_pairs. */
 glgpu_status glgpu_plan_kelly(const glgpu_mesh *mesh, int n_inst, int64_t *n_pairs, int32_t *a, int8_t *fa,
                               int32_t *b, int8_t *fb, int8_t *sub);
+/* Multigrid prolongation from the first coarse level to the instance meshes, as the
+ * multigrid preconditioner builds it: node-level CSR over the fine nodes, ptr [n_nodes + 1],
+ * idx (coarse node ids), w; constrained fine nodes have empty rows, constrained coarse nodes
+ * are replaced by their parents.  coarse_xyz [n_coarse][3] are the coarse nodes'
+ * coordinates.  First call with NULL arrays for n_coarse and nnz; n_coarse = 0 when
+ * multigrid does not apply to the meshes. */
+glgpu_status glgpu_plan_prolongation(const glgpu_mesh *mesh, int n_inst, int64_t *n_coarse, int64_t *nnz,
+                                     int32_t *ptr, int32_t *idx, double *w, double *coarse_xyz);
 
 /* ---------------------------------------------------------------------------
  * Learned initial guess (no counterpart in the reference, which starts Newton from a

@@ -1,8 +1,8 @@
 """Geometric multigrid preconditioner (flexible GMRES) on the GPU: the coarse Jacobians
 are the Galerkin products P^T J P of the level above, tight linear solves agree with the
 oracle's Jacobian, Newton with multigrid reproduces the oracle's answer, batched
-instances of different sizes work, and non-uniform (refined) meshes fall back to
-block-Jacobi."""
+instances of different sizes work, and once-refined boxes (hanging nodes) get their
+unrefined grid as first coarse level."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -130,11 +130,72 @@ def test_multigrid_batched_uneven(gl):
     assert om["gmres_its"].sum() < ob["gmres_its"].sum()
 
 
-def test_multigrid_falls_back_on_refined_mesh(gl):
-    m = gl.cube_mesh(2.5, 4, 0.25)
-    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=1)
-    its, d, J, rhs, lev = _solve(gl, m, x0, gl.PC_MULTIGRID)
-    assert lev == 0 and its > 0
+@pytest.mark.parametrize("precision", [0, 1])
+def test_multigrid_on_refined_mesh(gl, oracle_gl, precision):
+    """A once-refined box (hanging nodes on the coarse-fine faces) gets multigrid with its
+    unrefined grid as first coarse level: that level's Jacobian is P^T J P over the free fine
+    nodes, and a tight solve satisfies the Jacobian in fewer iterations than block-Jacobi."""
+    m = gl.box_mesh([-5.0, -5.0, -5.0], [5.0, 5.0, 5.0], (8, 8, 8), refine_band=1.5)
+    assert m.n_hanging > 0
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=3)
+    tol = 1e-10 if precision == 0 else 1e-8
+    res = {}
+    for pc in (gl.PC_MULTIGRID, gl.PC_BLOCK_JACOBI):
+        prm = gl.Params.from_matep(20.0, 0.6, precond=pc, precision=precision)
+        with gl.FemGL(m, prm) as f:
+            f.set_solution(x0)
+            f.assemble_system()
+            its = f.solve(tol, allow_unconverged=pc == gl.PC_BLOCK_JACOBI)
+            res[pc] = (int(its[0]), f.update(), f.system(), f.mg_levels,
+                       f.mg_level(1) if pc == gl.PC_MULTIGRID else None)
+    its_mg, d, (rowptr, cols, vals, rhs), lev, (rp_c, c_c, v_c, (ptr, idx, w)) = res[gl.PC_MULTIGRID]
+    assert lev >= 3 and res[gl.PC_BLOCK_JACOBI][3] == 0
+    nf, nc = rowptr.size - 1, rp_c.size - 1
+    assert nc == 9 ** 3
+    hang = np.diff(np.asarray(m.hptr)) > 0
+    assert np.array_equal(np.diff(ptr) == 0, hang)
+    Pn = sp.csr_matrix((w, idx, ptr), shape=(nf, nc))
+    P = sp.kron(Pn, sp.identity(18), format="csr")
+    want = (P.T @ _bsr(rowptr, cols, vals) @ P).tocsr()
+    got = _bsr(rp_c, c_c, v_c)
+    single = (np.diff(ptr) == 1) & np.isclose(w[ptr[:-1].clip(max=w.size - 1)], 1.0)
+    assert np.bincount(idx[ptr[:-1][single]], minlength=nc).min() == 1
+    cmask = np.zeros(nc, np.uint32)
+    cmask[idx[ptr[:-1][single]]] = np.asarray(m.mask, np.uint32)[single]
+    free = ~((((cmask[:, None] >> np.arange(18)[None, :]) & 1) != 0).ravel())
+    Df = sp.diags(free.astype(float))
+    diff = (Df @ (want - got) @ Df).tocsr()
+    scale = np.abs((Df @ want @ Df).data).max()
+    assert np.abs(diff.data).max() <= (1e-13 if precision == 0 else 2e-6) * scale
+    # the solve: residual of the assembled Jacobian over the free fine rows
+    fr = np.repeat((np.asarray(m.mask) == 0) & ~hang, 18)
+    r = _bsr(rowptr, cols, vals) @ d - rhs
+    assert np.linalg.norm(r[fr]) <= (2e-10 if precision == 0 else 2e-5) * np.linalg.norm(rhs)
+    assert its_mg < res[gl.PC_BLOCK_JACOBI][0], (its_mg, res[gl.PC_BLOCK_JACOBI][0])
+
+
+def test_newton_multigrid_refined_matches_fp64(gl):
+    """Mixed-precision multigrid Newton on a refined box reaches the FP64 block-Jacobi
+    Newton's minimum: same free energy, |F| < 1e-10, and the same |A|^2 at every node.
+    Spin rotations and the global phase are exact symmetries with natural x / y faces, so
+    the two solvers may stop at different points of the same orbit: states are compared
+    through the invariant."""
+    m = gl.box_mesh([-5.0, -5.0, -4.0], [5.0, 5.0, 4.0], (8, 8, 6), refine_band=1.5)
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=2)
+    out = {}
+    for name, prec, pc, ltol in (("mg", gl.MIXED, gl.PC_MULTIGRID, 1e-4), ("ref", gl.FP64, gl.PC_BLOCK_JACOBI, 1e-12)):
+        prm = gl.Params.from_matep(20.0, 0.6, precision=prec, precond=pc)
+        with gl.FemGL(m, prm) as f:
+            f.set_solution(x0)
+            o = f.run(max_newton=40, linear_tol=ltol, converge_acc=1e-10)
+            out[name] = (o, f.free_energy()[0], f.solution(), f.mg_levels, f.mg_fallbacks)
+    om, Fm, xm, lev, fb = out["mg"]
+    orf, Fr, xr, _, _ = out["ref"]
+    assert om["converged"] and orf["converged"] and lev >= 2 and fb == 0
+    assert om["residual"][0] <= 1e-10
+    assert abs(Fm - Fr) <= 1e-9 * abs(Fr)
+    am, ar = (xm.reshape(-1, 18) ** 2).sum(1), (xr.reshape(-1, 18) ** 2).sum(1)
+    assert np.abs(am - ar).max() <= 1e-6 * ar.max()
 
 
 def test_preconditioner_reuse(gl):

@@ -303,3 +303,55 @@ def test_estimator_face_pairs_match_oracle(gl, kind):
         assert fa[k] // 2 == fb[k] // 2 and fa[k] != fb[k]
     _, ref = ok.kelly(oracle_mesh(m), np.zeros(18 * m.nn), lo, hi, n, periodic=per, return_pairs=True)
     assert mine == ref
+
+
+def _trilinear(x):
+    return 1.5 + 0.3 * x[:, 0] - 0.7 * x[:, 1] + 0.2 * x[:, 2] + 0.05 * x[:, 0] * x[:, 1] * x[:, 2]
+
+
+@pytest.mark.parametrize("kind", ["uniform", "band", "flags", "periodic_band", "batch"])
+def test_multigrid_prolongation_reproduces_q1(gl, kind):
+    """The first multigrid transfer: a once-refined box gets its unrefined grid as first coarse
+    level, and P interpolates that grid's Q1 field at the fine nodes.  A trilinear field
+    (periodic meshes: one of z only) on the coarse nodes comes back exactly at every free fine
+    node; constrained fine nodes (hanging nodes, periodic images) have empty rows."""
+    lo, hi, n = [-2.0, -2.5, -1.5], [2.0, 2.5, 1.5], (4, 5, 3)
+    if kind == "uniform":
+        meshes = [gl.box_mesh(lo, hi, n)]
+    elif kind == "band":
+        meshes = [gl.box_mesh(lo, hi, n, refine_band=0.9)]
+    elif kind == "flags":
+        flags = np.zeros(np.prod(n), np.int8)
+        flags[np.random.default_rng(5).choice(flags.size, 11, replace=False)] = 1
+        meshes = [gl.box_mesh_refine(lo, hi, n, flags)]
+    elif kind == "periodic_band":
+        meshes = [gl.box_mesh(lo, hi, n, refine_band=0.9, periodic_xy=(1, 1))]
+    else:
+        meshes = [gl.box_mesh(lo, hi, n, refine_band=0.9), gl.cube_mesh(2.0, 4)]
+    out = gl.plan_prolongation(meshes)
+    assert out is not None
+    ptr, idx, w, xc = out
+    xf = np.concatenate([np.asarray(m.xyz).reshape(-1, 3) for m in meshes])
+    hp = np.concatenate([np.diff(np.asarray(m.hptr)) if m.hptr is not None else np.zeros(m.nn, int) for m in meshes])
+    nco = xc.shape[0]
+    if kind in ("band", "flags", "periodic_band"):
+        assert nco == (n[0] + 1) * (n[1] + 1) * (n[2] + 1) and hp.sum() > 0
+    f = (lambda x: 1.0 + 0.4 * x[:, 2] ** 0 * x[:, 2]) if kind == "periodic_band" else _trilinear
+    rows = np.repeat(np.arange(ptr.size - 1), np.diff(ptr))
+    Pf = np.bincount(rows, weights=w * f(xc)[idx], minlength=ptr.size - 1)
+    free = hp == 0
+    assert np.array_equal(np.diff(ptr) == 0, ~free)
+    assert np.abs(Pf[free] - f(xf)[free]).max() <= 1e-12
+    assert np.allclose(np.bincount(rows, weights=w, minlength=ptr.size - 1)[free], 1.0, atol=1e-14)
+    assert idx.min() >= 0 and idx.max() < nco
+
+
+def test_multigrid_prolongation_declines_graded_grid(gl):
+    """A tensor grid with graded spacing is neither a uniform box grid nor a once-refined
+    one: multigrid does not apply (the preconditioner falls back to block-Jacobi)."""
+    m = gl.box_mesh([0.0, 0.0, 0.0], [4.0, 4.0, 4.0], (4, 4, 4))
+    xyz = np.asarray(m.xyz).reshape(-1, 3).copy()
+    xyz[:, 0] = xyz[:, 0] ** 2 / 4.0
+    g = gl.Mesh(3, xyz, np.asarray(m.cells), np.asarray(m.mask))
+    assert gl.plan_prolongation([m]) is not None
+    assert gl.plan_prolongation([g]) is None

@@ -959,107 +959,16 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       c->lv.push_back(L);
     }
   // transfer operators between level l (fine side) and l+1, and the Galerkin slot tables
-  std::vector<TensorGrid> fine_grid(n_inst);
-  for (int k = 0; k < n_inst; ++k)
-    {
-      BoxGeom g;
-      infer_box(mesh[k], g);
-      for (int d = 0; d < 3; ++d)
-        {
-          fine_grid[k].x[d].resize(g.n[d] + 1);
-          fine_grid[k].dir[d] = g.dir[d];
-          fine_grid[k].per[d] = g.per[d];
-        }
-    }
   c->tr.resize(nl);
   for (int l = 0; l < nl; ++l)
     {
-      glgpu_ctx *C = c->lv[l];
       const Plan &FP = (l == 0) ? c->P : c->lv[l - 1]->P;
-      const Plan &CP = C->P;
-      std::vector<int32_t> pp(1, 0), pi;
-      std::vector<double> pw;
-      for (int k = 0; k < n_inst; ++k)
-        {
-          const TensorGrid &fg = (l == 0) ? fine_grid[k] : lv[l - 1].grid[k];
-          int nc[3];
-          for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(lv[l].grid[k].x[d].size()) - 1;
-          std::vector<int32_t> a, b;
-          std::vector<double> w;
-          tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
-          if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
-            return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
-          // prolongation between the free spaces: constrained fine nodes (periodic images)
-          // get no row, constrained coarse nodes are replaced by their parents
-          const int64_t f0 = FP.node_off[k];
-          for (size_t i = 0; i + 1 < a.size(); ++i)
-            {
-              const int64_t fi = f0 + static_cast<int64_t>(i);
-              std::vector<std::pair<int32_t, double>> row;
-              if (FP.hptr[fi + 1] == FP.hptr[fi])
-                for (int32_t q = a[i]; q < a[i + 1]; ++q)
-                  {
-                    const int32_t j = b[q];
-                    if (CP.hptr[j + 1] == CP.hptr[j])
-                      row.push_back({j, w[q]});
-                    else
-                      for (int32_t h = CP.hptr[j]; h < CP.hptr[j + 1]; ++h) row.push_back({CP.hpar[h], w[q] * CP.hw[h]});
-                  }
-              std::sort(row.begin(), row.end());
-              size_t nr = 0;
-              for (size_t q = 0; q < row.size(); ++q)
-                if (nr > 0 && row[nr - 1].first == row[q].first)
-                  row[nr - 1].second += row[q].second;
-                else
-                  row[nr++] = row[q];
-              for (size_t q = 0; q < nr; ++q)
-                {
-                  pi.push_back(row[q].first);
-                  pw.push_back(row[q].second);
-                }
-              pp.push_back(static_cast<int32_t>(pi.size()));
-            }
-        }
-      std::vector<int32_t> rp, ri;
-      std::vector<double> rw;
-      transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
-      // Galerkin terms, grouped by coarse block: every (restriction entry i of row I,
-      // fine block (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to
-      // block (I, J); fine blocks come in increasing order within each list
-      std::vector<int64_t> gt(static_cast<size_t>(CP.nnzb) + 1, 0);
-      std::vector<int32_t> grow(CP.nnzb), gb;
-      std::vector<double> gw;
-      std::vector<std::vector<std::pair<int32_t, double>>> slot_terms(CP.max_row_blocks);
-      for (int64_t I = 0; I < CP.nn; ++I)
-        {
-          const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
-          const int32_t *c0 = CP.cols.data() + b0, *c1 = c0 + ns;
-          for (int s = 0; s < ns; ++s) slot_terms[s].clear();
-          for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
-            {
-              const int32_t i = ri[k];
-              for (int32_t b = FP.rowptr[i]; b < FP.rowptr[i + 1]; ++b)
-                {
-                  const int32_t j = FP.cols[b];
-                  for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
-                    {
-                      const int32_t *f = std::find(c0, c1, pi[q]);
-                      if (f == c1) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
-                      slot_terms[f - c0].emplace_back(b, rw[k] * pw[q]);
-                    }
-                }
-            }
-          for (int s = 0; s < ns; ++s)
-            {
-              grow[b0 + s] = static_cast<int32_t>(I);
-              for (const auto &tw : slot_terms[s])
-                {
-                  gb.push_back(tw.first);
-                  gw.push_back(tw.second);
-                }
-              gt[b0 + s + 1] = static_cast<int64_t>(gb.size());
-            }
-        }
+      TransferTables T;
+      glgpu_status ts = transfer_tables(mesh, n_inst, lv, l, FP, c->lv[l]->P, T);
+      if (ts != GLGPU_OK) return ts;
+      const std::vector<int32_t> &pp = T.pp, &pi = T.pi, &rp = T.rp, &ri = T.ri, &grow = T.g_row, &gb = T.g_blk;
+      const std::vector<double> &pw = T.pw, &rw = T.rw, &gw = T.g_w;
+      const std::vector<int64_t> &gt = T.g_toff;
       glgpu_ctx::Transfer &t = c->tr[l];
       t.h_ptr = pp;
       t.h_idx = pi;

@@ -63,8 +63,14 @@ struct MgLevel
   std::vector<TensorGrid> grid;                   // per instance
   std::vector<BoxMesh> meshes;                    // per instance
   std::vector<std::array<std::vector<Lin1>, 3>> map; // per instance: fine line -> coarse lines
+  // per instance: 1 when the finer level is the instance's once-refined mesh and this level
+  // its base grid (prolongation by interpolation at the fine node coordinates, map unused)
+  std::vector<uint8_t> coord;
 };
 bool infer_box(const glgpu_mesh &m, BoxGeom &g);
+bool infer_refined_box(const glgpu_mesh &m, BoxGeom &g);
+void coord_prolongation(const glgpu_mesh &m, const TensorGrid &c, std::vector<int32_t> &ptr, std::vector<int32_t> &idx,
+                        std::vector<double> &w, int64_t coarse_offset);
 int mesh_tensor(const TensorGrid &g, BoxMesh &m);
 void tensor_prolongation(const TensorGrid &f, const std::vector<Lin1> *map, std::vector<int32_t> &ptr,
                          std::vector<int32_t> &idx, std::vector<double> &w, int64_t coarse_offset, const int *nc);
@@ -143,6 +149,20 @@ struct Plan
 
 // Validates the meshes and builds the plan; returns 0 or sets an error message.
 glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &plan);
+
+// Transfer between multigrid level l (the instance meshes for l = 0, plan FP) and level
+// l + 1 (plan CP) of the hierarchy lv (mg.cc): the prolongation between the free spaces (pp,
+// pi, pw: rows of the fine nodes, constrained fine nodes empty, constrained coarse nodes
+// replaced by their parents), its transpose (rp, ri, rw), and the Galerkin term lists of
+// every coarse block (g_toff over coarse blocks, g_row, fine block g_blk with weight g_w).
+struct TransferTables
+{
+  std::vector<int32_t> pp, pi, rp, ri, g_row, g_blk;
+  std::vector<double> pw, rw, g_w;
+  std::vector<int64_t> g_toff;
+};
+glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
+                             const Plan &FP, const Plan &CP, TransferTables &T);
 
 // Robin (AdGR) faces of the 3D cells: bit f = 2 * axis + side of robin[e] is set when face f
 // of cell e is a pair-breaking boundary face (femgl/src/assemble.cc:286-348, boundary ids

@@ -3,13 +3,17 @@
 //
 // The reference preconditions its Krylov solve with Trilinos ML AMG
 // (femgl/src/solve.cc:141-152).  Here every instance of a context that is an axis-aligned
-// box with a tensor grid (no hanging nodes; periodic axes allowed) gets a hierarchy of nested coarser tensor
+// box with a tensor grid (periodic axes allowed) gets a hierarchy of nested coarser tensor
 // grids: a coarsened axis keeps every other node line and the last one.  Prolongation P
 // is the tensor product of 1D linear interpolation along the axes, restriction is P^T,
 // and the coarse Jacobians are the Galerkin products P^T J P (formed on the GPU after each
 // fine assembly), so every coarse operator is consistent with the fine Jacobian.  An axis
 // whose spacing is more than twice the smallest one is left alone until the others catch
 // up (semi-coarsening), so anisotropic slabs become isotropic before full coarsening.
+// A box grid whose flagged cells were refined once (hanging nodes on the coarse-fine
+// faces, as the reference's refine_grid produces them: femgl/src/refine.cc:131-176) has the
+// unrefined grid as its first coarse level: its Q1 space contains the base grid's, and P
+// interpolates the base grid's Q1 field at the fine nodes' coordinates.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -142,6 +146,138 @@ bool infer_box(const glgpu_mesh &m, BoxGeom &g)
   return true;
 }
 
+// A mesh is a once-refined box grid when every cell is an axis-aligned box whose edges are
+// those of the base grid (the largest cell's) on all three axes or half of them on all three
+// axes, the base-size cells start on the base lattice, every node lies on the half lattice,
+// and every constraint row is a hanging-node row or a periodic image (one parent, weight 1,
+// displaced by the box extent along the periodic axes).  g receives the base grid.
+bool infer_refined_box(const glgpu_mesh &m, BoxGeom &g)
+{
+  if (m.dim != 3 || m.n_nodes <= 0 || m.n_cells <= 0 || !m.xyz || !m.cells) return false;
+  for (int d = 0; d < 3; ++d)
+    {
+      g.lo[d] = 1e300;
+      g.hi[d] = -1e300;
+    }
+  for (int64_t i = 0; i < m.n_nodes; ++i)
+    for (int d = 0; d < 3; ++d)
+      {
+        g.lo[d] = std::min(g.lo[d], m.xyz[3 * i + d]);
+        g.hi[d] = std::max(g.hi[d], m.xyz[3 * i + d]);
+      }
+  double H[3] = {0.0, 0.0, 0.0};
+  for (int64_t e = 0; e < m.n_cells; ++e)
+    for (int d = 0; d < 3; ++d)
+      {
+        const int32_t *c = m.cells + 8 * e;
+        if (c[0] < 0 || c[0] >= m.n_nodes || c[7] < 0 || c[7] >= m.n_nodes) return false;
+        H[d] = std::max(H[d], m.xyz[3 * c[7] + d] - m.xyz[3 * c[0] + d]);
+      }
+  for (int d = 0; d < 3; ++d)
+    {
+      const double ext = g.hi[d] - g.lo[d];
+      if (!(H[d] > 0) || !(ext > 0)) return false;
+      g.n[d] = static_cast<int>(std::lround(ext / H[d]));
+      if (g.n[d] < 1 || std::fabs(g.n[d] * H[d] - ext) > 1e-9 * ext) return false;
+    }
+  // position on the half lattice of the base grid
+  auto half = [&](int d, double x, int64_t &r) {
+    const double u = 2.0 * (x - g.lo[d]) / (g.hi[d] - g.lo[d]) * g.n[d];
+    r = std::llround(u);
+    return std::fabs(u - static_cast<double>(r)) <= 1e-6;
+  };
+  for (int64_t i = 0; i < m.n_nodes; ++i)
+    for (int d = 0; d < 3; ++d)
+      {
+        int64_t r;
+        if (!half(d, m.xyz[3 * i + d], r)) return false;
+      }
+  for (int64_t e = 0; e < m.n_cells; ++e)
+    {
+      const int32_t *c = m.cells + 8 * e;
+      int kind = -1; // 0 base size, 1 half size
+      for (int d = 0; d < 3; ++d)
+        {
+          const double h = m.xyz[3 * c[7] + d] - m.xyz[3 * c[0] + d];
+          const int k = (std::fabs(h - H[d]) <= 1e-6 * H[d]) ? 0 : (std::fabs(2.0 * h - H[d]) <= 1e-6 * H[d]) ? 1 : -1;
+          if (k < 0 || (kind >= 0 && k != kind)) return false;
+          kind = k;
+          int64_t r;
+          half(d, m.xyz[3 * c[0] + d], r);
+          if (kind == 0 && (r & 1)) return false;
+        }
+    }
+  // constraint rows: hanging nodes (at least two parents) or periodic images
+  for (int d = 0; d < 3; ++d) g.per[d] = 0;
+  if (m.hang_ptr)
+    for (int64_t i = 0; i < m.n_nodes; ++i)
+      {
+        const int32_t h0 = m.hang_ptr[i], h1 = m.hang_ptr[i + 1];
+        if (h1 - h0 != 1) continue;
+        const int64_t p = m.hang_parent[h0];
+        if (m.hang_weight[h0] != 1.0 || p < 0 || p >= m.n_nodes) return false;
+        bool moved = false;
+        for (int d = 0; d < 3; ++d)
+          {
+            const double dx = m.xyz[3 * i + d] - m.xyz[3 * p + d], ext = g.hi[d] - g.lo[d];
+            if (std::fabs(dx) <= 1e-6 * H[d]) continue;
+            if (std::fabs(dx - ext) > 1e-6 * H[d]) return false;
+            g.per[d] = 1;
+            moved = true;
+          }
+        if (!moved) return false;
+      }
+  for (int d = 0; d < 3; ++d) g.dir[d] = 0;
+  if (m.dirichlet_mask)
+    for (int64_t i = 0; i < m.n_nodes; ++i)
+      for (int d = 0; d < 3; ++d)
+        if ((m.dirichlet_mask[i] & column_mask(d)) == column_mask(d)) g.dir[d] = 1;
+  for (int d = 0; d < 3; ++d)
+    if (g.dir[d] && g.per[d]) return false;
+  return true;
+}
+
+// Interpolation rows of the Q1 field of tensor grid c (nodes numbered as mesh_tensor numbers
+// them, plus coarse_offset) at the coordinates of every node of m: the tensor product of the
+// 1D linear interpolation between the two node lines around each coordinate.
+void coord_prolongation(const glgpu_mesh &m, const TensorGrid &c, std::vector<int32_t> &ptr, std::vector<int32_t> &idx,
+                        std::vector<double> &w, int64_t coarse_offset)
+{
+  int nc[3];
+  for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(c.x[d].size()) - 1;
+  ptr.assign(1, 0);
+  idx.clear();
+  w.clear();
+  for (int64_t i = 0; i < m.n_nodes; ++i)
+    {
+      Lin1 a[3];
+      for (int d = 0; d < 3; ++d)
+        {
+          const std::vector<double> &x = c.x[d];
+          const double v = m.xyz[3 * i + d], tol = 1e-9 * (x.back() - x.front());
+          int j = static_cast<int>(std::upper_bound(x.begin(), x.end(), v + tol) - x.begin()) - 1;
+          j = std::max(0, std::min(j, nc[d]));
+          if (j == nc[d] || std::fabs(v - x[j]) <= tol)
+            a[d] = Lin1{1, {j, 0}, {1.0, 0.0}};
+          else if (std::fabs(x[j + 1] - v) <= tol)
+            a[d] = Lin1{1, {j + 1, 0}, {1.0, 0.0}};
+          else
+            {
+              const double t = (v - x[j]) / (x[j + 1] - x[j]);
+              a[d] = Lin1{2, {j, j + 1}, {1.0 - t, t}};
+            }
+        }
+      for (int r = 0; r < a[2].n; ++r)
+        for (int q = 0; q < a[1].n; ++q)
+          for (int p = 0; p < a[0].n; ++p)
+            {
+              idx.push_back(static_cast<int32_t>(coarse_offset + grid_node(nc, a[0].c[p], a[1].c[q], a[2].c[r])));
+              w.push_back(a[0].w[p] * a[1].w[q] * a[2].w[r]);
+            }
+      ptr.push_back(static_cast<int32_t>(idx.size()));
+    }
+}
+
 // Hexahedral mesh of a tensor grid: nodes in (k, j, i) lexicographic order, cells in
 // deal.II vertex order, zero-Dirichlet masks on the faces of the axes flagged in dir, and
 // on periodic axes the upper face's nodes constrained to their images (weight 1).
@@ -255,19 +391,27 @@ void tensor_prolongation(const TensorGrid &f, const std::vector<Lin1> *map, std:
 }
 
 // Levels below the instance meshes, down to one cell per axis.  All instances must be
-// tensor box grids; returns the number of coarse levels (0 when multigrid does not apply).
+// tensor box grids or once-refined box grids (whose first coarse level is their base grid);
+// returns the number of coarse levels (0 when multigrid does not apply).
 int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vector<MgLevel> &levels,
                     std::string &why)
 {
   levels.clear();
   std::vector<TensorGrid> cur(n_inst);
+  std::vector<uint8_t> refined(n_inst, 0);
+  bool any_refined = false;
   for (int k = 0; k < n_inst; ++k)
     {
       BoxGeom g;
       if (!infer_box(mesh[k], g))
         {
-          why = "instance " + std::to_string(k) + " is not a uniform box grid";
-          return 0;
+          if (!infer_refined_box(mesh[k], g))
+            {
+              why = "instance " + std::to_string(k) + " is neither a box grid nor a once-refined box grid";
+              return 0;
+            }
+          refined[k] = 1;
+          any_refined = true;
         }
       for (int d = 0; d < 3; ++d)
         {
@@ -284,13 +428,27 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
       for (auto &g : cur)
         for (int d = 0; d < 3; ++d)
           if (g.x[d].size() > 2) all_min = false;
-      if (all_min) break;
+      if (all_min && !(l == 0 && any_refined)) break;
       MgLevel L;
       L.grid.resize(n_inst);
       L.meshes.resize(n_inst);
       L.map.resize(n_inst);
+      L.coord.assign(n_inst, 0);
       for (int k = 0; k < n_inst; ++k)
         {
+          if (l == 0 && refined[k])
+            {
+              // the base grid itself, reached by interpolation at the fine coordinates
+              L.grid[k] = cur[k];
+              L.coord[k] = 1;
+              if (mesh_tensor(L.grid[k], L.meshes[k]) != 0)
+                {
+                  why = "coarse mesh generation failed";
+                  levels.clear();
+                  return 0;
+                }
+              continue;
+            }
           const TensorGrid &f = cur[k];
           double h[3], hmin = 1e300;
           for (int d = 0; d < 3; ++d)
@@ -320,4 +478,150 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
   return static_cast<int>(levels.size());
 }
 
+glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
+                             const Plan &FP, const Plan &CP, TransferTables &T)
+{
+  std::vector<int32_t> &pp = T.pp, &pi = T.pi;
+  std::vector<double> &pw = T.pw;
+  pp.assign(1, 0);
+  pi.clear();
+  pw.clear();
+  for (int k = 0; k < n_inst; ++k)
+    {
+      std::vector<int32_t> a, b;
+      std::vector<double> w;
+      if (l == 0 && !lv[0].coord.empty() && lv[0].coord[k])
+        coord_prolongation(mesh[k], lv[0].grid[k], a, b, w, CP.node_off[k]);
+      else
+        {
+          TensorGrid fg;
+          if (l == 0)
+            {
+              BoxGeom g;
+              if (!infer_box(mesh[k], g)) return set_error(GLGPU_ERR_ARG, "multigrid: instance is not a box grid");
+              for (int d = 0; d < 3; ++d) fg.x[d].resize(g.n[d] + 1);
+            }
+          else
+            fg = lv[l - 1].grid[k];
+          int nc[3];
+          for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(lv[l].grid[k].x[d].size()) - 1;
+          tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
+        }
+      if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
+        return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
+      // prolongation between the free spaces: constrained fine nodes (hanging nodes,
+      // periodic images) get no row, constrained coarse nodes are replaced by their parents
+      const int64_t f0 = FP.node_off[k];
+      for (size_t i = 0; i + 1 < a.size(); ++i)
+        {
+          const int64_t fi = f0 + static_cast<int64_t>(i);
+          std::vector<std::pair<int32_t, double>> row;
+          if (FP.hptr[fi + 1] == FP.hptr[fi])
+            for (int32_t q = a[i]; q < a[i + 1]; ++q)
+              {
+                const int32_t j = b[q];
+                if (CP.hptr[j + 1] == CP.hptr[j])
+                  row.push_back({j, w[q]});
+                else
+                  for (int32_t h = CP.hptr[j]; h < CP.hptr[j + 1]; ++h) row.push_back({CP.hpar[h], w[q] * CP.hw[h]});
+              }
+          std::sort(row.begin(), row.end());
+          size_t nr = 0;
+          for (size_t q = 0; q < row.size(); ++q)
+            if (nr > 0 && row[nr - 1].first == row[q].first)
+              row[nr - 1].second += row[q].second;
+            else
+              row[nr++] = row[q];
+          for (size_t q = 0; q < nr; ++q)
+            {
+              pi.push_back(row[q].first);
+              pw.push_back(row[q].second);
+            }
+          pp.push_back(static_cast<int32_t>(pi.size()));
+        }
+    }
+  std::vector<int32_t> &rp = T.rp, &ri = T.ri;
+  std::vector<double> &rw = T.rw;
+  transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
+  // Galerkin terms, grouped by coarse block: every (restriction entry i of row I,
+  // fine block (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to
+  // block (I, J); fine blocks come in increasing order within each list
+  std::vector<int64_t> &gt = T.g_toff;
+  std::vector<int32_t> &grow = T.g_row, &gb = T.g_blk;
+  std::vector<double> &gw = T.g_w;
+  gt.assign(static_cast<size_t>(CP.nnzb) + 1, 0);
+  grow.assign(static_cast<size_t>(CP.nnzb), 0);
+  gb.clear();
+  gw.clear();
+  std::vector<std::vector<std::pair<int32_t, double>>> slot_terms(CP.max_row_blocks);
+  for (int64_t I = 0; I < CP.nn; ++I)
+    {
+      const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
+      const int32_t *c0 = CP.cols.data() + b0, *c1 = c0 + ns;
+      for (int s = 0; s < ns; ++s) slot_terms[s].clear();
+      for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
+        {
+          const int32_t i = ri[k];
+          for (int32_t b = FP.rowptr[i]; b < FP.rowptr[i + 1]; ++b)
+            {
+              const int32_t j = FP.cols[b];
+              for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
+                {
+                  const int32_t *f = std::find(c0, c1, pi[q]);
+                  if (f == c1) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
+                  slot_terms[f - c0].emplace_back(b, rw[k] * pw[q]);
+                }
+            }
+        }
+      for (int s = 0; s < ns; ++s)
+        {
+          grow[b0 + s] = static_cast<int32_t>(I);
+          for (const auto &tw : slot_terms[s])
+            {
+              gb.push_back(tw.first);
+              gw.push_back(tw.second);
+            }
+          gt[b0 + s + 1] = static_cast<int64_t>(gb.size());
+        }
+    }
+  return GLGPU_OK;
+}
+
 } // namespace glgpu
+
+extern "C" glgpu_status glgpu_plan_prolongation(const glgpu_mesh *mesh, int n_inst, int64_t *n_coarse, int64_t *nnz,
+                                                int32_t *ptr, int32_t *idx, double *w, double *coarse_xyz)
+{
+  using namespace glgpu;
+  if (!n_coarse || !nnz) return set_error(GLGPU_ERR_ARG, "glgpu_plan_prolongation: n_coarse or nnz is NULL");
+  *n_coarse = 0;
+  *nnz = 0;
+  Plan FP;
+  glgpu_status s = build_plan(mesh, n_inst, FP);
+  if (s != GLGPU_OK) return s;
+  if (FP.dim != 3) return GLGPU_OK;
+  std::vector<MgLevel> lv;
+  std::string why;
+  if (build_hierarchy(mesh, n_inst, 1, lv, why) == 0) return GLGPU_OK;
+  std::vector<glgpu_mesh> ms(n_inst);
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const BoxMesh &b = lv[0].meshes[k];
+      const bool con = !b.hpar.empty();
+      ms[k] = glgpu_mesh{3, b.nn, b.nc, b.xyz.data(), b.cells.data(), b.mask.data(),
+                         con ? b.hptr.data() : nullptr, con ? b.hpar.data() : nullptr, con ? b.hw.data() : nullptr};
+    }
+  Plan CP;
+  if ((s = build_plan(ms.data(), n_inst, CP)) != GLGPU_OK) return s;
+  TransferTables T;
+  if ((s = transfer_tables(mesh, n_inst, lv, 0, FP, CP, T)) != GLGPU_OK) return s;
+  *n_coarse = CP.nn;
+  *nnz = static_cast<int64_t>(T.pi.size());
+  if (ptr) std::copy(T.pp.begin(), T.pp.end(), ptr);
+  if (idx) std::copy(T.pi.begin(), T.pi.end(), idx);
+  if (w) std::copy(T.pw.begin(), T.pw.end(), w);
+  if (coarse_xyz)
+    for (int k = 0; k < n_inst; ++k)
+      std::copy(lv[0].meshes[k].xyz.begin(), lv[0].meshes[k].xyz.end(), coarse_xyz + 3 * CP.node_off[k]);
+  return GLGPU_OK;
+}

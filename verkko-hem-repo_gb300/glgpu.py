@@ -358,6 +358,24 @@ def plan_kelly(meshes: Sequence[Mesh]):
     return a, fa, b, fb, sub
 
 
+def plan_prolongation(meshes: Sequence[Mesh]):
+    """Host-only multigrid prolongation from the first coarse level to the instance meshes:
+    (ptr, idx, w, coarse_xyz) as node-level CSR over the fine nodes, or None when multigrid
+    does not apply."""
+    ms = (_Mesh * len(meshes))(*[m._struct() for m in meshes])
+    L = lib()
+    nco, nnz = ctypes.c_int64(), ctypes.c_int64()
+    _check(L.glgpu_plan_prolongation(ms, len(meshes), ctypes.byref(nco), ctypes.byref(nnz), None, None, None, None))
+    if nco.value == 0:
+        return None
+    ptr = np.zeros(sum(m.nn for m in meshes) + 1, np.int32)
+    idx, w = np.zeros(nnz.value, np.int32), np.zeros(nnz.value)
+    xyz = np.zeros((nco.value, 3))
+    _check(L.glgpu_plan_prolongation(ms, len(meshes), ctypes.byref(nco), ctypes.byref(nnz), _p(ptr, _ip), _p(idx, _ip),
+                                     _p(w, _dp), _p(xyz, _dp)))
+    return ptr, idx, w, xyz
+
+
 def plan_pattern(meshes: Sequence[Mesh]):
     """Host-only block pattern (rowptr, cols) of the condensed Jacobian."""
     info = plan_info(meshes)
