@@ -342,6 +342,11 @@ def main():
         gl.build()
         print(json.dumps({"config3": config3_leg(gl, args.linear_tol)}))
         return 0
+    if args.config4:
+        gl = importlib.import_module("verkko-hem-repo_gb300")
+        gl.build()
+        print(json.dumps({"config4": config4_leg(gl, args.config4, args.linear_tol)}))
+        return 0
     if args.impl == "reference":
         return reference_arm(args, rank)
     if int(os.environ.get("WORLD_SIZE", "1")) > 1 and rank != 0:
@@ -541,6 +546,46 @@ def config3_leg(gl, linear_tol):
     res["mixed_vs_fp64"] = res["fp64"]["ms"] / res["mixed"]["ms"]
     res["mixed_vs_fp64_mg"] = res["fp64_mg"]["ms"] / res["mixed"]["ms"]
     return res
+
+
+def config4_leg(gl, count, linear_tol):
+    """The batched sweep at full scale: `count` seeded slab instances of the phase-diagram
+    sweep (T/Tc ~ U(0.3, 0.95), p ~ U(0, 34) bar, D ~ U(8, 40) xi0, n ~ U{16..48} cells per
+    side), mixed precision with multigrid, solved in waves of batched contexts that fit the
+    device.  FP64 multigrid solves of the first instances, one at a time, check the free
+    energies."""
+    S = importlib.import_module("verkko-hem-repo_gb300.sweep")
+    t0 = time.perf_counter()
+    inst = batch_instances(gl, count)
+    mesh_s = time.perf_counter() - t0
+    meshes = [d["mesh"] for d in inst]
+    prms = [gl.Params.from_matep(d["p"], d["t"], precision=gl.MIXED, precond=gl.PC_MULTIGRID) for d in inst]
+    x0 = [d["x0"] for d in inst]
+    S.solve_sweep(gl, meshes[:2], prms[:2], x0[:2], linear_tol=linear_tol, converge_acc=TOL)  # warm-up
+    t0 = time.perf_counter()
+    r = S.solve_sweep(gl, meshes, prms, x0, linear_tol=linear_tol, converge_acc=TOL,
+                      log=lambda s: print(s, file=sys.stderr, flush=True))
+    wall_s = time.perf_counter() - t0
+    solve_s = sum(r["solve_ms"]) / 1000.0
+    rel = []
+    for d, Fm in list(zip(inst, r["free_energy"]))[:3]:
+        prm = gl.Params.from_matep(d["p"], d["t"], precision=gl.FP64, precond=gl.PC_MULTIGRID)
+        with gl.FemGL(d["mesh"], prm) as g:
+            g.set_solution(d["x0"])
+            g.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL)
+            Fd = g.free_energy()[0]
+        rel.append(abs(Fm - Fd) / abs(Fd))
+    return {"instances": count, "total_nodes": int(sum(m.nn for m in meshes)),
+            "total_dofs": int(sum(18 * m.nn for m in meshes)),
+            "solves_per_s": count / solve_s, "solves_per_s_with_setup": count / wall_s,
+            "solve_s": solve_s, "setup_s": float(sum(r["create_s"])), "wall_s": wall_s, "mesh_s": mesh_s,
+            "waves": r["waves"], "solve_ms_per_wave": r["solve_ms"], "create_s_per_wave": r["create_s"],
+            "wave_gib": [b / 2**30 for b in r["wave_bytes"]], "bytes_per_node": r["bytes_per_node"],
+            "budget_gib": r["budget"] / 2**30, "mg_fallbacks": r["mg_fallbacks"],
+            "all_converged": bool(r["converged"].all()), "max_final_residual": float(r["residual"].max()),
+            "newton_its_mean": float(r["newton_its"].mean()), "gmres_its_mean": float(r["gmres_its"].mean()),
+            "free_energy_rel_diff_vs_fp64_first3": rel,
+            "sample": "seeded (seed 4) instances of the sweep: T/Tc~U(0.3,0.95), p~U(0,34), D~U(8,40), n~U{16..48}"}
 
 
 def ncu_case(n, fp64):

@@ -227,6 +227,12 @@ glgpu_status glgpu_kernel_timing(glgpu_ctx *ctx, int enable, double *kernel_ms, 
 /* Number of kernels this context has launched since creation. */
 int64_t glgpu_launch_count(const glgpu_ctx *ctx);
 
+/* Device memory this context holds (its own allocations and its multigrid levels'), in
+ * bytes; and the device's free and total memory (cudaMemGetInfo).  A sweep larger than the
+ * device uses them to pack instances into batched contexts that fit. */
+int64_t glgpu_device_bytes(const glgpu_ctx *ctx);
+glgpu_status glgpu_mem_info(size_t *free_bytes, size_t *total_bytes);
+
 /* Coarse levels of the multigrid hierarchy (0 when the preconditioner is not multigrid
  * or an instance is neither a uniform box grid nor a once-refined one).  Levels are nested
  * tensor grids (every other node line per coarsened axis; the first coarse level of a

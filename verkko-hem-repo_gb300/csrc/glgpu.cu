@@ -87,6 +87,7 @@ struct glgpu_ctx
   int restart = 50;
   cudaStream_t st = nullptr;
   std::vector<void *> allocs;
+  size_t dev_bytes = 0; // sum of this context's device allocations
   // state
   double *x = nullptr, *xt = nullptr, *delta = nullptr, *R = nullptr, *rhs = nullptr;
   double *r_cell = nullptr, *e_cell = nullptr;
@@ -268,6 +269,7 @@ template <typename T> glgpu_status dalloc(glgpu_ctx *c, T **p, size_t n)
     return set_error(GLGPU_ERR_NOMEM, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " +
                                           cudaGetErrorString(e));
   c->allocs.push_back(*p);
+  c->dev_bytes += n * sizeof(T);
   return GLGPU_OK;
 }
 
@@ -1852,6 +1854,22 @@ extern "C" int64_t glgpu_launch_count(const glgpu_ctx *c)
   int64_t n = c->launches;
   for (const glgpu_ctx *l : c->lv) n += glgpu_launch_count(l);
   return n;
+}
+
+extern "C" int64_t glgpu_device_bytes(const glgpu_ctx *c)
+{
+  if (!c) return 0;
+  int64_t n = static_cast<int64_t>(c->dev_bytes);
+  for (const glgpu_ctx *l : c->lv) n += glgpu_device_bytes(l);
+  return n;
+}
+
+extern "C" glgpu_status glgpu_mem_info(size_t *free_bytes, size_t *total_bytes)
+{
+  if (!free_bytes || !total_bytes) return set_error(GLGPU_ERR_ARG, "glgpu_mem_info: NULL argument");
+  const cudaError_t e = cudaMemGetInfo(free_bytes, total_bytes);
+  if (e != cudaSuccess) return set_error(GLGPU_ERR_CUDA, std::string("cudaMemGetInfo: ") + cudaGetErrorString(e));
+  return GLGPU_OK;
 }
 
 extern "C" int glgpu_mg_levels(const glgpu_ctx *c) { return c ? c->n_levels : 0; }

@@ -161,11 +161,13 @@ int mesh_box(const double *lo, const double *hi, const int *n, double band, cons
   for (int64_t e = 0; e < ncell * 8; ++e)
     m.cells[e] = static_cast<int32_t>(std::lower_bound(ukey.begin(), ukey.end(), vkey[e]) - ukey.begin());
 
-  // hanging nodes on faces of coarse cells
+  // hanging nodes on faces of coarse cells (none unless some cell was refined)
   std::vector<int32_t> npar(nn, 0);
   std::vector<int32_t> par(nn * 4, -1);
   std::vector<double> wt(nn * 4, 0.0);
-  for (int64_t e = 0; e < ncell; ++e)
+  bool any_refined = false;
+  for (int64_t e = 0; e < ncell && !any_refined; ++e) any_refined = cl[e].s == 1;
+  for (int64_t e = 0; e < ncell && any_refined; ++e)
     {
       if (cl[e].s != 2) continue;
       const int32_t *b = cl[e].b;

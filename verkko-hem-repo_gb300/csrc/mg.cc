@@ -554,11 +554,16 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   gb.clear();
   gw.clear();
   std::vector<std::vector<std::pair<int32_t, double>>> slot_terms(CP.max_row_blocks);
+  std::vector<int32_t> slot_of(static_cast<size_t>(CP.nn), -1); // column -> slot of the current row
   for (int64_t I = 0; I < CP.nn; ++I)
     {
       const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
-      const int32_t *c0 = CP.cols.data() + b0, *c1 = c0 + ns;
-      for (int s = 0; s < ns; ++s) slot_terms[s].clear();
+      const int32_t *c0 = CP.cols.data() + b0;
+      for (int s = 0; s < ns; ++s)
+        {
+          slot_terms[s].clear();
+          slot_of[c0[s]] = s;
+        }
       for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
         {
           const int32_t i = ri[k];
@@ -567,15 +572,16 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
               const int32_t j = FP.cols[b];
               for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
                 {
-                  const int32_t *f = std::find(c0, c1, pi[q]);
-                  if (f == c1) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
-                  slot_terms[f - c0].emplace_back(b, rw[k] * pw[q]);
+                  const int32_t sl = slot_of[pi[q]];
+                  if (sl < 0) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
+                  slot_terms[sl].emplace_back(b, rw[k] * pw[q]);
                 }
             }
         }
       for (int s = 0; s < ns; ++s)
         {
           grow[b0 + s] = static_cast<int32_t>(I);
+          slot_of[c0[s]] = -1;
           for (const auto &tw : slot_terms[s])
             {
               gb.push_back(tw.first);

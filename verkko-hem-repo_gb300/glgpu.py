@@ -102,6 +102,9 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mg_prolongation.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
     L.glgpu_launch_count.argtypes = [vp]
     L.glgpu_launch_count.restype = ctypes.c_int64
+    L.glgpu_device_bytes.argtypes = [vp]
+    L.glgpu_device_bytes.restype = ctypes.c_int64
+    L.glgpu_mem_info.argtypes = [ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
     L.glgpu_sync.argtypes = [vp]
     L.glgpu_event_start.argtypes = [vp]
     L.glgpu_event_stop.argtypes = [vp, _dp]
@@ -298,6 +301,13 @@ class _Pinned:
         if getattr(self, "ptr", None) is not None and self.ptr.value:
             lib().glgpu_host_free(self.ptr)
             self.ptr = None
+
+
+def mem_info():
+    """(free, total) device memory in bytes."""
+    fr, tot = ctypes.c_size_t(), ctypes.c_size_t()
+    _check(lib().glgpu_mem_info(ctypes.byref(fr), ctypes.byref(tot)))
+    return int(fr.value), int(tot.value)
 
 
 def pinned_array(n: int, dtype=np.float64) -> np.ndarray:
@@ -572,6 +582,11 @@ class FemGL:
     @property
     def launch_count(self) -> int:
         return int(lib().glgpu_launch_count(self._ctx))
+
+    @property
+    def device_bytes(self) -> int:
+        """Device memory held by this context (multigrid levels included)."""
+        return int(lib().glgpu_device_bytes(self._ctx))
 
     @property
     def mg_levels(self) -> int:

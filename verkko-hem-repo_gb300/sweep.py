@@ -1,0 +1,103 @@
+"""Sweeps larger than the device: many instances solved in waves of batched contexts.
+
+A batched context keeps every instance's Jacobian blocks, Krylov bases and multigrid
+hierarchy resident (in mixed precision with multigrid, tens of KB per mesh node), so a
+phase-diagram sweep such as 256 slab instances of 16^3 to 48^3 cells (11.5M nodes) does not
+fit one context.  ``solve_sweep`` measures the per-node footprint on a probe context built
+from the largest instance, packs consecutive instances into waves that fit the free device
+memory, solves each wave as one batched context and returns the results in input order.
+Instances are independent inside a context (per-instance reductions, GMRES, line search and
+convergence), so an instance's result does not depend on the wave it lands in.
+
+The reference solves one configuration per program run (femgl/src/run.cc:157-258); the sweep
+is the batched form of running it over many (T, p, thickness) points."""
+import time
+from typing import Sequence
+
+import numpy as np
+
+
+def plan_waves(node_counts: Sequence[int], bytes_per_node: float, budget: float) -> list:
+    """Consecutive groups of instance indices whose estimated footprint (nodes x
+    bytes_per_node) stays within budget; raises ValueError for an instance that alone
+    exceeds it."""
+    waves, cur, used = [], [], 0.0
+    for i, nn in enumerate(node_counts):
+        need = float(nn) * bytes_per_node
+        if need > budget:
+            raise ValueError(f"instance {i} ({nn} nodes, {need / 2**30:.2f} GiB) exceeds the budget "
+                             f"of {budget / 2**30:.2f} GiB")
+        if cur and used + need > budget:
+            waves.append(cur)
+            cur, used = [], 0.0
+        cur.append(i)
+        used += need
+    if cur:
+        waves.append(cur)
+    return waves
+
+
+def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: float = 1e-4,
+                converge_acc: float = 1e-10, budget: float | None = None, margin: float = 1.1,
+                keep_solutions: bool = False, log=None) -> dict:
+    """Solve every instance (meshes[k], params[k], start x0[k]) to converge_acc, in waves.
+
+    budget: device bytes a wave may take (default: 90 % of the free memory less 2 GiB).
+    Returns per-instance arrays in input order (newton_its, gmres_its, residual,
+    free_energy, converged, wave) and per-wave timing: create_s (host plan, hierarchy and
+    device setup), solve_ms (device time of the Newton solve, CUDA events), mg_fallbacks
+    (multigrid solves of the wave handed to block-Jacobi: a context-wide switch, so only
+    waves without one give bitwise the results of any other packing).  With
+    keep_solutions the converged states come back as a list of arrays; log, when given, is
+    called with one line per finished wave."""
+    n = len(meshes)
+    if not (len(params) == n and len(x0) == n):
+        raise ValueError("meshes, params and x0 must have one entry per instance")
+    sizes = [int(m.nn) for m in meshes]
+    big = int(np.argmax(sizes))
+    with gl.FemGL(meshes[big], params[big]) as probe:
+        per_node = probe.device_bytes / sizes[big]
+    if budget is None:
+        free, _ = gl.mem_info()
+        budget = 0.9 * free - 2.0 * 2**30
+    waves = plan_waves(sizes, per_node * margin, budget)
+    res = {"newton_its": np.zeros(n, np.int32), "gmres_its": np.zeros(n, np.int32), "residual": np.zeros(n),
+           "free_energy": np.zeros(n), "converged": np.zeros(n, bool), "wave": np.zeros(n, np.int32)}
+    sols = [None] * n if keep_solutions else None
+    create_s, solve_ms, wave_bytes, fallbacks = [], [], [], []
+    for wi, w in enumerate(waves):
+        t0 = time.perf_counter()
+        f = gl.FemGL([meshes[i] for i in w], [params[i] for i in w])
+        try:
+            create_s.append(time.perf_counter() - t0)
+            wave_bytes.append(f.device_bytes)
+            f.set_solution(np.concatenate([np.asarray(x0[i], np.float64) for i in w]))
+            f.sync()
+            f.event_start()
+            out = f.run(max_newton=max_newton, linear_tol=linear_tol, converge_acc=converge_acc,
+                        allow_unconverged=True)
+            solve_ms.append(f.event_stop())
+            F = f.free_energy()
+            fallbacks.append(f.mg_fallbacks)
+            x = f.solution() if keep_solutions else None
+        finally:
+            f.close()
+        if log is not None:
+            log(f"wave {wi}: {len(w)} instances, {sum(sizes[i] for i in w)} nodes, "
+                f"{wave_bytes[-1] / 2**30:.1f} GiB, create {create_s[-1]:.1f} s, solve {solve_ms[-1]:.0f} ms")
+        off = 0
+        for j, i in enumerate(w):
+            res["newton_its"][i] = out["newton_its"][j]
+            res["gmres_its"][i] = out["gmres_its"][j]
+            res["residual"][i] = out["residual"][j]
+            res["free_energy"][i] = F[j]
+            res["converged"][i] = out["residual"][j] <= converge_acc
+            res["wave"][i] = wi
+            if keep_solutions:
+                sols[i] = x[off:off + 18 * sizes[i]].copy()
+            off += 18 * sizes[i]
+    res.update({"waves": [len(w) for w in waves], "create_s": create_s, "solve_ms": solve_ms,
+                "wave_bytes": wave_bytes, "mg_fallbacks": fallbacks, "bytes_per_node": per_node, "budget": budget})
+    if keep_solutions:
+        res["solutions"] = sols
+    return res
