@@ -1,5 +1,8 @@
-"""A sweep solved in waves of batched contexts gives each instance the result it gets in a
-single context holding the whole sweep (instances are independent inside a context)."""
+"""A sweep solved in waves of batched contexts gives each instance the minimum it reaches in a
+single context holding the whole sweep.  The preconditioner's storage and kernel shapes follow
+the context's total size (FP16 coarse levels from 2000 nodes, warps per block row), so the
+FP32 Krylov path of an instance changes with its wave at rounding level: the converged free
+energies agree to the Newton tolerance, not bitwise."""
 import importlib
 
 import numpy as np
@@ -32,9 +35,6 @@ def test_waves_match_single_context(gl):
     for r in (one, many):
         assert r["converged"].all() and (r["residual"] <= 1e-10).all()
     assert np.allclose(many["free_energy"], one["free_energy"], rtol=1e-10, atol=0)
-    if sum(one["mg_fallbacks"]) == 0 and sum(many["mg_fallbacks"]) == 0:
-        assert np.array_equal(many["newton_its"], one["newton_its"])
-        assert np.array_equal(many["free_energy"], one["free_energy"])
     assert [s.size for s in many["solutions"]] == [18 * m.nn for m in meshes]
     with pytest.raises(ValueError):
         sweep.solve_sweep(gl, meshes, prms, x0, budget=0.5 * per * nn_max, **kw)

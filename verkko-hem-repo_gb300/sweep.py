@@ -7,7 +7,10 @@ fit one context.  ``solve_sweep`` measures the per-node footprint on a probe con
 from the largest instance, packs consecutive instances into waves that fit the free device
 memory, solves each wave as one batched context and returns the results in input order.
 Instances are independent inside a context (per-instance reductions, GMRES, line search and
-convergence), so an instance's result does not depend on the wave it lands in.
+convergence); the preconditioner's storage and kernel shapes follow the context's total size
+(FP16 coarse levels from 2000 nodes, warps per block row), so an instance's FP32 Krylov path
+changes with its wave at rounding level and its converged state agrees to the Newton
+tolerance.
 
 The reference solves one configuration per program run (femgl/src/run.cc:157-258); the sweep
 is the batched form of running it over many (T, p, thickness) points."""
@@ -46,8 +49,7 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
     Returns per-instance arrays in input order (newton_its, gmres_its, residual,
     free_energy, converged, wave) and per-wave timing: create_s (host plan, hierarchy and
     device setup), solve_ms (device time of the Newton solve, CUDA events), mg_fallbacks
-    (multigrid solves of the wave handed to block-Jacobi: a context-wide switch, so only
-    waves without one give bitwise the results of any other packing).  With
+    (multigrid solves of the wave handed to block-Jacobi, a context-wide switch).  With
     keep_solutions the converged states come back as a list of arrays; log, when given, is
     called with one line per finished wave."""
     n = len(meshes)
