@@ -355,3 +355,32 @@ def test_multigrid_prolongation_declines_graded_grid(gl):
     g = gl.Mesh(3, xyz, np.asarray(m.cells), np.asarray(m.mask))
     assert gl.plan_prolongation([m]) is not None
     assert gl.plan_prolongation([g]) is None
+
+
+@pytest.mark.parametrize("kind", ["band", "flags", "periodic_band"])
+def test_refined_galerkin_stays_in_base_pattern(gl, kind):
+    """P^T J P of a once-refined box lies inside the block pattern of its unrefined grid (the
+    first coarse level), checked on the block sparsity: a fine cell lies inside one base cell
+    and a hanging node's parents are vertices of the base cell it borders."""
+    import scipy.sparse as sp
+
+    lo, hi, n = [-2.0, -2.5, -1.5], [2.0, 2.5, 1.5], (4, 5, 3)
+    per = (1, 1) if kind == "periodic_band" else (0, 0)
+    if kind == "flags":
+        flags = np.zeros(np.prod(n), np.int8)
+        flags[np.random.default_rng(9).choice(flags.size, 13, replace=False)] = 1
+        m = gl.box_mesh_refine(lo, hi, n, flags)
+    else:
+        m = gl.box_mesh(lo, hi, n, refine_band=0.9, periodic_xy=per)
+    base = gl.box_mesh(lo, hi, n, periodic_xy=per)
+    ptr, idx, w, xc = gl.plan_prolongation([m])
+    assert np.allclose(xc, np.asarray(base.xyz).reshape(-1, 3))
+    rp, cols = gl.plan_pattern([m])
+    crp, ccols = gl.plan_pattern([base])
+    nf, nc = rp.size - 1, crp.size - 1
+    S = sp.csr_matrix((np.ones(cols.size), cols, rp), shape=(nf, nf))
+    P = sp.csr_matrix((np.ones(idx.size), idx, ptr), shape=(nf, nc))
+    G = (P.T @ S @ P).tocoo()
+    C = sp.csr_matrix((np.ones(ccols.size), ccols, crp), shape=(nc, nc))
+    assert G.nnz > 0
+    assert np.all(np.asarray(C[G.row, G.col]).ravel() > 0)
