@@ -543,52 +543,74 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   std::vector<int32_t> &rp = T.rp, &ri = T.ri;
   std::vector<double> &rw = T.rw;
   transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
-  // Galerkin terms, grouped by coarse block: every (restriction entry i of row I,
-  // fine block (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to
-  // block (I, J); fine blocks come in increasing order within each list
+  // Galerkin terms, grouped by coarse block: every (restriction entry i of row I, fine block
+  // (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to block (I, J); within a
+  // block the terms follow (restriction entry, fine block, prolongation entry) order, so fine
+  // blocks come in increasing order.  Pass 0 counts the terms of every block, pass 1 writes
+  // them at their offsets; both run over the coarse rows on all host threads (a row's blocks
+  // belong to one thread), and the tables do not depend on the thread count.
   std::vector<int64_t> &gt = T.g_toff;
   std::vector<int32_t> &grow = T.g_row, &gb = T.g_blk;
   std::vector<double> &gw = T.g_w;
   gt.assign(static_cast<size_t>(CP.nnzb) + 1, 0);
   grow.assign(static_cast<size_t>(CP.nnzb), 0);
-  gb.clear();
-  gw.clear();
-  std::vector<std::vector<std::pair<int32_t, double>>> slot_terms(CP.max_row_blocks);
-  std::vector<int32_t> slot_of(static_cast<size_t>(CP.nn), -1); // column -> slot of the current row
-  for (int64_t I = 0; I < CP.nn; ++I)
+  const int64_t ncr = CP.nn;
+  for (int pass = 0; pass < 2; ++pass)
     {
-      const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
-      const int32_t *c0 = CP.cols.data() + b0;
-      for (int s = 0; s < ns; ++s)
+      if (pass == 1)
         {
-          slot_terms[s].clear();
-          slot_of[c0[s]] = s;
+          for (int64_t b = 0; b < CP.nnzb; ++b) gt[b + 1] += gt[b];
+          gb.assign(static_cast<size_t>(gt[CP.nnzb]), 0);
+          gw.assign(static_cast<size_t>(gt[CP.nnzb]), 0.0);
         }
-      for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
-        {
-          const int32_t i = ri[k];
-          for (int32_t b = FP.rowptr[i]; b < FP.rowptr[i + 1]; ++b)
-            {
-              const int32_t j = FP.cols[b];
-              for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
-                {
-                  const int32_t sl = slot_of[pi[q]];
-                  if (sl < 0) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
-                  slot_terms[sl].emplace_back(b, rw[k] * pw[q]);
-                }
-            }
-        }
-      for (int s = 0; s < ns; ++s)
-        {
-          grow[b0 + s] = static_cast<int32_t>(I);
-          slot_of[c0[s]] = -1;
-          for (const auto &tw : slot_terms[s])
-            {
-              gb.push_back(tw.first);
-              gw.push_back(tw.second);
-            }
-          gt[b0 + s + 1] = static_cast<int64_t>(gb.size());
-        }
+      int outside = 0;
+#pragma omp parallel reduction(| : outside)
+      {
+        std::vector<int32_t> slot_of(static_cast<size_t>(ncr), -1); // column -> slot of the current row
+        std::vector<int64_t> pos(static_cast<size_t>(CP.max_row_blocks));
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t I = 0; I < ncr; ++I)
+          {
+            const int32_t b0 = CP.rowptr[I], ns = CP.rowptr[I + 1] - b0;
+            const int32_t *c0 = CP.cols.data() + b0;
+            for (int s = 0; s < ns; ++s)
+              {
+                slot_of[c0[s]] = s;
+                if (pass == 1) pos[s] = gt[b0 + s];
+              }
+            for (int32_t k = rp[I]; k < rp[I + 1]; ++k)
+              {
+                const int32_t i = ri[k];
+                for (int32_t b = FP.rowptr[i]; b < FP.rowptr[i + 1]; ++b)
+                  {
+                    const int32_t j = FP.cols[b];
+                    for (int32_t q = pp[j]; q < pp[j + 1]; ++q)
+                      {
+                        const int32_t sl = slot_of[pi[q]];
+                        if (sl < 0)
+                          {
+                            outside = 1;
+                            continue;
+                          }
+                        if (pass == 0)
+                          ++gt[b0 + sl + 1];
+                        else
+                          {
+                            gb[pos[sl]] = b;
+                            gw[pos[sl]] = rw[k] * pw[q];
+                            ++pos[sl];
+                          }
+                      }
+                  }
+              }
+            for (int s = 0; s < ns; ++s)
+              {
+                slot_of[c0[s]] = -1;
+                grow[b0 + s] = static_cast<int32_t>(I);
+              }
+          }
+      }
+      if (outside) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
     }
   return GLGPU_OK;
 }
