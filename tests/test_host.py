@@ -346,6 +346,23 @@ def test_multigrid_prolongation_reproduces_q1(gl, kind):
     assert idx.min() >= 0 and idx.max() < nco
 
 
+def test_multigrid_prolongation_declines_l_shaped_domain(gl):
+    """Cells of a box lattice that do not fill the box (an L-shaped domain) have no base grid:
+    multigrid does not apply."""
+    m = gl.box_mesh([0.0, 0.0, 0.0], [4.0, 4.0, 4.0], (4, 4, 4))
+    cells = np.asarray(m.cells).reshape(-1, 8)
+    xyz = np.asarray(m.xyz).reshape(-1, 3)
+    lo_corner = xyz[cells[:, 0]]
+    keep = ~((lo_corner[:, 0] >= 2.0) & (lo_corner[:, 1] >= 2.0))
+    cells = cells[keep]
+    used = np.unique(cells)
+    renum = np.full(m.nn, -1, np.int64)
+    renum[used] = np.arange(used.size)
+    g = gl.Mesh(3, xyz[used], renum[cells].astype(np.int32), np.asarray(m.mask)[used])
+    assert gl.plan_info([g])["n_nodes"] == used.size
+    assert gl.plan_prolongation([g]) is None
+
+
 def test_multigrid_prolongation_declines_graded_grid(gl):
     """A tensor grid with graded spacing is neither a uniform box grid nor a once-refined
     one: multigrid does not apply (the preconditioner falls back to block-Jacobi)."""

@@ -146,9 +146,10 @@ bool infer_box(const glgpu_mesh &m, BoxGeom &g)
   return true;
 }
 
-// A mesh is a once-refined box grid when every cell is an axis-aligned box whose edges are
-// those of the base grid (the largest cell's) on all three axes or half of them on all three
-// axes, the base-size cells start on the base lattice, every node lies on the half lattice,
+// A mesh is a once-refined box grid when its cells fill its bounding box, every cell is an
+// axis-aligned box whose edges are those of the base grid (the largest cell's) on all three
+// axes or half of them on all three axes, the base-size cells start on the base lattice,
+// every node lies on the half lattice,
 // and every constraint row is a hanging-node row or a periodic image (one parent, weight 1,
 // displaced by the box extent along the periodic axes).  g receives the base grid.
 bool infer_refined_box(const glgpu_mesh &m, BoxGeom &g)
@@ -192,6 +193,20 @@ bool infer_refined_box(const glgpu_mesh &m, BoxGeom &g)
         int64_t r;
         if (!half(d, m.xyz[3 * i + d], r)) return false;
       }
+  // the cells must fill the bounding box (an L-shaped lattice domain would leave base-grid
+  // nodes outside the mesh, with empty rows in the coarse operator)
+  {
+    double vol = 0.0;
+    for (int64_t e = 0; e < m.n_cells; ++e)
+      {
+        const int32_t *c = m.cells + 8 * e;
+        double v = 1.0;
+        for (int d = 0; d < 3; ++d) v *= m.xyz[3 * c[7] + d] - m.xyz[3 * c[0] + d];
+        vol += v;
+      }
+    const double box = (g.hi[0] - g.lo[0]) * (g.hi[1] - g.lo[1]) * (g.hi[2] - g.lo[2]);
+    if (std::fabs(vol - box) > 1e-9 * box) return false;
+  }
   for (int64_t e = 0; e < m.n_cells; ++e)
     {
       const int32_t *c = m.cells + 8 * e;
