@@ -296,7 +296,7 @@ def cpu_port_baseline(m, x0, linear_tol):
                       f"oracle port ({nn} Newton its, {gi} block-Jacobi GMRES(50) its, final |F| {res:.2e}, {dt:.1f} s)"}
 
 
-def main():
+def make_parser():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -312,6 +312,8 @@ def main():
                     help="with --ncu-solve: keep the preconditioner while the last step is below this")
     ap.add_argument("--batch", type=int, default=8, help="instances in the batched leg (0 = skip)")
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
+    ap.add_argument("--config4", type=int, default=0,
+                    help="only the full-scale batched sweep: this many seeded slab instances, in waves")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
     ap.add_argument("--ncu-mlp", type=int, default=0, help="profiling case: surrogate forward on N points + one gradient")
     ap.add_argument("--precond", default="mg", choices=["mg", "bj"],
@@ -320,7 +322,11 @@ def main():
                     help="skip the autotuner (the headline then uses the default configuration)")
     ap.add_argument("--headline-start", default="bphase", choices=["bphase", "learned"],
                     help="start of the headline solves (the other start is reported beside it)")
-    args = ap.parse_args()
+    return ap
+
+
+def main():
+    args = make_parser().parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.ncu_case:
         return ncu_case(args.ncu_case, args.fp64)
