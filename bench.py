@@ -113,16 +113,24 @@ def batch_instances(gl, count, seed=4):
     D ~ U(8, 40) xi0 across z (pair-breaking faces), lateral 20 xi0, n^3 Q1 cells with
     n ~ U{16..48}; start = B phase + 0.05 N(0,1)."""
     rng = np.random.default_rng(seed)
-    out = []
-    for k in range(count):
+    pts = []
+    for _ in range(count):
         t = float(rng.uniform(0.3, 0.95))
         p = float(min(rng.uniform(0.0, 34.0), 34.0 - 1e-9))
         D = float(rng.uniform(8.0, 40.0))
         n = int(rng.integers(16, 49))
+        pts.append((t, p, D, n))
+
+    def make(k):
+        t, p, D, n = pts[k]
         m = gl.box_mesh([-10.0, -10.0, -D / 2], [10.0, 10.0, D / 2], (n, n, n))
         x0 = gl.bphase_guess(p, t, m.nn, noise=NOISE, seed=1000 + k)
-        out.append({"t": t, "p": p, "D": D, "n": n, "mesh": m, "x0": x0})
-    return out
+        return {"t": t, "p": p, "D": D, "n": n, "mesh": m, "x0": x0}
+
+    # the meshers release the interpreter lock: build the instances on the host threads
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(make, range(count)))
 
 
 def batched_leg(gl, count, linear_tol, sur=None, precond=None, cfg=None):
