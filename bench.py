@@ -127,8 +127,10 @@ def batch_instances(gl, count, seed=4):
         x0 = gl.bphase_guess(p, t, m.nn, noise=NOISE, seed=1000 + k)
         return {"t": t, "p": p, "D": D, "n": n, "mesh": m, "x0": x0}
 
-    # the meshers release the interpreter lock: build the instances on the host threads
+    # the meshers release the interpreter lock: build the instances on the host threads (the
+    # library is loaded and its signatures set before the threads start)
     from concurrent.futures import ThreadPoolExecutor
+    gl.lib()
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
         return list(ex.map(make, range(count)))
 
