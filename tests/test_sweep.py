@@ -2,7 +2,6 @@
 import importlib
 
 import numpy as np
-
 import pytest
 
 sweep = importlib.import_module("verkko-hem-repo_gb300.sweep")
