@@ -309,7 +309,7 @@ def _trilinear(x):
     return 1.5 + 0.3 * x[:, 0] - 0.7 * x[:, 1] + 0.2 * x[:, 2] + 0.05 * x[:, 0] * x[:, 1] * x[:, 2]
 
 
-@pytest.mark.parametrize("kind", ["uniform", "band", "flags", "periodic_band", "batch"])
+@pytest.mark.parametrize("kind", ["uniform", "band", "flags", "periodic_band", "periodic_flags", "batch"])
 def test_multigrid_prolongation_reproduces_q1(gl, kind):
     """The first multigrid transfer: a once-refined box gets its unrefined grid as first coarse
     level, and P interpolates that grid's Q1 field at the fine nodes.  A trilinear field
@@ -326,6 +326,13 @@ def test_multigrid_prolongation_reproduces_q1(gl, kind):
         meshes = [gl.box_mesh_refine(lo, hi, n, flags)]
     elif kind == "periodic_band":
         meshes = [gl.box_mesh(lo, hi, n, refine_band=0.9, periodic_xy=(1, 1))]
+    elif kind == "periodic_flags":
+        # refined cells on both faces of each periodic axis (mirrored, as periodicity needs):
+        # hanging nodes on the periodic faces resolve through the images
+        flags = np.zeros(np.prod(n), np.int8)
+        for i, j, k in ((0, 1, 1), (n[0] - 1, 1, 1), (2, 0, 0), (2, n[1] - 1, 0)):
+            flags[(k * n[1] + j) * n[0] + i] = 1
+        meshes = [gl.box_mesh_refine(lo, hi, n, flags, periodic_xy=(1, 1))]
     else:
         meshes = [gl.box_mesh(lo, hi, n, refine_band=0.9), gl.cube_mesh(2.0, 4)]
     out = gl.plan_prolongation(meshes)
@@ -334,9 +341,9 @@ def test_multigrid_prolongation_reproduces_q1(gl, kind):
     xf = np.concatenate([np.asarray(m.xyz).reshape(-1, 3) for m in meshes])
     hp = np.concatenate([np.diff(np.asarray(m.hptr)) if m.hptr is not None else np.zeros(m.nn, int) for m in meshes])
     nco = xc.shape[0]
-    if kind in ("band", "flags", "periodic_band"):
+    if kind in ("band", "flags", "periodic_band", "periodic_flags"):
         assert nco == (n[0] + 1) * (n[1] + 1) * (n[2] + 1) and hp.sum() > 0
-    f = (lambda x: 1.0 + 0.4 * x[:, 2] ** 0 * x[:, 2]) if kind == "periodic_band" else _trilinear
+    f = (lambda x: 1.0 + 0.4 * x[:, 2]) if kind.startswith("periodic") else _trilinear
     rows = np.repeat(np.arange(ptr.size - 1), np.diff(ptr))
     Pf = np.bincount(rows, weights=w * f(xc)[idx], minlength=ptr.size - 1)
     free = hp == 0
