@@ -48,6 +48,39 @@ def test_driver_reads_configuration(driver, tmp_path):
     assert "linear tol 0.0001, converge accuracy 1e-10" in out.stdout
 
 
+PDW_SLAB = """# the periodic slab of the weak-coupling PDW scenario
+subsection physical parameters
+  set pressure in bar = 22.0
+  set t_reduced = 0.5
+  set amplitude u parameter = 0.8
+end
+subsection control parameters
+  set half x length of retangle = 6.0
+  set half y length of retangle = 4.0
+  set half z length of retangle = 3.0
+  set Number of initial global refinments = 3
+end
+"""
+
+
+def test_driver_pdw_slab_scenario_reads_configuration(driver, tmp_path):
+    out = subprocess.run([driver, _write(tmp_path, PDW_SLAB), "--scenario", "pdw-slab", "--dry-run"],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert "periodic slab 12 x 8 x 6 (x, y periodic), 8^3 cells, PDW start u = 0.8" in out.stdout
+    # the declared defaults: half lengths 20, u = 1
+    out = subprocess.run([driver, _write(tmp_path, "subsection physical parameters\nend\n"), "--scenario",
+                          "pdw-slab", "--dry-run"], capture_output=True, text=True)
+    assert out.returncode == 0 and "periodic slab 40 x 40 x 40 (x, y periodic), 16^3 cells, PDW start u = 1" in out.stdout
+    bad = PDW_SLAB.replace("half y length of retangle = 4.0", "half y length of retangle = 0")
+    r = subprocess.run([driver, _write(tmp_path, bad, "bad.prm"), "--scenario", "pdw-slab", "--dry-run"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "half lengths" in r.stderr
+    r = subprocess.run([driver, _write(tmp_path, PDW_SLAB), "--scenario", "sphere", "--dry-run"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "unknown scenario" in r.stderr
+
+
 def test_driver_defaults_and_errors(driver, tmp_path):
     # unset keys take the reference's declared defaults (cube half side 20, 2^4 cells)
     out = subprocess.run([driver, _write(tmp_path, "subsection physical parameters\nend\n"), "--dry-run"],

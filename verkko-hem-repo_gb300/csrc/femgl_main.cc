@@ -1,13 +1,20 @@
 // femgl_gb300: host driver for the GPU Newton path, a stand-in for the reference's
-// sol/src/main.cc + FemGL<3>::run (femgl/src/run.cc:110-258) on the cube geometry of
-// femgl/src/makegrid_cube-z-normal_AdGR.cc.
+// sol/src/main.cc + FemGL<3>::run (femgl/src/run.cc:110-258) on two of its scenarios (the
+// reference picks make_grid / setup_system by linking one source of each, here --scenario):
+//   cube      femgl/src/makegrid_cube-z-normal_AdGR.cc + setup_uniform_B-phase.cc
+//   pdw-slab  femgl/src/makegrid_retangle-z-AdGR_xy-periodic.cc +
+//             setup_weak-coupling-PDW-configuration.cc: the rectangle of half lengths "half x /
+//             y / z length of retangle", 2^r cells per axis, x and y faces periodic, z faces
+//             pair-breaking, and the PDW start of amplitude "amplitude u parameter" across the
+//             slab (pdw_config.h:111-298), without noise.
 //
 // It reads the reference's configuration file format (deal.II ParameterHandler text:
 // "subsection <name>", "set <key> = <value>", "end", '#' comments) with the keys and
 // defaults of confreader/src/declare.cc:115-290, builds the 2^r x 2^r x 2^r cube of side
-// 2 * "cube half side length" (pair-breaking z faces), evaluates the material parameters
-// at (p, t), starts from the uniform B phase (setup_uniform_B-phase.cc:238-263, plus
-// optional seeded Gaussian noise), and runs the Newton loop through the C ABI of
+// 2 * "cube half side length" (pair-breaking z faces) or the periodic slab, evaluates the
+// material parameters at (p, t), starts from the uniform B phase (setup_uniform_B-phase.cc:
+// 238-263, plus optional seeded Gaussian noise) or the PDW state, and runs the Newton loop
+// through the C ABI of
 // include/glgpu.h: assemble_system, solve(tol of the cycle), newton_iteration, stop at
 // |R| <= "converge accuracy".  Refinement cycles follow run.cc:156-256: a cycle ends when
 // its residual stalls (change below "Cycle c refinement threshold") or converges; the next
@@ -15,11 +22,13 @@
 // estimate, the "adaptive refinment ratio" of cells with the largest estimates refined
 // once, refine.cc:131-176) and transfers the solution.  The host mesher supports one
 // adaptive level on top of any number of global ones; a further adaptive cycle ends the
-// cycle loop with a note.
+// cycle loop with a note.  On the periodic slab a cell flagged next to a periodic face also
+// flags its image cell across the box (the mesher refines both faces of a periodic pair
+// alike), so a few more cells than the fixed number may be refined.
 //
-// usage: femgl_gb300 [configuration.prm] [--precision mixed|fp64]
-//                    [--precond mg|bj|cheb|none] [--noise sigma] [--seed s]
-//                    [--out solution.bin] [--dry-run]
+// usage: femgl_gb300 [configuration.prm] [--scenario cube|pdw-slab]
+//                    [--precision mixed|fp64] [--precond mg|bj|cheb|none]
+//                    [--noise sigma] [--seed s] [--out solution.bin] [--dry-run]
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -53,6 +62,9 @@ struct Config
       {std::string(phys) + "trun on Strong Coupling Correction", "true"},
       {std::string(phys) + "amplitude u parameter", "1.0"},
       {std::string(ctrl) + "cube half side length", "20"},
+      {std::string(ctrl) + "half x length of retangle", "20"},
+      {std::string(ctrl) + "half y length of retangle", "20"},
+      {std::string(ctrl) + "half z length of retangle", "20"},
       {std::string(ctrl) + "Number of refinements", "4"},
       {std::string(ctrl) + "Number of interations", "40"},
       {std::string(ctrl) + "Cycle 0 refinement threshold", "1.0e0"},
@@ -169,7 +181,7 @@ int main(int argc, char **argv)
   int precision = GLGPU_MIXED, precond = GLGPU_PC_MULTIGRID;
   double noise = 0.0;
   uint64_t seed = 0;
-  bool dry = false;
+  bool dry = false, pdw = false;
   for (int i = 1; i < argc; ++i)
     {
       const std::string a = argv[i];
@@ -193,6 +205,16 @@ int main(int argc, char **argv)
                   : v == "cheb" ? GLGPU_PC_CHEBYSHEV
                   : v == "none" ? GLGPU_PC_NONE
                                 : GLGPU_PC_MULTIGRID;
+        }
+      else if (a == "--scenario")
+        {
+          const std::string v = next("--scenario");
+          if (v != "cube" && v != "pdw-slab")
+            {
+              std::fprintf(stderr, "femgl_gb300: unknown scenario %s (cube, pdw-slab)\n", v.c_str());
+              return 2;
+            }
+          pdw = v == "pdw-slab";
         }
       else if (a == "--noise")
         noise = std::strtod(next("--noise").c_str(), nullptr);
@@ -222,6 +244,9 @@ int main(int argc, char **argv)
   const bool scc = conf.flag(P + "trun on Strong Coupling Correction");
   const double bt = conf.num(P + "AdGR diffuse length");
   const double half = conf.num(C + "cube half side length");
+  const double half_r[3] = {conf.num(C + "half x length of retangle"), conf.num(C + "half y length of retangle"),
+                            conf.num(C + "half z length of retangle")};
+  const double amp_u = conf.num(P + "amplitude u parameter");
   const int nref = static_cast<int>(conf.num(C + "Number of initial global refinments"));
   const int n_iter = static_cast<int>(conf.num(C + "Number of interations"));
   const double tol0 = conf.num(C + "Cycle 0 linear solver tol");
@@ -229,8 +254,19 @@ int main(int argc, char **argv)
   const int n_cycles = static_cast<int>(conf.num(C + "Number of refinements"));
   const double ratio = conf.num(C + "adaptive refinment ratio"), coarsen = conf.num(C + "adaptive coarsen ratio");
   int n = 1 << nref;
-  std::printf("femgl_gb300: %s  p = %g bar, t = %g, SCC %s, cube half side %g, %d^3 cells\n", glgpu_version(), p, t,
-              scc ? "on" : "off", half, n);
+  if (pdw)
+    std::printf("femgl_gb300: %s  p = %g bar, t = %g, SCC %s, periodic slab %g x %g x %g (x, y periodic), %d^3 "
+                "cells, PDW start u = %g\n", glgpu_version(), p, t, scc ? "on" : "off", 2 * half_r[0], 2 * half_r[1],
+                2 * half_r[2], n, amp_u);
+  else
+    std::printf("femgl_gb300: %s  p = %g bar, t = %g, SCC %s, cube half side %g, %d^3 cells\n", glgpu_version(), p,
+                t, scc ? "on" : "off", half, n);
+  for (int d = 0; d < 3 && pdw; ++d)
+    if (!(half_r[d] > 0.0))
+      {
+        std::fprintf(stderr, "femgl_gb300: the half lengths of the rectangle must be > 0\n");
+        return 2;
+      }
   std::printf("  Newton: <= %d iterations, linear tol %g, converge accuracy %g, %s, %s\n", n_iter + 1, tol0, acc,
               precision == GLGPU_FP64 ? "FP64" : "mixed FP32/FP64",
               precond == GLGPU_PC_MULTIGRID ? "multigrid" : precond == GLGPU_PC_BLOCK_JACOBI ? "block-Jacobi"
@@ -263,9 +299,11 @@ int main(int argc, char **argv)
   prm.damped = conf.flag(C + "Using dampped Newton iteration") ? 1 : 0;
   prm.bt = bt;
 
-  // cube with pair-breaking z faces (zero orbital-z column); cells of an adaptive level
-  const double lo[3] = {-half, -half, -half}, hi[3] = {half, half, half};
-  const int dxy[2] = {0, 0};
+  // cube, or the slab with periodic x / y faces; pair-breaking z faces (zero orbital-z column)
+  // either way; cells of an adaptive level
+  const double lo[3] = {pdw ? -half_r[0] : -half, pdw ? -half_r[1] : -half, pdw ? -half_r[2] : -half};
+  const double hi[3] = {-lo[0], -lo[1], -lo[2]};
+  const int dxy[2] = {pdw ? 2 : 0, pdw ? 2 : 0};
   struct Mesh
   {
     int nn = 0, nc = 0, nh = 0;
@@ -305,8 +343,9 @@ int main(int argc, char **argv)
   };
   if (!open()) return fail("create");
   std::vector<double> x(18 * static_cast<size_t>(M.nn));
-  if (glgpu_bphase_guess(p, t, scc ? 1 : 0, M.nn, noise, seed, x.data()) || glgpu_set_solution(ctx, x.data()))
-    return fail("initial state");
+  const glgpu_status st0 = pdw ? glgpu_pdw_guess(p, t, scc ? 1 : 0, amp_u, half_r[2], M.nn, M.xyz.data(), x.data())
+                               : glgpu_bphase_guess(p, t, scc ? 1 : 0, M.nn, noise, seed, x.data());
+  if (st0 != GLGPU_OK || glgpu_set_solution(ctx, x.data())) return fail("initial state");
 
   const char *thr_key[4] = {"Cycle 0 refinement threshold", "Cycle 1 refinement threshold",
                             "Cycle 2 refinement threshold", "Cycle 3 refinement threshold"};
@@ -349,6 +388,27 @@ int main(int argc, char **argv)
               flags.resize(M.nc);
               if (glgpu_estimate_error(ctx, nullptr) || glgpu_refine_flags(ctx, ratio, coarsen, flags.data()))
                 return fail("error estimate");
+              // mirror the flags of the cells on periodic faces (cells x fastest), to a fixed point
+              for (bool changed = pdw; changed;)
+                {
+                  changed = false;
+                  auto mark = [&](int i, int j, int k) {
+                    int8_t &f = flags[(static_cast<size_t>(k) * n + j) * n + i];
+                    if (f <= 0)
+                      {
+                        f = 1;
+                        changed = true;
+                      }
+                  };
+                  for (int k = 0; k < n; ++k)
+                    for (int j = 0; j < n; ++j)
+                      for (int i = 0; i < n; ++i)
+                        {
+                          if (flags[(static_cast<size_t>(k) * n + j) * n + i] <= 0) continue;
+                          if (i == 0 || i == n - 1) mark(n - 1 - i, j, k);
+                          if (j == 0 || j == n - 1) mark(i, n - 1 - j, k);
+                        }
+                }
               if (!make_mesh(flags.data())) return fail("mesh");
               adaptive_done = true;
             }
