@@ -181,8 +181,10 @@ glgpu_status glgpu_newton_iteration(glgpu_ctx *ctx, double *res, int *trials);
 
 /*
  * The free energy F = integral of K1|grad A|^2 + (K2+K3) sum_mu |div A_mu|^2
- * + alpha tr(AA^+) + sum_t beta_t I_t at the current solution, per instance (FP64).
- * The reference's residual is (1/2) dF/dx; the reference itself never evaluates F.
+ * + alpha tr(AA^+) + sum_t beta_t I_t at the current solution, per instance, evaluated
+ * with the FP64 kernel in every precision mode (it also leaves the FP64 residual at the
+ * solution in residual_vector).  The reference's residual is (1/2) dF/dx; the reference
+ * itself never evaluates F.
  */
 glgpu_status glgpu_free_energy(glgpu_ctx *ctx, double *F);
 
@@ -191,9 +193,21 @@ glgpu_status glgpu_free_energy(glgpu_ctx *ctx, double *F);
  * up to max_newton+1 times assemble, solve(linear_tol), newton_iteration, stop an
  * instance when its residual <= converge_acc.  Per instance outputs (any may be
  * NULL): newton_its, total GMRES iterations, final residual norm.
+ * The stop test is always taken on an FP64 residual (run.cc:234): in GLGPU_MIXED mode the
+ * line search evaluates |R| in double-float arithmetic, and when that value passes, the
+ * FP64 residual at the accepted state decides; if it misses, Newton takes another step.
+ * final_res is then that FP64 norm.
  */
 glgpu_status glgpu_run(glgpu_ctx *ctx, int max_newton, double linear_tol, double converge_acc, int *newton_its,
                        int *gmres_its, double *final_res);
+
+/*
+ * The last glgpu_run step's residual norms per instance (either pointer may be NULL): the
+ * line search's value (double-float in GLGPU_MIXED mode) and the FP64 value that took the
+ * stop test.  They are equal in GLGPU_FP64 mode.  No reference counterpart: the reference
+ * evaluates every residual in FP64.
+ */
+glgpu_status glgpu_stop_norms(const glgpu_ctx *ctx, double *line_search_norm, double *fp64_norm);
 
 /* Downloads the pattern (rowptr [n_nodes+1], cols [nnzb]) and the Jacobian values
  * as FP64 [nnzb][B][B] (any pointer may be NULL), plus system_rhs [n_nodes*B]. */

@@ -39,8 +39,7 @@ def build(quiet: bool = True) -> None:
     """Compile the oracle restatement (and the reference kernels when the
     reference tree is present)."""
     out = subprocess.DEVNULL if quiet else None
-    subprocess.run(["make", "-s", "-C", HERE], check=True, stdout=out)
-    subprocess.run(["bash", os.path.join(HERE, "refshim", "build_ref.sh")], check=True, stdout=out)
+    subprocess.run(["make", "-s", "-C", HERE, "all", "ref"], check=True, stdout=out)
 
 
 def _p(a, t=_dp):
@@ -71,6 +70,7 @@ def lib():
         L.orc_gmres.restype = ctypes.c_int
         L.orc_gmres.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
                                 _dp]
+        L.orc_bphase_guess.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, _dp]
         _lib = L
     return _lib
 
@@ -110,6 +110,71 @@ def _coef9(coef):
     c = np.zeros(9)
     c[: len(coef)] = coef
     return c
+
+
+MATEP_FIELDS = ("alpha", "beta1", "beta2", "beta3", "beta4", "beta5", "gap_A", "gap_B", "Tc_mK", "f_A", "f_B",
+                "beta_A", "beta_B")
+GOLDEN_MATEP = os.path.join(os.path.dirname(HERE), "tests", "golden", "matep.json")
+
+
+def matep(p: float, t: float, scc: bool = True) -> dict:
+    """The reference's material parameters at (p bar, t = T/Tc): from its own matep
+    (matep/src/matep.cc, compiled unmodified into oracle/_ref) where that was built, else
+    from the committed table of that compiled matep's outputs (tests/golden/matep.json,
+    90 (p, t, SCC) points).  Raises KeyError for a point the table lacks."""
+    R = ref()
+    if R is not None:
+        out = np.zeros(13)
+        R.ref_matep(float(p), float(t), int(bool(scc)), _p(out))
+        return dict(zip(MATEP_FIELDS, out.tolist()))
+    import json
+
+    with open(GOLDEN_MATEP) as fh:
+        rows = json.load(fh)["rows"]
+    for r in rows:
+        if r["p"] == float(p) and r["t"] == float(t) and r["scc"] == int(bool(scc)):
+            return dict(zip(MATEP_FIELDS, r["out"]))
+    raise KeyError(f"matep({p}, {t}, scc={scc}) is not in the golden table and oracle/_ref is not built")
+
+
+def bphase_guess(gap_B: float, nn: int, noise: float = 0.0, seed: int = 0) -> np.ndarray:
+    """Uniform B-phase start (setup_uniform_B-phase.cc:238-259) plus the configurations'
+    seeded noise; not yet distributed through the constraints."""
+    x = np.zeros(18 * int(nn))
+    lib().orc_bphase_guess(float(gap_B), int(nn), float(noise), int(seed), _p(x))
+    return x
+
+
+def time_reference_cells(h, x_cells, coef9, threads: int = 1):
+    """Times the reference's own Jacobian + rhs loop over one Q1 cell at a time
+    (femgl/src/assemble.cc:188-280: q x i x j with the 18 cell_mat_vec kernels, compiled
+    unmodified into oracle/_ref) on the cell states x_cells [n][8][18], spread over
+    `threads` host threads.  coef9 = (K1, K2, K3, alpha, beta1..beta5).  Returns (seconds
+    of wall time, the cell matrices [n][144][144], the cell rhs [n][144]).  Needs oracle/_ref."""
+    import time
+    from concurrent.futures import ThreadPoolExecutor
+
+    R = ref()
+    if R is None:
+        raise RuntimeError("oracle/_ref (the reference's kernels) is not built on this host")
+    h = np.ascontiguousarray(h, np.float64)
+    c9 = np.ascontiguousarray(coef9, np.float64)
+    xs = np.ascontiguousarray(x_cells, np.float64).reshape(-1, 144)
+    n = xs.shape[0]
+    K = np.zeros((n, 144, 144))
+    r = np.zeros((n, 144))
+
+    def one(k):
+        R.ref_cell_assemble(_p(h), _p(xs[k]), _p(c9), _p(K[k]), _p(r[k]))
+
+    t0 = time.perf_counter()
+    if threads <= 1:
+        for k in range(n):
+            one(k)
+    else:  # ctypes releases the interpreter lock for the duration of each call
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(one, range(n)))
+    return time.perf_counter() - t0, K, r
 
 
 # ---------------------------------------------------------------------------------

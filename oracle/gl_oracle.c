@@ -826,3 +826,41 @@ int orc_gmres(int nn, const int *rowptr, const int *cols, const double *J, const
   free(Dinv); free(V); free(z); free(w); free(H); free(cs); free(sn); free(g); free(y);
   return total;
 }
+
+/*
+ * Seeded start vector of the benchmark configurations: the uniform B phase of
+ * femgl/src/setup_uniform_B-phase.cc:238-259 (u11 = u22 = u33 = gap_B * 0.577350269f, the
+ * single-precision literal of :248; everything else 0) plus noise_sigma * N(0,1) per dof.
+ * The reference draws its initial noise from an unseeded std::random_device
+ * (setup_uniform_B-phase.cc:218-220); the configurations need a reproducible draw that
+ * both sides share, so the draw is defined by (seed, dof index) alone: two splitmix64
+ * outputs per dof, Box-Muller.  Constraints are not applied here (the caller distributes).
+ */
+static uint64_t orc_mix64(uint64_t z)
+{
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static double orc_gauss(uint64_t seed, uint64_t index)
+{
+  const uint64_t base = seed * 0x632BE59BD9B4E019ull + 2 * index;
+  const uint64_t a = orc_mix64(base), b = orc_mix64(base + 1);
+  const double u1 = ((double)(a >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+void orc_bphase_guess(double gap_B, int nn, double noise_sigma, uint64_t seed, double *x)
+{
+  const double diag = gap_B * (double)0.577350269f;
+  for (int64_t i = 0; i < nn; ++i)
+    for (int c = 0; c < 18; ++c)
+      {
+        double v = (c == 0 || c == 4 || c == 8) ? diag : 0.0;
+        if (noise_sigma > 0) v += noise_sigma * orc_gauss(seed, (uint64_t)(18 * i + c));
+        x[18 * i + c] = v;
+      }
+}

@@ -5,15 +5,15 @@
 # stand-ins in oracle/refshim/.  TEST INFRASTRUCTURE: the product never links it.
 #
 # Usage: oracle/refshim/build_ref.sh [REFERENCE_ROOT]
-# REFERENCE_ROOT defaults to $GL_REFERENCE, then /root/reference.  Exits 0 and
-# prints "skipped" when the reference tree is absent (the GPU host has none).
+# REFERENCE_ROOT is the argument, else $GL_REFERENCE.  Exits 0 and prints "skipped"
+# when neither names a reference tree.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 ORACLE="$(dirname "$HERE")"
-REF="${1:-${GL_REFERENCE:-/root/reference}}"
+REF="${1:-${GL_REFERENCE:-}}"
 OUT="$ORACLE/_ref"
-if [ ! -d "$REF/femgl/src/cell_mat_vec" ]; then
-  echo "build_ref: reference tree not found at $REF: skipped"
+if [ -z "$REF" ] || [ ! -d "$REF/femgl/src/cell_mat_vec" ]; then
+  echo "build_ref: no reference tree given (argument or GL_REFERENCE): skipped"
   exit 0
 fi
 mkdir -p "$OUT/inc"

@@ -38,10 +38,10 @@ sys.path.insert(0, ROOT)
 
 
 def main(ref_root: str | None = None) -> None:
-    env = dict(os.environ)
+    cmd = ["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"]
     if ref_root:
-        env["GL_REFERENCE"] = ref_root
-    subprocess.run(["bash", os.path.join(ROOT, "oracle", "refshim", "build_ref.sh")], check=True, env=env)
+        cmd.append(f"REFERENCE_ROOT={ref_root}")
+    subprocess.run(cmd, check=True)
     from oracle import gl
 
     R = gl.ref()

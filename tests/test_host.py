@@ -408,3 +408,23 @@ def test_refined_galerkin_stays_in_base_pattern(gl, kind):
     C = sp.csr_matrix((np.ones(ccols.size), ccols, crp), shape=(nc, nc))
     assert G.nnz > 0
     assert np.all(np.asarray(C[G.row, G.col]).ravel() > 0)
+
+
+def test_oracle_start_and_coefficients_equal_the_product(gl, oracle_gl):
+    """The CPU reference arm builds its workload from oracle code alone; its seeded
+    B-phase start and its matep values must be the ones the GPU arm uses."""
+    mp = oracle_gl.matep(20.0, 0.6)
+    got = gl.matep(20.0, 0.6, True)
+    for f in oracle_gl.MATEP_FIELDS:
+        assert mp[f] == got[f], f
+    for seed, noise in ((2, 0.05), (7, 0.0), (1000, 0.3)):
+        a = oracle_gl.bphase_guess(mp["gap_B"], 777, noise, seed)
+        b = gl.bphase_guess(20.0, 0.6, 777, noise=noise, seed=seed)
+        assert np.array_equal(a, b), seed
+
+
+def test_oracle_matep_table_lookup_rejects_untabulated_points(oracle_gl, monkeypatch):
+    monkeypatch.setattr(oracle_gl, "ref", lambda: None)  # the GPU host has no compiled reference
+    assert oracle_gl.matep(20.0, 0.6)["alpha"] == -0.4
+    with pytest.raises(KeyError):
+        oracle_gl.matep(20.5, 0.6)

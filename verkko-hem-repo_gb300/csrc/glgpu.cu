@@ -147,6 +147,9 @@ struct glgpu_ctx
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
+  // per instance, the last glgpu_run step's |R|: the line search's value and the FP64 value
+  // that took the stop test (equal in FP64 mode and in steps that did not pass the test)
+  std::vector<double> stop_ls, stop_fp64;
   bool mf = false;                   // the Krylov operator is applied matrix-free at the state (FP32, 3D)
   float *ycell = nullptr;            // matrix-free scratch [Nc][8][18]
   float *x32 = nullptr;              // FP32 copy of the state the matrix-free operator linearises at
@@ -329,12 +332,14 @@ glgpu_status robin_res(glgpu_ctx *c, const double *v, double *ec, const uint8_t 
 // kernels of one matrix-free operator application: cell, (Robin faces,) gather
 int mf_launches(const glgpu_ctx *c) { return 2 + (c->dm.n_robin > 0 ? 1 : 0); }
 
-// residual at vector v (x or xt) for instances in act: R, e_cell
-// R at v (and the cell free energies when `energy`; the line search needs only |R|)
-glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act, bool energy = false)
+// R at v (x or xt) for the instances in act, and the cell free energies when `energy` (the
+// line search needs only |R|).  Mixed contexts evaluate it in double-float arithmetic unless
+// `fp64`: the FP64 kernel certifies the stop test and gives the free energy.
+glgpu_status residual_at(glgpu_ctx *c, const double *v, const uint8_t *act, bool energy = false, bool fp64 = false)
 {
   double *ec = energy ? c->e_cell : nullptr;
-  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, c->mixed, v, nullptr, c->r_cell, ec, act, c->st); }));
+  const bool df = c->mixed && !fp64;
+  CKS(launch(c, KK_RES, 1, [&] { return launch_cell(c->dm, df, v, nullptr, c->r_cell, ec, act, c->st); }));
   CKS(robin_res(c, v, ec, act));
   CKS(launch(c, KK_RES, 1, [&] { return launch_res_gather(c->dm, c->r_cell, c->R, act, c->st); }));
   return GLGPU_OK;
@@ -1307,6 +1312,8 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   c->res_norm.assign(n_inst, 0.0);
   c->inst_on.assign(n_inst, 1);
   c->r_ok.assign(n_inst, 0);
+  c->stop_ls.assign(n_inst, 0.0);
+  c->stop_fp64.assign(n_inst, 0.0);
   cudaEventCreate(&c->ev_user0);
   cudaEventCreate(&c->ev_user1);
   if (prm[0].precond == GLGPU_PC_MULTIGRID && P.dim == 3)
@@ -1582,7 +1589,7 @@ extern "C" glgpu_status glgpu_newton_iteration(glgpu_ctx *c, double *res, int *t
 extern "C" glgpu_status glgpu_free_energy(glgpu_ctx *c, double *F)
 {
   if (!c || !F) return set_error(GLGPU_ERR_ARG, "glgpu_free_energy: NULL argument");
-  CKS(residual_at(c, c->x, nullptr, true));
+  CKS(residual_at(c, c->x, nullptr, true, true)); // FP64 in every precision mode
   std::fill(c->r_ok.begin(), c->r_ok.end(), 1);
   CKS(launch(c, KK_VEC, 1, [&] { return launch_cell_sum(c->dm, c->e_cell, c->d_energy, c->st); }));
   CK(cudaMemcpyAsync(c->h_norm, c->d_energy, sizeof(double) * c->n_inst, cudaMemcpyDeviceToHost, c->st));
@@ -1725,14 +1732,44 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
       std::vector<double> r;
       std::vector<int> t;
       CKS(newton_impl(c, r, t));
-      bool any = false;
+      bool any = false, cert = false;
+      std::vector<uint8_t> passed(n, 0);
       for (int k = 0; k < n; ++k)
         if (c->inst_on[k])
           {
             nits[k] = it + 1;
             gits[k] += its[k];
             fres[k] = r[k];
+            c->stop_ls[k] = c->stop_fp64[k] = r[k];
             if (r[k] <= converge_acc)
+              {
+                passed[k] = 1;
+                cert |= c->mixed;
+              }
+          }
+      if (cert)
+        {
+          // mixed mode: the line search's double-float |R| passed; the stop test itself is
+          // taken on the FP64 residual at the accepted state (run.cc:234 in FP64).  R then
+          // holds the FP64 values at x, which the next assembly reuses
+          CKS(upload_act(c, c->d_act, passed));
+          CKS(residual_at(c, c->x, c->d_act, false, true));
+          std::vector<double> r64;
+          CKS(norms_d(c, c->R, c->d_act, r64));
+          for (int k = 0; k < n; ++k)
+            if (passed[k])
+              {
+                c->stop_fp64[k] = fres[k] = r64[k];
+                c->res_norm[k] = r64[k];
+                if (!std::isfinite(r64[k]))
+                  return set_error(GLGPU_ERR_NAN, "run: non-finite FP64 residual in instance " + std::to_string(k));
+                if (r64[k] > converge_acc) passed[k] = 0; // one more Newton step
+              }
+        }
+      for (int k = 0; k < n; ++k)
+        if (c->inst_on[k])
+          {
+            if (passed[k])
               c->inst_on[k] = 0;
             else
               any = true;
@@ -1746,6 +1783,14 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
   if (gmres_its) std::copy(gits.begin(), gits.end(), gmres_its);
   if (final_res) std::copy(fres.begin(), fres.end(), final_res);
   return result;
+}
+
+extern "C" glgpu_status glgpu_stop_norms(const glgpu_ctx *c, double *line_search_norm, double *fp64_norm)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_stop_norms: NULL context");
+  if (line_search_norm) std::copy(c->stop_ls.begin(), c->stop_ls.end(), line_search_norm);
+  if (fp64_norm) std::copy(c->stop_fp64.begin(), c->stop_fp64.end(), fp64_norm);
+  return GLGPU_OK;
 }
 
 extern "C" glgpu_status glgpu_get_system(const glgpu_ctx *cc, int32_t *rowptr, int32_t *cols, double *vals,

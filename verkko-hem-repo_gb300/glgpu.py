@@ -88,6 +88,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_newton_iteration.argtypes = [vp, _dp, _ip]
     L.glgpu_free_energy.argtypes = [vp, _dp]
     L.glgpu_run.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _ip, _ip, _dp]
+    L.glgpu_stop_norms.argtypes = [vp, _dp, _dp]
     L.glgpu_get_system.argtypes = [vp, _ip, _ip, _dp, _dp]
     L.glgpu_get_residual.argtypes = [vp, _dp]
     L.glgpu_get_update.argtypes = [vp, _dp]
@@ -533,7 +534,11 @@ class FemGL:
         res = np.zeros(self.n_inst)
         st = _check(lib().glgpu_run(self._ctx, int(max_newton), float(linear_tol), float(converge_acc),
                                     _p(nits, _ip), _p(gits, _ip), _p(res)), (NOT_CONVERGED,) if allow_unconverged else ())
-        return {"newton_its": nits, "gmres_its": gits, "residual": res, "converged": st == 0}
+        ls = np.zeros(self.n_inst)
+        r64 = np.zeros(self.n_inst)
+        _check(lib().glgpu_stop_norms(self._ctx, _p(ls), _p(r64)))
+        return {"newton_its": nits, "gmres_its": gits, "residual": res, "converged": st == 0,
+                "residual_line_search": ls, "residual_fp64": r64}
 
     def free_energy(self) -> np.ndarray:
         out = np.zeros(self.n_inst)
