@@ -305,22 +305,43 @@ def cpu_solves(sysr, x0, linear_tol, budget_s, min_solves=1):
     Returns (seconds per solve, solves, Newton its, GMRES its, threads, final |F|)."""
     from oracle import gl as ogl
 
-    times, hist = [], None
+    times, hist, x = [], None, None
     while len(times) < min_solves or sum(times) < budget_s:
         t0 = time.perf_counter()
-        _, hist = ogl.newton(sysr, x0, tol=TOL, max_iter=40, linear_tol=linear_tol)
+        x, hist = ogl.newton(sysr, x0, tol=TOL, max_iter=40, linear_tol=linear_tol)
         times.append(time.perf_counter() - t0)
         if sum(times) + times[-1] > budget_s:
             break
+    cpu_solves.last_x = x
     return (float(np.mean(times)), len(times), len(hist), sum(h["linear_its"] for h in hist),
             ogl.lib().orc_num_threads(), hist[-1]["res"])
 
 
+def err_vs_oracle(sysr, x_oracle, x_gpu, F_gpu):
+    """The GPU's converged state against the oracle's converged FP64 solve of the same
+    workload: max |x - x_oracle| / max |x_oracle|, the free energies, and the oracle's own
+    FP64 residual norm and free energy at the GPU's state."""
+    from oracle import gl as ogl
+
+    R_o, F_o = sysr.residual(x_gpu)
+    _, F_ref = sysr.residual(x_oracle)
+    xa, _, _ = ogl.gauge_align(x_gpu, x_oracle)
+    return {"x_max_rel": float(np.abs(xa - x_oracle).max() / np.abs(x_oracle).max()),
+            "x_max_rel_unaligned": float(np.abs(x_gpu - x_oracle).max() / np.abs(x_oracle).max()),
+            "x_note": "after the exact global phase and spin rotation that best align the two states (the "
+                      "functional's symmetries, along which the Jacobian is singular at a solution)",
+            "F_rel": abs(F_gpu - F_ref) / abs(F_ref),
+            "oracle_residual_at_gpu_state": float(np.linalg.norm(R_o)),
+            "oracle_F_at_gpu_state_rel": abs(F_gpu - F_o) / abs(F_o),
+            "oracle_solve": "FP64 Newton, block-Jacobi GMRES(50) to the same linear tolerance"}
+
+
 def cpu_port_baseline(linear_tol):
+    """Returns (the oracle system, the oracle's converged x, the cpu_baseline entry)."""
     sysr, x0 = oracle_problem()
     sysr.assemble(sysr.distribute(x0), want_J=False)  # warm-up of the timed object
     dt, ns, nn, gi, thr, res = cpu_solves(sysr, x0, linear_tol, budget_s=20.0)
-    return {"value": 1.0 / dt, "unit": "solves/s", "cores": thr, "kind": "port",
+    return sysr, cpu_solves.last_x, {"value": 1.0 / dt, "unit": "solves/s", "cores": thr, "kind": "port",
             "method": "block-Jacobi GMRES(50) port; compare with this line's mixed_block_jacobi entry (same method "
                       "on the GPU) for the hardware gap alone",
             "sample": f"{ns} complete FP64 Newton solve(s) of the same 32^3 workload on {thr} host threads with "
@@ -385,6 +406,9 @@ def make_parser():
     ap.add_argument("--config3", action="store_true", help="only the refined 64^3 mixed-vs-FP64 leg")
     ap.add_argument("--config4", type=int, default=0,
                     help="only the full-scale batched sweep: this many seeded slab instances, in waves")
+    ap.add_argument("--config5", type=int, nargs=2, default=None, metavar=("N_TRAIN", "N_TEST"),
+                    help="only the learned-start leg at scale: train on N_TRAIN converged states, test on N_TEST "
+                         "held-out 48^3 slab instances")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned initial guess")
     ap.add_argument("--ncu-mlp", type=int, default=0, help="profiling case: surrogate forward on N points + one gradient")
     ap.add_argument("--precond", default="mg", choices=["mg", "bj"],
@@ -423,6 +447,11 @@ def main():
         gl = importlib.import_module("verkko-hem-repo_gb300")
         gl.build()
         print(json.dumps({"config4": config4_leg(gl, args.config4, args.linear_tol)}))
+        return 0
+    if args.config5:
+        gl = importlib.import_module("verkko-hem-repo_gb300")
+        gl.build()
+        print(json.dumps({"config5": config5_leg(gl, args.config5[0], args.config5[1], args.linear_tol)}))
         return 0
     if args.impl == "reference":
         return reference_arm(args, rank)
@@ -597,7 +626,8 @@ def main():
         "batched": batched,
     }
     try:
-        line["cpu_baseline"] = cpu_port_baseline(args.linear_tol)
+        sysr, x_or, line["cpu_baseline"] = cpu_port_baseline(args.linear_tol)
+        line["err_vs_oracle"] = err_vs_oracle(sysr, x_or, mixed["x"], mixed["F"])
     except Exception as e:  # the CPU baseline must not hide the GPU line
         line["cpu_baseline"] = {"value": None, "error": str(e)}
     print(json.dumps(line))
@@ -670,6 +700,59 @@ def config4_leg(gl, count, linear_tol):
             "newton_its_mean": float(r["newton_its"].mean()), "gmres_its_mean": float(r["gmres_its"].mean()),
             "free_energy_rel_diff_vs_fp64_first3": rel,
             "sample": "seeded (seed 4) instances of the sweep: T/Tc~U(0.3,0.95), p~U(0,34), D~U(8,40), n~U{16..48}"}
+
+
+def config5_leg(gl, n_train, n_test, linear_tol, n_test_cells=48):
+    """The learned initial guess at scale: the surrogate is trained on n_train converged
+    slab states (seeded (t, p, D), 8^3-12^3 cells, solved in waves from the uniform B
+    phase), then n_test held-out (t, p, D) slab instances of n_test_cells^3 cells are
+    solved in waves (mixed precision, multigrid) from three starts: the surrogate's guess
+    (inference inside the timed region), the configurations' B phase + 0.05 N(0,1), and
+    the uniform B phase.  Reports solves/s, Newton and GMRES iterations and the
+    free-energy agreement between the starts."""
+    L = importlib.import_module("verkko-hem-repo_gb300.learned")
+    S = importlib.import_module("verkko-hem-repo_gb300.sweep")
+    t0 = time.perf_counter()
+    X, Y, ginfo = L.generate(gl, n_train, seed=11, n_lo=8, n_hi=12, per_instance=512, waves=True)
+    t_gen = time.perf_counter() - t0
+    sur, tinfo = L.train(gl, X, Y, steps=3000, batch=8192, lr=1e-3, seed=0)
+    rng = np.random.default_rng(55)
+    test = []
+    for _ in range(n_test):
+        t = float(rng.uniform(0.3, 0.95))
+        p = float(min(rng.uniform(0.0, 34.0), 34.0 - 1e-9))
+        D = float(rng.uniform(8.0, 40.0))
+        m = gl.box_mesh([-L.L_HALF, -L.L_HALF, -D / 2], [L.L_HALF, L.L_HALF, D / 2], (n_test_cells,) * 3)
+        test.append(L.Instance(t, p, D, n_test_cells, m))
+    prms = [gl.Params.from_matep(d.p, d.t, precision=gl.MIXED, precond=gl.PC_MULTIGRID) for d in test]
+    meshes = [d.mesh for d in test]
+    out = {"train": {"states": ginfo["converged"], "instances": n_train, "rows": tinfo["rows"],
+                     "generation_s": t_gen, "training_s": tinfo["train_s"], "loss": tinfo["loss"],
+                     "components_kept": tinfo["components_kept"]},
+           "test_instances": n_test, "test_cells": n_test_cells}
+    starts = {
+        "learned": lambda: L.guess(gl, sur, test),
+        "bphase_noise": lambda: L.bphase_starts(gl, test, NOISE, 7000),
+        "bphase_uniform": lambda: L.bphase_starts(gl, test, 0.0, 0),
+    }
+    F = {}
+    for name, mk in starts.items():
+        t0 = time.perf_counter()
+        x0 = mk()
+        t_start = time.perf_counter() - t0
+        r = S.solve_sweep(gl, meshes, prms, x0, linear_tol=linear_tol, converge_acc=TOL)
+        solve_s = sum(r["solve_ms"]) / 1000.0
+        F[name] = r["free_energy"]
+        out[name] = {"solves_per_s": n_test / (solve_s + t_start), "start_s": t_start, "solve_s": solve_s,
+                     "newton_its_total": int(r["newton_its"].sum()), "gmres_its_total": int(r["gmres_its"].sum()),
+                     "newton_its_mean": float(r["newton_its"].mean()), "gmres_its_mean": float(r["gmres_its"].mean()),
+                     "all_converged": bool(r["converged"].all()), "max_final_residual": float(r["residual"].max()),
+                     "waves": r["waves"]}
+    sur.close()
+    for name in ("bphase_noise", "bphase_uniform"):
+        out[f"learned_speedup_vs_{name}"] = out["learned"]["solves_per_s"] / out[name]["solves_per_s"]
+        out[f"max_free_energy_rel_diff_vs_{name}"] = float(np.max(np.abs(F["learned"] - F[name]) / np.abs(F[name])))
+    return out
 
 
 def ncu_case(n, fp64):

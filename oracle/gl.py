@@ -177,6 +177,33 @@ def time_reference_cells(h, x_cells, coef9, threads: int = 1):
     return time.perf_counter() - t0, K, r
 
 
+def gauge_align(x, ref, iters: int = 20):
+    """x moved onto ref by the exact symmetries of the functional: a global phase
+    e^{i phi} and a spin rotation R (A -> e^{i phi} R A, acting on the spin index mu of
+    A_{mu j}; the zero-Dirichlet columns stay zero).  The free energy and the residual norm
+    are invariant, and so is the solution set: near a minimum the Jacobian is singular
+    along these directions, so Newton runs that differ only in their linear solves stop at
+    different points of the same orbit.  (phi, R) maximise Re tr(e^{i phi} R C), C = sum
+    over nodes of A B^+ (B the reference), by alternating the phase and the orthogonal
+    Procrustes rotation.  Returns (aligned x, phi, R)."""
+    X = np.asarray(x, np.float64).reshape(-1, 18)
+    Y = np.asarray(ref, np.float64).reshape(-1, 18)
+    A = (X[:, :9] + 1j * X[:, 9:]).reshape(-1, 3, 3)
+    B = (Y[:, :9] + 1j * Y[:, 9:]).reshape(-1, 3, 3)
+    C = np.einsum("nij,nkj->ik", A, B.conj())  # sum_n A_n B_n^+
+    R = np.eye(3)
+    phi = 0.0
+    for _ in range(iters):
+        phi = -float(np.angle(np.trace(R @ C)))
+        M = np.real(np.exp(1j * phi) * C)  # maximise tr(R M)
+        U, _, Vt = np.linalg.svd(M)
+        D = np.diag([1.0, 1.0, np.sign(np.linalg.det(Vt.T @ U.T))])
+        R = Vt.T @ D @ U.T
+    Al = np.exp(1j * phi) * np.einsum("ij,njk->nik", R, A)
+    out = np.concatenate([Al.real.reshape(-1, 9), Al.imag.reshape(-1, 9)], axis=1).reshape(-1)
+    return out, phi, R
+
+
 # ---------------------------------------------------------------------------------
 # per-q and per-cell physics
 # ---------------------------------------------------------------------------------

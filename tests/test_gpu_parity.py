@@ -208,10 +208,11 @@ def test_batched_instances_match_single(gl):
         assert abs(Fb[k] - Fs) <= 1e-10 * abs(Fs)
 
 
-@pytest.mark.parametrize("n,L", [(16, 1.0), (24, 10.0)])
+@pytest.mark.parametrize("n,L", [(16, 1.0), (24, 10.0), (64, 1.0), (64, 10.0)])
 def test_complexgl_2d_matches_oracle(gl, oracle_gl, n, L):
-    """complexGL 2D (config 1 geometry at L = 1, where the normal state psi = 0 is the
-    stable solution; and L = 10, where the ordered state |psi|^2 = -alpha/beta forms)."""
+    """complexGL 2D: the benchmark configuration (64 x 64 Q1 on the unit square, where
+    the normal state psi = 0 is the stable solution), smaller grids, and L = 10, where
+    the ordered state |psi|^2 = -alpha/beta forms."""
     from oracle import mesh as om
 
     m = gl.square_mesh(n, L)

@@ -66,18 +66,24 @@ def test_training_reduces_loss(gl):
 
 
 def test_learned_guess_speeds_up_newton(gl):
-    """Trained on converged slab states, the surrogate start needs fewer Newton steps
-    than the B-phase start on held-out (t, p, D) instances, and reaches the same
-    converged free energy (the plain-Newton fallback covers any failure)."""
+    """Trained on converged slab states, the surrogate start needs fewer Newton steps and
+    fewer GMRES iterations in total than the B-phase start (+0.05 N(0,1), the benchmark
+    configurations' start) on held-out (t, p, D) instances, takes less device time, and
+    reaches the same converged free energy (the plain-Newton fallback covers any failure)."""
     import importlib
 
     L = importlib.import_module("verkko-hem-repo_gb300.learned")
-    X, Y, info = L.generate(gl, 12, seed=11, n_lo=8, n_hi=10, per_instance=1024)
-    s, tinfo = L.train(gl, X, Y, steps=800, batch=4096, lr=1e-3, seed=0)
+    X, Y, info = L.generate(gl, 24, seed=11, n_lo=8, n_hi=10, per_instance=1024)
+    s, tinfo = L.train(gl, X, Y, steps=1500, batch=4096, lr=1e-3, seed=0)
+    assert tinfo["components_kept"] < 18  # the symmetry zeros of the training states
     test = L.sample(gl, 4, seed=99, n_lo=10, n_hi=12)
-    _, ob, _ = L.solve(gl, test, L.bphase_starts(gl, test, 0.05, 5), gl.MIXED)
-    _, ol, _, finfo = L.solve_learned(gl, s, test, gl.MIXED)
+    L.solve(gl, test, L.bphase_starts(gl, test, 0.05, 5), gl.MIXED)  # warm-up
+    _, ob, ms_b = L.solve(gl, test, L.bphase_starts(gl, test, 0.05, 5), gl.MIXED)
+    _, ol, ms_l, finfo = L.solve_learned(gl, s, test, gl.MIXED)
     s.close()
     assert np.all(ob["residual"] <= 1e-10) and np.all(ol["residual"] <= 1e-10)
+    assert finfo["fallbacks"] == 0
     assert ol["newton_its"].sum() < ob["newton_its"].sum(), (ol["newton_its"], ob["newton_its"])
+    assert ol["gmres_its"].sum() < ob["gmres_its"].sum(), (ol["gmres_its"], ob["gmres_its"])
+    assert ms_l < ms_b, (ms_l, ms_b)
     assert np.allclose(ol["free_energy"], ob["free_energy"], rtol=1e-9)

@@ -90,15 +90,35 @@ def test_solve_sweep_bookkeeping():
     x0 = [np.full(18 * n, 0.5 * k) for k, n in enumerate(sizes)]
     _FakeGL.created = []
     r = sweep.solve_sweep(_FakeGL, meshes, params, x0, budget=100 * 1.1 * 12, keep_solutions=True)
-    # the probe is the largest instance; each wave holds at most 12 nodes (budget / margin)
-    assert _FakeGL.created[0] == [1]
-    waves = _FakeGL.created[1:]
+    # the probes are the largest and the smallest instance; each wave holds at most 12
+    # nodes (budget / margin)
+    assert _FakeGL.created[0] == [1] and _FakeGL.created[1] == [4]
+    waves = _FakeGL.created[2:]
     assert [i for w in waves for i in w] == params and r["waves"] == [len(w) for w in waves]
     assert all(sum(sizes[i] for i in w) <= 12 for w in waves)
     assert np.array_equal(r["newton_its"], params) and np.array_equal(r["free_energy"], params)
     for k, s in enumerate(r["solutions"]):
         assert np.array_equal(s, np.full(18 * sizes[k], 0.5 * k + k))
-    assert r["converged"].all() and r["bytes_per_node"] == 100.0
+    assert r["converged"].all() and r["bytes_per_node"] == 100.0 and r["bytes_per_instance"] == 0.0
     assert [int(r["wave"][i]) for i in params] == [j for j, w in enumerate(waves) for _ in w]
     with pytest.raises(ValueError):
         sweep.solve_sweep(_FakeGL, meshes, params, x0[:-1])
+
+
+def test_footprint_fits_a_constant_per_instance():
+    """Small instances carry fixed costs (coarse levels, Krylov bookkeeping): the fit
+    through the largest and the smallest probe recovers constant and slope, and the waves
+    charge the constant to every instance."""
+
+    class GL(_FakeGL):
+        class FemGL(_FakeGL.FemGL):
+            def __init__(self, meshes, params):
+                super().__init__(meshes, params)
+                self.device_bytes = 5000 * len(self.meshes) + 100 * sum(m.nn for m in self.meshes)
+
+    meshes = [_FakeMesh(n) for n in (40, 2, 10, 25)]
+    slope, const = sweep.footprint(GL, meshes, [0, 1, 2, 3])
+    assert slope == pytest.approx(100.0) and const == pytest.approx(5000.0)
+    # budget 16000: with the constant, at most two instances of <= 25 nodes share a wave
+    waves = sweep.plan_waves([25, 2, 10, 25], slope, 16000.0, const)
+    assert waves == [[0, 1], [2, 3]]

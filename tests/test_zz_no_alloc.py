@@ -68,3 +68,42 @@ def test_dot_noalloc_matches_context_norm_twice():
     finally:
         rt.cudaFree(d_vec)
         rt.cudaFree(d_out)
+
+
+@pytest.mark.parametrize("n", [0, 1_000_003, MAX_N])
+def test_dot_noalloc_sizes_against_host_dot(n):
+    """Lengths the first test does not reach: none, a large ragged last segment (more
+    than 256 partials, so each lane of the final pass sums several) and the maximum.
+    Checked against an exactly rounded host sum, within 1e-12 of sum |x_i y_i|, and
+    bitwise equal over two calls on the same data (the reduction order is fixed)."""
+    gl = product()
+    L = gl.lib()
+    rt = _cudart()
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n)
+    y = rng.standard_normal(n)
+    d_x, d_y, d_out = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(d_x), max(8, 8 * n)) == 0
+    assert rt.cudaMalloc(ctypes.byref(d_y), max(8, 8 * n)) == 0
+    assert rt.cudaMalloc(ctypes.byref(d_out), 8) == 0
+    try:
+        if n:
+            assert rt.cudaMemcpy(d_x, x.ctypes.data, 8 * n, H2D) == 0
+            assert rt.cudaMemcpy(d_y, y.ctypes.data, 8 * n, H2D) == 0
+        got = []
+        for _ in range(2):
+            st = L.glgpu_dot_noalloc(d_x, d_y, n, d_out, None)
+            assert st == 0, L.glgpu_last_error().decode()
+            out = np.zeros(1)
+            assert rt.cudaMemcpy(out.ctypes.data, d_out, 8, D2H) == 0
+            got.append(out[0])
+        exact = math.fsum((x * y).tolist()) if n else 0.0
+        scale = float(np.abs(x * y).sum()) if n else 0.0
+        assert abs(got[0] - exact) <= 1e-12 * scale, (got[0], exact)
+        assert got[0] == got[1]
+        if n == 0:
+            assert got[0] == 0.0
+    finally:
+        rt.cudaFree(d_x)
+        rt.cudaFree(d_y)
+        rt.cudaFree(d_out)

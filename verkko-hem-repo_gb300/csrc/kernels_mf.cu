@@ -24,11 +24,16 @@
 
 namespace glgpu
 {
-// cells per CTA (NC = 4, 8 or 16, a run-time choice): 8 NC (cell, point) pairs and 24 NC
-// threads (3 per point in the Hessian-vector product)
+// cells per CTA (NC = 4, 8 or 16, a run-time choice); 16 NC threads: two per Gauss point in
+// the Hessian-vector product, one per (cell, component pair) in the interpolation and the
+// contraction.  A component pair is (c, c + 9) = (u_c, v_c), the real and imaginary part of
+// one entry of A: the pair is one float2 and its arithmetic runs as packed FP32x2
+// (fma.rn.f32x2), two lanes per instruction.
 constexpr float kGaF = 0.21132486540518711775f; // Gauss point 1/2 - sqrt(3)/6 on [0, 1]
 constexpr float kGbF = 0.78867513459481288225f;
 
+// Shared layouts: per point the 9 complex entries in pair order [2 k + part] (k = 3 mu + j),
+// padded to 20 floats (80 bytes, so a point's row loads as 16-byte vectors).
 template <int NC> struct MfSmem
 {
   union
@@ -38,24 +43,65 @@ template <int NC> struct MfSmem
       float zs[NC][8][18]; // nodal values of the direction (gather -> interpolation)
       float xs[NC][8][18]; // nodal values of the state
     } g;
-    float part[3][NC * 8][18]; // H Z per point, in three partial sums (product -> contraction)
+    float part[2][NC * 8][20]; // H Z per point, two partial sums (product -> contraction)
   } u;
-  float Z[NC * 8][19];
-  float X[NC * 8][19]; // the state A at the points
-  float gZ[NC * 8][3][18];
+  float X[NC * 8][20]; // the state A at the points
+  float Z[NC * 8][20]; // the direction Z at the points
+  float gZ[NC * 8][3][18]; // dZ / dx_k at the points, pair order
   float ih[NC][3];
   float jxw[NC];
   float K1[NC], K23[NC];
   float bulk[NC][6]; // alpha, beta1..beta5
 };
 
-__device__ __forceinline__ void gauss2f(float f0, float f1, float &q0, float &q1)
+using C2 = float2; // complex (re, im), or a component pair (u_c, v_c)
+
+__device__ __forceinline__ C2 c2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ C2 add2(C2 a, C2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ C2 sub2(C2 a, C2 b) { return __fadd2_rn(a, c2(-b.x, -b.y)); }
+__device__ __forceinline__ C2 scl2(C2 a, float s) { return __fmul2_rn(a, c2(s, s)); }
+// c + a s, s real (both lanes)
+__device__ __forceinline__ C2 macr(C2 a, float s, C2 c) { return __ffma2_rn(a, c2(s, s), c); }
+// c + a b, complex
+__device__ __forceinline__ C2 cmac(C2 a, C2 b, C2 c)
 {
-  q0 = kGbF * f0 + kGaF * f1;
-  q1 = kGaF * f0 + kGbF * f1;
+  c = __ffma2_rn(c2(a.x, a.x), b, c);
+  return __ffma2_rn(c2(-a.y, a.y), c2(b.y, b.x), c);
+}
+// c + a conj(b)
+__device__ __forceinline__ C2 cmacc(C2 a, C2 b, C2 c)
+{
+  c = __ffma2_rn(c2(a.x, a.x), c2(b.x, -b.y), c);
+  return __ffma2_rn(c2(a.y, a.y), c2(b.y, b.x), c);
+}
+// Gauss values of a linear function with end values f0, f1
+__device__ __forceinline__ void gauss2(C2 f0, C2 f1, C2 &q0, C2 &q1)
+{
+  q0 = __ffma2_rn(f0, c2(kGbF, kGbF), __fmul2_rn(f1, c2(kGaF, kGaF)));
+  q1 = __ffma2_rn(f0, c2(kGaF, kGaF), __fmul2_rn(f1, c2(kGbF, kGbF)));
 }
 
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void load_c9(const float *row, C2 (&a)[9])
+{
+  const float4 *v = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    {
+      const float4 t = v[k];
+      a[2 * k] = c2(t.x, t.y);
+      a[2 * k + 1] = c2(t.z, t.w);
+    }
+  const float2 t = reinterpret_cast<const float2 *>(row)[8];
+  a[8] = t;
+}
+
+__device__ __forceinline__ void store_c9(float *row, const C2 (&a)[9])
+{
+  float4 *v = reinterpret_cast<float4 *>(row);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = make_float4(a[2 * k].x, a[2 * k].y, a[2 * k + 1].x, a[2 * k + 1].y);
+  reinterpret_cast<float2 *>(row)[8] = a[8];
+}
 
 // ---------------------------------------------------------------------------------
 // The bulk Hessian applied to a direction without forming it.  With A = u + i v the 3x3
@@ -69,275 +115,231 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) { return static_cas
 //   dG_5 = (S + S^+) A + Q^* F,     S = F^* A^T
 // (G_t = (1/2) d I_t / dA^*, I_1 = |tr A A^T|^2, I_2 = (tr A A^+)^2, I_3 = tr(A A^T (A A^T)^*),
 // I_4 = tr((A A^+)^2), I_5 = tr(A A^+ (A A^+)^*): femgl/src/cell_mat_vec/cell_mat_lhs_beta*.cc).
-// FP32 complex 3x3 algebra in registers; every index is a compile-time constant.
+// Grouped by the right factor (w_t = 2 beta_t):
+//   H F = Y1 A + Y2 A^* + M F + N F^*
+//   Y1 = w4 (S4 + S4^+) + w5 (S4^* + S4^T) + w2 dq 1,  S4 = F A^+
+//   Y2 = w3 (S3 + S3^T) + w1 dp 1,                     S3 = A F^T
+//   M  = (alpha + w2 q) 1 + w4 Q + w5 Q^*,   N = w3 P + w1 p 1,
+// and with A = Ar + i Ai, F = Fr + i Fi (real 3x3 matrices)
+//   Y1 A + Y2 A^* = (Y1 + Y2) Ar + i (Y1 - Y2) Ai,   M F + N F^* = (M + N) Fr + i (M - N) Fi:
+// four complex-by-real 3x3 products, 27 packed FMAs each.  Role 0 forms the direction-
+// dependent Y1, Y2 and their products with A; role 1 the state-only M, N and their products
+// with F.  Both write their share of H F; the contraction adds the two.
 // ---------------------------------------------------------------------------------
-struct Cf
+template <int ROLE>
+__device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], const float *cf, C2 (&out)[9])
 {
-  float r, i;
-};
-__device__ __forceinline__ Cf cm(Cf a, Cf b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
-__device__ __forceinline__ Cf cma(Cf a, Cf b, Cf acc) // acc + a b
-{
-  return {fmaf(a.r, b.r, fmaf(-a.i, b.i, acc.r)), fmaf(a.r, b.i, fmaf(a.i, b.r, acc.i))};
-}
-__device__ __forceinline__ Cf cj(Cf a) { return {a.r, -a.i}; }
-using M3 = Cf[3][3];
-
-__device__ __forceinline__ void load_m3(const float *a, M3 &A)
-{
-#pragma unroll
-  for (int k = 0; k < 9; ++k) A[k / 3][k % 3] = {a[k], a[9 + k]};
-}
-// out += w D
-__device__ __forceinline__ void acc_m3(const M3 &D, float w, float (&out)[18])
-{
-#pragma unroll
-  for (int k = 0; k < 9; ++k)
+  const float w1 = 2.f * cf[1], w2 = 2.f * cf[2], w3 = 2.f * cf[3], w4 = 2.f * cf[4], w5 = 2.f * cf[5];
+  const float wp = w4 + w5, wm = w4 - w5;
+  C2 L[9], R[9]; // left factors of the real and imaginary parts
+  if constexpr (ROLE == 0)
     {
-      out[k] = fmaf(w, D[k / 3][k % 3].r, out[k]);
-      out[9 + k] = fmaf(w, D[k / 3][k % 3].i, out[9 + k]);
-    }
-}
-// C = op_a(X) op_b(Y) with op: 0 plain, 1 transpose, 2 conjugate, 3 conjugate transpose
-template <int OA, int OB> __device__ __forceinline__ void mm3(const M3 &X, const M3 &Y, M3 &C)
-{
+      C2 dp = c2(0.f, 0.f);
+      float dq = 0.f;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      {
-        Cf acc = {0.f, 0.f};
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          {
-            Cf x = (OA & 1) ? X[k][i] : X[i][k];
-            if (OA & 2) x = cj(x);
-            Cf y = (OB & 1) ? Y[j][k] : Y[k][j];
-            if (OB & 2) y = cj(y);
-            acc = cma(x, y, acc);
-          }
-        C[i][j] = acc;
-      }
-}
-
-// out += w op_a(X) op_b(Y), packed like A (no 3x3 temporary)
-template <int OA, int OB> __device__ __forceinline__ void mm3_acc(const M3 &X, const M3 &Y, float w, float (&out)[18])
-{
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      {
-        Cf acc = {0.f, 0.f};
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          {
-            Cf x = (OA & 1) ? X[k][i] : X[i][k];
-            if (OA & 2) x = cj(x);
-            Cf y = (OB & 1) ? Y[j][k] : Y[k][j];
-            if (OB & 2) y = cj(y);
-            acc = cma(x, y, acc);
-          }
-        out[3 * i + j] = fmaf(w, acc.r, out[3 * i + j]);
-        out[9 + 3 * i + j] = fmaf(w, acc.i, out[9 + 3 * i + j]);
-      }
-}
-
-// terms of thread group G for the point with state a and direction f: out = the group's
-// share of alpha f + sum_t 2 beta_t dG_t[f].  dG_4 and dG_5 are evaluated together: with
-// S = F A^+ the matrix of dG_5 is conj(S) (F^* A^T = conj(F A^+)), and both terms multiply A and
-// F from the right, so
-//   w4 dG_4 + w5 dG_5 = [w4 (S + S^+) + w5 (conj(S) + S^T)] A + (w4 Q + w5 Q^*) F.
-// G = 0: alpha f + dG_3;  G = 1: dG_1 and the A-product of dG_4, dG_5;  G = 2: dG_2 and their
-// F-product.
-template <int G>
-__device__ __forceinline__ void hvp_part(const float (&a)[18], const float (&f)[18], const float *cf, float (&out)[18])
-{
-  M3 A, F, S, X;
-  load_m3(a, A);
-  load_m3(f, F);
-  if constexpr (G == 0)
-    {
-#pragma unroll
-      for (int k = 0; k < 18; ++k) out[k] = cf[0] * f[k];
-      // dG_3 = (S + S^T) A^* + P F^*, S = A F^T, P = A A^T
-      const float w3 = 2.f * cf[3];
-      mm3<0, 1>(A, F, S);
+      for (int k = 0; k < 9; ++k)
+        {
+          dp = cmac(A[k], F[k], dp);
+          dq = fmaf(A[k].x, F[k].x, fmaf(A[k].y, F[k].y, dq));
+        }
+      // Y2 in L: S3 = A F^T, symmetrised
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) X[i][j] = {S[i][j].r + S[j][i].r, S[i][j].i + S[j][i].i};
-      mm3_acc<0, 2>(X, A, w3, out);
-      mm3<0, 1>(A, A, S); // P
-      mm3_acc<0, 2>(S, F, w3, out);
+        for (int j = 0; j < 3; ++j)
+          {
+            C2 acc = c2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc = cmac(A[3 * i + k], F[3 * j + k], acc);
+            L[3 * i + j] = acc;
+          }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        {
+#pragma unroll
+          for (int j = i + 1; j < 3; ++j)
+            {
+              const C2 s = scl2(add2(L[3 * i + j], L[3 * j + i]), w3);
+              L[3 * i + j] = s;
+              L[3 * j + i] = s;
+            }
+          L[4 * i] = __ffma2_rn(L[4 * i], c2(2.f * w3, 2.f * w3), scl2(dp, 2.f * w1));
+        }
+      // Y1 in R: S4 = F A^+; Re part (w4 + w5)(Sr + Sr^T), Im part (w4 - w5)(Si - Si^T)
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          {
+            C2 acc = c2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc = cmacc(F[3 * i + k], A[3 * j + k], acc);
+            R[3 * i + j] = acc;
+          }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        {
+#pragma unroll
+          for (int j = i + 1; j < 3; ++j)
+            {
+              const float sr = wp * (R[3 * i + j].x + R[3 * j + i].x);
+              const float si = wm * (R[3 * i + j].y - R[3 * j + i].y);
+              R[3 * i + j] = c2(sr, si);
+              R[3 * j + i] = c2(sr, -si);
+            }
+          R[4 * i] = c2(fmaf(2.f * wp, R[4 * i].x, 2.f * w2 * dq), 0.f);
+        }
+      // (Y1 + Y2) and i (Y1 - Y2)
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        {
+          const C2 y1 = R[k], y2 = L[k];
+          L[k] = add2(y1, y2);
+          R[k] = c2(y2.y - y1.y, y1.x - y2.x);
+        }
     }
   else
     {
+      C2 p = c2(0.f, 0.f);
+      float q = 0.f;
 #pragma unroll
-      for (int k = 0; k < 18; ++k) out[k] = 0.f;
-      const float w4 = 2.f * cf[4], w5 = 2.f * cf[5];
-      if constexpr (G == 1)
+      for (int k = 0; k < 9; ++k)
         {
-          // dG_1 = dp A^* + p F^*, p = tr A A^T, dp = 2 sum A_ij F_ij
-          Cf p = {0.f, 0.f}, dp = {0.f, 0.f};
-#pragma unroll
-          for (int k = 0; k < 9; ++k)
-            {
-              const Cf x = A[k / 3][k % 3], y = F[k / 3][k % 3];
-              p = cma(x, x, p);
-              dp = cma(x, y, dp);
-            }
-          dp = {2.f * dp.r, 2.f * dp.i};
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) X[i][j] = cma(p, cj(F[i][j]), cm(dp, cj(A[i][j])));
-          acc_m3(X, 2.f * cf[1], out);
-          // [w4 (S + S^+) + w5 (conj(S) + S^T)] A, S = F A^+
-          mm3<0, 3>(F, A, S);
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-              {
-                const Cf sij = S[i][j], sji = S[j][i];
-                // S + S^+ = (s_ij + conj s_ji); conj(S) + S^T = (conj s_ij + s_ji)
-                X[i][j] = {(w4 + w5) * (sij.r + sji.r), w4 * (sij.i - sji.i) + w5 * (sji.i - sij.i)};
-              }
-          mm3_acc<0, 0>(X, A, 1.f, out);
+          p = cmac(A[k], A[k], p);
+          q = fmaf(A[k].x, A[k].x, fmaf(A[k].y, A[k].y, q));
         }
-      else
+      // M in L, N in R
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j)
+          {
+            C2 P = c2(0.f, 0.f), Q = c2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+              {
+                P = cmac(A[3 * i + k], A[3 * j + k], P);
+                Q = cmacc(A[3 * i + k], A[3 * j + k], Q);
+              }
+            if (i == j)
+              {
+                L[4 * i] = c2(cf[0] + w2 * q + wp * Q.x, 0.f);
+                R[4 * i] = __ffma2_rn(P, c2(w3, w3), scl2(p, w1));
+              }
+            else
+              {
+                L[3 * i + j] = c2(wp * Q.x, wm * Q.y);
+                L[3 * j + i] = c2(wp * Q.x, -wm * Q.y);
+                R[3 * i + j] = R[3 * j + i] = scl2(P, w3);
+              }
+          }
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
         {
-          // dG_2 = dq A + q F, q = tr A A^+, dq = 2 Re sum conj(A_ij) F_ij
-          float q = 0.f, dq = 0.f;
-#pragma unroll
-          for (int k = 0; k < 9; ++k)
-            {
-              const Cf x = A[k / 3][k % 3], y = F[k / 3][k % 3];
-              q = fmaf(x.r, x.r, fmaf(x.i, x.i, q));
-              dq = fmaf(x.r, y.r, fmaf(x.i, y.i, dq));
-            }
-          dq *= 2.f;
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-              X[i][j] = {fmaf(dq, A[i][j].r, q * F[i][j].r), fmaf(dq, A[i][j].i, q * F[i][j].i)};
-          acc_m3(X, 2.f * cf[2], out);
-          // (w4 Q + w5 Q^*) F, Q = A A^+
-          mm3<0, 3>(A, A, S);
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) X[i][j] = {(w4 + w5) * S[i][j].r, (w4 - w5) * S[i][j].i};
-          mm3_acc<0, 0>(X, F, 1.f, out);
+          const C2 m = L[k], n = R[k];
+          L[k] = add2(m, n);
+          R[k] = c2(n.y - m.y, m.x - n.x);
         }
     }
+  const C2(&B)[9] = ROLE == 0 ? A : F;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      {
+        C2 o = c2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          {
+            o = macr(L[3 * i + k], B[3 * k + j].x, o);
+            o = macr(R[3 * i + k], B[3 * k + j].y, o);
+          }
+        out[3 * i + j] = o;
+      }
 }
 
 // r[a] = sum_q val_q(a) w[q] + sum_k sum_q dval_q(a)/dxi_k F_k[q] (reference cube), a = ax + 2 ay + 4 az:
-// the transposed interpolation, sum-factorised axis by axis
-__device__ __forceinline__ void mf_contract(const float (&w)[8], const float (&F)[3][8], float (&r)[8])
+// the transposed interpolation, sum-factorised axis by axis, on component pairs
+__device__ __forceinline__ void mf_contract(const C2 (&w)[8], const C2 (&F)[3][8], C2 (&r)[8])
 {
-      {
-    float tx[2][4];
+  {
+    C2 tx[2][4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t)
-      {
-        tx[0][t] = kGbF * w[2 * t] + kGaF * w[2 * t + 1];
-        tx[1][t] = kGaF * w[2 * t] + kGbF * w[2 * t + 1];
-      }
-    float ty[2][2][2];
+    for (int t = 0; t < 4; ++t) gauss2(w[2 * t], w[2 * t + 1], tx[0][t], tx[1][t]);
+    C2 ty[2][2][2];
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
-      for (int qz = 0; qz < 2; ++qz)
-        {
-          ty[ax][0][qz] = kGbF * tx[ax][2 * qz] + kGaF * tx[ax][2 * qz + 1];
-          ty[ax][1][qz] = kGaF * tx[ax][2 * qz] + kGbF * tx[ax][2 * qz + 1];
-        }
+      for (int qz = 0; qz < 2; ++qz) gauss2(tx[ax][2 * qz], tx[ax][2 * qz + 1], ty[ax][0][qz], ty[ax][1][qz]);
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax)
 #pragma unroll
-      for (int ay = 0; ay < 2; ++ay)
-        {
-          r[ax + 2 * ay] = kGbF * ty[ax][ay][0] + kGaF * ty[ax][ay][1];
-          r[ax + 2 * ay + 4] = kGaF * ty[ax][ay][0] + kGbF * ty[ax][ay][1];
-        }
+      for (int ay = 0; ay < 2; ++ay) gauss2(ty[ax][ay][0], ty[ax][ay][1], r[ax + 2 * ay], r[ax + 2 * ay + 4]);
   }
   {
-    float sx[4];
+    C2 sx[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) sx[t] = F[0][2 * t] + F[0][2 * t + 1];
-    float uy[2][2];
+    for (int t = 0; t < 4; ++t) sx[t] = add2(F[0][2 * t], F[0][2 * t + 1]);
+    C2 uy[2][2];
 #pragma unroll
-    for (int qz = 0; qz < 2; ++qz)
-      {
-        uy[0][qz] = kGbF * sx[2 * qz] + kGaF * sx[2 * qz + 1];
-        uy[1][qz] = kGaF * sx[2 * qz] + kGbF * sx[2 * qz + 1];
-      }
+    for (int qz = 0; qz < 2; ++qz) gauss2(sx[2 * qz], sx[2 * qz + 1], uy[0][qz], uy[1][qz]);
 #pragma unroll
     for (int ay = 0; ay < 2; ++ay)
-#pragma unroll
-      for (int az = 0; az < 2; ++az)
-        {
-          const float v = az ? kGaF * uy[ay][0] + kGbF * uy[ay][1] : kGbF * uy[ay][0] + kGaF * uy[ay][1];
-          r[1 + 2 * ay + 4 * az] += v;
-          r[2 * ay + 4 * az] -= v;
-        }
+      {
+        C2 v0, v1;
+        gauss2(uy[ay][0], uy[ay][1], v0, v1);
+        r[1 + 2 * ay] = add2(r[1 + 2 * ay], v0);
+        r[2 * ay] = sub2(r[2 * ay], v0);
+        r[5 + 2 * ay] = add2(r[5 + 2 * ay], v1);
+        r[4 + 2 * ay] = sub2(r[4 + 2 * ay], v1);
+      }
   }
   {
-    float sy[4];
+    C2 sy[4];
 #pragma unroll
     for (int qz = 0; qz < 2; ++qz)
 #pragma unroll
-      for (int qx = 0; qx < 2; ++qx) sy[qx + 2 * qz] = F[1][qx + 4 * qz] + F[1][qx + 2 + 4 * qz];
-    float ux[2][2];
+      for (int qx = 0; qx < 2; ++qx) sy[qx + 2 * qz] = add2(F[1][qx + 4 * qz], F[1][qx + 2 + 4 * qz]);
+    C2 ux[2][2];
 #pragma unroll
-    for (int qz = 0; qz < 2; ++qz)
-      {
-        ux[0][qz] = kGbF * sy[2 * qz] + kGaF * sy[2 * qz + 1];
-        ux[1][qz] = kGaF * sy[2 * qz] + kGbF * sy[2 * qz + 1];
-      }
+    for (int qz = 0; qz < 2; ++qz) gauss2(sy[2 * qz], sy[2 * qz + 1], ux[0][qz], ux[1][qz]);
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-      for (int az = 0; az < 2; ++az)
-        {
-          const float v = az ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
-          r[ax + 2 + 4 * az] += v;
-          r[ax + 4 * az] -= v;
-        }
+      {
+        C2 v0, v1;
+        gauss2(ux[ax][0], ux[ax][1], v0, v1);
+        r[ax + 2] = add2(r[ax + 2], v0);
+        r[ax] = sub2(r[ax], v0);
+        r[ax + 6] = add2(r[ax + 6], v1);
+        r[ax + 4] = sub2(r[ax + 4], v1);
+      }
   }
   {
-    float sz[4];
+    C2 sz[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) sz[t] = F[2][t] + F[2][t + 4];
-    float ux[2][2];
+    for (int t = 0; t < 4; ++t) sz[t] = add2(F[2][t], F[2][t + 4]);
+    C2 ux[2][2];
 #pragma unroll
-    for (int qy = 0; qy < 2; ++qy)
-      {
-        ux[0][qy] = kGbF * sz[2 * qy] + kGaF * sz[2 * qy + 1];
-        ux[1][qy] = kGaF * sz[2 * qy] + kGbF * sz[2 * qy + 1];
-      }
+    for (int qy = 0; qy < 2; ++qy) gauss2(sz[2 * qy], sz[2 * qy + 1], ux[0][qy], ux[1][qy]);
 #pragma unroll
     for (int ax = 0; ax < 2; ++ax)
-#pragma unroll
-      for (int ay = 0; ay < 2; ++ay)
-        {
-          const float v = ay ? kGaF * ux[ax][0] + kGbF * ux[ax][1] : kGbF * ux[ax][0] + kGaF * ux[ax][1];
-          r[ax + 2 * ay + 4] += v;
-          r[ax + 2 * ay] -= v;
-        }
+      {
+        C2 v0, v1;
+        gauss2(ux[ax][0], ux[ax][1], v0, v1);
+        r[ax + 4] = add2(r[ax + 4], v0);
+        r[ax] = sub2(r[ax], v0);
+        r[ax + 6] = add2(r[ax + 6], v1);
+        r[ax + 2] = sub2(r[ax + 2], v1);
+      }
   }
 }
 
 template <int NC>
-__global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
-                                                     const float *__restrict__ z, float *__restrict__ ycell,
-                                                     const uint8_t *__restrict__ act)
+__global__ void __launch_bounds__(16 * NC, 32 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
+                                                        const float *__restrict__ z, float *__restrict__ ycell,
+                                                        const uint8_t *__restrict__ act)
 {
-  constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 24 * NC;
+  constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 16 * NC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   MfSmem<NC> &S = *reinterpret_cast<MfSmem<NC> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -367,11 +369,11 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
 #pragma unroll
       for (int k = 0; k < 6; ++k) S.bulk[tid][k] = bk[k];
     }
-  // nodal values: thread entries idx = tid + k kMThreads, k < 6 (144 NC entries over 24 NC
+  // nodal values: thread entries idx = tid + k kMThreads, k < 9 (144 NC entries over 16 NC
   // threads); node ids, then values, ranges and masks are requested together
   {
-    constexpr int kPer = 6;
-    static_assert(kMCells * 144 == kPer * kMThreads, "six entries per thread");
+    constexpr int kPer = 9;
+    static_assert(kMCells * 144 == kPer * kMThreads, "nine entries per thread");
     int node[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k)
@@ -412,25 +414,23 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
       }
   }
   __syncthreads();
-  // Z and its physical gradient at the points: thread (cell, component)
-  if (tid < kMCells * 18)
+  // A, Z and dZ/dx at the points: thread (cell, component pair)
+  if (tid < kMCells * 9)
     {
-      const int cl = tid / 18, c = tid - 18 * cl;
-      const float *xv = &S.u.g.zs[cl][0][c]; // xv[18 v], v = vx + 2 vy + 4 vz
-      // the state at the 8 points: the same tensor interpolation, values only
+      const int cl = tid / 9, cp = tid - 9 * cl;
       {
-        const float *sv = &S.u.g.xs[cl][0][c];
-        float aq[2][4];
+        C2 aq[2][4];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) gauss2f(sv[18 * t], sv[18 * (t + 4)], aq[0][t], aq[1][t]);
-        // along y, in place: aq[qz][2 qy + vx]
+        for (int t = 0; t < 4; ++t)
+          gauss2(c2(S.u.g.xs[cl][t][cp], S.u.g.xs[cl][t][cp + 9]),
+                 c2(S.u.g.xs[cl][t + 4][cp], S.u.g.xs[cl][t + 4][cp + 9]), aq[0][t], aq[1][t]);
 #pragma unroll
         for (int qz = 0; qz < 2; ++qz)
 #pragma unroll
           for (int vx = 0; vx < 2; ++vx)
             {
-              float y0, y1;
-              gauss2f(aq[qz][vx], aq[qz][2 + vx], y0, y1);
+              C2 y0, y1;
+              gauss2(aq[qz][vx], aq[qz][2 + vx], y0, y1);
               aq[qz][vx] = y0;
               aq[qz][2 + vx] = y1;
             }
@@ -439,32 +439,33 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
 #pragma unroll
           for (int qy = 0; qy < 2; ++qy)
             {
-              float v0, v1;
-              gauss2f(aq[qz][2 * qy], aq[qz][2 * qy + 1], v0, v1);
+              C2 v0, v1;
+              gauss2(aq[qz][2 * qy], aq[qz][2 * qy + 1], v0, v1);
               const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              S.X[p0][c] = v0;
-              S.X[p0 + 1][c] = v1;
+              reinterpret_cast<float2 *>(S.X[p0])[cp] = v0;
+              reinterpret_cast<float2 *>(S.X[p0 + 1])[cp] = v1;
             }
       }
-      float zq[2][4], zd[4];
+      C2 zq[2][4], zd[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t)
         {
-          const float f0 = xv[18 * t], f1 = xv[18 * (t + 4)];
-          gauss2f(f0, f1, zq[0][t], zq[1][t]);
-          zd[t] = f1 - f0;
+          const C2 f0 = c2(S.u.g.zs[cl][t][cp], S.u.g.zs[cl][t][cp + 9]);
+          const C2 f1 = c2(S.u.g.zs[cl][t + 4][cp], S.u.g.zs[cl][t + 4][cp + 9]);
+          gauss2(f0, f1, zq[0][t], zq[1][t]);
+          zd[t] = sub2(f1, f0);
         }
-      float yq[2][2][2], ydy[2][2], zdq[2][2];
+      C2 yq[2][2][2], ydy[2][2], zdq[2][2];
 #pragma unroll
       for (int vx = 0; vx < 2; ++vx)
         {
 #pragma unroll
           for (int qz = 0; qz < 2; ++qz)
             {
-              gauss2f(zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
-              ydy[qz][vx] = zq[qz][2 + vx] - zq[qz][vx];
+              gauss2(zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
+              ydy[qz][vx] = sub2(zq[qz][2 + vx], zq[qz][vx]);
             }
-          gauss2f(zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
+          gauss2(zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
         }
       const float i0 = S.ih[cl][0], i1 = S.ih[cl][1], i2 = S.ih[cl][2];
 #pragma unroll
@@ -472,97 +473,100 @@ __global__ void __launch_bounds__(24 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
 #pragma unroll
         for (int qy = 0; qy < 2; ++qy)
           {
-            float v0, v1;
-            gauss2f(yq[qz][qy][0], yq[qz][qy][1], v0, v1);
-            const float dx = (yq[qz][qy][1] - yq[qz][qy][0]) * i0;
+            C2 v0, v1;
+            gauss2(yq[qz][qy][0], yq[qz][qy][1], v0, v1);
+            const C2 dx = scl2(sub2(yq[qz][qy][1], yq[qz][qy][0]), i0);
             const int p0 = cl * 8 + 2 * qy + 4 * qz;
-            S.Z[p0][c] = v0;
-            S.Z[p0 + 1][c] = v1;
-            S.gZ[p0][0][c] = dx;
-            S.gZ[p0 + 1][0][c] = dx;
+            reinterpret_cast<float2 *>(S.Z[p0])[cp] = v0;
+            reinterpret_cast<float2 *>(S.Z[p0 + 1])[cp] = v1;
+            reinterpret_cast<float2 *>(S.gZ[p0][0])[cp] = dx;
+            reinterpret_cast<float2 *>(S.gZ[p0 + 1][0])[cp] = dx;
           }
 #pragma unroll
       for (int qz = 0; qz < 2; ++qz)
         {
-          float d0, d1;
-          gauss2f(ydy[qz][0], ydy[qz][1], d0, d1);
+          C2 d0, d1;
+          gauss2(ydy[qz][0], ydy[qz][1], d0, d1);
 #pragma unroll
           for (int qy = 0; qy < 2; ++qy)
             {
               const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              S.gZ[p0][1][c] = d0 * i1;
-              S.gZ[p0 + 1][1][c] = d1 * i1;
+              reinterpret_cast<float2 *>(S.gZ[p0][1])[cp] = scl2(d0, i1);
+              reinterpret_cast<float2 *>(S.gZ[p0 + 1][1])[cp] = scl2(d1, i1);
             }
         }
 #pragma unroll
       for (int qy = 0; qy < 2; ++qy)
         {
-          float d0, d1;
-          gauss2f(zdq[qy][0], zdq[qy][1], d0, d1);
+          C2 d0, d1;
+          gauss2(zdq[qy][0], zdq[qy][1], d0, d1);
 #pragma unroll
           for (int qz = 0; qz < 2; ++qz)
             {
               const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              S.gZ[p0][2][c] = d0 * i2;
-              S.gZ[p0 + 1][2][c] = d1 * i2;
+              reinterpret_cast<float2 *>(S.gZ[p0][2])[cp] = scl2(d0, i2);
+              reinterpret_cast<float2 *>(S.gZ[p0 + 1][2])[cp] = scl2(d1, i2);
             }
         }
     }
-  __syncthreads(); // Z, gZ complete
-  // w = H_q Z_q in three partial sums, thread (point, group of bulk terms), from the state
-  // and the direction at the point (hvp_part)
+  __syncthreads(); // X, Z, gZ complete; the gathered nodal values are no longer read
+  // H Z at each point in two shares: thread (role, point), role uniform over a warp for NC >= 4
   {
-    const int pq = tid & (kMPts - 1), g = tid / kMPts, cl = pq >> 3;
-    float zq[18], aq[18], acc[18];
-#pragma unroll
-    for (int i = 0; i < 18; ++i)
-      {
-        zq[i] = S.Z[pq][i];
-        aq[i] = S.X[pq][i];
-      }
-    float cf[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) cf[k] = S.bulk[cl][k];
-    __syncthreads(); // zs / xs (aliased by the partial sums) are no longer read
+    const int role = tid / kMPts, pq = tid - role * kMPts, cl = pq >> 3;
     if (cl < ncb)
       {
-        if (g == 0)
-          hvp_part<0>(aq, zq, cf, acc);
-        else if (g == 1)
-          hvp_part<1>(aq, zq, cf, acc);
-        else
-          hvp_part<2>(aq, zq, cf, acc);
+        C2 A[9], F[9], out[9];
+        load_c9(S.X[pq], A);
+        load_c9(S.Z[pq], F);
+        float cf[6];
 #pragma unroll
-        for (int i = 0; i < 18; ++i) S.u.part[g][pq][i] = acc[i];
+        for (int k = 0; k < 6; ++k) cf[k] = S.bulk[cl][k];
+        if (role == 0)
+          hvp_role<0>(A, F, cf, out);
+        else
+          hvp_role<1>(A, F, cf, out);
+        store_c9(S.u.part[role][pq], out);
       }
   }
   __syncthreads();
-  // contraction with the test functions: thread (cell, component)
-  if (tid < kMCells * 18)
+  // contraction with the test functions: thread (cell, component pair)
+  if (tid < kMCells * 9)
     {
-      const int cl = tid / 18, c = tid - 18 * cl;
-      const int part = c / 9, mu = (c % 9) / 3, jc = c % 3;
+      const int cl = tid / 9, cp = tid - 9 * cl;
+      const int mu = cp / 3, jc = cp % 3;
       const float K1 = S.K1[cl], K23 = S.K23[cl];
       const float ih[3] = {S.ih[cl][0], S.ih[cl][1], S.ih[cl][2]};
-      float w[8], F[3][8];
+      C2 w[8], F[3][8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
         {
           const int pq = cl * 8 + q;
-          w[q] = S.u.part[0][pq][c] + S.u.part[1][pq][c] + S.u.part[2][pq][c];
-          const int base = 9 * part + 3 * mu;
-          const float dterm = K23 * (S.gZ[pq][0][base] + S.gZ[pq][1][base + 1] + S.gZ[pq][2][base + 2]);
+          w[q] = add2(reinterpret_cast<const float2 *>(S.u.part[0][pq])[cp],
+                      reinterpret_cast<const float2 *>(S.u.part[1][pq])[cp]);
+          const C2 dv = scl2(add2(add2(reinterpret_cast<const float2 *>(S.gZ[pq][0])[3 * mu],
+                                       reinterpret_cast<const float2 *>(S.gZ[pq][1])[3 * mu + 1]),
+                                  reinterpret_cast<const float2 *>(S.gZ[pq][2])[3 * mu + 2]),
+                             K23);
 #pragma unroll
-          for (int k = 0; k < 3; ++k) F[k][q] = ih[k] * (K1 * S.gZ[pq][k][c] + (k == jc ? dterm : 0.f));
+          for (int k = 0; k < 3; ++k)
+            {
+              C2 g = scl2(reinterpret_cast<const float2 *>(S.gZ[pq][k])[cp], K1);
+              if (k == jc) g = add2(g, dv);
+              F[k][q] = scl2(g, ih[k]);
+            }
         }
-      float r[8];
+      C2 r[8];
       mf_contract(w, F, r);
       if (cl < ncb)
         {
           const float jxw = S.jxw[cl];
-          float *out = ycell + (e0 + cl) * 144 + c;
+          float *out = ycell + (e0 + cl) * 144 + cp;
 #pragma unroll
-          for (int a = 0; a < 8; ++a) out[18 * a] = r[a] * jxw;
+          for (int a = 0; a < 8; ++a)
+            {
+              out[18 * a] = r[a].x * jxw;
+              out[18 * a + 9] = r[a].y * jxw;
+            }
         }
     }
   (void)act;
@@ -700,7 +704,7 @@ static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float
       attr = true;
     }
   const int64_t gc = (m.nc + NC - 1) / NC;
-  k_mf_cell<NC><<<static_cast<unsigned>(gc), 24 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act);
+  k_mf_cell<NC><<<static_cast<unsigned>(gc), 16 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act);
   return cudaGetLastError();
 }
 

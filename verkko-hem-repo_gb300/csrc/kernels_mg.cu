@@ -302,16 +302,17 @@ cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, con
 // of the slightly shifted matrix in shared memory, FP32, one CTA per instance.  It is a preconditioner component, so
 // FP32 suffices in both precision modes (the outer flexible GMRES is exact).
 // ---------------------------------------------------------------------------------
-constexpr int kGjThreads = 320;       // >= the 2 * 144 + 1 columns of one augmented row
+constexpr int kGjThreads = 1024;      // (augmented column, row chunk) pairs
 constexpr int kMaxDense = 160;        // largest coarsest system (unknowns per instance)
 constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest solve
 
 // Gauss-Jordan on [A + shift I | I] with implicit partial pivoting: in step k one warp
 // picks the largest unused entry of column k (row p_k) and snapshots the column; then
-// every thread updates the augmented columns it owns (every row minus its column-k
-// multiple, then row p_k scaled), so a step needs two barriers.  Afterwards row p_k of
-// the right half is row k of the inverse.  Rows are padded to an odd length so that
-// column reads hit distinct banks.
+// every thread updates the rows of its chunk in the augmented column it owns (every row
+// minus its column-k multiple, then row p_k scaled).  A step reads the pivot row before
+// anyone overwrites it, so it takes three barriers.  Afterwards row p_k of the right half
+// is row k of the inverse.  Rows are padded to an odd length so that column reads hit
+// distinct banks; a warp's threads own consecutive columns.
 template <typename T>
 __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T *__restrict__ vals,
                                                              const int64_t *__restrict__ dense_off,
@@ -331,7 +332,14 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
   const int nd = static_cast<int>((n1 - n0) * B);
   const int ld = 2 * nd + 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (nd > kMaxDense) return; // rejected by the host before launch
+  if (nd > kMaxDense || nd == 0) return; // rejected by the host before launch
+  // this thread's augmented column and row chunk
+  const int ncol = 2 * nd;
+  const int nch = min(nd, kGjThreads / ncol);
+  const int rows_per = (nd + nch - 1) / nch;
+  const int my_c = tid % ncol, my_ch = tid / ncol;
+  const bool worker = my_ch < nch;
+  const int r0 = worker ? my_ch * rows_per : 0, r1 = worker ? min(nd, r0 + rows_per) : 0;
   for (int e = tid; e < nd * ld; e += kGjThreads)
     {
       const int r = e / ld, c = e - r * ld;
@@ -355,12 +363,17 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       W[row * ld + col] = to_f(vals[blk * B * B + e]);
     }
   __syncthreads();
-  if (tid == 0)
+  if (warp == 0)
     {
-      s_sing = 0;
       float sd = 0.f;
-      for (int i = 0; i < nd; ++i) sd += fabsf(W[i * ld + i]);
-      s_shift = nd > 0 ? kCoarseShift * sd / static_cast<float>(nd) : 0.f;
+      for (int i = lane; i < nd; i += 32) sd += fabsf(W[i * ld + i]);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
+      if (lane == 0)
+        {
+          s_sing = 0;
+          s_shift = kCoarseShift * sd / static_cast<float>(nd);
+        }
     }
   __syncthreads();
   // near-null modes (global phase and spin rotations near a solution) would be amplified
@@ -410,17 +423,19 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       __syncthreads();
       if (s_sing) break;
       const int p = s_p;
-      const float rp = 1.f / s_piv;
-      // columns left of k are unit columns already: row p is zero there.  Every row,
-      // the pivot row included, takes W -= colk * wp (branch-free, so the loop pipelines);
-      // that zeroes row p (colk[p] is the pivot), which then receives the scaled row.
-      for (int c = k + tid; c < 2 * nd; c += kGjThreads)
+      // columns left of k are unit columns already: row p is zero there
+      const bool upd = worker && my_c >= k;
+      const float wp = upd ? W[p * ld + my_c] * (1.f / s_piv) : 0.f;
+      __syncthreads(); // row p read by every chunk of the column before it is overwritten
+      if (upd)
         {
-          const float wp = W[p * ld + c] * rp;
-          float *col = W + c;
+          // every row, the pivot row included, takes W -= colk * wp (branch-free, so the
+          // loop pipelines); that zeroes row p (colk[p] is the pivot), which then
+          // receives the scaled row
+          float *col = W + my_c;
 #pragma unroll 8
-          for (int i = 0; i < nd; ++i) col[i * ld] = fmaf(-colk[i], wp, col[i * ld]);
-          col[p * ld] = wp;
+          for (int i = r0; i < r1; ++i) col[i * ld] = fmaf(-colk[i], wp, col[i * ld]);
+          if (p >= r0 && p < r1) col[p * ld] = wp;
         }
       __syncthreads();
     }

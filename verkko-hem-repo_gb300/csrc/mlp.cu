@@ -101,19 +101,55 @@ __device__ __forceinline__ float dsilu(float z)
   return s * (1.f + z * (1.f - s));
 }
 
+// operand bytes of one K chunk: A 128 x 64 and B NT x 64 (BF16)
+template <int NT> __host__ __device__ constexpr int stage_bytes() { return (kTileM + NT) * kKChunk * 2; }
+
+// one 16-byte unit global -> shared, asynchronously; zero-filled when !valid
+__device__ __forceinline__ void cp16(void *dst, const void *src, bool valid)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0));
+}
+
+// K chunk [k0, k0 + kc) of A (128 rows from m0) and B (NT rows from n0) into one stage, in
+// the no-swizzle K-major core-matrix layout: 16-byte unit (row r, k group kg) at
+// ((r / 8) kgc + kg) 128 + (r % 8) 16
+template <int NT>
+__device__ __forceinline__ void stage_chunk(const GemmArgs &g, unsigned char *st, int m0, int n0, int k0, int kc, int tid)
+{
+  const int kgc = kc / 8;
+  unsigned char *sA = st, *sB = st + kTileM * kKChunk * 2;
+  for (int u = tid; u < kTileM * kgc; u += kGemmThreads)
+    {
+      const int r = u / kgc, kg = u % kgc;
+      const bool ok = m0 + r < g.M;
+      const __nv_bfloat16 *src = g.A + (ok ? static_cast<int64_t>(m0 + r) * g.lda + k0 + kg * 8 : 0);
+      cp16(sA + ((r >> 3) * kgc + kg) * 128 + (r & 7) * 16, src, ok);
+    }
+  for (int u = tid; u < NT * kgc; u += kGemmThreads)
+    {
+      const int r = u / kgc, kg = u % kgc;
+      const bool ok = n0 + r < g.N;
+      const __nv_bfloat16 *src = g.B + (ok ? static_cast<int64_t>(n0 + r) * g.ldb + k0 + kg * 8 : 0);
+      cp16(sB + ((r >> 3) * kgc + kg) * 128 + (r & 7) * 16, src, ok);
+    }
+  asm volatile("cp.async.commit_group;");
+}
+
+// Two operand stages: the copies of chunk i + 1 run while the tensor core works on chunk i;
+// a stage is refilled only after the MMAs that read it have committed (one mbarrier per
+// stage).
 template <int NT, int EPI>
 __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);                    // 128 x 64
-  __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(smem + kTileM * kKChunk * 2); // NT x 64
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * NT;
   const int split = blockIdx.z;
   const int kb = split * g.k_per_split;
   const int ke = min(g.K, kb + g.k_per_split);
+  const int nchunks = ke > kb ? (ke - kb + kKChunk - 1) / kKChunk : 0;
   constexpr uint32_t kCols = NT < 32 ? 32 : NT;
   if (warp == 0)
     {
@@ -123,7 +159,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
     }
   if (tid == 0)
     {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[0])), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar[1])), "r"(1));
       asm volatile("fence.mbarrier_init.release.cluster;");
     }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -131,27 +168,28 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
   bool ok = true;
-  uint32_t phase = 0;
-  int issued = 0;
-  for (int k0 = kb; k0 < ke; k0 += kKChunk)
+  int committed = 0; // chunks whose MMAs were committed
+  if (nchunks > 0) stage_chunk<NT>(g, smem, m0, n0, kb, min(kKChunk, ke - kb), tid);
+  for (int i = 0; i < nchunks && ok; ++i)
     {
+      const int k0 = kb + i * kKChunk;
       const int kc = min(kKChunk, ke - k0); // multiple of 16
-      const int kgc = kc / 8;               // core matrices along K
-      // stage A (128 x kc) and B (NT x kc): 16-byte units into core(r/8, kg) row r%8
-      for (int u = tid; u < kTileM * kgc; u += kGemmThreads)
+      const int kgc = kc / 8;
+      unsigned char *st = smem + (i & 1) * stage_bytes<NT>();
+      if (i + 1 < nchunks)
         {
-          const int r = u / kgc, kg = u % kgc;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (m0 + r < g.M) v = *reinterpret_cast<const uint4 *>(g.A + static_cast<int64_t>(m0 + r) * g.lda + k0 + kg * 8);
-          *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(sA) + ((r >> 3) * kgc + kg) * 128 + (r & 7) * 16) = v;
+          // the other stage was read by the MMAs of chunk i - 1: wait for their commit
+          if (i >= 1 && !mbar_wait(smem_u32(&mbar[(i - 1) & 1]), static_cast<uint32_t>(((i - 1) >> 1) & 1)))
+            {
+              ok = false;
+              break;
+            }
+          const int k1 = k0 + kKChunk;
+          stage_chunk<NT>(g, smem + ((i + 1) & 1) * stage_bytes<NT>(), m0, n0, k1, min(kKChunk, ke - k1), tid);
+          asm volatile("cp.async.wait_group 1;"); // chunk i has landed; chunk i + 1 may be in flight
         }
-      for (int u = tid; u < NT * kgc; u += kGemmThreads)
-        {
-          const int r = u / kgc, kg = u % kgc;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (n0 + r < g.N) v = *reinterpret_cast<const uint4 *>(g.B + static_cast<int64_t>(n0 + r) * g.ldb + k0 + kg * 8);
-          *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(sB) + ((r >> 3) * kgc + kg) * 128 + (r & 7) * 16) = v;
-        }
+      else
+        asm volatile("cp.async.wait_group 0;");
       asm volatile("fence.proxy.async.shared::cta;");
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncthreads();
@@ -159,37 +197,39 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
       if (tid == 0)
         {
           constexpr uint32_t idesc = idesc_bf16(NT);
+          const uint32_t sa = smem_u32(st), sb = smem_u32(st + kTileM * kKChunk * 2);
           for (int ks = 0; ks < kc / 16; ++ks)
             {
-              const uint64_t ad = smem_desc(smem_u32(sA) + ks * 256, 128, kgc * 128);
-              const uint64_t bd = smem_desc(smem_u32(sB) + ks * 256, 128, kgc * 128);
-              const uint32_t acc = (k0 > kb || ks > 0) ? 1u : 0u;
+              const uint64_t ad = smem_desc(sa + ks * 256, 128, kgc * 128);
+              const uint64_t bd = smem_desc(sb + ks * 256, 128, kgc * 128);
+              const uint32_t acc = (i > 0 || ks > 0) ? 1u : 0u;
               asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
           asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(&mbar)));
+            smem_u32(&mbar[i & 1])));
         }
-      ++issued;
-      // the MMAs read shared memory asynchronously: wait before it is overwritten
-      if (!mbar_wait(smem_u32(&mbar), phase))
+      committed = i + 1;
+    }
+  asm volatile("cp.async.wait_group 0;");
+  // every MMA is tracked by the last commit: wait for it before reading the accumulator
+  if (committed > 0)
+    {
+      const int j = committed - 1;
+      if (!mbar_wait(smem_u32(&mbar[j & 1]), static_cast<uint32_t>((j >> 1) & 1)))
         {
           ok = false;
-          break;
+          mbar_wait(smem_u32(&mbar[j & 1]), static_cast<uint32_t>((j >> 1) & 1)); // bounded second wait
         }
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;");
     }
-  if (!ok)
-    {
-      if (lane == 0) atomicExch(g.err, 1);
-      mbar_wait(smem_u32(&mbar), phase); // bounded second wait for the MMAs in flight
-    }
-  // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes), 16 columns per load
+  if (!ok && lane == 0) atomicExch(g.err, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes), 16 columns per load;
+  // a thread's 16 consecutive outputs of its row are written as 16-byte vectors
   const int row = warp * 32 + lane;
   const int m = m0 + row;
-  if (ok && issued > 0)
+  if (ok && committed > 0)
     for (int c0 = 0; c0 < NT; c0 += 16)
       {
         uint32_t r[16];
@@ -202,10 +242,54 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;");
         if (m >= g.M) continue;
+        const int nb = n0 + c0;
+        const bool full = nb + 16 <= g.N;
+        if (EPI == EPI_HIDDEN && full)
+          {
+            float z[16];
+            __nv_bfloat16 h[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              {
+                z[j] = __uint_as_float(r[j]) + g.bias[nb + j];
+                h[j] = __float2bfloat16(silu(z[j]));
+              }
+            float4 *zo = reinterpret_cast<float4 *>(g.out_f32 + static_cast<int64_t>(m) * g.ldo + nb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) zo[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+            uint4 *ho = reinterpret_cast<uint4 *>(g.out_h + static_cast<int64_t>(m) * g.ldh + nb);
+            ho[0] = *reinterpret_cast<const uint4 *>(&h[0]);
+            ho[1] = *reinterpret_cast<const uint4 *>(&h[8]);
+            if (g.out_t)
+#pragma unroll
+              for (int j = 0; j < 16; ++j) g.out_t[static_cast<int64_t>(nb + j) * g.ldt + m] = h[j];
+            continue;
+          }
+        if (EPI == EPI_DELTA && full)
+          {
+            __nv_bfloat16 d[16];
+            const float4 *zi = reinterpret_cast<const float4 *>(g.z_in + static_cast<int64_t>(m) * g.ldz + nb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              {
+                const float4 zz = zi[q];
+                d[4 * q] = __float2bfloat16(__uint_as_float(r[4 * q]) * dsilu(zz.x));
+                d[4 * q + 1] = __float2bfloat16(__uint_as_float(r[4 * q + 1]) * dsilu(zz.y));
+                d[4 * q + 2] = __float2bfloat16(__uint_as_float(r[4 * q + 2]) * dsilu(zz.z));
+                d[4 * q + 3] = __float2bfloat16(__uint_as_float(r[4 * q + 3]) * dsilu(zz.w));
+              }
+            uint4 *ho = reinterpret_cast<uint4 *>(g.out_h + static_cast<int64_t>(m) * g.ldh + nb);
+            ho[0] = *reinterpret_cast<const uint4 *>(&d[0]);
+            ho[1] = *reinterpret_cast<const uint4 *>(&d[8]);
+            if (g.out_t)
+#pragma unroll
+              for (int j = 0; j < 16; ++j) g.out_t[static_cast<int64_t>(nb + j) * g.ldt + m] = d[j];
+            continue;
+          }
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           {
-            const int n = n0 + c0 + j;
+            const int n = nb + j;
             if (n >= g.N) continue;
             const float acc = __uint_as_float(r[j]);
             if (EPI == EPI_HIDDEN)
@@ -386,7 +470,7 @@ template <typename T> glgpu_status salloc(glgpu_surrogate *s, T **p, size_t n)
     }                                                                                                                \
   while (0)
 
-constexpr size_t kGemmSmem = 76 * 1024; // 48 KB of operands; sized so that at most two CTAs share an SM (TMEM <= 512 columns)
+constexpr size_t kGemmSmem = 100 * 1024; // two operand stages (96 KB at NT = 256); at most two CTAs share an SM (TMEM <= 512 columns)
 
 template <int NT, int EPI> glgpu_status gemm(glgpu_surrogate *s, GemmArgs g, int splits)
 {

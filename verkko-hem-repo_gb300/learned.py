@@ -4,12 +4,18 @@ Pipeline (no counterpart in the reference, which always starts from a uniform B 
 femgl/src/setup_uniform_B-phase.cc:238-259):
 
 1. converged states: batched mixed-precision Newton solves of seeded (t, p, D) slab
-   instances (`generate`);
+   instances from the uniform B phase (`generate`).  The uniform start has the symmetry of
+   the slab (real, diagonal, u11 = u22), and Newton keeps it, so every training state lies
+   in one gauge: the global phase and spin rotations, exact symmetries of the functional,
+   are fixed by the data rather than left to a random draw;
 2. training: the tcgen05 MLP of :class:`Surrogate` is fitted on per-node
-   (features -> order parameter / bulk amplitude) pairs (`train`);
-3. inference: the network predicts every node of new instances (`guess`); plain Newton
-   from that guess, and from the B phase for any instance whose residual stalls or that
-   does not converge (`solve`).
+   (features -> order parameter / bulk amplitude) pairs (`train`); the components that
+   vanish in every training state (the symmetry zeros) are recorded;
+3. inference: the network predicts every node of new instances and the symmetry zeros are
+   set exactly (`guess`), so the start carries no error along the near-null phase and
+   rotation directions, where Newton's linear solves converge slowly; plain Newton from
+   that guess, and from the B phase for any instance whose residual stalls or that does
+   not converge (`solve_learned`).
 
 Features of a node at (x, y, z) of an instance (t, p, D) on a slab [-10, 10]^2 x
 [-D/2, D/2]: (x/10, y/10, 2z/D, t, p/34, D/40).  Targets: the 18 components divided by
@@ -91,36 +97,63 @@ def solve(gl, insts, starts, precision, linear_tol=1e-4, tol=1e-10, max_newton=4
 
 
 def generate(gl, count: int, seed: int = 11, n_lo: int = 10, n_hi: int = 14, per_instance: int = 2048,
-             noise: float = 0.05, precond=None):
-    """Training pairs from `count` converged batched solves."""
+             noise: float = 0.0, precond=None, waves: bool = False):
+    """Training pairs from `count` converged batched solves (from the uniform B phase
+    unless noise > 0).  With waves, the instances are solved in device-sized waves of
+    batched contexts (sweep.solve_sweep), for training sets larger than one context."""
     insts = sample(gl, count, seed, n_lo, n_hi)
-    sols, out, ms = solve(gl, insts, bphase_starts(gl, insts, noise, seed * 1000), gl.MIXED, precond=precond)
+    starts = bphase_starts(gl, insts, noise, seed * 1000)
+    if waves:
+        import importlib
+
+        S = importlib.import_module(__package__ + ".sweep")
+        pc = gl.PC_MULTIGRID if precond is None else precond
+        prms = [gl.Params.from_matep(d.p, d.t, precision=gl.MIXED, precond=pc) for d in insts]
+        r = S.solve_sweep(gl, [d.mesh for d in insts], prms, starts, keep_solutions=True)
+        sols, ok, ms = r["solutions"], r["converged"], float(sum(r["solve_ms"]))
+    else:
+        sols, out, ms = solve(gl, insts, starts, gl.MIXED, precond=precond)
+        ok = out["residual"] <= 1e-10
     rng = np.random.default_rng(seed)
     X, Y = [], []
-    for d, x, ok in zip(insts, sols, out["residual"] <= 1e-10):
-        if not ok:
+    for d, x, good in zip(insts, sols, ok):
+        if not good:
             continue
         f = features(d.mesh, d.t, d.p, d.D)
         y = (x.reshape(-1, 18) / amplitude(gl, d.t, d.p)).astype(np.float32)
         idx = rng.choice(f.shape[0], size=min(per_instance, f.shape[0]), replace=False)
         X.append(f[idx])
         Y.append(y[idx])
-    return np.concatenate(X), np.concatenate(Y), {"instances": count, "solve_ms": ms,
-                                                   "converged": int(np.sum(out["residual"] <= 1e-10))}
+    return np.concatenate(X), np.concatenate(Y), {"instances": count, "solve_ms": ms, "converged": int(np.sum(ok))}
+
+
+def symmetry_zeros(Y, rel: float = 1e-4) -> np.ndarray:
+    """Output mask: 0 for the components that vanish (below rel times the largest target)
+    in every training state, 1 elsewhere."""
+    amax = np.abs(Y).max(axis=0)
+    return (amax > rel * amax.max()).astype(np.float32)
 
 
 def train(gl, X, Y, steps: int = 1500, batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+    """Fits a Surrogate on (X, Y); its `out_mask` attribute holds the symmetry zeros."""
     s = gl.Surrogate(seed=seed)
+    mask = symmetry_zeros(Y)
     t0 = time.perf_counter()
-    loss = s.train(X, Y, steps=steps, batch=batch, lr=lr, seed=seed)
-    return s, {"loss": loss, "train_s": time.perf_counter() - t0, "steps": steps, "batch": batch, "rows": int(X.shape[0])}
+    loss = s.train(X, Y * mask, steps=steps, batch=batch, lr=lr, seed=seed)
+    s.out_mask = mask
+    return s, {"loss": loss, "train_s": time.perf_counter() - t0, "steps": steps, "batch": batch,
+               "rows": int(X.shape[0]), "components_kept": int(mask.sum())}
 
 
 def guess(gl, surrogate, insts):
-    """Surrogate initial guesses (FP64 node-major vectors) for the instances."""
+    """Surrogate initial guesses (FP64 node-major vectors) for the instances, with the
+    symmetry zeros of the training data set exactly."""
+    mask = getattr(surrogate, "out_mask", None)
     out = []
     for d in insts:
         y = surrogate.predict(features(d.mesh, d.t, d.p, d.D)).astype(np.float64)
+        if mask is not None:
+            y *= mask
         out.append((y * amplitude(gl, d.t, d.p)).ravel())
     return out
 

@@ -3,9 +3,10 @@
 A batched context keeps every instance's Jacobian blocks, Krylov bases and multigrid
 hierarchy resident (in mixed precision with multigrid, tens of KB per mesh node), so a
 phase-diagram sweep such as 256 slab instances of 16^3 to 48^3 cells (11.5M nodes) does not
-fit one context.  ``solve_sweep`` measures the per-node footprint on a probe context built
-from the largest instance, packs consecutive instances into waves that fit the free device
-memory, solves each wave as one batched context and returns the results in input order.
+fit one context.  ``solve_sweep`` measures the footprint on probe contexts of the largest
+and the smallest instance (a constant per instance plus a slope per node), packs
+consecutive instances into waves that fit the free device memory, solves each wave as one
+batched context and returns the results in input order.
 Instances are independent inside a context (per-instance reductions, GMRES, line search and
 convergence); the preconditioner's storage and kernel shapes follow the context's total size
 (FP16 coarse levels from 2000 nodes, warps per block row), so an instance's FP32 Krylov path
@@ -20,13 +21,14 @@ from typing import Sequence
 import numpy as np
 
 
-def plan_waves(node_counts: Sequence[int], bytes_per_node: float, budget: float) -> list:
-    """Consecutive groups of instance indices whose estimated footprint (nodes x
-    bytes_per_node) stays within budget; raises ValueError for an instance that alone
-    exceeds it."""
+def plan_waves(node_counts: Sequence[int], bytes_per_node: float, budget: float,
+               bytes_per_instance: float = 0.0) -> list:
+    """Consecutive groups of instance indices whose estimated footprint
+    (bytes_per_instance + nodes x bytes_per_node per instance) stays within budget; raises
+    ValueError for an instance that alone exceeds it."""
     waves, cur, used = [], [], 0.0
     for i, nn in enumerate(node_counts):
-        need = float(nn) * bytes_per_node
+        need = bytes_per_instance + float(nn) * bytes_per_node
         if need > budget:
             raise ValueError(f"instance {i} ({nn} nodes, {need / 2**30:.2f} GiB) exceeds the budget "
                              f"of {budget / 2**30:.2f} GiB")
@@ -38,6 +40,24 @@ def plan_waves(node_counts: Sequence[int], bytes_per_node: float, budget: float)
     if cur:
         waves.append(cur)
     return waves
+
+
+def footprint(gl, meshes, params):
+    """(bytes per node, bytes per instance) of a context, from probe contexts of the
+    largest and the smallest instance: the hierarchy's small coarse levels, the Krylov
+    bookkeeping and the per-instance tables weigh more per node on small meshes, so the
+    footprint is fitted as a constant plus a per-node slope through the two probes."""
+    sizes = [int(m.nn) for m in meshes]
+    big, small = int(np.argmax(sizes)), int(np.argmin(sizes))
+    with gl.FemGL(meshes[big], params[big]) as probe:
+        b_big = float(probe.device_bytes)
+    if sizes[small] == sizes[big]:
+        return b_big / sizes[big], 0.0
+    with gl.FemGL(meshes[small], params[small]) as probe:
+        b_small = float(probe.device_bytes)
+    slope = max(0.0, (b_big - b_small) / (sizes[big] - sizes[small]))
+    const = max(0.0, b_small - slope * sizes[small])
+    return slope, const
 
 
 def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: float = 1e-4,
@@ -56,13 +76,11 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
     if not (len(params) == n and len(x0) == n):
         raise ValueError("meshes, params and x0 must have one entry per instance")
     sizes = [int(m.nn) for m in meshes]
-    big = int(np.argmax(sizes))
-    with gl.FemGL(meshes[big], params[big]) as probe:
-        per_node = probe.device_bytes / sizes[big]
+    per_node, per_inst = footprint(gl, meshes, params)
     if budget is None:
         free, _ = gl.mem_info()
         budget = 0.9 * free - 2.0 * 2**30
-    waves = plan_waves(sizes, per_node * margin, budget)
+    waves = plan_waves(sizes, per_node * margin, budget, per_inst * margin)
     res = {"newton_its": np.zeros(n, np.int32), "gmres_its": np.zeros(n, np.int32), "residual": np.zeros(n),
            "free_energy": np.zeros(n), "converged": np.zeros(n, bool), "wave": np.zeros(n, np.int32)}
     sols = [None] * n if keep_solutions else None
@@ -99,7 +117,8 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
                 sols[i] = x[off:off + 18 * sizes[i]].copy()
             off += 18 * sizes[i]
     res.update({"waves": [len(w) for w in waves], "create_s": create_s, "solve_ms": solve_ms,
-                "wave_bytes": wave_bytes, "mg_fallbacks": fallbacks, "bytes_per_node": per_node, "budget": budget})
+                "wave_bytes": wave_bytes, "mg_fallbacks": fallbacks, "bytes_per_node": per_node,
+                "bytes_per_instance": per_inst, "budget": budget})
     if keep_solutions:
         res["solutions"] = sols
     return res
