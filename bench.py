@@ -524,6 +524,13 @@ def main():
     with ClockSampler() as clk:
         mixed = time_mode(gl, m, head_x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
                           flush=flush, precond=pc, cfg=head_cfg)
+    # the same solve with the kernels in plain stream order (programmatic dependent launch off)
+    gl.set_launch_mode(False)
+    try:
+        plain = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                          precond=pc, cfg=head_cfg)
+    finally:
+        gl.set_launch_mode(True)
     e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
     batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc, cfg=head_cfg) if args.batch > 0 else None
 
@@ -590,6 +597,8 @@ def main():
             "newton_its": int(bj["out"]["newton_its"][0]), "gmres_its": int(bj["out"]["gmres_its"][0]),
             "free_energy": bj["F"]},
         "mg_fallbacks": mixed["mg"]["fallbacks"],
+        "launch_mode": {"programmatic_ms_per_solve": ms_step, "plain_ms_per_solve": float(np.mean(plain["ms"])),
+                        "note": "programmatic dependent launch (the default) against plain stream order"},
         "autotune": None if tuned is None else {
             "config": tuned["config"], "ms_best_trial": tuned["ms"], "tuning_s": tuned["tuning_s"],
             "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]]},

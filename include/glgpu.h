@@ -270,6 +270,15 @@ glgpu_status glgpu_mg_level_system(const glgpu_ctx *ctx, int level, int32_t *row
  * every component of a node; restriction is its transpose. */
 glgpu_status glgpu_mg_prolongation(const glgpu_ctx *ctx, int level, int32_t *ptr, int32_t *idx, double *w);
 
+/*
+ * Launch mode of the solve's kernels, process-wide (default 1): with 1 they are launched
+ * with programmatic dependent launch, so each kernel's CTAs are scheduled while its
+ * predecessor finishes and wait on the device (griddepcontrol.wait) before touching
+ * memory; 0 gives plain stream order.  Results are identical; contexts created (and
+ * V-cycle graphs captured) afterwards use the new mode.  No reference counterpart.
+ */
+glgpu_status glgpu_set_launch_mode(int programmatic);
+
 /* Blocks until all work of the context's stream is done. */
 glgpu_status glgpu_sync(glgpu_ctx *ctx);
 

@@ -261,3 +261,27 @@ def test_galerkin_fp16_level(gl):
     r = _bsr(rowptr, cols, vals) @ d - rhs
     fr = np.repeat(np.asarray(m.mask) == 0, 18)  # interior nodes carry no constrained component
     assert int(its[0]) > 0 and np.linalg.norm(r[fr]) <= 2e-5 * np.linalg.norm(rhs)
+
+
+def test_programmatic_launch_gives_identical_solves(gl):
+    """Programmatic dependent launch changes only when CTAs are scheduled: every kernel
+    waits on the device for its predecessor before touching memory, so the mixed
+    multigrid solve (V-cycle graph, matrix-free operator, in-kernel reductions) is
+    bitwise the same with it on and off."""
+    m = gl.cube_mesh(5.0, 10)
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=3)
+    prm = gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID)
+    out = {}
+    try:
+        for mode in (True, False):
+            gl.set_launch_mode(mode)
+            with gl.FemGL(m, prm) as f:
+                f.set_solution(x0)
+                o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+                out[mode] = (o, f.solution())
+    finally:
+        gl.set_launch_mode(True)
+    (o1, x1), (o0, x0b) = out[True], out[False]
+    assert o1["converged"] and o0["converged"]
+    assert np.array_equal(o1["newton_its"], o0["newton_its"]) and np.array_equal(o1["gmres_its"], o0["gmres_its"])
+    assert np.array_equal(x1, x0b)

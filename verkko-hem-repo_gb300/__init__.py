@@ -7,7 +7,7 @@ it in-tree.  The directory name is not a Python identifier, so import it with
 """
 from . import build as build_mod  # noqa: F401
 from .glgpu import (FP64, MIXED, PC_BLOCK_JACOBI, PC_CHEBYSHEV, PC_MULTIGRID, PC_NONE, FemGL, GLGPUError, Mesh, Params, Surrogate,  # noqa: F401
-                    bphase_guess, box_interpolate, box_mesh, box_mesh_refine, cube_mesh, lib, matep, mem_info, pdw_guess, pinned_array, plan_info, plan_kelly, plan_pattern, plan_prolongation,
+                    bphase_guess, box_interpolate, box_mesh, box_mesh_refine, cube_mesh, lib, matep, mem_info, pdw_guess, pinned_array, plan_info, plan_kelly, plan_pattern, plan_prolongation, set_launch_mode,
                     plan_robin,
                     square_mesh)
 

@@ -3,10 +3,43 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
+
 #include <cuda_runtime.h>
 
 namespace glgpu
 {
+// Programmatic dependent launch.  The solve's kernels are launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization, so a kernel's CTAs may be scheduled
+// while the kernel before it in the stream is finishing.  Every such kernel executes
+// pdl_wait() (griddepcontrol.wait: the previous grid has completed and its writes are
+// visible) before it touches memory, in every CTA, so ordering stays transitive along the
+// stream; pdl_trigger() then lets its own successor be scheduled.  glgpu_set_launch_mode
+// turns the attribute off (plain stream order) for comparison.
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args &&...args)
+{
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+#endif
+
 constexpr int kNS3 = 171;   // unique entries of a symmetric 18x18 block
 constexpr int kCoef = 9;    // {K1, K2+K3, alpha, beta1..beta5, K1/bt (0: no Robin term)}
 constexpr int kSegThreads = 256;

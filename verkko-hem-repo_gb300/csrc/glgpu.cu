@@ -10,6 +10,7 @@
 // All device work goes to the context's stream; the host only decides control flow
 // from per-instance scalars (norms, flags) it reads back.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1783,6 +1784,18 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
   if (gmres_its) std::copy(gits.begin(), gits.end(), gmres_its);
   if (final_res) std::copy(fres.begin(), fres.end(), final_res);
   return result;
+}
+
+namespace glgpu
+{
+static std::atomic<bool> g_pdl{true};
+bool pdl_enabled() { return g_pdl.load(std::memory_order_relaxed); }
+} // namespace glgpu
+
+extern "C" glgpu_status glgpu_set_launch_mode(int programmatic)
+{
+  g_pdl.store(programmatic != 0, std::memory_order_relaxed);
+  return GLGPU_OK;
 }
 
 extern "C" glgpu_status glgpu_stop_norms(const glgpu_ctx *c, double *line_search_norm, double *fp64_norm)

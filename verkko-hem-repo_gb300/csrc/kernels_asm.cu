@@ -320,6 +320,8 @@ __global__ void __launch_bounds__(kCellThreads) k_cell3d(DevMesh m, const double
                                                           double *__restrict__ r_cell, double *__restrict__ e_cell,
                                                           const uint8_t *__restrict__ inst_active)
 {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CellSmem<T> &S = *reinterpret_cast<CellSmem<T> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -565,6 +567,8 @@ template <typename R>
 __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__restrict__ x, double *__restrict__ r_cell,
                                                      double *__restrict__ e_cell, const uint8_t *__restrict__ inst_active)
 {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ResSmemT<R> &S = *reinterpret_cast<ResSmemT<R> *>(smem_raw);
   const R ga = from_d<R>(kGa), gb = from_d<R>(kGb);
@@ -932,6 +936,8 @@ constexpr int kRegThreads = 324;
 template <typename T>
 __global__ void __launch_bounds__(kRegThreads) k_rows3d_reg(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ uint32_t s_cmask[27];
   const int64_t n = m.reg_rows[blockIdx.x];
   const int tid = threadIdx.x;
@@ -976,6 +982,8 @@ template <typename T>
 __global__ void __launch_bounds__(kRowThreads) k_rows3d_reg_sym(DevMesh m, const T *__restrict__ H,
                                                                T *__restrict__ vals)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ uint32_t s_cmask[27];
   const int64_t n = m.reg_rows[blockIdx.x];
   const int tid = threadIdx.x;
@@ -1025,6 +1033,8 @@ constexpr int kRowMaxContrib = 96; // contributions staged in shared memory per 
 template <typename T>
 __global__ void __launch_bounds__(kRowThreads) k_rows3d(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
 {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *acc = reinterpret_cast<T *>(smem_raw);
   __shared__ T sD[8 * 8 * 9];
@@ -1149,6 +1159,8 @@ template <typename T, bool WH, bool WR>
 __global__ void k_cell2d(DevMesh m, const double *__restrict__ x, T *__restrict__ Hout, double *__restrict__ r_cell,
                          double *__restrict__ e_cell, const uint8_t *__restrict__ inst_active)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= m.nc) return;
   const int inst = m.cell_inst[e];
@@ -1214,6 +1226,8 @@ __global__ void k_cell2d(DevMesh m, const double *__restrict__ x, T *__restrict_
 template <typename T>
 __global__ void k_rows2d(DevMesh m, const T *__restrict__ H, T *__restrict__ vals)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (n >= m.nn) return;
   const int r0 = m.rowptr[n], nb = m.rowptr[n + 1] - r0;
@@ -1281,6 +1295,8 @@ __global__ void k_rows2d(DevMesh m, const T *__restrict__ H, T *__restrict__ val
 __global__ void k_res_gather(DevMesh m, const double *__restrict__ r_cell, double *__restrict__ R,
                              const uint8_t *__restrict__ inst_active)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= m.nn * m.B) return;
   const int64_t n = idx / m.B;
@@ -1316,12 +1332,12 @@ static cudaError_t launch_cell_t(const DevMesh &m, const double *x, T *H, double
           attr_set = true;
         }
       const int64_t grid = (m.nc + kCPB - 1) / kCPB;
-      k_cell3d<T, WH, WR><<<static_cast<unsigned>(grid), kCellThreads, sm, s>>>(m, x, H, r_cell, e_cell, act);
+      pdl_launch(k_cell3d<T, WH, WR>, static_cast<unsigned>(grid), kCellThreads, sm, s, m, x, H, r_cell, e_cell, act);
     }
   else
     {
       const int64_t grid = (m.nc + 127) / 128;
-      k_cell2d<T, WH, WR><<<static_cast<unsigned>(grid), 128, 0, s>>>(m, x, H, r_cell, e_cell, act);
+      pdl_launch(k_cell2d<T, WH, WR>, static_cast<unsigned>(grid), 128, 0, s, m, x, H, r_cell, e_cell, act);
     }
   return cudaGetLastError();
 }
@@ -1339,7 +1355,7 @@ static cudaError_t launch_res3d(const DevMesh &m, const double *x, double *r_cel
       attr = true;
     }
   const int64_t grid = (m.nc + kRCells - 1) / kRCells;
-  k_res3d<R><<<static_cast<unsigned>(grid), kRThreads, sizeof(ResSmemT<R>), s>>>(m, x, r_cell, e_cell, act);
+  pdl_launch(k_res3d<R>, static_cast<unsigned>(grid), kRThreads, sizeof(ResSmemT<R>), s, m, x, r_cell, e_cell, act);
   return cudaGetLastError();
 }
 
@@ -1373,17 +1389,17 @@ template <typename T> static cudaError_t launch_rows_t(const DevMesh &m, const T
           if (e != cudaSuccess) return e;
           attr = sm;
         }
-      if (m.n_gen > 0) k_rows3d<T><<<static_cast<unsigned>(m.n_gen), kRowThreads, sm, s>>>(m, H, vals);
+      if (m.n_gen > 0) pdl_launch(k_rows3d<T>, static_cast<unsigned>(m.n_gen), kRowThreads, sm, s, m, H, vals);
       if (m.n_reg > 0)
         {
           if (sizeof(T) == 4)
-            k_rows3d_reg<T><<<static_cast<unsigned>(m.n_reg), kRegThreads, 0, s>>>(m, H, vals);
+            pdl_launch(k_rows3d_reg<T>, static_cast<unsigned>(m.n_reg), kRegThreads, 0, s, m, H, vals);
           else
-            k_rows3d_reg_sym<T><<<static_cast<unsigned>(m.n_reg), kRowThreads, 0, s>>>(m, H, vals);
+            pdl_launch(k_rows3d_reg_sym<T>, static_cast<unsigned>(m.n_reg), kRowThreads, 0, s, m, H, vals);
         }
     }
   else
-    k_rows2d<T><<<static_cast<unsigned>((m.nn + 127) / 128), 128, 0, s>>>(m, H, vals);
+    pdl_launch(k_rows2d<T>, static_cast<unsigned>((m.nn + 127) / 128), 128, 0, s, m, H, vals);
   return cudaGetLastError();
 }
 
@@ -1407,6 +1423,8 @@ __global__ void __launch_bounds__(kRobinThreads) k_robin_res(DevMesh m, const do
                                                              double *__restrict__ r_cell, double *__restrict__ e_cell,
                                                              const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double xs[144];
   __shared__ double red[kRobinThreads / 32];
   const int64_t e = m.robin_cells[blockIdx.x];
@@ -1444,14 +1462,14 @@ cudaError_t launch_robin_res(const DevMesh &m, const double *x, double *r_cell, 
 {
   if (m.n_robin == 0) return cudaSuccess;
   if (m.dim != 3 || m.B != 18 || !m.robin || !m.robin_cells) return cudaErrorInvalidValue;
-  k_robin_res<<<static_cast<unsigned>(m.n_robin), kRobinThreads, 0, s>>>(m, x, r_cell, e_cell, act);
+  pdl_launch(k_robin_res, static_cast<unsigned>(m.n_robin), kRobinThreads, 0, s, m, x, r_cell, e_cell, act);
   return cudaGetLastError();
 }
 
 cudaError_t launch_res_gather(const DevMesh &m, const double *r_cell, double *R, const uint8_t *act, cudaStream_t s)
 {
   const int64_t n = m.nn * m.B;
-  k_res_gather<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(m, r_cell, R, act);
+  pdl_launch(k_res_gather, static_cast<unsigned>((n + 255) / 256), 256, 0, s, m, r_cell, R, act);
   return cudaGetLastError();
 }
 

@@ -142,6 +142,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_spmv18(DevMesh m, const MT 
                                                             const T *__restrict__ x, T *__restrict__ y,
                                                             const uint8_t *__restrict__ act, const T *__restrict__ b)
 {
+  pdl_wait();
+  pdl_trigger();
   constexpr int NV = Vec16<MT>::n;
   constexpr int NIT = (324 / NV + 31) / 32;
   __shared__ T red[kSpmvWarps][324];
@@ -179,6 +181,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_smooth18(DevMesh m, const M
                                                               const T *__restrict__ z, T *__restrict__ y, T omega,
                                                               const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   using V = typename Vec16<T>::type;
   constexpr int NV = Vec16<T>::n;
   constexpr int NCH = 324 / NV;
@@ -241,6 +245,8 @@ template <typename T>
 __global__ void k_spmv2(DevMesh m, const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y,
                         const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (n >= m.nn) return;
   if (act && !act[m.node_inst[n]]) return;
@@ -267,7 +273,7 @@ static void spmv18_t(const DevMesh &m, const void *vals, const void *x, void *y,
 {
   constexpr int rows = kSpmvWarps / WPR;
   const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
-  k_spmv18<T, MT, RES, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const MT *>(vals),
+  pdl_launch(k_spmv18<T, MT, RES, WPR>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const MT *>(vals),
                                                               static_cast<const T *>(x), static_cast<T *>(y), act,
                                                               static_cast<const T *>(b));
 }
@@ -303,10 +309,10 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
       if (b) return cudaErrorInvalidValue; // the residual form exists for 18x18 blocks only
       const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
       if (fp32)
-        k_spmv2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(vals), static_cast<const float *>(x),
+        pdl_launch(k_spmv2<float>, grid, 256, 0, s, m, static_cast<const float *>(vals), static_cast<const float *>(x),
                                             static_cast<float *>(y), act);
       else
-        k_spmv2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(vals), static_cast<const double *>(x),
+        pdl_launch(k_spmv2<double>, grid, 256, 0, s, m, static_cast<const double *>(vals), static_cast<const double *>(x),
                                              static_cast<double *>(y), act);
     }
   return cudaGetLastError();
@@ -322,6 +328,8 @@ __global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, cons
                                                                  const T *__restrict__ b, T *__restrict__ y, T omega,
                                                                  const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T b_s[kSzNodes][18];
   const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kSzNodes + ln;
@@ -342,7 +350,7 @@ static void smooth18_t(const DevMesh &m, const void *vals, const void *dinv, con
 {
   constexpr int rows = kSpmvWarps / WPR;
   const unsigned grid = static_cast<unsigned>((m.nn + rows - 1) / rows);
-  k_smooth18<T, MT, WPR><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const MT *>(vals),
+  pdl_launch(k_smooth18<T, MT, WPR>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const MT *>(vals),
                                                            static_cast<const T *>(dinv), static_cast<const T *>(b),
                                                            static_cast<const T *>(z), static_cast<T *>(y),
                                                            static_cast<T>(omega), act);
@@ -365,11 +373,11 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kSzNodes - 1) / kSzNodes);
       if (fp32)
-        k_smooth_zero18<float><<<grid, kSzNodes * 18, 0, s>>>(m, static_cast<const float *>(dinv),
+        pdl_launch(k_smooth_zero18<float>, grid, kSzNodes * 18, 0, s, m, static_cast<const float *>(dinv),
                                                              static_cast<const float *>(b), static_cast<float *>(y),
                                                              static_cast<float>(omega), act);
       else
-        k_smooth_zero18<double><<<grid, kSzNodes * 18, 0, s>>>(m, static_cast<const double *>(dinv),
+        pdl_launch(k_smooth_zero18<double>, grid, kSzNodes * 18, 0, s, m, static_cast<const double *>(dinv),
                                                               static_cast<const double *>(b), static_cast<double *>(y),
                                                               omega, act);
       return cudaGetLastError();
@@ -394,6 +402,8 @@ template <typename T, typename MT = T>
 __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const MT *__restrict__ vals,
                                                               T *__restrict__ dinv, int l1)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T M[kBjWarps][18][37];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kBjWarps + warp;
@@ -482,6 +492,8 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const M
 template <typename T>
 __global__ void k_bj_setup2(DevMesh m, const T *__restrict__ vals, T *__restrict__ dinv)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (n >= m.nn) return;
   const T *D = vals + static_cast<int64_t>(m.diag[n]) * 4;
@@ -510,22 +522,22 @@ cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void 
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kBjWarps - 1) / kBjWarps);
       if (fp32 && m.half_vals)
-        k_bj_setup18<float, __half><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const __half *>(vals),
+        pdl_launch(k_bj_setup18<float, __half>, grid, kBjWarps * 32, 0, s, m, static_cast<const __half *>(vals),
                                                                    static_cast<float *>(dinv), l1 ? 1 : 0);
       else if (fp32)
-        k_bj_setup18<float><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv),
+        pdl_launch(k_bj_setup18<float>, grid, kBjWarps * 32, 0, s, m, static_cast<const float *>(vals), static_cast<float *>(dinv),
                                                            l1 ? 1 : 0);
       else
-        k_bj_setup18<double><<<grid, kBjWarps * 32, 0, s>>>(m, static_cast<const double *>(vals),
+        pdl_launch(k_bj_setup18<double>, grid, kBjWarps * 32, 0, s, m, static_cast<const double *>(vals),
                                                             static_cast<double *>(dinv), l1 ? 1 : 0);
     }
   else
     {
       const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
       if (fp32)
-        k_bj_setup2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(vals), static_cast<float *>(dinv));
+        pdl_launch(k_bj_setup2<float>, grid, 256, 0, s, m, static_cast<const float *>(vals), static_cast<float *>(dinv));
       else
-        k_bj_setup2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(vals), static_cast<double *>(dinv));
+        pdl_launch(k_bj_setup2<double>, grid, 256, 0, s, m, static_cast<const double *>(vals), static_cast<double *>(dinv));
     }
   return cudaGetLastError();
 }
@@ -536,6 +548,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_bj_apply18(DevMesh m, const
                                                                 const T *__restrict__ x, T *__restrict__ y,
                                                                 const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   using V = typename Vec16<T>::type;
   constexpr int NV = Vec16<T>::n;
   constexpr int NCH = 324 / NV;
@@ -578,6 +592,8 @@ template <typename T>
 __global__ void k_bj_apply2(DevMesh m, const T *__restrict__ dinv, const T *__restrict__ x, T *__restrict__ y,
                             const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (n >= m.nn) return;
   if (act && !act[m.node_inst[n]]) return;
@@ -594,10 +610,10 @@ cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const
     {
       const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
       if (fp32)
-        k_bj_apply18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(dinv),
+        pdl_launch(k_bj_apply18<float>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const float *>(dinv),
                                                             static_cast<const float *>(x), static_cast<float *>(y), act);
       else
-        k_bj_apply18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(dinv),
+        pdl_launch(k_bj_apply18<double>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const double *>(dinv),
                                                              static_cast<const double *>(x), static_cast<double *>(y),
                                                              act);
     }
@@ -605,10 +621,10 @@ cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const
     {
       const unsigned grid = static_cast<unsigned>((m.nn + 255) / 256);
       if (fp32)
-        k_bj_apply2<float><<<grid, 256, 0, s>>>(m, static_cast<const float *>(dinv), static_cast<const float *>(x),
+        pdl_launch(k_bj_apply2<float>, grid, 256, 0, s, m, static_cast<const float *>(dinv), static_cast<const float *>(x),
                                                 static_cast<float *>(y), act);
       else
-        k_bj_apply2<double><<<grid, 256, 0, s>>>(m, static_cast<const double *>(dinv), static_cast<const double *>(x),
+        pdl_launch(k_bj_apply2<double>, grid, 256, 0, s, m, static_cast<const double *>(dinv), static_cast<const double *>(x),
                                                  static_cast<double *>(y), act);
     }
   return cudaGetLastError();
@@ -638,6 +654,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_mdot(DevMesh m, const TX *_
                                                           const TY *__restrict__ y, double *__restrict__ partial,
                                                           const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ TY ys[kSegMax];
   const int s = blockIdx.x;
   const int64_t b = m.seg_begin[s];
@@ -688,10 +706,10 @@ cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t 
                             double *partial, const uint8_t *act, cudaStream_t s)
 {
   if (fp32)
-    k_seg_mdot<float, float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+    pdl_launch(k_seg_mdot<float, float>, m.n_seg, kSegThreads, 0, s, m, static_cast<const float *>(X), ld, nvec,
                                                              static_cast<const float *>(y), partial, act);
   else
-    k_seg_mdot<double, double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+    pdl_launch(k_seg_mdot<double, double>, m.n_seg, kSegThreads, 0, s, m, static_cast<const double *>(X), ld, nvec,
                                                                static_cast<const double *>(y), partial, act);
   return cudaGetLastError();
 }
@@ -702,6 +720,8 @@ cudaError_t launch_seg_mdot(const DevMesh &m, bool fp32, const void *X, int64_t 
 __global__ void k_seg_finalize(DevMesh m, const double *__restrict__ partial, int nvec, double *__restrict__ out,
                                int ld_out, int take_sqrt)
 {
+  pdl_wait();
+  pdl_trigger();
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= m.n_inst * nvec) return;
   const int inst = w / nvec, v = w % nvec;
@@ -726,7 +746,7 @@ cudaError_t launch_seg_finalize(const DevMesh &m, const double *partial, int nve
                                 int take_sqrt, cudaStream_t s)
 {
   const int nw = m.n_inst * nvec;
-  k_seg_finalize<<<(nw + 3) / 4, 128, 0, s>>>(m, partial, nvec, out, ld_out, take_sqrt);
+  pdl_launch(k_seg_finalize, (nw + 3) / 4, 128, 0, s, m, partial, nvec, out, ld_out, take_sqrt);
   return cudaGetLastError();
 }
 
@@ -740,6 +760,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_update(DevMesh m, const T *
                                                             double *__restrict__ partial_norm,
                                                             const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T cf[64];
   __shared__ T ys[kSegMax];
   const int s = blockIdx.x;
@@ -805,10 +827,10 @@ cudaError_t launch_seg_update(const DevMesh &m, bool fp32, const void *X, int64_
 {
   if (nvec > 64) return cudaErrorInvalidValue;
   if (fp32)
-    k_seg_update<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec, coef, ldc,
+    pdl_launch(k_seg_update<float>, m.n_seg, kSegThreads, 0, s, m, static_cast<const float *>(X), ld, nvec, coef, ldc,
                                                         static_cast<float *>(y), nvec2, partial2, partial_norm, act);
   else
-    k_seg_update<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec, coef, ldc,
+    pdl_launch(k_seg_update<double>, m.n_seg, kSegThreads, 0, s, m, static_cast<const double *>(X), ld, nvec, coef, ldc,
                                                          static_cast<double *>(y), nvec2, partial2, partial_norm, act);
   return cudaGetLastError();
 }
@@ -824,6 +846,8 @@ __global__ void __launch_bounds__(kSegThreads) k_seg_axpby(DevMesh m, const TX *
                                                            const TZ *__restrict__ z, Axpby k,
                                                            const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int s = blockIdx.x;
   const int inst = m.seg_inst[s];
   if (act && !act[inst]) return;
@@ -848,10 +872,10 @@ static void axpby_z(const DevMesh &m, const void *x, void *y, bool z32, const vo
                     const uint8_t *act, cudaStream_t s)
 {
   if (z32)
-    k_seg_axpby<TX, TY, float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const TX *>(x), static_cast<TY *>(y),
+    pdl_launch(k_seg_axpby<TX, TY, float>, m.n_seg, kSegThreads, 0, s, m, static_cast<const TX *>(x), static_cast<TY *>(y),
                                                                static_cast<const float *>(z), k, act);
   else
-    k_seg_axpby<TX, TY, double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const TX *>(x), static_cast<TY *>(y),
+    pdl_launch(k_seg_axpby<TX, TY, double>, m.n_seg, kSegThreads, 0, s, m, static_cast<const TX *>(x), static_cast<TY *>(y),
                                                                 static_cast<const double *>(z), k, act);
 }
 
@@ -871,6 +895,8 @@ cudaError_t launch_seg_axpby(const DevMesh &m, bool x32, const void *x, bool y32
 __global__ void k_trial(DevMesh m, const double *__restrict__ x, const double *__restrict__ dl,
                         const double *__restrict__ a, double *__restrict__ xt, const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= m.nn * m.B) return;
   const int64_t n = idx / m.B;
@@ -899,13 +925,15 @@ cudaError_t launch_trial(const DevMesh &m, const double *x, const double *delta,
                          const uint8_t *act, cudaStream_t s)
 {
   const int64_t n = m.nn * m.B;
-  k_trial<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(m, x, delta, a, xt, act);
+  pdl_launch(k_trial, static_cast<unsigned>((n + 255) / 256), 256, 0, s, m, x, delta, a, xt, act);
   return cudaGetLastError();
 }
 
 // two passes: Dirichlet zeros on regular nodes, then hanging nodes from parents
 __global__ void k_dist_regular(DevMesh m, double *__restrict__ v)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= m.nn * m.B) return;
   const int64_t n = idx / m.B;
@@ -915,6 +943,8 @@ __global__ void k_dist_regular(DevMesh m, double *__restrict__ v)
 
 __global__ void k_dist_hanging(DevMesh m, double *__restrict__ v)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= m.nn * m.B) return;
   const int64_t n = idx / m.B;
@@ -929,8 +959,8 @@ cudaError_t launch_distribute(const DevMesh &m, double *v, cudaStream_t s)
 {
   const int64_t n = m.nn * m.B;
   const unsigned grid = static_cast<unsigned>((n + 255) / 256);
-  k_dist_regular<<<grid, 256, 0, s>>>(m, v);
-  k_dist_hanging<<<grid, 256, 0, s>>>(m, v);
+  pdl_launch(k_dist_regular, grid, 256, 0, s, m, v);
+  pdl_launch(k_dist_hanging, grid, 256, 0, s, m, v);
   return cudaGetLastError();
 }
 
@@ -938,6 +968,8 @@ cudaError_t launch_distribute(const DevMesh &m, double *v, cudaStream_t s)
 __global__ void __launch_bounds__(kSegThreads) k_cell_sum(DevMesh m, const double *__restrict__ ec,
                                                           double *__restrict__ out)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double sh[kSegThreads / 32];
   const int inst = blockIdx.x;
   const int64_t b = m.cell_off[inst], e = m.cell_off[inst + 1];
@@ -949,7 +981,7 @@ __global__ void __launch_bounds__(kSegThreads) k_cell_sum(DevMesh m, const doubl
 
 cudaError_t launch_cell_sum(const DevMesh &m, const double *e_cell, double *out, cudaStream_t s)
 {
-  k_cell_sum<<<m.n_inst, kSegThreads, 0, s>>>(m, e_cell, out);
+  pdl_launch(k_cell_sum, m.n_inst, kSegThreads, 0, s, m, e_cell, out);
   return cudaGetLastError();
 }
 
@@ -958,6 +990,8 @@ cudaError_t launch_cell_sum(const DevMesh &m, const double *e_cell, double *out,
 // ---------------------------------------------------------------------------------
 __global__ void k_gmres_start(GmresDev g, int n_inst, const uint8_t *__restrict__ solve_active)
 {
+  pdl_wait();
+  pdl_trigger();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_inst) return;
   const double beta = g.beta[k];
@@ -972,13 +1006,15 @@ __global__ void k_gmres_start(GmresDev g, int n_inst, const uint8_t *__restrict_
 
 cudaError_t launch_gmres_start(const GmresDev &g, int n_inst, const uint8_t *solve_active, cudaStream_t s)
 {
-  k_gmres_start<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst, solve_active);
+  pdl_launch(k_gmres_start, (n_inst + 127) / 128, 128, 0, s, g, n_inst, solve_active);
   return cudaGetLastError();
 }
 
 // hcol[k][0..j] + hcol2[k][0..j]: projections; hcol[k][j+1]: norm of the new vector
 __global__ void k_gmres_column(GmresDev g, int n_inst, int j)
 {
+  pdl_wait();
+  pdl_trigger();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_inst) return;
   if (!g.active[k])
@@ -1025,13 +1061,15 @@ __global__ void k_gmres_column(GmresDev g, int n_inst, int j)
 cudaError_t launch_gmres_column(const GmresDev &g, int n_inst, int j, cudaStream_t s)
 {
   if (g.m > 64) return cudaErrorInvalidValue;
-  k_gmres_column<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst, j);
+  pdl_launch(k_gmres_column, (n_inst + 127) / 128, 128, 0, s, g, n_inst, j);
   return cudaGetLastError();
 }
 
 // y = H(0:its,0:its)^-1 g(0:its); stored negated so that maxpy (y -= sum c_v V_v) adds V y
 __global__ void k_gmres_solve_y(GmresDev g, int n_inst)
 {
+  pdl_wait();
+  pdl_trigger();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_inst) return;
   const int m = g.m, nk = g.its[k];
@@ -1051,12 +1089,14 @@ __global__ void k_gmres_solve_y(GmresDev g, int n_inst)
 
 cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s)
 {
-  k_gmres_solve_y<<<(n_inst + 127) / 128, 128, 0, s>>>(g, n_inst);
+  pdl_launch(k_gmres_solve_y, (n_inst + 127) / 128, 128, 0, s, g, n_inst);
   return cudaGetLastError();
 }
 
 __global__ void k_inv(const double *__restrict__ in, double *__restrict__ out, int n)
 {
+  pdl_wait();
+  pdl_trigger();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const double v = in[k];
@@ -1065,7 +1105,7 @@ __global__ void k_inv(const double *__restrict__ in, double *__restrict__ out, i
 
 cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s)
 {
-  k_inv<<<(n + 127) / 128, 128, 0, s>>>(in, out, n);
+  pdl_launch(k_inv, (n + 127) / 128, 128, 0, s, in, out, n);
   return cudaGetLastError();
 }
 
@@ -1133,6 +1173,8 @@ __global__ void __launch_bounds__(kSegThreads) k_arnoldi_dot(DevMesh m, const T 
                                                              unsigned int *__restrict__ cnt,
                                                              const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T ys[kSegMax];
   const int s = blockIdx.x;
   const int inst = m.seg_inst[s];
@@ -1216,6 +1258,8 @@ __global__ void __launch_bounds__(kSegThreads) k_arnoldi_update(DevMesh m, const
                                                                 double *__restrict__ partial, GmresDev g,
                                                                 unsigned int *__restrict__ cnt)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T cf[64];
   __shared__ T ys[kSegMax];
   const int s = blockIdx.x;
@@ -1306,6 +1350,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_bj_apply_scale18(DevMesh m,
                                                                       const double *__restrict__ scale,
                                                                       const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   using V = typename Vec16<T>::type;
   constexpr int NV = Vec16<T>::n;
   constexpr int NCH = 324 / NV;
@@ -1352,10 +1398,10 @@ cudaError_t launch_arnoldi_dot(const DevMesh &m, bool fp32, const void *X, int64
                                cudaStream_t s)
 {
   if (fp32)
-    k_arnoldi_dot<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+    pdl_launch(k_arnoldi_dot<float>, m.n_seg, kSegThreads, 0, s, m, static_cast<const float *>(X), ld, nvec,
                                                          static_cast<const float *>(w), partial, hout, ldh, cnt, act);
   else
-    k_arnoldi_dot<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+    pdl_launch(k_arnoldi_dot<double>, m.n_seg, kSegThreads, 0, s, m, static_cast<const double *>(X), ld, nvec,
                                                           static_cast<const double *>(w), partial, hout, ldh, cnt, act);
   return cudaGetLastError();
 }
@@ -1365,10 +1411,10 @@ cudaError_t launch_arnoldi_update(const DevMesh &m, bool fp32, const void *X, in
 {
   if (nvec > 64 || g.m > 64) return cudaErrorInvalidValue;
   if (fp32)
-    k_arnoldi_update<float><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const float *>(X), ld, nvec,
+    pdl_launch(k_arnoldi_update<float>, m.n_seg, kSegThreads, 0, s, m, static_cast<const float *>(X), ld, nvec,
                                                             static_cast<float *>(w), mode, j, partial, g, cnt);
   else
-    k_arnoldi_update<double><<<m.n_seg, kSegThreads, 0, s>>>(m, static_cast<const double *>(X), ld, nvec,
+    pdl_launch(k_arnoldi_update<double>, m.n_seg, kSegThreads, 0, s, m, static_cast<const double *>(X), ld, nvec,
                                                              static_cast<double *>(w), mode, j, partial, g, cnt);
   return cudaGetLastError();
 }
@@ -1379,11 +1425,11 @@ cudaError_t launch_bj_apply_scale(const DevMesh &m, bool fp32, const void *dinv,
   if (m.B != 18) return cudaErrorInvalidValue;
   const unsigned grid = static_cast<unsigned>((m.nn + kSpmvWarps - 1) / kSpmvWarps);
   if (fp32)
-    k_bj_apply_scale18<float><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const float *>(dinv),
+    pdl_launch(k_bj_apply_scale18<float>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const float *>(dinv),
                                                                static_cast<float *>(x), static_cast<float *>(y), scale,
                                                                act);
   else
-    k_bj_apply_scale18<double><<<grid, kSpmvWarps * 32, 0, s>>>(m, static_cast<const double *>(dinv),
+    pdl_launch(k_bj_apply_scale18<double>, grid, kSpmvWarps * 32, 0, s, m, static_cast<const double *>(dinv),
                                                                 static_cast<double *>(x), static_cast<double *>(y),
                                                                 scale, act);
   return cudaGetLastError();

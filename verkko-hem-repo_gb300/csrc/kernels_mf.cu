@@ -339,6 +339,8 @@ __global__ void __launch_bounds__(16 * NC, 32 / NC) k_mf_cell(DevMesh m, const f
                                                         const float *__restrict__ z, float *__restrict__ ycell,
                                                         const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 16 * NC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   MfSmem<NC> &S = *reinterpret_cast<MfSmem<NC> *>(smem_raw);
@@ -586,6 +588,8 @@ __global__ void __launch_bounds__(kMgThreads, 5) k_mf_gather(DevMesh m, const fl
                                                           const float *__restrict__ dinv, float *__restrict__ y,
                                                           float omega, int mode, const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float t_s[kMgNodes][18];
   const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kMgNodes + ln;
@@ -651,6 +655,8 @@ constexpr int kRobinMfThreads = 160;
 __global__ void __launch_bounds__(kRobinMfThreads) k_robin_mf(DevMesh m, const float *__restrict__ z,
                                                               float *__restrict__ ycell, const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float zs[144];
   const int64_t e = m.robin_cells[blockIdx.x];
   const int inst = m.cell_inst[e];
@@ -687,7 +693,7 @@ cudaError_t launch_robin_mf(const DevMesh &m, const float *z, float *ycell, cons
 {
   if (m.n_robin == 0) return cudaSuccess;
   if (m.dim != 3 || m.B != 18 || !m.robin || !m.robin_cells) return cudaErrorInvalidValue;
-  k_robin_mf<<<static_cast<unsigned>(m.n_robin), kRobinMfThreads, 0, s>>>(m, z, ycell, act);
+  pdl_launch(k_robin_mf, static_cast<unsigned>(m.n_robin), kRobinMfThreads, 0, s, m, z, ycell, act);
   return cudaGetLastError();
 }
 
@@ -704,7 +710,7 @@ static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float
       attr = true;
     }
   const int64_t gc = (m.nc + NC - 1) / NC;
-  k_mf_cell<NC><<<static_cast<unsigned>(gc), 16 * NC, sizeof(MfSmem<NC>), s>>>(m, xs, z, ycell, act);
+  pdl_launch(k_mf_cell<NC>, static_cast<unsigned>(gc), 16 * NC, sizeof(MfSmem<NC>), s, m, xs, z, ycell, act);
   return cudaGetLastError();
 }
 
@@ -721,7 +727,7 @@ cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *
   if (e != cudaSuccess) return e;
   if ((e = launch_robin_mf(m, z, ycell, act, s)) != cudaSuccess) return e;
   const int64_t gn = (m.nn + kMgNodes - 1) / kMgNodes;
-  k_mf_gather<<<static_cast<unsigned>(gn), kMgThreads, 0, s>>>(m, ycell, z, b, dinv, y, omega, mode, act);
+  pdl_launch(k_mf_gather, static_cast<unsigned>(gn), kMgThreads, 0, s, m, ycell, z, b, dinv, y, omega, mode, act);
   return cudaGetLastError();
 }
 

@@ -25,6 +25,8 @@ __global__ void k_prolong_add(int64_t nn_f, int B, const int32_t *__restrict__ p
                               const int32_t *__restrict__ node_inst, const uint8_t *__restrict__ act,
                               const T *__restrict__ base)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= nn_f * B) return;
   const int64_t n = t / B;
@@ -47,6 +49,8 @@ __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr,
                            const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ node_inst,
                            const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= nn_c * B) return;
   const int64_t n = t / B;
@@ -71,6 +75,8 @@ __global__ void __launch_bounds__(kRsNodes * 18)
                     const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ node_inst,
                     const uint8_t *__restrict__ act, const T *__restrict__ dinv, T omega, T *__restrict__ z)
 {
+  pdl_wait();
+  pdl_trigger();
   __shared__ T t_s[kRsNodes][18];
   const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kRsNodes + ln;
@@ -159,6 +165,8 @@ __global__ void __launch_bounds__(kGalWarps * 32)
              const int64_t *__restrict__ g_toff, const int32_t *__restrict__ g_blk, const T *__restrict__ g_w,
              const IN *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   using V = typename GVec<T>::type;
   constexpr int NV = GVec<T>::n;
   constexpr int NCH = 324 / NV;
@@ -216,7 +224,7 @@ cudaError_t launch_prolong_add(int64_t nn_f, int B, const int32_t *ptr, const in
                                const int32_t *node_inst, const uint8_t *act, const void *base, cudaStream_t s)
 {
   const int64_t n = nn_f * B;
-  k_prolong_add<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
+  pdl_launch(k_prolong_add<T>, static_cast<unsigned>((n + 255) / 256), 256, 0, s, 
     nn_f, B, ptr, idx, static_cast<const T *>(w), static_cast<const T *>(zc), static_cast<T *>(zf), mask_f, hptr_f,
     node_inst, act, static_cast<const T *>(base));
   return cudaGetLastError();
@@ -237,10 +245,10 @@ cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, 
   const int64_t n = nn_c * B;
   const unsigned g = static_cast<unsigned>((n + 255) / 256);
   if (fp32)
-    k_restrict<float><<<g, 256, 0, s>>>(nn_c, B, ptr, idx, static_cast<const float *>(w),
+    pdl_launch(k_restrict<float>, g, 256, 0, s, nn_c, B, ptr, idx, static_cast<const float *>(w),
                                         static_cast<const float *>(rf), static_cast<float *>(rc), mask_c, node_inst, act);
   else
-    k_restrict<double><<<g, 256, 0, s>>>(nn_c, B, ptr, idx, static_cast<const double *>(w),
+    pdl_launch(k_restrict<double>, g, 256, 0, s, nn_c, B, ptr, idx, static_cast<const double *>(w),
                                          static_cast<const double *>(rf), static_cast<double *>(rc), mask_c, node_inst,
                                          act);
   return cudaGetLastError();
@@ -252,11 +260,11 @@ cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, 
 {
   const unsigned g = static_cast<unsigned>((nn_c + kRsNodes - 1) / kRsNodes);
   if (fp32)
-    k_restrict_smooth<float><<<g, kRsNodes * 18, 0, s>>>(
+    pdl_launch(k_restrict_smooth<float>, g, kRsNodes * 18, 0, s, 
       nn_c, ptr, idx, static_cast<const float *>(w), static_cast<const float *>(rf), static_cast<float *>(rc), mask_c,
       node_inst, act, static_cast<const float *>(dinv), static_cast<float>(omega), static_cast<float *>(z));
   else
-    k_restrict_smooth<double><<<g, kRsNodes * 18, 0, s>>>(
+    pdl_launch(k_restrict_smooth<double>, g, kRsNodes * 18, 0, s, 
       nn_c, ptr, idx, static_cast<const double *>(w), static_cast<const double *>(rf), static_cast<double *>(rc), mask_c,
       node_inst, act, static_cast<const double *>(dinv), omega, static_cast<double *>(z));
   return cudaGetLastError();
@@ -273,23 +281,23 @@ cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, con
   const unsigned g = static_cast<unsigned>(grid);
   const float *wf = static_cast<const float *>(g_w);
   if (fp32 && half_in && half_out)
-    k_galerkin<float, __half, __half><<<g, kGalWarps * 32, 0, s>>>(
+    pdl_launch(k_galerkin<float, __half, __half>, g, kGalWarps * 32, 0, s, 
       nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
       static_cast<const __half *>(vals_f), node_inst_c, act);
   else if (fp32 && half_out)
-    k_galerkin<float, float, __half><<<g, kGalWarps * 32, 0, s>>>(
+    pdl_launch(k_galerkin<float, float, __half>, g, kGalWarps * 32, 0, s, 
       nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
       static_cast<const float *>(vals_f), node_inst_c, act);
   else if (fp32 && half_in)
-    k_galerkin<float, __half, float><<<g, kGalWarps * 32, 0, s>>>(
+    pdl_launch(k_galerkin<float, __half, float>, g, kGalWarps * 32, 0, s, 
       nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
       static_cast<const __half *>(vals_f), node_inst_c, act);
   else if (fp32)
-    k_galerkin<float, float, float><<<g, kGalWarps * 32, 0, s>>>(
+    pdl_launch(k_galerkin<float, float, float>, g, kGalWarps * 32, 0, s, 
       nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
       static_cast<const float *>(vals_f), node_inst_c, act);
   else if (!fp32 && !half_in && !half_out)
-    k_galerkin<double, double, double><<<g, kGalWarps * 32, 0, s>>>(
+    pdl_launch(k_galerkin<double, double, double>, g, kGalWarps * 32, 0, s, 
       nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<double *>(vals_c), g_toff, g_blk,
       static_cast<const double *>(g_w), static_cast<const double *>(vals_f), node_inst_c, act);
   else
@@ -318,6 +326,8 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
                                                              const int64_t *__restrict__ dense_off,
                                                              float *__restrict__ inv, int *__restrict__ singular)
 {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ float W[]; // [nd][ld]
   __shared__ float colk[kMaxDense];
   __shared__ int prow[kMaxDense];
@@ -453,6 +463,8 @@ template <typename T>
 __global__ void k_dense_apply(DevMesh m, const int64_t *__restrict__ dense_off, const float *__restrict__ inv,
                               const T *__restrict__ r, T *__restrict__ z, const uint8_t *__restrict__ act)
 {
+  pdl_wait();
+  pdl_trigger();
   const int inst = blockIdx.y;
   if (act && !act[inst]) return;
   const int64_t n0 = m.node_off_ptr[inst], n1 = m.node_off_ptr[inst + 1];
@@ -478,7 +490,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
       cudaError_t e = cudaFuncSetAttribute(k_dense_invert<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
-      k_dense_invert<__half><<<m.n_inst, kGjThreads, sm, s>>>(m, static_cast<const __half *>(vals), dense_off, inv,
+      pdl_launch(k_dense_invert<__half>, m.n_inst, kGjThreads, sm, s, m, static_cast<const __half *>(vals), dense_off, inv,
                                                               singular);
     }
   else if (fp32)
@@ -486,7 +498,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
       cudaError_t e = cudaFuncSetAttribute(k_dense_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
-      k_dense_invert<float><<<m.n_inst, kGjThreads, sm, s>>>(m, static_cast<const float *>(vals), dense_off, inv,
+      pdl_launch(k_dense_invert<float>, m.n_inst, kGjThreads, sm, s, m, static_cast<const float *>(vals), dense_off, inv,
                                                              singular);
     }
   else
@@ -494,7 +506,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
       cudaError_t e = cudaFuncSetAttribute(k_dense_invert<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
-      k_dense_invert<double><<<m.n_inst, kGjThreads, sm, s>>>(m, static_cast<const double *>(vals), dense_off, inv,
+      pdl_launch(k_dense_invert<double>, m.n_inst, kGjThreads, sm, s, m, static_cast<const double *>(vals), dense_off, inv,
                                                               singular);
     }
   return cudaGetLastError();
@@ -505,10 +517,10 @@ cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const in
 {
   dim3 g((max_nd * 32 + 255) / 256, m.n_inst);
   if (fp32)
-    k_dense_apply<float><<<g, 256, 0, s>>>(m, dense_off, inv, static_cast<const float *>(r), static_cast<float *>(z),
+    pdl_launch(k_dense_apply<float>, g, 256, 0, s, m, dense_off, inv, static_cast<const float *>(r), static_cast<float *>(z),
                                            act);
   else
-    k_dense_apply<double><<<g, 256, 0, s>>>(m, dense_off, inv, static_cast<const double *>(r),
+    pdl_launch(k_dense_apply<double>, g, 256, 0, s, m, dense_off, inv, static_cast<const double *>(r),
                                             static_cast<double *>(z), act);
   return cudaGetLastError();
 }

@@ -89,6 +89,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_free_energy.argtypes = [vp, _dp]
     L.glgpu_run.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _ip, _ip, _dp]
     L.glgpu_stop_norms.argtypes = [vp, _dp, _dp]
+    L.glgpu_set_launch_mode.argtypes = [ctypes.c_int]
     L.glgpu_get_system.argtypes = [vp, _ip, _ip, _dp, _dp]
     L.glgpu_get_residual.argtypes = [vp, _dp]
     L.glgpu_get_update.argtypes = [vp, _dp]
@@ -328,6 +329,12 @@ def pdw_guess(p: float, t: float, xyz: np.ndarray, u: float, half_D: float, scc:
     x = np.zeros(18 * nn)
     _check(lib().glgpu_pdw_guess(float(p), float(t), int(bool(scc)), float(u), float(half_D), int(nn), _p(xyz), _p(x)))
     return x
+
+
+def set_launch_mode(programmatic: bool) -> None:
+    """Programmatic dependent launch of the solve's kernels (default on); contexts created
+    afterwards use the new mode."""
+    _check(lib().glgpu_set_launch_mode(int(bool(programmatic))))
 
 
 def bphase_guess(p: float, t: float, nn: int, noise: float = 0.0, seed: int = 0, scc: bool = True) -> np.ndarray:
