@@ -715,10 +715,10 @@ def config5_leg(gl, n_train, n_test, linear_tol, n_test_cells=48):
     """The learned initial guess at scale: the surrogate is trained on n_train converged
     slab states (seeded (t, p, D), 8^3-12^3 cells, solved in waves from the uniform B
     phase), then n_test held-out (t, p, D) slab instances of n_test_cells^3 cells are
-    solved in waves (mixed precision, multigrid) from three starts: the surrogate's guess
-    (inference inside the timed region), the configurations' B phase + 0.05 N(0,1), and
-    the uniform B phase.  Reports solves/s, Newton and GMRES iterations and the
-    free-energy agreement between the starts."""
+    solved in waves (mixed precision, multigrid) from three starts on the same wave
+    contexts: the surrogate's guess (its inference inside the timed region), the
+    configurations' B phase + 0.05 N(0,1), and the uniform B phase.  Reports solves/s,
+    Newton and GMRES iterations and the free-energy agreement between the starts."""
     L = importlib.import_module("verkko-hem-repo_gb300.learned")
     S = importlib.import_module("verkko-hem-repo_gb300.sweep")
     t0 = time.perf_counter()
@@ -731,33 +731,66 @@ def config5_leg(gl, n_train, n_test, linear_tol, n_test_cells=48):
         t = float(rng.uniform(0.3, 0.95))
         p = float(min(rng.uniform(0.0, 34.0), 34.0 - 1e-9))
         D = float(rng.uniform(8.0, 40.0))
+        test.append((t, p, D))
+
+    def make(k):
+        t, p, D = test[k]
         m = gl.box_mesh([-L.L_HALF, -L.L_HALF, -D / 2], [L.L_HALF, L.L_HALF, D / 2], (n_test_cells,) * 3)
-        test.append(L.Instance(t, p, D, n_test_cells, m))
+        return L.Instance(t, p, D, n_test_cells, m)
+
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        test = list(ex.map(make, range(n_test)))
     prms = [gl.Params.from_matep(d.p, d.t, precision=gl.MIXED, precond=gl.PC_MULTIGRID) for d in test]
     meshes = [d.mesh for d in test]
+    slope, const = S.footprint(gl, meshes, prms)
+    free, _ = gl.mem_info()
+    waves = S.plan_waves([m.nn for m in meshes], slope * 1.1, 0.9 * free - 2.0 * 2**30, const * 1.1)
+    starts = {
+        "learned": lambda idx: L.guess(gl, sur, [test[i] for i in idx]),
+        "bphase_noise": lambda idx: [gl.bphase_guess(test[i].p, test[i].t, test[i].mesh.nn, noise=NOISE, seed=7000 + i)
+                                     for i in idx],
+        "bphase_uniform": lambda idx: [gl.bphase_guess(test[i].p, test[i].t, test[i].mesh.nn) for i in idx],
+    }
+    acc = {k: {"s": 0.0, "start_s": 0.0, "newton": [], "gmres": [], "res": [], "F": [], "ok": []} for k in starts}
+    setup_s = 0.0
+    for w in waves:
+        t0 = time.perf_counter()
+        with gl.FemGL([meshes[i] for i in w], [prms[i] for i in w]) as f:
+            setup_s += time.perf_counter() - t0
+            # untimed warm-up: one-time work of a new context (V-cycle graph capture, kernel
+            # attributes) is paid before any start is timed
+            f.set_solution(np.concatenate(starts["bphase_uniform"](w)))
+            f.assemble_system()
+            f.solve(1e-1, allow_unconverged=True)
+            for name, mk in starts.items():
+                t0 = time.perf_counter()
+                x0 = np.concatenate(mk(w))  # inference (learned start) is timed with the solve
+                f.set_solution(x0)
+                f.sync()
+                t_start = time.perf_counter() - t0
+                f.event_start()
+                o = f.run(max_newton=40, linear_tol=linear_tol, converge_acc=TOL, allow_unconverged=True)
+                a = acc[name]
+                a["s"] += f.event_stop() / 1000.0 + t_start
+                a["start_s"] += t_start
+                a["newton"] += o["newton_its"].tolist()
+                a["gmres"] += o["gmres_its"].tolist()
+                a["res"] += o["residual"].tolist()
+                a["F"] += f.free_energy().tolist()
+    sur.close()
     out = {"train": {"states": ginfo["converged"], "instances": n_train, "rows": tinfo["rows"],
                      "generation_s": t_gen, "training_s": tinfo["train_s"], "loss": tinfo["loss"],
                      "components_kept": tinfo["components_kept"]},
-           "test_instances": n_test, "test_cells": n_test_cells}
-    starts = {
-        "learned": lambda: L.guess(gl, sur, test),
-        "bphase_noise": lambda: L.bphase_starts(gl, test, NOISE, 7000),
-        "bphase_uniform": lambda: L.bphase_starts(gl, test, 0.0, 0),
-    }
-    F = {}
-    for name, mk in starts.items():
-        t0 = time.perf_counter()
-        x0 = mk()
-        t_start = time.perf_counter() - t0
-        r = S.solve_sweep(gl, meshes, prms, x0, linear_tol=linear_tol, converge_acc=TOL)
-        solve_s = sum(r["solve_ms"]) / 1000.0
-        F[name] = r["free_energy"]
-        out[name] = {"solves_per_s": n_test / (solve_s + t_start), "start_s": t_start, "solve_s": solve_s,
-                     "newton_its_total": int(r["newton_its"].sum()), "gmres_its_total": int(r["gmres_its"].sum()),
-                     "newton_its_mean": float(r["newton_its"].mean()), "gmres_its_mean": float(r["gmres_its"].mean()),
-                     "all_converged": bool(r["converged"].all()), "max_final_residual": float(r["residual"].max()),
-                     "waves": r["waves"]}
-    sur.close()
+           "test_instances": n_test, "test_cells": n_test_cells, "waves": [len(w) for w in waves],
+           "context_setup_s": setup_s}
+    F = {k: np.array(a["F"]) for k, a in acc.items()}
+    for name, a in acc.items():
+        out[name] = {"solves_per_s": n_test / a["s"], "time_s": a["s"], "start_s": a["start_s"],
+                     "newton_its_total": int(sum(a["newton"])), "gmres_its_total": int(sum(a["gmres"])),
+                     "newton_its_mean": float(np.mean(a["newton"])), "gmres_its_mean": float(np.mean(a["gmres"])),
+                     "all_converged": bool(np.all(np.array(a["res"]) <= TOL)), "max_final_residual": float(max(a["res"]))}
     for name in ("bphase_noise", "bphase_uniform"):
         out[f"learned_speedup_vs_{name}"] = out["learned"]["solves_per_s"] / out[name]["solves_per_s"]
         out[f"max_free_energy_rel_diff_vs_{name}"] = float(np.max(np.abs(F["learned"] - F[name]) / np.abs(F[name])))

@@ -108,6 +108,10 @@ typedef struct
                            Robin term (K1/bt) int |A_t|^2 dS of the pair-breaking faces
                            (assemble.cc:286-348, residual.cc:235-278), A_t = A with the face's
                            normal column zeroed; default 1e10 (no Robin term); must be > 0 */
+  double mg_coarse_shift; /* multigrid: the coarsest level is solved with the dense inverse of
+                           A + mg_coarse_shift * mean|diag A| * 1 (default 1e-4).  The shift bounds
+                           the amplification of the near-null modes (global phase and spin
+                           rotations are exact symmetries of the functional); must be > 0 */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;

@@ -119,8 +119,11 @@ def test_config2_mixed_multigrid_matches_oracle(gl, oracle_gl, cube32, oracle_so
     assert out["converged"]
     assert out["residual"][0] == out["residual_fp64"][0] <= 1e-10
     Rg, Fg = sysr.residual(x)
-    # the FP64 stop-test value is the oracle's residual norm at the same state
-    assert abs(np.linalg.norm(Rg) - out["residual_fp64"][0]) <= 1e-12 * np.linalg.norm(Rg) + 1e-20
+    # the FP64 stop-test value is the oracle's residual norm at the same state.  At a
+    # converged state |R| ~ 1e-11 is what is left of O(1) terms that cancel, so two FP64
+    # evaluations that sum in different orders agree on it to ~1e-15 absolute (1e-5 relative)
+    assert abs(np.linalg.norm(Rg) - out["residual_fp64"][0]) <= 1e-14, (np.linalg.norm(Rg), out["residual_fp64"])
+    assert np.linalg.norm(Rg) <= 1.5e-10
     assert abs(F[0] - Fg) <= 1e-12 * abs(Fg)
     # up to the exact symmetries (see the FP64 test)
     xa, _, _ = oracle_gl.gauge_align(x, xr)

@@ -268,7 +268,7 @@ cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, con
                             const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
                             const uint8_t *act, cudaStream_t s, bool half_in = false, bool half_out = false);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
-                               float *inv, int *singular, cudaStream_t s);
+                               float *inv, int *singular, float shift, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,
                                const void *r, void *z, const uint8_t *act, cudaStream_t s);
 

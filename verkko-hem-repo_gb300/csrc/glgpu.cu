@@ -848,7 +848,8 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
     }
   glgpu_ctx *Lc = c->lv[c->n_levels - 1];
   CKS(launch(c, KK_PREC, 1, [&] {
-    return launch_dense_setup(Lc->dm, c->mixed, Lc->vals, c->d_dense_off, c->max_nd, c->d_inv, c->d_sing, c->st);
+    return launch_dense_setup(Lc->dm, c->mixed, Lc->vals, c->d_dense_off, c->max_nd, c->d_inv, c->d_sing,
+                              static_cast<float>(c->prm[0].mg_coarse_shift), c->st);
   }));
   return GLGPU_OK;
 }
@@ -1064,6 +1065,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->mf_cells = 8;
   p->prec_reuse = 0.0;
   p->bt = 1e10;
+  p->mg_coarse_shift = 1e-4;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1083,6 +1085,8 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
     }
   for (int k = 0; k < n_inst; ++k)
     if (!(prm[k].bt > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_create: bt (AdGR diffuse length) must be > 0");
+  for (int k = 0; k < n_inst; ++k)
+    if (!(prm[k].mg_coarse_shift > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_create: mg_coarse_shift must be > 0");
   if (prm[0].gmres_restart < 1 || prm[0].gmres_restart > 64)
     return set_error(GLGPU_ERR_ARG, "glgpu_create: gmres_restart must be in [1, 64]");
   if (prm[0].mf_cells != 4 && prm[0].mf_cells != 8 && prm[0].mf_cells != 16)

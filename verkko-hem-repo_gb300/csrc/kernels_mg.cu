@@ -312,7 +312,6 @@ cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, con
 // ---------------------------------------------------------------------------------
 constexpr int kGjThreads = 1024;      // (augmented column, row chunk) pairs
 constexpr int kMaxDense = 160;        // largest coarsest system (unknowns per instance)
-constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest solve
 
 // Gauss-Jordan on [A + shift I | I] with implicit partial pivoting: in step k one warp
 // picks the largest unused entry of column k (row p_k) and snapshots the column; then
@@ -324,7 +323,8 @@ constexpr float kCoarseShift = 1e-4f; // relative diagonal shift of the coarsest
 template <typename T>
 __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T *__restrict__ vals,
                                                              const int64_t *__restrict__ dense_off,
-                                                             float *__restrict__ inv, int *__restrict__ singular)
+                                                             float *__restrict__ inv, int *__restrict__ singular,
+                                                             float shift)
 {
   pdl_wait();
   pdl_trigger();
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       if (lane == 0)
         {
           s_sing = 0;
-          s_shift = kCoarseShift * sd / static_cast<float>(nd);
+          s_shift = shift * sd / static_cast<float>(nd);
         }
     }
   __syncthreads();
@@ -481,7 +481,7 @@ __global__ void k_dense_apply(DevMesh m, const int64_t *__restrict__ dense_off, 
 }
 
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
-                               float *inv, int *singular, cudaStream_t s)
+                               float *inv, int *singular, float shift, cudaStream_t s)
 {
   const size_t sm = static_cast<size_t>(max_nd) * (2 * max_nd + 1) * sizeof(float);
   if (max_nd > kMaxDense || sm > 227 * 1024) return cudaErrorInvalidValue;
@@ -491,7 +491,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
       pdl_launch(k_dense_invert<__half>, m.n_inst, kGjThreads, sm, s, m, static_cast<const __half *>(vals), dense_off, inv,
-                                                              singular);
+                                                              singular, shift);
     }
   else if (fp32)
     {
@@ -499,7 +499,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
       pdl_launch(k_dense_invert<float>, m.n_inst, kGjThreads, sm, s, m, static_cast<const float *>(vals), dense_off, inv,
-                                                             singular);
+                                                             singular, shift);
     }
   else
     {
@@ -507,7 +507,7 @@ cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, co
                                            static_cast<int>(sm));
       if (e != cudaSuccess) return e;
       pdl_launch(k_dense_invert<double>, m.n_inst, kGjThreads, sm, s, m, static_cast<const double *>(vals), dense_off, inv,
-                                                              singular);
+                                                              singular, shift);
     }
   return cudaGetLastError();
 }

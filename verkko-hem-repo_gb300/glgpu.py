@@ -59,7 +59,7 @@ class _Params(ctypes.Structure):
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
                 ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
                 ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double),
-                ("bt", ctypes.c_double)]
+                ("bt", ctypes.c_double), ("mg_coarse_shift", ctypes.c_double)]
 
 
 _lib = None
@@ -427,6 +427,8 @@ class Params:
     prec_reuse: float = 0.0
     #: "AdGR diffuse length": bt < 1e10 adds the Robin term (K1/bt) |A_t|^2 on the pair-breaking faces
     bt: float = 1e10
+    #: multigrid: relative diagonal shift of the coarsest level's dense solve
+    mg_coarse_shift: float = 1e-4
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -446,6 +448,7 @@ class Params:
         s.mf_cells = int(self.mf_cells)
         s.prec_reuse = float(self.prec_reuse)
         s.bt = float(self.bt)
+        s.mg_coarse_shift = float(self.mg_coarse_shift)
         return s
 
 
