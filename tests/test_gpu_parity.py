@@ -253,7 +253,13 @@ def test_complexgl_2d_matches_oracle(gl, oracle_gl, n, L):
             break
     _, Fo = sysr.residual(xo)
     assert out["converged"] and out["newton_its"][0] == it + 1
-    assert np.abs(x - xo).max() <= 1e-9 * max(1.0, np.abs(xo).max())
+    # psi -> e^{i phi} psi is an exact symmetry (the psi = 0 edge keeps it), so the two
+    # Newton runs may stop at different points of the same orbit: compare after the phase
+    # that best aligns them
+    psi, ref = x[0::2] + 1j * x[1::2], xo[0::2] + 1j * xo[1::2]
+    psi = psi * np.exp(1j * np.angle(np.vdot(psi, ref)))
+    xa = np.stack([psi.real, psi.imag], axis=1).ravel()
+    assert np.abs(xa - xo).max() <= 1e-9 * max(1.0, np.abs(xo).max()), np.abs(xa - xo).max()
     assert abs(F[0] - Fo) <= 1e-9 * max(1.0, abs(Fo))
     if L > 1.0:
         # ordered bulk: |psi|^2 -> -alpha/beta = 2 away from the Dirichlet edge

@@ -62,18 +62,6 @@ __device__ __forceinline__ C2 sub2(C2 a, C2 b) { return __fadd2_rn(a, c2(-b.x, -
 __device__ __forceinline__ C2 scl2(C2 a, float s) { return __fmul2_rn(a, c2(s, s)); }
 // c + a s, s real (both lanes)
 __device__ __forceinline__ C2 macr(C2 a, float s, C2 c) { return __ffma2_rn(a, c2(s, s), c); }
-// c + a b, complex
-__device__ __forceinline__ C2 cmac(C2 a, C2 b, C2 c)
-{
-  c = __ffma2_rn(c2(a.x, a.x), b, c);
-  return __ffma2_rn(c2(-a.y, a.y), c2(b.y, b.x), c);
-}
-// c + a conj(b)
-__device__ __forceinline__ C2 cmacc(C2 a, C2 b, C2 c)
-{
-  c = __ffma2_rn(c2(a.x, a.x), c2(b.x, -b.y), c);
-  return __ffma2_rn(c2(a.y, a.y), c2(b.y, b.x), c);
-}
 // Gauss values of a linear function with end values f0, f1
 __device__ __forceinline__ void gauss2(C2 f0, C2 f1, C2 &q0, C2 &q1)
 {
@@ -131,15 +119,18 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 {
   const float w1 = 2.f * cf[1], w2 = 2.f * cf[2], w3 = 2.f * cf[3], w4 = 2.f * cf[4], w5 = 2.f * cf[5];
   const float wp = w4 + w5, wm = w4 - w5;
-  C2 L[9], R[9]; // left factors of the real and imaginary parts
+  // left factors of the real and imaginary parts of the right factor (A for role 0, F for
+  // role 1), as separate real and imaginary arrays: the complex-by-complex products below
+  // run as scalar FMAs
+  float Lr[9], Li[9], Rr[9], Ri[9];
   if constexpr (ROLE == 0)
     {
-      C2 dp = c2(0.f, 0.f);
-      float dq = 0.f;
+      float dpr = 0.f, dpi = 0.f, dq = 0.f;
 #pragma unroll
       for (int k = 0; k < 9; ++k)
         {
-          dp = cmac(A[k], F[k], dp);
+          dpr = fmaf(A[k].x, F[k].x, fmaf(-A[k].y, F[k].y, dpr));
+          dpi = fmaf(A[k].x, F[k].y, fmaf(A[k].y, F[k].x, dpi));
           dq = fmaf(A[k].x, F[k].x, fmaf(A[k].y, F[k].y, dq));
         }
       // Y2 in L: S3 = A F^T, symmetrised
@@ -148,10 +139,16 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           {
-            C2 acc = c2(0.f, 0.f);
+            float sr = 0.f, si = 0.f;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) acc = cmac(A[3 * i + k], F[3 * j + k], acc);
-            L[3 * i + j] = acc;
+            for (int k = 0; k < 3; ++k)
+              {
+                const C2 a = A[3 * i + k], f = F[3 * j + k];
+                sr = fmaf(a.x, f.x, fmaf(-a.y, f.y, sr));
+                si = fmaf(a.x, f.y, fmaf(a.y, f.x, si));
+              }
+            Lr[3 * i + j] = sr;
+            Li[3 * i + j] = si;
           }
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -159,11 +156,12 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 #pragma unroll
           for (int j = i + 1; j < 3; ++j)
             {
-              const C2 s = scl2(add2(L[3 * i + j], L[3 * j + i]), w3);
-              L[3 * i + j] = s;
-              L[3 * j + i] = s;
+              const float sr = w3 * (Lr[3 * i + j] + Lr[3 * j + i]), si = w3 * (Li[3 * i + j] + Li[3 * j + i]);
+              Lr[3 * i + j] = Lr[3 * j + i] = sr;
+              Li[3 * i + j] = Li[3 * j + i] = si;
             }
-          L[4 * i] = __ffma2_rn(L[4 * i], c2(2.f * w3, 2.f * w3), scl2(dp, 2.f * w1));
+          Lr[4 * i] = fmaf(2.f * w3, Lr[4 * i], 2.f * w1 * dpr);
+          Li[4 * i] = fmaf(2.f * w3, Li[4 * i], 2.f * w1 * dpi);
         }
       // Y1 in R: S4 = F A^+; Re part (w4 + w5)(Sr + Sr^T), Im part (w4 - w5)(Si - Si^T)
 #pragma unroll
@@ -171,10 +169,16 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 #pragma unroll
         for (int j = 0; j < 3; ++j)
           {
-            C2 acc = c2(0.f, 0.f);
+            float sr = 0.f, si = 0.f;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) acc = cmacc(F[3 * i + k], A[3 * j + k], acc);
-            R[3 * i + j] = acc;
+            for (int k = 0; k < 3; ++k)
+              {
+                const C2 f = F[3 * i + k], a = A[3 * j + k];
+                sr = fmaf(f.x, a.x, fmaf(f.y, a.y, sr));
+                si = fmaf(f.y, a.x, fmaf(-f.x, a.y, si));
+              }
+            Rr[3 * i + j] = sr;
+            Ri[3 * i + j] = si;
           }
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -182,30 +186,34 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 #pragma unroll
           for (int j = i + 1; j < 3; ++j)
             {
-              const float sr = wp * (R[3 * i + j].x + R[3 * j + i].x);
-              const float si = wm * (R[3 * i + j].y - R[3 * j + i].y);
-              R[3 * i + j] = c2(sr, si);
-              R[3 * j + i] = c2(sr, -si);
+              const float sr = wp * (Rr[3 * i + j] + Rr[3 * j + i]);
+              const float si = wm * (Ri[3 * i + j] - Ri[3 * j + i]);
+              Rr[3 * i + j] = Rr[3 * j + i] = sr;
+              Ri[3 * i + j] = si;
+              Ri[3 * j + i] = -si;
             }
-          R[4 * i] = c2(fmaf(2.f * wp, R[4 * i].x, 2.f * w2 * dq), 0.f);
+          Rr[4 * i] = fmaf(2.f * wp, Rr[4 * i], 2.f * w2 * dq);
+          Ri[4 * i] = 0.f;
         }
-      // (Y1 + Y2) and i (Y1 - Y2)
+      // (Y1 + Y2) in L and i (Y1 - Y2) in R
 #pragma unroll
       for (int k = 0; k < 9; ++k)
         {
-          const C2 y1 = R[k], y2 = L[k];
-          L[k] = add2(y1, y2);
-          R[k] = c2(y2.y - y1.y, y1.x - y2.x);
+          const float y1r = Rr[k], y1i = Ri[k], y2r = Lr[k], y2i = Li[k];
+          Lr[k] = y1r + y2r;
+          Li[k] = y1i + y2i;
+          Rr[k] = y2i - y1i;
+          Ri[k] = y1r - y2r;
         }
     }
   else
     {
-      C2 p = c2(0.f, 0.f);
-      float q = 0.f;
+      float pr = 0.f, pi = 0.f, q = 0.f;
 #pragma unroll
       for (int k = 0; k < 9; ++k)
         {
-          p = cmac(A[k], A[k], p);
+          pr = fmaf(A[k].x, A[k].x, fmaf(-A[k].y, A[k].y, pr));
+          pi = fmaf(2.f * A[k].x, A[k].y, pi);
           q = fmaf(A[k].x, A[k].x, fmaf(A[k].y, A[k].y, q));
         }
       // M in L, N in R
@@ -214,47 +222,59 @@ __device__ __forceinline__ void hvp_role(const C2 (&A)[9], const C2 (&F)[9], con
 #pragma unroll
         for (int j = i; j < 3; ++j)
           {
-            C2 P = c2(0.f, 0.f), Q = c2(0.f, 0.f);
+            float Pr = 0.f, Pi = 0.f, Qr = 0.f, Qi = 0.f;
 #pragma unroll
             for (int k = 0; k < 3; ++k)
               {
-                P = cmac(A[3 * i + k], A[3 * j + k], P);
-                Q = cmacc(A[3 * i + k], A[3 * j + k], Q);
+                const C2 a = A[3 * i + k], b = A[3 * j + k];
+                Pr = fmaf(a.x, b.x, fmaf(-a.y, b.y, Pr));
+                Pi = fmaf(a.x, b.y, fmaf(a.y, b.x, Pi));
+                Qr = fmaf(a.x, b.x, fmaf(a.y, b.y, Qr));
+                Qi = fmaf(a.y, b.x, fmaf(-a.x, b.y, Qi));
               }
             if (i == j)
               {
-                L[4 * i] = c2(cf[0] + w2 * q + wp * Q.x, 0.f);
-                R[4 * i] = __ffma2_rn(P, c2(w3, w3), scl2(p, w1));
+                Lr[4 * i] = cf[0] + w2 * q + wp * Qr;
+                Li[4 * i] = 0.f;
+                Rr[4 * i] = fmaf(w3, Pr, w1 * pr);
+                Ri[4 * i] = fmaf(w3, Pi, w1 * pi);
               }
             else
               {
-                L[3 * i + j] = c2(wp * Q.x, wm * Q.y);
-                L[3 * j + i] = c2(wp * Q.x, -wm * Q.y);
-                R[3 * i + j] = R[3 * j + i] = scl2(P, w3);
+                Lr[3 * i + j] = Lr[3 * j + i] = wp * Qr;
+                Li[3 * i + j] = wm * Qi;
+                Li[3 * j + i] = -wm * Qi;
+                Rr[3 * i + j] = Rr[3 * j + i] = w3 * Pr;
+                Ri[3 * i + j] = Ri[3 * j + i] = w3 * Pi;
               }
           }
 #pragma unroll
       for (int k = 0; k < 9; ++k)
         {
-          const C2 m = L[k], n = R[k];
-          L[k] = add2(m, n);
-          R[k] = c2(n.y - m.y, m.x - n.x);
+          const float mr = Lr[k], mi = Li[k], nr = Rr[k], ni = Ri[k];
+          Lr[k] = mr + nr;
+          Li[k] = mi + ni;
+          Rr[k] = ni - mi;
+          Ri[k] = mr - nr;
         }
     }
+  // out = L Re(B) + R Im(B): complex-by-real products, each real entry of B broadcast to a
+  // pair once and used for the three rows
   const C2(&B)[9] = ROLE == 0 ? A : F;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int k = 0; k < 9; ++k) out[k] = c2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       {
-        C2 o = c2(0.f, 0.f);
+        const C2 br = c2(B[3 * k + j].x, B[3 * k + j].x), bi = c2(B[3 * k + j].y, B[3 * k + j].y);
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 3; ++i)
           {
-            o = macr(L[3 * i + k], B[3 * k + j].x, o);
-            o = macr(R[3 * i + k], B[3 * k + j].y, o);
+            out[3 * i + j] = __ffma2_rn(c2(Lr[3 * i + k], Li[3 * i + k]), br, out[3 * i + j]);
+            out[3 * i + j] = __ffma2_rn(c2(Rr[3 * i + k], Ri[3 * i + k]), bi, out[3 * i + j]);
           }
-        out[3 * i + j] = o;
       }
 }
 
@@ -335,7 +355,7 @@ __device__ __forceinline__ void mf_contract(const C2 (&w)[8], const C2 (&F)[3][8
 }
 
 template <int NC>
-__global__ void __launch_bounds__(16 * NC, 32 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
+__global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
                                                         const float *__restrict__ z, float *__restrict__ ycell,
                                                         const uint8_t *__restrict__ act)
 {

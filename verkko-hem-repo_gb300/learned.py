@@ -5,9 +5,9 @@ femgl/src/setup_uniform_B-phase.cc:238-259):
 
 1. converged states: batched mixed-precision Newton solves of seeded (t, p, D) slab
    instances from the uniform B phase (`generate`).  The uniform start has the symmetry of
-   the slab (real, diagonal, u11 = u22), and Newton keeps it, so every training state lies
-   in one gauge: the global phase and spin rotations, exact symmetries of the functional,
-   are fixed by the data rather than left to a random draw;
+   the slab (real, diagonal, u11 = u22); every converged state is then moved into one
+   gauge (`canonical_gauge`): the global phase and spin rotations, exact symmetries of the
+   functional, are fixed for the data rather than left to rounding;
 2. training: the tcgen05 MLP of :class:`Surrogate` is fitted on per-node
    (features -> order parameter / bulk amplitude) pairs (`train`); the components that
    vanish in every training state (the symmetry zeros) are recorded;
@@ -120,11 +120,33 @@ def generate(gl, count: int, seed: int = 11, n_lo: int = 10, n_hi: int = 14, per
         if not good:
             continue
         f = features(d.mesh, d.t, d.p, d.D)
-        y = (x.reshape(-1, 18) / amplitude(gl, d.t, d.p)).astype(np.float32)
+        y = (canonical_gauge(x).reshape(-1, 18) / amplitude(gl, d.t, d.p)).astype(np.float32)
         idx = rng.choice(f.shape[0], size=min(per_instance, f.shape[0]), replace=False)
         X.append(f[idx])
         Y.append(y[idx])
     return np.concatenate(X), np.concatenate(Y), {"instances": count, "solve_ms": ms, "converged": int(np.sum(ok))}
+
+
+def canonical_gauge(x: np.ndarray, iters: int = 20) -> np.ndarray:
+    """The state moved by the functional's exact symmetries (a global phase e^{i phi} and a
+    spin rotation R acting on the spin index: A -> e^{i phi} R A) so that its mean order
+    parameter is as close as possible to a positive multiple of the identity, i.e. the
+    real diagonal form of the (distorted) B phase.  Converged states carry small arbitrary
+    rotations: FP32 rounding in the linear solves is amplified along the near-null rotation
+    directions.  (phi, R) maximise Re tr(e^{i phi} R C), C = sum over nodes of A, by
+    alternating the phase and an orthogonal Procrustes rotation."""
+    X = np.asarray(x, np.float64).reshape(-1, 18)
+    A = (X[:, :9] + 1j * X[:, 9:]).reshape(-1, 3, 3)
+    C = A.sum(axis=0)
+    R = np.eye(3)
+    phi = 0.0
+    for _ in range(iters):
+        phi = -float(np.angle(np.trace(R @ C)))
+        U, _, Vt = np.linalg.svd(np.real(np.exp(1j * phi) * C))
+        D = np.diag([1.0, 1.0, np.sign(np.linalg.det(Vt.T @ U.T))])
+        R = Vt.T @ D @ U.T
+    Al = np.exp(1j * phi) * np.einsum("ij,njk->nik", R, A)
+    return np.concatenate([Al.real.reshape(-1, 9), Al.imag.reshape(-1, 9)], axis=1).reshape(-1)
 
 
 def symmetry_zeros(Y, rel: float = 1e-4) -> np.ndarray:
