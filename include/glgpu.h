@@ -112,11 +112,6 @@ typedef struct
                            A + mg_coarse_shift * mean|diag A| * 1 (default 1e-4).  The shift bounds
                            the amplification of the near-null modes (global phase and spin
                            rotations are exact symmetries of the functional); must be > 0 */
-  int sym_deflate;      /* multigrid, 3D: 1 keeps the flexible GMRES basis free of the exact symmetry
-                           directions (global phase, spin rotations) at the current state, which are
-                           nearly null near a solution: every preconditioned direction is projected
-                           off them, and while the last Newton step was not yet short the generators
-                           themselves open the basis; 0 (default) off */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;

@@ -285,26 +285,3 @@ def test_programmatic_launch_gives_identical_solves(gl):
     assert o1["converged"] and o0["converged"]
     assert np.array_equal(o1["newton_its"], o0["newton_its"]) and np.array_equal(o1["gmres_its"], o0["gmres_its"])
     assert np.array_equal(x1, x0b)
-
-
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_symmetry_deflation_reaches_the_same_solution(gl, oracle_gl, precision):
-    """With the exact-symmetry directions kept out of the flexible GMRES basis the Newton
-    solve converges to the same free energy and, up to the global phase and spin
-    rotation, the same state; the FP64 stop test holds as before."""
-    prec = gl.MIXED if precision == "mixed" else gl.FP64
-    m = gl.cube_mesh(5.0, 10)
-    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=4)
-    res = {}
-    for sym in (False, True):
-        prm = gl.Params.from_matep(20.0, 0.6, precision=prec, precond=gl.PC_MULTIGRID, sym_deflate=sym)
-        with gl.FemGL(m, prm) as f:
-            f.set_solution(x0)
-            o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
-            res[sym] = (o, f.solution(), f.free_energy()[0], f.mg_fallbacks)
-    (o0, x_0, F0, _), (o1, x_1, F1, fb1) = res[False], res[True]
-    assert o0["converged"] and o1["converged"] and o1["residual"][0] <= 1e-10
-    assert fb1 == 0
-    assert abs(F1 - F0) <= 1e-9 * abs(F0)
-    xa, _, _ = oracle_gl.gauge_align(x_1, x_0)
-    assert np.abs(xa - x_0).max() <= 1e-7 * np.abs(x_0).max()

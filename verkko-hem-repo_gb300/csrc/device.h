@@ -244,11 +244,6 @@ cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);
 // scale factors for the new basis vector from the norm (inv_scale = 1/norm or 0)
 cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s);
 
-// The four generators of the functional's exact symmetries at the state x (global phase,
-// three spin rotations), t[k * ld + i] in the Krylov precision, zero on constrained rows and
-// zero-Dirichlet components (3D, 18 components).
-cudaError_t launch_sym_gen(const DevMesh &m, bool fp32, const double *x, void *t, int64_t ld, cudaStream_t s);
-
 // ---- multigrid (kernels_mg.cu) ----
 // zf = base + P zc, or zf += P zc when base is nullptr (constrained components keep base)
 cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,

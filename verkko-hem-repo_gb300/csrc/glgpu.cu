@@ -146,12 +146,6 @@ struct glgpu_ctx
   int *d_sing = nullptr;
   int max_nd = 0;
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
-  // symmetry deflation (flexible GMRES, 3D): generators T [4][N] of the exact symmetries at
-  // the current state, an orthonormal basis Q [4][N] of their span per instance, the Gram
-  // matrices [n_inst][16], the combination coefficients [n_inst][16], projection scratch
-  void *symT = nullptr, *symQ = nullptr;
-  double *sym_gram = nullptr, *sym_w = nullptr, *sym_coef = nullptr;
-  int sym_k = 0;                     // directions kept in every instance (0: none)
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   // per instance, the last glgpu_run step's |R|: the line search's value and the FP64 value
@@ -592,130 +586,6 @@ glgpu_status vcycle_run(glgpu_ctx *c, const void *r, void *z)
 }
 
 // ---------------------------------------------------------------------------------
-// Symmetry deflation of the flexible GMRES basis.  The functional is invariant under a
-// global phase and spin rotations, so R(x) is orthogonal to their generators T(x) and the
-// Jacobian maps T to L R (the generators applied to the residual): near a solution these
-// four directions are nearly null.  The exact Newton step then has an O(1) part along
-// them that GMRES resolves only through the tiny eigenvalues, at the cost of extra
-// iterations, while that part only moves the state along the symmetry orbit.
-//   - projection: every preconditioned direction Z_j loses its component in span(T), so
-//     the Krylov space never contains the near-null directions.  Restricting the step to
-//     span(T)^perp leaves a residual floor of about 2 |delta| / |x| relative to |rhs|
-//     (|J T| ~ |R|), harmless once the last Newton step was short;
-//   - augmentation (earlier steps, where the floor could exceed the tolerance): the first
-//     directions of the first restart cycle are the orthonormalised generators
-//     themselves, so the step can still use them, and GMRES resolves them in its small
-//     least-squares problem instead of through the preconditioned Krylov space.
-// ---------------------------------------------------------------------------------
-namespace
-{
-// eigen-decomposition of a symmetric 4x4 matrix (cyclic Jacobi): columns of V, values in d
-void jacobi4(double (&a)[4][4], double (&v)[4][4], double (&d)[4])
-{
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) v[i][j] = (i == j) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 50; ++sweep)
-    {
-      double off = 0.0;
-      for (int p = 0; p < 4; ++p)
-        for (int q = p + 1; q < 4; ++q) off += a[p][q] * a[p][q];
-      if (off < 1e-30) break;
-      for (int p = 0; p < 4; ++p)
-        for (int q = p + 1; q < 4; ++q)
-          {
-            if (std::fabs(a[p][q]) < 1e-300) continue;
-            const double th = 0.5 * (a[q][q] - a[p][p]) / a[p][q];
-            const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-            const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
-            for (int k = 0; k < 4; ++k)
-              {
-                const double akp = a[k][p], akq = a[k][q];
-                a[k][p] = cs * akp - sn * akq;
-                a[k][q] = sn * akp + cs * akq;
-              }
-            for (int k = 0; k < 4; ++k)
-              {
-                const double apk = a[p][k], aqk = a[q][k];
-                a[p][k] = cs * apk - sn * aqk;
-                a[q][k] = sn * apk + cs * aqk;
-              }
-            for (int k = 0; k < 4; ++k)
-              {
-                const double vkp = v[k][p], vkq = v[k][q];
-                v[k][p] = cs * vkp - sn * vkq;
-                v[k][q] = sn * vkp + cs * vkq;
-              }
-          }
-    }
-  for (int i = 0; i < 4; ++i) d[i] = a[i][i];
-}
-
-// T and an orthonormal basis Q of span(T) per instance at the current state
-glgpu_status sym_setup(glgpu_ctx *c)
-{
-  const bool m32 = c->mixed;
-  const int n = c->n_inst;
-  const int64_t N = c->N;
-  CKS(launch(c, KK_VEC, 1, [&] { return launch_sym_gen(c->dm, m32, c->x, c->symT, N, c->st); }));
-  for (int v = 0; v < 4; ++v)
-    {
-      void *tv = tptr(c, c->symT, v * N);
-      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m32, c->symT, N, 4, tv, c->partial, nullptr, c->st); }));
-      CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, 4, c->sym_gram + 4 * v, 16, 0, c->st); }));
-    }
-  std::vector<double> G(static_cast<size_t>(n) * 16), W(static_cast<size_t>(n) * 16, 0.0);
-  CK(cudaMemcpyAsync(G.data(), c->sym_gram, sizeof(double) * 16 * n, cudaMemcpyDeviceToHost, c->st));
-  CKS(sync(c));
-  int keep_min = 4;
-  for (int k = 0; k < n; ++k)
-    {
-      double a[4][4], V[4][4], d[4];
-      for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) a[i][j] = 0.5 * (G[16 * k + 4 * i + j] + G[16 * k + 4 * j + i]);
-      jacobi4(a, V, d);
-      int ord[4] = {0, 1, 2, 3};
-      std::sort(ord, ord + 4, [&](int x, int y) { return d[x] > d[y]; });
-      const double dmax = std::max(d[ord[0]], 0.0);
-      int keep = 0;
-      for (int col = 0; col < 4; ++col)
-        {
-          const int e = ord[col];
-          if (!(dmax > 0.0) || !(d[e] > 1e-10 * dmax)) break;
-          // Q_col = sum_j V[j][e] / sqrt(d_e) T_j; seg_maxpy subtracts, so store the negation
-          for (int j = 0; j < 4; ++j) W[16 * k + 4 * col + j] = -V[j][e] / std::sqrt(d[e]);
-          ++keep;
-        }
-      keep_min = std::min(keep_min, keep);
-    }
-  c->sym_k = keep_min;
-  if (keep_min == 0) return GLGPU_OK;
-  CK(cudaMemcpyAsync(c->sym_w, W.data(), sizeof(double) * 16 * n, cudaMemcpyHostToDevice, c->st));
-  for (int col = 0; col < keep_min; ++col)
-    {
-      void *q = tptr(c, c->symQ, col * N);
-      CKS(axpby(c, nullptr, q, nullptr, coefs(0.0, 0.0), nullptr, m32, m32, m32));
-      CKS(launch(c, KK_VEC, 1, [&] {
-        return launch_seg_maxpy(c->dm, m32, c->symT, N, 4, c->sym_w + 4 * col, 16, q, nullptr, c->st);
-      }));
-    }
-  CKS(sync(c)); // W is a host array
-  return GLGPU_OK;
-}
-
-// z -= Q (Q^T z) for the active instances
-glgpu_status sym_project(glgpu_ctx *c, void *z, const uint8_t *act)
-{
-  const bool m32 = c->mixed;
-  const int k = c->sym_k;
-  const int64_t N = c->N;
-  CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_mdot(c->dm, m32, c->symQ, N, k, z, c->partial, act, c->st); }));
-  CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_finalize(c->dm, c->partial, k, c->sym_coef, 4, 0, c->st); }));
-  CKS(launch(c, KK_VEC, 1, [&] { return launch_seg_maxpy(c->dm, m32, c->symQ, N, k, c->sym_coef, 4, z, act, c->st); }));
-  return GLGPU_OK;
-}
-} // namespace
-
-// ---------------------------------------------------------------------------------
 // GMRES(m), right preconditioned, classical Gram-Schmidt with one reorthogonalization
 // ---------------------------------------------------------------------------------
 constexpr double kMgStall = 0.5; // least reduction of the true residual per multigrid cycle
@@ -741,16 +611,6 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
   // hands the rest of the solve to block-Jacobi GMRES
   bool use_mg = c->n_levels > 0;
   std::vector<double> prev_res(c->rhs_norm);
-  // symmetry deflation of the flexible basis: projection always, augmentation with the
-  // generators unless the last Newton step was short enough for the projection's residual
-  // floor (about 2 |delta| / |x|) to stay below the tolerance
-  const bool sym_on = use_mg && c->symT != nullptr;
-  bool sym_aug = false;
-  if (sym_on)
-    {
-      CKS(sym_setup(c));
-      sym_aug = c->sym_k > 0 && !(2.0 * c->last_step_rel < tol);
-    }
   for (int cycle = 0;; ++cycle)
     {
       // V0 = b - J X
@@ -800,16 +660,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
               }));
             }
           else if (mg)
-            {
-              if (sym_on && sym_aug && cycle == 0 && j < c->sym_k)
-                CK(cudaMemcpyAsync(Zj, tptr(c, c->symQ, static_cast<int64_t>(j) * N), tsz(c) * static_cast<size_t>(N),
-                                   cudaMemcpyDeviceToDevice, c->st));
-              else
-                {
-                  CKS(vcycle_run(c, Vj, Zj));
-                  if (sym_on && c->sym_k > 0) CKS(sym_project(c, Zj, c->g.active));
-                }
-            }
+            CKS(vcycle_run(c, Vj, Zj));
           else
             CKS(precond(c, Vj, c->Z, c->g.active));
           CKS(spmv(c, Zj, Vj1, c->g.active));
@@ -1185,17 +1036,6 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     CK(cudaMemset(zb, 0, tsz(c) * static_cast<size_t>(c->restart) * c->N));
     c->Zb = zb;
   }
-  if (prm[0].sym_deflate && c->B == 18 && c->P.dim == 3 && c->restart >= 2)
-    {
-      char *t = nullptr, *q = nullptr;
-      CKS(dalloc(c, &t, tsz(c) * 4 * static_cast<size_t>(c->N)));
-      CKS(dalloc(c, &q, tsz(c) * 4 * static_cast<size_t>(c->N)));
-      c->symT = t;
-      c->symQ = q;
-      CKS(dalloc(c, &c->sym_gram, static_cast<size_t>(n_inst) * 16));
-      CKS(dalloc(c, &c->sym_w, static_cast<size_t>(n_inst) * 16));
-      CKS(dalloc(c, &c->sym_coef, static_cast<size_t>(n_inst) * 4));
-    }
   c->n_levels = nl;
   return GLGPU_OK;
 }
@@ -1226,7 +1066,6 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->prec_reuse = 0.0;
   p->bt = 1e10;
   p->mg_coarse_shift = 1e-4;
-  p->sym_deflate = 0;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1725,7 +1564,7 @@ static glgpu_status newton_impl(glgpu_ctx *c, std::vector<double> &res, std::vec
   // R, r_cell, e_cell now hold the values at the new x of every instance of the step
   for (int k = 0; k < n; ++k)
     if (c->inst_on[k]) c->r_ok[k] = 1;
-  if (c->prm[0].prec_reuse > 0 || c->prm[0].sym_deflate)
+  if (c->prm[0].prec_reuse > 0)
     {
       std::vector<double> nd, nx;
       CKS(norms_d(c, c->delta, c->d_act, nd));

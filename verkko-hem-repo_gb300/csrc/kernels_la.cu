@@ -1434,48 +1434,4 @@ cudaError_t launch_bj_apply_scale(const DevMesh &m, bool fp32, const void *dinv,
                                                                 scale, act);
   return cudaGetLastError();
 }
-// ---------------------------------------------------------------------------------
-// Exact symmetries of the functional at the state x: the generators of the global phase
-// (A -> i A) and of the three spin rotations (A -> L_a A, (L_a)_{mu nu} = -eps_{a mu nu},
-// acting on the spin index mu of A_{mu j}), as four vectors in the Krylov precision,
-// zero on constrained rows (hanging nodes, periodic images) and zero-Dirichlet components
-// (where the generators vanish anyway: the masks act on whole orbital columns).  The
-// free energy is invariant along them, so R(x) is orthogonal to all four and, at a
-// solution, the Jacobian annihilates them.
-// ---------------------------------------------------------------------------------
-template <typename T>
-__global__ void k_sym_gen(DevMesh m, const double *__restrict__ x, T *__restrict__ t, int64_t ld)
-{
-  pdl_wait();
-  pdl_trigger();
-  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= m.nn * 18) return;
-  const int64_t n = idx / 18;
-  const int c = static_cast<int>(idx - n * 18);
-  const bool off = (m.hptr[n + 1] > m.hptr[n]) || ((m.mask[n] >> c) & 1u);
-  const double *a = x + n * 18;
-  const int part = c / 9, mu = (c % 9) / 3, j = c % 3;
-  double g0 = part == 0 ? -a[9 + c] : a[c - 9]; // i A: u -> -v, v -> u
-  const double *ap = a + 9 * part;               // this part's 3x3 (rows mu, columns j)
-  double g1 = mu == 1 ? -ap[6 + j] : (mu == 2 ? ap[3 + j] : 0.0); // L_0 A
-  double g2 = mu == 0 ? ap[6 + j] : (mu == 2 ? -ap[j] : 0.0);     // L_1 A
-  double g3 = mu == 0 ? -ap[3 + j] : (mu == 1 ? ap[j] : 0.0);     // L_2 A
-  if (off) g0 = g1 = g2 = g3 = 0.0;
-  t[idx] = static_cast<T>(g0);
-  t[ld + idx] = static_cast<T>(g1);
-  t[2 * ld + idx] = static_cast<T>(g2);
-  t[3 * ld + idx] = static_cast<T>(g3);
-}
-
-cudaError_t launch_sym_gen(const DevMesh &m, bool fp32, const double *x, void *t, int64_t ld, cudaStream_t s)
-{
-  const int64_t n = m.nn * 18;
-  const unsigned g = static_cast<unsigned>((n + 255) / 256);
-  if (fp32)
-    pdl_launch(k_sym_gen<float>, g, 256, 0, s, m, x, static_cast<float *>(t), ld);
-  else
-    pdl_launch(k_sym_gen<double>, g, 256, 0, s, m, x, static_cast<double *>(t), ld);
-  return cudaGetLastError();
-}
-
 } // namespace glgpu

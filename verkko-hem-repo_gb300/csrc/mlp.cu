@@ -34,7 +34,7 @@ namespace glgpu
 namespace mlp
 {
 constexpr int kIn = 6, kInPad = 16, kHid = 256, kOut = 18, kOutPad = 32, kLayers = 5;
-constexpr int kTileM = 128, kKChunk = 64, kGemmThreads = 128;
+constexpr int kTileM = 128, kKChunk = 64, kGemmThreads = 256;
 constexpr int kSplitMax = 64;
 constexpr uint32_t kWaitLimit = 1u << 26;
 
@@ -225,15 +225,18 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
     }
   if (!ok && lane == 0) atomicExch(g.err, 1);
   asm volatile("tcgen05.fence::after_thread_sync;");
-  // epilogue: warp w owns accumulator rows 32w..32w+31 (TMEM lanes), 16 columns per load;
-  // a thread's 16 consecutive outputs of its row are written as 16-byte vectors
-  const int row = warp * 32 + lane;
+  // epilogue: warps w and w + 4 own accumulator rows 32 (w % 4) .. + 31 (the TMEM lane
+  // quarter a warp may read) and one half of the columns each, 16 columns per load; a
+  // thread's 16 consecutive outputs of its row are written as 16-byte vectors
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = quarter * 32 + lane;
   const int m = m0 + row;
+  constexpr int kHalfCols = NT / 2 < 16 ? 16 : NT / 2;
   if (ok && committed > 0)
-    for (int c0 = 0; c0 < NT; c0 += 16)
+    for (int c0 = half * kHalfCols; c0 < NT && c0 < (half + 1) * kHalfCols; c0 += 16)
       {
         uint32_t r[16];
-        const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + c0;
+        const uint32_t taddr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + c0;
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
                      "[%16];"
                      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
@@ -254,9 +257,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
                 z[j] = __uint_as_float(r[j]) + g.bias[nb + j];
                 h[j] = __float2bfloat16(silu(z[j]));
               }
-            float4 *zo = reinterpret_cast<float4 *>(g.out_f32 + static_cast<int64_t>(m) * g.ldo + nb);
+            if (g.out_f32) // pre-activations only when a backward pass follows
+              {
+                float4 *zo = reinterpret_cast<float4 *>(g.out_f32 + static_cast<int64_t>(m) * g.ldo + nb);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) zo[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+                for (int q = 0; q < 4; ++q) zo[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+              }
             uint4 *ho = reinterpret_cast<uint4 *>(g.out_h + static_cast<int64_t>(m) * g.ldh + nb);
             ho[0] = *reinterpret_cast<const uint4 *>(&h[0]);
             ho[1] = *reinterpret_cast<const uint4 *>(&h[8]);
@@ -295,7 +301,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
             if (EPI == EPI_HIDDEN)
               {
                 const float z = acc + g.bias[n];
-                g.out_f32[static_cast<int64_t>(m) * g.ldo + n] = z;
+                if (g.out_f32) g.out_f32[static_cast<int64_t>(m) * g.ldo + n] = z;
                 const __nv_bfloat16 h = __float2bfloat16(silu(z));
                 g.out_h[static_cast<int64_t>(m) * g.ldh + n] = h;
                 if (g.out_t) g.out_t[static_cast<int64_t>(n) * g.ldt + m] = h;
@@ -312,7 +318,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tc(GemmArgs g)
               g.out_f32[(static_cast<int64_t>(split) * g.M + m) * g.ldo + n] = acc;
           }
       }
-  else if (EPI == EPI_PARTIAL && m < g.M)
+  else if (EPI == EPI_PARTIAL && m < g.M && half == 0)
     for (int n = n0; n < min(g.N, n0 + NT); ++n) g.out_f32[(static_cast<int64_t>(split) * g.M + m) * g.ldo + n] = 0.f;
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -582,7 +588,7 @@ glgpu_status forward(glgpu_surrogate *s, int P, bool want_transposes)
       g.K = kShape[l].in_pad;
       g.k_per_split = g.K;
       g.bias = s->b[l];
-      g.out_f32 = s->Z[l];
+      g.out_f32 = want_transposes ? s->Z[l] : nullptr; // the backward pass reads them
       g.ldo = kHid;
       g.out_h = s->H[l];
       g.ldh = kHid;

@@ -59,7 +59,7 @@ class _Params(ctypes.Structure):
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
                 ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
                 ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double),
-                ("bt", ctypes.c_double), ("mg_coarse_shift", ctypes.c_double), ("sym_deflate", ctypes.c_int)]
+                ("bt", ctypes.c_double), ("mg_coarse_shift", ctypes.c_double)]
 
 
 _lib = None
@@ -429,8 +429,6 @@ class Params:
     bt: float = 1e10
     #: multigrid: relative diagonal shift of the coarsest level's dense solve
     mg_coarse_shift: float = 1e-4
-    #: multigrid, 3D: keep the flexible GMRES basis free of the exact symmetry directions
-    sym_deflate: bool = False
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -451,7 +449,6 @@ class Params:
         s.prec_reuse = float(self.prec_reuse)
         s.bt = float(self.bt)
         s.mg_coarse_shift = float(self.mg_coarse_shift)
-        s.sym_deflate = int(bool(self.sym_deflate))
         return s
 
 
