@@ -415,8 +415,9 @@ def make_parser():
                     help="preconditioner of every GPU leg: geometric multigrid (default) or block-Jacobi")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (the headline then uses the default configuration)")
-    ap.add_argument("--headline-start", default="bphase", choices=["bphase", "learned"],
-                    help="start of the headline solves (the other start is reported beside it)")
+    ap.add_argument("--headline-start", default="auto", choices=["auto", "bphase", "learned"],
+                    help="start of the headline solves: the learned guess where it solves faster than the B phase "
+                         "(auto), or either one (the other start is reported beside it)")
     return ap
 
 
@@ -493,7 +494,7 @@ def main():
         t0 = time.perf_counter()
         Xtr, Ytr, ginfo = L.generate(gl, 32, seed=11, n_lo=10, n_hi=14, per_instance=2048, precond=pc)
         t_gen = time.perf_counter() - t0
-        sur, tinfo = L.train(gl, Xtr, Ytr, steps=1500, batch=4096, lr=1e-3, seed=0)
+        sur, tinfo = L.train(gl, Xtr, Ytr, steps=3000, batch=4096, lr=1e-3, seed=0)
         inst2 = L.Instance(T_RED, P_BAR, 2 * HALF, NCELL, m)
         learned_x0 = lambda: L.guess(gl, sur, [inst2])[0]  # noqa: E731
         learn_info = {"train_states": ginfo["converged"], "train_rows": tinfo["rows"], "train_steps": tinfo["steps"],
@@ -506,21 +507,34 @@ def main():
     # block-Jacobi beside multigrid (same start, same precision)
     bj = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
                    precond=gl.PC_BLOCK_JACOBI) if pc != gl.PC_BLOCK_JACOBI else None
-    # the headline uses the start that solves faster; the other start is reported beside it
-    alt_x0 = learned_x0 if sur is not None else None
-    alt = time_mode(gl, m, alt_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol,
-                    flush=flush, precond=pc) if alt_x0 is not None else None
-    use_learned = alt is not None and args.headline_start == "learned"
-    head_x0 = learned_x0 if use_learned else x0
-    # the autotuner picks preconditioner, restart, multigrid sweeps and the matrix-free
-    # operator's cell batch for this workload (complete solves timed before the timed region)
-    tuned = None
+    # the autotuner picks preconditioner, restart, multigrid sweeps, the matrix-free
+    # operator's cell batch and the preconditioner-reuse threshold for this workload, once
+    # per start (complete solves timed before the timed region)
+    AT = importlib.import_module("verkko-hem-repo_gb300.autotune")
+    base_prm = [gl.Params.from_matep(P_BAR, T_RED, precision=gl.MIXED)]
+    tuned = tuned_l = None
     if args.autotune:
-        AT = importlib.import_module("verkko-hem-repo_gb300.autotune")
         t0 = time.perf_counter()
-        tuned = AT.tune(gl, [m], [gl.Params.from_matep(P_BAR, T_RED, precision=gl.MIXED)], x0, args.linear_tol, TOL)
+        tuned = AT.tune(gl, [m], base_prm, x0, args.linear_tol, TOL)
         tuned["tuning_s"] = time.perf_counter() - t0
-    head_cfg = tuned["config"] if tuned else None
+        if sur is not None:
+            t0 = time.perf_counter()
+            tuned_l = AT.tune(gl, [m], base_prm, learned_x0(), args.linear_tol, TOL)
+            tuned_l["tuning_s"] = time.perf_counter() - t0
+    cfg_b = tuned["config"] if tuned else None
+    cfg_l = tuned_l["config"] if tuned_l else cfg_b
+    # the learned start, network inference inside every timed solve, with its own tuning
+    alt = time_mode(gl, m, learned_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                    precond=pc, cfg=cfg_l) if sur is not None else None
+    # the headline start: the learned guess when it solves faster (auto), or as asked
+    if args.headline_start == "auto" and alt is not None:
+        ref_b = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                          precond=pc, cfg=cfg_b)
+        use_learned = float(np.mean(alt["ms"])) < float(np.mean(ref_b["ms"]))
+    else:
+        use_learned = alt is not None and args.headline_start == "learned"
+    head_x0 = learned_x0 if use_learned else x0
+    head_cfg = cfg_l if use_learned else cfg_b
     with ClockSampler() as clk:
         mixed = time_mode(gl, m, head_x0, gl.MIXED, args.steps, args.warmup, args.linear_tol, kernel_timing=True,
                           flush=flush, precond=pc, cfg=head_cfg)
@@ -601,10 +615,13 @@ def main():
                         "note": "programmatic dependent launch (the default) against plain stream order"},
         "autotune": None if tuned is None else {
             "config": tuned["config"], "ms_best_trial": tuned["ms"], "tuning_s": tuned["tuning_s"],
-            "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]]},
+            "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]],
+            "learned_start": None if tuned_l is None else {"config": tuned_l["config"], "ms_best_trial": tuned_l["ms"],
+                                                           "tuning_s": tuned_l["tuning_s"]}},
         "mixed_learned_start": None if alt is None else {
             "solves_per_s": 1000.0 / float(np.mean(alt["ms"])), "newton_its": int(alt["out"]["newton_its"][0]),
-            "gmres_its": int(alt["out"]["gmres_its"][0]), "free_energy": alt["F"]},
+            "gmres_its": int(alt["out"]["gmres_its"][0]), "free_energy": alt["F"],
+            "final_residual": float(alt["out"]["residual"][0]), "solver_config": cfg_l},
         "start": "learned (surrogate) guess" if use_learned else "B phase + 0.05 N(0,1)",
         "learned": learn_info,
         "mixed_vs_fp64": (1000.0 / ms_step) / (1000.0 / float(np.mean(fp64["ms"]))),
