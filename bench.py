@@ -209,9 +209,9 @@ def batched_leg(gl, count, linear_tol, sur=None, precond=None, cfg=None):
 
 
 def time_mode(gl, m, x0, precision, steps, warmup, linear_tol, kernel_timing=False, flush=None, precond=None,
-              cfg=None):
+              cfg=None, **prm_kw):
     prm = gl.Params.from_matep(P_BAR, T_RED, precision=precision,
-                               precond=gl.PC_BLOCK_JACOBI if precond is None else precond)
+                               precond=gl.PC_BLOCK_JACOBI if precond is None else precond, **prm_kw)
     if cfg is not None:
         prm = importlib.import_module("verkko-hem-repo_gb300.autotune").params_with(gl, prm, cfg)
     f = gl.FemGL(m, prm)
@@ -545,6 +545,9 @@ def main():
                           precond=pc, cfg=head_cfg)
     finally:
         gl.set_launch_mode(True)
+    # the small coarse levels as separate launches instead of one cooperative launch
+    unfused = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                        precond=pc, cfg=head_cfg, mg_small_fuse=False)
     e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
     batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc, cfg=head_cfg) if args.batch > 0 else None
 
@@ -613,6 +616,9 @@ def main():
         "mg_fallbacks": mixed["mg"]["fallbacks"],
         "launch_mode": {"programmatic_ms_per_solve": ms_step, "plain_ms_per_solve": float(np.mean(plain["ms"])),
                         "note": "programmatic dependent launch (the default) against plain stream order"},
+        "small_level_fusion": {"fused_ms_per_solve": ms_step, "separate_ms_per_solve": float(np.mean(unfused["ms"])),
+                               "note": "coarse levels below 20,000 nodes as one cooperative launch per V-cycle "
+                                       "(the default) against one launch per sweep, residual and transfer"},
         "autotune": None if tuned is None else {
             "config": tuned["config"], "ms_best_trial": tuned["ms"], "tuning_s": tuned["tuning_s"],
             "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]],

@@ -267,6 +267,35 @@ cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, con
                             const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
                             const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
                             const uint8_t *act, cudaStream_t s, bool half_in = false, bool half_out = false);
+// The small coarse levels of a V-cycle fused into one cooperative launch (levels whose
+// block values are FP32/FP64, 18x18 blocks): the recursion below the first such level
+// (pre-sweeps beyond the one that came with the restriction, residual, restriction fused
+// with the next level's first sweep, the coarsest dense solve, prolongation, post-sweeps)
+// runs phase by phase over all levels and instances, separated by grid-wide barriers.
+template <typename T> struct SmallLevel
+{
+  DevMesh m;                // the level's plan (rowptr, cols, mask, hptr, node_inst, nn)
+  const T *vals, *dinv;     // block values and the l1 block-Jacobi inverse blocks
+  T *r, *z, *t, *t2;        // right-hand side, iterate, residual, ping-pong buffer
+  const int32_t *r_ptr, *r_idx, *p_ptr, *p_idx; // restriction to / prolongation from the next level
+  const T *r_w, *p_w;
+};
+template <typename T> struct SmallCycle
+{
+  int n_small;              // smoothing levels in the fused range; levels[n_small] is the coarsest
+  int pre, post;            // sweeps before / after the coarse correction
+  T omega;
+  int max_nd;               // coarsest dense solve
+  const int64_t *dense_off;
+  const float *inv;
+  unsigned int *bar;        // [2]: arrival count, generation (zero at allocation)
+  int *err;                 // set when a grid barrier gave up waiting
+};
+// levels: device array of SmallLevel<T> [n_small + 1]; grid: cooperative, all CTAs resident
+cudaError_t launch_vcycle_small(bool fp32, const void *levels, const void *cycle, int grid, const uint8_t *act,
+                                cudaStream_t s);
+// CTAs per SM the fused small-level V-cycle is launched with (the occupancy limit, at most 4)
+int vcycle_small_blocks_per_sm(bool fp32);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, float shift, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

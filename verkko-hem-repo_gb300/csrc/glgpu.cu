@@ -146,6 +146,13 @@ struct glgpu_ctx
   int *d_sing = nullptr;
   int max_nd = 0;
   void *Zb = nullptr;                // flexible GMRES: preconditioned basis [m][N]
+  // the small coarse levels fused into one cooperative launch per V-cycle (level index
+  // small_ls .. n_levels; 0: not fused): device descriptors, cycle constants, barrier state
+  int small_ls = 0, small_grid = 0;
+  void *small_levels = nullptr;
+  std::vector<unsigned char> small_cycle; // SmallCycle<T>, passed by value at launch
+  unsigned int *small_bar = nullptr;
+  int *small_err = nullptr;
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   // per instance, the last glgpu_run step's |R|: the line search's value and the FP64 value
@@ -862,6 +869,12 @@ glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
 glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *act, bool pre_done)
 {
   const bool m = c->mixed;
+  if (l > 0 && l == c->small_ls && pre_done)
+    // this level and every coarser one in one cooperative launch (r, z are this level's
+    // Bv and X, which the descriptors hold)
+    return launch(c, KK_PREC, 1, [&] {
+      return launch_vcycle_small(m, c->small_levels, c->small_cycle.data(), c->small_grid, act, c->st);
+    });
   if (l == c->n_levels)
     {
       glgpu_ctx *L = c->lv[l - 1];
@@ -926,6 +939,98 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
     }
   if (cur != z) CKS(axpby(L, cur, z, nullptr, coefs(1.0, 0.0), act, m, m, m));
   return GLGPU_OK;
+}
+
+// Small coarse levels below which one cooperative launch runs the rest of the V-cycle:
+// levels of at most kSmallNodes nodes (all instances together), FP32/FP64 blocks, down
+// to the dense coarsest level.
+constexpr int64_t kSmallNodes = 20000;
+
+template <typename T> glgpu_status small_setup_t(glgpu_ctx *c, int ls)
+{
+  const int nl = c->n_levels;
+  std::vector<SmallLevel<T>> lev(static_cast<size_t>(nl - ls + 1));
+  for (int l = ls; l <= nl; ++l)
+    {
+      glgpu_ctx *L = c->lv[l - 1];
+      SmallLevel<T> &d = lev[static_cast<size_t>(l - ls)];
+      d.m = L->dm;
+      d.vals = static_cast<const T *>(L->vals);
+      d.dinv = static_cast<const T *>(L->dinv);
+      d.r = static_cast<T *>(L->Bv);
+      d.z = static_cast<T *>(L->X);
+      d.t = static_cast<T *>(L->Tmp);
+      d.t2 = static_cast<T *>(L->C1);
+      if (l < nl)
+        {
+          const glgpu_ctx::Transfer &t = c->tr[l];
+          d.r_ptr = t.r_ptr;
+          d.r_idx = t.r_idx;
+          d.r_w = static_cast<const T *>(t.r_w);
+          d.p_ptr = t.p_ptr;
+          d.p_idx = t.p_idx;
+          d.p_w = static_cast<const T *>(t.p_w);
+        }
+    }
+  std::vector<unsigned char> bytes(sizeof(SmallLevel<T>) * lev.size());
+  std::memcpy(bytes.data(), lev.data(), bytes.size());
+  unsigned char *dl = nullptr;
+  CKS(dupload(c, &dl, bytes));
+  c->small_levels = dl;
+  CKS(dalloc(c, &c->small_bar, 2));
+  CKS(dalloc(c, &c->small_err, 1));
+  CK(cudaMemset(c->small_bar, 0, 2 * sizeof(unsigned int)));
+  CK(cudaMemset(c->small_err, 0, sizeof(int)));
+  SmallCycle<T> cy{};
+  cy.n_small = nl - ls;
+  cy.pre = std::max(1, c->prm[0].mg_pre);
+  cy.post = std::max(0, c->prm[0].mg_post);
+  cy.omega = static_cast<T>(c->prm[0].mg_omega);
+  cy.max_nd = c->max_nd;
+  cy.dense_off = c->d_dense_off;
+  cy.inv = c->d_inv;
+  cy.bar = c->small_bar;
+  cy.err = c->small_err;
+  c->small_cycle.resize(sizeof(cy));
+  std::memcpy(c->small_cycle.data(), &cy, sizeof(cy));
+  c->small_ls = ls;
+  return GLGPU_OK;
+}
+
+glgpu_status small_setup(glgpu_ctx *c)
+{
+  const int nl = c->n_levels;
+  if (nl < 2 || c->B != 18 || !c->prm[0].mg_small_fuse) return GLGPU_OK;
+  int ls = nl;
+  while (ls - 1 >= 1)
+    {
+      const glgpu_ctx *L = c->lv[ls - 2]; // level ls - 1
+      if (L->nn > kSmallNodes || L->dm.half_vals || L->B != 18) break;
+      --ls;
+    }
+  if (ls >= nl) return GLGPU_OK; // no smoothing level small enough
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int per_sm = vcycle_small_blocks_per_sm(c->mixed);
+  if (per_sm < 1 || sms < 1) return GLGPU_OK;
+  c->small_grid = sms * per_sm;
+  return c->mixed ? small_setup_t<float>(c, ls) : small_setup_t<double>(c, ls);
+}
+
+// a grid barrier of the fused small-level V-cycle gave up waiting: clear its state and
+// report the timeout
+glgpu_status small_check(glgpu_ctx *c)
+{
+  if (!c->small_ls) return GLGPU_OK;
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, c->small_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CKS(sync(c));
+  if (!err) return GLGPU_OK;
+  CK(cudaMemsetAsync(c->small_bar, 0, 2 * sizeof(unsigned int), c->st));
+  CK(cudaMemsetAsync(c->small_err, 0, sizeof(int), c->st));
+  CKS(sync(c));
+  return set_error(GLGPU_ERR_TIMEOUT, "multigrid: a grid barrier of the fused coarse-level cycle timed out");
 }
 
 glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst)
@@ -1037,6 +1142,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     c->Zb = zb;
   }
   c->n_levels = nl;
+  CKS(small_setup(c));
   return GLGPU_OK;
 }
 
@@ -1066,6 +1172,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->prec_reuse = 0.0;
   p->bt = 1e10;
   p->mg_coarse_shift = 1e-4;
+  p->mg_small_fuse = 1;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }
@@ -1499,6 +1606,7 @@ static glgpu_status solve_impl(glgpu_ctx *c, double tol, std::vector<int> &its, 
   if (!all_on) CKS(upload_act(c, c->d_act, c->inst_on));
   CKS(prec_setup(c, all_on ? nullptr : c->d_act));
   CKS(gmres(c, tol, c->inst_on, its, conv));
+  CKS(small_check(c));
   c->has_delta = true;
   return GLGPU_OK;
 }

@@ -1434,4 +1434,264 @@ cudaError_t launch_bj_apply_scale(const DevMesh &m, bool fp32, const void *dinv,
                                                                 scale, act);
   return cudaGetLastError();
 }
+// ---------------------------------------------------------------------------------
+// The small coarse levels of a V-cycle in one cooperative launch.  Below a few thousand
+// nodes a level's sweep, residual, restriction or prolongation is a short launch whose time
+// is mostly launch latency and ramp; here all CTAs stay resident and walk the levels phase
+// by phase, with a grid-wide barrier between phases.  The phases compute exactly what the
+// separate kernels compute (the same row map: the 8 warps of a CTA share a block row).
+// ---------------------------------------------------------------------------------
+constexpr int kSmallThreads = 256;
+constexpr unsigned kBarrierSpins = 20u * 1000u * 1000u; // with 64 ns naps: about a second
+
+// Grid-wide barrier (every CTA of the launch is resident: cooperative launch).  The last
+// CTA to arrive resets the count and advances the generation; the others wait for the
+// generation to move, at most kBarrierSpins polls, after which they record the failure in
+// *err and go on (the results are then invalid and the host reports a timeout).
+__device__ __forceinline__ void grid_barrier(unsigned int *bar, int *err)
+{
+  __syncthreads();
+  if (threadIdx.x == 0)
+    {
+      volatile unsigned int *gen = bar + 1;
+      const unsigned int g = *gen;
+      __threadfence();
+      if (atomicAdd(bar, 1u) == gridDim.x - 1)
+        {
+          atomicExch(bar, 0u);
+          __threadfence();
+          atomicAdd(bar + 1, 1u);
+        }
+      else
+        {
+          unsigned int spins = 0;
+          while (*gen == g)
+            {
+              if (++spins > kBarrierSpins)
+                {
+                  atomicExch(err, 1);
+                  break;
+                }
+              __nanosleep(64);
+            }
+        }
+      __threadfence();
+    }
+  __syncthreads();
+}
+
+// y = zin + omega D^-1 (r - A zin) (zin == nullptr: y = omega D^-1 r), or, with RES, the
+// residual y = r - A zin; one block row per CTA iteration, its blocks split over 8 warps
+template <typename T, bool RES>
+__device__ void small_rows(const SmallLevel<T> &L, const T *zin, T *y, T omega, const uint8_t *act,
+                           T (*red)[324])
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t n = blockIdx.x; n < L.m.nn; n += gridDim.x)
+    {
+      const bool on = !(act && !act[L.m.node_inst[n]]); // uniform over the CTA
+      if (!on) continue;
+      T t = (lane < 18) ? L.r[n * 18 + lane] : T(0);
+      if (zin)
+        {
+          T acc[NIT][NV];
+          row_products<T, T, kSpmvWarps>(L.m, L.vals, zin, n, lane, warp, acc);
+          store_products<T, T>(red[warp], acc, lane);
+          __syncthreads();
+          if (warp == 0 && lane < 18) t -= row_sum<T, kSpmvWarps>(red, 0, lane);
+          __syncthreads();
+        }
+      if (RES)
+        {
+          if (warp == 0 && lane < 18) y[n * 18 + lane] = t;
+          continue;
+        }
+      if (warp == 0)
+        {
+          T acc[NIT][NV];
+          const V *bp = reinterpret_cast<const V *>(L.dinv + n * 324);
+#pragma unroll
+          for (int it = 0; it < NIT; ++it)
+            {
+              const int ch = lane + 32 * it;
+              const V w = (ch < NCH) ? __ldg(bp + ch) : V{};
+#pragma unroll
+              for (int v = 0; v < NV; ++v)
+                {
+                  const int e = (ch < NCH) ? ch * NV + v : 0;
+                  acc[it][v] = vget<V, T>(w, v) * __shfl_sync(0xffffffffu, t, e % 18);
+                }
+            }
+          store_products<T>(red[0], acc, lane);
+          __syncwarp();
+          if (lane < 18) y[n * 18 + lane] = (zin ? zin[n * 18 + lane] : T(0)) + omega * row_sum<T, 1>(red, 0, lane);
+        }
+      __syncthreads(); // red is reused by the next row
+    }
+}
+
+// rc = P^T rf on the coarse level C (zero on its zero-Dirichlet components); with `smooth`
+// also C.z = omega D_c^-1 rc, the coarse level's first sweep from zero.  Warp per coarse node.
+template <typename T>
+__device__ void small_restrict(const SmallLevel<T> &F, const SmallLevel<T> &C, bool smooth, T omega,
+                               const uint8_t *act)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t n = gw; n < C.m.nn; n += nw)
+    {
+      if (act && !act[C.m.node_inst[n]]) continue;
+      T s = T(0);
+      if (lane < 18 && !((C.m.mask[n] >> lane) & 1u))
+        for (int k = F.r_ptr[n]; k < F.r_ptr[n + 1]; ++k) s += F.r_w[k] * F.t[static_cast<int64_t>(F.r_idx[k]) * 18 + lane];
+      if (lane < 18) C.r[n * 18 + lane] = s;
+      if (smooth)
+        {
+          const T *row = C.dinv + n * 324 + (lane < 18 ? lane : 0) * 18;
+          T u = T(0);
+#pragma unroll
+          for (int d = 0; d < 18; ++d) u += row[d] * __shfl_sync(0xffffffffu, s, d);
+          if (lane < 18) C.z[n * 18 + lane] = omega * u;
+        }
+    }
+}
+
+// out = base + P zc on level F (constrained components keep base); thread per (node, component)
+template <typename T>
+__device__ void small_prolong(const SmallLevel<T> &F, const T *zc, const T *base, T *out, const uint8_t *act)
+{
+  const int64_t total = F.m.nn * 18;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+      const int64_t n = i / 18;
+      const int c = static_cast<int>(i - n * 18);
+      if (act && !act[F.m.node_inst[n]]) continue;
+      const T b0 = base[i];
+      if (F.m.hptr[n + 1] > F.m.hptr[n] || ((F.m.mask[n] >> c) & 1u))
+        {
+          out[i] = b0;
+          continue;
+        }
+      T s = T(0);
+      for (int k = F.p_ptr[n]; k < F.p_ptr[n + 1]; ++k) s += F.p_w[k] * zc[static_cast<int64_t>(F.p_idx[k]) * 18 + c];
+      out[i] = b0 + s;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads) k_vcycle_small(const SmallLevel<T> *__restrict__ lev, SmallCycle<T> cy,
+                                                                const uint8_t *__restrict__ act)
+{
+  pdl_wait();
+  __shared__ T red[kSpmvWarps][324];
+  constexpr int kMaxSmall = 16;
+  T *curs[kMaxSmall];
+  // descent: every level entered with r and its first sweep from the restriction
+  for (int i = 0; i < cy.n_small; ++i)
+    {
+      const SmallLevel<T> &L = lev[i];
+      T *cur = L.z, *oth = L.t2;
+      for (int sw = 1; sw < cy.pre; ++sw)
+        {
+          small_rows<T, false>(L, cur, oth, cy.omega, act, red);
+          grid_barrier(cy.bar, cy.err);
+          T *tmp = cur;
+          cur = oth;
+          oth = tmp;
+        }
+      small_rows<T, true>(L, cur, L.t, cy.omega, act, red);
+      grid_barrier(cy.bar, cy.err);
+      small_restrict<T>(L, lev[i + 1], i + 1 < cy.n_small, cy.omega, act);
+      grid_barrier(cy.bar, cy.err);
+      curs[i] = cur;
+    }
+  // coarsest level: z = inverse r per instance, warp per row
+  {
+    const SmallLevel<T> &D = lev[cy.n_small];
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t units = static_cast<int64_t>(D.m.n_inst) * cy.max_nd;
+    for (int64_t u = gw; u < units; u += nw)
+      {
+        const int inst = static_cast<int>(u / cy.max_nd), row = static_cast<int>(u - inst * static_cast<int64_t>(cy.max_nd));
+        if (act && !act[inst]) continue;
+        const int64_t n0 = D.m.node_off_ptr[inst], n1 = D.m.node_off_ptr[inst + 1];
+        const int nd = static_cast<int>((n1 - n0) * 18);
+        if (row >= nd) continue;
+        const float *A = cy.inv + cy.dense_off[inst] + static_cast<int64_t>(row) * nd;
+        const T *rv = D.r + n0 * 18;
+        float s = 0.f;
+        for (int j = lane; j < nd; j += 32) s += A[j] * static_cast<float>(rv[j]);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) D.z[n0 * 18 + row] = static_cast<T>(s);
+      }
+    grid_barrier(cy.bar, cy.err);
+  }
+  // ascent: prolongation into the other buffer, post-sweeps, result in z
+  for (int i = cy.n_small - 1; i >= 0; --i)
+    {
+      const SmallLevel<T> &L = lev[i];
+      T *cur = curs[i];
+      T *oth = (cur == L.z) ? L.t2 : L.z;
+      small_prolong<T>(L, lev[i + 1].z, cur, oth, act);
+      grid_barrier(cy.bar, cy.err);
+      T *tmp = cur;
+      cur = oth;
+      oth = tmp;
+      for (int sw = 0; sw < cy.post; ++sw)
+        {
+          small_rows<T, false>(L, cur, oth, cy.omega, act, red);
+          grid_barrier(cy.bar, cy.err);
+          tmp = cur;
+          cur = oth;
+          oth = tmp;
+        }
+      if (cur != L.z)
+        {
+          const int64_t total = L.m.nn * 18;
+          for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total;
+               k += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            if (!(act && !act[L.m.node_inst[k / 18]])) L.z[k] = cur[k];
+          grid_barrier(cy.bar, cy.err);
+        }
+    }
+}
+
+int vcycle_small_blocks_per_sm(bool fp32)
+{
+  int nb = 0;
+  const cudaError_t e =
+    fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_vcycle_small<float>, kSmallThreads, 0)
+         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_vcycle_small<double>, kSmallThreads, 0);
+  if (e != cudaSuccess) return 0;
+  return nb < 4 ? nb : 4;
+}
+
+cudaError_t launch_vcycle_small(bool fp32, const void *levels, const void *cycle, int grid, const uint8_t *act,
+                                cudaStream_t s)
+{
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(grid));
+  cfg.blockDim = dim3(kSmallThreads);
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (fp32)
+    return cudaLaunchKernelEx(&cfg, k_vcycle_small<float>, static_cast<const SmallLevel<float> *>(levels),
+                              *static_cast<const SmallCycle<float> *>(cycle), act);
+  return cudaLaunchKernelEx(&cfg, k_vcycle_small<double>, static_cast<const SmallLevel<double> *>(levels),
+                            *static_cast<const SmallCycle<double> *>(cycle), act);
+}
+
 } // namespace glgpu

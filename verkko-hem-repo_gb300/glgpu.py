@@ -59,7 +59,7 @@ class _Params(ctypes.Structure):
                 ("gmres_max_iter", ctypes.c_int), ("ls_step", ctypes.c_double), ("ls_max_trials", ctypes.c_int),
                 ("damped", ctypes.c_int), ("mg_pre", ctypes.c_int), ("mg_post", ctypes.c_int),
                 ("mg_omega", ctypes.c_double), ("mf_cells", ctypes.c_int), ("prec_reuse", ctypes.c_double),
-                ("bt", ctypes.c_double), ("mg_coarse_shift", ctypes.c_double)]
+                ("bt", ctypes.c_double), ("mg_coarse_shift", ctypes.c_double), ("mg_small_fuse", ctypes.c_int)]
 
 
 _lib = None
@@ -429,6 +429,8 @@ class Params:
     bt: float = 1e10
     #: multigrid: relative diagonal shift of the coarsest level's dense solve
     mg_coarse_shift: float = 1e-4
+    #: multigrid: the small coarse levels as one cooperative launch per V-cycle
+    mg_small_fuse: bool = True
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -449,6 +451,7 @@ class Params:
         s.prec_reuse = float(self.prec_reuse)
         s.bt = float(self.bt)
         s.mg_coarse_shift = float(self.mg_coarse_shift)
+        s.mg_small_fuse = int(bool(self.mg_small_fuse))
         return s
 
 
