@@ -1008,6 +1008,7 @@ glgpu_status small_setup(glgpu_ctx *c)
       if (L->nn > kSmallNodes || L->dm.half_vals || L->B != 18) break;
       --ls;
     }
+  ls = std::max(ls, nl - 16);    // the kernel keeps one iterate pointer per level, at most 16
   if (ls >= nl) return GLGPU_OK; // no smoothing level small enough
   int dev = 0, sms = 0;
   CK(cudaGetDevice(&dev));
