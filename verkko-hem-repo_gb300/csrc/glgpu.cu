@@ -1173,7 +1173,7 @@ extern "C" void glgpu_default_params(glgpu_params *p)
   p->prec_reuse = 0.0;
   p->bt = 1e10;
   p->mg_coarse_shift = 1e-4;
-  p->mg_small_fuse = 1;
+  p->mg_small_fuse = 0;
 }
 
 extern "C" const char *glgpu_version(void) { return "glgpu 0.1 (sm_103a)"; }

@@ -430,7 +430,7 @@ class Params:
     #: multigrid: relative diagonal shift of the coarsest level's dense solve
     mg_coarse_shift: float = 1e-4
     #: multigrid: the small coarse levels as one cooperative launch per V-cycle
-    mg_small_fuse: bool = True
+    mg_small_fuse: bool = False
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
