@@ -528,9 +528,9 @@ def main():
     alt = time_mode(gl, m, learned_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
                     precond=pc, cfg=cfg_l) if sur is not None else None
     # the headline start: the learned guess when it solves faster (auto), or as asked
+    ref_b = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                      precond=pc, cfg=cfg_b)
     if args.headline_start == "auto" and alt is not None:
-        ref_b = time_mode(gl, m, x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
-                          precond=pc, cfg=cfg_b)
         use_learned = float(np.mean(alt["ms"])) < float(np.mean(ref_b["ms"]))
     else:
         use_learned = alt is not None and args.headline_start == "learned"
@@ -625,6 +625,10 @@ def main():
             "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]],
             "learned_start": None if tuned_l is None else {"config": tuned_l["config"], "ms_best_trial": tuned_l["ms"],
                                                            "tuning_s": tuned_l["tuning_s"]}},
+        "mixed_bphase_start": {"solves_per_s": 1000.0 / float(np.mean(ref_b["ms"])),
+                               "newton_its": int(ref_b["out"]["newton_its"][0]),
+                               "gmres_its": int(ref_b["out"]["gmres_its"][0]), "solver_config": cfg_b,
+                               "start": "B phase + 0.05 N(0,1), seed 2"},
         "mixed_learned_start": None if alt is None else {
             "solves_per_s": 1000.0 / float(np.mean(alt["ms"])), "newton_its": int(alt["out"]["newton_its"][0]),
             "gmres_its": int(alt["out"]["gmres_its"][0]), "free_energy": alt["F"],
