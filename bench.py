@@ -841,8 +841,15 @@ def config5_leg(gl, n_train, n_test, linear_tol, n_test_cells=48):
                      "newton_its_mean": float(np.mean(a["newton"])), "gmres_its_mean": float(np.mean(a["gmres"])),
                      "all_converged": bool(np.all(np.array(a["res"]) <= TOL)), "max_final_residual": float(max(a["res"]))}
     for name in ("bphase_noise", "bphase_uniform"):
+        rel = np.abs(F["learned"] - F[name]) / np.abs(F[name])
         out[f"learned_speedup_vs_{name}"] = out["learned"]["solves_per_s"] / out[name]["solves_per_s"]
-        out[f"max_free_energy_rel_diff_vs_{name}"] = float(np.max(np.abs(F["learned"] - F[name]) / np.abs(F[name])))
+        out[f"max_free_energy_rel_diff_vs_{name}"] = float(rel.max())
+        # instances whose two starts ended at different stationary points, and which start
+        # found the lower free energy there
+        diff = rel > 1e-9
+        out[f"instances_other_stationary_point_vs_{name}"] = int(diff.sum())
+        out[f"of_those_learned_lower_F_vs_{name}"] = int(np.sum(diff & (F["learned"] < F[name])))
+        out[f"median_free_energy_rel_diff_vs_{name}"] = float(np.median(rel))
     return out
 
 

@@ -613,6 +613,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
   CKS(axpby(c, nullptr, c->X, nullptr, coefs(0.0, 0.0), nullptr, m32, m32, m32));
   std::vector<int> total(n, 0);
   std::vector<uint8_t> solve_on(on);
+  std::vector<uint8_t> deferred(static_cast<size_t>(n), 0); // set aside for block-Jacobi
   all_conv = false;
   // multigrid runs flexible GMRES; a cycle whose true residual does not at least halve
   // hands the rest of the solve to block-Jacobi GMRES
@@ -764,7 +765,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
       if (use_mg)
         {
           std::vector<uint8_t> bad(n, 0);
-          bool any_bad = false, stall = false;
+          bool any_bad = false;
           for (int k = 0; k < n; ++k)
             {
               if (!solve_on[k] || c->h_norm[k] <= tol_abs[k]) continue;
@@ -774,7 +775,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
                   any_bad = true;
                 }
               else if (c->h_norm[k] > kMgStall * prev_res[k])
-                stall = true;
+                deferred[k] = 1;
             }
           if (any_bad)
             {
@@ -786,12 +787,11 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
             }
           for (int k = 0; k < n; ++k)
             if (solve_on[k]) prev_res[k] = c->h_norm[k];
-          if (any_bad || stall)
-            {
-              use_mg = false;
-              c->mg_fallbacks++;
-              CKS(bj_setup(c));
-            }
+          // an instance whose cycle diverged or stalled leaves the multigrid solve; it is
+          // finished with block-Jacobi GMRES once the other instances have converged, so one
+          // hard instance does not slow the rest of its batch
+          for (int k = 0; k < n; ++k)
+            if (bad[k]) deferred[k] = 1;
         }
       bool more = false;
       for (int k = 0; k < n; ++k)
@@ -800,9 +800,29 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
           total[k] += c->h_its[k];
           const bool conv = c->h_norm[k] <= tol_abs[k];
           if (conv || total[k] >= maxit || !std::isfinite(c->h_norm[k]))
-            solve_on[k] = 0;
+            {
+              solve_on[k] = 0;
+              deferred[k] = 0;
+            }
+          else if (deferred[k])
+            solve_on[k] = 0; // set aside for the block-Jacobi pass
           else
             more = true;
+        }
+      if (!more && use_mg)
+        {
+          bool any_def = false;
+          for (int k = 0; k < n; ++k) any_def |= deferred[k] != 0;
+          if (any_def)
+            {
+              // the set-aside instances continue from their current X with block-Jacobi GMRES
+              use_mg = false;
+              c->mg_fallbacks++;
+              CKS(bj_setup(c));
+              solve_on = deferred;
+              std::fill(deferred.begin(), deferred.end(), 0);
+              more = true;
+            }
         }
       if (!more)
         {

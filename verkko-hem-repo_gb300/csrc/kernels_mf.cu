@@ -367,6 +367,17 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
   const int tid = threadIdx.x;
   const int64_t e0 = static_cast<int64_t>(blockIdx.x) * kMCells;
   const int ncb = static_cast<int>((m.nc - e0) < kMCells ? (m.nc - e0) : kMCells);
+  if (act)
+    {
+      // a CTA whose cells all belong to inactive instances (converged, or waiting in a
+      // batched solve) has nothing to contribute: the gather skips their nodes
+      __shared__ int any_on;
+      if (tid == 0) any_on = 0;
+      __syncthreads();
+      if (tid < ncb && act[m.cell_inst[e0 + tid]]) any_on = 1;
+      __syncthreads();
+      if (!any_on) return;
+    }
   if (tid < kMCells)
     {
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -591,7 +602,6 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
             }
         }
     }
-  (void)act;
 }
 
 // Node gather: thread (node, component), 16 nodes per CTA.  s = sum of the row's cell
