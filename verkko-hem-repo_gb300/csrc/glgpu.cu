@@ -613,10 +613,12 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
   CKS(axpby(c, nullptr, c->X, nullptr, coefs(0.0, 0.0), nullptr, m32, m32, m32));
   std::vector<int> total(n, 0);
   std::vector<uint8_t> solve_on(on);
-  std::vector<uint8_t> deferred(static_cast<size_t>(n), 0); // set aside for block-Jacobi
+  std::vector<uint8_t> deferred(static_cast<size_t>(n), 0); // set aside (multigrid retry, then block-Jacobi)
+  bool mg_retried = false;
   all_conv = false;
-  // multigrid runs flexible GMRES; a cycle whose true residual does not at least halve
-  // hands the rest of the solve to block-Jacobi GMRES
+  // multigrid runs flexible GMRES; an instance whose restart cycle does not at least halve its
+  // true residual is set aside, retried with a fresh multigrid pass once the others are done,
+  // and finished with block-Jacobi GMRES if it stalls again
   bool use_mg = c->n_levels > 0;
   std::vector<double> prev_res(c->rhs_norm);
   for (int cycle = 0;; ++cycle)
@@ -813,7 +815,19 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
         {
           bool any_def = false;
           for (int k = 0; k < n; ++k) any_def |= deferred[k] != 0;
-          if (any_def)
+          if (any_def && !mg_retried)
+            {
+              // first the set-aside instances get one fresh multigrid pass from their current X
+              // (a stall of flexible GMRES can be a poor Krylov space rather than a failing
+              // V-cycle); those that stall again finish with block-Jacobi
+              mg_retried = true;
+              for (int k = 0; k < n; ++k)
+                if (deferred[k]) prev_res[k] = c->h_norm[k];
+              solve_on = deferred;
+              std::fill(deferred.begin(), deferred.end(), 0);
+              more = true;
+            }
+          else if (any_def)
             {
               // the set-aside instances continue from their current X with block-Jacobi GMRES
               use_mg = false;
