@@ -97,6 +97,8 @@ struct DevMesh
   const uint8_t *robin;
   const int32_t *robin_cells;
   int64_t n_robin;
+  // some node has a constraint row (hanging node or periodic image): gathers must expand them
+  int has_constraints;
 };
 
 #ifdef __CUDACC__

@@ -1368,6 +1368,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   d.node_inst = p_ni;
   d.mask = p_mask;
   d.hptr = p_hptr;
+  d.has_constraints = (!P.hptr.empty() && P.hptr.back() > 0) ? 1 : 0;
   d.hpar = p_hpar;
   d.hw = p_hw;
   d.rowptr = p_rowptr;

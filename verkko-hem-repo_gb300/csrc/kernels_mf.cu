@@ -402,48 +402,53 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
 #pragma unroll
       for (int k = 0; k < 6; ++k) S.bulk[tid][k] = bk[k];
     }
-  // nodal values: thread entries idx = tid + k kMThreads, k < 9 (144 NC entries over 16 NC
-  // threads); node ids, then values, ranges and masks are requested together
+  // nodal values: the 16 threads of cell cl = tid / 16 take its 144 (vertex, component)
+  // entries e = lt + 16 k, k < 9 (lt = tid % 16); node ids, then values and masks are
+  // requested together.  Constraint rows (hanging nodes, periodic images) are expanded from
+  // their parents only on meshes that have them.
   {
     constexpr int kPer = 9;
-    static_assert(kMCells * 144 == kPer * kMThreads, "nine entries per thread");
+    static_assert(kMThreads == 16 * kMCells, "16 threads per cell");
+    const int cl = tid >> 4, lt = tid & 15;
+    const bool cell_ok = cl < ncb;
+    const int32_t *cn = m.cells + (e0 + cl) * 8;
     int node[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      {
-        const int idx = tid + k * kMThreads, cl = idx / 144, v = (idx - 144 * cl) / 18;
-        node[k] = (cl < ncb) ? m.cells[(e0 + cl) * 8 + v] : -1;
-      }
+    for (int k = 0; k < kPer; ++k) node[k] = cell_ok ? cn[(lt + 16 * k) / 18] : -1;
     float zv[kPer], xv[kPer];
-    int h0[kPer], h1[kPer];
     uint32_t mk[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; ++k)
       {
-        const int idx = tid + k * kMThreads, c = (idx % 144) % 18;
+        const int c = (lt + 16 * k) % 18;
         const bool ok = node[k] >= 0;
         const int64_t b = ok ? static_cast<int64_t>(node[k]) * 18 + c : 0;
         zv[k] = ok ? z[b] : 0.f;
         xv[k] = ok ? xs[b] : 0.f;
-        h0[k] = ok ? m.hptr[node[k]] : 0;
-        h1[k] = ok ? m.hptr[node[k] + 1] : 0;
         mk[k] = ok ? m.mask[node[k]] : ~0u;
       }
+    float *zs = &S.u.g.zs[cl][0][0], *xsh = &S.u.g.xs[cl][0][0];
 #pragma unroll
     for (int k = 0; k < kPer; ++k)
       {
-        const int idx = tid + k * kMThreads, cl = idx / 144, rem = idx - 144 * cl, v = rem / 18, c = rem - 18 * v;
-        float val = 0.f;
-        if (h1[k] > h0[k])
-          for (int j = h0[k]; j < h1[k]; ++j)
-            {
-              const int par = m.hpar[j]; // a parent's zero-Dirichlet components do not enter
-              if (!((m.mask[par] >> c) & 1u)) val += static_cast<float>(m.hw[j]) * z[static_cast<int64_t>(par) * 18 + c];
-            }
-        else if (!((mk[k] >> c) & 1u))
-          val = zv[k];
-        S.u.g.zs[cl][v][c] = val;
-        S.u.g.xs[cl][v][c] = xv[k]; // the state is stored distributed: vertex values as they are
+        const int e = lt + 16 * k, c = e % 18;
+        float val = ((mk[k] >> c) & 1u) ? 0.f : zv[k];
+        if (m.has_constraints && node[k] >= 0)
+          {
+            const int h0 = m.hptr[node[k]], h1 = m.hptr[node[k] + 1];
+            if (h1 > h0)
+              {
+                val = 0.f;
+                for (int j = h0; j < h1; ++j)
+                  {
+                    const int par = m.hpar[j]; // a parent's zero-Dirichlet components do not enter
+                    if (!((m.mask[par] >> c) & 1u))
+                      val += static_cast<float>(m.hw[j]) * z[static_cast<int64_t>(par) * 18 + c];
+                  }
+              }
+          }
+        zs[e] = val;
+        xsh[e] = xv[k]; // the state is stored distributed: vertex values as they are
       }
   }
   __syncthreads();
