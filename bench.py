@@ -548,7 +548,10 @@ def main():
         gl.set_launch_mode(True)
     # the small coarse levels as one cooperative launch per V-cycle instead of separate launches
     fused = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
-                      precond=pc, cfg=head_cfg, mg_small_fuse=True)
+                      precond=pc, cfg=head_cfg, mg_small_fuse=1)
+    # the V-cycle's tail (levels of at most 160 nodes and the dense solve) as one cluster launch
+    tail = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                     precond=pc, cfg=head_cfg, mg_small_fuse=2)
     e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
     batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc, cfg=head_cfg) if args.batch > 0 else None
 
@@ -618,8 +621,12 @@ def main():
         "launch_mode": {"programmatic_ms_per_solve": ms_step, "plain_ms_per_solve": float(np.mean(plain["ms"])),
                         "note": "programmatic dependent launch (the default) against plain stream order"},
         "small_level_fusion": {"separate_ms_per_solve": ms_step, "fused_ms_per_solve": float(np.mean(fused["ms"])),
-                               "note": "coarse levels below 20,000 nodes as one launch per sweep, residual and "
-                                       "transfer (the default) against one cooperative launch per V-cycle"},
+                               "cluster_tail_ms_per_solve": float(np.mean(tail["ms"])),
+                               "cluster_tail_gmres_its": int(tail["out"]["gmres_its"][0]),
+                               "note": "coarse levels as one launch per sweep, residual and transfer (the headline) "
+                                       "against one cooperative launch per V-cycle for the levels below 20,000 "
+                                       "nodes (fused) and one thread-block cluster launch for the levels of at "
+                                       "most 160 nodes and the dense solve (cluster_tail)"},
         "autotune": None if tuned is None else {
             "config": tuned["config"], "ms_best_trial": tuned["ms"], "tuning_s": tuned["tuning_s"],
             "trials": [{"config": t["config"], "ms": t["ms"]} for t in tuned["trials"]],

@@ -112,11 +112,15 @@ typedef struct
                            A + mg_coarse_shift * mean|diag A| * 1 (default 1e-4).  The shift bounds
                            the amplification of the near-null modes (global phase and spin
                            rotations are exact symmetries of the functional); must be > 0 */
-  int mg_small_fuse;    /* multigrid: 1 runs the coarse levels of at most 20,000 nodes (all instances
-                           together), down to the dense coarsest solve, as one cooperative launch per
-                           V-cycle whose CTAs walk the levels phase by phase with grid-wide barriers
-                           (bounded waits: GLGPU_ERR_TIMEOUT if one gives up); 0 (default): one launch
-                           per sweep, residual and transfer (measured faster on GB300) */
+  int mg_small_fuse;    /* multigrid, how the small coarse levels run.  0 (default): one launch per
+                           sweep, residual and transfer.  1: the levels of at most 20,000 nodes (all
+                           instances together), down to the dense coarsest solve, as one cooperative
+                           launch per V-cycle whose CTAs walk the levels phase by phase with
+                           grid-wide barriers (bounded waits: GLGPU_ERR_TIMEOUT if one gives up).
+                           2: the levels of at most 160 nodes per instance and the dense solve as one
+                           launch of one thread-block cluster per instance (hardware cluster barriers
+                           between phases); contexts with too many instances for clusters of at least
+                           4 CTAs keep separate launches */
 } glgpu_params;
 
 typedef struct glgpu_ctx glgpu_ctx;

@@ -287,25 +287,29 @@ def test_programmatic_launch_gives_identical_solves(gl):
     assert np.array_equal(x1, x0b)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("precision,n_inst", [("mixed", 1), ("mixed", 3), ("fp64", 1)])
-def test_fused_small_levels_match_separate_launches(gl, oracle_gl, precision, n_inst):
-    """The coarse levels below 20,000 nodes run as one cooperative launch per V-cycle; the
-    Newton solve reaches the same free energy and state (up to the exact symmetries) as
-    with one launch per sweep and transfer, with iteration counts within one or two."""
+def test_fused_small_levels_match_separate_launches(gl, oracle_gl, precision, n_inst, mode):
+    """The small coarse levels in fewer launches: mode 1 the levels below 20,000 nodes as one
+    cooperative launch per V-cycle, mode 2 the levels of at most 160 nodes per instance and the
+    dense solve as one cluster launch per instance.  The Newton solve reaches the same free
+    energy and state (up to the exact symmetries) as with one launch per sweep and transfer,
+    with iteration counts within one or two, and launches fewer kernels per GMRES iteration."""
     prec = gl.MIXED if precision == "mixed" else gl.FP64
     meshes = [gl.cube_mesh(5.0, 12), gl.box_mesh([-4, -4, -3], [4, 4, 3], (10, 10, 8)), gl.cube_mesh(4.0, 8)][:n_inst]
     pts = [(20.0, 0.6), (10.0, 0.5), (30.0, 0.8)][:n_inst]
     x0 = np.concatenate([gl.bphase_guess(p, t, m.nn, noise=0.05, seed=5 + k) for k, (m, (p, t)) in enumerate(zip(meshes, pts))])
     res = {}
-    for fuse in (False, True):
+    for fuse in (0, mode):
         prms = [gl.Params.from_matep(p, t, precision=prec, precond=gl.PC_MULTIGRID, mg_small_fuse=fuse) for p, t in pts]
         with gl.FemGL(meshes, prms) as f:
             assert f.mg_levels >= 2
             f.set_solution(x0)
             o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
-            res[fuse] = (o, f.solution(), f.free_energy(), f.mg_fallbacks)
-    (o0, x_0, F0, _), (o1, x_1, F1, fb1) = res[False], res[True]
+            res[fuse] = (o, f.solution(), f.free_energy(), f.mg_fallbacks, f.launch_count)
+    (o0, x_0, F0, _, n0), (o1, x_1, F1, fb1, n1) = res[0], res[mode]
     assert o0["converged"] and o1["converged"] and fb1 == 0
+    assert n1 / o1["gmres_its"].sum() < n0 / o0["gmres_its"].sum()
     assert np.all(np.abs(o1["gmres_its"] - o0["gmres_its"]) <= 2 + 0.1 * o0["gmres_its"])
     assert np.allclose(F1, F0, rtol=1e-9, atol=0)
     off = np.cumsum([0] + [18 * m.nn for m in meshes])

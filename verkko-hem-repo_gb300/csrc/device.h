@@ -298,6 +298,27 @@ cudaError_t launch_vcycle_small(bool fp32, const void *levels, const void *cycle
                                 cudaStream_t s);
 // CTAs per SM the fused small-level V-cycle is launched with (the occupancy limit, at most 4)
 int vcycle_small_blocks_per_sm(bool fp32);
+
+// The tail of a V-cycle (the few smallest levels and the dense coarsest solve) in one launch
+// of one thread-block cluster per instance: the CTAs of a cluster split each phase's rows
+// and meet at the cluster's hardware barrier between phases.  It starts from the parent
+// level's residual (the finest level outside the tail) and ends with the parent's coarse
+// correction out = cur + P e.  levels: device array of SmallLevel<T> [n_tail + 2]: [0] the
+// parent (its plan and the transfers to [1]), [1 .. n_tail] the smoothing levels, [n_tail
+// + 1] the dense level.
+template <typename T> struct TailCycle
+{
+  int n_tail;               // smoothing levels in the tail (>= 1)
+  int pre, post;
+  T omega;
+  const int64_t *dense_off;
+  const float *inv;
+};
+// cluster size (CTAs per instance) the tail can be launched with for n_inst instances on
+// this device (16, 8, 4, 2 or 1; 0: not available); also sets the kernel's attributes
+int vcycle_tail_cluster(bool fp32, int n_inst);
+cudaError_t launch_vcycle_tail(bool fp32, const void *levels, const void *cycle, int n_inst, int cluster,
+                               const void *p_res, const void *p_cur, void *p_out, const uint8_t *act, cudaStream_t s);
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, float shift, cudaStream_t s);
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

@@ -153,6 +153,12 @@ struct glgpu_ctx
   std::vector<unsigned char> small_cycle; // SmallCycle<T>, passed by value at launch
   unsigned int *small_bar = nullptr;
   int *small_err = nullptr;
+  // the V-cycle's tail as one cluster launch per instance (first tail level tail_ls, its
+  // parent tail_ls - 1; 0: separate launches): device descriptors, cycle constants, CTAs per
+  // cluster
+  int tail_ls = 0, tail_cs = 0;
+  void *tail_levels = nullptr;
+  std::vector<unsigned char> tail_cycle; // TailCycle<T>, passed by value at launch
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   // per instance, the last glgpu_run step's |R|: the line search's value and the FP64 value
@@ -949,22 +955,31 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
     CKS(launch(L, KK_SPMV, 1, [&] { return launch_spmv(L->dm, m, L->vals, cur, t, act, L->st, r); }));
   glgpu_ctx *C = c->lv[l];
   const glgpu_ctx::Transfer &tr = c->tr[l];
-  const bool fuse = (l + 1 < c->n_levels) && C->B == 18; // the next level smooths (not the dense solve)
-  if (fuse)
+  if (c->tail_ls == l + 1)
+    // every coarser level in one cluster launch per instance, ending with oth = cur + P e
     CKS(launch(c, KK_PREC, 1, [&] {
-      return launch_restrict_smooth(m, C->nn, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask, C->dm.node_inst, act,
-                                    C->dinv, om, C->X, c->st);
+      return launch_vcycle_tail(m, c->tail_levels, c->tail_cycle.data(), c->n_inst, c->tail_cs, t, cur, oth, act,
+                                c->st);
     }));
   else
-    CKS(launch(c, KK_PREC, 1, [&] {
-      return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
-                             C->dm.node_inst, act, c->st);
-    }));
-  CKS(vcycle(c, l + 1, C->Bv, C->X, act, fuse));
-  CKS(launch(c, KK_PREC, 1, [&] {
-    return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, oth, L->dm.mask, L->dm.hptr,
-                          L->dm.node_inst, act, c->st, cur);
-  }));
+    {
+      const bool fuse = (l + 1 < c->n_levels) && C->B == 18; // the next level smooths (not the dense solve)
+      if (fuse)
+        CKS(launch(c, KK_PREC, 1, [&] {
+          return launch_restrict_smooth(m, C->nn, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask, C->dm.node_inst,
+                                        act, C->dinv, om, C->X, c->st);
+        }));
+      else
+        CKS(launch(c, KK_PREC, 1, [&] {
+          return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
+                                 C->dm.node_inst, act, c->st);
+        }));
+      CKS(vcycle(c, l + 1, C->Bv, C->X, act, fuse));
+      CKS(launch(c, KK_PREC, 1, [&] {
+        return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, oth, L->dm.mask, L->dm.hptr,
+                              L->dm.node_inst, act, c->st, cur);
+      }));
+    }
   std::swap(cur, oth);
   for (int s = 0; s < post; ++s)
     {
@@ -1034,7 +1049,7 @@ template <typename T> glgpu_status small_setup_t(glgpu_ctx *c, int ls)
 glgpu_status small_setup(glgpu_ctx *c)
 {
   const int nl = c->n_levels;
-  if (nl < 2 || c->B != 18 || !c->prm[0].mg_small_fuse) return GLGPU_OK;
+  if (nl < 2 || c->B != 18 || c->prm[0].mg_small_fuse != 1) return GLGPU_OK;
   int ls = nl;
   while (ls - 1 >= 1)
     {
@@ -1066,6 +1081,78 @@ glgpu_status small_check(glgpu_ctx *c)
   CK(cudaMemsetAsync(c->small_err, 0, sizeof(int), c->st));
   CKS(sync(c));
   return set_error(GLGPU_ERR_TIMEOUT, "multigrid: a grid barrier of the fused coarse-level cycle timed out");
+}
+
+// The V-cycle's tail in one cluster launch per instance: the smoothing levels whose
+// instances have at most kTailNodes nodes each (FP32/FP64 blocks), the dense level below
+// them, and their parent, the finest level outside the tail.
+constexpr int64_t kTailNodes = 160;
+constexpr int kTailMaxLevels = 8; // smoothing levels the kernel walks
+
+template <typename T> glgpu_status tail_setup_t(glgpu_ctx *c, int lp)
+{
+  const int nl = c->n_levels;
+  std::vector<SmallLevel<T>> lev(static_cast<size_t>(nl - lp + 1));
+  for (int l = lp; l <= nl; ++l)
+    {
+      glgpu_ctx *L = (l == 0) ? c : c->lv[l - 1];
+      SmallLevel<T> &d = lev[static_cast<size_t>(l - lp)];
+      d.m = L->dm;
+      const bool smoothing = l > lp && l < nl; // the parent and the dense level only transfer
+      d.vals = smoothing ? static_cast<const T *>(L->vals) : nullptr;
+      d.dinv = smoothing ? static_cast<const T *>(L->dinv) : nullptr;
+      d.r = static_cast<T *>(L->Bv);
+      d.z = static_cast<T *>(L->X);
+      d.t = static_cast<T *>(L->Tmp);
+      d.t2 = static_cast<T *>(L->C1);
+      if (l < nl)
+        {
+          const glgpu_ctx::Transfer &t = c->tr[l];
+          d.r_ptr = t.r_ptr;
+          d.r_idx = t.r_idx;
+          d.r_w = static_cast<const T *>(t.r_w);
+          d.p_ptr = t.p_ptr;
+          d.p_idx = t.p_idx;
+          d.p_w = static_cast<const T *>(t.p_w);
+        }
+    }
+  std::vector<unsigned char> bytes(sizeof(SmallLevel<T>) * lev.size());
+  std::memcpy(bytes.data(), lev.data(), bytes.size());
+  unsigned char *dl = nullptr;
+  CKS(dupload(c, &dl, bytes));
+  c->tail_levels = dl;
+  TailCycle<T> cy{};
+  cy.n_tail = nl - lp - 1;
+  cy.pre = std::max(1, c->prm[0].mg_pre);
+  cy.post = std::max(0, c->prm[0].mg_post);
+  cy.omega = static_cast<T>(c->prm[0].mg_omega);
+  cy.dense_off = c->d_dense_off;
+  cy.inv = c->d_inv;
+  c->tail_cycle.resize(sizeof(cy));
+  std::memcpy(c->tail_cycle.data(), &cy, sizeof(cy));
+  c->tail_ls = lp + 1;
+  return GLGPU_OK;
+}
+
+glgpu_status tail_setup(glgpu_ctx *c)
+{
+  const int nl = c->n_levels;
+  if (nl < 2 || c->B != 18 || c->prm[0].mg_small_fuse != 2) return GLGPU_OK;
+  int ls = nl; // first tail level
+  while (ls - 1 >= 1)
+    {
+      const glgpu_ctx *L = c->lv[ls - 2]; // level ls - 1
+      int64_t most = 0;
+      for (int k = 0; k < c->n_inst; ++k) most = std::max(most, L->P.node_off[k + 1] - L->P.node_off[k]);
+      if (most > kTailNodes || L->dm.half_vals || L->B != 18) break;
+      --ls;
+    }
+  ls = std::max(ls, nl - kTailMaxLevels);
+  if (ls >= nl) return GLGPU_OK; // no smoothing level small enough
+  const int cs = vcycle_tail_cluster(c->mixed, c->n_inst);
+  if (cs < 1) return GLGPU_OK;   // too many instances for clusters of useful size
+  c->tail_cs = cs;
+  return c->mixed ? tail_setup_t<float>(c, ls - 1) : tail_setup_t<double>(c, ls - 1);
 }
 
 glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst)
@@ -1178,6 +1265,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
   }
   c->n_levels = nl;
   CKS(small_setup(c));
+  CKS(tail_setup(c));
   return GLGPU_OK;
 }
 
@@ -1229,6 +1317,9 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
     if (!(prm[k].bt > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_create: bt (AdGR diffuse length) must be > 0");
   for (int k = 0; k < n_inst; ++k)
     if (!(prm[k].mg_coarse_shift > 0.0)) return set_error(GLGPU_ERR_ARG, "glgpu_create: mg_coarse_shift must be > 0");
+  for (int k = 0; k < n_inst; ++k)
+    if (prm[k].mg_small_fuse < 0 || prm[k].mg_small_fuse > 2)
+      return set_error(GLGPU_ERR_ARG, "glgpu_create: mg_small_fuse must be 0, 1 or 2");
   if (prm[0].gmres_restart < 1 || prm[0].gmres_restart > 64)
     return set_error(GLGPU_ERR_ARG, "glgpu_create: gmres_restart must be in [1, 64]");
   if (prm[0].mf_cells != 4 && prm[0].mf_cells != 8 && prm[0].mf_cells != 16)

@@ -65,8 +65,9 @@ constexpr int kSpmvWarps = 8;
 // row's column ids are loaded once, one per lane, and broadcast by shuffle, and the block
 // loop is unrolled, so the loads of several blocks are in flight together.  With WPR > 1
 // warps per row (small coarse levels, where one warp per 27-block row would leave the
-// GPU latency-bound) warp kw of the row takes every WPR-th block.
-template <typename T, typename MT, int WPR>
+// GPU latency-bound) warp kw of the row takes every WPR-th block.  With CG, x is read from L2
+// (ld.global.cg): inside one launch it was written by other CTAs.
+template <typename T, typename MT, int WPR, bool CG = false>
 __device__ __forceinline__ void row_products(const DevMesh &m, const MT *__restrict__ vals, const T *__restrict__ x,
                                              int64_t n, int lane, int kw,
                                              T (&acc)[(324 / Vec16<MT>::n + 31) / 32][Vec16<MT>::n])
@@ -88,7 +89,7 @@ __device__ __forceinline__ void row_products(const DevMesh &m, const MT *__restr
       for (int k = kw; k < nbk; k += WPR)
         {
           const int64_t col = __shfl_sync(0xffffffffu, mycol, k);
-          const T xv = (lane < 18) ? x[col * 18 + lane] : T(0);
+          const T xv = (lane < 18) ? (CG ? __ldcg(x + col * 18 + lane) : x[col * 18 + lane]) : T(0);
           const V *bp = reinterpret_cast<const V *>(vals + static_cast<int64_t>(base + k) * 324);
 #pragma unroll
           for (int it = 0; it < NIT; ++it)
@@ -1692,6 +1693,329 @@ cudaError_t launch_vcycle_small(bool fp32, const void *levels, const void *cycle
                               *static_cast<const SmallCycle<float> *>(cycle), act);
   return cudaLaunchKernelEx(&cfg, k_vcycle_small<double>, static_cast<const SmallLevel<double> *>(levels),
                             *static_cast<const SmallCycle<double> *>(cycle), act);
+}
+
+// ---------------------------------------------------------------------------------
+// The V-cycle's tail (the smallest levels and the dense solve) as one launch of one
+// thread-block cluster per instance.  Each of those levels is a few hundred nodes at most,
+// so a separate launch per sweep, residual and transfer is almost all latency; here the
+// cluster's CTAs split each phase's rows and wait for each other at the cluster barrier
+// (barrier.cluster, release / acquire: a hardware barrier over co-scheduled CTAs, no
+// polling).  Vectors written in one phase and read in the next by other CTAs are read
+// from L2 (ld.global.cg).  The phases compute what the separate kernels compute, row for
+// row: the same lane maps, the same summation orders.
+// ---------------------------------------------------------------------------------
+constexpr int kTailThreads = 512;
+constexpr int kTailWarps = kTailThreads / 32;
+constexpr int kTailWpr = 2;                      // warps per block row
+constexpr int kTailRows = kTailWarps / kTailWpr; // block rows per CTA and pass
+constexpr int kTailNodes = kTailThreads / 18;    // nodes per CTA and pass, thread per component
+constexpr int kMaxTail = 8;                      // smoothing levels in a tail
+
+template <typename T> constexpr size_t tail_smem_bytes() { return sizeof(T) * (kTailWarps * 324 + kTailNodes * 18); }
+
+__device__ __forceinline__ unsigned tail_rank()
+{
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned tail_csize()
+{
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+// all threads of the cluster: the writes before are visible to the reads after
+__device__ __forceinline__ void tail_sync()
+{
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// rows [n0, n1) of level L: RES: y = r - A zin; otherwise y = zin + omega D^-1 (r - A zin)
+// (zin == nullptr: y = omega D^-1 r).  The loop is uniform over the CTA (it depends on the
+// rank only), so the CTA barriers inside are reached by every thread.
+template <typename T, bool RES>
+__device__ void tail_rows(const SmallLevel<T> &L, int64_t n0, int64_t n1, const T *zin, T *y, T omega, unsigned rank,
+                          unsigned cs, T (*red)[324])
+{
+  using V = typename Vec16<T>::type;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int NCH = 324 / NV;
+  constexpr int NIT = (NCH + 31) / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int kw = warp % kTailWpr, w0 = warp - kw;
+  for (int64_t base = n0 + static_cast<int64_t>(rank) * kTailRows; base < n1;
+       base += static_cast<int64_t>(cs) * kTailRows)
+    {
+      const int64_t n = base + warp / kTailWpr;
+      const bool on = n < n1; // uniform over the warp
+      T t = (on && lane < 18) ? __ldcg(L.r + n * 18 + lane) : T(0);
+      if (zin)
+        {
+          T acc[NIT][NV];
+          if (on)
+            row_products<T, T, kTailWpr, true>(L.m, L.vals, zin, n, lane, kw, acc);
+          else
+#pragma unroll
+            for (int it = 0; it < NIT; ++it)
+#pragma unroll
+              for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
+          store_products<T, T>(red[warp], acc, lane);
+          __syncthreads();
+          if (on && lane < 18) t -= row_sum<T, kTailWpr>(red, w0, lane);
+          __syncthreads();
+        }
+      if (RES)
+        {
+          if (on && kw == 0 && lane < 18) y[n * 18 + lane] = t;
+          continue;
+        }
+      if (on && kw == 0)
+        {
+          T acc[NIT][NV];
+          const V *bp = reinterpret_cast<const V *>(L.dinv + n * 324);
+#pragma unroll
+          for (int it = 0; it < NIT; ++it)
+            {
+              const int ch = lane + 32 * it;
+              const V w = (ch < NCH) ? __ldg(bp + ch) : V{};
+#pragma unroll
+              for (int v = 0; v < NV; ++v)
+                {
+                  const int e = (ch < NCH) ? ch * NV + v : 0;
+                  acc[it][v] = vget<V, T>(w, v) * __shfl_sync(0xffffffffu, t, e % 18);
+                }
+            }
+          store_products<T>(red[warp], acc, lane);
+          __syncwarp();
+          if (lane < 18)
+            y[n * 18 + lane] = (zin ? __ldcg(zin + n * 18 + lane) : T(0)) + omega * row_sum<T, 1>(red, warp, lane);
+        }
+      __syncthreads(); // red is reused by the next pass
+    }
+}
+
+// rc = P^T rf on the coarse rows [c0, c1) of C (zero on zero-Dirichlet components); with
+// SMOOTH also C.z = omega D^-1 rc, the coarse level's first sweep from zero
+template <typename T, bool SMOOTH>
+__device__ void tail_restrict(const SmallLevel<T> &F, const T *rf, const SmallLevel<T> &C, int64_t c0, int64_t c1,
+                              T omega, unsigned rank, unsigned cs, T (*ts)[18])
+{
+  const int ln = threadIdx.x / 18, c = threadIdx.x - 18 * (threadIdx.x / 18);
+  for (int64_t base = c0 + static_cast<int64_t>(rank) * kTailNodes; base < c1;
+       base += static_cast<int64_t>(cs) * kTailNodes)
+    {
+      const int64_t n = base + ln;
+      const bool on = ln < kTailNodes && n < c1;
+      T s = T(0);
+      if (on && !((C.m.mask[n] >> c) & 1u))
+        for (int k = F.r_ptr[n]; k < F.r_ptr[n + 1]; ++k)
+          s += F.r_w[k] * __ldcg(rf + static_cast<int64_t>(F.r_idx[k]) * 18 + c);
+      if (on) C.r[n * 18 + c] = s;
+      if (SMOOTH)
+        {
+          if (ln < kTailNodes) ts[ln][c] = s;
+          __syncthreads();
+          if (on)
+            {
+              const T *row = C.dinv + n * 324 + c * 18;
+              T u = T(0);
+#pragma unroll
+              for (int d = 0; d < 18; ++d) u += __ldg(row + d) * ts[ln][d];
+              C.z[n * 18 + c] = omega * u;
+            }
+          __syncthreads();
+        }
+    }
+}
+
+// out = base + P zc on the rows [f0, f1) of F (hanging nodes and constrained components keep base)
+template <typename T>
+__device__ void tail_prolong(const SmallLevel<T> &F, int64_t f0, int64_t f1, const T *zc, const T *base, T *out,
+                             unsigned rank, unsigned cs)
+{
+  const int64_t total = (f1 - f0) * 18;
+  for (int64_t i = static_cast<int64_t>(rank) * kTailThreads + threadIdx.x; i < total;
+       i += static_cast<int64_t>(cs) * kTailThreads)
+    {
+      const int64_t g = f0 * 18 + i;
+      const int64_t n = g / 18;
+      const int c = static_cast<int>(g - n * 18);
+      const T b0 = __ldcg(base + g);
+      if (F.m.hptr[n + 1] > F.m.hptr[n] || ((F.m.mask[n] >> c) & 1u))
+        {
+          out[g] = b0;
+          continue;
+        }
+      T s = T(0);
+      for (int k = F.p_ptr[n]; k < F.p_ptr[n + 1]; ++k)
+        s += F.p_w[k] * __ldcg(zc + static_cast<int64_t>(F.p_idx[k]) * 18 + c);
+      out[g] = b0 + s;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTailThreads, 1)
+  k_vcycle_tail(const SmallLevel<T> *__restrict__ lev, TailCycle<T> cy, const T *__restrict__ p_res,
+                const T *__restrict__ p_cur, T *__restrict__ p_out, const uint8_t *__restrict__ act)
+{
+  pdl_wait();
+  pdl_trigger();
+  extern __shared__ __align__(16) unsigned char tail_smem[];
+  T(*red)[324] = reinterpret_cast<T(*)[324]>(tail_smem);
+  T(*ts)[18] = reinterpret_cast<T(*)[18]>(tail_smem + sizeof(T) * kTailWarps * 324);
+  const unsigned rank = tail_rank(), cs = tail_csize();
+  const int inst = static_cast<int>(blockIdx.x / cs);
+  if (act && !act[inst]) return; // the whole cluster: the flag is per instance
+  const int nt = cy.n_tail;
+  const T om = cy.omega;
+  T *curs[kMaxTail + 1];
+  // descent: level 1's right-hand side and first sweep from the parent's residual
+  tail_restrict<T, true>(lev[0], p_res, lev[1], lev[1].m.node_off_ptr[inst], lev[1].m.node_off_ptr[inst + 1], om, rank,
+                         cs, ts);
+  tail_sync();
+  for (int i = 1; i <= nt; ++i)
+    {
+      const SmallLevel<T> &L = lev[i];
+      const int64_t a = L.m.node_off_ptr[inst], b = L.m.node_off_ptr[inst + 1];
+      T *cur = L.z, *oth = L.t2;
+      for (int sw = 1; sw < cy.pre; ++sw)
+        {
+          tail_rows<T, false>(L, a, b, cur, oth, om, rank, cs, red);
+          tail_sync();
+          T *tmp = cur;
+          cur = oth;
+          oth = tmp;
+        }
+      tail_rows<T, true>(L, a, b, cur, L.t, om, rank, cs, red);
+      tail_sync();
+      const SmallLevel<T> &C = lev[i + 1];
+      const int64_t ca = C.m.node_off_ptr[inst], cb = C.m.node_off_ptr[inst + 1];
+      if (i < nt)
+        tail_restrict<T, true>(L, L.t, C, ca, cb, om, rank, cs, ts);
+      else
+        tail_restrict<T, false>(L, L.t, C, ca, cb, om, rank, cs, ts);
+      tail_sync();
+      curs[i] = cur;
+    }
+  // the dense coarsest level: z = inverse r, warp per row (FP32 inverse and accumulation)
+  {
+    const SmallLevel<T> &D = lev[nt + 1];
+    const int64_t d0 = D.m.node_off_ptr[inst], d1 = D.m.node_off_ptr[inst + 1];
+    const int nd = static_cast<int>((d1 - d0) * 18);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float *Ai = cy.inv + cy.dense_off[inst];
+    const T *rv = D.r + d0 * 18;
+    for (int row = static_cast<int>(rank) * kTailWarps + warp; row < nd; row += static_cast<int>(cs) * kTailWarps)
+      {
+        const float *A = Ai + static_cast<int64_t>(row) * nd;
+        float s = 0.f;
+        for (int j = lane; j < nd; j += 32) s += __ldg(A + j) * static_cast<float>(__ldcg(rv + j));
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) D.z[d0 * 18 + row] = static_cast<T>(s);
+      }
+  }
+  tail_sync();
+  // ascent: prolongation into the other buffer, post-sweeps
+  const T *zc = lev[nt + 1].z;
+  for (int i = nt; i >= 1; --i)
+    {
+      const SmallLevel<T> &L = lev[i];
+      const int64_t a = L.m.node_off_ptr[inst], b = L.m.node_off_ptr[inst + 1];
+      T *cur = curs[i];
+      T *oth = (cur == L.z) ? L.t2 : L.z;
+      tail_prolong<T>(L, a, b, zc, cur, oth, rank, cs);
+      tail_sync();
+      T *tmp = cur;
+      cur = oth;
+      oth = tmp;
+      for (int sw = 0; sw < cy.post; ++sw)
+        {
+          tail_rows<T, false>(L, a, b, cur, oth, om, rank, cs, red);
+          tail_sync();
+          tmp = cur;
+          cur = oth;
+          oth = tmp;
+        }
+      zc = cur;
+    }
+  // the parent's coarse correction (read by the next launch)
+  tail_prolong<T>(lev[0], lev[0].m.node_off_ptr[inst], lev[0].m.node_off_ptr[inst + 1], zc, p_cur, p_out, rank, cs);
+}
+
+template <typename T> static cudaError_t tail_attributes(int cs)
+{
+  cudaError_t e = cudaFuncSetAttribute(k_vcycle_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(tail_smem_bytes<T>()));
+  if (e == cudaSuccess && cs > 8) e = cudaFuncSetAttribute(k_vcycle_tail<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  return e;
+}
+
+template <typename T> static int tail_cluster_t(int n_inst)
+{
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    {
+      cudaGetLastError();
+      return 0;
+    }
+  // at least 4 CTAs per instance (fewer leave each phase's rows to too few SMs), and all
+  // clusters co-resident in about two waves
+  for (int cs = 16; cs >= 4; cs /= 2)
+    {
+      if (static_cast<int64_t>(n_inst) * cs > 2 * static_cast<int64_t>(sms)) continue;
+      if (tail_attributes<T>(cs) != cudaSuccess)
+        {
+          cudaGetLastError();
+          continue;
+        }
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = static_cast<unsigned>(cs);
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(static_cast<unsigned>(cs * n_inst));
+      cfg.blockDim = dim3(kTailThreads);
+      cfg.dynamicSmemBytes = tail_smem_bytes<T>();
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nc = 0;
+      if (cudaOccupancyMaxActiveClusters(&nc, k_vcycle_tail<T>, &cfg) == cudaSuccess && nc > 0) return cs;
+      cudaGetLastError();
+    }
+  return 0;
+}
+
+int vcycle_tail_cluster(bool fp32, int n_inst) { return fp32 ? tail_cluster_t<float>(n_inst) : tail_cluster_t<double>(n_inst); }
+
+cudaError_t launch_vcycle_tail(bool fp32, const void *levels, const void *cycle, int n_inst, int cluster,
+                               const void *p_res, const void *p_cur, void *p_out, const uint8_t *act, cudaStream_t s)
+{
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(cluster * n_inst));
+  cfg.blockDim = dim3(kTailThreads);
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (fp32)
+    {
+      cfg.dynamicSmemBytes = tail_smem_bytes<float>();
+      return cudaLaunchKernelEx(&cfg, k_vcycle_tail<float>, static_cast<const SmallLevel<float> *>(levels),
+                                *static_cast<const TailCycle<float> *>(cycle), static_cast<const float *>(p_res),
+                                static_cast<const float *>(p_cur), static_cast<float *>(p_out), act);
+    }
+  cfg.dynamicSmemBytes = tail_smem_bytes<double>();
+  return cudaLaunchKernelEx(&cfg, k_vcycle_tail<double>, static_cast<const SmallLevel<double> *>(levels),
+                            *static_cast<const TailCycle<double> *>(cycle), static_cast<const double *>(p_res),
+                            static_cast<const double *>(p_cur), static_cast<double *>(p_out), act);
 }
 
 } // namespace glgpu

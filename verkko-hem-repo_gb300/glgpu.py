@@ -429,8 +429,9 @@ class Params:
     bt: float = 1e10
     #: multigrid: relative diagonal shift of the coarsest level's dense solve
     mg_coarse_shift: float = 1e-4
-    #: multigrid: the small coarse levels as one cooperative launch per V-cycle
-    mg_small_fuse: bool = False
+    #: multigrid, the small coarse levels: 0 one launch per sweep and transfer, 1 one cooperative
+    #: launch per V-cycle, 2 one cluster launch per instance for the tail (True means 1)
+    mg_small_fuse: int = 0
 
     @classmethod
     def from_matep(cls, p: float, t: float, scc: bool = True, **kw) -> "Params":
@@ -451,7 +452,7 @@ class Params:
         s.prec_reuse = float(self.prec_reuse)
         s.bt = float(self.bt)
         s.mg_coarse_shift = float(self.mg_coarse_shift)
-        s.mg_small_fuse = int(bool(self.mg_small_fuse))
+        s.mg_small_fuse = int(self.mg_small_fuse)
         return s
 
 
