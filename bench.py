@@ -761,6 +761,10 @@ def config4_leg(gl, count, linear_tol):
             "waves": r["waves"], "solve_ms_per_wave": r["solve_ms"], "create_s_per_wave": r["create_s"],
             "wave_gib": [b / 2**30 for b in r["wave_bytes"]], "bytes_per_node": r["bytes_per_node"],
             "budget_gib": r["budget"] / 2**30, "mg_fallbacks": r["mg_fallbacks"],
+            "handed_off": [int(i) for i in np.flatnonzero(r["handed_off"])], "handoff_ms_per_wave": r["handoff_ms"],
+            "handoff_note": "instances whose mixed multigrid solve stalled twice leave their wave at the state they "
+                            "reached and are finished alone (two pre- and post-sweeps, then FP64); their device time "
+                            "is part of solve_ms_per_wave",
             "all_converged": bool(r["converged"].all()), "max_final_residual": float(r["residual"].max()),
             "newton_its_mean": float(r["newton_its"].mean()), "gmres_its_mean": float(r["gmres_its"].mean()),
             "free_energy_rel_diff_vs_fp64_sample": rel,

@@ -270,6 +270,16 @@ int glgpu_mg_levels(const glgpu_ctx *ctx);
  * cycle) or diverged and that finished with block-Jacobi GMRES. */
 int64_t glgpu_mg_fallbacks(const glgpu_ctx *ctx);
 
+/* Handoff (default off): an instance whose multigrid solve stalls again after its fresh
+ * multigrid pass does not finish with block-Jacobi GMRES in this context; glgpu_run stops its
+ * Newton iteration at the state it reached (no update from the unfinished solve), counts it
+ * as not converged (GLGPU_ERR_NOT_CONVERGED) and flags it, so that the caller can finish it in
+ * a context of its own (a batch then does not wait for one hard instance on launches sized
+ * for the whole batch). */
+glgpu_status glgpu_set_mg_handoff(glgpu_ctx *ctx, int on);
+/* flags[k] = 1 when instance k was handed off in the last glgpu_run, else 0 (n_inst bytes). */
+glgpu_status glgpu_mg_handed_off(const glgpu_ctx *ctx, uint8_t *flags);
+
 /* Sizes of coarse level `level` (1 = first coarse level .. glgpu_mg_levels): its node
  * count, block count, and the entries of the prolongation from it to level - 1. */
 glgpu_status glgpu_mg_level_info(const glgpu_ctx *ctx, int level, int64_t *n_nodes, int64_t *nnzb, int64_t *p_nnz);

@@ -317,3 +317,37 @@ def test_fused_small_levels_match_separate_launches(gl, oracle_gl, precision, n_
         a, b = x_1[off[k]:off[k + 1]], x_0[off[k]:off[k + 1]]
         xa, _, _ = oracle_gl.gauge_align(a, b)
         assert np.abs(xa - b).max() <= 1e-7 * np.abs(b).max()
+
+
+def test_stalled_instance_handed_off_and_finished(gl):
+    """A slab of the phase-diagram sweep (19^3 cells, T = 0.544 Tc, p = 11.8 bar, D = 39.1 xi0)
+    whose mixed-precision multigrid solve stalls: batched with an easy instance and handoff on,
+    it leaves the batch at the state it reached (flagged, unconverged) while the other converges
+    unchanged; the sweep finishes it alone (stronger smoothing, then FP64), at the free energy of
+    an FP64 multigrid solve from its start."""
+    sweep = __import__("importlib").import_module("verkko-hem-repo_gb300.sweep")
+    t, p, D, n = 0.5444804785663939, 11.833486443002236, 39.11806936676019, 19
+    hard = gl.box_mesh([-10.0, -10.0, -D / 2], [10.0, 10.0, D / 2], (n, n, n))
+    easy = gl.box_mesh([-10.0, -10.0, -6.0], [10.0, 10.0, 6.0], (16, 16, 16))
+    xh = gl.bphase_guess(p, t, hard.nn, noise=0.05, seed=1016)
+    xe = gl.bphase_guess(20.0, 0.6, easy.nn, noise=0.05, seed=7)
+    prms = [gl.Params.from_matep(p, t, precision=gl.MIXED, precond=gl.PC_MULTIGRID),
+            gl.Params.from_matep(20.0, 0.6, precision=gl.MIXED, precond=gl.PC_MULTIGRID)]
+    with gl.FemGL([hard, easy], prms) as f:
+        f.set_mg_handoff(True)
+        f.set_solution(np.concatenate([xh, xe]))
+        o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10, allow_unconverged=True)
+        handed = f.handed_off
+        assert handed.tolist() == [True, False] and f.mg_fallbacks == 0
+        assert o["residual"][0] > 1e-10 and o["residual"][1] <= 1e-10
+    with gl.FemGL(easy, prms[1]) as g:
+        g.set_solution(xe)
+        oe = g.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        assert int(oe["newton_its"][0]) == int(o["newton_its"][1])
+    r = sweep.solve_sweep(gl, [hard, easy], prms, [xh, xe])
+    assert r["converged"].all() and r["handed_off"].tolist() == [True, False]
+    with gl.FemGL(hard, gl.Params.from_matep(p, t, precision=gl.FP64, precond=gl.PC_MULTIGRID)) as h:
+        h.set_solution(xh)
+        h.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+        F64 = float(h.free_energy()[0])
+    assert abs(r["free_energy"][0] - F64) <= 1e-9 * abs(F64)

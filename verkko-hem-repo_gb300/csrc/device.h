@@ -6,6 +6,7 @@
 #include <utility>
 
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 
 namespace glgpu
 {
@@ -165,10 +166,11 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
 // Matrix-free FP32 Jacobian at the state xs [Nn][18] (FP32 copy of the distributed Newton
 // state; 3D, 18 components): the bulk Hessian is applied at each quadrature point from the
 // interpolated state without forming it.
-// mode 0: y = J z, 1: y = b - J z, 2: y = z + omega D^-1 (b - J z) with D^-1 [Nn][324].
-// ycell [Nc][8][18] is scratch; constrained rows act as the identity.
+// mode 0: y = J z, 1: y = b - J z, 2: y = z + omega D^-1 (b - J z) with D^-1 [Nn][324]
+// (FP16: the finest level's l1 block-Jacobi smoother).  ycell [Nc][8][18] is scratch;
+// constrained rows act as the identity.
 cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
-                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
+                      const __half *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
                       int cells_per_cta = 8);
 // One fused block-Jacobi sweep: y = z + omega D^-1 (b - A z); z == nullptr gives
 // y = omega D^-1 b.  18x18 blocks only; y must not alias z.
@@ -176,6 +178,12 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
                           void *y, double omega, const uint8_t *act, cudaStream_t s);
 // l1: add each row's absolute off-block sum to its diagonal (l1 block-Jacobi smoother)
 cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s, bool l1 = false);
+// the l1 smoother of a mixed context's finest level (FP32 or FP16 blocks in), inverse blocks
+// stored in FP16 (computed in FP64 arithmetic like the others); 18x18 blocks
+cudaError_t launch_bj_setup_half(const DevMesh &m, const void *vals, __half *dinv, cudaStream_t s);
+// y = omega D^-1 b with FP16 inverse blocks (the finest level's first sweep from zero)
+cudaError_t launch_smooth_zero_half(const DevMesh &m, const __half *dinv, const float *b, float *y, double omega,
+                                    const uint8_t *act, cudaStream_t s);
 cudaError_t launch_bj_apply(const DevMesh &m, bool fp32, const void *dinv, const void *x, void *y,
                             const uint8_t *inst_active, cudaStream_t s);
 // partial[s][v] = sum over segment s of X[v][i] * y[i], v < nv (X rows strided by ld)
@@ -260,15 +268,17 @@ cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, 
                                    const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
                                    const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s);
 // Galerkin product J_c = P^T J_f P on the coarse block pattern, one warp per coarse
-// block: block cb (row g_row[cb], column cols_c[cb]) is the sum over its term list
-// [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and
+// block: block cb = up[u] (row g_row[cb], column cols_c[cb] >= the row) is the sum over its
+// term list [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and
 // columns and the constrained nodes (hptr_c) of the coarse level become identity rows /
-// zero columns.
+// zero columns.  Then each block below the diagonal, lo[2 i], is set to the transpose of
+// its mirror lo[2 i + 1] (J_c is symmetric like J_f).
 // half_in / half_out: the fine / coarse blocks are stored in FP16 (mixed mode, summed in FP32).
-cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
-                            const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
-                            const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
-                            const uint8_t *act, cudaStream_t s, bool half_in = false, bool half_out = false);
+cudaError_t launch_galerkin(bool fp32, int64_t n_up, const int32_t *up, int64_t n_lo, const int32_t *lo,
+                            const int32_t *g_row, const int32_t *cols_c, const uint32_t *mask_c, const int32_t *hptr_c,
+                            void *vals_c, const int64_t *g_toff, const int32_t *g_blk, const void *g_w,
+                            const void *vals_f, const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s,
+                            bool half_in = false, bool half_out = false);
 // The small coarse levels of a V-cycle fused into one cooperative launch (levels whose
 // block values are FP32/FP64, 18x18 blocks): the recursion below the first such level
 // (pre-sweeps beyond the one that came with the restriction, residual, restriction fused

@@ -136,6 +136,8 @@ struct glgpu_ctx
     // Galerkin terms of every coarse block: [g_toff[cb], g_toff[cb+1]) of (fine block, weight)
     int64_t *g_toff = nullptr;
     int32_t *g_row = nullptr, *g_blk = nullptr;
+    int32_t *g_up = nullptr, *g_lo = nullptr; // blocks on / above the diagonal; (block, mirror) pairs below
+    int64_t n_up = 0, n_lo = 0;
     void *g_w = nullptr;
     std::vector<int32_t> h_ptr, h_idx;   // host copy of P
     std::vector<double> h_w;
@@ -160,6 +162,7 @@ struct glgpu_ctx
   void *tail_levels = nullptr;
   std::vector<unsigned char> tail_cycle; // TailCycle<T>, passed by value at launch
   void *sinv = nullptr;              // l1 block-Jacobi smoother of the finest level
+  bool sinv_half = false;            // ... stored in FP16 (mixed mode, matrix-free operator)
   std::vector<uint8_t> r_ok;         // per instance: R, r_cell, e_cell were evaluated at x
   // per instance, the last glgpu_run step's |R|: the line search's value and the FP64 value
   // that took the stop test (equal in FP64 mode and in steps that did not pass the test)
@@ -177,6 +180,10 @@ struct glgpu_ctx
   int64_t vc_nodes = 0;
   bool vc_failed = false;
   int64_t mg_fallbacks = 0;          // solves handed from multigrid to block-Jacobi
+  // instances whose multigrid solve stalled twice stop where they are instead of finishing
+  // with block-Jacobi in this context (mg_handoff); the caller finishes them elsewhere
+  bool mg_handoff = false;
+  std::vector<uint8_t> handed;       // per instance, set during the last glgpu_run
 };
 
 namespace
@@ -833,6 +840,14 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
               std::fill(deferred.begin(), deferred.end(), 0);
               more = true;
             }
+          else if (any_def && c->mg_handoff)
+            {
+              // handed off: these instances leave the solve with the X they reached; the
+              // Newton loop stops them without an update
+              for (int k = 0; k < n; ++k)
+                if (deferred[k]) c->handed[k] = 1;
+              std::fill(deferred.begin(), deferred.end(), 0);
+            }
           else if (any_def)
             {
               // the set-aside instances continue from their current X with block-Jacobi GMRES
@@ -879,16 +894,19 @@ template <typename T> glgpu_status upload_w(glgpu_ctx *c, void **dst, const std:
 // the coarsest level
 glgpu_status mg_assemble(glgpu_ctx *c, const uint8_t *act)
 {
-  CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(c->dm, c->mixed, c->vals, c->sinv, c->st, true); }));
+  CKS(launch(c, KK_PREC, 1, [&] {
+    return c->sinv_half ? launch_bj_setup_half(c->dm, c->vals, static_cast<__half *>(c->sinv), c->st)
+                        : launch_bj_setup(c->dm, c->mixed, c->vals, c->sinv, c->st, true);
+  }));
   for (int l = 0; l < c->n_levels; ++l)
     {
       glgpu_ctx *F = (l == 0) ? c : c->lv[l - 1];
       glgpu_ctx *L = c->lv[l];
       const glgpu_ctx::Transfer &t = c->tr[l];
       CKS(launch(c, KK_PREC, 1, [&] {
-        return launch_galerkin(c->mixed, L->nnzb, t.g_row, L->dm.cols, L->dm.mask, L->dm.hptr, L->vals, t.g_toff,
-                               t.g_blk, t.g_w, F->vals, L->dm.node_inst, act, c->st, F->dm.half_vals != 0,
-                               L->dm.half_vals != 0);
+        return launch_galerkin(c->mixed, t.n_up, t.g_up, t.n_lo, t.g_lo, t.g_row, L->dm.cols, L->dm.mask, L->dm.hptr,
+                               L->vals, t.g_toff, t.g_blk, t.g_w, F->vals, L->dm.node_inst, act, c->st,
+                               F->dm.half_vals != 0, L->dm.half_vals != 0);
       }));
       CKS(launch(c, KK_PREC, 1, [&] { return launch_bj_setup(L->dm, L->mixed, L->vals, L->dinv, L->st, true); }));
       L->has_J = true;
@@ -928,12 +946,18 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
   void *t2 = (l == 0) ? c->C3 : L->C1;
   const double om = c->prm[0].mg_omega;
   const int pre = std::max(1, c->prm[0].mg_pre), post = std::max(0, c->prm[0].mg_post);
+  const bool half_sm = (l == 0) && c->sinv_half;
   auto smooth = [&](const void *zin, void *zout) {
     if (L->mf && zin)
       return launch(L, KK_PREC, mf_launches(L), [&] {
         return launch_mf(L->dm, L->x32, static_cast<const float *>(zin), L->ycell,
-                         static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const float *>(sm),
+                         static_cast<float *>(zout), static_cast<const float *>(r), static_cast<const __half *>(sm),
                          static_cast<float>(om), 2, act, L->st, L->prm[0].mf_cells);
+      });
+    if (half_sm && !zin)
+      return launch(L, KK_PREC, 1, [&] {
+        return launch_smooth_zero_half(L->dm, static_cast<const __half *>(sm), static_cast<const float *>(r),
+                                       static_cast<float *>(zout), om, act, L->st);
       });
     return launch(L, KK_PREC, 1, [&] { return launch_smooth(L->dm, m, L->vals, sm, r, zin, zout, om, act, L->st); });
   };
@@ -1216,6 +1240,10 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       CKS(dupload(c, &t.g_toff, gt));
       CKS(dupload(c, &t.g_row, grow));
       CKS(dupload(c, &t.g_blk, gb));
+      CKS(dupload(c, &t.g_up, T.g_up));
+      CKS(dupload(c, &t.g_lo, T.g_lo));
+      t.n_up = static_cast<int64_t>(T.g_up.size());
+      t.n_lo = static_cast<int64_t>(T.g_lo.size() / 2);
       if (c->mixed)
         {
           CKS(upload_w<float>(c, &t.p_w, pw));
@@ -1242,8 +1270,12 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
   if (max_nd > 160) return set_error(GLGPU_ERR_ARG, "multigrid: coarsest level too large for the dense solve");
   c->max_nd = max_nd;
   {
+    // the finest level's smoother blocks are read twice per V-cycle (the sweep from zero and
+    // the post-sweep); with the matrix-free operator they are the largest array the cycle
+    // reads there, so mixed mode stores them in FP16
+    c->sinv_half = c->mixed && c->mf && c->B == 18;
     char *si = nullptr;
-    CKS(dalloc(c, &si, tsz(c) * static_cast<size_t>(c->nn) * c->B * c->B));
+    CKS(dalloc(c, &si, (c->sinv_half ? sizeof(__half) : tsz(c)) * static_cast<size_t>(c->nn) * c->B * c->B));
     c->sinv = si;
     char *a = nullptr, *b = nullptr;
     CKS(dalloc(c, &a, tsz(c) * static_cast<size_t>(c->N)));
@@ -1550,6 +1582,7 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   c->rhs_norm.assign(n_inst, 0.0);
   c->res_norm.assign(n_inst, 0.0);
   c->inst_on.assign(n_inst, 1);
+  c->handed.assign(n_inst, 0);
   c->r_ok.assign(n_inst, 0);
   c->stop_ls.assign(n_inst, 0.0);
   c->stop_fp64.assign(n_inst, 0.0);
@@ -1961,6 +1994,7 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
   std::vector<int> nits(n, 0), gits(n, 0);
   std::vector<double> fres(n, 0.0);
   std::fill(c->inst_on.begin(), c->inst_on.end(), 1);
+  std::fill(c->handed.begin(), c->handed.end(), 0);
   glgpu_status result = GLGPU_OK;
   for (int it = 0; it <= max_newton; ++it)
     {
@@ -1969,6 +2003,17 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
       std::vector<int> its;
       bool conv = false;
       CKS(solve_impl(c, linear_tol, its, conv));
+      bool any_on = false;
+      for (int k = 0; k < n; ++k)
+        if (c->inst_on[k] && c->handed[k])
+          {
+            // handed off: keep the state, count the linear iterations spent
+            c->inst_on[k] = 0;
+            gits[k] += its[k];
+          }
+        else
+          any_on |= c->inst_on[k] != 0;
+      if (!any_on) break;
       std::vector<double> r;
       std::vector<int> t;
       CKS(newton_impl(c, r, t));
@@ -2018,6 +2063,10 @@ extern "C" glgpu_status glgpu_run(glgpu_ctx *c, int max_newton, double linear_to
     }
   for (int k = 0; k < n; ++k)
     if (c->inst_on[k]) result = set_error(GLGPU_ERR_NOT_CONVERGED, "run: Newton iteration limit reached");
+  for (int k = 0; k < n; ++k)
+    if (c->handed[k])
+      result = set_error(GLGPU_ERR_NOT_CONVERGED, "run: instance " + std::to_string(k) +
+                                                      " handed off (its multigrid solve stalled)");
   std::fill(c->inst_on.begin(), c->inst_on.end(), 1);
   if (newton_its) std::copy(nits.begin(), nits.end(), newton_its);
   if (gmres_its) std::copy(gits.begin(), gits.end(), gmres_its);
@@ -2172,6 +2221,20 @@ extern "C" glgpu_status glgpu_mem_info(size_t *free_bytes, size_t *total_bytes)
 extern "C" int glgpu_mg_levels(const glgpu_ctx *c) { return c ? c->n_levels : 0; }
 
 extern "C" int64_t glgpu_mg_fallbacks(const glgpu_ctx *c) { return c ? c->mg_fallbacks : 0; }
+
+extern "C" glgpu_status glgpu_set_mg_handoff(glgpu_ctx *c, int on)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_set_mg_handoff: NULL context");
+  c->mg_handoff = on != 0;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_mg_handed_off(const glgpu_ctx *c, uint8_t *flags)
+{
+  if (!c || !flags) return set_error(GLGPU_ERR_ARG, "glgpu_mg_handed_off: NULL argument");
+  std::copy(c->handed.begin(), c->handed.end(), flags);
+  return GLGPU_OK;
+}
 
 extern "C" glgpu_status glgpu_mg_level_info(const glgpu_ctx *c, int level, int64_t *n_nodes, int64_t *nnzb,
                                             int64_t *p_nnz)

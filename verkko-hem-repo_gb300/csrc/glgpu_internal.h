@@ -160,6 +160,10 @@ struct TransferTables
   std::vector<int32_t> pp, pi, rp, ri, g_row, g_blk;
   std::vector<double> pw, rw, g_w;
   std::vector<int64_t> g_toff;
+  // the coarse Jacobian is symmetric (a Galerkin product of the Hessian of a real functional):
+  // only the blocks on or above the block diagonal (column >= row) get Galerkin terms (g_up);
+  // each block below is the transpose of its mirror, g_lo = {block, mirror block} pairs
+  std::vector<int32_t> g_up, g_lo;
 };
 glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
                              const Plan &FP, const Plan &CP, TransferTables &T);

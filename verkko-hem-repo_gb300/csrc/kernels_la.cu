@@ -324,8 +324,8 @@ cudaError_t launch_spmv(const DevMesh &m, bool fp32, const void *vals, const voi
 // (the node's 18 threads read the block's 1296 contiguous bytes)
 constexpr int kSzNodes = 16;
 
-template <typename T>
-__global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, const T *__restrict__ dinv,
+template <typename T, typename DT = T>
+__global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, const DT *__restrict__ dinv,
                                                                  const T *__restrict__ b, T *__restrict__ y, T omega,
                                                                  const uint8_t *__restrict__ act)
 {
@@ -338,10 +338,10 @@ __global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, cons
   b_s[ln][c] = on ? b[n * 18 + c] : T(0);
   __syncthreads();
   if (!on) return;
-  const T *row = dinv + n * 324 + c * 18;
+  const DT *row = dinv + n * 324 + c * 18;
   T u = 0;
 #pragma unroll
-  for (int d = 0; d < 18; ++d) u += row[d] * b_s[ln][d];
+  for (int d = 0; d < 18; ++d) u += mval(row + d) * b_s[ln][d];
   y[n * 18 + c] = omega * u;
 }
 
@@ -364,6 +364,15 @@ static void smooth18_dispatch(const DevMesh &m, const void *vals, const void *di
   m.nn < kTinyRows    ? smooth18_t<T, MT, 8>(m, vals, dinv, b, z, y, omega, act, s)
   : m.nn < kSmallRows ? smooth18_t<T, MT, 4>(m, vals, dinv, b, z, y, omega, act, s)
                       : smooth18_t<T, MT, 1>(m, vals, dinv, b, z, y, omega, act, s);
+}
+
+cudaError_t launch_smooth_zero_half(const DevMesh &m, const __half *dinv, const float *b, float *y, double omega,
+                                    const uint8_t *act, cudaStream_t s)
+{
+  if (m.B != 18) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((m.nn + kSzNodes - 1) / kSzNodes);
+  pdl_launch(k_smooth_zero18<float, __half>, grid, kSzNodes * 18, 0, s, m, dinv, b, y, static_cast<float>(omega), act);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const void *dinv, const void *b, const void *z,
@@ -399,9 +408,10 @@ cudaError_t launch_smooth(const DevMesh &m, bool fp32, const void *vals, const v
 // ---------------------------------------------------------------------------------
 constexpr int kBjWarps = 4;
 
-template <typename T, typename MT = T>
+// OUT: storage of the inverse blocks (FP16 for the finest level's smoother in mixed mode)
+template <typename T, typename MT = T, typename OUT = T>
 __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const MT *__restrict__ vals,
-                                                              T *__restrict__ dinv, int l1)
+                                                              OUT *__restrict__ dinv, int l1)
 {
   pdl_wait();
   pdl_trigger();
@@ -482,11 +492,11 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const M
         }
       __syncwarp();
     }
-  T *out = dinv + n * 324;
+  OUT *out = dinv + n * 324;
   for (int i = lane; i < 324; i += 32)
     {
       const int r = i / 18, c = i % 18;
-      out[i] = singular ? T(r == c ? 1 : 0) : M[warp][r][18 + c];
+      out[i] = static_cast<OUT>(singular ? T(r == c ? 1 : 0) : M[warp][r][18 + c]);
     }
 }
 
@@ -515,6 +525,19 @@ __global__ void k_bj_setup2(DevMesh m, const T *__restrict__ vals, T *__restrict
       o[2] = T(0);
       o[3] = T(1);
     }
+}
+
+cudaError_t launch_bj_setup_half(const DevMesh &m, const void *vals, __half *dinv, cudaStream_t s)
+{
+  if (m.B != 18) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((m.nn + kBjWarps - 1) / kBjWarps);
+  if (m.half_vals)
+    pdl_launch(k_bj_setup18<float, __half, __half>, grid, kBjWarps * 32, 0, s, m, static_cast<const __half *>(vals),
+               dinv, 1);
+  else
+    pdl_launch(k_bj_setup18<float, float, __half>, grid, kBjWarps * 32, 0, s, m, static_cast<const float *>(vals), dinv,
+               1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_bj_setup(const DevMesh &m, bool fp32, const void *vals, void *dinv, cudaStream_t s, bool l1)

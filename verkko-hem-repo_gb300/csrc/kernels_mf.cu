@@ -402,54 +402,60 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
 #pragma unroll
       for (int k = 0; k < 6; ++k) S.bulk[tid][k] = bk[k];
     }
-  // nodal values: the 16 threads of cell cl = tid / 16 take its 144 (vertex, component)
-  // entries e = lt + 16 k, k < 9 (lt = tid % 16); node ids, then values and masks are
-  // requested together.  Constraint rows (hanging nodes, periodic images) are expanded from
-  // their parents only on meshes that have them.
+  // nodal values: the 16 threads of cell cl = tid / 16 take its vertices two per vertex;
+  // half h of vertex a loads the float2 pairs j0 = 5 h .. 4 + 4 h of the vertex's 18 values
+  // (a row is 72 bytes, 8-byte aligned) and the vertex's component mask once.  Constraint
+  // rows (hanging nodes, periodic images) are expanded from their parents only on meshes
+  // that have them.
   {
-    constexpr int kPer = 9;
     static_assert(kMThreads == 16 * kMCells, "16 threads per cell");
-    const int cl = tid >> 4, lt = tid & 15;
-    const bool cell_ok = cl < ncb;
-    const int32_t *cn = m.cells + (e0 + cl) * 8;
-    int node[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k) node[k] = cell_ok ? cn[(lt + 16 * k) / 18] : -1;
-    float zv[kPer], xv[kPer];
-    uint32_t mk[kPer];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k)
+    const int cl = tid >> 4, a = (tid & 15) >> 1, h = tid & 1;
+    const int j0 = 5 * h, nj = 5 - h;
+    const int node = (cl < ncb) ? m.cells[(e0 + cl) * 8 + a] : -1;
+    float2 zv[5], xv[5];
+    uint32_t mk = ~0u;
+    if (node >= 0)
       {
-        const int c = (lt + 16 * k) % 18;
-        const bool ok = node[k] >= 0;
-        const int64_t b = ok ? static_cast<int64_t>(node[k]) * 18 + c : 0;
-        zv[k] = ok ? z[b] : 0.f;
-        xv[k] = ok ? xs[b] : 0.f;
-        mk[k] = ok ? m.mask[node[k]] : ~0u;
-      }
-    float *zs = &S.u.g.zs[cl][0][0], *xsh = &S.u.g.xs[cl][0][0];
+        const float2 *zr = reinterpret_cast<const float2 *>(z + static_cast<int64_t>(node) * 18) + j0;
+        const float2 *xr = reinterpret_cast<const float2 *>(xs + static_cast<int64_t>(node) * 18) + j0;
 #pragma unroll
-    for (int k = 0; k < kPer; ++k)
-      {
-        const int e = lt + 16 * k, c = e % 18;
-        float val = ((mk[k] >> c) & 1u) ? 0.f : zv[k];
-        if (m.has_constraints && node[k] >= 0)
-          {
-            const int h0 = m.hptr[node[k]], h1 = m.hptr[node[k] + 1];
-            if (h1 > h0)
-              {
-                val = 0.f;
-                for (int j = h0; j < h1; ++j)
-                  {
-                    const int par = m.hpar[j]; // a parent's zero-Dirichlet components do not enter
-                    if (!((m.mask[par] >> c) & 1u))
-                      val += static_cast<float>(m.hw[j]) * z[static_cast<int64_t>(par) * 18 + c];
-                  }
-              }
-          }
-        zs[e] = val;
-        xsh[e] = xv[k]; // the state is stored distributed: vertex values as they are
+        for (int q = 0; q < 5; ++q)
+          if (q < nj)
+            {
+              zv[q] = zr[q];
+              xv[q] = xr[q];
+            }
+        mk = m.mask[node];
       }
+    else
+#pragma unroll
+      for (int q = 0; q < 5; ++q) zv[q] = xv[q] = make_float2(0.f, 0.f);
+    const bool hang = m.has_constraints && node >= 0 && m.hptr[node + 1] > m.hptr[node];
+    float2 *zs2 = reinterpret_cast<float2 *>(&S.u.g.zs[cl][a][0]) + j0;
+    float2 *xs2 = reinterpret_cast<float2 *>(&S.u.g.xs[cl][a][0]) + j0;
+#pragma unroll
+    for (int q = 0; q < 5; ++q)
+      if (q < nj)
+        {
+          const int c = 2 * (j0 + q);
+          float2 val = make_float2(((mk >> c) & 1u) ? 0.f : zv[q].x, ((mk >> (c + 1)) & 1u) ? 0.f : zv[q].y);
+          if (hang)
+            {
+              val = make_float2(0.f, 0.f);
+              for (int k = m.hptr[node]; k < m.hptr[node + 1]; ++k)
+                {
+                  // a parent's zero-Dirichlet components do not enter
+                  const int par = m.hpar[k];
+                  const uint32_t pm = m.mask[par];
+                  const float w = static_cast<float>(m.hw[k]);
+                  const float2 pv = reinterpret_cast<const float2 *>(z + static_cast<int64_t>(par) * 18)[j0 + q];
+                  if (!((pm >> c) & 1u)) val.x += w * pv.x;
+                  if (!((pm >> (c + 1)) & 1u)) val.y += w * pv.y;
+                }
+            }
+          zs2[q] = val;
+          xs2[q] = xv[q]; // the state is stored distributed: vertex values as they are
+        }
   }
   __syncthreads();
   // A, Z and dZ/dx at the points: thread (cell, component pair)
@@ -620,7 +626,7 @@ constexpr int kMgThreads = kMgNodes * 18;
 
 __global__ void __launch_bounds__(kMgThreads, 5) k_mf_gather(DevMesh m, const float *__restrict__ ycell,
                                                           const float *__restrict__ z, const float *__restrict__ b,
-                                                          const float *__restrict__ dinv, float *__restrict__ y,
+                                                          const __half *__restrict__ dinv, float *__restrict__ y,
                                                           float omega, int mode, const uint8_t *__restrict__ act)
 {
   pdl_wait();
@@ -675,10 +681,16 @@ __global__ void __launch_bounds__(kMgThreads, 5) k_mf_gather(DevMesh m, const fl
   t_s[ln][c] = t;
   __syncthreads();
   if (!on) return;
-  const float *row = dinv + n * 324 + c * 18;
+  // the row's 18 FP16 entries: 36 bytes at a 4-byte boundary, nine half2 loads
+  const __half2 *row = reinterpret_cast<const __half2 *>(dinv + n * 324 + c * 18);
   float u = 0.f;
 #pragma unroll
-  for (int d = 0; d < 18; ++d) u = fmaf(__ldg(row + d), t_s[ln][d], u);
+  for (int d = 0; d < 9; ++d)
+    {
+      const float2 w = __half22float2(__ldg(row + d));
+      u = fmaf(w.x, t_s[ln][2 * d], u);
+      u = fmaf(w.y, t_s[ln][2 * d + 1], u);
+    }
   y[n * 18 + c] = z[n * 18 + c] + omega * u;
 }
 
@@ -750,7 +762,7 @@ static cudaError_t launch_mf_cell(const DevMesh &m, const float *xs, const float
 }
 
 cudaError_t launch_mf(const DevMesh &m, const float *xs, const float *z, float *ycell, float *y, const float *b,
-                      const float *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
+                      const __half *dinv, float omega, int mode, const uint8_t *act, cudaStream_t s,
                       int cells_per_cta)
 {
   if (m.dim != 3 || m.B != 18 || m.nv != 8) return cudaErrorInvalidValue;

@@ -160,10 +160,11 @@ __device__ __forceinline__ void gstore(__half *blk, int ch, const float4 &v)
 // levels of a mixed context, summed in FP32)
 template <typename T, typename IN, typename OUT>
 __global__ void __launch_bounds__(kGalWarps * 32)
-  k_galerkin(int64_t nnzb_c, const int32_t *__restrict__ g_row, const int32_t *__restrict__ cols_c,
-             const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ hptr_c, OUT *__restrict__ vals_c,
-             const int64_t *__restrict__ g_toff, const int32_t *__restrict__ g_blk, const T *__restrict__ g_w,
-             const IN *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
+  k_galerkin(int64_t n_up, const int32_t *__restrict__ up, const int32_t *__restrict__ g_row,
+             const int32_t *__restrict__ cols_c, const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ hptr_c,
+             OUT *__restrict__ vals_c, const int64_t *__restrict__ g_toff, const int32_t *__restrict__ g_blk,
+             const T *__restrict__ g_w, const IN *__restrict__ vals_f, const int32_t *__restrict__ node_inst_c,
+             const uint8_t *__restrict__ act)
 {
   pdl_wait();
   pdl_trigger();
@@ -172,8 +173,9 @@ __global__ void __launch_bounds__(kGalWarps * 32)
   constexpr int NCH = 324 / NV;
   constexpr int NIT = (NCH + 31) / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t cb = static_cast<int64_t>(blockIdx.x) * kGalWarps + warp;
-  if (cb >= nnzb_c) return;
+  const int64_t u = static_cast<int64_t>(blockIdx.x) * kGalWarps + warp;
+  if (u >= n_up) return;
+  const int64_t cb = up[u];
   const int32_t I = g_row[cb];
   if (act && !act[node_inst_c[I]]) return;
   V acc[NIT];
@@ -215,6 +217,28 @@ __global__ void __launch_bounds__(kGalWarps * 32)
             if (((mI >> a) & 1u) || ((mJ >> bb) & 1u)) gcomp(o, q) = (J == I && a == bb) ? T(1) : T(0);
           }
       gstore(dst, ch, o);
+    }
+}
+
+// the blocks below the diagonal: block lo[2 i] = transpose of block lo[2 i + 1], warp per block
+template <typename OUT>
+__global__ void __launch_bounds__(kGalWarps * 32)
+  k_galerkin_mirror(int64_t n_lo, const int32_t *__restrict__ lo, const int32_t *__restrict__ g_row,
+                    OUT *__restrict__ vals_c, const int32_t *__restrict__ node_inst_c, const uint8_t *__restrict__ act)
+{
+  pdl_wait();
+  pdl_trigger();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * kGalWarps + warp;
+  if (i >= n_lo) return;
+  const int64_t dst = lo[2 * i], src = lo[2 * i + 1];
+  if (act && !act[node_inst_c[g_row[dst]]]) return;
+  const OUT *s = vals_c + src * 324;
+  OUT *d = vals_c + dst * 324;
+  for (int e = lane; e < 324; e += 32)
+    {
+      const int a = e / 18, b = e - 18 * (e / 18);
+      d[e] = s[b * 18 + a];
     }
 }
 
@@ -270,38 +294,46 @@ cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_galerkin(bool fp32, int64_t nnzb_c, const int32_t *g_row, const int32_t *cols_c,
-                            const uint32_t *mask_c, const int32_t *hptr_c, void *vals_c, const int64_t *g_toff,
-                            const int32_t *g_blk, const void *g_w, const void *vals_f, const int32_t *node_inst_c,
-                            const uint8_t *act, cudaStream_t s, bool half_in, bool half_out)
+cudaError_t launch_galerkin(bool fp32, int64_t n_up, const int32_t *up, int64_t n_lo, const int32_t *lo,
+                            const int32_t *g_row, const int32_t *cols_c, const uint32_t *mask_c, const int32_t *hptr_c,
+                            void *vals_c, const int64_t *g_toff, const int32_t *g_blk, const void *g_w,
+                            const void *vals_f, const int32_t *node_inst_c, const uint8_t *act, cudaStream_t s,
+                            bool half_in, bool half_out)
 {
-  if (nnzb_c == 0) return cudaSuccess;
-  const int64_t grid = (nnzb_c + kGalWarps - 1) / kGalWarps;
-  if (grid > 0x7fffffff) return cudaErrorInvalidValue;
-  const unsigned g = static_cast<unsigned>(grid);
+  if (n_up == 0) return cudaSuccess;
+  const int64_t grid = (n_up + kGalWarps - 1) / kGalWarps, grid_lo = (n_lo + kGalWarps - 1) / kGalWarps;
+  if (grid > 0x7fffffff || grid_lo > 0x7fffffff) return cudaErrorInvalidValue;
+  const unsigned g = static_cast<unsigned>(grid), gl = static_cast<unsigned>(grid_lo);
   const float *wf = static_cast<const float *>(g_w);
   if (fp32 && half_in && half_out)
-    pdl_launch(k_galerkin<float, __half, __half>, g, kGalWarps * 32, 0, s, 
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
-      static_cast<const __half *>(vals_f), node_inst_c, act);
+    pdl_launch(k_galerkin<float, __half, __half>, g, kGalWarps * 32, 0, s, n_up, up, g_row, cols_c, mask_c, hptr_c,
+               static_cast<__half *>(vals_c), g_toff, g_blk, wf, static_cast<const __half *>(vals_f), node_inst_c, act);
   else if (fp32 && half_out)
-    pdl_launch(k_galerkin<float, float, __half>, g, kGalWarps * 32, 0, s, 
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<__half *>(vals_c), g_toff, g_blk, wf,
-      static_cast<const float *>(vals_f), node_inst_c, act);
+    pdl_launch(k_galerkin<float, float, __half>, g, kGalWarps * 32, 0, s, n_up, up, g_row, cols_c, mask_c, hptr_c,
+               static_cast<__half *>(vals_c), g_toff, g_blk, wf, static_cast<const float *>(vals_f), node_inst_c, act);
   else if (fp32 && half_in)
-    pdl_launch(k_galerkin<float, __half, float>, g, kGalWarps * 32, 0, s, 
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
-      static_cast<const __half *>(vals_f), node_inst_c, act);
+    pdl_launch(k_galerkin<float, __half, float>, g, kGalWarps * 32, 0, s, n_up, up, g_row, cols_c, mask_c, hptr_c,
+               static_cast<float *>(vals_c), g_toff, g_blk, wf, static_cast<const __half *>(vals_f), node_inst_c, act);
   else if (fp32)
-    pdl_launch(k_galerkin<float, float, float>, g, kGalWarps * 32, 0, s, 
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<float *>(vals_c), g_toff, g_blk, wf,
-      static_cast<const float *>(vals_f), node_inst_c, act);
+    pdl_launch(k_galerkin<float, float, float>, g, kGalWarps * 32, 0, s, n_up, up, g_row, cols_c, mask_c, hptr_c,
+               static_cast<float *>(vals_c), g_toff, g_blk, wf, static_cast<const float *>(vals_f), node_inst_c, act);
   else if (!fp32 && !half_in && !half_out)
-    pdl_launch(k_galerkin<double, double, double>, g, kGalWarps * 32, 0, s, 
-      nnzb_c, g_row, cols_c, mask_c, hptr_c, static_cast<double *>(vals_c), g_toff, g_blk,
-      static_cast<const double *>(g_w), static_cast<const double *>(vals_f), node_inst_c, act);
+    pdl_launch(k_galerkin<double, double, double>, g, kGalWarps * 32, 0, s, n_up, up, g_row, cols_c, mask_c, hptr_c,
+               static_cast<double *>(vals_c), g_toff, g_blk, static_cast<const double *>(g_w),
+               static_cast<const double *>(vals_f), node_inst_c, act);
   else
     return cudaErrorInvalidValue;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || n_lo == 0) return e;
+  if (fp32 && half_out)
+    pdl_launch(k_galerkin_mirror<__half>, gl, kGalWarps * 32, 0, s, n_lo, lo, g_row, static_cast<__half *>(vals_c),
+               node_inst_c, act);
+  else if (fp32)
+    pdl_launch(k_galerkin_mirror<float>, gl, kGalWarps * 32, 0, s, n_lo, lo, g_row, static_cast<float *>(vals_c),
+               node_inst_c, act);
+  else
+    pdl_launch(k_galerkin_mirror<double>, gl, kGalWarps * 32, 0, s, n_lo, lo, g_row, static_cast<double *>(vals_c),
+               node_inst_c, act);
   return cudaGetLastError();
 }
 

@@ -561,9 +561,11 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   // Galerkin terms, grouped by coarse block: every (restriction entry i of row I, fine block
   // (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to block (I, J); within a
   // block the terms follow (restriction entry, fine block, prolongation entry) order, so fine
-  // blocks come in increasing order.  Pass 0 counts the terms of every block, pass 1 writes
-  // them at their offsets; both run over the coarse rows on all host threads (a row's blocks
-  // belong to one thread), and the tables do not depend on the thread count.
+  // blocks come in increasing order.  Only blocks with J >= I get terms: the blocks below
+  // the diagonal are the transposes of their mirrors.  Pass 0 counts the terms of every
+  // block, pass 1 writes them at their offsets; both run over the coarse rows on all host
+  // threads (a row's blocks belong to one thread), and the tables do not depend on the
+  // thread count.
   std::vector<int64_t> &gt = T.g_toff;
   std::vector<int32_t> &grow = T.g_row, &gb = T.g_blk;
   std::vector<double> &gw = T.g_w;
@@ -607,6 +609,7 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
                             outside = 1;
                             continue;
                           }
+                        if (c0[sl] < I) continue; // below the diagonal: a mirror
                         if (pass == 0)
                           ++gt[b0 + sl + 1];
                         else
@@ -627,6 +630,25 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
       }
       if (outside) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
     }
+  std::vector<int32_t> &up = T.g_up, &lo = T.g_lo;
+  up.clear();
+  lo.clear();
+  for (int64_t I = 0; I < ncr; ++I)
+    for (int32_t b = CP.rowptr[I]; b < CP.rowptr[I + 1]; ++b)
+      {
+        const int32_t J = CP.cols[b];
+        if (J >= I)
+          {
+            up.push_back(b);
+            continue;
+          }
+        int32_t m = -1;
+        for (int32_t e = CP.rowptr[J]; e < CP.rowptr[J + 1]; ++e)
+          if (CP.cols[e] == I) m = e;
+        if (m < 0) return set_error(GLGPU_ERR_ARG, "multigrid: the coarse pattern is not symmetric");
+        lo.push_back(b);
+        lo.push_back(m);
+      }
   return GLGPU_OK;
 }
 

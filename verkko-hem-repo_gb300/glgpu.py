@@ -99,6 +99,8 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mg_levels.argtypes = [vp]
     L.glgpu_mg_fallbacks.argtypes = [vp]
     L.glgpu_mg_fallbacks.restype = ctypes.c_int64
+    L.glgpu_set_mg_handoff.argtypes = [vp, ctypes.c_int]
+    L.glgpu_mg_handed_off.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8)]
     L.glgpu_mg_level_info.argtypes = [vp, ctypes.c_int, _lp, _lp, _lp]
     L.glgpu_mg_level_system.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
     L.glgpu_mg_prolongation.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
@@ -649,6 +651,19 @@ class FemGL:
     @property
     def mg_fallbacks(self) -> int:
         return int(lib().glgpu_mg_fallbacks(self._ctx))
+
+    def set_mg_handoff(self, on: bool = True) -> None:
+        """Instances whose multigrid solve stalls twice stop at the state they reached in
+        `run` (flagged in `handed_off`, reported unconverged) instead of finishing with
+        block-Jacobi GMRES in this context."""
+        _check(lib().glgpu_set_mg_handoff(self._ctx, int(bool(on))))
+
+    @property
+    def handed_off(self) -> np.ndarray:
+        """Per instance: handed off in the last `run`."""
+        flags = np.zeros(self.n_inst, np.uint8)
+        _check(lib().glgpu_mg_handed_off(self._ctx, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return flags.astype(bool)
 
     def sync(self) -> None:
         _check(lib().glgpu_sync(self._ctx))

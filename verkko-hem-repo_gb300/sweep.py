@@ -15,6 +15,7 @@ tolerance.
 
 The reference solves one configuration per program run (femgl/src/run.cc:157-258); the sweep
 is the batched form of running it over many (T, p, thickness) points."""
+import dataclasses
 import time
 from typing import Sequence
 
@@ -60,18 +61,55 @@ def footprint(gl, meshes, params):
     return slope, const
 
 
+def finish_instance(gl, mesh, prm, x, *, max_newton: int = 40, linear_tol: float = 1e-4,
+                    converge_acc: float = 1e-10) -> dict:
+    """Finish one instance that a batched context handed off (its multigrid solve stalled twice)
+    in a context of its own, from the state x it reached: first the same method with two pre-
+    and two post-sweeps per level (handoff on again), then the same in FP64 (where a stall
+    still finishes with block-Jacobi GMRES).  Returns newton_its, gmres_its, residual, free_energy, converged,
+    solve_ms (device time), create_s, stage (the step that finished it) and x."""
+    strong = {"mg_pre": max(2, int(prm.mg_pre)), "mg_post": max(2, int(prm.mg_post))}
+    stages = [strong, dict(strong, precision=gl.FP64)]
+    r = {"newton_its": 0, "gmres_its": 0, "solve_ms": 0.0, "create_s": 0.0}
+    for k, change in enumerate(stages):
+        last = k == len(stages) - 1
+        t0 = time.perf_counter()
+        with gl.FemGL(mesh, dataclasses.replace(prm, **change)) as g:
+            r["create_s"] += time.perf_counter() - t0
+            if not last:
+                g.set_mg_handoff(True)
+            g.set_solution(np.asarray(x, np.float64))
+            g.sync()
+            g.event_start()
+            out = g.run(max_newton=max_newton, linear_tol=linear_tol, converge_acc=converge_acc,
+                        allow_unconverged=True)
+            r["solve_ms"] += g.event_stop()
+            r["newton_its"] += int(out["newton_its"][0])
+            r["gmres_its"] += int(out["gmres_its"][0])
+            x = g.solution()
+            if not last and bool(g.handed_off[0]):
+                continue
+            r.update({"residual": float(out["residual"][0]), "free_energy": float(g.free_energy()[0]),
+                      "converged": bool(out["residual"][0] <= converge_acc), "stage": k, "x": x})
+            return r
+    raise AssertionError("unreachable")
+
+
 def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: float = 1e-4,
                 converge_acc: float = 1e-10, budget: float | None = None, margin: float = 1.1,
-                keep_solutions: bool = False, log=None) -> dict:
+                keep_solutions: bool = False, handoff: bool = True, log=None) -> dict:
     """Solve every instance (meshes[k], params[k], start x0[k]) to converge_acc, in waves.
 
     budget: device bytes a wave may take (default: 90 % of the free memory less 2 GiB).
     Returns per-instance arrays in input order (newton_its, gmres_its, residual,
-    free_energy, converged, wave) and per-wave timing: create_s (host plan, hierarchy and
-    device setup), solve_ms (device time of the Newton solve, CUDA events), mg_fallbacks
-    (multigrid solves of the wave handed to block-Jacobi, a context-wide switch).  With
-    keep_solutions the converged states come back as a list of arrays; log, when given, is
-    called with one line per finished wave."""
+    free_energy, converged, wave, handed_off) and per-wave timing: create_s (host plan,
+    hierarchy and device setup), solve_ms (device time of the Newton solves, CUDA events),
+    mg_fallbacks (multigrid solves of the wave finished with block-Jacobi).  With handoff (the
+    default) an instance of a multi-instance wave whose multigrid solve stalls twice leaves the
+    wave at the state it reached and is finished in a context of its own (finish_instance);
+    its device time counts in its wave's solve_ms and in handoff_ms.  With keep_solutions the
+    converged states come back as a list of arrays; log, when given, is called with one line
+    per finished wave."""
     n = len(meshes)
     if not (len(params) == n and len(x0) == n):
         raise ValueError("meshes, params and x0 must have one entry per instance")
@@ -82,15 +120,19 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
         budget = 0.9 * free - 2.0 * 2**30
     waves = plan_waves(sizes, per_node * margin, budget, per_inst * margin)
     res = {"newton_its": np.zeros(n, np.int32), "gmres_its": np.zeros(n, np.int32), "residual": np.zeros(n),
-           "free_energy": np.zeros(n), "converged": np.zeros(n, bool), "wave": np.zeros(n, np.int32)}
+           "free_energy": np.zeros(n), "converged": np.zeros(n, bool), "wave": np.zeros(n, np.int32),
+           "handed_off": np.zeros(n, bool)}
     sols = [None] * n if keep_solutions else None
-    create_s, solve_ms, wave_bytes, fallbacks = [], [], [], []
+    create_s, solve_ms, wave_bytes, fallbacks, handoff_ms = [], [], [], [], []
     for wi, w in enumerate(waves):
         t0 = time.perf_counter()
         f = gl.FemGL([meshes[i] for i in w], [params[i] for i in w])
+        hand = handoff and len(w) > 1
         try:
             create_s.append(time.perf_counter() - t0)
             wave_bytes.append(f.device_bytes)
+            if hand:
+                f.set_mg_handoff(True)
             f.set_solution(np.concatenate([np.asarray(x0[i], np.float64) for i in w]))
             f.sync()
             f.event_start()
@@ -99,13 +141,12 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
             solve_ms.append(f.event_stop())
             F = f.free_energy()
             fallbacks.append(f.mg_fallbacks)
-            x = f.solution() if keep_solutions else None
+            handed = f.handed_off if hand else np.zeros(len(w), bool)
+            x = f.solution() if (keep_solutions or handed.any()) else None
         finally:
             f.close()
-        if log is not None:
-            log(f"wave {wi}: {len(w)} instances, {sum(sizes[i] for i in w)} nodes, "
-                f"{wave_bytes[-1] / 2**30:.1f} GiB, create {create_s[-1]:.1f} s, solve {solve_ms[-1]:.0f} ms")
         off = 0
+        hand_ms = 0.0
         for j, i in enumerate(w):
             res["newton_its"][i] = out["newton_its"][j]
             res["gmres_its"][i] = out["gmres_its"][j]
@@ -113,12 +154,31 @@ def solve_sweep(gl, meshes, params, x0, *, max_newton: int = 40, linear_tol: flo
             res["free_energy"][i] = F[j]
             res["converged"][i] = out["residual"][j] <= converge_acc
             res["wave"][i] = wi
+            xi = x[off:off + 18 * sizes[i]].copy() if x is not None else None
+            if handed[j]:
+                fin = finish_instance(gl, meshes[i], params[i], xi, max_newton=max_newton, linear_tol=linear_tol,
+                                      converge_acc=converge_acc)
+                res["newton_its"][i] += fin["newton_its"]
+                res["gmres_its"][i] += fin["gmres_its"]
+                res["residual"][i] = fin["residual"]
+                res["free_energy"][i] = fin["free_energy"]
+                res["converged"][i] = fin["converged"]
+                res["handed_off"][i] = True
+                hand_ms += fin["solve_ms"]
+                create_s[-1] += fin["create_s"]
+                xi = fin["x"]
             if keep_solutions:
-                sols[i] = x[off:off + 18 * sizes[i]].copy()
+                sols[i] = xi
             off += 18 * sizes[i]
+        solve_ms[-1] += hand_ms
+        handoff_ms.append(hand_ms)
+        if log is not None:
+            log(f"wave {wi}: {len(w)} instances, {sum(sizes[i] for i in w)} nodes, "
+                f"{wave_bytes[-1] / 2**30:.1f} GiB, create {create_s[-1]:.1f} s, solve {solve_ms[-1]:.0f} ms"
+                f" ({int(handed.sum())} handed off: {hand_ms:.0f} ms)")
     res.update({"waves": [len(w) for w in waves], "create_s": create_s, "solve_ms": solve_ms,
-                "wave_bytes": wave_bytes, "mg_fallbacks": fallbacks, "bytes_per_node": per_node,
-                "bytes_per_instance": per_inst, "budget": budget})
+                "handoff_ms": handoff_ms, "wave_bytes": wave_bytes, "mg_fallbacks": fallbacks,
+                "bytes_per_node": per_node, "bytes_per_instance": per_inst, "budget": budget})
     if keep_solutions:
         res["solutions"] = sols
     return res
