@@ -280,6 +280,11 @@ glgpu_status glgpu_set_mg_handoff(glgpu_ctx *ctx, int on);
 /* flags[k] = 1 when instance k was handed off in the last glgpu_run, else 0 (n_inst bytes). */
 glgpu_status glgpu_mg_handed_off(const glgpu_ctx *ctx, uint8_t *flags);
 
+/* GMRES orthogonalization: classical Gram-Schmidt with one reorthogonalization (on, the
+ * default: three passes over the basis per iteration) or with one projection (off: two
+ * passes).  The true residual is checked after every restart cycle either way. */
+glgpu_status glgpu_set_reorthogonalization(glgpu_ctx *ctx, int on);
+
 /* Sizes of coarse level `level` (1 = first coarse level .. glgpu_mg_levels): its node
  * count, block count, and the entries of the prolongation from it to level - 1. */
 glgpu_status glgpu_mg_level_info(const glgpu_ctx *ctx, int level, int64_t *n_nodes, int64_t *nnzb, int64_t *p_nnz);

@@ -351,3 +351,23 @@ def test_stalled_instance_handed_off_and_finished(gl):
         h.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
         F64 = float(h.free_energy()[0])
     assert abs(r["free_energy"][0] - F64) <= 1e-9 * abs(F64)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_one_projection_gram_schmidt(gl, precision):
+    """GMRES with one Gram-Schmidt projection per iteration (no reorthogonalization) reaches
+    the same converged state and free energy, with iteration counts close to the default."""
+    m = gl.cube_mesh(5.0, 12)
+    x0 = gl.bphase_guess(20.0, 0.6, m.nn, noise=0.05, seed=5)
+    prm = gl.Params.from_matep(20.0, 0.6, precision=precision, precond=gl.PC_MULTIGRID)
+    res = {}
+    for reorth in (True, False):
+        with gl.FemGL(m, prm) as f:
+            f.set_reorthogonalization(reorth)
+            f.set_solution(x0)
+            o = f.run(max_newton=40, linear_tol=1e-4, converge_acc=1e-10)
+            res[reorth] = (o, f.free_energy()[0])
+    (o1, F1), (o0, F0) = res[True], res[False]
+    assert o1["converged"] and o0["converged"]
+    assert abs(F0 - F1) <= 1e-12 * abs(F1)
+    assert abs(int(o0["gmres_its"][0]) - int(o1["gmres_its"][0])) <= 2 + 0.2 * int(o1["gmres_its"][0])

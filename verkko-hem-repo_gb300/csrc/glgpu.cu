@@ -183,6 +183,7 @@ struct glgpu_ctx
   // instances whose multigrid solve stalled twice stop where they are instead of finishing
   // with block-Jacobi in this context (mg_handoff); the caller finishes them elsewhere
   bool mg_handoff = false;
+  bool reorth = true;                // Gram-Schmidt with one reorthogonalization (else one projection)
   std::vector<uint8_t> handed;       // per instance, set during the last glgpu_run
 };
 
@@ -693,12 +694,21 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
                 return launch_arnoldi_dot(c->dm, m32, c->V, N, j + 1, Vj1, c->partial, c->g.hcol, mr + 2, c->d_cnt,
                                           c->g.active, c->st);
               }));
-              CKS(launch(c, KK_VEC, 1, [&] {
-                return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 1, j, c->partial, c->g, c->d_cnt, c->st);
-              }));
-              CKS(launch(c, KK_VEC, 1, [&] {
-                return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 2, j, c->partial, c->g, c->d_cnt, c->st);
-              }));
+              if (c->reorth)
+                {
+                  CKS(launch(c, KK_VEC, 1, [&] {
+                    return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 1, j, c->partial, c->g, c->d_cnt,
+                                                 c->st);
+                  }));
+                  CKS(launch(c, KK_VEC, 1, [&] {
+                    return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 2, j, c->partial, c->g, c->d_cnt,
+                                                 c->st);
+                  }));
+                }
+              else
+                CKS(launch(c, KK_VEC, 1, [&] {
+                  return launch_arnoldi_update(c->dm, m32, c->V, N, j + 1, Vj1, 3, j, c->partial, c->g, c->d_cnt, c->st);
+                }));
               if (mg)
                 {
                   Axpby k{};
@@ -2226,6 +2236,13 @@ extern "C" glgpu_status glgpu_set_mg_handoff(glgpu_ctx *c, int on)
 {
   if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_set_mg_handoff: NULL context");
   c->mg_handoff = on != 0;
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_set_reorthogonalization(glgpu_ctx *c, int on)
+{
+  if (!c) return set_error(GLGPU_ERR_ARG, "glgpu_set_reorthogonalization: NULL context");
+  c->reorth = on != 0;
   return GLGPU_OK;
 }
 

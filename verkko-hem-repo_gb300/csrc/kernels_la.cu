@@ -1234,14 +1234,15 @@ __global__ void __launch_bounds__(kSegThreads) k_arnoldi_dot(DevMesh m, const T 
     }
 }
 
-// Givens update of column j for one instance (same arithmetic as k_gmres_column)
-__device__ void givens_column(GmresDev &g, int k, int j)
+// Givens update of column j for one instance (same arithmetic as k_gmres_column); with
+// reorth the column is the sum of both Gram-Schmidt projections
+__device__ void givens_column(GmresDev &g, int k, int j, bool reorth = true)
 {
   const int m = g.m;
   double *h = g.hcol + k * (m + 2);
   const double *h2 = g.hcol2 + k * (m + 2);
   double col[64 + 2];
-  for (int i = 0; i <= j; ++i) col[i] = h[i] + h2[i];
+  for (int i = 0; i <= j; ++i) col[i] = reorth ? h[i] + h2[i] : h[i];
   col[j + 1] = h[j + 1];
   double *cs = g.cs + k * m, *sn = g.sn + k * m, *gg = g.g + k * (m + 1);
   for (int i = 0; i < j; ++i)
@@ -1276,6 +1277,7 @@ __device__ void givens_column(GmresDev &g, int k, int j)
 // w -= V h (h = hcol or hcol2 of the instance); then
 //   mode 1: hcol2 = V^T w                     (second Gram-Schmidt projection)
 //   mode 2: hcol[j+1] = |w|, then the Givens update of column j
+//   mode 3: as mode 2 with h = hcol: one projection, no reorthogonalization
 template <typename T>
 __global__ void __launch_bounds__(kSegThreads) k_arnoldi_update(DevMesh m, const T *__restrict__ X, int64_t ld,
                                                                 int nvec, T *__restrict__ w, int mode, int j,
@@ -1290,7 +1292,7 @@ __global__ void __launch_bounds__(kSegThreads) k_arnoldi_update(DevMesh m, const
   const int inst = m.seg_inst[s];
   if (!g.active[inst]) return;
   const int mr = g.m;
-  const double *h = (mode == 1 ? g.hcol : g.hcol2) + inst * (mr + 2);
+  const double *h = (mode == 2 ? g.hcol2 : g.hcol) + inst * (mr + 2);
   for (int v = threadIdx.x; v < nvec; v += kSegThreads) cf[v] = static_cast<T>(__ldcg(h + v));
   __syncthreads();
   const int64_t b = m.seg_begin[s];
@@ -1357,10 +1359,10 @@ __global__ void __launch_bounds__(kSegThreads) k_arnoldi_update(DevMesh m, const
       if (threadIdx.x == 0)
         {
           cnt[inst] = 0u;
-          if (mode == 2)
+          if (mode >= 2)
             {
               __threadfence();
-              givens_column(g, inst, j);
+              givens_column(g, inst, j, mode == 2);
             }
         }
     }

@@ -101,6 +101,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mg_fallbacks.restype = ctypes.c_int64
     L.glgpu_set_mg_handoff.argtypes = [vp, ctypes.c_int]
     L.glgpu_mg_handed_off.argtypes = [vp, ctypes.POINTER(ctypes.c_uint8)]
+    L.glgpu_set_reorthogonalization.argtypes = [vp, ctypes.c_int]
     L.glgpu_mg_level_info.argtypes = [vp, ctypes.c_int, _lp, _lp, _lp]
     L.glgpu_mg_level_system.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
     L.glgpu_mg_prolongation.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
@@ -657,6 +658,10 @@ class FemGL:
         `run` (flagged in `handed_off`, reported unconverged) instead of finishing with
         block-Jacobi GMRES in this context."""
         _check(lib().glgpu_set_mg_handoff(self._ctx, int(bool(on))))
+
+    def set_reorthogonalization(self, on: bool = True) -> None:
+        """GMRES Gram-Schmidt with one reorthogonalization (default) or one projection."""
+        _check(lib().glgpu_set_reorthogonalization(self._ctx, int(bool(on))))
 
     @property
     def handed_off(self) -> np.ndarray:
