@@ -554,9 +554,10 @@ def main():
     # the V-cycle's tail (levels of at most 160 nodes and the dense solve) as one cluster launch
     tail = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
                      precond=pc, cfg=head_cfg, mg_small_fuse=2)
-    # GMRES with one Gram-Schmidt projection instead of two (one pass over the basis less)
-    cgs1 = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
-                     precond=pc, cfg=head_cfg, prepare=lambda f: f.set_reorthogonalization(False))
+    # GMRES with a reorthogonalized Gram-Schmidt (one more pass over the basis) beside the
+    # default single projection
+    cgs2 = time_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps // 2), 1, args.linear_tol, flush=flush,
+                     precond=pc, cfg=head_cfg, prepare=lambda f: f.set_reorthogonalization(True))
     e2e_val, x_e2e = e2e_mode(gl, m, head_x0, gl.MIXED, max(1, args.steps), args.linear_tol, precond=pc, cfg=head_cfg)
     batched = batched_leg(gl, args.batch, args.linear_tol, sur, precond=pc, cfg=head_cfg) if args.batch > 0 else None
 
@@ -625,12 +626,12 @@ def main():
         "mg_fallbacks": mixed["mg"]["fallbacks"],
         "launch_mode": {"programmatic_ms_per_solve": ms_step, "plain_ms_per_solve": float(np.mean(plain["ms"])),
                         "note": "programmatic dependent launch (the default) against plain stream order"},
-        "gram_schmidt": {"reorthogonalized_ms_per_solve": ms_step,
-                         "one_projection_ms_per_solve": float(np.mean(cgs1["ms"])),
-                         "one_projection_gmres_its": int(cgs1["out"]["gmres_its"][0]),
-                         "one_projection_newton_its": int(cgs1["out"]["newton_its"][0]),
-                         "note": "GMRES orthogonalization: classical Gram-Schmidt with one reorthogonalization "
-                                 "(the headline) against one projection"},
+        "gram_schmidt": {"one_projection_ms_per_solve": ms_step,
+                         "reorthogonalized_ms_per_solve": float(np.mean(cgs2["ms"])),
+                         "reorthogonalized_gmres_its": int(cgs2["out"]["gmres_its"][0]),
+                         "reorthogonalized_newton_its": int(cgs2["out"]["newton_its"][0]),
+                         "note": "GMRES orthogonalization: classical Gram-Schmidt with one projection (the "
+                                 "headline) against one reorthogonalization"},
         "small_level_fusion": {"separate_ms_per_solve": ms_step, "fused_ms_per_solve": float(np.mean(fused["ms"])),
                                "cluster_tail_ms_per_solve": float(np.mean(tail["ms"])),
                                "cluster_tail_gmres_its": int(tail["out"]["gmres_its"][0]),

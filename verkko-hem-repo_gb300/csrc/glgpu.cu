@@ -183,7 +183,7 @@ struct glgpu_ctx
   // instances whose multigrid solve stalled twice stop where they are instead of finishing
   // with block-Jacobi in this context (mg_handoff); the caller finishes them elsewhere
   bool mg_handoff = false;
-  bool reorth = true;                // Gram-Schmidt with one reorthogonalization (else one projection)
+  bool reorth = false;               // Gram-Schmidt with one reorthogonalization (default: one projection)
   std::vector<uint8_t> handed;       // per instance, set during the last glgpu_run
 };
 

@@ -660,7 +660,7 @@ class FemGL:
         _check(lib().glgpu_set_mg_handoff(self._ctx, int(bool(on))))
 
     def set_reorthogonalization(self, on: bool = True) -> None:
-        """GMRES Gram-Schmidt with one reorthogonalization (default) or one projection."""
+        """GMRES Gram-Schmidt with one reorthogonalization, or one projection (the default)."""
         _check(lib().glgpu_set_reorthogonalization(self._ctx, int(bool(on))))
 
     @property
