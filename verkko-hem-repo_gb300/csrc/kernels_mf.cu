@@ -34,6 +34,9 @@ constexpr float kGbF = 0.78867513459481288225f;
 
 // Shared layouts: per point the 9 complex entries in pair order [2 k + part] (k = 3 mu + j),
 // padded to 20 floats (80 bytes, so a point's row loads as 16-byte vectors).
+// per-cell constants: 1/hx, 1/hy, 1/hz, JxW, K1, K2+K3, alpha, beta1..beta5
+constexpr int kParIh = 0, kParJxw = 3, kParK1 = 4, kParK23 = 5, kParBulk = 6, kPar = 12;
+
 template <int NC> struct MfSmem
 {
   union
@@ -48,10 +51,20 @@ template <int NC> struct MfSmem
   float X[NC * 8][20]; // the state A at the points
   float Z[NC * 8][20]; // the direction Z at the points
   float gZ[NC * 8][3][18]; // dZ / dx_k at the points, pair order
-  float ih[NC][3];
-  float jxw[NC];
-  float K1[NC], K23[NC];
-  float bulk[NC][6]; // alpha, beta1..beta5
+  float par[NC][kPar];
+};
+
+// the shared arrays the compute phases read and write (NC cells, 8 NC points); part rows
+// are PLD floats apart
+template <int NC, int PLD> struct MfView
+{
+  const float (*zs)[8][18];
+  const float (*xs)[8][18];
+  float (*X)[20];
+  float (*Z)[20];
+  float (*gZ)[3][18];
+  float (*part)[NC * 8][PLD];
+  const float (*par)[kPar];
 };
 
 using C2 = float2; // complex (re, im), or a component pair (u_c, v_c)
@@ -354,6 +367,188 @@ __device__ __forceinline__ void mf_contract(const C2 (&w)[8], const C2 (&F)[3][8
   }
 }
 
+// A, Z and dZ/dx at the points from the nodal values: thread (cell, component pair)
+template <int NC, int PLD>
+__device__ __forceinline__ void mf_points(const MfView<NC, PLD> &v, int tid)
+{
+  if (tid >= NC * 9) return;
+  const int cl = tid / 9, cp = tid - 9 * cl;
+  auto zval = [&](int t, int c) -> float { return v.zs[cl][t][c]; };
+  {
+    C2 aq[2][4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      gauss2(c2(v.xs[cl][t][cp], v.xs[cl][t][cp + 9]), c2(v.xs[cl][t + 4][cp], v.xs[cl][t + 4][cp + 9]), aq[0][t],
+             aq[1][t]);
+#pragma unroll
+    for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+      for (int vx = 0; vx < 2; ++vx)
+        {
+          C2 y0, y1;
+          gauss2(aq[qz][vx], aq[qz][2 + vx], y0, y1);
+          aq[qz][vx] = y0;
+          aq[qz][2 + vx] = y1;
+        }
+#pragma unroll
+    for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+      for (int qy = 0; qy < 2; ++qy)
+        {
+          C2 v0, v1;
+          gauss2(aq[qz][2 * qy], aq[qz][2 * qy + 1], v0, v1);
+          const int p0 = cl * 8 + 2 * qy + 4 * qz;
+          reinterpret_cast<float2 *>(v.X[p0])[cp] = v0;
+          reinterpret_cast<float2 *>(v.X[p0 + 1])[cp] = v1;
+        }
+  }
+  C2 zq[2][4], zd[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t)
+    {
+      const C2 f0 = c2(zval(t, cp), zval(t, cp + 9));
+      const C2 f1 = c2(zval(t + 4, cp), zval(t + 4, cp + 9));
+      gauss2(f0, f1, zq[0][t], zq[1][t]);
+      zd[t] = sub2(f1, f0);
+    }
+  C2 yq[2][2][2], ydy[2][2], zdq[2][2];
+#pragma unroll
+  for (int vx = 0; vx < 2; ++vx)
+    {
+#pragma unroll
+      for (int qz = 0; qz < 2; ++qz)
+        {
+          gauss2(zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
+          ydy[qz][vx] = sub2(zq[qz][2 + vx], zq[qz][vx]);
+        }
+      gauss2(zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
+    }
+  const float i0 = v.par[cl][kParIh], i1 = v.par[cl][kParIh + 1], i2 = v.par[cl][kParIh + 2];
+#pragma unroll
+  for (int qz = 0; qz < 2; ++qz)
+#pragma unroll
+    for (int qy = 0; qy < 2; ++qy)
+      {
+        C2 v0, v1;
+        gauss2(yq[qz][qy][0], yq[qz][qy][1], v0, v1);
+        const C2 dx = scl2(sub2(yq[qz][qy][1], yq[qz][qy][0]), i0);
+        const int p0 = cl * 8 + 2 * qy + 4 * qz;
+        reinterpret_cast<float2 *>(v.Z[p0])[cp] = v0;
+        reinterpret_cast<float2 *>(v.Z[p0 + 1])[cp] = v1;
+        reinterpret_cast<float2 *>(v.gZ[p0][0])[cp] = dx;
+        reinterpret_cast<float2 *>(v.gZ[p0 + 1][0])[cp] = dx;
+      }
+#pragma unroll
+  for (int qz = 0; qz < 2; ++qz)
+    {
+      C2 d0, d1;
+      gauss2(ydy[qz][0], ydy[qz][1], d0, d1);
+#pragma unroll
+      for (int qy = 0; qy < 2; ++qy)
+        {
+          const int p0 = cl * 8 + 2 * qy + 4 * qz;
+          reinterpret_cast<float2 *>(v.gZ[p0][1])[cp] = scl2(d0, i1);
+          reinterpret_cast<float2 *>(v.gZ[p0 + 1][1])[cp] = scl2(d1, i1);
+        }
+    }
+#pragma unroll
+  for (int qy = 0; qy < 2; ++qy)
+    {
+      C2 d0, d1;
+      gauss2(zdq[qy][0], zdq[qy][1], d0, d1);
+#pragma unroll
+      for (int qz = 0; qz < 2; ++qz)
+        {
+          const int p0 = cl * 8 + 2 * qy + 4 * qz;
+          reinterpret_cast<float2 *>(v.gZ[p0][2])[cp] = scl2(d0, i2);
+          reinterpret_cast<float2 *>(v.gZ[p0 + 1][2])[cp] = scl2(d1, i2);
+        }
+    }
+}
+
+// H Z at each point in two shares: thread (role, point), role uniform over a warp for NC >= 4
+template <int NC, int PLD>
+__device__ __forceinline__ void mf_products(const MfView<NC, PLD> &v, int tid, int ncb)
+{
+  constexpr int kMPts = 8 * NC;
+  const int role = tid / kMPts, pq = tid - role * kMPts, cl = pq >> 3;
+  if (cl >= ncb) return;
+  C2 A[9], F[9], out[9];
+  load_c9(v.X[pq], A);
+  load_c9(v.Z[pq], F);
+  float cf[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) cf[k] = v.par[cl][kParBulk + k];
+  if (role == 0)
+    hvp_role<0>(A, F, cf, out);
+  else
+    hvp_role<1>(A, F, cf, out);
+  float2 *row = reinterpret_cast<float2 *>(v.part[role][pq]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) row[k] = out[k];
+}
+
+// contraction with the test functions and the cell results: thread (cell, component pair)
+template <int NC, int PLD>
+__device__ __forceinline__ void mf_contract_store(const MfView<NC, PLD> &v, int tid, int ncb, float *__restrict__ yc)
+{
+  if (tid >= NC * 9) return;
+  const int cl = tid / 9, cp = tid - 9 * cl;
+  const int mu = cp / 3, jc = cp % 3;
+  const float K1 = v.par[cl][kParK1], K23 = v.par[cl][kParK23];
+  const float ih[3] = {v.par[cl][kParIh], v.par[cl][kParIh + 1], v.par[cl][kParIh + 2]};
+  C2 w[8], F[3][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    {
+      const int pq = cl * 8 + q;
+      w[q] = add2(reinterpret_cast<const float2 *>(v.part[0][pq])[cp], reinterpret_cast<const float2 *>(v.part[1][pq])[cp]);
+      const C2 dv = scl2(add2(add2(reinterpret_cast<const float2 *>(v.gZ[pq][0])[3 * mu],
+                                   reinterpret_cast<const float2 *>(v.gZ[pq][1])[3 * mu + 1]),
+                              reinterpret_cast<const float2 *>(v.gZ[pq][2])[3 * mu + 2]),
+                         K23);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        {
+          C2 g = scl2(reinterpret_cast<const float2 *>(v.gZ[pq][k])[cp], K1);
+          if (k == jc) g = add2(g, dv);
+          F[k][q] = scl2(g, ih[k]);
+        }
+    }
+  C2 r[8];
+  mf_contract(w, F, r);
+  if (cl < ncb)
+    {
+      const float jxw = v.par[cl][kParJxw];
+      float *out = yc + cl * 144 + cp;
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+        {
+          out[18 * a] = r[a].x * jxw;
+          out[18 * a + 9] = r[a].y * jxw;
+        }
+    }
+}
+
+// per-cell constants of cell e into p (zeros past the mesh)
+__device__ __forceinline__ void mf_cell_par(const DevMesh &m, int64_t e, float (&p)[kPar])
+{
+#pragma unroll
+  for (int k = 0; k < kPar; ++k) p[k] = 0.f;
+  if (e >= m.nc) return;
+  const int inst = m.cell_inst[e];
+  const float4 g = m.geo_f[e];
+  p[kParIh] = g.x;
+  p[kParIh + 1] = g.y;
+  p[kParIh + 2] = g.z;
+  p[kParJxw] = 0.125f * g.w;
+  p[kParK1] = m.coef_f[inst * kCoef + 0];
+  p[kParK23] = m.coef_f[inst * kCoef + 1];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) p[kParBulk + k] = m.coef_f[inst * kCoef + 2 + k];
+}
+
+// One CTA per NC cells.
 template <int NC>
 __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const float *__restrict__ xs,
                                                         const float *__restrict__ z, float *__restrict__ ycell,
@@ -361,7 +556,7 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
 {
   pdl_wait();
   pdl_trigger();
-  constexpr int kMCells = NC, kMPts = 8 * NC, kMThreads = 16 * NC;
+  constexpr int kMCells = NC, kMThreads = 16 * NC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   MfSmem<NC> &S = *reinterpret_cast<MfSmem<NC> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -371,42 +566,19 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
     {
       // a CTA whose cells all belong to inactive instances (converged, or waiting in a
       // batched solve) has nothing to contribute: the gather skips their nodes
-      __shared__ int any_on;
-      if (tid == 0) any_on = 0;
-      __syncthreads();
-      if (tid < ncb && act[m.cell_inst[e0 + tid]]) any_on = 1;
-      __syncthreads();
-      if (!any_on) return;
+      if (!__syncthreads_or(tid < ncb && act[m.cell_inst[e0 + tid]])) return;
     }
   if (tid < kMCells)
     {
-      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-      float K1 = 0.f, K23 = 0.f;
-      float bk[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (tid < ncb)
-        {
-          const int64_t e = e0 + tid;
-          const int inst = m.cell_inst[e];
-          g = m.geo_f[e];
-          K1 = m.coef_f[inst * kCoef + 0];
-          K23 = m.coef_f[inst * kCoef + 1];
+      float p[kPar];
+      mf_cell_par(m, e0 + tid, p);
 #pragma unroll
-          for (int k = 0; k < 6; ++k) bk[k] = m.coef_f[inst * kCoef + 2 + k];
-        }
-      S.ih[tid][0] = g.x;
-      S.ih[tid][1] = g.y;
-      S.ih[tid][2] = g.z;
-      S.jxw[tid] = 0.125f * g.w;
-      S.K1[tid] = K1;
-      S.K23[tid] = K23;
-#pragma unroll
-      for (int k = 0; k < 6; ++k) S.bulk[tid][k] = bk[k];
+      for (int k = 0; k < kPar; ++k) S.par[tid][k] = p[k];
     }
   // nodal values: the 16 threads of cell cl = tid / 16 take its vertices two per vertex;
   // half h of vertex a loads the float2 pairs j0 = 5 h .. 4 + 4 h of the vertex's 18 values
   // (a row is 72 bytes, 8-byte aligned) and the vertex's component mask once.  Constraint
-  // rows (hanging nodes, periodic images) are expanded from their parents only on meshes
-  // that have them.
+  // rows (hanging nodes, periodic images) are expanded from their parents.
   {
     static_assert(kMThreads == 16 * kMCells, "16 threads per cell");
     const int cl = tid >> 4, a = (tid & 15) >> 1, h = tid & 1;
@@ -458,161 +630,12 @@ __global__ void __launch_bounds__(16 * NC, 40 / NC) k_mf_cell(DevMesh m, const f
         }
   }
   __syncthreads();
-  // A, Z and dZ/dx at the points: thread (cell, component pair)
-  if (tid < kMCells * 9)
-    {
-      const int cl = tid / 9, cp = tid - 9 * cl;
-      {
-        C2 aq[2][4];
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-          gauss2(c2(S.u.g.xs[cl][t][cp], S.u.g.xs[cl][t][cp + 9]),
-                 c2(S.u.g.xs[cl][t + 4][cp], S.u.g.xs[cl][t + 4][cp + 9]), aq[0][t], aq[1][t]);
-#pragma unroll
-        for (int qz = 0; qz < 2; ++qz)
-#pragma unroll
-          for (int vx = 0; vx < 2; ++vx)
-            {
-              C2 y0, y1;
-              gauss2(aq[qz][vx], aq[qz][2 + vx], y0, y1);
-              aq[qz][vx] = y0;
-              aq[qz][2 + vx] = y1;
-            }
-#pragma unroll
-        for (int qz = 0; qz < 2; ++qz)
-#pragma unroll
-          for (int qy = 0; qy < 2; ++qy)
-            {
-              C2 v0, v1;
-              gauss2(aq[qz][2 * qy], aq[qz][2 * qy + 1], v0, v1);
-              const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              reinterpret_cast<float2 *>(S.X[p0])[cp] = v0;
-              reinterpret_cast<float2 *>(S.X[p0 + 1])[cp] = v1;
-            }
-      }
-      C2 zq[2][4], zd[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t)
-        {
-          const C2 f0 = c2(S.u.g.zs[cl][t][cp], S.u.g.zs[cl][t][cp + 9]);
-          const C2 f1 = c2(S.u.g.zs[cl][t + 4][cp], S.u.g.zs[cl][t + 4][cp + 9]);
-          gauss2(f0, f1, zq[0][t], zq[1][t]);
-          zd[t] = sub2(f1, f0);
-        }
-      C2 yq[2][2][2], ydy[2][2], zdq[2][2];
-#pragma unroll
-      for (int vx = 0; vx < 2; ++vx)
-        {
-#pragma unroll
-          for (int qz = 0; qz < 2; ++qz)
-            {
-              gauss2(zq[qz][vx], zq[qz][2 + vx], yq[qz][0][vx], yq[qz][1][vx]);
-              ydy[qz][vx] = sub2(zq[qz][2 + vx], zq[qz][vx]);
-            }
-          gauss2(zd[vx], zd[2 + vx], zdq[0][vx], zdq[1][vx]);
-        }
-      const float i0 = S.ih[cl][0], i1 = S.ih[cl][1], i2 = S.ih[cl][2];
-#pragma unroll
-      for (int qz = 0; qz < 2; ++qz)
-#pragma unroll
-        for (int qy = 0; qy < 2; ++qy)
-          {
-            C2 v0, v1;
-            gauss2(yq[qz][qy][0], yq[qz][qy][1], v0, v1);
-            const C2 dx = scl2(sub2(yq[qz][qy][1], yq[qz][qy][0]), i0);
-            const int p0 = cl * 8 + 2 * qy + 4 * qz;
-            reinterpret_cast<float2 *>(S.Z[p0])[cp] = v0;
-            reinterpret_cast<float2 *>(S.Z[p0 + 1])[cp] = v1;
-            reinterpret_cast<float2 *>(S.gZ[p0][0])[cp] = dx;
-            reinterpret_cast<float2 *>(S.gZ[p0 + 1][0])[cp] = dx;
-          }
-#pragma unroll
-      for (int qz = 0; qz < 2; ++qz)
-        {
-          C2 d0, d1;
-          gauss2(ydy[qz][0], ydy[qz][1], d0, d1);
-#pragma unroll
-          for (int qy = 0; qy < 2; ++qy)
-            {
-              const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              reinterpret_cast<float2 *>(S.gZ[p0][1])[cp] = scl2(d0, i1);
-              reinterpret_cast<float2 *>(S.gZ[p0 + 1][1])[cp] = scl2(d1, i1);
-            }
-        }
-#pragma unroll
-      for (int qy = 0; qy < 2; ++qy)
-        {
-          C2 d0, d1;
-          gauss2(zdq[qy][0], zdq[qy][1], d0, d1);
-#pragma unroll
-          for (int qz = 0; qz < 2; ++qz)
-            {
-              const int p0 = cl * 8 + 2 * qy + 4 * qz;
-              reinterpret_cast<float2 *>(S.gZ[p0][2])[cp] = scl2(d0, i2);
-              reinterpret_cast<float2 *>(S.gZ[p0 + 1][2])[cp] = scl2(d1, i2);
-            }
-        }
-    }
+  const MfView<NC, 20> v = {S.u.g.zs, S.u.g.xs, S.X, S.Z, S.gZ, S.u.part, S.par};
+  mf_points<NC, 20>(v, tid);
   __syncthreads(); // X, Z, gZ complete; the gathered nodal values are no longer read
-  // H Z at each point in two shares: thread (role, point), role uniform over a warp for NC >= 4
-  {
-    const int role = tid / kMPts, pq = tid - role * kMPts, cl = pq >> 3;
-    if (cl < ncb)
-      {
-        C2 A[9], F[9], out[9];
-        load_c9(S.X[pq], A);
-        load_c9(S.Z[pq], F);
-        float cf[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) cf[k] = S.bulk[cl][k];
-        if (role == 0)
-          hvp_role<0>(A, F, cf, out);
-        else
-          hvp_role<1>(A, F, cf, out);
-        store_c9(S.u.part[role][pq], out);
-      }
-  }
+  mf_products<NC, 20>(v, tid, ncb);
   __syncthreads();
-  // contraction with the test functions: thread (cell, component pair)
-  if (tid < kMCells * 9)
-    {
-      const int cl = tid / 9, cp = tid - 9 * cl;
-      const int mu = cp / 3, jc = cp % 3;
-      const float K1 = S.K1[cl], K23 = S.K23[cl];
-      const float ih[3] = {S.ih[cl][0], S.ih[cl][1], S.ih[cl][2]};
-      C2 w[8], F[3][8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        {
-          const int pq = cl * 8 + q;
-          w[q] = add2(reinterpret_cast<const float2 *>(S.u.part[0][pq])[cp],
-                      reinterpret_cast<const float2 *>(S.u.part[1][pq])[cp]);
-          const C2 dv = scl2(add2(add2(reinterpret_cast<const float2 *>(S.gZ[pq][0])[3 * mu],
-                                       reinterpret_cast<const float2 *>(S.gZ[pq][1])[3 * mu + 1]),
-                                  reinterpret_cast<const float2 *>(S.gZ[pq][2])[3 * mu + 2]),
-                             K23);
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-            {
-              C2 g = scl2(reinterpret_cast<const float2 *>(S.gZ[pq][k])[cp], K1);
-              if (k == jc) g = add2(g, dv);
-              F[k][q] = scl2(g, ih[k]);
-            }
-        }
-      C2 r[8];
-      mf_contract(w, F, r);
-      if (cl < ncb)
-        {
-          const float jxw = S.jxw[cl];
-          float *out = ycell + (e0 + cl) * 144 + cp;
-#pragma unroll
-          for (int a = 0; a < 8; ++a)
-            {
-              out[18 * a] = r[a].x * jxw;
-              out[18 * a + 9] = r[a].y * jxw;
-            }
-        }
-    }
+  mf_contract_store<NC, 20>(v, tid, ncb, ycell + e0 * 144);
 }
 
 // Node gather: thread (node, component), 16 nodes per CTA.  s = sum of the row's cell
