@@ -340,8 +340,21 @@ __global__ void __launch_bounds__(kSzNodes * 18) k_smooth_zero18(DevMesh m, cons
   if (!on) return;
   const DT *row = dinv + n * 324 + c * 18;
   T u = 0;
+  if constexpr (sizeof(DT) == 2)
+    {
+      // FP16 row: 36 bytes at a 4-byte boundary, nine half2 loads
+      const __half2 *r2 = reinterpret_cast<const __half2 *>(row);
 #pragma unroll
-  for (int d = 0; d < 18; ++d) u += mval(row + d) * b_s[ln][d];
+      for (int d = 0; d < 9; ++d)
+        {
+          const float2 w = __half22float2(__ldg(r2 + d));
+          u += w.x * b_s[ln][2 * d];
+          u += w.y * b_s[ln][2 * d + 1];
+        }
+    }
+  else
+#pragma unroll
+    for (int d = 0; d < 18; ++d) u += mval(row + d) * b_s[ln][d];
   y[n * 18 + c] = omega * u;
 }
 
