@@ -429,6 +429,7 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const M
   pdl_wait();
   pdl_trigger();
   __shared__ T M[kBjWarps][18][37];
+  __shared__ T L1s[kBjWarps][324]; // l1: per-entry absolute sums of the row's off-diagonal blocks
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kBjWarps + warp;
   if (n >= m.nn) return;
@@ -443,17 +444,49 @@ __global__ void __launch_bounds__(kBjWarps * 32) k_bj_setup18(DevMesh m, const M
     {
       // l1 block-Jacobi: row r's diagonal grows by the absolute sum of its entries outside
       // the diagonal block (with the diagonal's sign), which makes the smoother convergent
-      // for every symmetric positive definite matrix, mass-dominated ones included
+      // for every symmetric positive definite matrix, mass-dominated ones included.  The
+      // warp streams the row's blocks with the SpMV lane map (lane l owns entries
+      // e = (l + 32 it) NV + v of every block, 16- or 8-byte loads); the per-entry sums then
+      // meet per row in shared memory.
+      using V = typename Vec16<MT>::type;
+      constexpr int NV = Vec16<MT>::n;
+      constexpr int NCH = 324 / NV;
+      constexpr int NIT = (NCH + 31) / 32;
+      T acc[NIT][NV];
+#pragma unroll
+      for (int it = 0; it < NIT; ++it)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
+      const int32_t rb0 = m.rowptr[n], rb1 = m.rowptr[n + 1], rd = m.diag[n];
+#pragma unroll 4
+      for (int32_t b = rb0; b < rb1; ++b)
+        {
+          if (b == rd) continue;
+          const V *bp = reinterpret_cast<const V *>(vals + static_cast<int64_t>(b) * 324);
+#pragma unroll
+          for (int it = 0; it < NIT; ++it)
+            {
+              const int ch = lane + 32 * it;
+              const V w = (ch < NCH) ? __ldg(bp + ch) : V{};
+#pragma unroll
+              for (int v = 0; v < NV; ++v) acc[it][v] += fabs(static_cast<T>(vget<V, T>(w, v)));
+            }
+        }
+      T *l1s = L1s[warp];
+#pragma unroll
+      for (int it = 0; it < NIT; ++it)
+        {
+          const int ch = lane + 32 * it;
+          if (ch < NCH)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) l1s[ch * NV + v] = acc[it][v];
+        }
+      __syncwarp();
       if (lane < 18)
         {
           T sum = 0;
-          for (int32_t b = m.rowptr[n]; b < m.rowptr[n + 1]; ++b)
-            {
-              if (b == m.diag[n]) continue;
-              const MT *row = vals + static_cast<int64_t>(b) * 324 + lane * 18;
 #pragma unroll
-              for (int c = 0; c < 18; ++c) sum += fabs(static_cast<T>(mval(row + c)));
-            }
+          for (int c = 0; c < 18; ++c) sum += l1s[lane * 18 + c];
           const T d = M[warp][lane][lane];
           M[warp][lane][lane] = d + (d < T(0) ? -sum : sum);
         }
