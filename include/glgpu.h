@@ -155,7 +155,7 @@ glgpu_status glgpu_get_solution(const glgpu_ctx *ctx, double *x);
 
 /* Page-locked host memory for the arrays passed to set_solution / get_solution (and the
  * other host-array entry points): copies from and to it run as direct DMA instead of
- * being staged by the driver.  Free with glgpu_host_free. */
+ * being staged through a CUDA-internal bounce buffer.  Free with glgpu_host_free. */
 glgpu_status glgpu_host_alloc(size_t bytes, void **p);
 glgpu_status glgpu_host_free(void *p);
 

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path through the C ABI against the FP64 CPU oracle.
 
-Tolerances (spec bar for FP64 mode): Jacobian and residual 1e-12 relative,
+Tolerances (FP64 mode): Jacobian and residual 1e-12 relative,
 Newton iteration counts equal, converged order parameter and free energy 1e-9
 relative.  Mixed mode (FP32 Jacobian/GMRES, FP64 residual): Jacobian 1e-5 relative
 to the FP64 oracle, converged residual and free energy as in FP64 mode.

@@ -777,7 +777,7 @@ glgpu_status gmres(glgpu_ctx *c, double tol, const std::vector<uint8_t> &on, std
       if (use_mg)
         {
           // flexible GMRES can stop on a breakdown of the preconditioned basis with a small
-          // estimate: judge the cycle by the true residual |b - J X| instead
+          // estimate: measure the cycle by the true residual |b - J X| instead
           CKS(spmv(c, c->X, c->Tmp, c->d_act2));
           CKS(axpby(c, c->Bv, c->Tmp, nullptr, coefs(1.0, -1.0), c->d_act2, m32, m32, m32));
           CKS(launch(c, KK_VEC, 1, [&] {
