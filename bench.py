@@ -33,10 +33,10 @@ sys.path.insert(0, ROOT)
 
 P_BAR, T_RED, HALF, NCELL, NOISE, SEED = 20.0, 0.6, 10.0, 32, 0.05, 2
 TOL = 1e-10
-# DRAM bytes of one matrix-free apply (k_mf_cell + k_mf_gather) on this workload, from one ncu
-# capture of the two kernels on the 32^3 cube (cold caches: the cell results the gather reads
-# come from DRAM there, from L2 in the live solve)
-MF_NCU_TRAFFIC = 7.239424e6 + 0.0 + 2.2761216e7
+# DRAM bytes of one matrix-free apply (k_mf_cell + k_mf_gather in the y = J z form) on this
+# workload, from ncu captures of the two kernels on the 32^3 cube (`--ncu-case 32`; cold caches:
+# the cell results the gather reads come from DRAM there, from L2 in the live solve)
+MF_NCU_TRAFFIC = 7.073536e6 + 0.0 + 2.2761216e7
 # FP32 operations of one matrix-free apply per cell: the closed-form Hessian-vector product at
 # 8 points, regrouped as C Re(A) + D Im(A) + E Re(F) + G Im(F) (about 1,500 per point: the
 # products A F^T and F A^+, the state-only A A^T and A A^+, four complex-by-real 3x3 products)
