@@ -100,6 +100,10 @@ struct DevMesh
   int64_t n_robin;
   // some node has a constraint row (hanging node or periodic image): gathers must expand them
   int has_constraints;
+  // [nn][8] offsets cell * 144 + vertex * 18 of each node's cell contributions (list order, -1
+  // past the end), on meshes whose contributions all have weight 1 and number at most 8 per
+  // node (no constraint rows); nullptr elsewhere
+  const int32_t *rc_off8;
 };
 
 #ifdef __CUDACC__

@@ -1502,6 +1502,30 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
   d.mask = p_mask;
   d.hptr = p_hptr;
   d.has_constraints = (!P.hptr.empty() && P.hptr.back() > 0) ? 1 : 0;
+  {
+    // the matrix-free gather's contribution table: on meshes without constraint rows every
+    // node takes at most 8 cell contributions, all of weight 1; rc_off8[n][k] is the offset
+    // cell * 144 + vertex * 18 of its k-th contribution in list order, -1 past the end
+    int32_t *p_off8 = nullptr;
+    if (P.dim == 3 && P.B == 18 && P.nv == 8 && !d.has_constraints && P.nc * 144 < INT32_MAX)
+      {
+        bool ok = true;
+        std::vector<int32_t> off8(static_cast<size_t>(P.nn) * 8, -1);
+        for (int64_t n = 0; n < P.nn && ok; ++n)
+          {
+            const int32_t k0 = P.rc_ptr[n], k1 = P.rc_ptr[n + 1];
+            ok = k1 - k0 <= 8;
+            for (int32_t k = k0; ok && k < k1; ++k)
+              {
+                ok = P.rc_w[k] == 1.0;
+                off8[static_cast<size_t>(n) * 8 + (k - k0)] = static_cast<int32_t>(P.rc_cell[k] * 144 + P.rc_a[k] * 18);
+              }
+          }
+        if (ok && (s = dupload(c, &p_off8, off8))) return fail(s);
+        if (!ok) p_off8 = nullptr;
+      }
+    d.rc_off8 = p_off8;
+  }
   d.hpar = p_hpar;
   d.hw = p_hw;
   d.rowptr = p_rowptr;

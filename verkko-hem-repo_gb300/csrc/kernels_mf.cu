@@ -659,7 +659,22 @@ __global__ void __launch_bounds__(kMgThreads, 5) k_mf_gather(DevMesh m, const fl
   const int64_t n = static_cast<int64_t>(blockIdx.x) * kMgNodes + ln;
   const bool on = n < m.nn && !(act && !act[m.node_inst[n]]);
   float s = 0.f;
-  if (on)
+  if (on && m.rc_off8)
+    {
+      // meshes without constraint rows: the node's (at most 8) contribution offsets in one
+      // 32-byte load, then the values; the same additions in the same order as the list path
+      // (weight 1, padded slots add 0)
+      const int4 *op = reinterpret_cast<const int4 *>(m.rc_off8 + n * 8);
+      const int4 o0 = __ldg(op), o1 = __ldg(op + 1);
+      const int off[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = (off[k] >= 0) ? __ldg(ycell + off[k] + c) : 0.f;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) s = fmaf(off[k] >= 0 ? 1.f : 0.f, v[k], s);
+      if ((m.mask[n] >> c) & 1u) s = z[n * 18 + c];
+    }
+  else if (on)
     {
       const int k0 = m.rc_ptr[n], k1 = m.rc_ptr[n + 1];
       for (int base = k0; base < k1; base += 8)
