@@ -259,18 +259,29 @@ cudaError_t launch_gmres_solve_y(const GmresDev &g, int n_inst, cudaStream_t s);
 cudaError_t launch_inv(const double *in, double *out, int n, cudaStream_t s);
 
 // ---- multigrid (kernels_mg.cu) ----
+// A transfer's entries in fixed slots per row (kProlongSlots per fine node, kRestrictSlots per
+// coarse node; list order, index -1 past the end): a row's slots come in one pass of 16-byte
+// loads instead of its bounds and then its entries.  idx == nullptr: the CSR lists are used.
+constexpr int kProlongSlots = 8, kRestrictSlots = 28;
+struct TransferSlots
+{
+  const int32_t *idx = nullptr;
+  const void *w = nullptr; // T weights
+};
 // zf = base + P zc, or zf += P zc when base is nullptr (constrained components keep base)
 cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                            const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base = nullptr);
+                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base = nullptr,
+                           TransferSlots sl = {});
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
-                            const uint8_t *act, cudaStream_t s);
+                            const uint8_t *act, cudaStream_t s, TransferSlots sl = {});
 // restriction fused with the coarse level's first sweep from zero (18x18 blocks):
 // rc = P^T rf, z = omega D^-1 rc
 cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, const int32_t *idx, const void *w,
                                    const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
-                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s);
+                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s,
+                                   TransferSlots sl = {});
 // Galerkin product J_c = P^T J_f P on the coarse block pattern, one warp per coarse
 // block: block cb = up[u] (row g_row[cb], column cols_c[cb] >= the row) is the sum over its
 // term list [g_toff[cb], g_toff[cb+1]) of g_w * (fine block g_blk).  Zero-Dirichlet rows and

@@ -133,6 +133,7 @@ struct glgpu_ctx
   {
     int32_t *p_ptr = nullptr, *p_idx = nullptr, *r_ptr = nullptr, *r_idx = nullptr;
     void *p_w = nullptr, *r_w = nullptr; // T weights
+    TransferSlots p_slots, r_slots;       // the same entries in fixed slots per row (when they fit)
     // Galerkin terms of every coarse block: [g_toff[cb], g_toff[cb+1]) of (fine block, weight)
     int64_t *g_toff = nullptr;
     int32_t *g_row = nullptr, *g_blk = nullptr;
@@ -1001,17 +1002,17 @@ glgpu_status vcycle(glgpu_ctx *c, int l, const void *r, void *z, const uint8_t *
       if (fuse)
         CKS(launch(c, KK_PREC, 1, [&] {
           return launch_restrict_smooth(m, C->nn, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask, C->dm.node_inst,
-                                        act, C->dinv, om, C->X, c->st);
+                                        act, C->dinv, om, C->X, c->st, tr.r_slots);
         }));
       else
         CKS(launch(c, KK_PREC, 1, [&] {
           return launch_restrict(m, C->nn, C->B, tr.r_ptr, tr.r_idx, tr.r_w, t, C->Bv, C->dm.mask,
-                                 C->dm.node_inst, act, c->st);
+                                 C->dm.node_inst, act, c->st, tr.r_slots);
         }));
       CKS(vcycle(c, l + 1, C->Bv, C->X, act, fuse));
       CKS(launch(c, KK_PREC, 1, [&] {
         return launch_prolong(m, L->nn, L->B, tr.p_ptr, tr.p_idx, tr.p_w, C->X, oth, L->dm.mask, L->dm.hptr,
-                              L->dm.node_inst, act, c->st, cur);
+                              L->dm.node_inst, act, c->st, cur, tr.p_slots);
       }));
     }
   std::swap(cur, oth);
@@ -1266,6 +1267,33 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
           CKS(upload_w<double>(c, &t.r_w, rw));
           CKS(upload_w<double>(c, &t.g_w, gw));
         }
+      // fixed-slot copies of the two transfers (rows with more entries than slots keep the lists)
+      auto slots = [&](const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx, const std::vector<double> &w,
+                       int S, TransferSlots &out) -> glgpu_status {
+        const int64_t rows = static_cast<int64_t>(ptr.size()) - 1;
+        for (int64_t r = 0; r < rows; ++r)
+          if (ptr[r + 1] - ptr[r] > S) return GLGPU_OK;
+        std::vector<int32_t> si(static_cast<size_t>(rows) * S, -1);
+        std::vector<double> sw(static_cast<size_t>(rows) * S, 0.0);
+        for (int64_t r = 0; r < rows; ++r)
+          for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k)
+            {
+              si[static_cast<size_t>(r) * S + (k - ptr[r])] = idx[k];
+              sw[static_cast<size_t>(r) * S + (k - ptr[r])] = w[k];
+            }
+        int32_t *d_si = nullptr;
+        void *d_sw = nullptr;
+        CKS(dupload(c, &d_si, si));
+        if (c->mixed)
+          CKS(upload_w<float>(c, &d_sw, sw));
+        else
+          CKS(upload_w<double>(c, &d_sw, sw));
+        out.idx = d_si;
+        out.w = d_sw;
+        return GLGPU_OK;
+      };
+      CKS(slots(pp, pi, pw, kProlongSlots, t.p_slots));
+      CKS(slots(rp, ri, rw, kRestrictSlots, t.r_slots));
     }
   // coarsest level: dense inverses
   glgpu_ctx *Lc = c->lv[nl - 1];

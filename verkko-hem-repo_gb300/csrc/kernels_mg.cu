@@ -17,13 +17,37 @@
 
 namespace glgpu
 {
+// sum over row n's fixed slots of w * v[idx * B + c], in slot (list) order
+template <typename T, int S>
+__device__ __forceinline__ T slot_sum(const int32_t *__restrict__ sidx, const T *__restrict__ sw, int64_t n,
+                                      const T *__restrict__ v, int B, int c)
+{
+  static_assert(S % 4 == 0, "slots in 16-byte groups");
+  int id[S];
+  const int4 *ip = reinterpret_cast<const int4 *>(sidx + n * S);
+#pragma unroll
+  for (int q = 0; q < S / 4; ++q)
+    {
+      const int4 t = __ldg(ip + q);
+      id[4 * q] = t.x;
+      id[4 * q + 1] = t.y;
+      id[4 * q + 2] = t.z;
+      id[4 * q + 3] = t.w;
+    }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < S; ++k)
+    if (id[k] >= 0) s += __ldg(sw + n * S + k) * v[static_cast<int64_t>(id[k]) * B + c];
+  return s;
+}
+
 // zf = base + P zc (base == nullptr: zf += P zc); constrained components keep base
 template <typename T>
 __global__ void k_prolong_add(int64_t nn_f, int B, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
                               const T *__restrict__ w, const T *__restrict__ zc, T *__restrict__ zf,
                               const uint32_t *__restrict__ mask_f, const int32_t *__restrict__ hptr_f,
                               const int32_t *__restrict__ node_inst, const uint8_t *__restrict__ act,
-                              const T *__restrict__ base)
+                              const T *__restrict__ base, const int32_t *__restrict__ sidx, const T *__restrict__ sw)
 {
   pdl_wait();
   pdl_trigger();
@@ -39,7 +63,10 @@ __global__ void k_prolong_add(int64_t nn_f, int B, const int32_t *__restrict__ p
       return;
     }
   T s = 0;
-  for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * zc[static_cast<int64_t>(idx[k]) * B + c];
+  if (sidx)
+    s = slot_sum<T, kProlongSlots>(sidx, sw, n, zc, B, c);
+  else
+    for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * zc[static_cast<int64_t>(idx[k]) * B + c];
   zf[t] = b0 + s;
 }
 
@@ -47,7 +74,7 @@ template <typename T>
 __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
                            const T *__restrict__ w, const T *__restrict__ rf, T *__restrict__ rc,
                            const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ node_inst,
-                           const uint8_t *__restrict__ act)
+                           const uint8_t *__restrict__ act, const int32_t *__restrict__ sidx, const T *__restrict__ sw)
 {
   pdl_wait();
   pdl_trigger();
@@ -58,7 +85,12 @@ __global__ void k_restrict(int64_t nn_c, int B, const int32_t *__restrict__ ptr,
   if (act && !act[node_inst[n]]) return;
   T s = 0;
   if (!((mask_c[n] >> c) & 1u))
-    for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * rf[static_cast<int64_t>(idx[k]) * B + c];
+    {
+      if (sidx)
+        s = slot_sum<T, kRestrictSlots>(sidx, sw, n, rf, B, c);
+      else
+        for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * rf[static_cast<int64_t>(idx[k]) * B + c];
+    }
   rc[t] = s;
 }
 
@@ -73,7 +105,8 @@ __global__ void __launch_bounds__(kRsNodes * 18)
   k_restrict_smooth(int64_t nn_c, const int32_t *__restrict__ ptr, const int32_t *__restrict__ idx,
                     const T *__restrict__ w, const T *__restrict__ rf, T *__restrict__ rc,
                     const uint32_t *__restrict__ mask_c, const int32_t *__restrict__ node_inst,
-                    const uint8_t *__restrict__ act, const T *__restrict__ dinv, T omega, T *__restrict__ z)
+                    const uint8_t *__restrict__ act, const T *__restrict__ dinv, T omega, T *__restrict__ z,
+                    const int32_t *__restrict__ sidx, const T *__restrict__ sw)
 {
   pdl_wait();
   pdl_trigger();
@@ -83,7 +116,12 @@ __global__ void __launch_bounds__(kRsNodes * 18)
   const bool on = n < nn_c && !(act && !act[node_inst[n]]);
   T s = 0;
   if (on && !((mask_c[n] >> c) & 1u))
-    for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * rf[static_cast<int64_t>(idx[k]) * 18 + c];
+    {
+      if (sidx)
+        s = slot_sum<T, kRestrictSlots>(sidx, sw, n, rf, 18, c);
+      else
+        for (int k = ptr[n]; k < ptr[n + 1]; ++k) s += w[k] * rf[static_cast<int64_t>(idx[k]) * 18 + c];
+    }
   if (on) rc[n * 18 + c] = s;
   t_s[ln][c] = s;
   __syncthreads();
@@ -245,52 +283,58 @@ __global__ void __launch_bounds__(kGalWarps * 32)
 template <typename T>
 cudaError_t launch_prolong_add(int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                                const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                               const int32_t *node_inst, const uint8_t *act, const void *base, cudaStream_t s)
+                               const int32_t *node_inst, const uint8_t *act, const void *base, cudaStream_t s,
+                               TransferSlots sl)
 {
   const int64_t n = nn_f * B;
-  pdl_launch(k_prolong_add<T>, static_cast<unsigned>((n + 255) / 256), 256, 0, s, 
-    nn_f, B, ptr, idx, static_cast<const T *>(w), static_cast<const T *>(zc), static_cast<T *>(zf), mask_f, hptr_f,
-    node_inst, act, static_cast<const T *>(base));
+  pdl_launch(k_prolong_add<T>, static_cast<unsigned>((n + 255) / 256), 256, 0, s, nn_f, B, ptr, idx,
+             static_cast<const T *>(w), static_cast<const T *>(zc), static_cast<T *>(zf), mask_f, hptr_f, node_inst, act,
+             static_cast<const T *>(base), sl.idx, static_cast<const T *>(sl.w));
   return cudaGetLastError();
 }
 
 cudaError_t launch_prolong(bool fp32, int64_t nn_f, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                            const void *zc, void *zf, const uint32_t *mask_f, const int32_t *hptr_f,
-                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base)
+                           const int32_t *node_inst, const uint8_t *act, cudaStream_t s, const void *base,
+                           TransferSlots sl)
 {
-  return fp32 ? launch_prolong_add<float>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s)
-              : launch_prolong_add<double>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s);
+  return fp32 ? launch_prolong_add<float>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s, sl)
+              : launch_prolong_add<double>(nn_f, B, ptr, idx, w, zc, zf, mask_f, hptr_f, node_inst, act, base, s, sl);
 }
 
 cudaError_t launch_restrict(bool fp32, int64_t nn_c, int B, const int32_t *ptr, const int32_t *idx, const void *w,
                             const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
-                            const uint8_t *act, cudaStream_t s)
+                            const uint8_t *act, cudaStream_t s, TransferSlots sl)
 {
   const int64_t n = nn_c * B;
   const unsigned g = static_cast<unsigned>((n + 255) / 256);
   if (fp32)
     pdl_launch(k_restrict<float>, g, 256, 0, s, nn_c, B, ptr, idx, static_cast<const float *>(w),
-                                        static_cast<const float *>(rf), static_cast<float *>(rc), mask_c, node_inst, act);
+               static_cast<const float *>(rf), static_cast<float *>(rc), mask_c, node_inst, act, sl.idx,
+               static_cast<const float *>(sl.w));
   else
     pdl_launch(k_restrict<double>, g, 256, 0, s, nn_c, B, ptr, idx, static_cast<const double *>(w),
-                                         static_cast<const double *>(rf), static_cast<double *>(rc), mask_c, node_inst,
-                                         act);
+               static_cast<const double *>(rf), static_cast<double *>(rc), mask_c, node_inst, act, sl.idx,
+               static_cast<const double *>(sl.w));
   return cudaGetLastError();
 }
 
 cudaError_t launch_restrict_smooth(bool fp32, int64_t nn_c, const int32_t *ptr, const int32_t *idx, const void *w,
                                    const void *rf, void *rc, const uint32_t *mask_c, const int32_t *node_inst,
-                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s)
+                                   const uint8_t *act, const void *dinv, double omega, void *z, cudaStream_t s,
+                                   TransferSlots sl)
 {
   const unsigned g = static_cast<unsigned>((nn_c + kRsNodes - 1) / kRsNodes);
   if (fp32)
-    pdl_launch(k_restrict_smooth<float>, g, kRsNodes * 18, 0, s, 
-      nn_c, ptr, idx, static_cast<const float *>(w), static_cast<const float *>(rf), static_cast<float *>(rc), mask_c,
-      node_inst, act, static_cast<const float *>(dinv), static_cast<float>(omega), static_cast<float *>(z));
+    pdl_launch(k_restrict_smooth<float>, g, kRsNodes * 18, 0, s, nn_c, ptr, idx, static_cast<const float *>(w),
+               static_cast<const float *>(rf), static_cast<float *>(rc), mask_c, node_inst, act,
+               static_cast<const float *>(dinv), static_cast<float>(omega), static_cast<float *>(z), sl.idx,
+               static_cast<const float *>(sl.w));
   else
-    pdl_launch(k_restrict_smooth<double>, g, kRsNodes * 18, 0, s, 
-      nn_c, ptr, idx, static_cast<const double *>(w), static_cast<const double *>(rf), static_cast<double *>(rc), mask_c,
-      node_inst, act, static_cast<const double *>(dinv), omega, static_cast<double *>(z));
+    pdl_launch(k_restrict_smooth<double>, g, kRsNodes * 18, 0, s, nn_c, ptr, idx, static_cast<const double *>(w),
+               static_cast<const double *>(rf), static_cast<double *>(rc), mask_c, node_inst, act,
+               static_cast<const double *>(dinv), omega, static_cast<double *>(z), sl.idx,
+               static_cast<const double *>(sl.w));
   return cudaGetLastError();
 }
 
