@@ -104,6 +104,10 @@ struct DevMesh
   // past the end), on meshes whose contributions all have weight 1 and number at most 8 per
   // node (no constraint rows); nullptr elsewhere
   const int32_t *rc_off8;
+  // [nn][27] the block-column ids of each row (CSR order, -1 past the end) on 18x18 levels whose
+  // rows have at most 27 blocks (box grids): the row kernels read them without waiting for the
+  // row bounds; nullptr elsewhere
+  const int32_t *cols27;
 };
 
 #ifdef __CUDACC__

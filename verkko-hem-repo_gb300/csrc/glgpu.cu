@@ -1554,6 +1554,18 @@ extern "C" glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params 
       }
     d.rc_off8 = p_off8;
   }
+  {
+    int32_t *p_c27 = nullptr;
+    if (P.B == 18 && P.max_row_blocks <= 27)
+      {
+        std::vector<int32_t> c27(static_cast<size_t>(P.nn) * 27, -1);
+        for (int64_t n = 0; n < P.nn; ++n)
+          for (int32_t b = P.rowptr[n]; b < P.rowptr[n + 1]; ++b)
+            c27[static_cast<size_t>(n) * 27 + (b - P.rowptr[n])] = P.cols[b];
+        if ((s = dupload(c, &p_c27, c27))) return fail(s);
+      }
+    d.cols27 = p_c27;
+  }
   d.hpar = p_hpar;
   d.hw = p_hw;
   d.rowptr = p_rowptr;

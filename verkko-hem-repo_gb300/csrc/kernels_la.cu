@@ -80,11 +80,14 @@ __device__ __forceinline__ void row_products(const DevMesh &m, const MT *__restr
   for (int it = 0; it < NIT; ++it)
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[it][v] = T(0);
+  // column ids from the fixed 27-slot table where the level has one: the load does not wait
+  // for the row bounds (such rows have at most 27 blocks: one pass of the loop below)
+  const int fixed_col = (m.cols27 && lane < 27) ? m.cols27[n * 27 + lane] : 0;
   const int b0 = m.rowptr[n], b1 = m.rowptr[n + 1];
   for (int base = b0; base < b1; base += 32)
     {
       const int nbk = (b1 - base) < 32 ? (b1 - base) : 32;
-      const int mycol = (lane < nbk) ? m.cols[base + lane] : 0;
+      const int mycol = m.cols27 ? fixed_col : ((lane < nbk) ? m.cols[base + lane] : 0);
 #pragma unroll 4
       for (int k = kw; k < nbk; k += WPR)
         {
