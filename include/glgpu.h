@@ -299,6 +299,13 @@ glgpu_status glgpu_mg_level_system(const glgpu_ctx *ctx, int level, int32_t *row
  * every component of a node; restriction is its transpose. */
 glgpu_status glgpu_mg_prolongation(const glgpu_ctx *ctx, int level, int32_t *ptr, int32_t *idx, double *w);
 
+/* The coarsest level's dense FP32 inverse of instance `inst` as of the last preconditioner
+ * setup: *nd = its unknowns; inv (nd * nd, row-major, may be NULL to query nd) receives
+ * (A + shift * mean|diag A| * I)^-1 with A that level's Jacobian and shift the
+ * mg_coarse_shift parameter, or the identity when the factorisation met a zero pivot.
+ * Synchronises the context's stream. */
+glgpu_status glgpu_mg_coarse_inverse(glgpu_ctx *ctx, int inst, int *nd, float *inv);
+
 /*
  * Launch mode of the solve's kernels, process-wide (default 1): with 1 they are launched
  * with programmatic dependent launch, so each kernel's CTAs are scheduled while its

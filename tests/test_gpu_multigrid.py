@@ -371,3 +371,43 @@ def test_one_projection_gram_schmidt(gl, precision):
     assert o1["converged"] and o0["converged"]
     assert abs(F0 - F1) <= 1e-12 * abs(F1)
     assert abs(int(o0["gmres_its"][0]) - int(o1["gmres_its"][0])) <= 2 + 0.2 * int(o1["gmres_its"][0])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_coarsest_dense_inverse(gl, precision):
+    """The coarsest level's dense inverse (in-place Gauss-Jordan with partial pivoting, one CTA
+    per instance, rows held in registers) inverts that level's shifted Galerkin matrix for
+    every instance of a batch: small normwise residual and agreement with an FP64 inverse."""
+    meshes = [gl.box_mesh([-10, -10, -4], [10, 10, 4], (9, 9, 9)), gl.cube_mesh(5.0, 6),
+              gl.box_mesh([-10, -10, -12], [10, 10, 12], (12, 12, 12))]
+    pts = [(20.0, 0.6), (12.0, 0.45), (30.0, 0.85)]
+    x0 = np.concatenate([gl.bphase_guess(p, t, m.nn, noise=0.05, seed=k) for k, (m, (p, t)) in
+                         enumerate(zip(meshes, pts))])
+    prms = [gl.Params.from_matep(p, t, precond=gl.PC_MULTIGRID, precision=precision) for p, t in pts]
+    with gl.FemGL(meshes, prms) as f:
+        f.set_solution(x0)
+        f.assemble_system()
+        f.solve(1e-2, allow_unconverged=True)  # the hierarchy and the inverses are built by the setup
+        nl = f.mg_levels
+        rp, cols, vals, _ = f.mg_level(nl)
+        invs = [f.mg_coarse_inverse(k) for k in range(len(meshes))]
+    A = _bsr(rp, cols, vals).toarray()
+    assert sum(x.shape[0] for x in invs) == A.shape[0]
+    off = 0
+    for inv in invs:
+        nd = inv.shape[0]
+        assert nd % 18 == 0 and 0 < nd <= 144
+        # instances are independent: the level matrix is block diagonal over them
+        assert not A[off:off + nd, :off].any() and not A[off:off + nd, off + nd:].any()
+        M = A[off:off + nd, off:off + nd].astype(np.float32).astype(np.float64)
+        s = np.float32(prms[0].mg_coarse_shift) * np.abs(np.diag(M)).astype(np.float32).sum() / np.float32(nd)
+        M += float(s) * np.eye(nd)
+        X = inv.astype(np.float64)
+        assert np.isfinite(X).all() and not np.array_equal(X, np.eye(nd))  # no zero pivot met
+        res = np.linalg.norm(M @ X - np.eye(nd)) / (np.linalg.norm(M) * np.linalg.norm(X))
+        assert res < 1e-5, res
+        Xr = np.linalg.inv(M)
+        # FP32 elimination: forward error within a few ulps times the condition number
+        err = np.linalg.norm(X - Xr) / np.linalg.norm(Xr)
+        assert err < 1e-5 * np.linalg.cond(M), (err, np.linalg.cond(M))
+        off += nd

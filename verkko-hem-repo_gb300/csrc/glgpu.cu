@@ -1305,7 +1305,7 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       max_nd = std::max(max_nd, nd);
       doff[k + 1] = doff[k] + static_cast<int64_t>(nd) * nd;
     }
-  if (max_nd > 160) return set_error(GLGPU_ERR_ARG, "multigrid: coarsest level too large for the dense solve");
+  if (max_nd > 144) return set_error(GLGPU_ERR_ARG, "multigrid: coarsest level too large for the dense solve (144 unknowns)");
   c->max_nd = max_nd;
   {
     // the finest level's smoother blocks are read twice per V-cycle (the sweep from zero and
@@ -2342,6 +2342,25 @@ extern "C" glgpu_status glgpu_mg_prolongation(const glgpu_ctx *c, int level, int
   if (ptr) std::memcpy(ptr, t.h_ptr.data(), sizeof(int32_t) * t.h_ptr.size());
   if (idx) std::memcpy(idx, t.h_idx.data(), sizeof(int32_t) * t.h_idx.size());
   if (w) std::memcpy(w, t.h_w.data(), sizeof(double) * t.h_w.size());
+  return GLGPU_OK;
+}
+
+extern "C" glgpu_status glgpu_mg_coarse_inverse(glgpu_ctx *c, int inst, int *nd, float *inv)
+{
+  if (!c || !nd || c->n_levels < 1 || inst < 0 || inst >= c->n_inst || !c->d_inv)
+    return set_error(GLGPU_ERR_ARG, "glgpu_mg_coarse_inverse: no multigrid hierarchy or bad instance");
+  const glgpu_ctx *Lc = c->lv[c->n_levels - 1];
+  int64_t off = 0;
+  int n = 0;
+  for (int k = 0; k <= inst; ++k)
+    {
+      n = static_cast<int>((Lc->P.node_off[k + 1] - Lc->P.node_off[k]) * Lc->B);
+      if (k < inst) off += static_cast<int64_t>(n) * n;
+    }
+  *nd = n;
+  if (!inv) return GLGPU_OK;
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpy(inv, c->d_inv + off, sizeof(float) * static_cast<size_t>(n) * n, cudaMemcpyDeviceToHost));
   return GLGPU_OK;
 }
 

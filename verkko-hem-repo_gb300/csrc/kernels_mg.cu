@@ -386,52 +386,59 @@ cudaError_t launch_galerkin(bool fp32, int64_t n_up, const int32_t *up, int64_t 
 // of the slightly shifted matrix in shared memory, FP32, one CTA per instance.  It is a preconditioner component, so
 // FP32 suffices in both precision modes (the outer flexible GMRES is exact).
 // ---------------------------------------------------------------------------------
-constexpr int kGjThreads = 1024;      // (augmented column, row chunk) pairs
-constexpr int kMaxDense = 160;        // largest coarsest system (unknowns per instance)
+constexpr int kGjThreads = 864;       // (column, row chunk) pairs: 6 chunks of the 144 columns
+constexpr int kMaxDense = 144;        // largest coarsest system (unknowns per instance): 8 nodes x 18
+constexpr int kGjRows = 24;           // register rows per thread: a multiple of 4, >= every chunk
+constexpr int kGjPad = kMaxDense + kGjRows; // pivot-column length: chunks x rows < nd + rows
+// rows per chunk for nd unknowns: at least kGjThreads / nd >= 6 chunks, so at most 24 rows;
+// 864 threads leave 72 registers each, which hold 24 rows without spilling
+__host__ __device__ constexpr int gj_rows(int nd)
+{
+  return ((nd + (kGjThreads / nd) - 1) / (kGjThreads / nd) + 3) & ~3;
+}
+static_assert(gj_rows(kMaxDense) <= kGjRows && gj_rows(kMaxDense - 1) <= kGjRows, "register rows");
 
-// Gauss-Jordan on [A + shift I | I] with implicit partial pivoting: in step k one warp
-// picks the largest unused entry of column k (row p_k) and snapshots the column; then
-// every thread updates the rows of its chunk in the augmented column it owns (every row
-// minus its column-k multiple, then row p_k scaled).  A step reads the pivot row before
-// anyone overwrites it, so it takes three barriers.  Afterwards row p_k of the right half
-// is row k of the inverse.  Rows are padded to an odd length so that column reads hit
-// distinct banks; a warp's threads own consecutive columns.
+// Gauss-Jordan on A + shift I with implicit partial pivoting, in place: column k is replaced in
+// step k by the column of the inverse's row-permuted form that the augmented scheme [A | I]
+// would build in its right half for the unit vector of the pivot row, so every step updates
+// exactly nd columns.  Thread (column c, chunk) holds a 4-aligned run of rows of column c in
+// registers; shared memory carries only the pivot column and the pivot row.  Step k:
+//  * every warp picks the same pivot p_k (largest unused |entry| of column k, lowest index on a
+//    tie) from the published column; the threads holding row p_k publish it; one barrier;
+//  * every entry takes W -= colk * wp, wp = W[p][c] / pivot, and row p receives wp (the same
+//    floating-point operations as the augmented scheme, entry for entry); the holders of column
+//    k + 1 publish it into the other buffer; one barrier.
+// Afterwards row p_k holds row k of the inverse with its columns in pivot order (column j of
+// the inverse sits in the column of the step whose pivot row was j).
 template <typename T>
-__global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T *__restrict__ vals,
-                                                             const int64_t *__restrict__ dense_off,
-                                                             float *__restrict__ inv, int *__restrict__ singular,
-                                                             float shift)
+__global__ void __launch_bounds__(kGjThreads, 1) k_dense_invert(DevMesh m, const T *__restrict__ vals,
+                                                                const int64_t *__restrict__ dense_off,
+                                                                float *__restrict__ inv, int *__restrict__ singular,
+                                                                float shift)
 {
   pdl_wait();
   pdl_trigger();
-  extern __shared__ float W[]; // [nd][ld]
-  __shared__ float colk[kMaxDense];
+  extern __shared__ float W[]; // column-major [nd][ld]: load and write-back staging
+  __shared__ __align__(16) float colk[2][kGjPad];
+  __shared__ float prowv[2][kMaxDense];
   __shared__ int prow[kMaxDense];
-  __shared__ unsigned char used[kMaxDense];
-  __shared__ int s_p;
-  __shared__ int s_sing;
-  __shared__ float s_piv;
+  __shared__ int pinv[kMaxDense];
   __shared__ float s_shift;
   const int inst = blockIdx.x;
   const int64_t n0 = m.node_off_ptr[inst], n1 = m.node_off_ptr[inst + 1];
   const int B = m.B;
   const int nd = static_cast<int>((n1 - n0) * B);
-  const int ld = 2 * nd + 1;
+  const int ld = nd | 1; // odd: a warp's lanes (consecutive columns) hit distinct banks
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (nd > kMaxDense || nd == 0) return; // rejected by the host before launch
-  // this thread's augmented column and row chunk
-  const int ncol = 2 * nd;
-  const int nch = min(nd, kGjThreads / ncol);
-  const int rows_per = (nd + nch - 1) / nch;
-  const int my_c = tid % ncol, my_ch = tid / ncol;
+  // chunks of rows_per rows (a multiple of 4 for the float4 reads of the pivot column)
+  const int rows_per = gj_rows(nd);
+  const int nch = (nd + rows_per - 1) / rows_per;
+  const int my_c = tid % nd, my_ch = tid / nd;
   const bool worker = my_ch < nch;
-  const int r0 = worker ? my_ch * rows_per : 0, r1 = worker ? min(nd, r0 + rows_per) : 0;
-  for (int e = tid; e < nd * ld; e += kGjThreads)
-    {
-      const int r = e / ld, c = e - r * ld;
-      W[e] = (c >= nd && c - nd == r) ? 1.f : 0.f;
-    }
-  for (int i = tid; i < nd; i += kGjThreads) used[i] = 0;
+  const int r0 = worker ? my_ch * rows_per : 0;
+  for (int e = tid; e < nd * ld; e += kGjThreads) W[e] = 0.f;
+  for (int e = tid; e < 2 * kGjPad; e += kGjThreads) (&colk[0][0])[e] = 0.f;
   __syncthreads();
   const int64_t b0 = m.rowptr[n0], b1 = m.rowptr[n1];
   for (int64_t i = tid; i < (b1 - b0) * B * B; i += kGjThreads)
@@ -446,7 +453,7 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
           else hi = mid - 1;
         }
       const int row = static_cast<int>((lo - n0) * B + cr), col = static_cast<int>((m.cols[blk] - n0) * B + cd);
-      W[row * ld + col] = to_f(vals[blk * B * B + e]);
+      W[col * ld + row] = to_f(vals[blk * B * B + e]);
     }
   __syncthreads();
   if (warp == 0)
@@ -455,83 +462,113 @@ __global__ void __launch_bounds__(kGjThreads) k_dense_invert(DevMesh m, const T 
       for (int i = lane; i < nd; i += 32) sd += fabsf(W[i * ld + i]);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, off);
-      if (lane == 0)
-        {
-          s_sing = 0;
-          s_shift = shift * sd / static_cast<float>(nd);
-        }
+      if (lane == 0) s_shift = shift * sd / static_cast<float>(nd);
     }
   __syncthreads();
   // near-null modes (global phase and spin rotations near a solution) would be amplified
   // without bound by an exact inverse: invert A + shift * mean|diag| * I instead
-  for (int i = tid; i < nd; i += kGjThreads) W[i * ld + i] += s_shift;
-  __syncthreads();
+  float w[kGjRows];
+  const float *wc = W + my_c * ld + r0; // this thread's rows, contiguous
+#pragma unroll
+  for (int j = 0; j < kGjRows; ++j)
+    {
+      const int r = r0 + j;
+      w[j] = 0.f;
+      if (worker && j < rows_per && r < nd) w[j] = wc[j] + (r == my_c ? s_shift : 0.f);
+    }
+  if (worker && my_c == 0)
+#pragma unroll
+    for (int j = 0; j < kGjRows; ++j)
+      if (j < rows_per) colk[0][r0 + j] = w[j];
+  unsigned used = 0; // bit j: row lane + 32 j is a pivot row already
+  bool sing = false;
+  int b = 0;
   for (int k = 0; k < nd; ++k)
     {
-      if (warp == 0)
+      __syncthreads(); // column k published; the other buffers are free again
+      float best = -1.f;
+      int bi = nd;
+#pragma unroll
+      for (int j = 0; j < (kMaxDense + 31) / 32; ++j)
         {
-          float best = -1.f;
-          int bi = nd;
-          for (int i = lane; i < nd; i += 32)
+          const int i = lane + 32 * j;
+          if (i < nd)
             {
-              const float v = W[i * ld + k];
-              colk[i] = v;
-              if (!used[i] && fabsf(v) > best)
+              const float v = colk[b][i];
+              if (!((used >> j) & 1u) && fabsf(v) > best)
                 {
                   best = fabsf(v);
                   bi = i;
                 }
             }
+        }
 #pragma unroll
-          for (int off = 16; off > 0; off >>= 1)
-            {
-              const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-              const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-              if (ob > best || (ob == best && oi < bi))
-                {
-                  best = ob;
-                  bi = oi;
-                }
-            }
-          if (lane == 0)
-            {
-              if (!(best > 1e-30f) || bi >= nd)
-                s_sing = 1;
-              else
-                {
-                  s_p = bi;
-                  s_piv = W[bi * ld + k];
-                  used[bi] = 1;
-                  prow[k] = bi;
-                }
-            }
-        }
-      __syncthreads();
-      if (s_sing) break;
-      const int p = s_p;
-      // columns left of k are unit columns already: row p is zero there
-      const bool upd = worker && my_c >= k;
-      const float wp = upd ? W[p * ld + my_c] * (1.f / s_piv) : 0.f;
-      __syncthreads(); // row p read by every chunk of the column before it is overwritten
-      if (upd)
+      for (int off = 16; off > 0; off >>= 1)
         {
-          // every row, the pivot row included, takes W -= colk * wp (branch-free, so the
-          // loop pipelines); that zeroes row p (colk[p] is the pivot), which then
-          // receives the scaled row
-          float *col = W + my_c;
-#pragma unroll 8
-          for (int i = r0; i < r1; ++i) col[i * ld] = fmaf(-colk[i], wp, col[i * ld]);
-          if (p >= r0 && p < r1) col[p * ld] = wp;
+          const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi))
+            {
+              best = ob;
+              bi = oi;
+            }
         }
-      __syncthreads();
+      if (!(best > 1e-30f) || bi >= nd)
+        {
+          sing = true; // every warp reads the same column: the whole block leaves here
+          break;
+        }
+      const int p = bi;
+      const float piv = colk[b][p];
+      if ((p & 31) == lane) used |= 1u << (p >> 5);
+      if (worker && p >= r0 && p < r0 + rows_per)
+        {
+          float v = 0.f;
+#pragma unroll
+          for (int j = 0; j < kGjRows; ++j)
+            if (r0 + j == p) v = w[j];
+          prowv[b][my_c] = v;
+        }
+      if (tid == 0) prow[k] = p;
+      __syncthreads(); // row p published
+      if (worker)
+        {
+          // column k stands for the unit vector of row p: zero except 1 in row p
+          const bool pc = my_c == k;
+          const float wp = (pc ? 1.f : prowv[b][my_c]) * (1.f / piv);
+          const float *ck = colk[b] + r0;
+#pragma unroll
+          for (int j = 0; j < kGjRows; j += 4)
+            if (j < rows_per)
+              {
+                const float4 c4 = *reinterpret_cast<const float4 *>(ck + j);
+                const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                  w[j + t] = (r0 + j + t == p) ? wp : fmaf(-cv[t], wp, pc ? 0.f : w[j + t]);
+              }
+          if (my_c == k + 1)
+#pragma unroll
+            for (int j = 0; j < kGjRows; ++j)
+              if (j < rows_per) colk[b ^ 1][r0 + j] = w[j];
+        }
+      b ^= 1;
     }
+  if (worker)
+#pragma unroll
+    for (int j = 0; j < kGjRows; ++j)
+      if (j < rows_per && r0 + j < nd) W[my_c * ld + r0 + j] = w[j];
+  __syncthreads();
+  if (!sing)
+    for (int k = tid; k < nd; k += kGjThreads) pinv[prow[k]] = k;
+  __syncthreads();
   float *out = inv + dense_off[inst];
   for (int e = tid; e < nd * nd; e += kGjThreads)
     {
       const int i = e / nd, c = e - i * nd;
-      out[e] = s_sing ? (i == c ? 1.f : 0.f) : W[prow[i] * ld + nd + c];
+      out[e] = sing ? (i == c ? 1.f : 0.f) : W[pinv[c] * ld + prow[i]];
     }
-  if (tid == 0 && s_sing) singular[inst] = 1;
+  if (tid == 0 && sing) singular[inst] = 1;
 }
 
 // z = inv r per instance: one warp per row
@@ -556,36 +593,26 @@ __global__ void k_dense_apply(DevMesh m, const int64_t *__restrict__ dense_off, 
   if (lane == 0) z[n0 * m.B + warp] = static_cast<T>(s);
 }
 
+template <typename T>
+static cudaError_t launch_dense_invert(const DevMesh &m, const void *vals, const int64_t *dense_off, float *inv,
+                                      int *singular, float shift, size_t sm, cudaStream_t s)
+{
+  cudaError_t e =
+      cudaFuncSetAttribute(k_dense_invert<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+  if (e != cudaSuccess) return e;
+  pdl_launch(k_dense_invert<T>, m.n_inst, kGjThreads, sm, s, m, static_cast<const T *>(vals), dense_off, inv, singular,
+             shift);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dense_setup(const DevMesh &m, bool fp32, const void *vals, const int64_t *dense_off, int max_nd,
                                float *inv, int *singular, float shift, cudaStream_t s)
 {
-  const size_t sm = static_cast<size_t>(max_nd) * (2 * max_nd + 1) * sizeof(float);
-  if (max_nd > kMaxDense || sm > 227 * 1024) return cudaErrorInvalidValue;
-  if (fp32 && m.half_vals)
-    {
-      cudaError_t e = cudaFuncSetAttribute(k_dense_invert<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(sm));
-      if (e != cudaSuccess) return e;
-      pdl_launch(k_dense_invert<__half>, m.n_inst, kGjThreads, sm, s, m, static_cast<const __half *>(vals), dense_off, inv,
-                                                              singular, shift);
-    }
-  else if (fp32)
-    {
-      cudaError_t e = cudaFuncSetAttribute(k_dense_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(sm));
-      if (e != cudaSuccess) return e;
-      pdl_launch(k_dense_invert<float>, m.n_inst, kGjThreads, sm, s, m, static_cast<const float *>(vals), dense_off, inv,
-                                                             singular, shift);
-    }
-  else
-    {
-      cudaError_t e = cudaFuncSetAttribute(k_dense_invert<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(sm));
-      if (e != cudaSuccess) return e;
-      pdl_launch(k_dense_invert<double>, m.n_inst, kGjThreads, sm, s, m, static_cast<const double *>(vals), dense_off, inv,
-                                                              singular, shift);
-    }
-  return cudaGetLastError();
+  const size_t sm = static_cast<size_t>(max_nd) * (max_nd | 1) * sizeof(float);
+  if (max_nd > kMaxDense || max_nd < 1) return cudaErrorInvalidValue;
+  if (fp32 && m.half_vals) return launch_dense_invert<__half>(m, vals, dense_off, inv, singular, shift, sm, s);
+  if (fp32) return launch_dense_invert<float>(m, vals, dense_off, inv, singular, shift, sm, s);
+  return launch_dense_invert<double>(m, vals, dense_off, inv, singular, shift, sm, s);
 }
 
 cudaError_t launch_dense_apply(const DevMesh &m, bool fp32, int max_nd, const int64_t *dense_off, const float *inv,

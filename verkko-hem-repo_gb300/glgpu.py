@@ -105,6 +105,7 @@ def lib() -> ctypes.CDLL:
     L.glgpu_mg_level_info.argtypes = [vp, ctypes.c_int, _lp, _lp, _lp]
     L.glgpu_mg_level_system.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
     L.glgpu_mg_prolongation.argtypes = [vp, ctypes.c_int, _ip, _ip, _dp]
+    L.glgpu_mg_coarse_inverse.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]
     L.glgpu_launch_count.argtypes = [vp]
     L.glgpu_launch_count.restype = ctypes.c_int64
     L.glgpu_device_bytes.argtypes = [vp]
@@ -630,6 +631,17 @@ class FemGL:
         w = np.zeros(pn[0])
         _check(L.glgpu_mg_prolongation(self._ctx, int(level), _p(ptr, _ip), _p(idx, _ip), _p(w)))
         return rowptr, cols, vals, (ptr, idx, w)
+
+    def mg_coarse_inverse(self, inst: int = 0) -> np.ndarray:
+        """The coarsest level's dense FP32 inverse of instance `inst` (nd x nd) from the last
+        preconditioner setup: (A + shift mean|diag A| I)^-1, the identity after a zero pivot."""
+        L = lib()
+        nd = ctypes.c_int(0)
+        _check(L.glgpu_mg_coarse_inverse(self._ctx, int(inst), ctypes.byref(nd), None))
+        inv = np.zeros((nd.value, nd.value), np.float32)
+        _check(L.glgpu_mg_coarse_inverse(self._ctx, int(inst), ctypes.byref(nd),
+                                         inv.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return inv
 
     def mg_level_sizes(self, level: int):
         nn, nb, pn = np.zeros(1, np.int64), np.zeros(1, np.int64), np.zeros(1, np.int64)
