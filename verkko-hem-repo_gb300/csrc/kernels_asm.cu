@@ -676,7 +676,9 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
   {
     const int pq = tid / 3, i = tid - 3 * pq;
     const R *A = S.A[pq];
-#pragma unroll
+    // j and l (below) index shared memory only: the loops stay rolled, which keeps the
+    // double-float kernel's code within the instruction cache
+#pragma unroll 1
     for (int j = 0; j < 3; ++j)
       {
         cx<R> pp = {R(0.f), R(0.f)}, qq = {R(0.f), R(0.f)};
@@ -710,7 +712,7 @@ __global__ void __launch_bounds__(kRThreads) k_res3d(DevMesh m, const double *__
         if (k == i) N[k] = cadd(N[k], cscale(p, R(2.f) * cf[3]));
         M[k] = {R(2.f) * (cf[6] + cf[7]) * qik.r, R(2.f) * (cf[6] - cf[7]) * qik.i};
       }
-#pragma unroll
+#pragma unroll 1
     for (int l = 0; l < 3; ++l)
       {
         cx<R> r = cscale(at(A, i, l), s0);
