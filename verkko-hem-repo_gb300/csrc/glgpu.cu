@@ -299,7 +299,7 @@ template <typename T> glgpu_status dalloc(glgpu_ctx *c, T **p, size_t n)
   return GLGPU_OK;
 }
 
-template <typename T> glgpu_status dupload(glgpu_ctx *c, T **p, const std::vector<T> &v)
+template <typename T, typename A> glgpu_status dupload(glgpu_ctx *c, T **p, const std::vector<T, A> &v)
 {
   CKS(dalloc(c, p, v.size()));
   if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -1237,8 +1237,9 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
       TransferTables T;
       glgpu_status ts = transfer_tables(mesh, n_inst, lv, l, FP, c->lv[l]->P, T);
       if (ts != GLGPU_OK) return ts;
-      const std::vector<int32_t> &pp = T.pp, &pi = T.pi, &rp = T.rp, &ri = T.ri, &grow = T.g_row, &gb = T.g_blk;
-      const std::vector<double> &pw = T.pw, &rw = T.rw, &gw = T.g_w;
+      const std::vector<int32_t> &pp = T.pp, &pi = T.pi, &rp = T.rp, &ri = T.ri, &grow = T.g_row;
+      const std::vector<double> &pw = T.pw, &rw = T.rw;
+      const bulk_vector<int32_t> &gb = T.g_blk;
       const std::vector<int64_t> &gt = T.g_toff;
       glgpu_ctx::Transfer &t = c->tr[l];
       t.h_ptr = pp;
@@ -1259,13 +1260,20 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
         {
           CKS(upload_w<float>(c, &t.p_w, pw));
           CKS(upload_w<float>(c, &t.r_w, rw));
-          CKS(upload_w<float>(c, &t.g_w, gw));
+          // the term weights are the largest table: converted on all host threads
+          bulk_vector<float> gwf;
+          to_float(T.g_w, gwf);
+          float *gp = nullptr;
+          CKS(dupload(c, &gp, gwf));
+          t.g_w = gp;
         }
       else
         {
           CKS(upload_w<double>(c, &t.p_w, pw));
           CKS(upload_w<double>(c, &t.r_w, rw));
-          CKS(upload_w<double>(c, &t.g_w, gw));
+          double *gp = nullptr;
+          CKS(dupload(c, &gp, T.g_w));
+          t.g_w = gp;
         }
       // fixed-slot copies of the two transfers (rows with more entries than slots keep the lists)
       auto slots = [&](const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx, const std::vector<double> &w,

@@ -4,6 +4,9 @@
 #include <cstdint>
 #include <string>
 #include <array>
+#include <new>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "glgpu.h"
@@ -14,6 +17,29 @@ namespace glgpu
 // errors
 // ---------------------------------------------------------------------------------
 glgpu_status set_error(glgpu_status s, const std::string &msg);
+
+// Allocator that leaves elements default-initialised (for arithmetic types: not zeroed) when a
+// vector grows by resize: the multi-gigabyte multigrid term tables are written in full by a
+// parallel pass, which then also takes their first-touch page faults, instead of a serial
+// zero fill before it.
+template <typename T> struct NoInitAlloc : std::allocator<T>
+{
+  template <typename U> struct rebind
+  {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <typename U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  template <typename U> void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value)
+  {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <typename U, typename... A> void construct(U *p, A &&...a)
+  {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <typename T> using bulk_vector = std::vector<T, NoInitAlloc<T>>;
 
 // ---------------------------------------------------------------------------------
 // host helpers (host_util.cc)
@@ -124,14 +150,16 @@ struct Plan
   std::vector<uint32_t> mask;                 // [nn]
   std::vector<int32_t> hptr, hpar;            // [nn+1], global parents
   std::vector<double> hw;
-  std::vector<int32_t> rowptr, cols;          // block CSR pattern
+  std::vector<int32_t> rowptr;                // block CSR pattern
+  bulk_vector<int32_t> cols;
   std::vector<int32_t> diag;                  // [nn] index of the diagonal block
   std::vector<int32_t> rc_ptr;                // [nn+1] contributions per row
-  std::vector<int32_t> rc_cell;
-  std::vector<int32_t> rc_a;
-  std::vector<double> rc_w;
-  std::vector<int16_t> rc_slot;               // [ncontrib][nv]: slot, or -1 - (index into hang_tg - ht_off[row])
-  std::vector<HangTarget> hang_tg;
+  // the per-contribution tables are written in full by the plan's parallel row pass
+  bulk_vector<int32_t> rc_cell;
+  bulk_vector<int32_t> rc_a;
+  bulk_vector<double> rc_w;
+  bulk_vector<int16_t> rc_slot;               // [ncontrib][nv]: slot, or -1 - (index into hang_tg - ht_off[row])
+  bulk_vector<HangTarget> hang_tg;
   std::vector<int64_t> ht_off;                // [nn+1] first hanging target of each row
   int max_row_blocks = 0;
   // rows of the specialised 3D row kernel (full 27-block stencil, eight unit-weight cell
@@ -157,8 +185,10 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &plan);
 // every coarse block (g_toff over coarse blocks, g_row, fine block g_blk with weight g_w).
 struct TransferTables
 {
-  std::vector<int32_t> pp, pi, rp, ri, g_row, g_blk;
-  std::vector<double> pw, rw, g_w;
+  std::vector<int32_t> pp, pi, rp, ri, g_row;
+  std::vector<double> pw, rw;
+  bulk_vector<int32_t> g_blk;
+  bulk_vector<double> g_w;
   std::vector<int64_t> g_toff;
   // the coarse Jacobian is symmetric (a Galerkin product of the Hessian of a real functional):
   // only the blocks on or above the block diagonal (column >= row) get Galerkin terms (g_up);
@@ -167,6 +197,8 @@ struct TransferTables
 };
 glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
                              const Plan &FP, const Plan &CP, TransferTables &T);
+// out = in rounded to FP32, on all host threads
+void to_float(const bulk_vector<double> &in, bulk_vector<float> &out);
 
 // Robin (AdGR) faces of the 3D cells: bit f = 2 * axis + side of robin[e] is set when face f
 // of cell e is a pair-breaking boundary face (femgl/src/assemble.cc:286-348, boundary ids

@@ -501,6 +501,7 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   pp.assign(1, 0);
   pi.clear();
   pw.clear();
+  std::vector<std::pair<int32_t, double>> row; // one fine row's entries, reused
   for (int k = 0; k < n_inst; ++k)
     {
       std::vector<int32_t> a, b;
@@ -530,7 +531,7 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
       for (size_t i = 0; i + 1 < a.size(); ++i)
         {
           const int64_t fi = f0 + static_cast<int64_t>(i);
-          std::vector<std::pair<int32_t, double>> row;
+          row.clear();
           if (FP.hptr[fi + 1] == FP.hptr[fi])
             for (int32_t q = a[i]; q < a[i + 1]; ++q)
               {
@@ -567,8 +568,9 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   // threads (a row's blocks belong to one thread), and the tables do not depend on the
   // thread count.
   std::vector<int64_t> &gt = T.g_toff;
-  std::vector<int32_t> &grow = T.g_row, &gb = T.g_blk;
-  std::vector<double> &gw = T.g_w;
+  std::vector<int32_t> &grow = T.g_row;
+  bulk_vector<int32_t> &gb = T.g_blk;
+  bulk_vector<double> &gw = T.g_w;
   gt.assign(static_cast<size_t>(CP.nnzb) + 1, 0);
   grow.assign(static_cast<size_t>(CP.nnzb), 0);
   const int64_t ncr = CP.nn;
@@ -577,8 +579,11 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
       if (pass == 1)
         {
           for (int64_t b = 0; b < CP.nnzb; ++b) gt[b + 1] += gt[b];
-          gb.assign(static_cast<size_t>(gt[CP.nnzb]), 0);
-          gw.assign(static_cast<size_t>(gt[CP.nnzb]), 0.0);
+          // every entry is written below (pass 1 visits exactly the terms pass 0 counted)
+          gb.clear();
+          gw.clear();
+          gb.resize(static_cast<size_t>(gt[CP.nnzb]));
+          gw.resize(static_cast<size_t>(gt[CP.nnzb]));
         }
       int outside = 0;
 #pragma omp parallel reduction(| : outside)
@@ -650,6 +655,15 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
         lo.push_back(m);
       }
   return GLGPU_OK;
+}
+
+void to_float(const bulk_vector<double> &in, bulk_vector<float> &out)
+{
+  out.clear();
+  out.resize(in.size());
+  const int64_t n = static_cast<int64_t>(in.size());
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) out[i] = static_cast<float>(in[i]);
 }
 
 } // namespace glgpu

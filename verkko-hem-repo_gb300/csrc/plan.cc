@@ -23,7 +23,8 @@ namespace
 {
 struct Incidence
 {
-  std::vector<int32_t> ptr, cell, loc;
+  std::vector<int32_t> ptr;
+  bulk_vector<int32_t> cell, loc; // written in full by the fill
 };
 
 glgpu_status check_mesh(const glgpu_mesh &m, int k)
@@ -76,12 +77,18 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
 {
   if (!mesh || n_inst <= 0) return set_error(GLGPU_ERR_ARG, "glgpu_create: no instances");
   P.dim = mesh[0].dim;
-  for (int k = 0; k < n_inst; ++k)
-    {
-      glgpu_status s = check_mesh(mesh[k], k);
-      if (s != GLGPU_OK) return s;
-      if (mesh[k].dim != P.dim) return set_error(GLGPU_ERR_ARG, "glgpu_create: all instances must share dim");
-    }
+  {
+    // instances are validated on all host threads; the first failure is validated again on
+    // the calling thread, whose error slot the caller reads
+    std::vector<glgpu_status> st(n_inst, GLGPU_OK);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < n_inst; ++k) st[k] = check_mesh(mesh[k], k);
+    for (int k = 0; k < n_inst; ++k)
+      {
+        if (st[k] != GLGPU_OK) return check_mesh(mesh[k], k);
+        if (mesh[k].dim != P.dim) return set_error(GLGPU_ERR_ARG, "glgpu_create: all instances must share dim");
+      }
+  }
   P.B = (P.dim == 3) ? 18 : 2;
   P.nv = 1 << P.dim;
   const int nv = P.nv, B = P.B;
@@ -105,6 +112,9 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   P.node_inst.resize(nn);
   P.mask.assign(nn, 0u);
   P.hptr.assign(nn + 1, 0);
+  // instances own disjoint node and cell ranges (their cells reference only their own
+  // nodes): the per-instance loops below run on all host threads
+#pragma omp parallel for schedule(dynamic, 1)
   for (int k = 0; k < n_inst; ++k)
     {
       const glgpu_mesh &m = mesh[k];
@@ -130,6 +140,7 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
   for (int64_t i = 0; i < nn; ++i) P.hptr[i + 1] += P.hptr[i];
   P.hpar.resize(P.hptr[nn]);
   P.hw.resize(P.hptr[nn]);
+#pragma omp parallel for schedule(dynamic, 1)
   for (int k = 0; k < n_inst; ++k)
     {
       const glgpu_mesh &m = mesh[k];
@@ -149,40 +160,51 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
     if (hanging(i)) P.mask[i] = 0u;
 
   // node -> (cell, local vertex) incidence
+  // (counting sorts per instance: a node's entries keep ascending cell order)
   Incidence inc;
   inc.ptr.assign(nn + 1, 0);
-  for (int64_t e = 0; e < nc * nv; ++e) inc.ptr[P.cells[e] + 1]++;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < n_inst; ++k)
+    for (int64_t e = P.cell_off[k] * nv; e < P.cell_off[k + 1] * nv; ++e) inc.ptr[P.cells[e] + 1]++;
   for (int64_t i = 0; i < nn; ++i) inc.ptr[i + 1] += inc.ptr[i];
   inc.cell.resize(nc * nv);
   inc.loc.resize(nc * nv);
-  {
-    std::vector<int32_t> fill(inc.ptr.begin(), inc.ptr.end() - 1);
-    for (int64_t e = 0; e < nc; ++e)
-      for (int v = 0; v < nv; ++v)
-        {
-          const int32_t n = P.cells[e * nv + v];
-          inc.cell[fill[n]] = static_cast<int32_t>(e);
-          inc.loc[fill[n]] = v;
-          fill[n]++;
-        }
-  }
-  // parent -> hanging children
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const int64_t no = P.node_off[k];
+      std::vector<int32_t> fill(inc.ptr.begin() + no, inc.ptr.begin() + P.node_off[k + 1]);
+      for (int64_t e = P.cell_off[k]; e < P.cell_off[k + 1]; ++e)
+        for (int v = 0; v < nv; ++v)
+          {
+            const int64_t n = P.cells[e * nv + v] - no;
+            inc.cell[fill[n]] = static_cast<int32_t>(e);
+            inc.loc[fill[n]] = v;
+            fill[n]++;
+          }
+    }
+  // parent -> hanging children (parents lie in their child's instance)
   std::vector<int32_t> ch_ptr(nn + 1, 0), ch_node, ch_idx;
-  for (int64_t i = 0; i < nn; ++i)
-    for (int j = P.hptr[i]; j < P.hptr[i + 1]; ++j) ch_ptr[P.hpar[j] + 1]++;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < n_inst; ++k)
+    for (int64_t i = P.node_off[k]; i < P.node_off[k + 1]; ++i)
+      for (int j = P.hptr[i]; j < P.hptr[i + 1]; ++j) ch_ptr[P.hpar[j] + 1]++;
   for (int64_t i = 0; i < nn; ++i) ch_ptr[i + 1] += ch_ptr[i];
   ch_node.resize(ch_ptr[nn]);
   ch_idx.resize(ch_ptr[nn]);
-  {
-    std::vector<int32_t> fill(ch_ptr.begin(), ch_ptr.end() - 1);
-    for (int64_t i = 0; i < nn; ++i)
-      for (int j = P.hptr[i]; j < P.hptr[i + 1]; ++j)
-        {
-          const int32_t p = P.hpar[j];
-          ch_node[fill[p]] = static_cast<int32_t>(i);
-          ch_idx[fill[p]] = j;
-          fill[p]++;
-        }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < n_inst; ++k)
+    {
+      const int64_t no = P.node_off[k];
+      std::vector<int32_t> fill(ch_ptr.begin() + no, ch_ptr.begin() + P.node_off[k + 1]);
+      for (int64_t i = no; i < P.node_off[k + 1]; ++i)
+        for (int j = P.hptr[i]; j < P.hptr[i + 1]; ++j)
+          {
+            const int64_t p = P.hpar[j] - no;
+            ch_node[fill[p]] = static_cast<int32_t>(i);
+            ch_idx[fill[p]] = j;
+            fill[p]++;
+          }
   }
 
   // per-row contribution lists and column sets (rows independent)
@@ -255,9 +277,16 @@ glgpu_status build_plan(const glgpu_mesh *mesh, int n_inst, Plan &P)
     }
   P.nnzb = P.rowptr[nn];
   P.max_row_blocks = *std::max_element(row_len.begin(), row_len.end());
+  // not zero-filled: the row pass below writes every entry (the lengths come from the pass above)
+  P.cols.clear();
   P.cols.resize(P.nnzb);
   P.diag.assign(nn, -1);
   const int64_t nrc = P.rc_ptr[nn];
+  P.rc_cell.clear();
+  P.rc_a.clear();
+  P.rc_w.clear();
+  P.rc_slot.clear();
+  P.hang_tg.clear();
   P.rc_cell.resize(nrc);
   P.rc_a.resize(nrc);
   P.rc_w.resize(nrc);
