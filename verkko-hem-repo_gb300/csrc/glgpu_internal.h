@@ -159,7 +159,7 @@ struct Plan
   bulk_vector<int32_t> rc_a;
   bulk_vector<double> rc_w;
   bulk_vector<int16_t> rc_slot;               // [ncontrib][nv]: slot, or -1 - (index into hang_tg - ht_off[row])
-  bulk_vector<HangTarget> hang_tg;
+  std::vector<HangTarget> hang_tg;            // zero-initialised: its padding is uploaded too
   std::vector<int64_t> ht_off;                // [nn+1] first hanging target of each row
   int max_row_blocks = 0;
   // rows of the specialised 3D row kernel (full 27-block stencil, eight unit-weight cell

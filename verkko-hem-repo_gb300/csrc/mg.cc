@@ -498,64 +498,110 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
 {
   std::vector<int32_t> &pp = T.pp, &pi = T.pi;
   std::vector<double> &pw = T.pw;
-  pp.assign(1, 0);
-  pi.clear();
-  pw.clear();
-  std::vector<std::pair<int32_t, double>> row; // one fine row's entries, reused
+  // prolongation rows per instance on all host threads, then concatenated in instance order;
+  // err[k]: 1 = not a box grid, 2 = level grid and mesh disagree (the first failing instance
+  // is reported, as a serial loop would)
+  std::vector<std::vector<int32_t>> ipp(n_inst), ipi(n_inst);
+  std::vector<std::vector<double>> ipw(n_inst);
+  std::vector<int> err(n_inst, 0);
+#pragma omp parallel
+  {
+    std::vector<std::pair<int32_t, double>> row; // one fine row's entries, reused
+#pragma omp for schedule(dynamic, 1)
+    for (int k = 0; k < n_inst; ++k)
+      {
+        std::vector<int32_t> a, b;
+        std::vector<double> w;
+        if (l == 0 && !lv[0].coord.empty() && lv[0].coord[k])
+          coord_prolongation(mesh[k], lv[0].grid[k], a, b, w, CP.node_off[k]);
+        else
+          {
+            TensorGrid fg;
+            if (l == 0)
+              {
+                BoxGeom g;
+                if (!infer_box(mesh[k], g))
+                  {
+                    err[k] = 1;
+                    continue;
+                  }
+                for (int d = 0; d < 3; ++d) fg.x[d].resize(g.n[d] + 1);
+              }
+            else
+              fg = lv[l - 1].grid[k];
+            int nc[3];
+            for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(lv[l].grid[k].x[d].size()) - 1;
+            tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
+          }
+        if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
+          {
+            err[k] = 2;
+            continue;
+          }
+        // prolongation between the free spaces: constrained fine nodes (hanging nodes,
+        // periodic images) get no row, constrained coarse nodes are replaced by their parents
+        std::vector<int32_t> &lpp = ipp[k], &lpi = ipi[k];
+        std::vector<double> &lpw = ipw[k];
+        lpp.assign(1, 0);
+        const int64_t f0 = FP.node_off[k];
+        for (size_t i = 0; i + 1 < a.size(); ++i)
+          {
+            const int64_t fi = f0 + static_cast<int64_t>(i);
+            row.clear();
+            if (FP.hptr[fi + 1] == FP.hptr[fi])
+              for (int32_t q = a[i]; q < a[i + 1]; ++q)
+                {
+                  const int32_t j = b[q];
+                  if (CP.hptr[j + 1] == CP.hptr[j])
+                    row.push_back({j, w[q]});
+                  else
+                    for (int32_t h = CP.hptr[j]; h < CP.hptr[j + 1]; ++h) row.push_back({CP.hpar[h], w[q] * CP.hw[h]});
+                }
+            std::sort(row.begin(), row.end());
+            size_t nr = 0;
+            for (size_t q = 0; q < row.size(); ++q)
+              if (nr > 0 && row[nr - 1].first == row[q].first)
+                row[nr - 1].second += row[q].second;
+              else
+                row[nr++] = row[q];
+            for (size_t q = 0; q < nr; ++q)
+              {
+                lpi.push_back(row[q].first);
+                lpw.push_back(row[q].second);
+              }
+            lpp.push_back(static_cast<int32_t>(lpi.size()));
+          }
+      }
+  }
   for (int k = 0; k < n_inst; ++k)
     {
-      std::vector<int32_t> a, b;
-      std::vector<double> w;
-      if (l == 0 && !lv[0].coord.empty() && lv[0].coord[k])
-        coord_prolongation(mesh[k], lv[0].grid[k], a, b, w, CP.node_off[k]);
-      else
-        {
-          TensorGrid fg;
-          if (l == 0)
-            {
-              BoxGeom g;
-              if (!infer_box(mesh[k], g)) return set_error(GLGPU_ERR_ARG, "multigrid: instance is not a box grid");
-              for (int d = 0; d < 3; ++d) fg.x[d].resize(g.n[d] + 1);
-            }
-          else
-            fg = lv[l - 1].grid[k];
-          int nc[3];
-          for (int d = 0; d < 3; ++d) nc[d] = static_cast<int>(lv[l].grid[k].x[d].size()) - 1;
-          tensor_prolongation(fg, lv[l].map[k].data(), a, b, w, CP.node_off[k], nc);
-        }
-      if (static_cast<int64_t>(a.size()) - 1 != FP.node_off[k + 1] - FP.node_off[k])
-        return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
-      // prolongation between the free spaces: constrained fine nodes (hanging nodes,
-      // periodic images) get no row, constrained coarse nodes are replaced by their parents
-      const int64_t f0 = FP.node_off[k];
-      for (size_t i = 0; i + 1 < a.size(); ++i)
-        {
-          const int64_t fi = f0 + static_cast<int64_t>(i);
-          row.clear();
-          if (FP.hptr[fi + 1] == FP.hptr[fi])
-            for (int32_t q = a[i]; q < a[i + 1]; ++q)
-              {
-                const int32_t j = b[q];
-                if (CP.hptr[j + 1] == CP.hptr[j])
-                  row.push_back({j, w[q]});
-                else
-                  for (int32_t h = CP.hptr[j]; h < CP.hptr[j + 1]; ++h) row.push_back({CP.hpar[h], w[q] * CP.hw[h]});
-              }
-          std::sort(row.begin(), row.end());
-          size_t nr = 0;
-          for (size_t q = 0; q < row.size(); ++q)
-            if (nr > 0 && row[nr - 1].first == row[q].first)
-              row[nr - 1].second += row[q].second;
-            else
-              row[nr++] = row[q];
-          for (size_t q = 0; q < nr; ++q)
-            {
-              pi.push_back(row[q].first);
-              pw.push_back(row[q].second);
-            }
-          pp.push_back(static_cast<int32_t>(pi.size()));
-        }
+      if (err[k] == 1) return set_error(GLGPU_ERR_ARG, "multigrid: instance is not a box grid");
+      if (err[k] == 2) return set_error(GLGPU_ERR_ARG, "multigrid: level grid does not match the mesh");
     }
+  {
+    size_t total = 0, rows = 0;
+    for (int k = 0; k < n_inst; ++k)
+      {
+        total += ipi[k].size();
+        rows += ipp[k].size() - 1;
+      }
+    if (total >= (size_t(1) << 31)) return set_error(GLGPU_ERR_ARG, "multigrid: prolongation too large");
+    pp.assign(1, 0);
+    pp.reserve(rows + 1);
+    pi.clear();
+    pw.clear();
+    pi.reserve(total);
+    pw.reserve(total);
+    for (int k = 0; k < n_inst; ++k)
+      {
+        const int32_t base = static_cast<int32_t>(pi.size());
+        for (size_t r = 1; r < ipp[k].size(); ++r) pp.push_back(base + ipp[k][r]);
+        pi.insert(pi.end(), ipi[k].begin(), ipi[k].end());
+        pw.insert(pw.end(), ipw[k].begin(), ipw[k].end());
+        std::vector<int32_t>().swap(ipi[k]);
+        std::vector<double>().swap(ipw[k]);
+      }
+  }
   std::vector<int32_t> &rp = T.rp, &ri = T.ri;
   std::vector<double> &rw = T.rw;
   transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
@@ -635,25 +681,48 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
       }
       if (outside) return set_error(GLGPU_ERR_ARG, "multigrid: Galerkin product leaves the coarse pattern");
     }
+  // blocks on or above the diagonal, and (block, mirror) pairs below it, in block order:
+  // counted per coarse row, then written at their offsets on all host threads (a row's
+  // columns are sorted, so the mirror is a binary search in row J)
   std::vector<int32_t> &up = T.g_up, &lo = T.g_lo;
-  up.clear();
-  lo.clear();
+  std::vector<int64_t> nup(static_cast<size_t>(ncr) + 1, 0), nlo(static_cast<size_t>(ncr) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
   for (int64_t I = 0; I < ncr; ++I)
-    for (int32_t b = CP.rowptr[I]; b < CP.rowptr[I + 1]; ++b)
-      {
-        const int32_t J = CP.cols[b];
-        if (J >= I)
-          {
-            up.push_back(b);
-            continue;
-          }
-        int32_t m = -1;
-        for (int32_t e = CP.rowptr[J]; e < CP.rowptr[J + 1]; ++e)
-          if (CP.cols[e] == I) m = e;
-        if (m < 0) return set_error(GLGPU_ERR_ARG, "multigrid: the coarse pattern is not symmetric");
-        lo.push_back(b);
-        lo.push_back(m);
-      }
+    {
+      int64_t u = 0;
+      for (int32_t b = CP.rowptr[I]; b < CP.rowptr[I + 1]; ++b) u += CP.cols[b] >= I;
+      nup[I + 1] = u;
+      nlo[I + 1] = (CP.rowptr[I + 1] - CP.rowptr[I]) - u;
+    }
+  for (int64_t I = 0; I < ncr; ++I)
+    {
+      nup[I + 1] += nup[I];
+      nlo[I + 1] += nlo[I];
+    }
+  up.assign(static_cast<size_t>(nup[ncr]), 0);
+  lo.assign(static_cast<size_t>(2 * nlo[ncr]), 0);
+  int asym = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : asym)
+  for (int64_t I = 0; I < ncr; ++I)
+    {
+      int64_t u = nup[I], q = nlo[I];
+      for (int32_t b = CP.rowptr[I]; b < CP.rowptr[I + 1]; ++b)
+        {
+          const int32_t J = CP.cols[b];
+          if (J >= I)
+            {
+              up[u++] = b;
+              continue;
+            }
+          const int32_t *r0 = CP.cols.data() + CP.rowptr[J], *r1 = CP.cols.data() + CP.rowptr[J + 1];
+          const int32_t *it = std::lower_bound(r0, r1, static_cast<int32_t>(I));
+          if (it == r1 || *it != I) asym = 1;
+          lo[2 * q] = b;
+          lo[2 * q + 1] = (it != r1 && *it == I) ? static_cast<int32_t>(it - CP.cols.data()) : -1;
+          ++q;
+        }
+    }
+  if (asym) return set_error(GLGPU_ERR_ARG, "multigrid: the coarse pattern is not symmetric");
   return GLGPU_OK;
 }
 
