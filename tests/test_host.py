@@ -428,3 +428,47 @@ def test_oracle_matep_table_lookup_rejects_untabulated_points(oracle_gl, monkeyp
     assert oracle_gl.matep(20.0, 0.6)["alpha"] == -0.4
     with pytest.raises(KeyError):
         oracle_gl.matep(20.5, 0.6)
+
+
+_THREADS_SCRIPT = r"""
+import hashlib, importlib, json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+gl = importlib.import_module("verkko-hem-repo_gb300")
+ms = [gl.box_mesh([-10, -10, -4], [10, 10, 4], (9, 9, 9)),
+      gl.box_mesh([-6, -6, -6], [6, 6, 6], (8, 8, 8), refine_band=2.0),
+      gl.box_mesh([-5, -5, -3], [5, 5, 3], (6, 6, 5), periodic_xy=(1, 1)),
+      gl.box_mesh([-4, -4, -4], [4, 4, 4], (6, 6, 6), refine_band=1.5, periodic_xy=(1, 0))]
+h = hashlib.sha256()
+for a in (*gl.plan_pattern(ms), *gl.plan_prolongation(ms), *gl.plan_kelly(ms), gl.plan_robin(ms)):
+    h.update(np.ascontiguousarray(a).tobytes())
+bad = gl.box_mesh([-1, -1, -1], [1, 1, 1], (4, 4, 4))
+bad.cells[5, 3] = bad.nn + 7
+skew = gl.box_mesh([-1, -1, -1], [1, 1, 1], (4, 4, 4))
+skew.xyz[skew.cells[2, 7], 0] += 0.3
+try:
+    gl.plan_info([ms[0], skew, ms[2], bad])
+    err = None
+except gl.GLGPUError as e:
+    err = str(e)
+print(json.dumps({"info": gl.plan_info(ms), "hash": h.hexdigest(), "err": err}))
+"""
+
+
+def test_host_plans_do_not_depend_on_the_thread_count(gl):
+    """The host builders split their work over instances and rows on all host threads; the
+    block pattern, the multigrid prolongation (built with every level's plan, the transfer
+    and the Galerkin tables), the estimator's face pairs and the Robin faces of a batch of
+    plain, once-refined and periodic boxes are bitwise the same on 1 and 4 threads, and a
+    batch with two invalid instances reports the first one."""
+    import subprocess
+    import sys
+    out = []
+    for threads in (1, 4):
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        r = subprocess.run([sys.executable, "-c", _THREADS_SCRIPT, ROOT], env=env, capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert out[0] == out[1]
+    assert "instance 1:" in out[0]["err"] and "axis-aligned box" in out[0]["err"]
