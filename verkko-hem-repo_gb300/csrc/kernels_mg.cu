@@ -396,7 +396,18 @@ __host__ __device__ constexpr int gj_rows(int nd)
 {
   return ((nd + (kGjThreads / nd) - 1) / (kGjThreads / nd) + 3) & ~3;
 }
-static_assert(gj_rows(kMaxDense) <= kGjRows && gj_rows(kMaxDense - 1) <= kGjRows, "register rows");
+// every system size fits: its rows in registers, its chunks in the block, its padded pivot
+// column in shared memory
+__host__ __device__ constexpr bool gj_chunks_fit()
+{
+  for (int nd = 1; nd <= kMaxDense; ++nd)
+    {
+      const int r = gj_rows(nd), nch = (nd + r - 1) / r;
+      if (r > kGjRows || nch * nd > kGjThreads || nch * r > kGjPad) return false;
+    }
+  return true;
+}
+static_assert(gj_chunks_fit(), "Gauss-Jordan chunking");
 
 // Gauss-Jordan on A + shift I with implicit partial pivoting, in place: column k is replaced in
 // step k by the column of the inverse's row-permuted form that the augmented scheme [A | I]
