@@ -1235,7 +1235,8 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
     {
       const Plan &FP = (l == 0) ? c->P : c->lv[l - 1]->P;
       TransferTables T;
-      glgpu_status ts = transfer_tables(mesh, n_inst, lv, l, FP, c->lv[l]->P, T);
+      // mixed mode keeps the Galerkin term weights in FP32: written so by the term pass
+      glgpu_status ts = transfer_tables(mesh, n_inst, lv, l, FP, c->lv[l]->P, T, c->mixed);
       if (ts != GLGPU_OK) return ts;
       const std::vector<int32_t> &pp = T.pp, &pi = T.pi, &rp = T.rp, &ri = T.ri, &grow = T.g_row;
       const std::vector<double> &pw = T.pw, &rw = T.rw;
@@ -1260,11 +1261,8 @@ glgpu_status mg_setup(glgpu_ctx *c, const glgpu_mesh *mesh, const glgpu_params *
         {
           CKS(upload_w<float>(c, &t.p_w, pw));
           CKS(upload_w<float>(c, &t.r_w, rw));
-          // the term weights are the largest table: converted on all host threads
-          bulk_vector<float> gwf;
-          to_float(T.g_w, gwf);
           float *gp = nullptr;
-          CKS(dupload(c, &gp, gwf));
+          CKS(dupload(c, &gp, T.g_wf));
           t.g_w = gp;
         }
       else

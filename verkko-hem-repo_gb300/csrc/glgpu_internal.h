@@ -188,7 +188,8 @@ struct TransferTables
   std::vector<int32_t> pp, pi, rp, ri, g_row;
   std::vector<double> pw, rw;
   bulk_vector<int32_t> g_blk;
-  bulk_vector<double> g_w;
+  bulk_vector<double> g_w;  // term weights in FP64 (fp32_weights false)
+  bulk_vector<float> g_wf;  // or rounded once to FP32 (fp32_weights true; g_w stays empty)
   std::vector<int64_t> g_toff;
   // the coarse Jacobian is symmetric (a Galerkin product of the Hessian of a real functional):
   // only the blocks on or above the block diagonal (column >= row) get Galerkin terms (g_up);
@@ -196,9 +197,7 @@ struct TransferTables
   std::vector<int32_t> g_up, g_lo;
 };
 glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
-                             const Plan &FP, const Plan &CP, TransferTables &T);
-// out = in rounded to FP32, on all host threads
-void to_float(const bulk_vector<double> &in, bulk_vector<float> &out);
+                             const Plan &FP, const Plan &CP, TransferTables &T, bool fp32_weights = false);
 
 // Robin (AdGR) faces of the 3D cells: bit f = 2 * axis + side of robin[e] is set when face f
 // of cell e is a pair-breaking boundary face (femgl/src/assemble.cc:286-348, boundary ids

@@ -494,7 +494,7 @@ int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vec
 }
 
 glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vector<MgLevel> &lv, int l,
-                             const Plan &FP, const Plan &CP, TransferTables &T)
+                             const Plan &FP, const Plan &CP, TransferTables &T, bool fp32_weights)
 {
   std::vector<int32_t> &pp = T.pp, &pi = T.pi;
   std::vector<double> &pw = T.pw;
@@ -617,6 +617,7 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   std::vector<int32_t> &grow = T.g_row;
   bulk_vector<int32_t> &gb = T.g_blk;
   bulk_vector<double> &gw = T.g_w;
+  bulk_vector<float> &gwf = T.g_wf;
   gt.assign(static_cast<size_t>(CP.nnzb) + 1, 0);
   grow.assign(static_cast<size_t>(CP.nnzb), 0);
   const int64_t ncr = CP.nn;
@@ -628,8 +629,12 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
           // every entry is written below (pass 1 visits exactly the terms pass 0 counted)
           gb.clear();
           gw.clear();
+          gwf.clear();
           gb.resize(static_cast<size_t>(gt[CP.nnzb]));
-          gw.resize(static_cast<size_t>(gt[CP.nnzb]));
+          if (fp32_weights)
+            gwf.resize(static_cast<size_t>(gt[CP.nnzb]));
+          else
+            gw.resize(static_cast<size_t>(gt[CP.nnzb]));
         }
       int outside = 0;
 #pragma omp parallel reduction(| : outside)
@@ -666,7 +671,11 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
                         else
                           {
                             gb[pos[sl]] = b;
-                            gw[pos[sl]] = rw[k] * pw[q];
+                            const double wt = rw[k] * pw[q];
+                            if (fp32_weights)
+                              gwf[pos[sl]] = static_cast<float>(wt);
+                            else
+                              gw[pos[sl]] = wt;
                             ++pos[sl];
                           }
                       }
@@ -724,15 +733,6 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
     }
   if (asym) return set_error(GLGPU_ERR_ARG, "multigrid: the coarse pattern is not symmetric");
   return GLGPU_OK;
-}
-
-void to_float(const bulk_vector<double> &in, bulk_vector<float> &out)
-{
-  out.clear();
-  out.resize(in.size());
-  const int64_t n = static_cast<int64_t>(in.size());
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < n; ++i) out[i] = static_cast<float>(in[i]);
 }
 
 } // namespace glgpu
