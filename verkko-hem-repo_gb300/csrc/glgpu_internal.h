@@ -100,9 +100,13 @@ void coord_prolongation(const glgpu_mesh &m, const TensorGrid &c, std::vector<in
 int mesh_tensor(const TensorGrid &g, BoxMesh &m);
 void tensor_prolongation(const TensorGrid &f, const std::vector<Lin1> *map, std::vector<int32_t> &ptr,
                          std::vector<int32_t> &idx, std::vector<double> &w, int64_t coarse_offset, const int *nc);
-void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx,
-                   const std::vector<double> &w, std::vector<int32_t> &tptr, std::vector<int32_t> &tidx,
-                   std::vector<double> &tw);
+// Transpose of a CSR matrix that is block diagonal over parts (rows row_off[k]..row_off[k+1]
+// couple only to columns col_off[k]..col_off[k+1]): per part on all host threads, each
+// column's entries in ascending row order.  False (outputs unspecified) when an entry lies
+// outside its block.
+bool transpose_csr(const std::vector<int64_t> &row_off, const std::vector<int64_t> &col_off,
+                   const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx, const std::vector<double> &w,
+                   std::vector<int32_t> &tptr, std::vector<int32_t> &tidx, std::vector<double> &tw);
 int build_hierarchy(const glgpu_mesh *mesh, int n_inst, int max_levels, std::vector<MgLevel> &levels,
                     std::string &why);
 double gaussian(uint64_t seed, uint64_t index);

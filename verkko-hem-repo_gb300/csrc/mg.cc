@@ -359,24 +359,43 @@ int mesh_tensor(const TensorGrid &g, BoxMesh &m)
   return 0;
 }
 
-void transpose_csr(int64_t nrows, int64_t ncols, const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx,
-                   const std::vector<double> &w, std::vector<int32_t> &tptr, std::vector<int32_t> &tidx,
-                   std::vector<double> &tw)
+bool transpose_csr(const std::vector<int64_t> &row_off, const std::vector<int64_t> &col_off,
+                   const std::vector<int32_t> &ptr, const std::vector<int32_t> &idx, const std::vector<double> &w,
+                   std::vector<int32_t> &tptr, std::vector<int32_t> &tidx, std::vector<double> &tw)
 {
+  const int parts = static_cast<int>(row_off.size()) - 1;
+  const int64_t ncols = col_off[parts];
   tptr.assign(ncols + 1, 0);
-  for (int32_t j : idx) tptr[j + 1]++;
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+  for (int k = 0; k < parts; ++k)
+    for (int64_t r = row_off[k]; r < row_off[k + 1]; ++r)
+      for (int32_t q = ptr[r]; q < ptr[r + 1]; ++q)
+        {
+          if (idx[q] < col_off[k] || idx[q] >= col_off[k + 1])
+            bad = 1; // an entry outside the block's columns
+          else
+            tptr[idx[q] + 1]++;
+        }
+  if (bad) return false;
   for (int64_t c = 0; c < ncols; ++c) tptr[c + 1] += tptr[c];
   tidx.resize(idx.size());
   tw.resize(w.size());
-  std::vector<int32_t> fill(tptr.begin(), tptr.end() - 1);
-  for (int64_t r = 0; r < nrows; ++r)
-    for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k)
-      {
-        const int32_t c = idx[k];
-        tidx[fill[c]] = static_cast<int32_t>(r);
-        tw[fill[c]] = w[k];
-        fill[c]++;
-      }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < parts; ++k)
+    {
+      const int64_t c0 = col_off[k];
+      std::vector<int32_t> fill(tptr.begin() + c0, tptr.begin() + col_off[k + 1]);
+      for (int64_t r = row_off[k]; r < row_off[k + 1]; ++r)
+        for (int32_t q = ptr[r]; q < ptr[r + 1]; ++q)
+          {
+            const int64_t c = idx[q] - c0;
+            tidx[fill[c]] = static_cast<int32_t>(r);
+            tw[fill[c]] = w[q];
+            fill[c]++;
+          }
+    }
+  return true;
 }
 
 // Prolongation of one instance from level grid `c` to the next finer grid `f` (local node
@@ -604,7 +623,8 @@ glgpu_status transfer_tables(const glgpu_mesh *mesh, int n_inst, const std::vect
   }
   std::vector<int32_t> &rp = T.rp, &ri = T.ri;
   std::vector<double> &rw = T.rw;
-  transpose_csr(FP.nn, CP.nn, pp, pi, pw, rp, ri, rw);
+  if (!transpose_csr(FP.node_off, CP.node_off, pp, pi, pw, rp, ri, rw))
+    return set_error(GLGPU_ERR_ARG, "multigrid: prolongation couples instances");
   // Galerkin terms, grouped by coarse block: every (restriction entry i of row I, fine block
   // (i, j), prolongation entry J of j) adds w(i, I) w(j, J) J_f(i, j) to block (I, J); within a
   // block the terms follow (restriction entry, fine block, prolongation entry) order, so fine
