@@ -138,7 +138,9 @@ const char *glgpu_last_error(void);
  * Creates a context for n_inst instances (mesh[k], prm[k]); builds the block-CSR
  * pattern and the assembly plan once per mesh (the reference does this in
  * setup_system(), femgl/src/setup_uniform_B-phase.cc:188-198) and allocates all
- * device memory.  The solution starts at zero.
+ * device memory.  The solution starts at zero.  The host side (plans, multigrid
+ * transfer and Galerkin tables) runs on OpenMP threads, all host cores unless
+ * OMP_NUM_THREADS says otherwise; its tables do not depend on the thread count.
  */
 glgpu_status glgpu_create(const glgpu_mesh *mesh, const glgpu_params *prm, int n_inst, glgpu_ctx **out);
 glgpu_status glgpu_destroy(glgpu_ctx *ctx);
