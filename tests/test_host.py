@@ -442,6 +442,15 @@ ms = [gl.box_mesh([-10, -10, -4], [10, 10, 4], (9, 9, 9)),
 h = hashlib.sha256()
 for a in (*gl.plan_pattern(ms), *gl.plan_prolongation(ms), *gl.plan_kelly(ms), gl.plan_robin(ms)):
     h.update(np.ascontiguousarray(a).tobytes())
+sq = []
+for nx, ny in ((40, 24), (9, 13)):
+    X, Y = np.meshgrid(np.linspace(-1, 1, nx + 1), np.linspace(-1, 1, ny + 1))
+    v0 = (np.arange(ny)[:, None] * (nx + 1) + np.arange(nx)[None, :]).ravel()
+    cells = np.stack([v0, v0 + 1, v0 + nx + 1, v0 + nx + 2], 1).astype(np.int32)
+    mask = ((np.abs(X) == 1) | (np.abs(Y) == 1)).ravel().astype(np.uint32)
+    sq.append(gl.Mesh(2, np.stack([X.ravel(), Y.ravel()], 1), cells, mask))
+for a in gl.plan_pattern(sq):
+    h.update(np.ascontiguousarray(a).tobytes())
 bad = gl.box_mesh([-1, -1, -1], [1, 1, 1], (4, 4, 4))
 bad.cells[5, 3] = bad.nn + 7
 skew = gl.box_mesh([-1, -1, -1], [1, 1, 1], (4, 4, 4))
@@ -459,8 +468,9 @@ def test_host_plans_do_not_depend_on_the_thread_count(gl):
     """The host builders split their work over instances and rows on all host threads; the
     block pattern, the multigrid prolongation (built with every level's plan, the transfer
     and the Galerkin tables), the estimator's face pairs and the Robin faces of a batch of
-    plain, once-refined and periodic boxes are bitwise the same on 1 and 4 threads, and a
-    batch with two invalid instances reports the first one."""
+    plain, once-refined and periodic boxes, and the pattern of a batch of 2D meshes, are
+    bitwise the same on 1 and 4 threads, and a batch with two invalid instances reports the
+    first one."""
     import subprocess
     import sys
     out = []
